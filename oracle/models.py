@@ -1,0 +1,426 @@
+"""Lattice models and the MPOHamiltonian builder (oracle; test infrastructure only).
+
+Restates:
+  * `FiniteMPOHamiltonian(lattice, terms)`   -- src/operators/mpohamiltonian.jl:439-519
+  * `InfiniteMPOHamiltonian(lattice, terms)` -- src/operators/mpohamiltonian.jl:521-641
+  * `_find_channel`                           -- src/operators/mpohamiltonian.jl:408-416
+  * `instantiate_operator`                    -- src/operators/mpohamiltonian.jl:349-386
+  * `decompose_localmpo` (2-site SVD split)   -- src/utility/utility.jl:54-66
+  * test models `transverse_field_ising`, `heisenberg_XXX`
+                                              -- test/setup/testsetup.jl:102-134
+
+The MPO is stored densely over the channel sum space: W[wl, s, s', wr] with the
+flat channel index; `chans[i]` lists the per-channel dimensions of bond i so the
+Jordan blocks (start = first channel, finished = last channel) are recoverable.
+"""
+import numpy as np
+
+# ---------------------------------------------------------------- spin operators
+# S = sigma/2 (TensorKitTensors convention, test/setup/testsetup.jl:13)
+
+
+def spin_ops(dtype=np.complex128):
+    sx = np.array([[0, 1], [1, 0]], dtype=np.complex128) / 2
+    sy = np.array([[0, -1j], [1j, 0]], dtype=np.complex128) / 2
+    sz = np.array([[1, 0], [0, -1]], dtype=np.complex128) / 2
+    if np.dtype(dtype).kind == "f":
+        # S_y S_y is real; single S_y is not -- only used inside products below
+        pass
+    return sx, sy, sz
+
+
+def two_site(op1, op2):
+    """2-site operator O[s1, s2, s1', s2'] = op1[s1, s1'] op2[s2, s2']."""
+    return np.einsum("ac,bd->abcd", op1, op2)
+
+
+def S_exchange(dtype=np.complex128):
+    """S.S for spin-1/2: O[s1, s2, s1', s2'] (testsetup.jl:121-134 uses S_exchange)."""
+    sx, sy, sz = spin_ops()
+    h = two_site(sx, sx) + two_site(sy, sy) + two_site(sz, sz)
+    return _cast(h, dtype)
+
+
+def _cast(a, dtype):
+    dtype = np.dtype(dtype)
+    if dtype.kind == "f":
+        assert np.abs(a.imag).max() < 1e-14, "operator is not real"
+        return np.ascontiguousarray(a.real.astype(dtype))
+    return np.ascontiguousarray(a.astype(dtype))
+
+
+def decompose_two_site(O, atol=None):
+    """Split O[s1,s2,s1',s2'] = sum_k W1[s1,s1',k] W2[k,s2,s2'] by truncated SVD.
+
+    Follows `decompose_localmpo` (utility.jl:54-66): left_orth with
+    trunctol(atol = eps^(3/4)); the left factor is the isometry U, the right factor S*Vh.
+    """
+    d1, d2 = O.shape[0], O.shape[1]
+    if atol is None:
+        atol = np.finfo(np.float64).eps ** 0.75
+    M = np.transpose(O, (0, 2, 1, 3)).reshape(d1 * d1, d2 * d2)
+    U, S, Vh = np.linalg.svd(M, full_matrices=False)
+    k = int(np.sum(S > atol))
+    W1 = U[:, :k].reshape(d1, d1, k)
+    W2 = (S[:k, None] * Vh[:k]).reshape(k, d2, d2)
+    return W1.astype(O.dtype), W2.astype(O.dtype)
+
+
+# ---------------------------------------------------------------- builder
+
+class MPOHam:
+    """Dense Jordan-form MPO Hamiltonian.
+
+    W[i] has shape (wl, d, d, wr); chans[i] are the channel dims of the bond left of
+    site i (chans[i+1] right of it).  For a finite chain chans[0] = chans[L] = [1].
+    """
+
+    def __init__(self, W, chans, finite=True):
+        self.W = W
+        self.chans = chans
+        self.finite = finite
+
+    def __len__(self):
+        return len(self.W)
+
+    def __getitem__(self, i):
+        return self.W[i % len(self.W)] if not self.finite else self.W[i]
+
+    @property
+    def dtype(self):
+        return self.W[0].dtype
+
+    def bond_dim(self, i):
+        return int(sum(self.chans[i]))
+
+    def max_width(self):
+        return max(w.shape[0] for w in self.W)
+
+
+def _instantiate(term_sites, ops):
+    """instantiate_operator (mpohamiltonian.jl:360-386): fill identity between sites.
+
+    term_sites: sorted unique site list; ops: list of per-site MPO pieces
+    ('t', tensor[kl, s, s', kr]) aligned with term_sites.  Returns (sites, local_mpo)
+    where local_mpo entries are tensors or the scalar 1 (identity pass-through).
+    """
+    sites, local = [], []
+    j = 0
+    for s in range(term_sites[0], term_sites[-1] + 1):
+        if s == term_sites[j]:
+            local.append(ops[j])
+            j += 1
+        else:
+            local.append(1.0)
+        sites.append(s)
+    return sites, local
+
+
+def _find_channel(keys, init=2):
+    """_find_channel (mpohamiltonian.jl:408-416), 1-based channel labels."""
+    init = max(init, 2)
+    rng = sorted(set(k[1] for k in keys))
+    if not rng:
+        return init
+    for i in range(init, max(max(rng), 2) + 1):
+        if i not in rng:
+            return i
+    return max(max(rng) + 1, init)
+
+
+def _term_pieces(sites, op):
+    """Turn a 1- or 2-site operator into per-site MPO pieces with unit legs."""
+    if len(sites) == 1:
+        return [op.reshape(1, op.shape[0], op.shape[1], 1)]
+    assert len(sites) == 2
+    W1, W2 = decompose_two_site(op)
+    k = W1.shape[2]
+    return [W1.reshape(1, W1.shape[0], W1.shape[1], k),
+            W2.reshape(k, W2.shape[1], W2.shape[2], 1)]
+
+
+def _canonical_term(sites, op):
+    """Sort the two sites of a term ascending (canonicalize_indices!, mpohamiltonian.jl:388-404)."""
+    if len(sites) == 2 and sites[0] > sites[1]:
+        sites = (sites[1], sites[0])
+        op = np.transpose(op, (1, 0, 3, 2))
+    assert len(sites) == 1 or sites[0] != sites[1]
+    return tuple(sites), op
+
+
+def finite_mpo_hamiltonian(L, d, terms, dtype=np.complex128):
+    """FiniteMPOHamiltonian(lattice, terms) -- mpohamiltonian.jl:439-519.
+
+    terms: iterable of (sites_tuple (0-based), operator) with 1-site op[s; s'] or
+    2-site op[s1, s2; s1', s2'] (any site distance).
+    """
+    keys = [[] for _ in range(L)]
+    opps = [[] for _ in range(L)]
+    local_mpos = []
+    for sites, op in terms:
+        sites, op = _canonical_term(tuple(sites), np.asarray(op, dtype=dtype))
+        pieces = _term_pieces(sites, op)
+        local_mpos.append(_instantiate(list(sites), pieces))
+    local_mpos.sort(key=lambda x: len(x[0]))  # stable, like Julia's default sort
+    for sites, local in local_mpos:
+        key_R = None
+        for i, (site, O) in enumerate(zip(sites, local)):
+            key_L = 1 if i == 0 else key_R
+            key_R = 0 if i == len(local) - 1 else _find_channel(keys[site], init=key_L)
+            keys[site].append((key_L, key_R))
+            opps[site].append(O)
+
+    # virtual sum spaces (mpohamiltonian.jl:484-500); channel dims per bond
+    chans = [None] * (L + 1)
+    chans[0] = [1]
+    chans[L] = [1]
+    for i in range(L - 1):
+        n = max([k[1] for k in keys[i]] + [1]) + 1
+        V = [1] * n
+        if n > 2:
+            for (kl, kr), O in zip(keys[i], opps[i]):
+                idx = n - 1 if kr == 0 else kr - 1
+                V[idx] = chans[i][kl - 1] if not isinstance(O, np.ndarray) else O.shape[3]
+        chans[i + 1] = V
+
+    Ws = []
+    for site in range(L):
+        cl, cr = chans[site], chans[site + 1]
+        offl = np.concatenate([[0], np.cumsum(cl)]).astype(int)
+        offr = np.concatenate([[0], np.cumsum(cr)]).astype(int)
+        W = np.zeros((offl[-1], d, d, offr[-1]), dtype=dtype)
+        # JordanMPOTensor(undef) identities at the corners (jordanmpotensor.jl:58-66)
+        rows, cols = len(cl), len(cr)
+        if cols > 1:
+            W[0, :, :, 0] += np.eye(d)
+        if rows > 1:
+            W[offl[-2], :, :, offr[-2]] += np.eye(d)
+        for (kl, kr_), o in zip(keys[site], opps[site]):
+            kr = cols if kr_ == 0 else kr_
+            sl = slice(offl[kl - 1], offl[kl])
+            sr = slice(offr[kr - 1], offr[kr])
+            if isinstance(o, np.ndarray):
+                W[sl, :, :, sr] += o
+            else:
+                if o == 0:
+                    continue
+                dl = offl[kl] - offl[kl - 1]
+                assert dl == offr[kr] - offr[kr - 1]
+                W[sl, :, :, sr] += o * np.einsum("ac,bd->abdc", np.eye(dl), np.eye(d))
+        Ws.append(W)
+    return MPOHam(Ws, chans, finite=True)
+
+
+def infinite_mpo_hamiltonian(Lc, d, terms, dtype=np.complex128):
+    """InfiniteMPOHamiltonian(lattice, terms) -- mpohamiltonian.jl:521-641 (unit cell Lc).
+
+    Sites of a term may exceed the unit cell; they are taken modulo Lc.
+    """
+    keys = [[] for _ in range(Lc)]
+    opps = [[] for _ in range(Lc)]
+    local_mpos = []
+    for sites, op in terms:
+        sites, op = _canonical_term(tuple(sites), np.asarray(op, dtype=dtype))
+        pieces = _term_pieces(sites, op)
+        local_mpos.append(_instantiate(list(sites), pieces))
+    local_mpos.sort(key=lambda x: len(x[0]))
+    for sites, local in local_mpos:
+        key_R = None
+        for i, (site, O) in enumerate(zip(sites, local)):
+            s = site % Lc
+            key_L = 1 if i == 0 else key_R
+            key_R = 0 if i == len(local) - 1 else _find_channel(keys[s], init=key_L)
+            keys[s].append((key_L, key_R))
+            opps[s].append(O)
+    nop = max(max([k[1] for k in K] + [1]) + 1 for K in keys)
+    # virtualspaces[i] = bond right of site i (mpohamiltonian.jl:549-600)
+    vs = [[None] * nop for _ in range(Lc)]
+    for V in vs:
+        V[0] = 1
+        V[-1] = 1
+    for i in range(Lc):
+        for (kl, kr_), O in zip(keys[i], opps[i]):
+            if not isinstance(O, np.ndarray):
+                continue
+            kr = nop if kr_ == 0 else kr_
+            left = vs[(i - 1) % Lc]
+            if left[kl - 1] is None:
+                left[kl - 1] = O.shape[0]
+            assert left[kl - 1] == O.shape[0]
+            if vs[i][kr - 1] is None:
+                vs[i][kr - 1] = O.shape[3]
+            assert vs[i][kr - 1] == O.shape[3]
+    changed = True
+    while changed:
+        changed = False
+        for i in range(Lc):
+            for (kl, kr_), O in zip(keys[i], opps[i]):
+                if isinstance(O, np.ndarray):
+                    continue
+                kr = nop if kr_ == 0 else kr_
+                left = vs[(i - 1) % Lc]
+                if left[kl - 1] is not None and vs[i][kr - 1] is None:
+                    vs[i][kr - 1] = left[kl - 1]
+                    changed = True
+                if left[kl - 1] is None and vs[i][kr - 1] is not None:
+                    left[kl - 1] = vs[i][kr - 1]
+                    changed = True
+    vs = [[1 if v is None else v for v in V] for V in vs]
+    chans = [vs[(i - 1) % Lc] for i in range(Lc)] + [vs[Lc - 1]]
+    Ws = []
+    for site in range(Lc):
+        cl, cr = vs[(site - 1) % Lc], vs[site]
+        offl = np.concatenate([[0], np.cumsum(cl)]).astype(int)
+        offr = np.concatenate([[0], np.cumsum(cr)]).astype(int)
+        W = np.zeros((offl[-1], d, d, offr[-1]), dtype=dtype)
+        W[0, :, :, 0] += np.eye(d)
+        W[offl[-2], :, :, offr[-2]] += np.eye(d)
+        for (kl, kr_), o in zip(keys[site], opps[site]):
+            kr = nop if kr_ == 0 else kr_
+            sl = slice(offl[kl - 1], offl[kl])
+            sr = slice(offr[kr - 1], offr[kr])
+            if isinstance(o, np.ndarray):
+                W[sl, :, :, sr] += o
+            else:
+                if o == 0:
+                    continue
+                dl = offl[kl] - offl[kl - 1]
+                W[sl, :, :, sr] += o * np.einsum("ac,bd->abdc", np.eye(dl), np.eye(d))
+        Ws.append(W)
+    return MPOHam(Ws, chans, finite=False)
+
+
+# ---------------------------------------------------------------- model terms
+
+def heisenberg_terms(L, J=1.0, dtype=np.complex128, periodic=False):
+    """H = J sum_i S_i.S_{i+1} (heisenberg_XXX, testsetup.jl:121-134)."""
+    h = J * S_exchange(np.complex128)
+    n = L if periodic else L - 1
+    return [((i, i + 1), _cast(h, dtype)) for i in range(n)]
+
+
+def xxz_terms(L, Jxy=1.0, Jz=1.0, hz=0.0, dtype=np.complex128, periodic=False):
+    """H = sum Jxy (SxSx + SySy) + Jz SzSz - hz sum Sz."""
+    sx, sy, sz = spin_ops()
+    h = Jxy * (two_site(sx, sx) + two_site(sy, sy)) + Jz * two_site(sz, sz)
+    n = L if periodic else L - 1
+    terms = [((i, i + 1), _cast(h, dtype)) for i in range(n)]
+    if hz != 0.0:
+        terms += [((i,), _cast(-hz * sz, dtype)) for i in range(L)]
+    return terms
+
+
+def tfim_terms(L, g=1.0, J=1.0, dtype=np.complex128, periodic=False):
+    """H = -J sum ZZ - g sum X with X = 2Sx, ZZ = 4SzSz (testsetup.jl:102-119)."""
+    sx, sy, sz = spin_ops()
+    X = 2 * sx
+    ZZ = 4 * two_site(sz, sz)
+    n = L if periodic else L - 1
+    terms = [((i,), _cast(-g * X, dtype)) for i in range(L)]
+    terms += [((i, i + 1), _cast(-J * ZZ, dtype)) for i in range(n)]
+    return terms
+
+
+def tfim_doctest_terms(L, dtype=np.float64):
+    """find_groundstate.jl:49-64 doctest: H = -sum X X - sum Z with Pauli matrices."""
+    X = np.array([[0, 1], [1, 0]], dtype=np.float64)
+    Z = np.array([[1, 0], [0, -1]], dtype=np.float64)
+    terms = [((i, i + 1), -two_site(X, X).astype(dtype)) for i in range(L - 1)]
+    terms += [((i,), -Z.astype(dtype)) for i in range(L)]
+    return terms
+
+
+def cylinder_sites(Lx, Ly):
+    """Snake (boustrophedon) order of an Lx x Ly cylinder: column x runs up for even x,
+    down for odd x.  Returns index(x, y)."""
+    def idx(x, y):
+        y %= Ly
+        return x * Ly + (y if x % 2 == 0 else Ly - 1 - y)
+    return idx
+
+
+def j1j2_cylinder_terms(Lx, Ly, J1=1.0, J2=0.5, dtype=np.float64):
+    """J1-J2 Heisenberg on an Lx x Ly cylinder (periodic y, open x), snake-ordered chain."""
+    idx = cylinder_sites(Lx, Ly)
+    h = S_exchange(np.complex128)
+    bonds = {}
+
+    def add(a, b, J):
+        if a == b:
+            return
+        key = (min(a, b), max(a, b))
+        bonds[key] = bonds.get(key, 0.0) + J
+
+    for x in range(Lx):
+        for y in range(Ly):
+            if Ly > 2 or y + 1 < Ly:
+                add(idx(x, y), idx(x, y + 1), J1)
+            if x + 1 < Lx:
+                add(idx(x, y), idx(x + 1, y), J1)
+                add(idx(x, y), idx(x + 1, y + 1), J2)
+                add(idx(x, y), idx(x + 1, y - 1), J2)
+    return [((a, b), _cast(J * h, dtype)) for (a, b), J in sorted(bonds.items())]
+
+
+# ---------------------------------------------------------------- exact diagonalisation
+
+def ed_hamiltonian(L, d, terms):
+    """Sparse H on (C^d)^L straight from the lattice terms (independent of the builder).
+    Site 0 is the most significant tensor factor."""
+    import scipy.sparse as sp
+    dim = d ** L
+    H = sp.csr_matrix((dim, dim), dtype=np.complex128)
+    for sites, op in terms:
+        op = np.asarray(op, dtype=np.complex128)
+        if len(sites) == 1:
+            (i,) = sites
+            m = sp.kron(sp.kron(sp.identity(d ** i), sp.csr_matrix(op)), sp.identity(d ** (L - i - 1)))
+            H = H + m
+        else:
+            i, j = sites
+            if i > j:
+                i, j = j, i
+                op = np.transpose(op, (1, 0, 3, 2))
+            # decompose into sum of products to place on non-adjacent sites
+            W1, W2 = decompose_two_site(op)
+            for k in range(W1.shape[2]):
+                a = sp.csr_matrix(W1[:, :, k])
+                b = sp.csr_matrix(W2[k])
+                m = sp.kron(sp.identity(d ** i), a)
+                m = sp.kron(m, sp.identity(d ** (j - i - 1)))
+                m = sp.kron(m, b)
+                m = sp.kron(m, sp.identity(d ** (L - j - 1)))
+                H = H + m
+    return H.tocsr()
+
+
+def ed_ground_energy(L, d, terms, k=1):
+    import scipy.sparse.linalg as sla
+    H = ed_hamiltonian(L, d, terms)
+    if H.shape[0] <= 256:
+        return np.linalg.eigvalsh(H.toarray())[:k]
+    vals = sla.eigsh(H, k=k, which="SA", tol=1e-13)[0]
+    return np.sort(vals)
+
+
+def tfim_open_chain_energy(L, g=1.0, J=1.0):
+    """Free-fermion ground energy of H = -J sum_{i<L} s^z s^z - g sum s^x (Pauli), open chain."""
+    # Jordan-Wigner: quadratic form with A (hopping) and B (pairing); E0 = -sum(eps)/2... use BdG
+    # 2L x 2L Majorana form; the single-particle energies are the |imag| eigenvalues.
+    M = np.zeros((2 * L, 2 * L))
+    for i in range(L):
+        M[2 * i, 2 * i + 1] += g
+        M[2 * i + 1, 2 * i] -= g
+    for i in range(L - 1):
+        M[2 * i + 1, 2 * i + 2] += J
+        M[2 * i + 2, 2 * i + 1] -= J
+    ev = np.linalg.eigvals(M)
+    eps = np.sort(np.abs(ev.imag))[::2]
+    return -float(np.sum(eps))
+
+
+def tfim_infinite_energy_density(g, J=1.0, n=200001):
+    """e(g) = -(1/pi) int_0^pi sqrt(J^2 + g^2 + 2 J g cos k) dk (Pauli convention)."""
+    k = np.linspace(0, np.pi, n)
+    f = np.sqrt(J * J + g * g + 2 * J * g * np.cos(k))
+    return -float(np.trapezoid(f, k) / np.pi)

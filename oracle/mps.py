@@ -1,0 +1,432 @@
+"""Finite MPS containers, gauge steps and the DMRG / DMRG2 drivers (oracle).
+
+Restates:
+  * FiniteMPS(f, elt, P, maxV) random constructor + QR normalisation sweep
+      -- src/states/finitemps.jl:229-282 (positive QR at :234-237)
+  * AC2(psi, site; kind)                    -- src/states/finitemps.jl:376-385
+  * left_gauge / right_gauge / gauge2!      -- src/states/orthoview.jl:322-420
+  * project_complement!                     -- src/utility/utility.jl:22
+  * calc_galerkin                           -- src/algorithms/toolbox.jl:63-70
+  * adapt_solver(::AdaptiveKrylov)          -- src/utility/dynamictols.jl:182-235
+  * DMRG / DMRG2 local_update! and sweep    -- src/algorithms/groundstate/dmrg.jl:121-354
+  * FiniteEnvironments leftenv / rightenv   -- src/environments/finite_envs.jl:31-49, 110-151
+  * expectation_value(FiniteMPS, H)         -- src/algorithms/expval.jl:136-141
+
+Sites are 0-based.  C[b] is the bond matrix between site b-1 and site b
+(C[0], C[L] are the 1x1 boundaries).  GL[i] is the left environment of site i,
+GR[i] the right environment of site i.
+"""
+import numpy as np
+
+from . import derivatives as dv
+from .krylov import lanczos_eigsolve
+
+
+# ---------------------------------------------------------------- factorisations
+
+def qr_pos(M):
+    """QR with non-negative diagonal of R (MatrixAlgebraKit Householder(positive=true))."""
+    Q, R = np.linalg.qr(M)
+    s = np.sign(np.diag(R).real)
+    s[s == 0] = 1
+    # for complex diagonal, rotate the phase to the positive real axis
+    ph = np.diag(R) / np.where(np.abs(np.diag(R)) > 0, np.abs(np.diag(R)), 1)
+    ph[np.abs(np.diag(R)) == 0] = 1
+    Q = Q * ph[None, :]
+    R = R * ph.conj()[:, None]
+    return Q, R
+
+
+def lq_pos(M):
+    """LQ with non-negative diagonal of L."""
+    Q, R = qr_pos(M.conj().T)
+    return R.conj().T, Q.conj().T
+
+
+def svd_trunc(M, maxdim=None, atol=0.0):
+    """svd_trunc with truncrank(maxdim) & trunctol(atol=atol).  Returns U, S, Vh, eps
+    where eps is the 2-norm of the discarded singular values."""
+    U, S, Vh = np.linalg.svd(M, full_matrices=False)
+    keep = int(np.sum(S > atol))
+    if maxdim is not None:
+        keep = min(keep, maxdim)
+    keep = max(keep, 1)
+    eps = float(np.linalg.norm(S[keep:]))
+    return U[:, :keep], S[:keep], Vh[:keep], eps
+
+
+# ---------------------------------------------------------------- FiniteMPS
+
+class FiniteMPS:
+    """AL/AR/C storage with an explicit centre bond: AL[i] is valid for i < center,
+    AR[i] for i >= center, C[center] is the current centre matrix."""
+
+    def __init__(self, AL, AR, C, center=0):
+        self.AL = AL
+        self.AR = AR
+        self.C = C
+        self.center = center
+
+    def __len__(self):
+        return len(self.AL)
+
+    def copy(self):
+        cp = lambda xs: [None if x is None else x.copy() for x in xs]
+        return FiniteMPS(cp(self.AL), cp(self.AR), cp(self.C), self.center)
+
+    def ac(self, i):
+        """The centre-site tensor AC[i] for a centre bond at i or i+1."""
+        if self.center == i:
+            return self.AC(i)
+        if self.center == i + 1:
+            return self.ACL(i)
+        raise ValueError(f"site {i} is not adjacent to the centre bond {self.center}")
+
+    def al(self, i):
+        """AL[i]; computed from AC[i] by a positive QR when the centre bond is i
+        (the reference computes it lazily the same way)."""
+        if i < self.center:
+            return self.AL[i]
+        ac = self.ac(i)
+        Dl, d, Dr = ac.shape
+        Q, _ = qr_pos(ac.reshape(Dl * d, Dr, order="F"))
+        return Q.reshape(Dl, d, Q.shape[1], order="F")
+
+    def AC(self, i):
+        """AC[i] = C[i] * AR[i] (valid when the centre bond is i)."""
+        return np.einsum("ab,bsc->asc", self.C[i], self.AR[i])
+
+    def ACL(self, i):
+        """AC[i] = AL[i] * C[i+1] (valid when the centre bond is i+1)."""
+        return np.einsum("asb,bc->asc", self.AL[i], self.C[i + 1])
+
+    @property
+    def dtype(self):
+        return self.AL[0].dtype
+
+
+def bond_dims(L, d, D):
+    """Virtual dims limited to full rank (finitemps.jl:257-274)."""
+    V = [1] * (L + 1)
+    for k in range(1, L):
+        V[k] = min(V[k - 1] * d, D)
+    for k in range(L - 1, 0, -1):
+        V[k] = min(V[k], V[k + 1] * d)
+    return V
+
+
+def random_initial_tensors(L, d, D, seed, dtype=np.complex128):
+    """Seeded i.i.d. normal entries (re, im ~ N(0,1) for complex) on the full-rank
+    virtual spaces -- the synthetic stand-in for `FiniteMPS(randn, elt, ...)`."""
+    rng = np.random.default_rng(seed)
+    V = bond_dims(L, d, D)
+    As = []
+    for i in range(L):
+        shape = (V[i], d, V[i + 1])
+        if np.dtype(dtype).kind == "c":
+            a = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+        else:
+            a = rng.standard_normal(shape)
+        # store in Fortran (column-major) order like TensorKit; values are order-agnostic
+        As.append(np.asarray(a, dtype=dtype))
+    return As
+
+
+def finite_mps_from_tensors(As, normalize=True):
+    """FiniteMPS(As; normalize) (finitemps.jl:229-250): positive-QR sweep left->right,
+    then an LQ sweep right->left to build the AR gauge (what the reference does lazily
+    on first access of `psi.AR`)."""
+    L = len(As)
+    As = [a.copy() for a in As]
+    AL = [None] * L
+    C = [None] * (L + 1)
+    for i in range(L):
+        Dl, d, Dr = As[i].shape
+        M = As[i].reshape(Dl * d, Dr, order="F")
+        Q, R = qr_pos(M)
+        AL[i] = Q.reshape(Dl, d, Q.shape[1], order="F")
+        if normalize:
+            R = R / np.linalg.norm(R)
+        if i < L - 1:
+            As[i + 1] = np.einsum("ab,bsc->asc", R, As[i + 1])
+    C[L] = R
+    psi = FiniteMPS(AL, [None] * L, C, center=L)
+    right_canonicalize(psi)
+    return psi
+
+
+def right_canonicalize(psi):
+    """Build AR[i] and C[i] from the centre at bond L by positive LQ moves."""
+    L = len(psi)
+    X = psi.C[L]
+    for i in range(L - 1, -1, -1):
+        A = np.einsum("asb,bc->asc", psi.AL[i], X)
+        Dl, d, Dr = A.shape
+        M = A.reshape(Dl, d * Dr, order="F")
+        Lm, Q = lq_pos(M)
+        psi.AR[i] = Q.reshape(Q.shape[0], d, Dr, order="F")
+        X = Lm
+        psi.C[i] = Lm
+    # C[0] is the 1x1 norm factor
+    psi.center = 0
+    return psi
+
+
+# ---------------------------------------------------------------- environments
+
+class FiniteEnvironments:
+    """Lazy GL/GR cache keyed on object identity of AL/AR (finite_envs.jl:110-151)."""
+
+    def __init__(self, psi, H):
+        L = len(psi)
+        dt = np.result_type(psi.dtype, H.dtype)
+        self.H = H
+        self.GL = [None] * (L + 1)
+        self.GR = [None] * (L + 1)
+        self.GL[0] = np.ones((1, 1, 1), dtype=dt)
+        self.GR[L - 1] = np.ones((1, 1, 1), dtype=dt)
+        self.ldep = [None] * L
+        self.rdep = [None] * L
+
+    def leftenv(self, i, psi):
+        a = None
+        for j in range(i):
+            if psi.AL[j] is not self.ldep[j]:
+                a = j
+                break
+        if a is not None:
+            for j in range(a, i):
+                self.GL[j + 1] = dv.transfer_left(self.GL[j], self.H[j], psi.AL[j], psi.AL[j])
+                self.ldep[j] = psi.AL[j]
+        return self.GL[i]
+
+    def rightenv(self, i, psi):
+        L = len(psi)
+        a = None
+        for j in range(L - 1, i, -1):
+            if psi.AR[j] is not self.rdep[j]:
+                a = j
+                break
+        if a is not None:
+            for j in range(a, i, -1):
+                self.GR[j - 1] = dv.transfer_right(self.GR[j], self.H[j], psi.AR[j], psi.AR[j])
+                self.rdep[j] = psi.AR[j]
+        return self.GR[i]
+
+
+def AC2_hamiltonian(pos, psi, H, envs, prepare=True):
+    return dv.JordanAC2(envs.leftenv(pos, psi), H[pos], H[pos + 1],
+                        envs.rightenv(pos + 1, psi), prepare=prepare)
+
+
+def AC_hamiltonian(pos, psi, H, envs, prepare=True):
+    return dv.JordanAC(envs.leftenv(pos, psi), H[pos], envs.rightenv(pos, psi), prepare=prepare)
+
+
+def expectation_value(psi, H, envs, site=0):
+    """<psi|H|psi> / <psi|psi> evaluated at a site whose AC is current (expval.jl:136-141)."""
+    AC = psi.ac(site)
+    Heff = AC_hamiltonian(site, psi, H, envs)
+    return np.vdot(AC, Heff(AC)).real / np.vdot(AC, AC).real
+
+
+# ---------------------------------------------------------------- adaptive solver
+
+class AdaptiveKrylov:
+    """AdaptiveKrylov defaults (dynamictols.jl:182-194)."""
+
+    def __init__(self, krylovdim_min=3, krylovdim_max=20, iter_min=1, iter_max=1,
+                 tol_min=1e-12, tol_max=1e-2, truncation_factor=1e-1, tol_factor=1e-1,
+                 eager=True):
+        self.krylovdim_min = krylovdim_min
+        self.krylovdim_max = krylovdim_max
+        self.iter_min = iter_min
+        self.iter_max = iter_max
+        self.tol_min = tol_min
+        self.tol_max = tol_max
+        self.truncation_factor = truncation_factor
+        self.tol_factor = tol_factor
+        self.eager = eager
+
+    def adapt(self, decay_rate=0.0, g_local=0.0, g_global=0.0, eps_trunc=0.0):
+        """adapt_solver(::AdaptiveKrylov) (dynamictols.jl:204-235) -> (krylovdim, maxiter, tol)."""
+        tol = min(max(max(self.truncation_factor * eps_trunc, self.tol_factor * g_global),
+                      self.tol_min), self.tol_max)
+        rho = min(max(decay_rate, 0.0), 1.0)
+        if not (0 < rho < 1):
+            if rho == 0:
+                return self.krylovdim_min, self.iter_min, tol
+            return self.krylovdim_max, self.iter_max, tol
+        R = max(g_local, self.tol_min) / tol
+        nmat = int(round(np.log(R) / np.log(1 / rho)))
+        kd = min(max(nmat, self.krylovdim_min), self.krylovdim_max)
+        cld = -((-5 * nmat) // (2 * kd))
+        mi = min(max(cld - 3, self.iter_min), self.iter_max)
+        return kd, mi, tol
+
+
+# ---------------------------------------------------------------- DMRG2 / DMRG
+
+class DMRG2:
+    def __init__(self, maxdim, cutoff=0.0, tol=1e-10, maxiter=200, alg_eigsolve=None):
+        self.maxdim = maxdim
+        self.cutoff = cutoff
+        self.tol = tol
+        self.maxiter = maxiter
+        self.alg_eigsolve = alg_eigsolve or AdaptiveKrylov()
+
+
+class DMRG:
+    def __init__(self, tol=1e-10, maxiter=200, alg_eigsolve=None):
+        self.tol = tol
+        self.maxiter = maxiter
+        self.alg_eigsolve = alg_eigsolve or AdaptiveKrylov()
+
+
+def _as_mat(x, nl):
+    """Column-major matricisation: first `nl` legs are rows."""
+    s = x.shape
+    return x.reshape(int(np.prod(s[:nl])), -1, order="F")
+
+
+def project_complement(Y, AL):
+    """Y <- (1 - AL AL') Y on the first two legs (utility.jl:22)."""
+    Dl, d, Dm = AL.shape
+    Ym = _as_mat(Y, 2)
+    A = AL.reshape(Dl * d, Dm, order="F")
+    Ym = Ym - A @ (A.conj().T @ Ym)
+    return Ym.reshape(Y.shape, order="F")
+
+
+def dmrg2_local_update(pos, right, psi, H, alg, envs, eps_global, eps_trunc, decay_rate, stats):
+    """local_update!(..., ::DMRG2) (dmrg.jl:211-244)."""
+    Heff = AC2_hamiltonian(pos, psi, H, envs)
+    if right:   # kind = :ACAR
+        ac2 = np.einsum("asm,mtb->asbt", psi.ac(pos), psi.AR[pos + 1])
+    else:       # kind = :ALAC
+        ac2 = np.einsum("asm,mtb->asbt", psi.AL[pos], psi.ac(pos + 1))
+    y = Heff(ac2)
+    stats["matvecs"] += 1
+    y = y / np.linalg.norm(y)
+    y = project_complement(y, psi.al(pos))
+    eps_local = float(np.linalg.norm(y))
+    kd, mi, tol = alg.alg_eigsolve.adapt(decay_rate, eps_local, eps_global, eps_trunc)
+    val, new, info = lanczos_eigsolve(Heff, ac2, krylovdim=kd, maxiter=mi, tol=tol,
+                                      eager=alg.alg_eigsolve.eager)
+    stats["matvecs"] += info.numops
+    # gauge2! with truncated SVD (orthoview.jl:401-420)
+    Dl, d1, Dr, d2 = new.shape
+    M = new.reshape(Dl * d1, Dr * d2, order="F")
+    U, S, Vh, eps_tr = svd_trunc(M, alg.maxdim, alg.cutoff)
+    S = S / np.linalg.norm(S)
+    k = S.size
+    al = U.reshape(Dl, d1, k, order="F")
+    ar = np.transpose(Vh.reshape(k, Dr, d2, order="F"), (0, 2, 1))
+    C = np.diag(S).astype(psi.dtype)
+    psi.AL[pos] = np.ascontiguousarray(al.astype(psi.dtype))
+    psi.AR[pos + 1] = np.ascontiguousarray(ar.astype(psi.dtype))
+    psi.C[pos + 1] = C
+    psi.center = pos + 1
+    decay = min(max((info.normres / eps_local) ** (1 / max(1, info.numops)), 1e-3), 0.999) \
+        if eps_local > 0 else 0.999
+    return eps_local, eps_tr, decay, val
+
+
+def find_groundstate_dmrg2(psi, H, alg, envs=None, maxsweeps=None, verbose=False):
+    """_find_groundstate_sweep! for DMRG2 (dmrg.jl:286-354).  Returns (psi, envs, eps, hist)."""
+    psi = psi.copy()
+    envs = envs or FiniteEnvironments(psi, H)
+    L = len(psi)
+    n = L - 1
+    eps_locals = np.ones(n)
+    eps_global = float(eps_locals.max())
+    eps_truncs = np.zeros(n)
+    decays = np.zeros(n)
+    fwd = list(range(0, L - 1))
+    bwd = list(range(L - 3, -1, -1))
+    hist = []
+    stats = {"matvecs": 0}
+    niter = alg.maxiter if maxsweeps is None else maxsweeps
+    for it in range(niter):
+        for pos in fwd:
+            eps_locals[pos], eps_truncs[pos], decays[pos], val = dmrg2_local_update(
+                pos, True, psi, H, alg, envs, eps_global, eps_truncs[pos], decays[pos], stats)
+            eps_global = float(eps_locals.max())
+        for pos in bwd:
+            eps_locals[pos], eps_truncs[pos], decays[pos], val = dmrg2_local_update(
+                pos, False, psi, H, alg, envs, eps_global, eps_truncs[pos], decays[pos], stats)
+            eps_global = float(eps_locals.max())
+        eps_global = float(eps_locals.max())
+        E = expectation_value_center(psi, H, envs, 0)
+        hist.append((it, E, eps_global))
+        if verbose:
+            print(f"DMRG2 sweep {it}: E={E:.14f} eps={eps_global:.3e}")
+        if eps_global <= max(alg.tol, float(eps_truncs.max())):
+            break
+    return psi, envs, eps_global, hist
+
+
+def expectation_value_center(psi, H, envs, pos):
+    """Energy with the centre at bond pos+1 after a backward sweep (AC[pos] = AL C)."""
+    AC = psi.ac(pos)
+    Heff = dv.JordanAC(envs.leftenv(pos, psi), H[pos], envs.rightenv(pos, psi))
+    return float(np.vdot(AC, Heff(AC)).real / np.vdot(AC, AC).real)
+
+
+def dmrg1_local_update(pos, right, psi, H, alg, envs, eps_global, eps_trunc, decay_rate, stats):
+    """local_update!(..., ::DMRG) with the QR gauge (dmrg.jl:121-158)."""
+    ac = psi.ac(pos)
+    # calc_galerkin (toolbox.jl:63-70): AC_projection, normalise, project_complement
+    Heff = AC_hamiltonian(pos, psi, H, envs)
+    y = Heff(ac)
+    stats["matvecs"] += 1
+    y = y / np.linalg.norm(y)
+    # the galerkin error uses the AL of the current centre site
+    Dl, d, Dr = ac.shape
+    eps_local = float(np.linalg.norm(project_complement(y, psi.al(pos))))
+    kd, mi, tol = alg.alg_eigsolve.adapt(decay_rate, eps_local, eps_global, eps_trunc)
+    val, new, info = lanczos_eigsolve(Heff, ac, krylovdim=kd, maxiter=mi, tol=tol,
+                                      eager=alg.alg_eigsolve.eager)
+    stats["matvecs"] += info.numops
+    if right:
+        Q, R = qr_pos(new.reshape(Dl * d, Dr, order="F"))
+        R = R / np.linalg.norm(R)
+        psi.AL[pos] = Q.reshape(Dl, d, Dr, order="F")
+        psi.C[pos + 1] = R
+        psi.center = pos + 1
+    else:
+        Lm, Q = lq_pos(new.reshape(Dl, d * Dr, order="F"))
+        Lm = Lm / np.linalg.norm(Lm)
+        psi.AR[pos] = Q.reshape(Dl, d, Dr, order="F")
+        psi.C[pos] = Lm
+        psi.center = pos
+    decay = min(max((info.normres / eps_local) ** (1 / max(1, info.numops)), 1e-3), 0.999) \
+        if eps_local > 0 else 0.999
+    return eps_local, 0.0, decay, val
+
+
+def find_groundstate_dmrg(psi, H, alg, envs=None, maxsweeps=None):
+    """_find_groundstate_sweep! for single-site DMRG (dmrg.jl:250-354)."""
+    psi = psi.copy()
+    envs = envs or FiniteEnvironments(psi, H)
+    L = len(psi)
+    eps_locals = np.ones(L)
+    eps_global = 1.0
+    decays = np.zeros(L)
+    stats = {"matvecs": 0}
+    hist = []
+    niter = alg.maxiter if maxsweeps is None else maxsweeps
+    for it in range(niter):
+        for pos in range(0, L - 1):
+            eps_locals[pos], _, decays[pos], val = dmrg1_local_update(
+                pos, True, psi, H, alg, envs, eps_global, 0.0, decays[pos], stats)
+            eps_global = float(eps_locals.max())
+        for pos in range(L - 1, 0, -1):
+            eps_locals[pos], _, decays[pos], val = dmrg1_local_update(
+                pos, False, psi, H, alg, envs, eps_global, 0.0, decays[pos], stats)
+            eps_global = float(eps_locals.max())
+        E = float(val)
+        hist.append((it, E, eps_global))
+        if eps_global <= alg.tol:
+            break
+    return psi, envs, eps_global, hist
