@@ -1,0 +1,187 @@
+/*
+ * mpsgb.h -- C ABI of libmpsgb.so, the GB300 (sm_103a) effective-Hamiltonian engine
+ * that stands in for MPSKit.jl's derivative-operator hot path.
+ *
+ * Every entry point returns an int status (GB_OK = 0).  No C++ exception crosses the
+ * ABI; the message of the last failure on the calling thread is gb_last_error().
+ *
+ * Host buffers passed to *_upload / *_download hold tensors exactly as TensorKit stores
+ * a dense (Trivial-sector) TensorMap block: column-major, legs in TensorMap order
+ * (codomain legs, then domain legs).  The library keeps its own device layouts and
+ * converts at the boundary:
+ *
+ *   kind            reference leg order (host)    device layout (column-major)
+ *   GB_KIND_MPS     A[l s; r]                     (l, s, r)
+ *   GB_KIND_BOND    C[l; r]                       (l, r)
+ *   GB_KIND_AC2     x[l s1; r s2]                 (l, s1, s2, r)
+ *   GB_KIND_GL      GL[a w; a']                   (a, a', w)
+ *   GB_KIND_GR      GR[b' w; b]                   (b', w, b)
+ *   GB_KIND_MPO     W[wl s; s' wr] (dense over the (wl, s, s', wr)
+ *                   channel sum space; channel 0 = "not started", last = "finished")
+ *
+ * References (MPSKit.jl v0.13.13, paths relative to the project root) are given for
+ * each entry point: the reference interface the call replaces.
+ */
+#ifndef MPSGB_H
+#define MPSGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status codes */
+enum {
+  GB_OK = 0,
+  GB_ERR_ARG = 1,      /* invalid argument / shape mismatch                         */
+  GB_ERR_OOM = 2,      /* device allocation failed                                  */
+  GB_ERR_CUDA = 3,     /* CUDA runtime / library failure                            */
+  GB_ERR_NOCONV = 4,   /* reserved: non-convergence is reported in info.converged   */
+  GB_ERR_TIMEOUT = 5,  /* a bounded device wait gave up (kernel status word)        */
+  GB_ERR_NAN = 6,      /* non-finite value detected in a result                     */
+  GB_ERR_UNSUPPORTED = 7
+};
+
+enum { GB_F64 = 1, GB_C128 = 2 };
+
+enum {
+  GB_KIND_GENERIC = 0,
+  GB_KIND_MPS = 1,
+  GB_KIND_BOND = 2,
+  GB_KIND_AC2 = 3,
+  GB_KIND_GL = 4,
+  GB_KIND_GR = 5,
+  GB_KIND_MPO = 6
+};
+
+/* derivative-operator kinds */
+enum { GB_HEFF_C = 0, GB_HEFF_AC = 1, GB_HEFF_AC2 = 2 };
+
+/* arithmetic of the bulk contractions */
+enum {
+  GB_PREC_FP64 = 0,    /* plain FP64 (CUDA-core FMA)                                 */
+  GB_PREC_BF16X3 = 1   /* split precision: hi/lo BF16 operands, 3 products
+                          (hi*hi + hi*lo + lo*hi), FP32 accumulate in TMEM
+                          (tcgen05), FP64 output                                      */
+};
+
+typedef struct gb_ctx gb_ctx;
+typedef struct gb_tensor gb_tensor;
+typedef struct gb_heff gb_heff;
+
+/* KrylovKit ConvergenceInfo fields read by MPSKit (src/algorithms/groundstate/dmrg.jl:153,239,
+ * src/algorithms/timestep/integrators.jl:27) */
+typedef struct {
+  int converged;
+  int numops;
+  int numiter;
+  double normres;
+} gb_krylov_info;
+
+/* ---------------------------------------------------------------- library / context */
+int gb_version(void);
+const char* gb_last_error(void);
+
+/* One context per device and per host task; holds the stream, library handles and the
+ * launch counter.  (Replaces the per-sweep allocator/scheduler state of
+ * src/utility/allocator.jl:29-41.) */
+int gb_ctx_create(int device, uint32_t flags, gb_ctx** out);
+int gb_ctx_destroy(gb_ctx* ctx);
+int gb_ctx_synchronize(gb_ctx* ctx);
+/* number of libmpsgb kernels launched through this context so far */
+int gb_ctx_kernel_launches(gb_ctx* ctx, int64_t* out);
+/* device status word written by bounded waits inside kernels (0 = clean); cleared on read */
+int gb_ctx_device_status(gb_ctx* ctx, int32_t* out);
+/* arithmetic of the auxiliary state contractions of this context (gb_mps_ac2,
+ * gb_mps_mul_front, gb_mps_mul_tail); GB_PREC_FP64 by default */
+int gb_ctx_set_precision(gb_ctx* ctx, int precision);
+
+/* ---------------------------------------------------------------- tensors */
+/* Storage of TensorMap blocks (TensorKit `TensorMap{T,S,N1,N2}` with Trivial sectors). */
+int gb_tensor_create(gb_ctx* ctx, int kind, int dtype, int ndim, const int64_t* dims,
+                     gb_tensor** out);
+int gb_tensor_free(gb_tensor* t);
+int gb_tensor_shape(const gb_tensor* t, int* kind, int* dtype, int* ndim, int64_t* dims);
+int gb_tensor_upload(gb_tensor* t, const void* host, size_t bytes);
+int gb_tensor_download(const gb_tensor* t, void* host, size_t bytes);
+
+/* VectorInterface operations used by the Krylov solvers (KrylovKit over TensorMaps) */
+int gb_tensor_copy(gb_tensor* dst, const gb_tensor* src);
+int gb_tensor_scale(gb_tensor* t, double re, double im);
+int gb_tensor_axpy(gb_tensor* y, double re, double im, const gb_tensor* x);
+int gb_tensor_dot(const gb_tensor* x, const gb_tensor* y, double* re, double* im);
+int gb_tensor_norm(const gb_tensor* x, double* out);
+
+/* ---------------------------------------------------------------- derivative operators */
+/* Build and prepare an effective local operator.
+ *   GB_HEFF_AC2: JordanMPO_AC2_Hamiltonian(GL, W1, W2, GR) + prepare_operator!!
+ *                (src/algorithms/derivatives/hamiltonian_derivatives.jl:206-217, 272-468)
+ *   GB_HEFF_AC : JordanMPO_AC_Hamiltonian(GL, W, GR) + prepare_operator!!
+ *                (hamiltonian_derivatives.jl:44-157);  W2 must be NULL
+ *   GB_HEFF_C  : MPO_C_Hamiltonian(GL, GR)  (src/algorithms/derivatives/mpo_derivatives.jl:37-45,
+ *                92-98, 216-219);  W1 and W2 must be NULL
+ * GL/GR must be GB_KIND_GL/GB_KIND_GR tensors, W* GB_KIND_MPO. */
+int gb_heff_build(gb_ctx* ctx, int kind, const gb_tensor* GL, const gb_tensor* W1,
+                  const gb_tensor* W2, const gb_tensor* GR, int precision, gb_heff** out);
+int gb_heff_free(gb_heff* h);
+/* comma-separated list of the terms left after prepare, e.g. "IC,BE" */
+int gb_heff_terms(const gb_heff* h, char* buf, size_t len);
+/* algorithmic flops of one application (unsplit shapes; 2 flops/real MAC, 8/complex MAC) */
+int gb_heff_flops(const gb_heff* h, double* flops);
+int gb_heff_set_precision(gb_heff* h, int precision);
+/* y = H(x)   (hamiltonian_derivatives.jl:472-500; mpo_derivatives.jl:85-98) */
+int gb_heff_apply(gb_heff* h, const gb_tensor* x, gb_tensor* y);
+/* fixedpoint(H, x0, :SR, Lanczos(krylovdim, maxiter, tol, eager)) run entirely on the
+ * device (src/algorithms/fixedpoint.jl:15-18 -> KrylovKit.eigsolve).  x is overwritten with
+ * the normalised Ritz vector. */
+int gb_heff_eigsolve(gb_heff* h, gb_tensor* x, int krylovdim, int maxiter, double tol,
+                     int eager, double* lambda, gb_krylov_info* info);
+/* x <- exp(t H) x with t = t_re + i t_im  (src/algorithms/timestep/integrators.jl:44-53 ->
+ * KrylovKit.exponentiate).  x must be GB_C128 unless t is real. */
+int gb_heff_exponentiate(gb_heff* h, gb_tensor* x, double t_re, double t_im, int krylovdim,
+                         int maxiter, double tol, gb_krylov_info* info);
+
+/* ---------------------------------------------------------------- environments */
+/* GL_out = GL * TransferMatrix(A, W, Abar)   (src/transfermatrix/transfer.jl:125-127) */
+int gb_env_transfer_left(gb_ctx* ctx, const gb_tensor* GL, const gb_tensor* W,
+                         const gb_tensor* A, const gb_tensor* Abar, int precision,
+                         gb_tensor* GL_out);
+/* GR_out = TransferMatrix(A, W, Abar) * GR   (src/transfermatrix/transfer.jl:128-130) */
+int gb_env_transfer_right(gb_ctx* ctx, const gb_tensor* GR, const gb_tensor* W,
+                          const gb_tensor* A, const gb_tensor* Abar, int precision,
+                          gb_tensor* GR_out);
+/* regularize!(v, lvec, rvec): v -= tr(lvec * v) * rvec on the channel slice `chan` of an
+ * environment (src/transfermatrix/transfermatrix.jl:231-237) */
+int gb_env_regularize(gb_ctx* ctx, gb_tensor* env, int64_t chan, const gb_tensor* lvec,
+                      const gb_tensor* rvec);
+
+/* ---------------------------------------------------------------- state manipulation */
+/* AC2 = A * _transpose_tail(B)   (src/states/finitemps.jl:376-385) */
+int gb_mps_ac2(gb_ctx* ctx, const gb_tensor* A, const gb_tensor* B, gb_tensor* AC2);
+/* out = C * A   (mul_front, src/utility/utility.jl:11) */
+int gb_mps_mul_front(gb_ctx* ctx, const gb_tensor* C, const gb_tensor* A, gb_tensor* out);
+/* out = A * C   (mul_tail) */
+int gb_mps_mul_tail(gb_ctx* ctx, const gb_tensor* A, const gb_tensor* C, gb_tensor* out);
+/* Y <- (1 - X X') Y on the first two legs of Y (project_complement!, src/utility/utility.jl:22) */
+int gb_project_complement(gb_ctx* ctx, gb_tensor* Y, const gb_tensor* X);
+/* contract_mpo_expval-style scalar <x|y> after a heff apply is gb_tensor_dot. */
+
+/* ---------------------------------------------------------------- gauge */
+/* Truncated SVD of a two-site tensor, gauge2! (src/states/orthoview.jl:401-420) with
+ * truncrank(maxdim) & trunctol(atol): AL[l s1; k], S (diagonal, GB_KIND_BOND k x k),
+ * AR[k s2; r].  Returns the discarded-weight norm eps.  Outputs are newly created. */
+int gb_svd_trunc(gb_ctx* ctx, const gb_tensor* AC2, int64_t maxdim, double atol,
+                 int normalize, gb_tensor** AL, gb_tensor** S, gb_tensor** AR, double* eps);
+/* left_gauge(AC) with Householder(positive = true): AC = AL * C
+ * (src/states/orthoview.jl:322-326); outputs created. */
+int gb_left_orth(gb_ctx* ctx, const gb_tensor* AC, gb_tensor** AL, gb_tensor** C);
+/* right_gauge(AC): AC = C * AR (src/states/orthoview.jl:334-338); outputs created. */
+int gb_right_orth(gb_ctx* ctx, const gb_tensor* AC, gb_tensor** C, gb_tensor** AR);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MPSGB_H */

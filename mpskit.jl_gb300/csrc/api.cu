@@ -1,0 +1,1074 @@
+// C ABI of libmpsgb (declared in include/mpsgb.h): contexts, tensors with layout
+// conversion at the boundary, BLAS-1, environment transfers, state helpers and the
+// gauge factorisations.  Every entry point converts exceptions into status codes.
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <map>
+#include <mutex>
+#include <string>
+
+#include "gb_common.h"
+
+namespace gb {
+
+static thread_local std::string g_last_error;
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+void* scratch(gb_ctx* ctx, int slot, size_t bytes) {
+  Scratch& s = ctx->scratch[slot];
+  if (s.bytes >= bytes && s.ptr) return s.ptr;
+  if (s.ptr) {
+    GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+    cudaFree(s.ptr);
+    s.ptr = nullptr;
+    s.bytes = 0;
+  }
+  size_t nb = std::max<size_t>(bytes, 256);
+  cudaError_t e = cudaMalloc(&s.ptr, nb);
+  if (e != cudaSuccess) {
+    s.ptr = nullptr;
+    throw Error(GB_ERR_OOM, std::string("scratch cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  s.bytes = nb;
+  return s.ptr;
+}
+
+gb_heff* heff_build(gb_ctx* ctx, int kind, const gb_tensor* GL, const gb_tensor* W1,
+                    const gb_tensor* W2, const gb_tensor* GR, int prec);
+void heff_free(gb_heff* h);
+void heff_set_precision(gb_heff* h, int prec);
+void heff_apply_raw(gb_heff* h, const void* x, void* y);
+int heff_eigsolve_raw(gb_ctx* ctx, gb_heff* h, int64_t n, int dtype, void* x, int krylovdim,
+                      int maxiter, double tol, bool eager, double* lambda, gb_krylov_info* info);
+int heff_exponentiate_raw(gb_ctx* ctx, gb_heff* h, int64_t n, int dtype, void* x, double t_re,
+                          double t_im, int krylovdim, int maxiter, double tol,
+                          gb_krylov_info* info);
+
+}  // namespace gb
+
+// gb_heff is opaque here; these accessors live in heff_access below
+struct gb_heff;
+namespace gb {
+struct HeffInfo {
+  gb_ctx* ctx;
+  int kind, dtype, prec, xndim;
+  int64_t xdims[4];
+  int64_t xnumel;
+  double flops;
+  const char* terms;
+};
+HeffInfo heff_info(const gb_heff* h);
+}  // namespace gb
+
+using namespace gb;
+
+#define API_BEGIN try {
+#define API_END                                 \
+  }                                             \
+  catch (const gb::Error& e) {                  \
+    gb::set_last_error(e.what());               \
+    return e.code;                              \
+  }                                             \
+  catch (const std::exception& e) {             \
+    gb::set_last_error(e.what());               \
+    return GB_ERR_CUDA;                         \
+  }                                             \
+  catch (...) {                                 \
+    gb::set_last_error("unknown error");        \
+    return GB_ERR_CUDA;                         \
+  }                                             \
+  return GB_OK;
+
+namespace {
+
+struct DevGuard {
+  int prev = -1;
+  explicit DevGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DevGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+// device-layout strides of a tensor expressed over the reference leg order
+void ref_strides(int kind, int ndim, const int64_t* dims, int64_t* ref, int64_t* dev) {
+  // reference: plain column-major over dims
+  int64_t s = 1;
+  for (int i = 0; i < ndim; ++i) {
+    ref[i] = s;
+    s *= dims[i];
+  }
+  for (int i = 0; i < ndim; ++i) dev[i] = ref[i];
+  if (kind == GB_KIND_AC2) {  // ref (l, s1, r, s2) -> dev (l, s1, s2, r)
+    dev[0] = 1;
+    dev[1] = dims[0];
+    dev[3] = dims[0] * dims[1];
+    dev[2] = dims[0] * dims[1] * dims[3];
+  } else if (kind == GB_KIND_GL) {  // ref (a, w, a') -> dev (a, a', w)
+    dev[0] = 1;
+    dev[2] = dims[0];
+    dev[1] = dims[0] * dims[2];
+  }
+}
+
+bool needs_permute(int kind) { return kind == GB_KIND_AC2 || kind == GB_KIND_GL; }
+
+gb_tensor* new_tensor(gb_ctx* ctx, int kind, int dtype, int ndim, const int64_t* dims) {
+  GB_REQUIRE(ctx, "null context");
+  GB_REQUIRE(dtype == GB_F64 || dtype == GB_C128, "dtype must be GB_F64 or GB_C128");
+  GB_REQUIRE(ndim >= 1 && ndim <= 6, "ndim must be in 1..6");
+  int want = -1;
+  switch (kind) {
+    case GB_KIND_MPS: want = 3; break;
+    case GB_KIND_BOND: want = 2; break;
+    case GB_KIND_AC2: want = 4; break;
+    case GB_KIND_GL: want = 3; break;
+    case GB_KIND_GR: want = 3; break;
+    case GB_KIND_MPO: want = 4; break;
+    case GB_KIND_GENERIC: break;
+    default: throw Error(GB_ERR_ARG, "unknown tensor kind");
+  }
+  GB_REQUIRE(want < 0 || ndim == want, "tensor rank does not match its kind");
+  for (int i = 0; i < ndim; ++i) GB_REQUIRE(dims[i] >= 0, "negative dimension");
+  gb_tensor* t = new gb_tensor();
+  t->ctx = ctx;
+  t->kind = kind;
+  t->dtype = dtype;
+  t->ndim = ndim;
+  for (int i = 0; i < ndim; ++i) t->dims[i] = dims[i];
+  t->bytes = (size_t)numel(t) * elem_size(dtype);
+  if (t->bytes) {
+    cudaError_t e = cudaMallocAsync(&t->data, t->bytes, ctx->stream);
+    if (e != cudaSuccess) {
+      delete t;
+      throw Error(GB_ERR_OOM, std::string("tensor allocation: ") + cudaGetErrorString(e));
+    }
+  }
+  if (kind == GB_KIND_MPO) t->host_mpo.assign(numel(t) * (is_cplx(dtype) ? 2 : 1), 0.0);
+  return t;
+}
+
+void free_tensor(gb_tensor* t) {
+  if (!t) return;
+  if (t->data) cudaFreeAsync(t->data, t->ctx->stream);
+  delete t;
+}
+
+// ------------------------------------------------------------------ small kernels
+__global__ void conj_transpose_kernel(int64_t m, int64_t n, const double* __restrict__ A,
+                                      int64_t lda, double* __restrict__ B, int64_t ldb, int cx,
+                                      int conj) {
+  __shared__ double tr[32][33], ti[32][33];
+  int64_t i0 = (int64_t)blockIdx.x * 32, j0 = (int64_t)blockIdx.y * 32;
+  for (int k = threadIdx.y; k < 32; k += 8) {
+    int64_t i = i0 + threadIdx.x, j = j0 + k;
+    double re = 0, im = 0;
+    if (i < m && j < n) {
+      if (cx) {
+        re = A[2 * (i + lda * j)];
+        im = A[2 * (i + lda * j) + 1];
+      } else {
+        re = A[i + lda * j];
+      }
+    }
+    tr[k][threadIdx.x] = re;
+    ti[k][threadIdx.x] = conj ? -im : im;
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += 8) {
+    int64_t j = j0 + threadIdx.x, i = i0 + k;  // B[j, i] = A[i, j]
+    if (i < m && j < n) {
+      if (cx) {
+        B[2 * (j + ldb * i)] = tr[threadIdx.x][k];
+        B[2 * (j + ldb * i) + 1] = ti[threadIdx.x][k];
+      } else {
+        B[j + ldb * i] = tr[threadIdx.x][k];
+      }
+    }
+  }
+}
+
+void conj_transpose(gb_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A, int64_t lda,
+                    void* B, int64_t ldb) {
+  if (m == 0 || n == 0) return;
+  dim3 grid((unsigned)((m + 31) / 32), (unsigned)((n + 31) / 32));
+  conj_transpose_kernel<<<grid, dim3(32, 8), 0, ctx->stream>>>(
+      m, n, (const double*)A, lda, (double*)B, ldb, is_cplx(dtype), 1);
+  GB_CHECK_CUDA(cudaGetLastError());
+  count_launch(ctx);
+}
+
+// R (k x n) upper part of QR output A (lda), zero below the diagonal
+__global__ void extract_upper_kernel(int64_t k, int64_t n, const double* __restrict__ A,
+                                     int64_t lda, double* __restrict__ R, int cx) {
+  int64_t tot = k * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = e % k, j = e / k;
+    bool up = i <= j;
+    if (cx) {
+      R[2 * e] = up ? A[2 * (i + lda * j)] : 0.0;
+      R[2 * e + 1] = up ? A[2 * (i + lda * j) + 1] : 0.0;
+    } else {
+      R[e] = up ? A[i + lda * j] : 0.0;
+    }
+  }
+}
+
+// make diag(R) real non-negative: Q[:, j] *= ph_j, R[j, :] *= conj(ph_j)
+__global__ void fix_phase_kernel(int64_t m, int64_t k, int64_t n, double* __restrict__ Q,
+                                 int64_t ldq, double* __restrict__ R, int64_t ldr, int cx) {
+  int64_t j = blockIdx.x;
+  if (j >= k) return;
+  double pr, pi;
+  if (cx) {
+    double a = R[2 * (j + ldr * j)], b = R[2 * (j + ldr * j) + 1];
+    double r = hypot(a, b);
+    pr = r > 0 ? a / r : 1.0;
+    pi = r > 0 ? b / r : 0.0;
+  } else {
+    double a = R[j + ldr * j];
+    pr = a < 0 ? -1.0 : 1.0;
+    pi = 0.0;
+  }
+  __syncthreads();
+  for (int64_t i = threadIdx.x; i < m; i += blockDim.x) {
+    if (cx) {
+      double a = Q[2 * (i + ldq * j)], b = Q[2 * (i + ldq * j) + 1];
+      Q[2 * (i + ldq * j)] = a * pr - b * pi;
+      Q[2 * (i + ldq * j) + 1] = a * pi + b * pr;
+    } else {
+      Q[i + ldq * j] *= pr;
+    }
+  }
+  for (int64_t c = threadIdx.x; c < n; c += blockDim.x) {
+    if (cx) {  // times conj(ph)
+      double a = R[2 * (j + ldr * c)], b = R[2 * (j + ldr * c) + 1];
+      R[2 * (j + ldr * c)] = a * pr + b * pi;
+      R[2 * (j + ldr * c) + 1] = b * pr - a * pi;
+    } else {
+      R[j + ldr * c] *= pr;
+    }
+  }
+}
+
+// S (k reals) -> diagonal k x k matrix of dtype, scaled by s
+__global__ void diag_kernel(int64_t k, const double* __restrict__ S, double scl,
+                            double* __restrict__ out, int cx) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < k * k;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = e % k, j = e / k;
+    double v = (i == j) ? S[i] * scl : 0.0;
+    if (cx) {
+      out[2 * e] = v;
+      out[2 * e + 1] = 0.0;
+    } else {
+      out[e] = v;
+    }
+  }
+}
+
+cusolverDnHandle_t solver(gb_ctx* ctx) {
+  if (!ctx->solver) {
+    cusolverDnHandle_t h;
+    if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS)
+      throw Error(GB_ERR_CUDA, "cusolverDnCreate failed");
+    cusolverDnSetStream(h, ctx->stream);
+    cusolverDnParams_t p;
+    cusolverDnCreateParams(&p);
+    ctx->solver = h;
+    ctx->solver_params = p;
+  }
+  return (cusolverDnHandle_t)ctx->solver;
+}
+
+#define CUSOLVER_CHECK(x)                                                         \
+  do {                                                                            \
+    cusolverStatus_t _s = (x);                                                    \
+    if (_s != CUSOLVER_STATUS_SUCCESS)                                            \
+      throw Error(GB_ERR_CUDA, std::string(#x) + " failed: " + std::to_string(_s)); \
+  } while (0)
+
+// economy SVD of M (m x n, m >= n), col-major lda = m: U (m x n), S (n), VT (n x n)
+void svd_tall(gb_ctx* ctx, int dtype, int64_t m, int64_t n, void* A, void* U, double* S,
+              void* VT) {
+  cusolverDnHandle_t h = solver(ctx);
+  cudaDataType t = is_cplx(dtype) ? CUDA_C_64F : CUDA_R_64F;
+  size_t dws = 0, hws = 0;
+  CUSOLVER_CHECK(cusolverDnXgesvd_bufferSize(h, (cusolverDnParams_t)ctx->solver_params, 'S', 'S',
+                                             m, n, t, A, m, CUDA_R_64F, S, t, U, m, t, VT, n, t,
+                                             &dws, &hws));
+  void* dw = scratch(ctx, SLOT_TMP, dws + 256);
+  std::vector<char> hw(hws + 1);
+  int* dinfo = (int*)((char*)dw + ((dws + 127) & ~size_t(127)));
+  CUSOLVER_CHECK(cusolverDnXgesvd(h, (cusolverDnParams_t)ctx->solver_params, 'S', 'S', m, n, t,
+                                  A, m, CUDA_R_64F, S, t, U, m, t, VT, n, t, dw, dws, hw.data(),
+                                  hws, dinfo));
+  int hinfo = 0;
+  GB_CHECK_CUDA(cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  count_launch(ctx);
+  if (hinfo != 0) throw Error(GB_ERR_CUDA, "gesvd info = " + std::to_string(hinfo));
+}
+
+// positive QR of M (m x n): Q (m x k), R (k x n), k = min(m, n)
+void qr_pos(gb_ctx* ctx, int dtype, int64_t m, int64_t n, const void* M, void* Q, void* R) {
+  cusolverDnHandle_t h = solver(ctx);
+  const bool cx = is_cplx(dtype);
+  cudaDataType t = cx ? CUDA_C_64F : CUDA_R_64F;
+  const size_t es = elem_size(dtype);
+  int64_t k = std::min(m, n);
+  int64_t ncols = std::max(n, k);
+  // work matrix: m x n copy of M (plus room for orgqr on the first k columns)
+  char* A = (char*)scratch(ctx, SLOT_GAUGE, (size_t)m * ncols * es + 256);
+  GB_CHECK_CUDA(cudaMemcpyAsync(A, M, (size_t)m * n * es, cudaMemcpyDeviceToDevice, ctx->stream));
+  char* tau = (char*)scratch(ctx, SLOT_GAUGE3, (size_t)k * es + 256);
+  size_t dws = 0, hws = 0;
+  CUSOLVER_CHECK(cusolverDnXgeqrf_bufferSize(h, (cusolverDnParams_t)ctx->solver_params, m, n, t,
+                                             A, m, t, tau, t, &dws, &hws));
+  char* dw = (char*)scratch(ctx, SLOT_TMP, dws + 256);
+  int* dinfo = (int*)scratch(ctx, SLOT_TMP2, 256);
+  std::vector<char> hw(hws + 1);
+  CUSOLVER_CHECK(cusolverDnXgeqrf(h, (cusolverDnParams_t)ctx->solver_params, m, n, t, A, m, t,
+                                  tau, t, dw, dws, hw.data(), hws, dinfo));
+  count_launch(ctx);
+  // R = upper(A[:k, :])
+  extract_upper_kernel<<<256, 256, 0, ctx->stream>>>(k, n, (const double*)A, m, (double*)R, cx);
+  GB_CHECK_CUDA(cudaGetLastError());
+  count_launch(ctx);
+  // Q from the reflectors (first k columns)
+  int lwork = 0;
+  if (cx) {
+    CUSOLVER_CHECK(cusolverDnZungqr_bufferSize(h, (int)m, (int)k, (int)k, (cuDoubleComplex*)A,
+                                               (int)m, (cuDoubleComplex*)tau, &lwork));
+    char* wk = (char*)scratch(ctx, SLOT_TMP, (size_t)lwork * es + 256);
+    CUSOLVER_CHECK(cusolverDnZungqr(h, (int)m, (int)k, (int)k, (cuDoubleComplex*)A, (int)m,
+                                    (cuDoubleComplex*)tau, (cuDoubleComplex*)wk, lwork, dinfo));
+  } else {
+    CUSOLVER_CHECK(cusolverDnDorgqr_bufferSize(h, (int)m, (int)k, (int)k, (double*)A, (int)m,
+                                               (double*)tau, &lwork));
+    char* wk = (char*)scratch(ctx, SLOT_TMP, (size_t)lwork * es + 256);
+    CUSOLVER_CHECK(cusolverDnDorgqr(h, (int)m, (int)k, (int)k, (double*)A, (int)m, (double*)tau,
+                                    (double*)wk, lwork, dinfo));
+  }
+  count_launch(ctx);
+  GB_CHECK_CUDA(cudaMemcpyAsync(Q, A, (size_t)m * k * es, cudaMemcpyDeviceToDevice, ctx->stream));
+  fix_phase_kernel<<<(unsigned)k, 256, 0, ctx->stream>>>(m, k, n, (double*)Q, m, (double*)R, k,
+                                                         cx);
+  GB_CHECK_CUDA(cudaGetLastError());
+  count_launch(ctx);
+  int hinfo = 0;
+  GB_CHECK_CUDA(cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (hinfo != 0) throw Error(GB_ERR_CUDA, "QR info = " + std::to_string(hinfo));
+}
+
+// env-transfer mix plans cached per (W, side, dims)
+struct TransferKey {
+  const gb_tensor* W;
+  int side;
+  int64_t a, b, c;
+  bool operator<(const TransferKey& o) const {
+    return std::tie(W, side, a, b, c) < std::tie(o.W, o.side, o.a, o.b, o.c);
+  }
+};
+std::mutex g_tr_mu;
+std::map<TransferKey, MixDev> g_tr_cache;
+
+void drop_transfer_cache(const gb_tensor* W) {
+  std::lock_guard<std::mutex> lk(g_tr_mu);
+  for (auto it = g_tr_cache.begin(); it != g_tr_cache.end();) {
+    if (it->first.W == W) {
+      mix_free(it->second);
+      it = g_tr_cache.erase(it);
+    } else {
+      ++it;
+    }
+  }
+}
+
+double wval(const gb_tensor* W, int64_t a, int64_t s, int64_t t, int64_t b, double* im) {
+  int64_t i = a + W->dims[0] * (s + W->dims[1] * (t + W->dims[2] * b));
+  if (is_cplx(W->dtype)) {
+    *im = W->host_mpo[2 * i + 1];
+    return W->host_mpo[2 * i];
+  }
+  *im = 0;
+  return W->host_mpo[i];
+}
+
+const MixDev& transfer_plan(gb_ctx* ctx, const gb_tensor* W, int side, int64_t D1, int64_t D2,
+                            int64_t D3, bool cx) {
+  TransferKey key{W, side * 2 + (cx ? 1 : 0), D1, D2, D3};
+  std::lock_guard<std::mutex> lk(g_tr_mu);
+  auto it = g_tr_cache.find(key);
+  if (it != g_tr_cache.end()) return it->second;
+  const int64_t wl = W->dims[0], d = W->dims[1], wr = W->dims[3];
+  MixPlan p;
+  p.cplx = cx;
+  if (side == 0) {
+    // left: T1 (bra, s', kn, w) -> T2 (bra, s, kn, w'); D1 = Dbra, D2 = Dkn
+    p.A = D1;
+    p.N = D2;
+    p.xa = 1;
+    p.xn = D1 * d;
+    p.ya = 1;
+    p.yn = D1 * d;
+    p.nI = d * wl;
+    p.nJ = d * wr;
+    p.in_off.resize(p.nI);
+    p.out_off.resize(p.nJ);
+    for (int64_t u = 0; u < d; ++u)
+      for (int64_t w = 0; w < wl; ++w) p.in_off[u + d * w] = D1 * u + D1 * d * D2 * w;
+    for (int64_t s = 0; s < d; ++s)
+      for (int64_t v = 0; v < wr; ++v) p.out_off[s + d * v] = D1 * s + D1 * d * D2 * v;
+    p.row_ptr.push_back(0);
+    for (int64_t J = 0; J < p.nJ; ++J) {
+      int64_t s = J % d, v = J / d;
+      for (int64_t w = 0; w < wl; ++w)
+        for (int64_t u = 0; u < d; ++u) {
+          double im;
+          double re = wval(W, w, s, u, v, &im);
+          if (re == 0.0 && im == 0.0) continue;
+          p.col.push_back((int)(u + d * w));
+          p.val.push_back(re);
+          if (cx) p.val.push_back(im);
+        }
+      p.row_ptr.push_back((int)p.col.size());
+    }
+  } else {
+    // right: T1 (a, t, v, r) -> T2 (a, w, s, r); D1 = Dk, D3 = Dbra_r
+    p.A = D1;
+    p.N = D3;
+    p.xa = 1;
+    p.xn = D1 * d * wr;
+    p.ya = 1;
+    p.yn = D1 * wl * d;
+    p.nI = d * wr;
+    p.nJ = wl * d;
+    p.in_off.resize(p.nI);
+    p.out_off.resize(p.nJ);
+    for (int64_t t = 0; t < d; ++t)
+      for (int64_t v = 0; v < wr; ++v) p.in_off[t + d * v] = D1 * t + D1 * d * v;
+    for (int64_t w = 0; w < wl; ++w)
+      for (int64_t s = 0; s < d; ++s) p.out_off[w + wl * s] = D1 * w + D1 * wl * s;
+    p.row_ptr.push_back(0);
+    for (int64_t J = 0; J < p.nJ; ++J) {
+      int64_t w = J % wl, s = J / wl;
+      for (int64_t v = 0; v < wr; ++v)
+        for (int64_t t = 0; t < d; ++t) {
+          double im;
+          double re = wval(W, w, s, t, v, &im);
+          if (re == 0.0 && im == 0.0) continue;
+          p.col.push_back((int)(t + d * v));
+          p.val.push_back(re);
+          if (cx) p.val.push_back(im);
+        }
+      p.row_ptr.push_back((int)p.col.size());
+    }
+  }
+  MixDev m = mix_upload(ctx, p);
+  auto res = g_tr_cache.emplace(key, m);
+  return res.first->second;
+}
+
+void check_ctx(const gb_tensor* t, gb_ctx* ctx) {
+  GB_REQUIRE(t, "null tensor");
+  GB_REQUIRE(t->ctx == ctx, "tensor belongs to a different context");
+}
+
+}  // namespace
+
+// ================================================================== C ABI
+extern "C" {
+
+int gb_version(void) { return 10000; }
+
+const char* gb_last_error(void) { return g_last_error.c_str(); }
+
+int gb_ctx_create(int device, uint32_t flags, gb_ctx** out) {
+  API_BEGIN
+  GB_REQUIRE(out, "null output");
+  (void)flags;
+  int n = 0;
+  GB_CHECK_CUDA(cudaGetDeviceCount(&n));
+  GB_REQUIRE(device >= 0 && device < n, "device index out of range");
+  GB_CHECK_CUDA(cudaSetDevice(device));
+  gb_ctx* c = new gb_ctx();
+  c->device = device;
+  GB_CHECK_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  GB_CHECK_CUDA(cudaMalloc(&c->d_status, 256));
+  GB_CHECK_CUDA(cudaMemset(c->d_status, 0, 256));
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  *out = c;
+  API_END
+}
+
+int gb_ctx_destroy(gb_ctx* ctx) {
+  API_BEGIN
+  if (!ctx) return GB_OK;
+  DevGuard g(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& s : ctx->scratch)
+    if (s.ptr) cudaFree(s.ptr);
+  if (ctx->solver) {
+    cusolverDnDestroyParams((cusolverDnParams_t)ctx->solver_params);
+    cusolverDnDestroy((cusolverDnHandle_t)ctx->solver);
+  }
+  if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+  cudaFree(ctx->d_status);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  API_END
+}
+
+int gb_ctx_synchronize(gb_ctx* ctx) {
+  API_BEGIN
+  GB_REQUIRE(ctx, "null context");
+  GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  API_END
+}
+
+int gb_ctx_kernel_launches(gb_ctx* ctx, int64_t* out) {
+  API_BEGIN
+  GB_REQUIRE(ctx && out, "null argument");
+  *out = ctx->launches;
+  API_END
+}
+
+int gb_ctx_device_status(gb_ctx* ctx, int32_t* out) {
+  API_BEGIN
+  GB_REQUIRE(ctx && out, "null argument");
+  int32_t v = 0;
+  GB_CHECK_CUDA(cudaMemcpyAsync(&v, ctx->d_status, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+  GB_CHECK_CUDA(cudaMemsetAsync(ctx->d_status, 0, sizeof(int32_t), ctx->stream));
+  GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  *out = v;
+  API_END
+}
+
+int gb_ctx_set_precision(gb_ctx* ctx, int precision) {
+  API_BEGIN
+  GB_REQUIRE(ctx, "null context");
+  GB_REQUIRE(precision == GB_PREC_FP64 || precision == GB_PREC_BF16X3, "unknown precision");
+  ctx->aux_prec = precision;
+  API_END
+}
+
+int gb_tensor_create(gb_ctx* ctx, int kind, int dtype, int ndim, const int64_t* dims,
+                     gb_tensor** out) {
+  API_BEGIN
+  GB_REQUIRE(out && dims, "null argument");
+  DevGuard g(ctx->device);
+  *out = new_tensor(ctx, kind, dtype, ndim, dims);
+  API_END
+}
+
+int gb_tensor_free(gb_tensor* t) {
+  API_BEGIN
+  if (!t) return GB_OK;
+  DevGuard g(t->ctx->device);
+  if (t->kind == GB_KIND_MPO) drop_transfer_cache(t);
+  free_tensor(t);
+  API_END
+}
+
+int gb_tensor_shape(const gb_tensor* t, int* kind, int* dtype, int* ndim, int64_t* dims) {
+  API_BEGIN
+  GB_REQUIRE(t, "null tensor");
+  if (kind) *kind = t->kind;
+  if (dtype) *dtype = t->dtype;
+  if (ndim) *ndim = t->ndim;
+  if (dims)
+    for (int i = 0; i < t->ndim; ++i) dims[i] = t->dims[i];
+  API_END
+}
+
+int gb_tensor_upload(gb_tensor* t, const void* host, size_t bytes) {
+  API_BEGIN
+  GB_REQUIRE(t && (host || bytes == 0), "null argument");
+  GB_REQUIRE(bytes == t->bytes, "upload: byte count does not match the tensor");
+  gb_ctx* ctx = t->ctx;
+  DevGuard g(ctx->device);
+  if (t->kind == GB_KIND_MPO) memcpy(t->host_mpo.data(), host, bytes), drop_transfer_cache(t);
+  if (bytes == 0) return GB_OK;
+  if (!needs_permute(t->kind)) {
+    GB_CHECK_CUDA(cudaMemcpyAsync(t->data, host, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  } else {
+    void* tmp = scratch(ctx, SLOT_TMP, bytes);
+    GB_CHECK_CUDA(cudaMemcpyAsync(tmp, host, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    int64_t rs[6], ds[6];
+    ref_strides(t->kind, t->ndim, t->dims, rs, ds);
+    permute(ctx, t->dtype, t->ndim, t->dims, tmp, rs, t->data, ds);
+    GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  API_END
+}
+
+int gb_tensor_download(const gb_tensor* t, void* host, size_t bytes) {
+  API_BEGIN
+  GB_REQUIRE(t && (host || bytes == 0), "null argument");
+  GB_REQUIRE(bytes == t->bytes, "download: byte count does not match the tensor");
+  gb_ctx* ctx = t->ctx;
+  DevGuard g(ctx->device);
+  if (bytes == 0) return GB_OK;
+  if (!needs_permute(t->kind)) {
+    GB_CHECK_CUDA(cudaMemcpyAsync(host, t->data, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  } else {
+    void* tmp = scratch(ctx, SLOT_TMP, bytes);
+    int64_t rs[6], ds[6];
+    ref_strides(t->kind, t->ndim, t->dims, rs, ds);
+    permute(ctx, t->dtype, t->ndim, t->dims, t->data, ds, tmp, rs);
+    GB_CHECK_CUDA(cudaMemcpyAsync(host, tmp, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  API_END
+}
+
+int gb_tensor_copy(gb_tensor* dst, const gb_tensor* src) {
+  API_BEGIN
+  GB_REQUIRE(dst && src, "null tensor");
+  GB_REQUIRE(dst->bytes == src->bytes && dst->dtype == src->dtype, "copy: size mismatch");
+  GB_REQUIRE(dst->kind == src->kind || !needs_permute(dst->kind) == !needs_permute(src->kind),
+             "copy: layout mismatch");
+  DevGuard g(dst->ctx->device);
+  GB_CHECK_CUDA(cudaMemcpyAsync(dst->data, src->data, src->bytes, cudaMemcpyDeviceToDevice,
+                                dst->ctx->stream));
+  API_END
+}
+
+int gb_tensor_scale(gb_tensor* t, double re, double im) {
+  API_BEGIN
+  GB_REQUIRE(t, "null tensor");
+  GB_REQUIRE(is_cplx(t->dtype) || im == 0.0, "scale: complex factor on a real tensor");
+  DevGuard g(t->ctx->device);
+  scale(t->ctx, t->dtype, numel(t), cplx{re, im}, t->data);
+  API_END
+}
+
+int gb_tensor_axpy(gb_tensor* y, double re, double im, const gb_tensor* x) {
+  API_BEGIN
+  GB_REQUIRE(x && y, "null tensor");
+  GB_REQUIRE(x->bytes == y->bytes && x->dtype == y->dtype, "axpy: size mismatch");
+  GB_REQUIRE(is_cplx(y->dtype) || im == 0.0, "axpy: complex factor on a real tensor");
+  DevGuard g(y->ctx->device);
+  axpy(y->ctx, y->dtype, numel(y), cplx{re, im}, x->data, y->data);
+  API_END
+}
+
+int gb_tensor_dot(const gb_tensor* x, const gb_tensor* y, double* re, double* im) {
+  API_BEGIN
+  GB_REQUIRE(x && y && re, "null argument");
+  GB_REQUIRE(x->bytes == y->bytes && x->dtype == y->dtype, "dot: size mismatch");
+  DevGuard g(x->ctx->device);
+  cplx r = dot(x->ctx, x->dtype, numel(x), x->data, y->data);
+  *re = r.re;
+  if (im) *im = r.im;
+  API_END
+}
+
+int gb_tensor_norm(const gb_tensor* x, double* out) {
+  API_BEGIN
+  GB_REQUIRE(x && out, "null argument");
+  DevGuard g(x->ctx->device);
+  *out = nrm2(x->ctx, x->dtype, numel(x), x->data);
+  API_END
+}
+
+// ---------------------------------------------------------------- derivative operators
+int gb_heff_build(gb_ctx* ctx, int kind, const gb_tensor* GL, const gb_tensor* W1,
+                  const gb_tensor* W2, const gb_tensor* GR, int precision, gb_heff** out) {
+  API_BEGIN
+  GB_REQUIRE(ctx && out, "null argument");
+  DevGuard g(ctx->device);
+  if (GL) check_ctx(GL, ctx);
+  if (GR) check_ctx(GR, ctx);
+  *out = heff_build(ctx, kind, GL, W1, W2, GR, precision);
+  API_END
+}
+
+int gb_heff_free(gb_heff* h) {
+  API_BEGIN
+  if (!h) return GB_OK;
+  heff_free(h);
+  API_END
+}
+
+int gb_heff_terms(const gb_heff* h, char* buf, size_t len) {
+  API_BEGIN
+  GB_REQUIRE(h && buf && len > 0, "null argument");
+  HeffInfo hi = heff_info(h);
+  snprintf(buf, len, "%s", hi.terms);
+  API_END
+}
+
+int gb_heff_flops(const gb_heff* h, double* flops) {
+  API_BEGIN
+  GB_REQUIRE(h && flops, "null argument");
+  *flops = heff_info(h).flops;
+  API_END
+}
+
+int gb_heff_set_precision(gb_heff* h, int precision) {
+  API_BEGIN
+  GB_REQUIRE(h, "null operator");
+  heff_set_precision(h, precision);
+  API_END
+}
+
+static void check_x(const gb_heff* h, const gb_tensor* x) {
+  HeffInfo hi = heff_info(h);
+  GB_REQUIRE(x, "null tensor");
+  GB_REQUIRE(x->dtype == hi.dtype, "operator and vector dtypes differ");
+  int want = hi.kind == GB_HEFF_AC2 ? GB_KIND_AC2 : (hi.kind == GB_HEFF_AC ? GB_KIND_MPS : GB_KIND_BOND);
+  GB_REQUIRE(x->kind == want, "vector kind does not match the operator");
+  for (int i = 0; i < hi.xndim; ++i) GB_REQUIRE(x->dims[i] == hi.xdims[i], "vector shape does not match the operator");
+}
+
+int gb_heff_apply(gb_heff* h, const gb_tensor* x, gb_tensor* y) {
+  API_BEGIN
+  GB_REQUIRE(h, "null operator");
+  check_x(h, x);
+  check_x(h, y);
+  GB_REQUIRE(x != y, "apply: x and y must be distinct");
+  HeffInfo hi = heff_info(h);
+  DevGuard g(hi.ctx->device);
+  heff_apply_raw(h, x->data, y->data);
+  API_END
+}
+
+int gb_heff_eigsolve(gb_heff* h, gb_tensor* x, int krylovdim, int maxiter, double tol, int eager,
+                     double* lambda, gb_krylov_info* info) {
+  API_BEGIN
+  GB_REQUIRE(h && lambda, "null argument");
+  check_x(h, x);
+  HeffInfo hi = heff_info(h);
+  DevGuard g(hi.ctx->device);
+  heff_eigsolve_raw(hi.ctx, h, hi.xnumel, hi.dtype, x->data, krylovdim, maxiter, tol, eager != 0,
+                    lambda, info);
+  API_END
+}
+
+int gb_heff_exponentiate(gb_heff* h, gb_tensor* x, double t_re, double t_im, int krylovdim,
+                         int maxiter, double tol, gb_krylov_info* info) {
+  API_BEGIN
+  GB_REQUIRE(h, "null operator");
+  check_x(h, x);
+  HeffInfo hi = heff_info(h);
+  DevGuard g(hi.ctx->device);
+  heff_exponentiate_raw(hi.ctx, h, hi.xnumel, hi.dtype, x->data, t_re, t_im, krylovdim, maxiter,
+                        tol, info);
+  API_END
+}
+
+// ---------------------------------------------------------------- environments
+int gb_env_transfer_left(gb_ctx* ctx, const gb_tensor* GL, const gb_tensor* W, const gb_tensor* A,
+                         const gb_tensor* Abar, int precision, gb_tensor* GL_out) {
+  API_BEGIN
+  GB_REQUIRE(ctx, "null context");
+  for (const gb_tensor* t : {GL, W, A, Abar, (const gb_tensor*)GL_out}) check_ctx(t, ctx);
+  GB_REQUIRE(GL->kind == GB_KIND_GL && GL_out->kind == GB_KIND_GL, "transfer_left: GL kinds");
+  GB_REQUIRE(W->kind == GB_KIND_MPO && A->kind == GB_KIND_MPS && Abar->kind == GB_KIND_MPS,
+             "transfer_left: operand kinds");
+  const int dt = GL->dtype;
+  GB_REQUIRE(A->dtype == dt && Abar->dtype == dt && GL_out->dtype == dt, "transfer_left: dtypes");
+  GB_REQUIRE(!(is_cplx(W->dtype) && !is_cplx(dt)), "transfer_left: complex MPO on real env");
+  const int64_t Dbra = GL->dims[0], wl = GL->dims[1], Dket = GL->dims[2];
+  const int64_t d = W->dims[1], wr = W->dims[3];
+  GB_REQUIRE(W->dims[0] == wl && W->dims[2] == d, "transfer_left: MPO shape");
+  GB_REQUIRE(A->dims[0] == Dket && A->dims[1] == d, "transfer_left: ket tensor shape");
+  GB_REQUIRE(Abar->dims[0] == Dbra && Abar->dims[1] == d, "transfer_left: bra tensor shape");
+  const int64_t Dkn = A->dims[2], Dbn = Abar->dims[2];
+  GB_REQUIRE(GL_out->dims[0] == Dbn && GL_out->dims[1] == wr && GL_out->dims[2] == Dkn,
+             "transfer_left: output shape");
+  DevGuard g(ctx->device);
+  const size_t es = elem_size(dt);
+  int prec = precision;
+  void* T1 = scratch(ctx, SLOT_T1, (size_t)Dbra * d * Dkn * wl * es);
+  void* T2 = scratch(ctx, SLOT_T2, (size_t)Dbra * d * Dkn * wr * es);
+  // T1[bra, (s' kn), w] = GL[bra, ket, w] A[ket, (s' kn)]  (batched over w)
+  gemm(ctx, prec, dt, 'N', 'N', Dbra, d * Dkn, Dket, 1.0, GL->data, Dbra, Dbra * Dket, A->data,
+       Dket, 0, 0.0, T1, Dbra, Dbra * d * Dkn, wl);
+  // T2[bra, s, kn, w'] = W[w, s, s', w'] T1[bra, s', kn, w]
+  const MixDev& m = transfer_plan(ctx, W, 0, Dbra, Dkn, 0, is_cplx(dt));
+  mix_run(ctx, m, dt, T1, T2, 0.0);
+  // GL'[bn, (kn w')] = conj(Abar)[(bra s), bn]^T T2[(bra s), (kn w')]
+  gemm(ctx, prec, dt, 'C', 'N', Dbn, Dkn * wr, Dbra * d, 1.0, Abar->data, Dbra * d, 0, T2,
+       Dbra * d, 0, 0.0, GL_out->data, Dbn, 0);
+  API_END
+}
+
+int gb_env_transfer_right(gb_ctx* ctx, const gb_tensor* GR, const gb_tensor* W, const gb_tensor* A,
+                          const gb_tensor* Abar, int precision, gb_tensor* GR_out) {
+  API_BEGIN
+  GB_REQUIRE(ctx, "null context");
+  for (const gb_tensor* t : {GR, W, A, Abar, (const gb_tensor*)GR_out}) check_ctx(t, ctx);
+  GB_REQUIRE(GR->kind == GB_KIND_GR && GR_out->kind == GB_KIND_GR, "transfer_right: GR kinds");
+  GB_REQUIRE(W->kind == GB_KIND_MPO && A->kind == GB_KIND_MPS && Abar->kind == GB_KIND_MPS,
+             "transfer_right: operand kinds");
+  const int dt = GR->dtype;
+  GB_REQUIRE(A->dtype == dt && Abar->dtype == dt && GR_out->dtype == dt, "transfer_right: dtypes");
+  GB_REQUIRE(!(is_cplx(W->dtype) && !is_cplx(dt)), "transfer_right: complex MPO on real env");
+  const int64_t Dket = GR->dims[0], wr = GR->dims[1], Dbra = GR->dims[2];
+  const int64_t wl = W->dims[0], d = W->dims[1];
+  GB_REQUIRE(W->dims[3] == wr && W->dims[2] == d, "transfer_right: MPO shape");
+  GB_REQUIRE(A->dims[2] == Dket && A->dims[1] == d, "transfer_right: ket tensor shape");
+  GB_REQUIRE(Abar->dims[2] == Dbra && Abar->dims[1] == d, "transfer_right: bra tensor shape");
+  const int64_t Dk = A->dims[0], Db = Abar->dims[0];
+  GB_REQUIRE(GR_out->dims[0] == Dk && GR_out->dims[1] == wl && GR_out->dims[2] == Db,
+             "transfer_right: output shape");
+  DevGuard g(ctx->device);
+  const size_t es = elem_size(dt);
+  int prec = precision;
+  void* T1 = scratch(ctx, SLOT_T1, (size_t)Dk * d * wr * Dbra * es);
+  void* T2 = scratch(ctx, SLOT_T2, (size_t)Dk * wl * d * Dbra * es);
+  // T1[(a t), (v r)] = A[(a t), q] GR[q, (v r)]
+  gemm(ctx, prec, dt, 'N', 'N', Dk * d, wr * Dbra, Dket, 1.0, A->data, Dk * d, 0, GR->data, Dket,
+       0, 0.0, T1, Dk * d, 0);
+  // T2[a, w, s, r] = W[w, s, t, v] T1[a, t, v, r]
+  const MixDev& m = transfer_plan(ctx, W, 1, Dk, 0, Dbra, is_cplx(dt));
+  mix_run(ctx, m, dt, T1, T2, 0.0);
+  // GR'[(a w), b] = T2[(a w), (s r)] conj(Abar[b, (s r)])^T
+  gemm(ctx, prec, dt, 'N', 'C', Dk * wl, Db, d * Dbra, 1.0, T2, Dk * wl, 0, Abar->data, Db, 0, 0.0,
+       GR_out->data, Dk * wl, 0);
+  API_END
+}
+
+int gb_env_regularize(gb_ctx* ctx, gb_tensor* env, int64_t chan, const gb_tensor* lvec,
+                      const gb_tensor* rvec) {
+  API_BEGIN
+  GB_REQUIRE(ctx && env && lvec && rvec, "null argument");
+  GB_REQUIRE(env->kind == GB_KIND_GL || env->kind == GB_KIND_GR, "regularize: env kind");
+  GB_REQUIRE(lvec->kind == GB_KIND_BOND && rvec->kind == GB_KIND_BOND, "regularize: vec kinds");
+  DevGuard g(ctx->device);
+  const int dt = env->dtype;
+  const int64_t D0 = env->dims[0], w = env->dims[1], D2 = env->dims[2];
+  GB_REQUIRE(chan >= 0 && chan < w, "regularize: channel out of range");
+  GB_REQUIRE(lvec->dims[0] == D2 && lvec->dims[1] == D0, "regularize: lvec shape");
+  GB_REQUIRE(rvec->dims[0] == D0 && rvec->dims[1] == D2, "regularize: rvec shape");
+  // v = channel slice as a D0 x D2 matrix; lambda = tr(lvec v) = sum lvec[j, i] v[i, j]
+  const size_t es = elem_size(dt);
+  void* vt = scratch(ctx, SLOT_TMP, (size_t)D0 * D2 * es);
+  int64_t dims[2] = {D0, D2};
+  int64_t ins[2], outs[2] = {1, D0};
+  if (env->kind == GB_KIND_GL) {  // dev (a, a', w): slice contiguous
+    ins[0] = 1;
+    ins[1] = D0;
+  } else {  // dev (b', w, b)
+    ins[0] = 1;
+    ins[1] = D0 * w;
+  }
+  const char* base = (const char*)env->data +
+                     (size_t)(env->kind == GB_KIND_GL ? D0 * D2 * chan : D0 * chan) * es;
+  permute(ctx, dt, 2, dims, base, ins, vt, outs);
+  // tr(lvec v) = sum_{i,j} lvec[j, i] v[i, j] = <conj(lvec^T), v>
+  void* lt = scratch(ctx, SLOT_TMP2, (size_t)D0 * D2 * es);
+  conj_transpose(ctx, dt, D2, D0, lvec->data, D2, lt, D0);  // lt = lvec^H (D0 x D2)
+  cplx lam = dot(ctx, dt, D0 * D2, lt, vt);                 // sum conj(lt) v = sum lvec^T v
+  // v -= lam * rvec, written back into the slice
+  axpy(ctx, dt, D0 * D2, cplx{-lam.re, -lam.im}, rvec->data, vt);
+  permute(ctx, dt, 2, dims, vt, outs, (void*)base, ins);
+  GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  API_END
+}
+
+// ---------------------------------------------------------------- state manipulation
+int gb_mps_ac2(gb_ctx* ctx, const gb_tensor* A, const gb_tensor* B, gb_tensor* AC2) {
+  API_BEGIN
+  for (const gb_tensor* t : {A, B, (const gb_tensor*)AC2}) check_ctx(t, ctx);
+  GB_REQUIRE(A->kind == GB_KIND_MPS && B->kind == GB_KIND_MPS && AC2->kind == GB_KIND_AC2,
+             "mps_ac2: kinds");
+  GB_REQUIRE(A->dtype == B->dtype && A->dtype == AC2->dtype, "mps_ac2: dtypes");
+  const int64_t Dl = A->dims[0], d1 = A->dims[1], m = A->dims[2];
+  const int64_t d2 = B->dims[1], Dr = B->dims[2];
+  GB_REQUIRE(B->dims[0] == m, "mps_ac2: bond mismatch");
+  GB_REQUIRE(AC2->dims[0] == Dl && AC2->dims[1] == d1 && AC2->dims[2] == Dr && AC2->dims[3] == d2,
+             "mps_ac2: output shape");
+  DevGuard g(ctx->device);
+  gemm(ctx, ctx->aux_prec, A->dtype, 'N', 'N', Dl * d1, d2 * Dr, m, 1.0, A->data, Dl * d1, 0,
+       B->data, m, 0, 0.0, AC2->data, Dl * d1, 0);
+  API_END
+}
+
+int gb_mps_mul_front(gb_ctx* ctx, const gb_tensor* C, const gb_tensor* A, gb_tensor* out) {
+  API_BEGIN
+  for (const gb_tensor* t : {C, A, (const gb_tensor*)out}) check_ctx(t, ctx);
+  GB_REQUIRE(C->kind == GB_KIND_BOND && A->kind == GB_KIND_MPS && out->kind == GB_KIND_MPS,
+             "mul_front: kinds");
+  GB_REQUIRE(C->dtype == A->dtype && out->dtype == A->dtype, "mul_front: dtypes");
+  const int64_t l = C->dims[0], m = C->dims[1], d = A->dims[1], r = A->dims[2];
+  GB_REQUIRE(A->dims[0] == m, "mul_front: bond mismatch");
+  GB_REQUIRE(out->dims[0] == l && out->dims[1] == d && out->dims[2] == r, "mul_front: output");
+  DevGuard g(ctx->device);
+  gemm(ctx, ctx->aux_prec, A->dtype, 'N', 'N', l, d * r, m, 1.0, C->data, l, 0, A->data, m, 0,
+       0.0, out->data, l, 0);
+  API_END
+}
+
+int gb_mps_mul_tail(gb_ctx* ctx, const gb_tensor* A, const gb_tensor* C, gb_tensor* out) {
+  API_BEGIN
+  for (const gb_tensor* t : {C, A, (const gb_tensor*)out}) check_ctx(t, ctx);
+  GB_REQUIRE(C->kind == GB_KIND_BOND && A->kind == GB_KIND_MPS && out->kind == GB_KIND_MPS,
+             "mul_tail: kinds");
+  GB_REQUIRE(C->dtype == A->dtype && out->dtype == A->dtype, "mul_tail: dtypes");
+  const int64_t l = A->dims[0], d = A->dims[1], m = A->dims[2], r = C->dims[1];
+  GB_REQUIRE(C->dims[0] == m, "mul_tail: bond mismatch");
+  GB_REQUIRE(out->dims[0] == l && out->dims[1] == d && out->dims[2] == r, "mul_tail: output");
+  DevGuard g(ctx->device);
+  gemm(ctx, ctx->aux_prec, A->dtype, 'N', 'N', l * d, r, m, 1.0, A->data, l * d, 0, C->data, m, 0,
+       0.0, out->data, l * d, 0);
+  API_END
+}
+
+int gb_project_complement(gb_ctx* ctx, gb_tensor* Y, const gb_tensor* X) {
+  API_BEGIN
+  check_ctx(Y, ctx);
+  check_ctx(X, ctx);
+  GB_REQUIRE(X->kind == GB_KIND_MPS, "project_complement: X must be an MPS tensor");
+  GB_REQUIRE(Y->kind == GB_KIND_MPS || Y->kind == GB_KIND_AC2, "project_complement: Y kind");
+  GB_REQUIRE(X->dtype == Y->dtype, "project_complement: dtypes");
+  const int64_t rows = X->dims[0] * X->dims[1], k = X->dims[2];
+  GB_REQUIRE(Y->dims[0] * Y->dims[1] == rows, "project_complement: leading legs mismatch");
+  const int64_t cols = numel(Y) / rows;
+  DevGuard g(ctx->device);
+  const size_t es = elem_size(Y->dtype);
+  void* T = scratch(ctx, SLOT_TMP, (size_t)k * cols * es);
+  gemm(ctx, GB_PREC_FP64, Y->dtype, 'C', 'N', k, cols, rows, 1.0, X->data, rows, 0, Y->data, rows,
+       0, 0.0, T, k, 0);
+  gemm(ctx, GB_PREC_FP64, Y->dtype, 'N', 'N', rows, cols, k, -1.0, X->data, rows, 0, T, k, 0, 1.0,
+       Y->data, rows, 0);
+  API_END
+}
+
+// ---------------------------------------------------------------- gauge
+int gb_svd_trunc(gb_ctx* ctx, const gb_tensor* AC2, int64_t maxdim, double atol, int normalize,
+                 gb_tensor** AL, gb_tensor** S, gb_tensor** AR, double* eps) {
+  API_BEGIN
+  check_ctx(AC2, ctx);
+  GB_REQUIRE(AL && S && AR, "null output");
+  GB_REQUIRE(AC2->kind == GB_KIND_AC2, "svd_trunc: input must be a two-site tensor");
+  DevGuard g(ctx->device);
+  const int dt = AC2->dtype;
+  const size_t es = elem_size(dt);
+  const int64_t Dl = AC2->dims[0], d1 = AC2->dims[1], Dr = AC2->dims[2], d2 = AC2->dims[3];
+  const int64_t m = Dl * d1, n = d2 * Dr, k = std::min(m, n);
+  // device layout (l, s1, s2, r) is the matrix [(l s1), (s2 r)]
+  char* Aw = (char*)scratch(ctx, SLOT_GAUGE, (size_t)m * n * es + 256);
+  char* U = (char*)scratch(ctx, SLOT_GAUGE2, (size_t)std::max(m, n) * k * es + 256);
+  char* VT = (char*)scratch(ctx, SLOT_GAUGE3, (size_t)k * std::max(m, n) * es + 256);
+  double* Sd = (double*)scratch(ctx, SLOT_RED, sizeof(double) * (k + 64) + 4096);
+  const bool tall = m >= n;
+  if (tall) {
+    GB_CHECK_CUDA(cudaMemcpyAsync(Aw, AC2->data, (size_t)m * n * es, cudaMemcpyDeviceToDevice,
+                                  ctx->stream));
+    svd_tall(ctx, dt, m, n, Aw, U, Sd, VT);  // U m x k, VT k x n
+  } else {
+    conj_transpose(ctx, dt, m, n, AC2->data, m, Aw, n);  // n x m
+    svd_tall(ctx, dt, n, m, Aw, U, Sd, VT);              // U' n x k, VT' k x m
+  }
+  std::vector<double> hs(k);
+  GB_CHECK_CUDA(cudaMemcpyAsync(hs.data(), Sd, sizeof(double) * k, cudaMemcpyDeviceToHost,
+                                ctx->stream));
+  GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  int64_t keep = 0;
+  for (int64_t i = 0; i < k; ++i)
+    if (hs[i] > atol) ++keep;
+  if (maxdim > 0) keep = std::min(keep, maxdim);
+  keep = std::max<int64_t>(keep, 1);
+  double e2 = 0.0, n2 = 0.0;
+  for (int64_t i = keep; i < k; ++i) e2 += hs[i] * hs[i];
+  for (int64_t i = 0; i < keep; ++i) n2 += hs[i] * hs[i];
+  if (eps) *eps = std::sqrt(e2);
+  double scl = normalize ? 1.0 / std::sqrt(n2) : 1.0;
+  int64_t dl[3] = {Dl, d1, keep}, dr[3] = {keep, d2, Dr}, dc[2] = {keep, keep};
+  gb_tensor* al = new_tensor(ctx, GB_KIND_MPS, dt, 3, dl);
+  gb_tensor* ar = new_tensor(ctx, GB_KIND_MPS, dt, 3, dr);
+  gb_tensor* sc = new_tensor(ctx, GB_KIND_BOND, dt, 2, dc);
+  if (tall) {
+    // AL = U[:, :keep] (m x keep); AR = VT[:keep, :] (keep x n, ld k)
+    GB_CHECK_CUDA(cudaMemcpyAsync(al->data, U, (size_t)m * keep * es, cudaMemcpyDeviceToDevice,
+                                  ctx->stream));
+    GB_CHECK_CUDA(cudaMemcpy2DAsync(ar->data, keep * es, VT, k * es, keep * es, n,
+                                    cudaMemcpyDeviceToDevice, ctx->stream));
+  } else {
+    // M = VT'^H S U'^H : AL = (VT'[:keep, :])^H (m x keep), AR = (U'[:, :keep])^H (keep x n)
+    conj_transpose(ctx, dt, keep, m, VT, k, al->data, m);
+    conj_transpose(ctx, dt, n, keep, U, n, ar->data, keep);
+  }
+  diag_kernel<<<64, 256, 0, ctx->stream>>>(keep, Sd, scl, (double*)sc->data, is_cplx(dt));
+  GB_CHECK_CUDA(cudaGetLastError());
+  count_launch(ctx);
+  GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  *AL = al;
+  *AR = ar;
+  *S = sc;
+  API_END
+}
+
+int gb_left_orth(gb_ctx* ctx, const gb_tensor* AC, gb_tensor** AL, gb_tensor** C) {
+  API_BEGIN
+  check_ctx(AC, ctx);
+  GB_REQUIRE(AL && C, "null output");
+  GB_REQUIRE(AC->kind == GB_KIND_MPS, "left_orth: input must be an MPS tensor");
+  DevGuard g(ctx->device);
+  const int dt = AC->dtype;
+  const int64_t Dl = AC->dims[0], d = AC->dims[1], Dr = AC->dims[2];
+  const int64_t m = Dl * d, n = Dr, k = std::min(m, n);
+  int64_t dq[3] = {Dl, d, k}, dc[2] = {k, n};
+  gb_tensor* q = new_tensor(ctx, GB_KIND_MPS, dt, 3, dq);
+  gb_tensor* r = new_tensor(ctx, GB_KIND_BOND, dt, 2, dc);
+  try {
+    qr_pos(ctx, dt, m, n, AC->data, q->data, r->data);
+  } catch (...) {
+    free_tensor(q);
+    free_tensor(r);
+    throw;
+  }
+  *AL = q;
+  *C = r;
+  API_END
+}
+
+int gb_right_orth(gb_ctx* ctx, const gb_tensor* AC, gb_tensor** C, gb_tensor** AR) {
+  API_BEGIN
+  check_ctx(AC, ctx);
+  GB_REQUIRE(AR && C, "null output");
+  GB_REQUIRE(AC->kind == GB_KIND_MPS, "right_orth: input must be an MPS tensor");
+  DevGuard g(ctx->device);
+  const int dt = AC->dtype;
+  const size_t es = elem_size(dt);
+  const int64_t Dl = AC->dims[0], d = AC->dims[1], Dr = AC->dims[2];
+  const int64_t m = Dl, n = d * Dr, k = std::min(m, n);
+  // M = L Q  <=>  M^H = Q^H L^H: positive QR of M^H (n x m)
+  char* Mh = (char*)scratch(ctx, SLOT_GAUGE2, (size_t)m * n * es + 256);
+  conj_transpose(ctx, dt, m, n, AC->data, m, Mh, n);
+  char* Qp = (char*)scratch(ctx, SLOT_GAUGE3, (size_t)n * k * es + 256);
+  char* Rp = (char*)scratch(ctx, SLOT_KRYLOV_W, (size_t)k * m * es + 256);
+  qr_pos(ctx, dt, n, m, Mh, Qp, Rp);  // Qp n x k, Rp k x m
+  int64_t dq[3] = {k, d, Dr}, dc[2] = {m, k};
+  gb_tensor* q = new_tensor(ctx, GB_KIND_MPS, dt, 3, dq);
+  gb_tensor* l = new_tensor(ctx, GB_KIND_BOND, dt, 2, dc);
+  conj_transpose(ctx, dt, n, k, Qp, n, q->data, k);  // AR = Qp^H (k x n)
+  conj_transpose(ctx, dt, k, m, Rp, k, l->data, m);  // L = Rp^H (m x k)
+  GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  *C = l;
+  *AR = q;
+  API_END
+}
+
+}  // extern "C"

@@ -1,0 +1,190 @@
+// Shared runtime of libmpsgb: context, tensors, error state, scratch slots and the
+// internal kernel entry points used by the operator, Krylov and gauge modules.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/mpsgb.h"
+
+namespace gb {
+
+// ------------------------------------------------------------------ errors
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void set_last_error(const std::string& msg);
+
+#define GB_CHECK_CUDA(expr)                                                                 \
+  do {                                                                                      \
+    cudaError_t _e = (expr);                                                                \
+    if (_e != cudaSuccess)                                                                  \
+      throw ::gb::Error(GB_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e)); \
+  } while (0)
+
+#define GB_REQUIRE(cond, msg)                                  \
+  do {                                                         \
+    if (!(cond)) throw ::gb::Error(GB_ERR_ARG, std::string(msg)); \
+  } while (0)
+
+// ------------------------------------------------------------------ complex scalar
+struct cplx {
+  double re, im;
+};
+
+// ------------------------------------------------------------------ context / tensors
+struct Scratch {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+
+enum ScratchSlot {
+  SLOT_PACK_A = 0,
+  SLOT_PACK_B,
+  SLOT_T1,
+  SLOT_T2,
+  SLOT_RED,       // reduction partials
+  SLOT_KRYLOV,    // Krylov basis
+  SLOT_KRYLOV_W,  // Krylov work vector
+  SLOT_GAUGE,     // factorisation buffers
+  SLOT_GAUGE2,
+  SLOT_GAUGE3,
+  SLOT_TMP,       // short-lived helper buffers
+  SLOT_TMP2,
+  SLOT_COUNT
+};
+
+}  // namespace gb
+
+struct gb_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int64_t launches = 0;
+  int32_t* d_status = nullptr;   // device status word (bounded waits)
+  void* solver = nullptr;        // cusolverDnHandle_t
+  void* solver_params = nullptr; // cusolverDnParams_t
+  gb::Scratch scratch[gb::SLOT_COUNT];
+  double* h_pinned = nullptr;    // small pinned host buffer for scalar readback
+  size_t h_pinned_elems = 0;
+  int num_sms = 0;
+  int aux_prec = GB_PREC_FP64;   // precision of auxiliary state contractions
+};
+
+struct gb_tensor {
+  gb_ctx* ctx = nullptr;
+  int kind = GB_KIND_GENERIC;
+  int dtype = GB_F64;
+  int ndim = 0;
+  int64_t dims[6] = {0, 0, 0, 0, 0, 0};  // reference leg order
+  void* data = nullptr;                  // device pointer, device layout
+  size_t bytes = 0;
+  std::vector<double> host_mpo;          // host mirror for GB_KIND_MPO (interleaved if complex)
+};
+
+namespace gb {
+
+inline size_t elem_size(int dtype) { return dtype == GB_C128 ? 16 : 8; }
+inline int64_t numel(const gb_tensor* t) {
+  int64_t n = 1;
+  for (int i = 0; i < t->ndim; ++i) n *= t->dims[i];
+  return n;
+}
+inline bool is_cplx(int dtype) { return dtype == GB_C128; }
+
+void* scratch(gb_ctx* ctx, int slot, size_t bytes);
+inline void count_launch(gb_ctx* ctx, int n = 1) { ctx->launches += n; }
+
+// ------------------------------------------------------------------ kernel launchers
+// All operate on ctx->stream and count their launches.
+
+// General strided permute/copy: out[o] = in[i] over up to 6 dims.
+// dims/out_strides/in_strides are element strides for each logical dim.
+void permute(gb_ctx* ctx, int dtype, int nd, const int64_t* dims, const void* in,
+             const int64_t* in_strides, void* out, const int64_t* out_strides);
+
+// Sparse mode mix (see kernels.cu):
+// y[a*ya + out_off[J] + n*yn] = beta*y + sum_{e in row J} val[e] * x[a*xa + in_off[col[e]] + n*xn]
+struct MixPlan {
+  int64_t A = 1, N = 1, nI = 0, nJ = 0;
+  int64_t xa = 1, xn = 0, ya = 1, yn = 0;
+  std::vector<int64_t> in_off, out_off;
+  std::vector<int> row_ptr, col;
+  std::vector<double> val;  // interleaved (re, im) when complex
+  bool cplx = false;
+};
+struct MixDev {
+  void* buf = nullptr;  // device copy of tables
+  size_t bytes = 0;
+  int64_t A = 1, N = 1, nJ = 0, xa = 1, xn = 0, ya = 1, yn = 0;
+  bool cplx = false;
+  const int64_t* in_off = nullptr;
+  const int64_t* out_off = nullptr;
+  const int* row_ptr = nullptr;
+  const int* col = nullptr;
+  const double* val = nullptr;
+};
+MixDev mix_upload(gb_ctx* ctx, const MixPlan& p);
+void mix_free(MixDev& m);
+void mix_run(gb_ctx* ctx, const MixDev& m, int dtype, const void* x, void* y, double beta);
+
+// y[off_J + i*ds] += val_J for i < count (diagonal additions of delta terms)
+void add_diag(gb_ctx* ctx, int dtype, void* y, const std::vector<int64_t>& offs,
+              const std::vector<double>& vals, int64_t count, int64_t ds);
+
+// FP64 / complex GEMM on CUDA cores, column-major, batched with strides.
+// op: 'N', 'T' or 'C'.  C = alpha*op(A)*op(B) + beta*C (beta = 0 does not read C).
+void gemm_fp64(gb_ctx* ctx, int dtype, char opA, char opB, int64_t M, int64_t N, int64_t K,
+               cplx alpha, const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb,
+               int64_t sB, cplx beta, void* C, int64_t ldc, int64_t sC, int64_t batch);
+
+// BLAS-1 style helpers over n elements of dtype
+void fill_zero(gb_ctx* ctx, void* p, size_t bytes);
+void axpy(gb_ctx* ctx, int dtype, int64_t n, cplx a, const void* x, void* y);
+void scale(gb_ctx* ctx, int dtype, int64_t n, cplx a, void* x);
+cplx dot(gb_ctx* ctx, int dtype, int64_t n, const void* x, const void* y);  // conj(x).y
+double nrm2(gb_ctx* ctx, int dtype, int64_t n, const void* x);
+// c[j] = sum_i conj(V[i + ld*j]) w[i] for j < k; result copied to host (k values)
+void multi_dot(gb_ctx* ctx, int dtype, int64_t n, int k, const void* V, int64_t ld,
+               const void* w, cplx* host_out);
+// w[i] += sum_j V[i + ld*j] * coef[j] for j < k (coef from host)
+void multi_axpy(gb_ctx* ctx, int dtype, int64_t n, int k, const void* V, int64_t ld,
+                const cplx* coef, void* w);
+// finite check: returns true when all entries are finite
+bool all_finite(gb_ctx* ctx, int dtype, int64_t n, const void* x);
+
+// ------------------------------------------------------------------ split precision
+// Operand packed for the tcgen05 BF16 GEMM: K-major rows, two planes (hi, lo),
+// realified when complex (see gemm_tc.cu).
+struct Packed {
+  void* data = nullptr;  // [batch][2 planes][rows][Kp] bf16
+  int64_t rows = 0, Kp = 0, batch = 1;
+  int64_t K = 0;         // logical K (per real/imag half when complex)
+  int64_t Kh = 0;        // offset of the imaginary half along K when complex
+  bool cplx = false;
+  bool owned = false;
+  size_t bytes = 0;
+};
+// which operand of C = op(A) op(B) is being packed
+enum PackRole { PACK_AS_A = 0, PACK_AS_B = 1 };
+size_t packed_bytes(int64_t rows, int64_t K, bool cplx, int role, int64_t batch);
+void pack_operand(gb_ctx* ctx, int dtype, int role, char op, int64_t M_or_N, int64_t K,
+                  const void* src, int64_t ld, int64_t stride, int64_t batch, Packed& out,
+                  void* dst);
+void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_t M,
+                int64_t N, double alpha, double beta, void* C, int64_t ldc, int64_t sC);
+bool tc_available(gb_ctx* ctx);
+
+// Unified GEMM: dispatches on precision; optional pre-packed operands.
+void gemm(gb_ctx* ctx, int prec, int dtype, char opA, char opB, int64_t M, int64_t N,
+          int64_t K, double alpha, const void* A, int64_t lda, int64_t sA, const void* B,
+          int64_t ldb, int64_t sB, double beta, void* C, int64_t ldc, int64_t sC,
+          int64_t batch = 1, const Packed* pA = nullptr, const Packed* pB = nullptr);
+
+}  // namespace gb

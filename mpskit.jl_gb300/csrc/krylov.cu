@@ -1,0 +1,275 @@
+// Device-resident Krylov solvers for the derivative operators.
+//
+// eigsolve: KrylovKit's Lanczos as MPSKit uses it through `fixedpoint`
+// (src/algorithms/fixedpoint.jl:15-18): start from x0/|x0|, one matvec per expansion,
+// full re-orthogonalisation (two classical Gram-Schmidt passes), diagonalise the
+// projected matrix when the space is full, when beta <= tol, or after every step when
+// `eager`; a Ritz pair is converged when |beta * U[K, i]| <= tol; thick restart keeps
+// (3*krylovdim + 2)/5 Ritz vectors at most `maxiter` times.
+//
+// exponentiate: Lanczos approximation of exp(t H) x with time-step halving until the
+// a-posteriori error estimate |beta_K c_K| |x| <= tol * tau (KrylovKit `exponentiate`,
+// used by `integrate`, src/algorithms/timestep/integrators.jl:44-53).
+//
+// The Krylov basis, the work vector and all reductions stay in HBM in FP64; only the
+// projected matrices (a few hundred numbers) visit the host.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <vector>
+
+#include "gb_common.h"
+
+namespace gb {
+
+void heff_apply_raw(gb_heff* h, const void* x, void* y);
+
+// Cyclic Jacobi eigen-decomposition of a small real symmetric matrix (row-major n x n).
+// D ascending; U[:, j] (row-major U[i*n + j]) the eigenvector of D[j].
+void sym_eig(int n, const std::vector<double>& Ain, std::vector<double>& D,
+             std::vector<double>& U) {
+  std::vector<double> A(Ain);
+  U.assign((size_t)n * n, 0.0);
+  for (int i = 0; i < n; ++i) U[i * n + i] = 1.0;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        double a = A[i * n + j] * A[i * n + j];
+        tot += a;
+        if (i != j) off += a;
+      }
+    if (off <= 1e-30 * std::max(tot, 1e-300)) break;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        double apq = A[p * n + q];
+        if (std::fabs(apq) < 1e-300) continue;
+        double app = A[p * n + p], aqq = A[q * n + q];
+        double theta = (aqq - app) / (2.0 * apq);
+        double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < n; ++k) {  // A <- J^T A J
+          double akp = A[k * n + p], akq = A[k * n + q];
+          A[k * n + p] = c * akp - s * akq;
+          A[k * n + q] = s * akp + c * akq;
+        }
+        for (int k = 0; k < n; ++k) {
+          double apk = A[p * n + k], aqk = A[q * n + k];
+          A[p * n + k] = c * apk - s * aqk;
+          A[q * n + k] = s * apk + c * aqk;
+        }
+        for (int k = 0; k < n; ++k) {
+          double ukp = U[k * n + p], ukq = U[k * n + q];
+          U[k * n + p] = c * ukp - s * ukq;
+          U[k * n + q] = s * ukp + c * ukq;
+        }
+      }
+  }
+  std::vector<int> idx(n);
+  for (int i = 0; i < n; ++i) idx[i] = i;
+  std::sort(idx.begin(), idx.end(), [&](int a, int b) { return A[a * n + a] < A[b * n + b]; });
+  D.resize(n);
+  std::vector<double> U2((size_t)n * n);
+  for (int j = 0; j < n; ++j) {
+    D[j] = A[idx[j] * n + idx[j]];
+    for (int i = 0; i < n; ++i) U2[i * n + j] = U[i * n + idx[j]];
+  }
+  U.swap(U2);
+}
+
+struct KrylovWork {
+  void* V = nullptr;  // (kd+1) vectors of n elements
+  void* w = nullptr;
+  void* tmp = nullptr;
+};
+
+static void orthogonalize(gb_ctx* ctx, int dtype, int64_t n, int k, void* V, void* w,
+                          std::vector<cplx>& h) {
+  std::vector<cplx> c(k), c2(k);
+  multi_dot(ctx, dtype, n, k, V, n, w, c.data());
+  std::vector<cplx> neg(k);
+  for (int j = 0; j < k; ++j) neg[j] = cplx{-c[j].re, -c[j].im};
+  multi_axpy(ctx, dtype, n, k, V, n, neg.data(), w);
+  multi_dot(ctx, dtype, n, k, V, n, w, c2.data());
+  for (int j = 0; j < k; ++j) neg[j] = cplx{-c2[j].re, -c2[j].im};
+  multi_axpy(ctx, dtype, n, k, V, n, neg.data(), w);
+  h.resize(k);
+  for (int j = 0; j < k; ++j) h[j] = cplx{c[j].re + c2[j].re, c[j].im + c2[j].im};
+}
+
+// x <- sum_j coef[j] V[j]
+static void combine(gb_ctx* ctx, int dtype, int64_t n, int k, const void* V,
+                    const std::vector<cplx>& coef, void* x) {
+  fill_zero(ctx, x, (size_t)n * elem_size(dtype));
+  multi_axpy(ctx, dtype, n, k, V, n, coef.data(), x);
+}
+
+int heff_eigsolve_raw(gb_ctx* ctx, gb_heff* h, int64_t n, int dtype, void* x, int krylovdim,
+                      int maxiter, double tol, bool eager, double* lambda, gb_krylov_info* info) {
+  GB_REQUIRE(krylovdim >= 1 && krylovdim <= 64 && maxiter >= 1, "eigsolve: krylovdim/maxiter");
+  const size_t es = elem_size(dtype);
+  const int kd = krylovdim;
+  char* V = (char*)scratch(ctx, SLOT_KRYLOV, (size_t)(kd + 1) * n * es);
+  void* w = scratch(ctx, SLOT_KRYLOV_W, (size_t)n * es);
+  auto vec = [&](int j) { return (void*)(V + (size_t)j * n * es); };
+  double nx = nrm2(ctx, dtype, n, x);
+  GB_REQUIRE(nx > 0 && std::isfinite(nx), "eigsolve: initial vector has zero or non-finite norm");
+  GB_CHECK_CUDA(cudaMemcpyAsync(vec(0), x, n * es, cudaMemcpyDeviceToDevice, ctx->stream));
+  scale(ctx, dtype, n, cplx{1.0 / nx, 0}, vec(0));
+  const int howmany = 1;
+  std::vector<double> H((size_t)(kd + 1) * (kd + 1), 0.0);  // row-major, stride kd+1
+  const int LD = kd + 1;
+  int K = 0, numops = 0, numiter = 1, converged = 0;
+  double beta = 0.0;
+  std::vector<double> D, U;
+  std::vector<double> f;
+  while (true) {
+    heff_apply_raw(h, vec(K), w);
+    ++numops;
+    std::vector<cplx> hc;
+    orthogonalize(ctx, dtype, n, K + 1, V, w, hc);
+    for (int i = 0; i <= K; ++i) {
+      H[i * LD + K] = hc[i].re;
+      H[K * LD + i] = hc[i].re;
+    }
+    ++K;
+    beta = nrm2(ctx, dtype, n, w);
+    GB_REQUIRE(std::isfinite(beta), "eigsolve: non-finite residual (NaN in operator or vector)");
+    if (K == kd || beta <= tol || (eager && K >= howmany)) {
+      std::vector<double> Hk((size_t)K * K);
+      for (int i = 0; i < K; ++i)
+        for (int j = 0; j < K; ++j) Hk[i * K + j] = H[i * LD + j];
+      sym_eig(K, Hk, D, U);
+      f.assign(K, 0.0);
+      for (int i = 0; i < K; ++i) f[i] = beta * U[(K - 1) * K + i];
+      converged = 0;
+      while (converged < K && std::fabs(f[converged]) <= tol) ++converged;
+      if (converged >= howmany || beta <= tol) break;
+    }
+    if (K < kd) {
+      GB_CHECK_CUDA(cudaMemcpyAsync(vec(K), w, n * es, cudaMemcpyDeviceToDevice, ctx->stream));
+      scale(ctx, dtype, n, cplx{1.0 / beta, 0}, vec(K));
+      continue;
+    }
+    if (numiter == maxiter) break;
+    // thick restart: V[:keep] <- V[:K] U[:, :keep]
+    int keep = (3 * kd + 2 * howmany) / 5;
+    keep = std::max(1, std::min(keep, K - 1));
+    void* tmp = scratch(ctx, SLOT_TMP, (size_t)keep * n * es);
+    for (int j = 0; j < keep; ++j) {
+      std::vector<cplx> coef(K);
+      for (int i = 0; i < K; ++i) coef[i] = cplx{U[i * K + j], 0.0};
+      combine(ctx, dtype, n, K, V, coef, (char*)tmp + (size_t)j * n * es);
+    }
+    GB_CHECK_CUDA(cudaMemcpyAsync(V, tmp, (size_t)keep * n * es, cudaMemcpyDeviceToDevice,
+                                  ctx->stream));
+    std::fill(H.begin(), H.end(), 0.0);
+    for (int j = 0; j < keep; ++j) {
+      H[j * LD + j] = D[j];
+      H[keep * LD + j] = f[j];
+      H[j * LD + keep] = f[j];
+    }
+    GB_CHECK_CUDA(cudaMemcpyAsync(vec(keep), w, n * es, cudaMemcpyDeviceToDevice, ctx->stream));
+    scale(ctx, dtype, n, cplx{1.0 / beta, 0}, vec(keep));
+    K = keep;
+    ++numiter;
+  }
+  std::vector<cplx> coef(K);
+  for (int i = 0; i < K; ++i) coef[i] = cplx{U[i * K + 0], 0.0};
+  combine(ctx, dtype, n, K, V, coef, x);
+  double nn = nrm2(ctx, dtype, n, x);
+  scale(ctx, dtype, n, cplx{1.0 / nn, 0}, x);
+  *lambda = D[0];
+  if (info) {
+    info->converged = converged;
+    info->numops = numops;
+    info->numiter = numiter;
+    info->normres = std::fabs(f[0]);
+  }
+  GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  return GB_OK;
+}
+
+int heff_exponentiate_raw(gb_ctx* ctx, gb_heff* h, int64_t n, int dtype, void* x, double t_re,
+                          double t_im, int krylovdim, int maxiter, double tol,
+                          gb_krylov_info* info) {
+  GB_REQUIRE(krylovdim >= 1 && krylovdim <= 64, "exponentiate: krylovdim");
+  GB_REQUIRE(is_cplx(dtype) || t_im == 0.0, "exponentiate: complex time needs complex storage");
+  const size_t es = elem_size(dtype);
+  const int kd = krylovdim;
+  char* V = (char*)scratch(ctx, SLOT_KRYLOV, (size_t)(kd + 1) * n * es);
+  void* w = scratch(ctx, SLOT_KRYLOV_W, (size_t)n * es);
+  auto vec = [&](int j) { return (void*)(V + (size_t)j * n * es); };
+  const std::complex<double> total(t_re, t_im);
+  double tau_left = 1.0, tau = 1.0;
+  int numops = 0, numiter = 0;
+  const int maxsteps = std::max(1, maxiter) * 50;
+  while (tau_left > 0 && numiter < maxsteps) {
+    ++numiter;
+    double nrm = nrm2(ctx, dtype, n, x);
+    if (nrm == 0.0) break;
+    GB_CHECK_CUDA(cudaMemcpyAsync(vec(0), x, n * es, cudaMemcpyDeviceToDevice, ctx->stream));
+    scale(ctx, dtype, n, cplx{1.0 / nrm, 0}, vec(0));
+    std::vector<double> alphas, betas;
+    int K = 0;
+    bool happy = false;
+    for (int j = 0; j < kd; ++j) {
+      heff_apply_raw(h, vec(j), w);
+      ++numops;
+      std::vector<cplx> hc;
+      orthogonalize(ctx, dtype, n, j + 1, V, w, hc);
+      double a = hc[j].re;
+      double b = nrm2(ctx, dtype, n, w);
+      alphas.push_back(a);
+      betas.push_back(b);
+      K = j + 1;
+      if (b <= tol * 1e-3) {
+        happy = true;
+        break;
+      }
+      if (j + 1 < kd + 1) {
+        GB_CHECK_CUDA(cudaMemcpyAsync(vec(j + 1), w, n * es, cudaMemcpyDeviceToDevice,
+                                      ctx->stream));
+        scale(ctx, dtype, n, cplx{1.0 / b, 0}, vec(j + 1));
+      }
+    }
+    std::vector<double> T((size_t)K * K, 0.0), D, U;
+    for (int i = 0; i < K; ++i) {
+      T[i * K + i] = alphas[i];
+      if (i + 1 < K) T[i * K + i + 1] = T[(i + 1) * K + i] = betas[i];
+    }
+    sym_eig(K, T, D, U);
+    tau = std::min(tau, tau_left);
+    std::vector<std::complex<double>> c(K);
+    while (true) {
+      for (int i = 0; i < K; ++i) {
+        std::complex<double> acc = 0.0;
+        for (int j = 0; j < K; ++j) acc += U[i * K + j] * std::exp(total * tau * D[j]) * U[0 * K + j];
+        c[i] = acc;
+      }
+      double err = happy ? 0.0 : std::abs(betas[K - 1] * c[K - 1]) * nrm;
+      if (err <= tol * tau || tau < 1e-12) break;
+      tau *= 0.5;
+    }
+    std::vector<cplx> coef(K);
+    for (int i = 0; i < K; ++i) coef[i] = cplx{nrm * c[i].real(), nrm * c[i].imag()};
+    if (!is_cplx(dtype))
+      for (auto& q : coef) q.im = 0.0;
+    combine(ctx, dtype, n, K, V, coef, x);
+    tau_left -= tau;
+    if (tau_left < 1e-15) tau_left = 0.0;
+    tau = std::min(2 * tau, 1.0);
+  }
+  if (info) {
+    info->converged = tau_left == 0.0 ? 1 : 0;
+    info->numops = numops;
+    info->numiter = numiter;
+    info->normres = 0.0;
+  }
+  GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  return GB_OK;
+}
+
+}  // namespace gb

@@ -1,0 +1,24 @@
+"""mpsgb -- GB300-native effective-Hamiltonian engine behind MPSKit.jl's derivative-operator API.
+
+Host-side mirror of the MPSKit interface for the hot path (derivative operators, their
+Krylov solvers, environment recursions and the DMRG drivers that call them); every
+contraction runs in libmpsgb.so on the GPU.
+"""
+from . import _lib
+from .core import Context, DeviceTensor, context
+from .derivatives import (AC2_hamiltonian, AC_hamiltonian, C_hamiltonian, DerivativeOperator,
+                          GB300Backend, Lanczos, exponentiate, fixedpoint, integrate)
+from .operators import (FiniteMPOHamiltonian, InfiniteMPOHamiltonian, MPOHamiltonian,
+                        heisenberg_XXX, j1j2_cylinder, transverse_field_ising, xxz)
+from .states import (FiniteEnvironments, FiniteMPS, ac2_from, left_orth, mul_front, mul_tail,
+                     project_complement_, right_orth, svd_trunc)
+from .algorithms import DMRG, DMRG2, AdaptiveKrylov, expectation_value, find_groundstate
+
+__all__ = [
+    "Context", "DeviceTensor", "context", "AC2_hamiltonian", "AC_hamiltonian", "C_hamiltonian",
+    "DerivativeOperator", "GB300Backend", "Lanczos", "exponentiate", "fixedpoint", "integrate",
+    "FiniteMPOHamiltonian", "InfiniteMPOHamiltonian", "MPOHamiltonian", "heisenberg_XXX",
+    "j1j2_cylinder", "transverse_field_ising", "xxz", "FiniteEnvironments", "FiniteMPS",
+    "ac2_from", "left_orth", "mul_front", "mul_tail", "project_complement_", "right_orth",
+    "svd_trunc", "DMRG", "DMRG2", "AdaptiveKrylov", "expectation_value", "find_groundstate",
+]

@@ -1,0 +1,201 @@
+"""Ground-state drivers on the device (host mirror of MPSKit's DMRG / DMRG2).
+
+  DMRG / DMRG2 local_update! and the sweep  -- src/algorithms/groundstate/dmrg.jl:121-354
+  AdaptiveKrylov / adapt_solver             -- src/utility/dynamictols.jl:182-235
+  calc_galerkin                             -- src/algorithms/toolbox.jl:63-70
+  expectation_value(FiniteMPS, H)           -- src/algorithms/expval.jl:136-141
+"""
+import math
+import time
+
+import numpy as np
+
+from . import _lib as L
+from .derivatives import (AC2_hamiltonian, AC_hamiltonian, GB300Backend, Lanczos, fixedpoint)
+from .states import (FiniteEnvironments, ac2_from, left_orth, project_complement_, right_orth,
+                     svd_trunc)
+
+
+class AdaptiveKrylov:
+    """Per-bond adaptive Krylov budget (dynamictols.jl:130-235), same defaults."""
+
+    def __init__(self, krylovdim_min=3, krylovdim_max=20, iter_min=1, iter_max=1,
+                 tol_min=1e-12, tol_max=1e-2, truncation_factor=1e-1, tol_factor=1e-1,
+                 eager=True):
+        if not (0 < krylovdim_min <= krylovdim_max):
+            raise ValueError("need 0 < krylovdim_min <= krylovdim_max")
+        if not (1 <= iter_min <= iter_max):
+            raise ValueError("need 1 <= iter_min <= iter_max")
+        self.krylovdim_min, self.krylovdim_max = krylovdim_min, krylovdim_max
+        self.iter_min, self.iter_max = iter_min, iter_max
+        self.tol_min, self.tol_max = tol_min, tol_max
+        self.truncation_factor, self.tol_factor = truncation_factor, tol_factor
+        self.eager = eager
+
+    def adapt(self, decay_rate=0.0, g_local=0.0, g_global=0.0, eps_trunc=0.0):
+        tol = min(max(max(self.truncation_factor * eps_trunc, self.tol_factor * g_global),
+                      self.tol_min), self.tol_max)
+        rho = min(max(decay_rate, 0.0), 1.0)
+        if not (0.0 < rho < 1.0):
+            if rho == 0.0:
+                return Lanczos(self.krylovdim_min, self.iter_min, tol, self.eager)
+            return Lanczos(self.krylovdim_max, self.iter_max, tol, self.eager)
+        R = max(g_local, self.tol_min) / tol
+        nmat = int(round(math.log(R) / math.log(1.0 / rho)))
+        kd = min(max(nmat, self.krylovdim_min), self.krylovdim_max)
+        mi = min(max(-((-5 * nmat) // (2 * kd)) - 3, self.iter_min), self.iter_max)
+        return Lanczos(kd, mi, tol, self.eager)
+
+
+class DMRG2:
+    def __init__(self, maxdim, cutoff=0.0, tol=1e-10, maxiter=200, alg_eigsolve=None,
+                 backend=None, verbosity=0):
+        self.maxdim, self.cutoff = maxdim, cutoff
+        self.tol, self.maxiter = tol, maxiter
+        self.alg_eigsolve = alg_eigsolve or AdaptiveKrylov()
+        self.backend = backend or GB300Backend()
+        self.verbosity = verbosity
+
+
+class DMRG:
+    def __init__(self, tol=1e-10, maxiter=200, alg_eigsolve=None, backend=None, verbosity=0):
+        self.tol, self.maxiter = tol, maxiter
+        self.alg_eigsolve = alg_eigsolve or AdaptiveKrylov()
+        self.backend = backend or GB300Backend()
+        self.verbosity = verbosity
+
+
+def _decay(normres, eps_local, numops):
+    if eps_local <= 0:
+        return 0.999
+    return min(max((normres / eps_local) ** (1.0 / max(1, numops)), 1e-3), 0.999)
+
+
+class SweepStats:
+    def __init__(self):
+        self.matvecs = 0
+        self.updates = 0
+        self.heff_flops = 0.0
+        self.t = {"heff_build": 0.0, "eigsolve": 0.0, "gauge": 0.0, "env": 0.0}
+
+
+def dmrg2_local_update(pos, right, psi, H, alg, envs, eps_global, eps_trunc, decay_rate, stats):
+    """local_update!(..., ::DMRG2) (dmrg.jl:211-244)."""
+    t0 = time.perf_counter()
+    Heff = AC2_hamiltonian(pos, psi, H, envs, alg.backend)
+    t1 = time.perf_counter()
+    ac2 = ac2_from(psi.ac(pos), psi.AR[pos + 1]) if right else ac2_from(psi.AL[pos], psi.ac(pos + 1))
+    y = Heff(ac2)
+    y.normalize_()
+    project_complement_(y, psi.al(pos))
+    eps_local = y.norm()
+    solver = alg.alg_eigsolve.adapt(decay_rate, eps_local, eps_global, eps_trunc)
+    val, new, info = fixedpoint(Heff, ac2, "SR", solver)
+    t2 = time.perf_counter()
+    al, S, ar, eps_tr = svd_trunc(new, alg.maxdim, alg.cutoff, normalize=True)
+    psi.AL[pos] = al
+    psi.AR[pos + 1] = ar
+    psi.C[pos + 1] = S
+    psi.center = pos + 1
+    t3 = time.perf_counter()
+    stats.matvecs += info.numops + 1
+    stats.updates += 1
+    stats.heff_flops += Heff.flops * (info.numops + 1)
+    stats.t["heff_build"] += t1 - t0
+    stats.t["eigsolve"] += t2 - t1
+    stats.t["gauge"] += t3 - t2
+    return eps_local, eps_tr, _decay(info.normres, eps_local, info.numops), val
+
+
+def expectation_value(psi, H, envs, site=0, backend=None):
+    """<psi|H|psi>/<psi|psi> contracted at a site adjacent to the centre."""
+    ac = psi.ac(site)
+    Heff = AC_hamiltonian(site, psi, H, envs, backend or GB300Backend())
+    return float(np.real(ac.dot(Heff(ac)) / ac.dot(ac)))
+
+
+def find_groundstate(psi, H, alg, envs=None, maxsweeps=None, callback=None):
+    """find_groundstate(psi, H, DMRG2()/DMRG()) on the device.  The input state is
+    modified in place (find_groundstate! semantics).  Returns (psi, envs, eps, history)."""
+    if isinstance(alg, DMRG2):
+        return _sweep_dmrg2(psi, H, alg, envs, maxsweeps, callback)
+    if isinstance(alg, DMRG):
+        return _sweep_dmrg1(psi, H, alg, envs, maxsweeps, callback)
+    raise TypeError("unsupported algorithm")
+
+
+def _sweep_dmrg2(psi, H, alg, envs, maxsweeps, callback):
+    envs = envs or FiniteEnvironments(psi, H)
+    envs.precision = alg.backend.code
+    n = len(psi) - 1
+    eps_locals = np.ones(n)
+    eps_truncs = np.zeros(n)
+    decays = np.zeros(n)
+    eps_global = float(eps_locals.max())
+    fwd = list(range(0, len(psi) - 1))
+    bwd = list(range(len(psi) - 3, -1, -1))
+    hist = []
+    stats = SweepStats()
+    niter = alg.maxiter if maxsweeps is None else maxsweeps
+    for it in range(niter):
+        t0 = time.perf_counter()
+        for right, rng in ((True, fwd), (False, bwd)):
+            for pos in rng:
+                eps_locals[pos], eps_truncs[pos], decays[pos], _ = dmrg2_local_update(
+                    pos, right, psi, H, alg, envs, eps_global, eps_truncs[pos], decays[pos], stats)
+                eps_global = float(eps_locals.max())
+        E = expectation_value(psi, H, envs, 0, alg.backend)
+        dt = time.perf_counter() - t0
+        hist.append({"sweep": it, "energy": float(np.real(E)), "eps": eps_global, "time": dt,
+                     "matvecs": stats.matvecs})
+        if alg.verbosity:
+            print(f"DMRG2 sweep {it}: E = {np.real(E):.14f}  eps = {eps_global:.3e}  t = {dt:.3f}s")
+        if callback:
+            callback(it, psi, envs)
+        if eps_global <= max(alg.tol, float(eps_truncs.max())):
+            break
+    return psi, envs, eps_global, hist
+
+
+def _sweep_dmrg1(psi, H, alg, envs, maxsweeps, callback):
+    envs = envs or FiniteEnvironments(psi, H)
+    envs.precision = alg.backend.code
+    n = len(psi)
+    eps_locals = np.ones(n)
+    decays = np.zeros(n)
+    eps_global = 1.0
+    hist = []
+    niter = alg.maxiter if maxsweeps is None else maxsweeps
+    val = 0.0
+    for it in range(niter):
+        for right, rng in ((True, range(0, n - 1)), (False, range(n - 1, 0, -1))):
+            for pos in rng:
+                ac = psi.ac(pos)
+                Heff = AC_hamiltonian(pos, psi, H, envs, alg.backend)
+                y = Heff(ac)
+                y.normalize_()
+                project_complement_(y, psi.al(pos))
+                eps_local = y.norm()
+                solver = alg.alg_eigsolve.adapt(decays[pos], eps_local, eps_global, 0.0)
+                val, new, info = fixedpoint(Heff, ac, "SR", solver)
+                if right:
+                    q, R = left_orth(new)
+                    R.scale_(1.0 / R.norm())
+                    psi.AL[pos] = q
+                    psi.C[pos + 1] = R
+                    psi.center = pos + 1
+                else:
+                    Lm, q = right_orth(new)
+                    Lm.scale_(1.0 / Lm.norm())
+                    psi.AR[pos] = q
+                    psi.C[pos] = Lm
+                    psi.center = pos
+                eps_locals[pos] = eps_local
+                decays[pos] = _decay(info.normres, eps_local, info.numops)
+                eps_global = float(eps_locals.max())
+        hist.append({"sweep": it, "energy": float(val), "eps": eps_global})
+        if callback:
+            callback(it, psi, envs)
+        if eps_global <= alg.tol:
+            break
+    return psi, envs, eps_global, hist

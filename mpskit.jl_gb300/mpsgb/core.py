@@ -1,0 +1,161 @@
+"""Device context and tensors (host side of libmpsgb).
+
+`DeviceTensor` is the analogue of a TensorKit `TensorMap` whose storage lives in GB300
+HBM: `from_numpy` / `numpy` exchange data in TensorKit's own layout (column-major,
+legs in TensorMap order) and the library converts to its device layout.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib as L
+
+_CTX = {}
+
+_KIND_NAMES = {
+    "mps": L.GB_KIND_MPS, "bond": L.GB_KIND_BOND, "ac2": L.GB_KIND_AC2,
+    "gl": L.GB_KIND_GL, "gr": L.GB_KIND_GR, "mpo": L.GB_KIND_MPO, "generic": L.GB_KIND_GENERIC,
+}
+
+
+class Context:
+    """One device context (stream, solver handles, launch counter)."""
+
+    def __init__(self, device=0):
+        h = ctypes.c_void_p()
+        L.check(L.lib().gb_ctx_create(device, 0, ctypes.byref(h)))
+        self.handle = h
+        self.device = device
+
+    def synchronize(self):
+        L.check(L.lib().gb_ctx_synchronize(self.handle))
+
+    def kernel_launches(self):
+        v = ctypes.c_int64()
+        L.check(L.lib().gb_ctx_kernel_launches(self.handle, ctypes.byref(v)))
+        return v.value
+
+    def device_status(self):
+        v = ctypes.c_int32()
+        L.check(L.lib().gb_ctx_device_status(self.handle, ctypes.byref(v)))
+        return v.value
+
+
+def context(device=0):
+    """Process-wide default context for `device`."""
+    ctx = _CTX.get(device)
+    if ctx is None:
+        ctx = Context(device)
+        _CTX[device] = ctx
+    return ctx
+
+
+def _dtype_code(dtype):
+    dtype = np.dtype(dtype)
+    if dtype == np.float64:
+        return L.GB_F64
+    if dtype == np.complex128:
+        return L.GB_C128
+    raise TypeError(f"unsupported dtype {dtype}; use float64 or complex128")
+
+
+class DeviceTensor:
+    """A dense TensorMap block resident on the GPU."""
+
+    __slots__ = ("ctx", "handle", "kind", "dtype", "dims", "__weakref__")
+
+    def __init__(self, ctx, kind, dtype, dims, handle=None):
+        self.ctx = ctx
+        self.kind = _KIND_NAMES[kind] if isinstance(kind, str) else kind
+        self.dtype = np.dtype(dtype)
+        self.dims = tuple(int(x) for x in dims)
+        if handle is None:
+            arr = (ctypes.c_int64 * len(self.dims))(*self.dims)
+            h = ctypes.c_void_p()
+            L.check(L.lib().gb_tensor_create(ctx.handle, self.kind, _dtype_code(self.dtype),
+                                             len(self.dims), arr, ctypes.byref(h)))
+            handle = h
+        self.handle = handle
+
+    @staticmethod
+    def wrap(ctx, handle):
+        """Adopt a tensor created by the library (e.g. an SVD output)."""
+        kind = ctypes.c_int()
+        dt = ctypes.c_int()
+        nd = ctypes.c_int()
+        dims = (ctypes.c_int64 * 6)()
+        L.check(L.lib().gb_tensor_shape(handle, ctypes.byref(kind), ctypes.byref(dt),
+                                        ctypes.byref(nd), dims))
+        dtype = np.float64 if dt.value == L.GB_F64 else np.complex128
+        return DeviceTensor(ctx, kind.value, dtype, [dims[i] for i in range(nd.value)], handle)
+
+    @staticmethod
+    def from_numpy(ctx, kind, arr, dtype=None):
+        arr = np.asarray(arr)
+        dtype = np.dtype(dtype or arr.dtype)
+        if dtype.kind == "f" and arr.dtype.kind == "c":
+            raise TypeError("cannot store complex data in a real tensor")
+        t = DeviceTensor(ctx, kind, dtype, arr.shape)
+        t.upload(arr)
+        return t
+
+    def upload(self, arr):
+        a = np.asfortranarray(np.asarray(arr, dtype=self.dtype))
+        if a.shape != self.dims:
+            raise ValueError(f"shape {a.shape} does not match tensor {self.dims}")
+        L.check(L.lib().gb_tensor_upload(self.handle, a.ctypes.data_as(ctypes.c_void_p), a.nbytes))
+
+    def numpy(self):
+        out = np.empty(self.dims, dtype=self.dtype, order="F")
+        L.check(L.lib().gb_tensor_download(self.handle, out.ctypes.data_as(ctypes.c_void_p),
+                                           out.nbytes))
+        return out
+
+    # ------------------------------------------------ VectorInterface-style operations
+    def similar(self):
+        return DeviceTensor(self.ctx, self.kind, self.dtype, self.dims)
+
+    def copy(self):
+        t = self.similar()
+        L.check(L.lib().gb_tensor_copy(t.handle, self.handle))
+        return t
+
+    def scale_(self, a):
+        a = complex(a)
+        L.check(L.lib().gb_tensor_scale(self.handle, a.real, a.imag))
+        return self
+
+    def axpy_(self, a, x):
+        a = complex(a)
+        L.check(L.lib().gb_tensor_axpy(self.handle, a.real, a.imag, x.handle))
+        return self
+
+    def dot(self, other):
+        re = ctypes.c_double()
+        im = ctypes.c_double()
+        L.check(L.lib().gb_tensor_dot(self.handle, other.handle, ctypes.byref(re), ctypes.byref(im)))
+        return complex(re.value, im.value) if self.dtype.kind == "c" else re.value
+
+    def norm(self):
+        v = ctypes.c_double()
+        L.check(L.lib().gb_tensor_norm(self.handle, ctypes.byref(v)))
+        return v.value
+
+    def normalize_(self):
+        return self.scale_(1.0 / self.norm())
+
+    @property
+    def size(self):
+        return int(np.prod(self.dims))
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and L._lib is not None:
+            try:
+                L.lib().gb_tensor_free(h)
+            except Exception:
+                pass
+            self.handle = None
+
+    def __repr__(self):
+        return f"DeviceTensor(kind={self.kind}, dtype={self.dtype}, dims={self.dims})"

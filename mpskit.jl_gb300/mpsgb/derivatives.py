@@ -1,0 +1,174 @@
+"""Derivative operators and their Krylov solvers (host mirror of MPSKit's API).
+
+  AC2_hamiltonian / AC_hamiltonian / C_hamiltonian
+      -- src/algorithms/derivatives/hamiltonian_derivatives.jl:44-55, 206-217,
+         src/algorithms/derivatives/mpo_derivatives.jl:37-45
+  fixedpoint(H, x0, :SR, Lanczos)       -- src/algorithms/fixedpoint.jl:15-18
+  integrate(H, y0, t, dt, Lanczos)      -- src/algorithms/timestep/integrators.jl:44-53
+
+Every operator is a handle to a prepared operator living on the GPU; applying it and
+solving with it run entirely on the device through libmpsgb.
+"""
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+from .core import DeviceTensor
+
+
+@dataclass
+class GB300Backend:
+    """Contraction backend selecting the GB300 engine (the `backend` seam of
+    DMRG/DMRG2/VUMPS/TDVP, src/algorithms/groundstate/dmrg.jl:86-87).
+
+    precision: "fp64" (plain) or "bf16x3" (split-precision tensor-core contractions with
+    FP64 Krylov/gauge steps)."""
+    precision: str = "fp64"
+    device: int = 0
+
+    @property
+    def code(self):
+        return {"fp64": L.GB_PREC_FP64, "bf16x3": L.GB_PREC_BF16X3}[self.precision]
+
+
+@dataclass
+class Lanczos:
+    """KrylovKit.Lanczos parameters used by MPSKit's eigensolves."""
+    krylovdim: int = 30
+    maxiter: int = 100
+    tol: float = 1e-12
+    eager: bool = False
+
+
+class DerivativeOperator:
+    """A prepared effective Hamiltonian (C, AC or AC2) on the device."""
+
+    def __init__(self, ctx, kind, GL, W1, W2, GR, backend):
+        self.ctx = ctx
+        self.kind = kind
+        self.backend = backend
+        h = ctypes.c_void_p()
+        L.check(L.lib().gb_heff_build(ctx.handle, kind, GL.handle,
+                                      W1.handle if W1 is not None else None,
+                                      W2.handle if W2 is not None else None,
+                                      GR.handle, backend.code, ctypes.byref(h)))
+        self.handle = h
+        # keep the environments alive: the operator references their device storage
+        self._keep = (GL, GR, W1, W2)
+        self.dtype = GL.dtype
+        Dl, Dr = GL.dims[0], GR.dims[0]
+        if kind == L.GB_HEFF_AC2:
+            self.xkind, self.xdims = L.GB_KIND_AC2, (Dl, W1.dims[1], Dr, W2.dims[1])
+        elif kind == L.GB_HEFF_AC:
+            self.xkind, self.xdims = L.GB_KIND_MPS, (Dl, W1.dims[1], Dr)
+        else:
+            self.xkind, self.xdims = L.GB_KIND_BOND, (Dl, Dr)
+
+    @property
+    def terms(self):
+        buf = ctypes.create_string_buffer(256)
+        L.check(L.lib().gb_heff_terms(self.handle, buf, 256))
+        return tuple(t for t in buf.value.decode().split(",") if t)
+
+    @property
+    def flops(self):
+        v = ctypes.c_double()
+        L.check(L.lib().gb_heff_flops(self.handle, ctypes.byref(v)))
+        return v.value
+
+    def set_precision(self, precision):
+        code = {"fp64": L.GB_PREC_FP64, "bf16x3": L.GB_PREC_BF16X3}[precision]
+        L.check(L.lib().gb_heff_set_precision(self.handle, code))
+
+    def new_vector(self):
+        return DeviceTensor(self.ctx, self.xkind, self.dtype, self.xdims)
+
+    def __call__(self, x, out=None):
+        y = out if out is not None else x.similar()
+        L.check(L.lib().gb_heff_apply(self.handle, x.handle, y.handle))
+        return y
+
+    __mul__ = __call__
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and L._lib is not None:
+            try:
+                L.lib().gb_heff_free(h)
+            except Exception:
+                pass
+            self.handle = None
+
+
+def AC2_hamiltonian(site, psi, H, envs, backend=None):
+    """JordanMPO_AC2_Hamiltonian for bond (site, site+1), prepared."""
+    backend = backend or GB300Backend()
+    ctx = envs.ctx
+    W = H.device(ctx, envs.dtype)
+    return DerivativeOperator(ctx, L.GB_HEFF_AC2, envs.leftenv(site, psi), W[site], W[site + 1],
+                              envs.rightenv(site + 1, psi), backend)
+
+
+def AC_hamiltonian(site, psi, H, envs, backend=None):
+    backend = backend or GB300Backend()
+    ctx = envs.ctx
+    W = H.device(ctx, envs.dtype)
+    return DerivativeOperator(ctx, L.GB_HEFF_AC, envs.leftenv(site, psi), W[site], None,
+                              envs.rightenv(site, psi), backend)
+
+
+def C_hamiltonian(site, psi, H, envs, backend=None):
+    """MPO_C_Hamiltonian of the bond right of `site` (GL[site+1], GR[site])."""
+    backend = backend or GB300Backend()
+    return DerivativeOperator(envs.ctx, L.GB_HEFF_C, envs.leftenv(site + 1, psi), None, None,
+                              envs.rightenv(site, psi), backend)
+
+
+class Info:
+    def __init__(self, ki):
+        self.converged = ki.converged
+        self.numops = ki.numops
+        self.numiter = ki.numiter
+        self.normres = ki.normres
+
+    def __repr__(self):
+        return (f"Info(converged={self.converged}, normres={self.normres:.3e}, "
+                f"numops={self.numops}, numiter={self.numiter})")
+
+
+def fixedpoint(A, x0, which="SR", alg=None):
+    """Lowest eigenpair (val, vec, info); x0 is not modified."""
+    if which != "SR":
+        raise NotImplementedError("only :SR eigensolves run on the device")
+    alg = alg or Lanczos()
+    x = x0.copy()
+    lam = ctypes.c_double()
+    ki = L.KrylovInfo()
+    L.check(L.lib().gb_heff_eigsolve(A.handle, x.handle, int(alg.krylovdim), int(alg.maxiter),
+                                     float(alg.tol), int(bool(alg.eager)), ctypes.byref(lam),
+                                     ctypes.byref(ki)))
+    return lam.value, x, Info(ki)
+
+
+def exponentiate(A, t, x0, alg=None):
+    """exp(t A) x0 (KrylovKit.exponentiate); returns (y, info)."""
+    alg = alg or Lanczos(tol=1e-12)
+    t = complex(t)
+    y = x0.copy()
+    ki = L.KrylovInfo()
+    L.check(L.lib().gb_heff_exponentiate(A.handle, y.handle, t.real, t.imag, int(alg.krylovdim),
+                                         int(alg.maxiter), float(alg.tol), ctypes.byref(ki)))
+    return y, Info(ki)
+
+
+def integrate(A, y0, t, dt, alg=None, imaginary_evolution=False):
+    """integrate(f, y0, t, dt, alg) for a time-independent operator
+    (integrators.jl:44-53): exp(-i dt A) y0, or exp(-dt A) y0 in imaginary time."""
+    tt = -dt if imaginary_evolution else -1j * dt
+    y, info = exponentiate(A, tt, y0, alg)
+    if info.converged == 0:
+        import warnings
+        warnings.warn(f"integrator failed to converge: {info}")
+    return y

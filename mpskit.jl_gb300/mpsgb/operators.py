@@ -1,0 +1,268 @@
+"""MPOHamiltonian in Jordan block form, built from lattice terms.
+
+Restates MPSKit's builder (src/operators/mpohamiltonian.jl:349-519 finite,
+:521-641 infinite): terms are instantiated with identity strings between their sites
+(`instantiate_operator`, :360-386), sorted by range, and every term gets its own
+continuing channel on each bond it crosses (`_find_channel`, :408-416: the smallest
+free channel label >= the incoming one).  Two-site operators are split by a truncated
+SVD into a left isometry and a right factor (`decompose_localmpo`,
+src/utility/utility.jl:54-66).  The result is stored densely over the channel sum
+space, W[wl, s, s', wr], with channel 0 = "not started" and the last channel =
+"finished" -- the JordanMPOTensor layout (src/operators/jordanmpotensor.jl:1-66)
+flattened, which is also the GB_KIND_MPO format of the C ABI.
+"""
+import numpy as np
+
+from . import _lib as L
+from .core import DeviceTensor
+
+_SX = np.array([[0, 1], [1, 0]], dtype=np.complex128) / 2
+_SY = np.array([[0, -1j], [1j, 0]], dtype=np.complex128) / 2
+_SZ = np.array([[1, 0], [0, -1]], dtype=np.complex128) / 2
+
+
+def spin_half():
+    """(Sx, Sy, Sz) = sigma/2."""
+    return _SX.copy(), _SY.copy(), _SZ.copy()
+
+
+def kron2(a, b):
+    """Two-site operator O[s1, s2; s1', s2'] = a[s1, s1'] b[s2, s2']."""
+    return np.einsum("ik,jl->ijkl", a, b)
+
+
+def _as(a, dtype):
+    a = np.asarray(a)
+    if np.dtype(dtype).kind == "f":
+        if np.abs(a.imag).max(initial=0.0) > 1e-14:
+            raise ValueError("operator is not real")
+        return np.ascontiguousarray(a.real, dtype=np.float64)
+    return np.ascontiguousarray(a, dtype=np.complex128)
+
+
+def split_two_site(op, atol=None):
+    """op[s1,s2,s1',s2'] = sum_k L[s1,s1',k] R[k,s2,s2'] with an isometric left factor."""
+    d1, d2 = op.shape[0], op.shape[1]
+    atol = np.finfo(np.float64).eps ** 0.75 if atol is None else atol
+    M = op.transpose(0, 2, 1, 3).reshape(d1 * d1, d2 * d2)
+    U, S, Vh = np.linalg.svd(M, full_matrices=False)
+    r = int((S > atol).sum())
+    left = U[:, :r].reshape(d1, d1, r)
+    right = (S[:r, None] * Vh[:r]).reshape(r, d2, d2)
+    return left.astype(op.dtype), right.astype(op.dtype)
+
+
+class MPOHamiltonian:
+    """Dense Jordan-form MPO.  `W[i]` has shape (wl, d, d, wr)."""
+
+    def __init__(self, W, finite=True):
+        self.W = list(W)
+        self.finite = finite
+        self._dev = {}
+
+    def __len__(self):
+        return len(self.W)
+
+    def __getitem__(self, i):
+        return self.W[i % len(self.W)]
+
+    @property
+    def dtype(self):
+        return self.W[0].dtype
+
+    def widths(self):
+        return [w.shape[3] for w in self.W]
+
+    def device(self, ctx, dtype=None):
+        """GB_KIND_MPO tensors of every site (cached per context and dtype)."""
+        dtype = np.dtype(dtype or self.dtype)
+        key = (id(ctx), dtype.str)
+        if key not in self._dev:
+            self._dev[key] = [DeviceTensor.from_numpy(ctx, L.GB_KIND_MPO, w, dtype) for w in self.W]
+        return self._dev[key]
+
+
+def _site_pieces(sites, op):
+    if len(sites) == 1:
+        return [op.reshape(1, op.shape[0], op.shape[1], 1)]
+    a, b = split_two_site(op)
+    return [a.reshape(1, a.shape[0], a.shape[1], a.shape[2]),
+            b.reshape(b.shape[0], b.shape[1], b.shape[2], 1)]
+
+
+def _normalize_terms(terms, dtype):
+    out = []
+    for sites, op in terms:
+        sites = tuple(int(s) for s in sites)
+        op = _as(op, dtype)
+        if len(sites) == 2 and sites[0] > sites[1]:
+            sites = (sites[1], sites[0])
+            op = op.transpose(1, 0, 3, 2)
+        if len(sites) == 2 and sites[0] == sites[1]:
+            raise ValueError("a two-site term needs two distinct sites")
+        pieces = _site_pieces(sites, op)
+        span = list(range(sites[0], sites[-1] + 1))
+        chain = []
+        it = iter(pieces)
+        for s in span:
+            chain.append(next(it) if s in sites else 1.0)
+        out.append((span, chain))
+    out.sort(key=lambda t: len(t[0]))
+    return out
+
+
+def _free_channel(used, start):
+    c = max(start, 2)
+    taken = set(used)
+    while c in taken:
+        c += 1
+    return c
+
+
+def _assign(terms, nsites, wrap):
+    keys = [[] for _ in range(nsites)]
+    ops = [[] for _ in range(nsites)]
+    for span, chain in terms:
+        incoming = 1
+        for j, (site, piece) in enumerate(zip(span, chain)):
+            s = site % nsites if wrap else site
+            outgoing = 0 if j == len(chain) - 1 else _free_channel([k[1] for k in keys[s]], incoming)
+            keys[s].append((incoming, outgoing))
+            ops[s].append(piece)
+            incoming = outgoing
+    return keys, ops
+
+
+def _fill(keys_s, ops_s, cl, cr, d, dtype, identity_corners):
+    offl = np.concatenate([[0], np.cumsum(cl)]).astype(int)
+    offr = np.concatenate([[0], np.cumsum(cr)]).astype(int)
+    W = np.zeros((offl[-1], d, d, offr[-1]), dtype=dtype)
+    nr, nc = len(cl), len(cr)
+    if identity_corners:
+        if nc > 1:
+            W[0, :, :, 0] += np.eye(d)
+        if nr > 1:
+            W[offl[-2], :, :, offr[-2]] += np.eye(d)
+    for (kl, kr), piece in zip(keys_s, ops_s):
+        kr = nc if kr == 0 else kr
+        rl = slice(offl[kl - 1], offl[kl])
+        rr = slice(offr[kr - 1], offr[kr])
+        if isinstance(piece, np.ndarray):
+            W[rl, :, :, rr] += piece
+        elif piece != 0:
+            n = offl[kl] - offl[kl - 1]
+            W[rl, :, :, rr] += piece * np.einsum("ab,st->astb", np.eye(n), np.eye(d))
+    return W
+
+
+def FiniteMPOHamiltonian(nsites, d, terms, dtype=np.complex128):
+    """Jordan-form MPO of sum(terms) on an open chain of `nsites` sites of dimension d."""
+    terms = _normalize_terms(terms, dtype)
+    keys, ops = _assign(terms, nsites, wrap=False)
+    chans = [[1] for _ in range(nsites + 1)]
+    for i in range(nsites - 1):
+        n = max([k[1] for k in keys[i]] + [1]) + 1
+        V = [1] * n
+        if n > 2:
+            for (kl, kr), piece in zip(keys[i], ops[i]):
+                idx = n - 1 if kr == 0 else kr - 1
+                V[idx] = piece.shape[3] if isinstance(piece, np.ndarray) else chans[i][kl - 1]
+        chans[i + 1] = V
+    W = [_fill(keys[i], ops[i], chans[i], chans[i + 1], d, np.dtype(dtype), True)
+         for i in range(nsites)]
+    return MPOHamiltonian(W, finite=True)
+
+
+def InfiniteMPOHamiltonian(ncell, d, terms, dtype=np.complex128):
+    """Jordan-form MPO of a translation-invariant sum of terms with unit cell `ncell`."""
+    terms = _normalize_terms(terms, dtype)
+    keys, ops = _assign(terms, ncell, wrap=True)
+    n = max(max([k[1] for k in K] + [1]) + 1 for K in keys)
+    V = [[None] * n for _ in range(ncell)]   # V[i] = channels right of site i
+    for v in V:
+        v[0] = 1
+        v[-1] = 1
+    for i in range(ncell):
+        for (kl, kr), piece in zip(keys[i], ops[i]):
+            if not isinstance(piece, np.ndarray):
+                continue
+            kr = n if kr == 0 else kr
+            V[i - 1][kl - 1] = piece.shape[0]
+            V[i][kr - 1] = piece.shape[3]
+    changed = True
+    while changed:
+        changed = False
+        for i in range(ncell):
+            for (kl, kr), piece in zip(keys[i], ops[i]):
+                if isinstance(piece, np.ndarray):
+                    continue
+                kr = n if kr == 0 else kr
+                a, b = V[i - 1][kl - 1], V[i][kr - 1]
+                if a is not None and b is None:
+                    V[i][kr - 1] = a
+                    changed = True
+                elif a is None and b is not None:
+                    V[i - 1][kl - 1] = b
+                    changed = True
+    V = [[1 if x is None else x for x in v] for v in V]
+    W = [_fill(keys[i], ops[i], V[i - 1], V[i], d, np.dtype(dtype), True) for i in range(ncell)]
+    return MPOHamiltonian(W, finite=False)
+
+
+# ------------------------------------------------------------------ models
+
+def heisenberg_XXX(L, J=1.0, dtype=np.complex128, infinite=False):
+    """J sum S_i . S_{i+1} for spin 1/2."""
+    sx, sy, sz = spin_half()
+    h = J * (kron2(sx, sx) + kron2(sy, sy) + kron2(sz, sz))
+    if infinite:
+        return InfiniteMPOHamiltonian(L, 2, [((i, i + 1), h) for i in range(L)], dtype)
+    return FiniteMPOHamiltonian(L, 2, [((i, i + 1), h) for i in range(L - 1)], dtype)
+
+
+def xxz(L, Jxy=1.0, Jz=1.0, hz=0.0, dtype=np.complex128, infinite=False):
+    sx, sy, sz = spin_half()
+    h = Jxy * (kron2(sx, sx) + kron2(sy, sy)) + Jz * kron2(sz, sz)
+    nb = L if infinite else L - 1
+    terms = [((i, i + 1), h) for i in range(nb)]
+    if hz:
+        terms += [((i,), -hz * sz) for i in range(L)]
+    build = InfiniteMPOHamiltonian if infinite else FiniteMPOHamiltonian
+    return build(L, 2, terms, dtype)
+
+
+def transverse_field_ising(L, g=1.0, J=1.0, dtype=np.complex128, infinite=False):
+    """-J sum Z Z - g sum X with Pauli X = 2Sx, Z Z = 4 Sz Sz."""
+    sx, sy, sz = spin_half()
+    nb = L if infinite else L - 1
+    terms = [((i,), -g * 2 * sx) for i in range(L)]
+    terms += [((i, i + 1), -J * 4 * kron2(sz, sz)) for i in range(nb)]
+    build = InfiniteMPOHamiltonian if infinite else FiniteMPOHamiltonian
+    return build(L, 2, terms, dtype)
+
+
+def j1j2_cylinder(Lx, Ly, J1=1.0, J2=0.5, dtype=np.float64):
+    """J1-J2 Heisenberg on an Lx x Ly cylinder (periodic in y, open in x), snake-ordered."""
+    def site(x, y):
+        y %= Ly
+        return x * Ly + (y if x % 2 == 0 else Ly - 1 - y)
+
+    sx, sy, sz = spin_half()
+    h = kron2(sx, sx) + kron2(sy, sy) + kron2(sz, sz)
+    bonds = {}
+
+    def add(a, b, J):
+        if a != b:
+            key = (min(a, b), max(a, b))
+            bonds[key] = bonds.get(key, 0.0) + J
+
+    for x in range(Lx):
+        for y in range(Ly):
+            if Ly > 2 or y + 1 < Ly:
+                add(site(x, y), site(x, y + 1), J1)
+            if x + 1 < Lx:
+                add(site(x, y), site(x + 1, y), J1)
+                add(site(x, y), site(x + 1, y + 1), J2)
+                add(site(x, y), site(x + 1, y - 1), J2)
+    terms = [((a, b), J * h) for (a, b), J in sorted(bonds.items())]
+    return FiniteMPOHamiltonian(Lx * Ly, 2, terms, dtype)

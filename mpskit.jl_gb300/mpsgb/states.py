@@ -1,0 +1,218 @@
+"""Device-resident FiniteMPS and FiniteEnvironments.
+
+  FiniteMPS(f, elt, P, maxV) + QR normalisation sweep -- src/states/finitemps.jl:229-282
+  AC2(psi, site; kind)                                 -- src/states/finitemps.jl:376-385
+  left_gauge / right_gauge / gauge2!                   -- src/states/orthoview.jl:322-420
+  FiniteEnvironments leftenv / rightenv                -- src/environments/finite_envs.jl:31-49, 110-151
+
+The state keeps AL/AR/C tensors in HBM with an explicit centre bond; environments
+are recomputed lazily when the object identity of the AL/AR tensor they were built
+from changes (the `===` dependency test of finite_envs.jl:111, 138).
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib as L
+from .core import DeviceTensor, context
+
+
+def _wrap_out(ctx, *handles):
+    return [DeviceTensor.wrap(ctx, h) for h in handles]
+
+
+def left_orth(AC):
+    """AC = AL * C with a positive-diagonal QR (Householder(positive = true))."""
+    a, c = ctypes.c_void_p(), ctypes.c_void_p()
+    L.check(L.lib().gb_left_orth(AC.ctx.handle, AC.handle, ctypes.byref(a), ctypes.byref(c)))
+    return tuple(_wrap_out(AC.ctx, a, c))
+
+
+def right_orth(AC):
+    """AC = C * AR with a positive-diagonal LQ."""
+    c, a = ctypes.c_void_p(), ctypes.c_void_p()
+    L.check(L.lib().gb_right_orth(AC.ctx.handle, AC.handle, ctypes.byref(c), ctypes.byref(a)))
+    return tuple(_wrap_out(AC.ctx, c, a))
+
+
+def svd_trunc(AC2, maxdim=None, atol=0.0, normalize=True):
+    """Truncated SVD of a two-site tensor -> (AL, S, AR, eps)."""
+    a, s, r = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+    eps = ctypes.c_double()
+    L.check(L.lib().gb_svd_trunc(AC2.ctx.handle, AC2.handle, int(maxdim or 0), float(atol),
+                                 int(bool(normalize)), ctypes.byref(a), ctypes.byref(s),
+                                 ctypes.byref(r), ctypes.byref(eps)))
+    al, S, ar = _wrap_out(AC2.ctx, a, s, r)
+    return al, S, ar, eps.value
+
+
+def mul_front(C, A):
+    out = DeviceTensor(A.ctx, L.GB_KIND_MPS, A.dtype, (C.dims[0], A.dims[1], A.dims[2]))
+    L.check(L.lib().gb_mps_mul_front(A.ctx.handle, C.handle, A.handle, out.handle))
+    return out
+
+
+def mul_tail(A, C):
+    out = DeviceTensor(A.ctx, L.GB_KIND_MPS, A.dtype, (A.dims[0], A.dims[1], C.dims[1]))
+    L.check(L.lib().gb_mps_mul_tail(A.ctx.handle, A.handle, C.handle, out.handle))
+    return out
+
+
+def ac2_from(A, B):
+    """AC2[l s1; r s2] = A[l s1; m] B[m s2; r]."""
+    out = DeviceTensor(A.ctx, L.GB_KIND_AC2, A.dtype, (A.dims[0], A.dims[1], B.dims[2], B.dims[1]))
+    L.check(L.lib().gb_mps_ac2(A.ctx.handle, A.handle, B.handle, out.handle))
+    return out
+
+
+def project_complement_(Y, X):
+    L.check(L.lib().gb_project_complement(Y.ctx.handle, Y.handle, X.handle))
+    return Y
+
+
+def bond_dims(L_, d, D):
+    V = [1] * (L_ + 1)
+    for k in range(1, L_):
+        V[k] = min(V[k - 1] * d, D)
+    for k in range(L_ - 1, 0, -1):
+        V[k] = min(V[k], V[k + 1] * d)
+    return V
+
+
+def random_tensors(L_, d, D, seed, dtype=np.complex128):
+    """Seeded i.i.d. normal entries (PCG64) on the full-rank virtual spaces."""
+    rng = np.random.default_rng(seed)
+    V = bond_dims(L_, d, D)
+    out = []
+    for i in range(L_):
+        shape = (V[i], d, V[i + 1])
+        if np.dtype(dtype).kind == "c":
+            a = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+        else:
+            a = rng.standard_normal(shape)
+        out.append(np.asarray(a, dtype=dtype))
+    return out
+
+
+class FiniteMPS:
+    """AL[i] valid for i < center, AR[i] for i >= center, C[center] the centre matrix."""
+
+    def __init__(self, AL, AR, C, center):
+        self.AL, self.AR, self.C, self.center = AL, AR, C, center
+
+    def __len__(self):
+        return len(self.AL)
+
+    @property
+    def ctx(self):
+        return self.C[self.center].ctx
+
+    @property
+    def dtype(self):
+        return self.C[self.center].dtype
+
+    @classmethod
+    def from_tensors(cls, As, ctx=None, normalize=True):
+        """FiniteMPS(As; normalize): positive-QR sweep left to right on the device, then
+        LQ moves right to left to build the AR gauge."""
+        ctx = ctx or context()
+        n = len(As)
+        A = [DeviceTensor.from_numpy(ctx, L.GB_KIND_MPS, a) for a in As]
+        AL = [None] * n
+        C = [None] * (n + 1)
+        R = None
+        for i in range(n):
+            q, R = left_orth(A[i])
+            if normalize:
+                R.scale_(1.0 / R.norm())
+            AL[i] = q
+            if i < n - 1:
+                A[i + 1] = mul_front(R, A[i + 1])
+        C[n] = R
+        psi = cls(AL, [None] * n, C, n)
+        psi.right_canonicalize()
+        return psi
+
+    @classmethod
+    def random(cls, L_, d, D, seed, dtype=np.complex128, ctx=None):
+        return cls.from_tensors(random_tensors(L_, d, D, seed, dtype), ctx)
+
+    def right_canonicalize(self):
+        n = len(self)
+        X = self.C[self.center]
+        for i in range(self.center - 1, -1, -1):
+            A = mul_tail(self.AL[i], X)
+            Lm, Q = right_orth(A)
+            self.AR[i] = Q
+            self.C[i] = Lm
+            X = Lm
+        self.center = 0
+        return self
+
+    def ac(self, i):
+        if self.center == i:
+            return mul_front(self.C[i], self.AR[i])
+        if self.center == i + 1:
+            return mul_tail(self.AL[i], self.C[i + 1])
+        raise ValueError(f"site {i} is not adjacent to the centre bond {self.center}")
+
+    def al(self, i):
+        if i < self.center:
+            return self.AL[i]
+        q, _ = left_orth(self.ac(i))
+        return q
+
+    def to_numpy(self):
+        """Host copies (AL, AR, C, center) in reference layout."""
+        f = lambda xs: [None if x is None else x.numpy() for x in xs]
+        return f(self.AL), f(self.AR), f(self.C), self.center
+
+
+class FiniteEnvironments:
+    def __init__(self, psi, H, ctx=None):
+        self.ctx = ctx or psi.ctx
+        self.H = H
+        n = len(psi)
+        self.dtype = np.result_type(psi.dtype, H.dtype)
+        one = np.ones((1, 1, 1), dtype=self.dtype)
+        self.GL = [None] * (n + 1)
+        self.GR = [None] * (n + 1)
+        self.GL[0] = DeviceTensor.from_numpy(self.ctx, L.GB_KIND_GL, one)
+        self.GR[n - 1] = DeviceTensor.from_numpy(self.ctx, L.GB_KIND_GR, one)
+        self.ldep = [None] * n
+        self.rdep = [None] * n
+        self.precision = L.GB_PREC_FP64
+
+    def _W(self):
+        return self.H.device(self.ctx, self.dtype)
+
+    def leftenv(self, i, psi):
+        first = next((j for j in range(i) if psi.AL[j] is not self.ldep[j]), None)
+        if first is not None:
+            W = self._W()
+            for j in range(first, i):
+                A = psi.AL[j]
+                out = DeviceTensor(self.ctx, L.GB_KIND_GL, self.dtype,
+                                   (A.dims[2], W[j].dims[3], A.dims[2]))
+                L.check(L.lib().gb_env_transfer_left(self.ctx.handle, self.GL[j].handle,
+                                                     W[j].handle, A.handle, A.handle,
+                                                     self.precision, out.handle))
+                self.GL[j + 1] = out
+                self.ldep[j] = A
+        return self.GL[i]
+
+    def rightenv(self, i, psi):
+        n = len(psi)
+        first = next((j for j in range(n - 1, i, -1) if psi.AR[j] is not self.rdep[j]), None)
+        if first is not None:
+            W = self._W()
+            for j in range(first, i, -1):
+                A = psi.AR[j]
+                out = DeviceTensor(self.ctx, L.GB_KIND_GR, self.dtype,
+                                   (A.dims[0], W[j].dims[0], A.dims[0]))
+                L.check(L.lib().gb_env_transfer_right(self.ctx.handle, self.GR[j].handle,
+                                                      W[j].handle, A.handle, A.handle,
+                                                      self.precision, out.handle))
+                self.GR[j - 1] = out
+                self.rdep[j] = A
+        return self.GR[i]

@@ -1,0 +1,163 @@
+"""GPU parity of the derivative operators (through the C ABI) against the oracle."""
+import os
+
+import numpy as np
+import pytest
+
+import mpsgb
+from mpsgb import _lib as L
+from oracle import derivatives as dv
+from oracle import models as M
+from oracle import mps as P
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+FP64_TOL = 1e-12      # relative, plain FP64 path
+SPLIT_TOL = 1e-4      # relative, bf16x3 split path (hi/lo BF16 operands, FP32 accumulate)
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    return mpsgb.context(0)
+
+
+def _envs(L_, terms, dt, D, seed):
+    H = M.finite_mpo_hamiltonian(L_, 2, terms, dtype=dt)
+    psi = P.finite_mps_from_tensors(P.random_initial_tensors(L_, 2, D, seed, dt))
+    return H, psi, P.FiniteEnvironments(psi, H)
+
+
+def _rand(rng, shape, dt):
+    x = rng.standard_normal(shape)
+    if np.dtype(dt).kind == "c":
+        x = x + 1j * rng.standard_normal(shape)
+    return x.astype(dt)
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def dev_op(ctx, kind, GL, W1, W2, GR, prec="fp64"):
+    dt = GL.dtype
+    g = mpsgb.DeviceTensor.from_numpy(ctx, "gl", GL)
+    r = mpsgb.DeviceTensor.from_numpy(ctx, "gr", GR)
+    w1 = mpsgb.DeviceTensor.from_numpy(ctx, "mpo", W1) if W1 is not None else None
+    w2 = mpsgb.DeviceTensor.from_numpy(ctx, "mpo", W2) if W2 is not None else None
+    return mpsgb.DerivativeOperator(ctx, kind, g, w1, w2, r, mpsgb.GB300Backend(prec))
+
+
+@pytest.mark.parametrize("name", ["ac2_heisenberg_c128", "ac2_tfim_edge_f64", "ac2_j1j2_f64"])
+def test_ac2_golden_fixtures(ctx, name):
+    f = np.load(os.path.join(HERE, "golden", f"{name}.npz"))
+    op = dev_op(ctx, L.GB_HEFF_AC2, f["GL"], f["W1"], f["W2"], f["GR"])
+    assert ",".join(op.terms) == str(f["terms"])
+    y = op(mpsgb.DeviceTensor.from_numpy(ctx, "ac2", f["x"])).numpy()
+    assert _rel(y, f["y"]) < FP64_TOL
+
+
+MODELS = {
+    "heis_c": lambda: (10, M.heisenberg_terms(10), np.complex128),
+    "heis_r": lambda: (10, M.heisenberg_terms(10, dtype=np.float64), np.float64),
+    "tfim_r": lambda: (9, M.tfim_terms(9, g=0.9, dtype=np.float64), np.float64),
+    "xxz_field_c": lambda: (9, M.xxz_terms(9, 1.0, 1.5, 0.25), np.complex128),
+    "j1j2_r": lambda: (12, M.j1j2_cylinder_terms(4, 3), np.float64),
+}
+
+
+@pytest.mark.parametrize("model", sorted(MODELS))
+def test_ac2_every_bond(ctx, model):
+    L_, terms, dt = MODELS[model]()
+    H, psi, envs = _envs(L_, terms, dt, 12, 21)
+    rng = np.random.default_rng(5)
+    for pos in range(L_ - 1):
+        GL, GR = envs.leftenv(pos, psi), envs.rightenv(pos + 1, psi)
+        op = dev_op(ctx, L.GB_HEFF_AC2, GL, H[pos], H[pos + 1], GR)
+        ref_op = dv.JordanAC2(GL, H[pos], H[pos + 1], GR)
+        assert op.terms == ref_op.terms(), (pos, op.terms, ref_op.terms())
+        x = _rand(rng, (GL.shape[0], 2, GR.shape[0], 2), dt)
+        y = op(mpsgb.DeviceTensor.from_numpy(ctx, "ac2", x)).numpy()
+        assert _rel(y, ref_op(x)) < FP64_TOL, (model, pos)
+
+
+@pytest.mark.parametrize("model", sorted(MODELS))
+def test_ac_every_site(ctx, model):
+    L_, terms, dt = MODELS[model]()
+    H, psi, envs = _envs(L_, terms, dt, 12, 22)
+    rng = np.random.default_rng(6)
+    for pos in range(L_):
+        GL, GR = envs.leftenv(pos, psi), envs.rightenv(pos, psi)
+        op = dev_op(ctx, L.GB_HEFF_AC, GL, H[pos], None, GR)
+        ref_op = dv.JordanAC(GL, H[pos], GR)
+        x = _rand(rng, (GL.shape[0], 2, GR.shape[0]), dt)
+        y = op(mpsgb.DeviceTensor.from_numpy(ctx, "mps", x)).numpy()
+        assert _rel(y, ref_op(x)) < FP64_TOL, (model, pos)
+
+
+@pytest.mark.parametrize("model", ["heis_c", "j1j2_r"])
+def test_c_every_bond(ctx, model):
+    L_, terms, dt = MODELS[model]()
+    H, psi, envs = _envs(L_, terms, dt, 12, 23)
+    rng = np.random.default_rng(7)
+    for pos in range(L_ - 1):
+        GL, GR = envs.leftenv(pos + 1, psi), envs.rightenv(pos, psi)
+        op = dev_op(ctx, L.GB_HEFF_C, GL, None, None, GR)
+        x = _rand(rng, (GL.shape[0], GR.shape[0]), dt)
+        y = op(mpsgb.DeviceTensor.from_numpy(ctx, "bond", x)).numpy()
+        assert _rel(y, dv.mpo_c_apply(GL, GR, x)) < FP64_TOL
+
+
+@pytest.mark.parametrize("model", ["heis_c", "heis_r", "j1j2_r"])
+def test_split_precision_apply(ctx, model):
+    L_, terms, dt = MODELS[model]()
+    H, psi, envs = _envs(L_, terms, dt, 32, 24)
+    rng = np.random.default_rng(8)
+    pos = L_ // 2 - 1
+    GL, GR = envs.leftenv(pos, psi), envs.rightenv(pos + 1, psi)
+    op = dev_op(ctx, L.GB_HEFF_AC2, GL, H[pos], H[pos + 1], GR, "bf16x3")
+    x = _rand(rng, (GL.shape[0], 2, GR.shape[0], 2), dt)
+    y = op(mpsgb.DeviceTensor.from_numpy(ctx, "ac2", x)).numpy()
+    err = _rel(y, dv.JordanAC2(GL, H[pos], H[pos + 1], GR)(x))
+    assert err < SPLIT_TOL, err
+    assert ctx.device_status() == 0
+
+
+def test_linearity_of_apply(ctx):
+    """H(a x + b z) = a H(x) + b H(z) on the device (size-independent property)."""
+    L_, terms, dt = MODELS["xxz_field_c"]()
+    H, psi, envs = _envs(L_, terms, dt, 16, 25)
+    pos = 3
+    GL, GR = envs.leftenv(pos, psi), envs.rightenv(pos + 1, psi)
+    op = dev_op(ctx, L.GB_HEFF_AC2, GL, H[pos], H[pos + 1], GR)
+    rng = np.random.default_rng(9)
+    shape = (GL.shape[0], 2, GR.shape[0], 2)
+    x, z = _rand(rng, shape, dt), _rand(rng, shape, dt)
+    a, b = 0.3 - 1.2j, 2.1 + 0.4j
+    dx = mpsgb.DeviceTensor.from_numpy(ctx, "ac2", x)
+    dz = mpsgb.DeviceTensor.from_numpy(ctx, "ac2", z)
+    lhs = op(mpsgb.DeviceTensor.from_numpy(ctx, "ac2", a * x + b * z)).numpy()
+    rhs = a * op(dx).numpy() + b * op(dz).numpy()
+    assert _rel(lhs, rhs) < 1e-13
+
+
+def test_hermiticity(ctx):
+    L_, terms, dt = MODELS["heis_c"]()
+    H, psi, envs = _envs(L_, terms, dt, 8, 26)
+    pos = 4
+    GL, GR = envs.leftenv(pos, psi), envs.rightenv(pos + 1, psi)
+    op = dev_op(ctx, L.GB_HEFF_AC2, GL, H[pos], H[pos + 1], GR)
+    rng = np.random.default_rng(10)
+    shape = (GL.shape[0], 2, GR.shape[0], 2)
+    x, z = _rand(rng, shape, dt), _rand(rng, shape, dt)
+    hx = op(mpsgb.DeviceTensor.from_numpy(ctx, "ac2", x)).numpy()
+    hz = op(mpsgb.DeviceTensor.from_numpy(ctx, "ac2", z)).numpy()
+    assert abs(np.vdot(z, hx) - np.conj(np.vdot(x, hz))) < 1e-11 * np.linalg.norm(hx)
+
+
+def test_errors_are_reported_not_crashing(ctx):
+    f = np.load(os.path.join(HERE, "golden", "ac2_heisenberg_c128.npz"))
+    op = dev_op(ctx, L.GB_HEFF_AC2, f["GL"], f["W1"], f["W2"], f["GR"])
+    wrong = mpsgb.DeviceTensor(ctx, "ac2", np.complex128, (3, 2, 3, 2))
+    with pytest.raises(L.GBError) as e:
+        op(wrong)
+    assert e.value.code == L.GB_ERR_ARG

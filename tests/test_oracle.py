@@ -1,0 +1,162 @@
+"""CPU tests of the oracle: pinned by the reference's known answers, by exact
+diagonalisation built from the lattice terms, and by closed forms."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import derivatives as dv
+from oracle import krylov as K
+from oracle import models as M
+from oracle import mps as P
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+KAT = json.load(open(os.path.join(HERE, "golden", "known_answers.json")))
+
+
+def test_tfim_doctest_known_answer():
+    """find_groundstate.jl:49-64: DMRG2 from the all-ones product state, truncrank(16)."""
+    L = 4
+    H = M.finite_mpo_hamiltonian(L, 2, M.tfim_doctest_terms(L), dtype=np.float64)
+    psi = P.finite_mps_from_tensors([np.ones((1, 2, 1)) for _ in range(L)])
+    _, _, _, hist = P.find_groundstate_dmrg2(psi, H, P.DMRG2(maxdim=16), maxsweeps=30)
+    kat = KAT["tfim_L4_doctest"]
+    assert round(hist[-1][1], 4) == kat["energy_rounded_4"]
+
+
+def test_heisenberg_L20_known_answer():
+    """test/algorithms/groundstate.jl:151-175: E = -8.6824724 for L = 20, spin 1/2."""
+    L = 20
+    H = M.finite_mpo_hamiltonian(L, 2, M.heisenberg_terms(L, dtype=np.float64), dtype=np.float64)
+    psi = P.finite_mps_from_tensors(P.random_initial_tensors(L, 2, 8, 5, np.float64))
+    _, _, _, hist = P.find_groundstate_dmrg2(psi, H, P.DMRG2(maxdim=48, cutoff=1e-12), maxsweeps=12)
+    kat = KAT["heisenberg_L20_spin_half"]
+    assert abs(hist[-1][1] - kat["energy"]) < kat["atol"]
+
+
+@pytest.mark.parametrize("L", [6, 9])
+def test_dmrg2_matches_ed(L):
+    terms = M.xxz_terms(L, Jxy=1.0, Jz=1.5, hz=0.3)
+    H = M.finite_mpo_hamiltonian(L, 2, terms)
+    psi = P.finite_mps_from_tensors(P.random_initial_tensors(L, 2, 8, L))
+    _, _, _, hist = P.find_groundstate_dmrg2(psi, H, P.DMRG2(maxdim=64), maxsweeps=20)
+    e = M.ed_ground_energy(L, 2, terms)[0]
+    assert abs(hist[-1][1] - e) < 1e-9
+
+
+def test_tfim_free_fermion_closed_form():
+    L = 10
+    terms = M.tfim_terms(L, g=0.8)
+    e_ff = M.tfim_open_chain_energy(L, g=0.8)
+    e_ed = M.ed_ground_energy(L, 2, terms)[0]
+    assert abs(e_ff - e_ed) < 1e-10
+
+
+def test_golden_ed_fixture():
+    e = float(np.load(os.path.join(HERE, "golden", "ed_heisenberg_L10.npz"))["energy"])
+    assert abs(e - M.ed_ground_energy(10, 2, M.heisenberg_terms(10))[0]) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["ac2_heisenberg_c128", "ac2_tfim_edge_f64", "ac2_j1j2_f64"])
+def test_golden_ac2_fixtures_reproduce(name):
+    f = np.load(os.path.join(HERE, "golden", f"{name}.npz"))
+    op = dv.JordanAC2(f["GL"], f["W1"], f["W2"], f["GR"])
+    y = op(f["x"])
+    assert np.allclose(y, f["y"], rtol=0, atol=1e-12 * np.abs(f["y"]).max())
+    assert ",".join(op.terms()) == str(f["terms"])
+
+
+@pytest.mark.parametrize("model", ["heis", "tfim", "j1j2", "xxz_field"])
+def test_jordan_ac2_equals_generic_mpo_contraction(model):
+    """The Jordan decomposition + prepare folds are the same linear map as the generic
+    MPO_AC2 contraction (mpo_derivatives.jl:144-153)."""
+    if model == "heis":
+        L, terms, dt = 8, M.heisenberg_terms(8), np.complex128
+    elif model == "tfim":
+        L, terms, dt = 8, M.tfim_terms(8, g=1.3, dtype=np.float64), np.float64
+    elif model == "xxz_field":
+        L, terms, dt = 8, M.xxz_terms(8, 1.0, 0.7, 0.4), np.complex128
+    else:
+        L, terms, dt = 12, M.j1j2_cylinder_terms(4, 3), np.float64
+    H = M.finite_mpo_hamiltonian(L, 2, terms, dtype=dt)
+    psi = P.finite_mps_from_tensors(P.random_initial_tensors(L, 2, 6, 3, dt))
+    envs = P.FiniteEnvironments(psi, H)
+    rng = np.random.default_rng(0)
+    for pos in (0, L // 2 - 1, L - 2):
+        GL, GR = envs.leftenv(pos, psi), envs.rightenv(pos + 1, psi)
+        x = rng.standard_normal((GL.shape[0], 2, GR.shape[0], 2)).astype(dt)
+        y1 = dv.JordanAC2(GL, H[pos], H[pos + 1], GR)(x)
+        y2 = dv.JordanAC2(GL, H[pos], H[pos + 1], GR, prepare=False)(x)
+        y3 = dv.mpo_ac2_apply(GL, H[pos], H[pos + 1], GR, x)
+        assert np.allclose(y1, y3, atol=1e-11 * np.abs(y3).max())
+        assert np.allclose(y2, y3, atol=1e-11 * np.abs(y3).max())
+
+
+def test_jordan_ac_equals_generic():
+    L = 8
+    H = M.finite_mpo_hamiltonian(L, 2, M.xxz_terms(L, 1.0, 0.6, 0.2))
+    psi = P.finite_mps_from_tensors(P.random_initial_tensors(L, 2, 6, 4))
+    envs = P.FiniteEnvironments(psi, H)
+    rng = np.random.default_rng(2)
+    for pos in (0, 3, L - 1):
+        GL, GR = envs.leftenv(pos, psi), envs.rightenv(pos, psi)
+        x = rng.standard_normal((GL.shape[0], 2, GR.shape[0])) + 0j
+        y1 = dv.JordanAC(GL, H[pos], GR)(x)
+        y2 = dv.mpo_ac_apply(GL, H[pos], GR, x)
+        assert np.allclose(y1, y2, atol=1e-12 * np.abs(y2).max())
+
+
+def test_linearity_of_ac2_in_the_hamiltonian():
+    """AC2_hamiltonian(H1 + H2) x == AC2(H1) x + AC2(H2) x at fixed environments of each
+    (the LazySum linearity property of test/operators/lazysum.jl:79-260) -- checked here
+    through the energy functional: <psi|H1+H2|psi> = <H1> + <H2>."""
+    L = 8
+    t1 = M.heisenberg_terms(L)
+    t2 = [((i,), 0.3 * M.spin_ops()[2]) for i in range(L)]
+    psi = P.finite_mps_from_tensors(P.random_initial_tensors(L, 2, 6, 9))
+    e = []
+    for terms in (t1, t2, t1 + t2):
+        H = M.finite_mpo_hamiltonian(L, 2, terms)
+        envs = P.FiniteEnvironments(psi, H)
+        e.append(P.expectation_value(psi, H, envs, 0))
+    assert abs(e[0] + e[1] - e[2]) < 1e-12
+
+
+def test_lanczos_restart_matches_dense():
+    rng = np.random.default_rng(3)
+    A = rng.standard_normal((200, 200))
+    A = A + A.T
+    x0 = rng.standard_normal(200)
+    val, vec, info = K.lanczos_eigsolve(lambda v: A @ v, x0, krylovdim=20, maxiter=200, tol=1e-10)
+    assert abs(val - np.linalg.eigvalsh(A)[0]) < 1e-8
+    assert info.numiter > 1
+
+
+def test_exponentiate_matches_expm():
+    import scipy.linalg as sl
+    rng = np.random.default_rng(4)
+    A = rng.standard_normal((60, 60))
+    A = (A + A.T) / 10
+    x0 = rng.standard_normal(60) + 0j
+    y, info = K.lanczos_exponentiate(lambda v: A @ v, -0.7j, x0, krylovdim=20, tol=1e-12)
+    assert np.allclose(y, sl.expm(-0.7j * A) @ x0, atol=1e-10)
+
+
+def test_transfer_environment_energy_consistency():
+    """GL/GR built by transfer_left/right give the same energy at every site."""
+    L = 8
+    H = M.finite_mpo_hamiltonian(L, 2, M.heisenberg_terms(L))
+    psi = P.finite_mps_from_tensors(P.random_initial_tensors(L, 2, 6, 8))
+    envs = P.FiniteEnvironments(psi, H)
+    e0 = P.expectation_value(psi, H, envs, 0)
+    # move the centre right with positive QR and evaluate again
+    for i in range(L - 1):
+        ac = psi.ac(i)
+        Dl, d, Dr = ac.shape
+        Q, R = P.qr_pos(ac.reshape(Dl * d, Dr, order="F"))
+        psi.AL[i] = Q.reshape(Dl, d, -1, order="F")
+        psi.C[i + 1] = R
+        psi.center = i + 1
+        ei = P.expectation_value(psi, H, envs, i + 1)
+        assert abs(ei - e0) < 1e-11
