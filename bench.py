@@ -1,0 +1,443 @@
+#!/usr/bin/env python
+"""Benchmark of the effective-Hamiltonian hot path on one GB300.
+
+Workload (the configuration the headline metric is quoted at, D = 2048): two-site DMRG
+on the spin-1/2 J1-J2 Heisenberg model (J1 = 1, J2 = 0.5) on a width-6 cylinder of
+length 24, snake-ordered into a 144-site chain, MPO from the channel-assignment builder,
+Float64, seeded random initial MPS at D = 2048, split-precision (bf16x3) contractions
+with FP64 Lanczos / SVD.  U(1) block sparsity is not exploited: every contraction is
+computed densely, which is strictly more work than the block-sparse form.
+
+One step = one DMRG2 local update (dmrg.jl:211-244) at the central bond -- H_eff build
+and prepare, the Galerkin matvec, the adaptive Lanczos eigensolve, the truncated SVD --
+plus the environment step the next bond of a sweep needs.
+
+value  = H_eff algorithmic flops executed per second of step time (TFLOP/s);
+e2e    = the same, driven through the C ABI with host buffers (x0 uploaded from pinned
+         host memory, the new AL / S / AR downloaded every step);
+roofline = the tcgen05 split GEMM (dominant kernel), timed with CUDA events on the
+         library's stream, against the measured dense BF16 peak.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "mpskit.jl_gb300"), ROOT):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "DMRG sweep s & H_eff TFLOP/s at D=2048, split-prec vs FP64 GPU at |ΔE/E|≤1e-9"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--D", type=int, default=2048)
+    ap.add_argument("--Lx", type=int, default=24)
+    ap.add_argument("--Ly", type=int, default=6)
+    ap.add_argument("--precision", default="bf16x3", choices=["bf16x3", "fp64"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--seed", type=int, default=1234 + 5)
+    return ap.parse_args()
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        sm, mx, reasons = [], [], set()
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 7:
+                    continue
+                try:
+                    sm.append(float(f[0]))
+                    mx.append(float(f[1]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, f[3:7]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        except Exception:
+            pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def allmax(pg, v):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allsum(pg, v):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- oracle timing (CPU)
+
+def oracle_sample(GL, W1, W2, GR, dtype, reps):
+    """Time the oracle's JordanAC2 matvec (the reference algorithm restated in numpy) on
+    the host cores.  Returns (seconds per matvec, threads)."""
+    from oracle import derivatives as odv
+    try:
+        from threadpoolctl import threadpool_info
+        threads = max([i.get("num_threads", 1) for i in threadpool_info()] + [1])
+    except Exception:
+        threads = os.cpu_count() or 1
+    op = odv.JordanAC2(GL, W1, W2, GR)
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((GL.shape[0], W1.shape[1], GR.shape[0], W2.shape[1])).astype(dtype)
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        op(x)
+        times.append(time.perf_counter() - t0)
+    return min(times), threads
+
+
+def run_reference(args):
+    """--impl reference: the oracle port on the host cores, one matvec per step, at the
+    workload's central-bond shapes with seeded synthetic environments."""
+    world, rank, local, pg = dist_setup(args)
+    if rank != 0:
+        return
+    import mpsgb
+    H = mpsgb.j1j2_cylinder(args.Lx, args.Ly, dtype=np.float64)
+    n = len(H)
+    pos = n // 2 - 1
+    W1, W2 = H.W[pos], H.W[pos + 1]
+    D = args.D
+    rng = np.random.default_rng(args.seed)
+    GL = rng.standard_normal((D, W1.shape[0], D))
+    GR = rng.standard_normal((D, W2.shape[3], D))
+    flops = heff_ac2_flops(GL.shape, GR.shape, W1, W2, False)
+    for _ in range(args.warmup):
+        oracle_sample(GL, W1, W2, GR, np.float64, 1)
+    ts = []
+    threads = 1
+    for _ in range(args.steps):
+        t, threads = oracle_sample(GL, W1, W2, GR, np.float64, 1)
+        ts.append(t)
+    tot = sum(ts)
+    value = flops * len(ts) / tot / 1e12
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * tot / len(ts), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"J1-J2 {args.Ly}x{args.Lx} cylinder DMRG2 H_eff matvec at the "
+                               f"central bond, D={D}, dense Float64", "D": D,
+                   "sample": "one AC2 H_eff application per step (oracle port, numpy)"},
+        "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": threads, "kind": "port",
+                         "sample": "one JordanAC2 matvec of the workload per step"},
+        "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def heff_ac2_flops(GL_shape, GR_shape, W1, W2, cplx):
+    """Algorithmic flops of one AC2 application in the form libmpsgb executes it:
+    the GEMMs left after prepare folding and channel pruning (2 flops / real MAC)."""
+    Dl, wl, _ = GL_shape
+    Dr, wr, _ = GR_shape
+    d1, d2 = W1.shape[1], W2.shape[1]
+    wm = W1.shape[3]
+    nz = lambda a: a.size > 0 and np.any(a != 0)
+    A1, A2 = W1[1:-1, :, :, 1:-1], W2[1:-1, :, :, 1:-1]
+    B1, B2 = W1[1:-1, :, :, -1], W2[1:-1, :, :, -1]
+    C1, C2 = W1[0, :, :, 1:-1], W2[0, :, :, 1:-1]
+    CA = nz(C1) and nz(A2)
+    AB = nz(A1) and nz(B2)
+    IC = nz(C2) and not CA
+    BE = nz(B1) and not AB
+    macs = 0.0
+    if nz(A1) and nz(A2):
+        f1 = np.any(A1 != 0, axis=(1, 2))
+        f2 = np.any(A2 != 0, axis=(1, 2))
+        both = f1.any(0) & f2.any(1)
+        if both.any():
+            chr_ = int(f1[:, both].any(1).sum())
+            chc = int(f2[both, :].any(0).sum())
+            macs += Dl * d1 * d2 * chc * Dr * Dr + Dl * d1 * d2 * Dr * Dl * chr_
+    if CA:
+        macs += Dl * (d1 * d2 * Dr) ** 2
+    if AB:
+        macs += (Dl * d1 * d2) ** 2 * Dr
+    if IC:
+        macs += Dl * d1 * (d2 * Dr) ** 2
+    if BE:
+        macs += (Dl * d1) ** 2 * d2 * Dr
+    return (8.0 if cplx else 2.0) * macs
+
+
+# ---------------------------------------------------------------- our arm
+
+def run_ours(args):
+    world, rank, local, pg = dist_setup(args)
+    import mpsgb
+    from mpsgb.algorithms import SweepStats, dmrg2_local_update
+
+    ctx = mpsgb.context(local)
+    prec = args.precision
+    ctx.set_precision(prec)
+    backend = mpsgb.GB300Backend(prec, local)
+    H = mpsgb.j1j2_cylinder(args.Lx, args.Ly, dtype=np.float64)
+    n = len(H)
+    pos = n // 2 - 1
+    D = args.D
+    t_setup = time.perf_counter()
+    As = mpsgb.states.random_tensors(n, 2, D, args.seed + rank, np.float64)
+    psi = mpsgb.FiniteMPS.from_tensors(As, ctx, center=pos + 1)
+    del As
+    envs = mpsgb.FiniteEnvironments(psi, H, resident=False)
+    envs.precision = backend.code
+    envs.leftenv(pos, psi)
+    envs.rightenv(pos + 1, psi)
+    ctx.synchronize()
+    t_setup = time.perf_counter() - t_setup
+    alg = mpsgb.DMRG2(maxdim=D, cutoff=1e-10, backend=backend)
+    state = {"eps_local": 1.0, "eps_trunc": 0.0, "decay": 0.0}
+
+    def step(stats):
+        el, et, dec, val = dmrg2_local_update(pos, False, psi, H, alg, envs, state["eps_local"],
+                                              state["eps_trunc"], state["decay"], stats)
+        state.update(eps_local=el, eps_trunc=et, decay=dec, val=val)
+        envs.rightenv(pos, psi)  # environment step of the next bond in the sweep
+
+    warm = SweepStats()
+    for _ in range(args.warmup):
+        step(warm)
+    ctx.synchronize()
+    stats = SweepStats()
+    launches0 = ctx.kernel_launches()
+    barrier(pg)
+    ctx.synchronize()
+    with ClockSampler(local) as clocks:
+        ctx.profile_begin()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step(stats)
+        ctx.synchronize()
+        t_wall = time.perf_counter() - t0
+        prof = ctx.profile_end()
+    barrier(pg)
+    launches = ctx.kernel_launches() - launches0
+    t_dev = prof["region_ms"] / 1e3          # CUDA-event time of the region on the stream
+    t_step = max(t_wall, t_dev)
+    t_max = allmax(pg, t_step)
+    flops_tot = allsum(pg, stats.heff_flops)
+    value = flops_tot / t_max / 1e12
+    ms_per_step = 1e3 * t_max / args.steps
+
+    pk = peaks() or {}
+    peak_bf16 = pk.get("bf16_tflops_sustained")
+    peak_src = "measured (sustained)" if peak_bf16 else "fallback"
+    peak_bf16 = peak_bf16 or 1700.0
+    split = 3.0 if prec == "bf16x3" else 1.0
+    gemm_alg = prof["gemm_flops"] / (prof["gemm_ms"] / 1e3) / 1e12 if prof["gemm_ms"] > 0 else 0.0
+    achieved = split * gemm_alg
+    roofline = {
+        "bound": "tensor", "kernel": "gemm_bf16x3_kernel", "achieved": achieved,
+        "peak": peak_bf16, "unit": "TFLOP/s", "frac": achieved / peak_bf16,
+        "peak_source": peak_src, "algorithmic_tflops": gemm_alg,
+        "launches": prof["gemm_launches"], "kernel_ms": prof["gemm_ms"],
+        "kernel_share_of_step": prof["gemm_ms"] / max(1e-9, prof["region_ms"]),
+        "traffic": None,
+    }
+
+    # ---------------- end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(args, ctx, psi, H, envs, alg, pos, state, pg)
+
+    cpu = None
+    if not args.no_cpu_baseline and rank == 0 and world == 1:
+        GL = envs.leftenv(pos, psi).numpy()
+        GR = envs.rightenv(pos + 1, psi).numpy()
+        f1 = heff_ac2_flops(GL.shape, GR.shape, H.W[pos], H.W[pos + 1], False)
+        t, threads = oracle_sample(GL, H.W[pos], H.W[pos + 1], GR, np.float64, 1)
+        cpu = {"value": f1 / t / 1e12, "unit": "TFLOP/s", "cores": threads, "kind": "port",
+               "sample": f"one JordanAC2 matvec of the workload's central bond (D={D}) "
+                         f"with the device-built environments, {t:.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if prec == "fp64" else "f64 (bf16x3 split contractions)",
+            "data": "synthetic",
+            "config": {
+                "workload": f"J1-J2 Heisenberg {args.Ly}x{args.Lx} cylinder ({n} sites), DMRG2 "
+                            f"local update + env step at bond {pos}, D={D}, dense Float64",
+                "model": "J1=1, J2=0.5, snake order", "D": D, "L": n,
+                "mpo_width_at_bond": int(H.W[pos].shape[3]), "precision": prec,
+                "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (GL/GR/T1 >> 129 MB)",
+            },
+            "gpu_launches": launches,
+            "sweep_s_estimate": ms_per_step / 1e3 * (2 * n - 3),
+            "heff_flops_per_step": stats.heff_flops / args.steps,
+            "matvecs_per_step": stats.matvecs / args.steps,
+            "phase_s_per_step": {k: v / args.steps for k, v in stats.t.items()},
+            "local_energy": state.get("val"), "eps_trunc": state.get("eps_trunc"),
+            "setup_s": t_setup,
+            "roofline": roofline,
+            "clocks": clocks.summary(),
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+def run_e2e(args, ctx, psi, H, envs, alg, pos, state, pg):
+    """Local updates driven through the C ABI with host buffers: x0 uploaded from pinned
+    host memory, eigensolve + truncated SVD on the device, AL/S/AR downloaded."""
+    import ctypes
+
+    import mpsgb
+    from mpsgb import _lib as L
+    try:
+        import torch
+        pin = lambda shape: torch.empty(int(np.prod(shape)), dtype=torch.float64, pin_memory=True)
+        host_ptr = lambda t: ctypes.c_void_p(t.data_ptr())
+    except Exception:
+        pin = lambda shape: np.empty(int(np.prod(shape)))
+        host_ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    ac2 = mpsgb.ac2_from(psi.AL[pos], psi.ac(pos + 1))
+    x_host = pin(ac2.dims)
+    L.check(L.lib().gb_tensor_download(ac2.handle, host_ptr(x_host), ac2.size * 8))
+    Heff = mpsgb.AC2_hamiltonian(pos, psi, H, envs, alg.backend)
+    flops = Heff.flops
+    outs = {}
+
+    def one():
+        x = mpsgb.DeviceTensor(ctx, L.GB_KIND_AC2, np.float64, ac2.dims)
+        L.check(L.lib().gb_tensor_upload(x.handle, host_ptr(x_host), x.size * 8))
+        solver = alg.alg_eigsolve.adapt(state["decay"], state["eps_local"], state["eps_local"],
+                                        state["eps_trunc"])
+        lam = ctypes.c_double()
+        ki = L.KrylovInfo()
+        L.check(L.lib().gb_heff_eigsolve(Heff.handle, x.handle, solver.krylovdim, solver.maxiter,
+                                         solver.tol, int(solver.eager), ctypes.byref(lam),
+                                         ctypes.byref(ki)))
+        al, S, ar, eps = mpsgb.svd_trunc(x, alg.maxdim, alg.cutoff, True)
+        d2h = 0
+        for t in (al, S, ar):
+            key = t.dims
+            if key not in outs:
+                outs[key] = pin(t.dims)
+            L.check(L.lib().gb_tensor_download(t.handle, host_ptr(outs[key]), t.size * 8))
+            d2h += t.size * 8
+        return ki.numops, d2h
+
+    for _ in range(max(1, args.warmup)):
+        one()
+    barrier(pg)
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    nops, d2h = 0, 0
+    for _ in range(args.steps):
+        k, b = one()
+        nops += k
+        d2h = b
+    ctx.synchronize()
+    t = allmax(pg, time.perf_counter() - t0)
+    fl = allsum(pg, flops * nops)
+    return {"value": fl / t / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": ac2.size * 8,
+            "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * t / args.steps,
+            "path": "gb_tensor_upload -> gb_heff_eigsolve -> gb_svd_trunc -> gb_tensor_download"}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

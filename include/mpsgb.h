@@ -97,6 +97,15 @@ int gb_ctx_device_status(gb_ctx* ctx, int32_t* out);
 /* arithmetic of the auxiliary state contractions of this context (gb_mps_ac2,
  * gb_mps_mul_front, gb_mps_mul_tail); GB_PREC_FP64 by default */
 int gb_ctx_set_precision(gb_ctx* ctx, int precision);
+/* Tracing of the tensor-core GEMM (the dominant kernel): between profile_begin and
+ * profile_end every split-precision GEMM launch is bracketed by CUDA events on the
+ * context's stream.  profile_end synchronises and returns the summed kernel time (ms),
+ * the number of launches, their algorithmic flops (unsplit shapes) and the wall time of
+ * the whole region measured by events on the same stream (ms).  (Replaces the
+ * TimerOutputs tracing of src/algorithms/groundstate/dmrg.jl:289-292.) */
+int gb_ctx_profile_begin(gb_ctx* ctx);
+int gb_ctx_profile_end(gb_ctx* ctx, double* gemm_ms, int64_t* gemm_launches,
+                       double* gemm_flops, double* region_ms);
 
 /* ---------------------------------------------------------------- tensors */
 /* Storage of TensorMap blocks (TensorKit `TensorMap{T,S,N1,N2}` with Trivial sectors). */

@@ -529,6 +529,9 @@ int gb_ctx_destroy(gb_ctx* ctx) {
     cusolverDnDestroy((cusolverDnHandle_t)ctx->solver);
   }
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+  for (auto e : ctx->prof_events) cudaEventDestroy(e);
+  for (auto e : ctx->prof_region)
+    if (e) cudaEventDestroy(e);
   cudaFree(ctx->d_status);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -566,6 +569,44 @@ int gb_ctx_set_precision(gb_ctx* ctx, int precision) {
   GB_REQUIRE(ctx, "null context");
   GB_REQUIRE(precision == GB_PREC_FP64 || precision == GB_PREC_BF16X3, "unknown precision");
   ctx->aux_prec = precision;
+  API_END
+}
+
+int gb_ctx_profile_begin(gb_ctx* ctx) {
+  API_BEGIN
+  GB_REQUIRE(ctx, "null context");
+  DevGuard g(ctx->device);
+  for (auto& e : ctx->prof_region)
+    if (!e) GB_CHECK_CUDA(cudaEventCreate(&e));
+  ctx->profiling = true;
+  ctx->prof_used = 0;
+  ctx->prof_flops = 0.0;
+  GB_CHECK_CUDA(cudaEventRecord(ctx->prof_region[0], ctx->stream));
+  API_END
+}
+
+int gb_ctx_profile_end(gb_ctx* ctx, double* gemm_ms, int64_t* gemm_launches, double* gemm_flops,
+                       double* region_ms) {
+  API_BEGIN
+  GB_REQUIRE(ctx, "null context");
+  GB_REQUIRE(ctx->profiling, "profile_end without profile_begin");
+  DevGuard g(ctx->device);
+  GB_CHECK_CUDA(cudaEventRecord(ctx->prof_region[1], ctx->stream));
+  GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  double tot = 0.0;
+  for (size_t i = 0; i + 1 < ctx->prof_used; i += 2) {
+    float ms = 0.f;
+    GB_CHECK_CUDA(cudaEventElapsedTime(&ms, ctx->prof_events[i], ctx->prof_events[i + 1]));
+    tot += ms;
+  }
+  float rms = 0.f;
+  GB_CHECK_CUDA(cudaEventElapsedTime(&rms, ctx->prof_region[0], ctx->prof_region[1]));
+  if (gemm_ms) *gemm_ms = tot;
+  if (gemm_launches) *gemm_launches = (int64_t)(ctx->prof_used / 2);
+  if (gemm_flops) *gemm_flops = ctx->prof_flops;
+  if (region_ms) *region_ms = rms;
+  ctx->profiling = false;
+  ctx->prof_used = 0;
   API_END
 }
 

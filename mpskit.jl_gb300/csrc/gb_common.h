@@ -75,6 +75,12 @@ struct gb_ctx {
   size_t h_pinned_elems = 0;
   int num_sms = 0;
   int aux_prec = GB_PREC_FP64;   // precision of auxiliary state contractions
+  // tracing of the tensor-core GEMM launches
+  bool profiling = false;
+  std::vector<cudaEvent_t> prof_events;  // pairs (start, stop) per launch
+  size_t prof_used = 0;
+  double prof_flops = 0.0;
+  cudaEvent_t prof_region[2] = {nullptr, nullptr};
 };
 
 struct gb_tensor {

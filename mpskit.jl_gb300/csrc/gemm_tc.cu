@@ -471,8 +471,23 @@ void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_
   dim3 grid((unsigned)((M + TC_BM - 1) / TC_BM), (unsigned)((Npk + TC_BN - 1) / TC_BN),
             (unsigned)batch);
   GB_REQUIRE(grid.y <= 65535 && grid.z <= 65535, "gemm_split: grid too large");
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  if (ctx->profiling) {
+    if (ctx->prof_used + 2 > ctx->prof_events.size()) {
+      for (int i = 0; i < 64; ++i) {
+        cudaEvent_t e;
+        GB_CHECK_CUDA(cudaEventCreate(&e));
+        ctx->prof_events.push_back(e);
+      }
+    }
+    ev0 = ctx->prof_events[ctx->prof_used++];
+    ev1 = ctx->prof_events[ctx->prof_used++];
+    ctx->prof_flops += (A.cplx ? 8.0 : 2.0) * (double)M * (double)N * (double)A.K;
+    GB_CHECK_CUDA(cudaEventRecord(ev0, ctx->stream));
+  }
   gemm_bf16x3_kernel<<<grid, TC_THREADS, TC_SMEM_BYTES, ctx->stream>>>(ma, mb, a);
   GB_CHECK_CUDA(cudaGetLastError());
+  if (ev1) GB_CHECK_CUDA(cudaEventRecord(ev1, ctx->stream));
   count_launch(ctx);
 }
 

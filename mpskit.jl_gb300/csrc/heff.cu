@@ -652,6 +652,12 @@ static void build_ac2(gb_heff* h, const gb_tensor* GL, const gb_tensor* W1,
   if (!y_written && steps.empty()) h->y_zero_first = true;
   // mixes before any GEMM wrote y need y zeroed; GEMMs after a mix accumulate
   h->steps = std::move(steps);
+  // report the terms in the reference's field order (hamiltonian_derivatives.jl:168-178)
+  static const char* order[] = {"II", "IC", "ID", "CB", "CA", "AB", "AA", "BE", "DE", "EE"};
+  std::vector<std::string> sorted;
+  for (const char* o : order)
+    if (std::find(names.begin(), names.end(), o) != names.end()) sorted.push_back(o);
+  names = sorted;
   std::ostringstream os;
   for (size_t i = 0; i < names.size(); ++i) os << (i ? "," : "") << names[i];
   h->terms = os.str();
@@ -923,6 +929,12 @@ static void build_ac(gb_heff* h, const gb_tensor* GL, const gb_tensor* W, const 
   }
   if (steps.empty()) h->y_zero_first = true;
   h->steps = std::move(steps);
+  // report the terms in the reference's field order (hamiltonian_derivatives.jl:15-21)
+  static const char* order[] = {"D", "I", "E", "C", "B", "A"};
+  std::vector<std::string> sorted;
+  for (const char* o : order)
+    if (std::find(names.begin(), names.end(), o) != names.end()) sorted.push_back(o);
+  names = sorted;
   std::ostringstream os;
   for (size_t i = 0; i < names.size(); ++i) os << (i ? "," : "") << names[i];
   h->terms = os.str();

@@ -67,6 +67,8 @@ _SIGS = {
     "gb_ctx_kernel_launches": ([P, PI64], INT),
     "gb_ctx_device_status": ([P, ctypes.POINTER(ctypes.c_int32)], INT),
     "gb_ctx_set_precision": ([P, INT], INT),
+    "gb_ctx_profile_begin": ([P], INT),
+    "gb_ctx_profile_end": ([P, PD, PI64, PD, PD], INT),
     "gb_tensor_create": ([P, INT, INT, INT, PI64, ctypes.POINTER(P)], INT),
     "gb_tensor_free": ([P], INT),
     "gb_tensor_shape": ([P, ctypes.POINTER(INT), ctypes.POINTER(INT), ctypes.POINTER(INT), PI64], INT),

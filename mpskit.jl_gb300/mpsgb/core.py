@@ -35,6 +35,22 @@ class Context:
         L.check(L.lib().gb_ctx_kernel_launches(self.handle, ctypes.byref(v)))
         return v.value
 
+    def set_precision(self, precision):
+        code = {"fp64": L.GB_PREC_FP64, "bf16x3": L.GB_PREC_BF16X3}[precision]
+        L.check(L.lib().gb_ctx_set_precision(self.handle, code))
+
+    def profile_begin(self):
+        L.check(L.lib().gb_ctx_profile_begin(self.handle))
+
+    def profile_end(self):
+        """-> dict(gemm_ms, gemm_launches, gemm_flops, region_ms) of the traced region."""
+        ms, fl, rms = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        n = ctypes.c_int64()
+        L.check(L.lib().gb_ctx_profile_end(self.handle, ctypes.byref(ms), ctypes.byref(n),
+                                           ctypes.byref(fl), ctypes.byref(rms)))
+        return {"gemm_ms": ms.value, "gemm_launches": n.value, "gemm_flops": fl.value,
+                "region_ms": rms.value}
+
     def device_status(self):
         v = ctypes.c_int32()
         L.check(L.lib().gb_ctx_device_status(self.handle, ctypes.byref(v)))

@@ -112,9 +112,9 @@ class FiniteMPS:
         return self.C[self.center].dtype
 
     @classmethod
-    def from_tensors(cls, As, ctx=None, normalize=True):
+    def from_tensors(cls, As, ctx=None, normalize=True, center=0):
         """FiniteMPS(As; normalize): positive-QR sweep left to right on the device, then
-        LQ moves right to left to build the AR gauge."""
+        LQ moves right to left down to the centre bond `center`."""
         ctx = ctx or context()
         n = len(As)
         A = [DeviceTensor.from_numpy(ctx, L.GB_KIND_MPS, a) for a in As]
@@ -130,23 +130,23 @@ class FiniteMPS:
                 A[i + 1] = mul_front(R, A[i + 1])
         C[n] = R
         psi = cls(AL, [None] * n, C, n)
-        psi.right_canonicalize()
+        psi.right_canonicalize(center)
         return psi
 
     @classmethod
     def random(cls, L_, d, D, seed, dtype=np.complex128, ctx=None):
         return cls.from_tensors(random_tensors(L_, d, D, seed, dtype), ctx)
 
-    def right_canonicalize(self):
-        n = len(self)
+    def right_canonicalize(self, stop=0):
+        """Move the centre bond down to `stop` with positive LQ factorisations."""
         X = self.C[self.center]
-        for i in range(self.center - 1, -1, -1):
+        for i in range(self.center - 1, stop - 1, -1):
             A = mul_tail(self.AL[i], X)
             Lm, Q = right_orth(A)
             self.AR[i] = Q
             self.C[i] = Lm
             X = Lm
-        self.center = 0
+        self.center = stop
         return self
 
     def ac(self, i):
@@ -169,7 +169,13 @@ class FiniteMPS:
 
 
 class FiniteEnvironments:
-    def __init__(self, psi, H, ctx=None):
+    """Lazy GL/GR cache.  With `resident=False` only the most recently computed
+    environment of each side stays in HBM (older ones are released and recomputed from
+    the boundary when asked for again) -- the memory policy for large D x w, where all
+    L environments do not fit on one device."""
+
+    def __init__(self, psi, H, ctx=None, resident=True):
+        self.resident = resident
         self.ctx = ctx or psi.ctx
         self.H = H
         n = len(psi)
@@ -199,6 +205,9 @@ class FiniteEnvironments:
                                                      self.precision, out.handle))
                 self.GL[j + 1] = out
                 self.ldep[j] = A
+                if not self.resident and j >= 1:
+                    self.GL[j] = None
+                    self.ldep[j - 1] = None
         return self.GL[i]
 
     def rightenv(self, i, psi):
@@ -215,4 +224,7 @@ class FiniteEnvironments:
                                                       self.precision, out.handle))
                 self.GR[j - 1] = out
                 self.rdep[j] = A
+                if not self.resident and j <= n - 2:
+                    self.GR[j] = None
+                    self.rdep[j + 1] = None
         return self.GR[i]
