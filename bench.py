@@ -53,6 +53,13 @@ def parse():
     return ap.parse_args()
 
 
+_T0 = time.perf_counter()
+
+
+def log(msg):
+    print(f"[bench {time.perf_counter() - _T0:8.1f}s] {msg}", file=sys.stderr, flush=True)
+
+
 def peaks():
     try:
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -268,13 +275,19 @@ def run_ours(args):
     D = args.D
     t_setup = time.perf_counter()
     As = mpsgb.states.random_tensors(n, 2, D, args.seed + rank, np.float64)
+    log(f"random tensors ready (L={n}, D={D})")
     psi = mpsgb.FiniteMPS.from_tensors(As, ctx, center=pos + 1)
     del As
+    ctx.synchronize()
+    log("canonical MPS built on the device")
     envs = mpsgb.FiniteEnvironments(psi, H, resident=False)
     envs.precision = backend.code
     envs.leftenv(pos, psi)
+    ctx.synchronize()
+    log("left environments built")
     envs.rightenv(pos + 1, psi)
     ctx.synchronize()
+    log(f"right environments built; device status {ctx.device_status()}")
     t_setup = time.perf_counter() - t_setup
     alg = mpsgb.DMRG2(maxdim=D, cutoff=1e-10, backend=backend)
     state = {"eps_local": 1.0, "eps_trunc": 0.0, "decay": 0.0}
@@ -286,8 +299,10 @@ def run_ours(args):
         envs.rightenv(pos, psi)  # environment step of the next bond in the sweep
 
     warm = SweepStats()
-    for _ in range(args.warmup):
+    for i in range(args.warmup):
         step(warm)
+        ctx.synchronize()
+        log(f"warmup step {i}: matvecs {warm.matvecs} phases {warm.t}")
     ctx.synchronize()
     stats = SweepStats()
     launches0 = ctx.kernel_launches()
@@ -327,16 +342,20 @@ def run_ours(args):
     }
 
     # ---------------- end to end through the C ABI with host buffers
+    log(f"timed region done: {t_wall:.3f}s wall, {t_dev:.3f}s device; status {ctx.device_status()}")
     e2e = None
     if not args.no_e2e:
         e2e = run_e2e(args, ctx, psi, H, envs, alg, pos, state, pg)
+        log("e2e done")
 
     cpu = None
     if not args.no_cpu_baseline and rank == 0 and world == 1:
         GL = envs.leftenv(pos, psi).numpy()
         GR = envs.rightenv(pos + 1, psi).numpy()
         f1 = heff_ac2_flops(GL.shape, GR.shape, H.W[pos], H.W[pos + 1], False)
+        log("cpu baseline sample starting")
         t, threads = oracle_sample(GL, H.W[pos], H.W[pos + 1], GR, np.float64, 1)
+        log("cpu baseline sample done")
         cpu = {"value": f1 / t / 1e12, "unit": "TFLOP/s", "cores": threads, "kind": "port",
                "sample": f"one JordanAC2 matvec of the workload's central bond (D={D}) "
                          f"with the device-built environments, {t:.1f} s"}

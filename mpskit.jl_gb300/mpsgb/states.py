@@ -193,38 +193,44 @@ class FiniteEnvironments:
         return self.H.device(self.ctx, self.dtype)
 
     def leftenv(self, i, psi):
-        first = next((j for j in range(i) if psi.AL[j] is not self.ldep[j]), None)
-        if first is not None:
-            W = self._W()
-            for j in range(first, i):
-                A = psi.AL[j]
-                out = DeviceTensor(self.ctx, L.GB_KIND_GL, self.dtype,
-                                   (A.dims[2], W[j].dims[3], A.dims[2]))
-                L.check(L.lib().gb_env_transfer_left(self.ctx.handle, self.GL[j].handle,
-                                                     W[j].handle, A.handle, A.handle,
-                                                     self.precision, out.handle))
-                self.GL[j + 1] = out
-                self.ldep[j] = A
-                if not self.resident and j >= 1:
-                    self.GL[j] = None
-                    self.ldep[j - 1] = None
+        """GL of site i, recomputed from the nearest valid environment below when an AL
+        it depends on changed (by identity) or when it was released."""
+        first = next((j for j in range(i) if psi.AL[j] is not self.ldep[j]), i)
+        if first == i and self.GL[i] is not None:
+            return self.GL[i]
+        start = max(k for k in range(first + 1) if self.GL[k] is not None)
+        W = self._W()
+        for j in range(start, i):
+            A = psi.AL[j]
+            out = DeviceTensor(self.ctx, L.GB_KIND_GL, self.dtype,
+                               (A.dims[2], W[j].dims[3], A.dims[2]))
+            L.check(L.lib().gb_env_transfer_left(self.ctx.handle, self.GL[j].handle,
+                                                 W[j].handle, A.handle, A.handle,
+                                                 self.precision, out.handle))
+            self.GL[j + 1] = out
+            self.ldep[j] = A
+            if not self.resident and j >= 1:
+                self.GL[j] = None
         return self.GL[i]
 
     def rightenv(self, i, psi):
+        """GR of site i (everything right of i), recomputed from the nearest valid
+        environment above when an AR it depends on changed or was released."""
         n = len(psi)
-        first = next((j for j in range(n - 1, i, -1) if psi.AR[j] is not self.rdep[j]), None)
-        if first is not None:
-            W = self._W()
-            for j in range(first, i, -1):
-                A = psi.AR[j]
-                out = DeviceTensor(self.ctx, L.GB_KIND_GR, self.dtype,
-                                   (A.dims[0], W[j].dims[0], A.dims[0]))
-                L.check(L.lib().gb_env_transfer_right(self.ctx.handle, self.GR[j].handle,
-                                                      W[j].handle, A.handle, A.handle,
-                                                      self.precision, out.handle))
-                self.GR[j - 1] = out
-                self.rdep[j] = A
-                if not self.resident and j <= n - 2:
-                    self.GR[j] = None
-                    self.rdep[j + 1] = None
+        first = next((j for j in range(n - 1, i, -1) if psi.AR[j] is not self.rdep[j]), i)
+        if first == i and self.GR[i] is not None:
+            return self.GR[i]
+        start = min(k for k in range(first, n) if self.GR[k] is not None)
+        W = self._W()
+        for j in range(start, i, -1):
+            A = psi.AR[j]
+            out = DeviceTensor(self.ctx, L.GB_KIND_GR, self.dtype,
+                               (A.dims[0], W[j].dims[0], A.dims[0]))
+            L.check(L.lib().gb_env_transfer_right(self.ctx.handle, self.GR[j].handle,
+                                                  W[j].handle, A.handle, A.handle,
+                                                  self.precision, out.handle))
+            self.GR[j - 1] = out
+            self.rdep[j] = A
+            if not self.resident and j <= n - 2:
+                self.GR[j] = None
         return self.GR[i]

@@ -17,9 +17,17 @@ def declared():
     return sorted(set(re.findall(r"\b(gb_[a-z0-9_]+)\s*\(", txt)))
 
 
+def _stale():
+    if not os.path.exists(LIB):
+        return True
+    csrc = os.path.join(ROOT, "mpskit.jl_gb300", "csrc")
+    newest = max(os.path.getmtime(os.path.join(csrc, f)) for f in os.listdir(csrc))
+    return max(newest, os.path.getmtime(HEADER)) > os.path.getmtime(LIB)
+
+
 @pytest.fixture(scope="module")
 def lib():
-    if not os.path.exists(LIB):
+    if _stale():
         from mpsgb.build import build
         build()
     return ctypes.CDLL(LIB)
