@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--seed", type=int, default=1234 + 5)
+    ap.add_argument("--svd", default="gesvd", choices=["gesvd", "gesvdp", "gram"])
     return ap.parse_args()
 
 
@@ -182,6 +183,20 @@ def oracle_sample(GL, W1, W2, GR, dtype, reps):
     return min(times), threads
 
 
+def cpu_sample_D(W1, W2, D_target, budget_s=20.0):
+    """Largest D <= D_target (halving) whose oracle matvec is predicted to fit in the
+    budget, predicted from a D=256 probe with the D^3 cost law."""
+    rng = np.random.default_rng(1)
+    D0 = min(256, D_target)
+    GL = rng.standard_normal((D0, W1.shape[0], D0))
+    GR = rng.standard_normal((D0, W2.shape[3], D0))
+    t0, _ = oracle_sample(GL, W1, W2, GR, np.float64, 1)
+    D = D_target
+    while D > D0 and t0 * (D / D0) ** 3 > budget_s:
+        D //= 2
+    return D
+
+
 def run_reference(args):
     """--impl reference: the oracle port on the host cores, one matvec per step, at the
     workload's central-bond shapes with seeded synthetic environments."""
@@ -193,7 +208,7 @@ def run_reference(args):
     n = len(H)
     pos = n // 2 - 1
     W1, W2 = H.W[pos], H.W[pos + 1]
-    D = args.D
+    D = cpu_sample_D(W1, W2, args.D)
     rng = np.random.default_rng(args.seed)
     GL = rng.standard_normal((D, W1.shape[0], D))
     GR = rng.standard_normal((D, W2.shape[3], D))
@@ -214,9 +229,11 @@ def run_reference(args):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"J1-J2 {args.Ly}x{args.Lx} cylinder DMRG2 H_eff matvec at the "
                                f"central bond, D={D}, dense Float64", "D": D,
-                   "sample": "one AC2 H_eff application per step (oracle port, numpy)"},
+                   "sample": f"one AC2 H_eff application per step at D={D} (oracle port, numpy; "
+                             f"D halved from {args.D} until one matvec fits ~20 s)"},
         "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": threads, "kind": "port",
-                         "sample": "one JordanAC2 matvec of the workload per step"},
+                         "sample": f"one JordanAC2 matvec of the workload's central bond at D={D} "
+                                   "per step"},
         "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -268,6 +285,7 @@ def run_ours(args):
     ctx = mpsgb.context(local)
     prec = args.precision
     ctx.set_precision(prec)
+    ctx.set_svd_method(args.svd)
     backend = mpsgb.GB300Backend(prec, local)
     H = mpsgb.j1j2_cylinder(args.Lx, args.Ly, dtype=np.float64)
     n = len(H)
@@ -298,13 +316,13 @@ def run_ours(args):
         state.update(eps_local=el, eps_trunc=et, decay=dec, val=val)
         envs.rightenv(pos, psi)  # environment step of the next bond in the sweep
 
-    warm = SweepStats()
+    warm = SweepStats(sync=True)
     for i in range(args.warmup):
         step(warm)
         ctx.synchronize()
         log(f"warmup step {i}: matvecs {warm.matvecs} phases {warm.t}")
     ctx.synchronize()
-    stats = SweepStats()
+    stats = SweepStats(sync=True)
     launches0 = ctx.kernel_launches()
     barrier(pg)
     ctx.synchronize()
@@ -350,15 +368,17 @@ def run_ours(args):
 
     cpu = None
     if not args.no_cpu_baseline and rank == 0 and world == 1:
-        GL = envs.leftenv(pos, psi).numpy()
-        GR = envs.rightenv(pos + 1, psi).numpy()
+        Dc = cpu_sample_D(H.W[pos], H.W[pos + 1], D)
+        GL = envs.leftenv(pos, psi).numpy()[:Dc, :, :Dc]
+        GR = envs.rightenv(pos + 1, psi).numpy()[:Dc, :, :Dc]
         f1 = heff_ac2_flops(GL.shape, GR.shape, H.W[pos], H.W[pos + 1], False)
-        log("cpu baseline sample starting")
+        log(f"cpu baseline sample starting (D={Dc})")
         t, threads = oracle_sample(GL, H.W[pos], H.W[pos + 1], GR, np.float64, 1)
         log("cpu baseline sample done")
         cpu = {"value": f1 / t / 1e12, "unit": "TFLOP/s", "cores": threads, "kind": "port",
-               "sample": f"one JordanAC2 matvec of the workload's central bond (D={D}) "
-                         f"with the device-built environments, {t:.1f} s"}
+               "sample": f"one JordanAC2 matvec (oracle, numpy) at the workload's central bond "
+                         f"restricted to D={Dc} (the leading block of the device-built "
+                         f"environments), {t:.1f} s"}
 
     if rank == 0:
         line = {
@@ -372,6 +392,7 @@ def run_ours(args):
                             f"local update + env step at bond {pos}, D={D}, dense Float64",
                 "model": "J1=1, J2=0.5, snake order", "D": D, "L": n,
                 "mpo_width_at_bond": int(H.W[pos].shape[3]), "precision": prec,
+                "svd": args.svd,
                 "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (GL/GR/T1 >> 129 MB)",
             },
             "gpu_launches": launches,

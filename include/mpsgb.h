@@ -178,6 +178,14 @@ int gb_project_complement(gb_ctx* ctx, gb_tensor* Y, const gb_tensor* X);
 /* contract_mpo_expval-style scalar <x|y> after a heff apply is gb_tensor_dot. */
 
 /* ---------------------------------------------------------------- gauge */
+/* factorisation used by gb_svd_trunc */
+enum {
+  GB_SVD_GESVD = 0,   /* cuSOLVER QR-iteration SVD (default)                          */
+  GB_SVD_GESVDP = 1,  /* cuSOLVER polar-decomposition SVD                             */
+  GB_SVD_GRAM = 2     /* eigendecomposition of the Gram matrix (FP64 syevd); singular
+                         values below ~1e-7 of the largest lose relative accuracy     */
+};
+int gb_ctx_set_svd_method(gb_ctx* ctx, int method);
 /* Truncated SVD of a two-site tensor, gauge2! (src/states/orthoview.jl:401-420) with
  * truncrank(maxdim) & trunctol(atol): AL[l s1; k], S (diagonal, GB_KIND_BOND k x k),
  * AR[k s2; r].  Returns the discarded-weight norm eps.  Outputs are newly created. */

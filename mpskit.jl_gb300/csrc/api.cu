@@ -297,12 +297,96 @@ cusolverDnHandle_t solver(gb_ctx* ctx) {
       throw Error(GB_ERR_CUDA, std::string(#x) + " failed: " + std::to_string(_s)); \
   } while (0)
 
-// economy SVD of M (m x n, m >= n), col-major lda = m: U (m x n), S (n), VT (n x n)
+__global__ void scale_columns_kernel(int64_t m, int64_t n, double* __restrict__ U,
+                                     const double* __restrict__ S, int cx) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m * n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t j = e / m;
+    double sj = S[j];
+    double f = sj > 0 ? 1.0 / sj : 0.0;
+    if (cx) {
+      U[2 * e] *= f;
+      U[2 * e + 1] *= f;
+    } else {
+      U[e] *= f;
+    }
+  }
+}
+
+// sigma_j = sqrt(max(lambda_{n-1-j}, 0)): eigenvalues ascending -> singular values descending
+__global__ void sqrt_reverse_kernel(int64_t n, const double* __restrict__ lam,
+                                    double* __restrict__ S) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    double v = lam[n - 1 - j];
+    S[j] = v > 0 ? sqrt(v) : 0.0;
+  }
+}
+
+// economy SVD of M (m x n, m >= n), col-major lda = m: U (m x n), S (n, descending), VT (n x n)
 void svd_tall(gb_ctx* ctx, int dtype, int64_t m, int64_t n, void* A, void* U, double* S,
               void* VT) {
   cusolverDnHandle_t h = solver(ctx);
   cudaDataType t = is_cplx(dtype) ? CUDA_C_64F : CUDA_R_64F;
+  const size_t es = elem_size(dtype);
   size_t dws = 0, hws = 0;
+  if (ctx->svd_method == GB_SVD_GESVDP) {
+    // V (n x n) into the first part of a scratch slot, then VT = V^H
+    char* V = (char*)scratch(ctx, SLOT_TMP2, (size_t)n * n * es + 256);
+    CUSOLVER_CHECK(cusolverDnXgesvdp_bufferSize(h, (cusolverDnParams_t)ctx->solver_params,
+                                                CUSOLVER_EIG_MODE_VECTOR, 1, m, n, t, A, m,
+                                                CUDA_R_64F, S, t, U, m, t, V, n, t, &dws, &hws));
+    char* dw = (char*)scratch(ctx, SLOT_TMP, dws + 512);
+    int* dinfo = (int*)(dw + ((dws + 255) & ~size_t(255)));
+    std::vector<char> hw(hws + 1);
+    double herr = 0.0;
+    CUSOLVER_CHECK(cusolverDnXgesvdp(h, (cusolverDnParams_t)ctx->solver_params,
+                                     CUSOLVER_EIG_MODE_VECTOR, 1, m, n, t, A, m, CUDA_R_64F, S, t,
+                                     U, m, t, V, n, t, dw, dws, hw.data(), hws, dinfo, &herr));
+    count_launch(ctx);
+    int hinfo = 0;
+    GB_CHECK_CUDA(cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (hinfo != 0) throw Error(GB_ERR_CUDA, "gesvdp info = " + std::to_string(hinfo));
+    conj_transpose(ctx, dtype, n, n, V, n, VT, n);
+    return;
+  }
+  if (ctx->svd_method == GB_SVD_GRAM) {
+    // G = M^H M (n x n), eigenvectors ascending -> V columns reversed; U = M V / sigma
+    char* G = (char*)scratch(ctx, SLOT_TMP2, (size_t)n * n * es + 256);
+    gemm_fp64(ctx, dtype, 'C', 'N', n, n, m, cplx{1, 0}, A, m, 0, A, m, 0, cplx{0, 0}, G, n, 0, 1);
+    double* lam = S;  // eigenvalues first land in S, then become singular values in place
+    double* lamtmp = (double*)scratch(ctx, SLOT_KRYLOV_W, sizeof(double) * (n + 64) + 4096);
+    CUSOLVER_CHECK(cusolverDnXsyevd_bufferSize(h, (cusolverDnParams_t)ctx->solver_params,
+                                               CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n,
+                                               t, G, n, CUDA_R_64F, lamtmp, t, &dws, &hws));
+    char* dw = (char*)scratch(ctx, SLOT_TMP, dws + 512);
+    int* dinfo = (int*)(dw + ((dws + 255) & ~size_t(255)));
+    std::vector<char> hw(hws + 1);
+    CUSOLVER_CHECK(cusolverDnXsyevd(h, (cusolverDnParams_t)ctx->solver_params,
+                                    CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, t, G, n,
+                                    CUDA_R_64F, lamtmp, t, dw, dws, hw.data(), hws, dinfo));
+    count_launch(ctx);
+    sqrt_reverse_kernel<<<64, 256, 0, ctx->stream>>>(n, lamtmp, lam);
+    GB_CHECK_CUDA(cudaGetLastError());
+    count_launch(ctx);
+    // V[:, j] = G[:, n-1-j]  and VT = V^H
+    int64_t dims[2] = {n, n}, ins[2] = {1, -n}, outs[2] = {1, n};
+    const char* Glast = G + (size_t)(n - 1) * n * es;
+    permute(ctx, dtype, 2, dims, Glast, ins, U, outs);          // U <- V (n x n, staging)
+    conj_transpose(ctx, dtype, n, n, U, n, VT, n);              // VT = V^H
+    // U = M V / sigma  (V staged back from VT^H into G)
+    conj_transpose(ctx, dtype, n, n, VT, n, G, n);
+    gemm_fp64(ctx, dtype, 'N', 'N', m, n, n, cplx{1, 0}, A, m, 0, G, n, 0, cplx{0, 0}, U, m, 0, 1);
+    scale_columns_kernel<<<256, 256, 0, ctx->stream>>>(m, n, (double*)U, lam, is_cplx(dtype));
+    GB_CHECK_CUDA(cudaGetLastError());
+    count_launch(ctx);
+    int hinfo = 0;
+    GB_CHECK_CUDA(cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (hinfo != 0) throw Error(GB_ERR_CUDA, "syevd info = " + std::to_string(hinfo));
+    return;
+  }
   CUSOLVER_CHECK(cusolverDnXgesvd_bufferSize(h, (cusolverDnParams_t)ctx->solver_params, 'S', 'S',
                                              m, n, t, A, m, CUDA_R_64F, S, t, U, m, t, VT, n, t,
                                              &dws, &hws));
@@ -569,6 +653,15 @@ int gb_ctx_set_precision(gb_ctx* ctx, int precision) {
   GB_REQUIRE(ctx, "null context");
   GB_REQUIRE(precision == GB_PREC_FP64 || precision == GB_PREC_BF16X3, "unknown precision");
   ctx->aux_prec = precision;
+  API_END
+}
+
+int gb_ctx_set_svd_method(gb_ctx* ctx, int method) {
+  API_BEGIN
+  GB_REQUIRE(ctx, "null context");
+  GB_REQUIRE(method == GB_SVD_GESVD || method == GB_SVD_GESVDP || method == GB_SVD_GRAM,
+             "unknown SVD method");
+  ctx->svd_method = method;
   API_END
 }
 

@@ -75,6 +75,7 @@ struct gb_ctx {
   size_t h_pinned_elems = 0;
   int num_sms = 0;
   int aux_prec = GB_PREC_FP64;   // precision of auxiliary state contractions
+  int svd_method = 0;            // GB_SVD_* of gb_svd_trunc
   // tracing of the tensor-core GEMM launches
   bool profiling = false;
   std::vector<cudaEvent_t> prof_events;  // pairs (start, stop) per launch

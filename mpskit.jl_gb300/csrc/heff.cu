@@ -132,7 +132,9 @@ namespace gb {
 static void* dalloc(gb_heff* h, size_t bytes) {
   void* p = nullptr;
   if (bytes == 0) bytes = 16;
-  cudaError_t e = cudaMalloc(&p, bytes);
+  // stream-ordered pool: operator buffers are recycled across local updates without
+  // the device-wide synchronisation of cudaMalloc/cudaFree
+  cudaError_t e = cudaMallocAsync(&p, bytes, h->ctx->stream);
   if (e != cudaSuccess) throw Error(GB_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
   h->owned.push_back(p);
   return p;
@@ -164,7 +166,7 @@ static void prepack(gb_heff* h, Step& s) {
 static void free_steps(gb_heff* h) {
   for (auto& s : h->steps)
     if (!s.is_gemm) mix_free(s.mix);
-  for (void* p : h->owned) cudaFree(p);
+  for (void* p : h->owned) cudaFreeAsync(p, h->ctx->stream);
   h->owned.clear();
   h->steps.clear();
 }
@@ -1041,7 +1043,6 @@ gb_heff* heff_build(gb_ctx* ctx, int kind, const gb_tensor* GL, const gb_tensor*
 
 void heff_free(gb_heff* h) {
   if (!h) return;
-  cudaStreamSynchronize(h->ctx->stream);
   free_steps(h);
   delete h;
 }

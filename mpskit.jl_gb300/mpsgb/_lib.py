@@ -68,6 +68,7 @@ _SIGS = {
     "gb_ctx_device_status": ([P, ctypes.POINTER(ctypes.c_int32)], INT),
     "gb_ctx_set_precision": ([P, INT], INT),
     "gb_ctx_profile_begin": ([P], INT),
+    "gb_ctx_set_svd_method": ([P, INT], INT),
     "gb_ctx_profile_end": ([P, PD, PI64, PD, PD], INT),
     "gb_tensor_create": ([P, INT, INT, INT, PI64, ctypes.POINTER(P)], INT),
     "gb_tensor_free": ([P], INT),

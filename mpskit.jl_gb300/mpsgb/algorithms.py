@@ -72,7 +72,11 @@ def _decay(normres, eps_local, numops):
 
 
 class SweepStats:
-    def __init__(self):
+    """Counters of a sweep; with sync=True the phase timers synchronise the device so
+    the per-phase times are exact (at the cost of host/device overlap)."""
+
+    def __init__(self, sync=False):
+        self.sync = sync
         self.matvecs = 0
         self.updates = 0
         self.heff_flops = 0.0
@@ -81,9 +85,14 @@ class SweepStats:
 
 def dmrg2_local_update(pos, right, psi, H, alg, envs, eps_global, eps_trunc, decay_rate, stats):
     """local_update!(..., ::DMRG2) (dmrg.jl:211-244)."""
-    t0 = time.perf_counter()
+    def now():
+        if stats.sync:
+            psi.ctx.synchronize()
+        return time.perf_counter()
+
+    t0 = now()
     Heff = AC2_hamiltonian(pos, psi, H, envs, alg.backend)
-    t1 = time.perf_counter()
+    t1 = now()
     ac2 = ac2_from(psi.ac(pos), psi.AR[pos + 1]) if right else ac2_from(psi.AL[pos], psi.ac(pos + 1))
     y = Heff(ac2)
     y.normalize_()
@@ -91,13 +100,13 @@ def dmrg2_local_update(pos, right, psi, H, alg, envs, eps_global, eps_trunc, dec
     eps_local = y.norm()
     solver = alg.alg_eigsolve.adapt(decay_rate, eps_local, eps_global, eps_trunc)
     val, new, info = fixedpoint(Heff, ac2, "SR", solver)
-    t2 = time.perf_counter()
+    t2 = now()
     al, S, ar, eps_tr = svd_trunc(new, alg.maxdim, alg.cutoff, normalize=True)
     psi.AL[pos] = al
     psi.AR[pos + 1] = ar
     psi.C[pos + 1] = S
     psi.center = pos + 1
-    t3 = time.perf_counter()
+    t3 = now()
     stats.matvecs += info.numops + 1
     stats.updates += 1
     stats.heff_flops += Heff.flops * (info.numops + 1)

@@ -39,6 +39,11 @@ class Context:
         code = {"fp64": L.GB_PREC_FP64, "bf16x3": L.GB_PREC_BF16X3}[precision]
         L.check(L.lib().gb_ctx_set_precision(self.handle, code))
 
+    def set_svd_method(self, method):
+        """'gesvd' (default), 'gesvdp' or 'gram' for gb_svd_trunc."""
+        code = {"gesvd": 0, "gesvdp": 1, "gram": 2}[method]
+        L.check(L.lib().gb_ctx_set_svd_method(self.handle, code))
+
     def profile_begin(self):
         L.check(L.lib().gb_ctx_profile_begin(self.handle))
 

@@ -64,14 +64,32 @@ def mpo_c_apply(GL, GR, x):
 
 def mpo_ac_apply(GL, W, GR, x):
     """MPO_AC_Hamiltonian apply (mpo_derivatives.jl:100-107):
-    y[-1 -2;-3] = GL[-1 5;4] x[4 2;1] W[5 -2;2 3] GR[1 3;-3]."""
-    return np.einsum("aec,ctb,esth,bhf->asf", GL, x, W, GR, optimize=True)
+    y[-1 -2;-3] = GL[-1 5;4] x[4 2;1] W[5 -2;2 3] GR[1 3;-3],
+    evaluated in the prepared order of mpo_derivatives.jl:221-231, 266-274:
+    L = GL*W fused to (l s) <- (w' l' s'), then y = L (x R)."""
+    # GL_O[a, s, w', a', s'] = GL[a, w, a'] W[w, s, s', w']
+    GLO = np.tensordot(GL, W, axes=([1], [0]))          # (a, a', s, s', w')
+    GLO = GLO.transpose(0, 2, 4, 1, 3)                   # (a, s, w', a', s')
+    # xR[a', s', w', b] = x[a', s', b'] GR[b', w', b]
+    xR = np.tensordot(x, GR, axes=([2], [0]))            # (a', s', w', b)
+    return np.tensordot(GLO, xR, axes=([2, 3, 4], [2, 0, 1]))   # (a, s, b)
 
 
 def mpo_ac2_apply(GL, W1, W2, GR, x):
     """MPO_AC2_Hamiltonian apply (mpo_derivatives.jl:144-153):
-    y[-1 -2;-3 -4] = GL[-1 7;6] x[6 5;1 3] W1[7 -2;5 4] W2[4 -4;3 2] GR[1 2;-3]."""
-    return np.einsum("agf,fecq,gpem,mrqh,chb->apbr", GL, x, W1, W2, GR, optimize=True)
+    y[-1 -2;-3 -4] = GL[-1 7;6] x[6 5;1 3] W1[7 -2;5 4] W2[4 -4;3 2] GR[1 2;-3],
+    evaluated as the prepared operator (mpo_derivatives.jl:233-247, 276-288):
+    GL_O[l s1 m; l' s1'] = GL[l c; l'] W1[c s1; s1' m],
+    O_GR[r' s2'; r s2 m] = W2[m s2; s2' c'] GR[r' c'; r],
+    y = GL_O . x . O_GR as two GEMMs."""
+    GLO = np.tensordot(GL, W1, axes=([1], [0]))          # (l, l', s1, s1', m)
+    GLO = GLO.transpose(0, 2, 4, 1, 3)                   # (l, s1, m, l', s1')
+    OGR = np.tensordot(W2, GR, axes=([3], [1]))          # (m, s2, s2', r', r)
+    OGR = OGR.transpose(3, 2, 4, 1, 0)                   # (r', s2', r, s2, m)
+    # T[l, s1, m, r', s2'] = GL_O[(l s1 m), (l' s1')] x[(l' s1'), (r' s2')]
+    T = np.tensordot(GLO, x, axes=([3, 4], [0, 1]))      # (l, s1, m, r', s2')
+    # y[l, s1, r, s2] = T[(l s1), (m r' s2')] O_GR[(m r' s2'), (r s2)]
+    return np.tensordot(T, OGR, axes=([2, 3, 4], [4, 0, 1]))    # (l, s1, r, s2)
 
 
 # ------------------------------------------------------------------ Jordan AC2
@@ -93,19 +111,19 @@ class JordanAC2:
         # finished (:287)
         t["EE"] = None if W1.shape[0] == 1 else GL[:, -1, :].copy()
         # starting right (:290-295): IC[-1 -2;-3 -4] = C2[-1;-3 1] GR2[-4 1;-2]
-        t["IC"] = np.einsum("suk,vkb->sbuv", C2, GR2) if _nz(C2) else None
+        t["IC"] = np.einsum("suk,vkb->sbuv", C2, GR2, optimize=True) if _nz(C2) else None
         t["DE"] = D1.copy() if _nz(D1) else None
         t["ID"] = D2.copy() if _nz(D2) else None
         # CB[-1 -2;-3 -4] = C1[-1;-3 1] B2[1 -2;-4]  (:304-310)
-        t["CB"] = np.einsum("suk,ktv->stuv", C1, B2) if (_nz(C1) and _nz(B2)) else None
+        t["CB"] = np.einsum("suk,ktv->stuv", C1, B2, optimize=True) if (_nz(C1) and _nz(B2)) else None
         # CA[-1 -2 -3;-4 -5 -6] = C1[-1;-4 1] A2[1 -2;-5 2] GR2[-6 2;-3]  (:313-319)
-        t["CA"] = (np.einsum("suk,ktgm,qmr->strugq", C1, A2, GR2)
+        t["CA"] = (np.einsum("suk,ktgm,qmr->strugq", C1, A2, GR2, optimize=True)
                    if (_nz(C1) and _nz(A2)) else None)
         # AB[-1 -2 -3;-4 -5 -6] = GL2[-1 2;-4] A1[2 -2;-5 1] B2[1 -3;-6]  (:322-328)
-        t["AB"] = (np.einsum("acl,csuk,ktv->astluv", GL2, A1, B2)
+        t["AB"] = (np.einsum("acl,csuk,ktv->astluv", GL2, A1, B2, optimize=True)
                    if (_nz(A1) and _nz(B2)) else None)
         # BE[-1 -2;-3 -4] = GL2[-1 2;-3] B1[2 -2;-4]  (:331-336)
-        t["BE"] = np.einsum("acl,csu->aslu", GL2, B1) if _nz(B1) else None
+        t["BE"] = np.einsum("acl,csu->aslu", GL2, B1, optimize=True) if _nz(B1) else None
         ch = connected_channels(A1, A2)
         if ch is None:
             t["AA"] = None
@@ -128,57 +146,57 @@ class JordanAC2:
         # CB (:379-389)
         if CA is not None and t["CB"] is not None:
             D = CA.shape[2]
-            CA += np.einsum("stuv,rq->struvq", t["CB"], np.eye(D))
+            CA += np.einsum("stuv,rq->struvq", t["CB"], np.eye(D), optimize=True)
             t["CB"] = None
         elif AB is not None and t["CB"] is not None:
             D = AB.shape[0]
-            AB += np.einsum("stuv,al->astluv", t["CB"], np.eye(D))
+            AB += np.einsum("stuv,al->astluv", t["CB"], np.eye(D), optimize=True)
             t["CB"] = None
         # IC into CA (:392-398)
         if CA is not None and t["IC"] is not None:
             d = CA.shape[0]
-            CA += np.einsum("su,tbvq->stbuvq", np.eye(d), t["IC"])
+            CA += np.einsum("su,tbvq->stbuvq", np.eye(d), t["IC"], optimize=True)
             t["IC"] = None
         # BE into AB (:401-407)
         if AB is not None and t["BE"] is not None:
             d = AB.shape[2]
-            AB += np.einsum("aslu,tv->astluv", t["BE"], np.eye(d))
+            AB += np.einsum("aslu,tv->astluv", t["BE"], np.eye(d), optimize=True)
             t["BE"] = None
         # DE (:410-422)
         if t["BE"] is not None and t["DE"] is not None:
             D = t["BE"].shape[0]
-            t["BE"] += np.einsum("al,su->aslu", np.eye(D), t["DE"])
+            t["BE"] += np.einsum("al,su->aslu", np.eye(D), t["DE"], optimize=True)
             t["DE"] = None
         elif AB is not None and t["DE"] is not None:
             D, d = AB.shape[0], AB.shape[2]
-            AB += np.einsum("al,su,tv->astluv", np.eye(D), t["DE"], np.eye(d))
+            AB += np.einsum("al,su,tv->astluv", np.eye(D), t["DE"], np.eye(d), optimize=True)
             t["DE"] = None
         # ID (:425-436)
         if t["IC"] is not None and t["ID"] is not None:
             D = t["IC"].shape[1]
-            t["IC"] += np.einsum("su,bq->sbuq", t["ID"], np.eye(D))
+            t["IC"] += np.einsum("su,bq->sbuq", t["ID"], np.eye(D), optimize=True)
             t["ID"] = None
         elif CA is not None and t["ID"] is not None:
             d, D = CA.shape[0], CA.shape[2]
-            CA += np.einsum("su,tv,rq->struvq", np.eye(d), t["ID"], np.eye(D))
+            CA += np.einsum("su,tv,rq->struvq", np.eye(d), t["ID"], np.eye(D), optimize=True)
             t["ID"] = None
         # II (:439-449)
         if t["IC"] is not None and t["II"] is not None:
             d = t["IC"].shape[0]
-            t["IC"] += np.einsum("su,bq->sbuq", np.eye(d), t["II"])
+            t["IC"] += np.einsum("su,bq->sbuq", np.eye(d), t["II"], optimize=True)
             t["II"] = None
         elif CA is not None and t["II"] is not None:
             d = CA.shape[0]
-            CA += np.einsum("su,tv,rq->struvq", np.eye(d), np.eye(d), t["II"])
+            CA += np.einsum("su,tv,rq->struvq", np.eye(d), np.eye(d), t["II"], optimize=True)
             t["II"] = None
         # EE (:452-462)
         if t["BE"] is not None and t["EE"] is not None:
             d = t["BE"].shape[1]
-            t["BE"] += np.einsum("al,su->aslu", t["EE"], np.eye(d))
+            t["BE"] += np.einsum("al,su->aslu", t["EE"], np.eye(d), optimize=True)
             t["EE"] = None
         elif AB is not None and t["EE"] is not None:
             d = AB.shape[1]
-            AB += np.einsum("al,su,tv->astluv", t["EE"], np.eye(d), np.eye(d))
+            AB += np.einsum("al,su,tv->astluv", t["EE"], np.eye(d), np.eye(d), optimize=True)
             t["EE"] = None
 
     def terms(self):
@@ -195,23 +213,23 @@ class JordanAC2:
         else:
             y = np.zeros(x.shape, dtype=dt)
         if t["II"] is not None:   # y[-1 -2;-3 -4] += x[-1 -2;1 -4] II[-3;1]
-            y += np.einsum("apqr,bq->apbr", x, t["II"])
+            y += np.einsum("apqr,bq->apbr", x, t["II"], optimize=True)
         if t["IC"] is not None:   # y += x[-1 -2;1 2] IC[-4 -3;2 1]
-            y += np.einsum("apqu,rbuq->apbr", x, t["IC"])
+            y += np.einsum("apqu,rbuq->apbr", x, t["IC"], optimize=True)
         if t["ID"] is not None:   # y += x[-1 -2;-3 1] ID[-4;1]
-            y += np.einsum("apbu,ru->apbr", x, t["ID"])
+            y += np.einsum("apbu,ru->apbr", x, t["ID"], optimize=True)
         if t["CB"] is not None:   # y += x[-1 1;-3 2] CB[-2 -4;1 2]
-            y += np.einsum("aubv,pruv->apbr", x, t["CB"])
+            y += np.einsum("aubv,pruv->apbr", x, t["CB"], optimize=True)
         if t["CA"] is not None:   # y += x[-1 1;3 2] CA[-2 -4 -3;1 2 3]
-            y += np.einsum("auqv,prbuvq->apbr", x, t["CA"])
+            y += np.einsum("auqv,prbuvq->apbr", x, t["CA"], optimize=True)
         if t["AB"] is not None:   # y += x[1 2;-3 3] AB[-1 -2 -4;1 2 3]
-            y += np.einsum("lubv,aprluv->apbr", x, t["AB"])
+            y += np.einsum("lubv,aprluv->apbr", x, t["AB"], optimize=True)
         if t["BE"] is not None:   # y += x[1 2;-3 -4] BE[-1 -2;1 2]
-            y += np.einsum("lubr,aplu->apbr", x, t["BE"])
+            y += np.einsum("lubr,aplu->apbr", x, t["BE"], optimize=True)
         if t["DE"] is not None:   # y += x[-1 1;-3 -4] DE[-2;1]
-            y += np.einsum("aubr,pu->apbr", x, t["DE"])
+            y += np.einsum("aubr,pu->apbr", x, t["DE"], optimize=True)
         if t["EE"] is not None:   # y += x[1 -2;-3 -4] EE[-1;1]
-            y += np.einsum("lpbr,al->apbr", x, t["EE"])
+            y += np.einsum("lpbr,al->apbr", x, t["EE"], optimize=True)
         return y
 
 
@@ -233,9 +251,9 @@ class JordanAC:
         t["I"] = None if W.shape[3] == 1 else GR[:, 0, :].copy()
         t["E"] = None if W.shape[0] == 1 else GL[:, -1, :].copy()
         # starting[-1 -2;-3 -4] = WC[-1;-3 1] GR2[-4 1;-2]  (:77-82)
-        t["C"] = np.einsum("suk,vkb->sbuv", C, GR2) if _nz(C) else None
+        t["C"] = np.einsum("suk,vkb->sbuv", C, GR2, optimize=True) if _nz(C) else None
         # ending[-1 -2;-3 -4] = GL2[-1 1;-3] WB[1 -2;-4]  (:85-90)
-        t["B"] = np.einsum("acl,csu->aslu", GL2, B) if _nz(B) else None
+        t["B"] = np.einsum("acl,csu->aslu", GL2, B, optimize=True) if _nz(B) else None
         t["A"] = (GL2, A, GR2) if _nz(A) else None
         for k in ("D", "I", "E", "C", "B"):
             if t[k] is not None:
@@ -249,19 +267,19 @@ class JordanAC:
         if t["D"] is not None:
             if t["C"] is not None:      # C[-1 -2;-3 -4] += D[-1;-3] Id[-2;-4]
                 D = t["C"].shape[1]
-                t["C"] += np.einsum("su,bq->sbuq", t["D"], np.eye(D))
+                t["C"] += np.einsum("su,bq->sbuq", t["D"], np.eye(D), optimize=True)
                 t["D"] = None
             elif t["B"] is not None:    # B[-1 -2;-3 -4] += Id[-1;-3] D[-2;-4]
                 D = t["B"].shape[0]
-                t["B"] += np.einsum("al,su->aslu", np.eye(D), t["D"])
+                t["B"] += np.einsum("al,su->aslu", np.eye(D), t["D"], optimize=True)
                 t["D"] = None
         if t["I"] is not None and t["C"] is not None:   # C += Id[-1;-3] I[-4;-2]
             d = t["C"].shape[0]
-            t["C"] += np.einsum("su,qb->sbuq", np.eye(d), t["I"])
+            t["C"] += np.einsum("su,qb->sbuq", np.eye(d), t["I"], optimize=True)
             t["I"] = None
         if t["E"] is not None and t["B"] is not None:   # B += E[-1;-3] Id[-2;-4]
             d = t["B"].shape[1]
-            t["B"] += np.einsum("al,su->aslu", t["E"], np.eye(d))
+            t["B"] += np.einsum("al,su->aslu", t["E"], np.eye(d), optimize=True)
             t["E"] = None
 
     def terms(self):
@@ -276,15 +294,15 @@ class JordanAC:
         else:
             y = np.zeros(x.shape, dtype=dt)
         if t["D"] is not None:  # y[-1 -2;-3] += x[-1 1;-3] D[-2;1]
-            y += np.einsum("aub,su->asb", x, t["D"])
+            y += np.einsum("aub,su->asb", x, t["D"], optimize=True)
         if t["E"] is not None:  # y += E[-1;1] x[1 -2;-3]
-            y += np.einsum("al,lsb->asb", t["E"], x)
+            y += np.einsum("al,lsb->asb", t["E"], x, optimize=True)
         if t["I"] is not None:  # y += x[-1 -2;1] I[1;-3]
-            y += np.einsum("asq,qb->asb", x, t["I"])
+            y += np.einsum("asq,qb->asb", x, t["I"], optimize=True)
         if t["C"] is not None:  # y += x[-1 2;1] C[-2 -3;2 1]
-            y += np.einsum("auq,sbuq->asb", x, t["C"])
+            y += np.einsum("auq,sbuq->asb", x, t["C"], optimize=True)
         if t["B"] is not None:  # y += B[-1 -2;1 2] x[1 2;-3]
-            y += np.einsum("aslu,lub->asb", t["B"], x)
+            y += np.einsum("aslu,lub->asb", t["B"], x, optimize=True)
         return y
 
 
