@@ -323,6 +323,8 @@ __global__ void sqrt_reverse_kernel(int64_t n, const double* __restrict__ lam,
   }
 }
 
+void qr_pos(gb_ctx* ctx, int dtype, int64_t m, int64_t n, const void* M, void* Q, void* R);
+
 // economy SVD of M (m x n, m >= n), col-major lda = m: U (m x n), S (n, descending), VT (n x n)
 void svd_tall(gb_ctx* ctx, int dtype, int64_t m, int64_t n, void* A, void* U, double* S,
               void* VT) {
@@ -351,42 +353,6 @@ void svd_tall(gb_ctx* ctx, int dtype, int64_t m, int64_t n, void* A, void* U, do
     conj_transpose(ctx, dtype, n, n, V, n, VT, n);
     return;
   }
-  if (ctx->svd_method == GB_SVD_GRAM) {
-    // G = M^H M (n x n), eigenvectors ascending -> V columns reversed; U = M V / sigma
-    char* G = (char*)scratch(ctx, SLOT_TMP2, (size_t)n * n * es + 256);
-    gemm_fp64(ctx, dtype, 'C', 'N', n, n, m, cplx{1, 0}, A, m, 0, A, m, 0, cplx{0, 0}, G, n, 0, 1);
-    double* lam = S;  // eigenvalues first land in S, then become singular values in place
-    double* lamtmp = (double*)scratch(ctx, SLOT_KRYLOV_W, sizeof(double) * (n + 64) + 4096);
-    CUSOLVER_CHECK(cusolverDnXsyevd_bufferSize(h, (cusolverDnParams_t)ctx->solver_params,
-                                               CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n,
-                                               t, G, n, CUDA_R_64F, lamtmp, t, &dws, &hws));
-    char* dw = (char*)scratch(ctx, SLOT_TMP, dws + 512);
-    int* dinfo = (int*)(dw + ((dws + 255) & ~size_t(255)));
-    std::vector<char> hw(hws + 1);
-    CUSOLVER_CHECK(cusolverDnXsyevd(h, (cusolverDnParams_t)ctx->solver_params,
-                                    CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, t, G, n,
-                                    CUDA_R_64F, lamtmp, t, dw, dws, hw.data(), hws, dinfo));
-    count_launch(ctx);
-    sqrt_reverse_kernel<<<64, 256, 0, ctx->stream>>>(n, lamtmp, lam);
-    GB_CHECK_CUDA(cudaGetLastError());
-    count_launch(ctx);
-    // V[:, j] = G[:, n-1-j]  and VT = V^H
-    int64_t dims[2] = {n, n}, ins[2] = {1, -n}, outs[2] = {1, n};
-    const char* Glast = G + (size_t)(n - 1) * n * es;
-    permute(ctx, dtype, 2, dims, Glast, ins, U, outs);          // U <- V (n x n, staging)
-    conj_transpose(ctx, dtype, n, n, U, n, VT, n);              // VT = V^H
-    // U = M V / sigma  (V staged back from VT^H into G)
-    conj_transpose(ctx, dtype, n, n, VT, n, G, n);
-    gemm_fp64(ctx, dtype, 'N', 'N', m, n, n, cplx{1, 0}, A, m, 0, G, n, 0, cplx{0, 0}, U, m, 0, 1);
-    scale_columns_kernel<<<256, 256, 0, ctx->stream>>>(m, n, (double*)U, lam, is_cplx(dtype));
-    GB_CHECK_CUDA(cudaGetLastError());
-    count_launch(ctx);
-    int hinfo = 0;
-    GB_CHECK_CUDA(cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
-    if (hinfo != 0) throw Error(GB_ERR_CUDA, "syevd info = " + std::to_string(hinfo));
-    return;
-  }
   CUSOLVER_CHECK(cusolverDnXgesvd_bufferSize(h, (cusolverDnParams_t)ctx->solver_params, 'S', 'S',
                                              m, n, t, A, m, CUDA_R_64F, S, t, U, m, t, VT, n, t,
                                              &dws, &hws));
@@ -401,6 +367,27 @@ void svd_tall(gb_ctx* ctx, int dtype, int64_t m, int64_t n, void* A, void* U, do
   GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
   count_launch(ctx);
   if (hinfo != 0) throw Error(GB_ERR_CUDA, "gesvd info = " + std::to_string(hinfo));
+}
+
+__global__ void scale_rows_kernel(int64_t m, int64_t n, double* __restrict__ A, int64_t lda,
+                                  const double* __restrict__ S, int cx) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m * n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i = e % m, j = e / m;
+    double f = S[i];
+    if (cx) {
+      A[2 * (i + lda * j)] *= f;
+      A[2 * (i + lda * j) + 1] *= f;
+    } else {
+      A[i + lda * j] *= f;
+    }
+  }
+}
+
+__global__ void inv_kernel(int64_t n, const double* __restrict__ S, double* __restrict__ out) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n;
+       j += (int64_t)gridDim.x * blockDim.x)
+    out[j] = S[j] > 0 ? 1.0 / S[j] : 0.0;
 }
 
 // positive QR of M (m x n): Q (m x k), R (k x n), k = min(m, n)
@@ -453,6 +440,118 @@ void qr_pos(gb_ctx* ctx, int dtype, int64_t m, int64_t n, const void* M, void* Q
   GB_CHECK_CUDA(cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
   if (hinfo != 0) throw Error(GB_ERR_CUDA, "QR info = " + std::to_string(hinfo));
+}
+
+
+// Truncated factorisation M ~ AL C AR through the eigendecomposition of the Gram matrix of
+// the smaller side (FP64 syevd).  The Gram eigenvectors give one exactly isometric factor;
+// the other factor (M V / sigma, or sigma^-1 U^H M) is made exactly isometric by a positive
+// QR / LQ, whose triangular factor is absorbed into the bond matrix C = R Sigma (or Sigma L).
+// The state AL C AR equals U Sigma V^H of the truncated SVD; C is triangular, not diagonal.
+void svd_trunc_gram(gb_ctx* ctx, const gb_tensor* AC2, int64_t maxdim, double atol, int normalize,
+                    gb_tensor** AL, gb_tensor** S, gb_tensor** AR, double* eps) {
+  cusolverDnHandle_t h = solver(ctx);
+  const int dt = AC2->dtype;
+  const bool cx = is_cplx(dt);
+  cudaDataType t = cx ? CUDA_C_64F : CUDA_R_64F;
+  const size_t es = elem_size(dt);
+  const int64_t Dl = AC2->dims[0], d1 = AC2->dims[1], Dr = AC2->dims[2], d2 = AC2->dims[3];
+  const int64_t m = Dl * d1, n = d2 * Dr;
+  const bool tall = m >= n;
+  const int64_t g = tall ? n : m;
+  const void* M = AC2->data;
+  char* G = (char*)scratch(ctx, SLOT_GAUGE, (size_t)g * g * es + 256);
+  if (tall)
+    gemm_fp64(ctx, dt, 'C', 'N', n, n, m, cplx{1, 0}, M, m, 0, M, m, 0, cplx{0, 0}, G, n, 0, 1);
+  else
+    gemm_fp64(ctx, dt, 'N', 'C', m, m, n, cplx{1, 0}, M, m, 0, M, m, 0, cplx{0, 0}, G, m, 0, 1);
+  double* lam = (double*)scratch(ctx, SLOT_KRYLOV_W, sizeof(double) * (2 * g + 64) + 4096);
+  double* sig = lam + g + 32;
+  size_t dws = 0, hws = 0;
+  CUSOLVER_CHECK(cusolverDnXsyevd_bufferSize(h, (cusolverDnParams_t)ctx->solver_params,
+                                             CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, g, t,
+                                             G, g, CUDA_R_64F, lam, t, &dws, &hws));
+  char* dw = (char*)scratch(ctx, SLOT_TMP, dws + 512);
+  int* dinfo = (int*)(dw + ((dws + 255) & ~size_t(255)));
+  std::vector<char> hw(hws + 1);
+  CUSOLVER_CHECK(cusolverDnXsyevd(h, (cusolverDnParams_t)ctx->solver_params,
+                                  CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, g, t, G, g,
+                                  CUDA_R_64F, lam, t, dw, dws, hw.data(), hws, dinfo));
+  count_launch(ctx);
+  sqrt_reverse_kernel<<<64, 256, 0, ctx->stream>>>(g, lam, sig);
+  GB_CHECK_CUDA(cudaGetLastError());
+  count_launch(ctx);
+  std::vector<double> hs(g);
+  int hinfo = 0;
+  GB_CHECK_CUDA(cudaMemcpyAsync(hs.data(), sig, sizeof(double) * g, cudaMemcpyDeviceToHost,
+                                ctx->stream));
+  GB_CHECK_CUDA(cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (hinfo != 0) throw Error(GB_ERR_CUDA, "syevd info = " + std::to_string(hinfo));
+  int64_t keep = 0;
+  for (int64_t i = 0; i < g; ++i)
+    if (hs[i] > atol) ++keep;
+  if (maxdim > 0) keep = std::min(keep, maxdim);
+  keep = std::max<int64_t>(keep, 1);
+  double e2 = 0.0;
+  for (int64_t i = keep; i < g; ++i) e2 += hs[i] * hs[i];
+  if (eps) *eps = std::sqrt(e2);
+  GB_REQUIRE(hs[keep - 1] > 0.0, "svd_trunc (Gram): a kept singular value is zero");
+  // E = eigenvectors of the kept singular values, descending: E[:, j] = G[:, g-1-j]
+  char* E = (char*)scratch(ctx, SLOT_GAUGE2, (size_t)g * keep * es + 256);
+  {
+    int64_t dims[2] = {g, keep}, ins[2] = {1, -g}, outs[2] = {1, g};
+    permute(ctx, dt, 2, dims, G + (size_t)(g - 1) * g * es, ins, E, outs);
+  }
+  double* isig = lam;  // lam no longer needed
+  inv_kernel<<<32, 256, 0, ctx->stream>>>(keep, sig, isig);
+  GB_CHECK_CUDA(cudaGetLastError());
+  count_launch(ctx);
+  int64_t dl[3] = {Dl, d1, keep}, dr[3] = {keep, d2, Dr}, dc[2] = {keep, keep};
+  gb_tensor* al = new_tensor(ctx, GB_KIND_MPS, dt, 3, dl);
+  gb_tensor* ar = new_tensor(ctx, GB_KIND_MPS, dt, 3, dr);
+  gb_tensor* cc = new_tensor(ctx, GB_KIND_BOND, dt, 2, dc);
+  char* F = (char*)scratch(ctx, SLOT_T1, (size_t)std::max(m, n) * keep * es + 256);
+  if (tall) {
+    // U_k = M E / sigma (m x keep) -> positive QR: U_k = Q R; AL = Q, C = R Sigma
+    gemm_fp64(ctx, dt, 'N', 'N', m, keep, n, cplx{1, 0}, M, m, 0, E, n, 0, cplx{0, 0}, F, m, 0, 1);
+    scale_columns_kernel<<<256, 256, 0, ctx->stream>>>(m, keep, (double*)F, sig, cx);
+    GB_CHECK_CUDA(cudaGetLastError());
+    count_launch(ctx);
+    qr_pos(ctx, dt, m, keep, F, al->data, cc->data);
+    // C = R diag(sigma): scale column j by sigma_j  (scale_columns divides, so pass 1/sigma)
+    scale_columns_kernel<<<64, 256, 0, ctx->stream>>>(keep, keep, (double*)cc->data, isig, cx);
+    GB_CHECK_CUDA(cudaGetLastError());
+    count_launch(ctx);
+    conj_transpose(ctx, dt, n, keep, E, n, ar->data, keep);  // AR = E^H
+  } else {
+    // W = sigma^-1 E^H M (keep x n) -> LQ: W = L Q; AR = Q, C = Sigma L; AL = E
+    GB_CHECK_CUDA(cudaMemcpyAsync(al->data, E, (size_t)m * keep * es, cudaMemcpyDeviceToDevice,
+                                  ctx->stream));
+    gemm_fp64(ctx, dt, 'C', 'N', keep, n, m, cplx{1, 0}, E, m, 0, M, m, 0, cplx{0, 0}, F, keep, 0, 1);
+    scale_rows_kernel<<<256, 256, 0, ctx->stream>>>(keep, n, (double*)F, keep, isig, cx);
+    GB_CHECK_CUDA(cudaGetLastError());
+    count_launch(ctx);
+    // LQ of W through the positive QR of W^H (n x keep)
+    char* Wh = (char*)scratch(ctx, SLOT_T2, (size_t)n * keep * es + 256);
+    conj_transpose(ctx, dt, keep, n, F, keep, Wh, n);
+    char* Qp = (char*)scratch(ctx, SLOT_GAUGE2, (size_t)n * keep * es + 256);
+    char* Rp = (char*)scratch(ctx, SLOT_RED, (size_t)keep * keep * es + 4096);
+    qr_pos(ctx, dt, n, keep, Wh, Qp, Rp);
+    conj_transpose(ctx, dt, n, keep, Qp, n, ar->data, keep);  // AR = Qp^H
+    conj_transpose(ctx, dt, keep, keep, Rp, keep, cc->data, keep);  // L = Rp^H
+    scale_rows_kernel<<<64, 256, 0, ctx->stream>>>(keep, keep, (double*)cc->data, keep, sig, cx);
+    GB_CHECK_CUDA(cudaGetLastError());
+    count_launch(ctx);
+  }
+  if (normalize) {
+    double nc = nrm2(ctx, dt, keep * keep, cc->data);
+    scale(ctx, dt, keep * keep, cplx{1.0 / nc, 0}, cc->data);
+  }
+  GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  *AL = al;
+  *AR = ar;
+  *S = cc;
 }
 
 // env-transfer mix plans cached per (W, side, dims)
@@ -1097,6 +1196,10 @@ int gb_svd_trunc(gb_ctx* ctx, const gb_tensor* AC2, int64_t maxdim, double atol,
   GB_REQUIRE(AL && S && AR, "null output");
   GB_REQUIRE(AC2->kind == GB_KIND_AC2, "svd_trunc: input must be a two-site tensor");
   DevGuard g(ctx->device);
+  if (ctx->svd_method == GB_SVD_GRAM) {
+    svd_trunc_gram(ctx, AC2, maxdim, atol, normalize, AL, S, AR, eps);
+    return GB_OK;
+  }
   const int dt = AC2->dtype;
   const size_t es = elem_size(dt);
   const int64_t Dl = AC2->dims[0], d1 = AC2->dims[1], Dr = AC2->dims[2], d2 = AC2->dims[3];

@@ -82,3 +82,28 @@ def test_dmrg2_split_precision_energy(ctx):
         fenvs = mpsgb.FiniteEnvironments(psi, H)
         res[prec] = mpsgb.expectation_value(psi, H, fenvs, 0)
     assert abs(res["bf16x3"] - res["fp64"]) < 1e-7 * abs(res["fp64"]), res
+
+
+def test_dmrg2_split_precision_gram_svd_vs_oracle(ctx):
+    """The chosen form (bf16x3 contractions, Gram SVD, FP64 Lanczos) against the FP64
+    oracle on the same seeded problem: relative energy error below 1e-9."""
+    L_, D = 16, 24
+    terms = M.heisenberg_terms(L_, dtype=np.float64)
+    As = P.random_initial_tensors(L_, 2, D, 77, np.float64)
+    oH = M.finite_mpo_hamiltonian(L_, 2, terms, dtype=np.float64)
+    _, _, _, ohist = P.find_groundstate_dmrg2(P.finite_mps_from_tensors(As), oH,
+                                              P.DMRG2(maxdim=D, cutoff=1e-12), maxsweeps=8)
+    H = mpsgb.heisenberg_XXX(L_, dtype=np.float64)
+    ctx.set_svd_method("gram")
+    ctx.set_precision("bf16x3")
+    try:
+        psi = mpsgb.FiniteMPS.from_tensors(As, ctx)
+        alg = mpsgb.DMRG2(maxdim=D, cutoff=1e-12, backend=mpsgb.GB300Backend("bf16x3"))
+        psi, envs, eps, hist = mpsgb.find_groundstate(psi, H, alg, maxsweeps=8)
+        fenvs = mpsgb.FiniteEnvironments(psi, H)
+        e = mpsgb.expectation_value(psi, H, fenvs, 0)
+    finally:
+        ctx.set_svd_method("gesvd")
+        ctx.set_precision("fp64")
+    e_ref = ohist[-1][1]
+    assert abs(e - e_ref) / abs(e_ref) < 1e-9, (e, e_ref)

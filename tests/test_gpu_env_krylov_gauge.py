@@ -180,3 +180,35 @@ def test_left_right_orth(ctx, dt, shape):
     Lm, Q2 = P.lq_pos(a.reshape(Dl, d * Dr, order="F"))
     assert np.allclose(l.numpy(), Lm, atol=1e-12)
     assert np.allclose(q2.numpy().reshape(q2.dims[0], -1, order="F"), Q2, atol=1e-12)
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex128])
+@pytest.mark.parametrize("shape", [(6, 2, 5, 2), (3, 2, 9, 2), (8, 2, 8, 2)])
+@pytest.mark.parametrize("method", ["gesvdp", "gram"])
+def test_svd_trunc_methods(ctx, dt, shape, method):
+    """The alternative factorisations give the same truncated state with exactly
+    isometric AL and AR (the Gram method returns a triangular bond matrix)."""
+    rng = np.random.default_rng(8)
+    x = rng.standard_normal(shape)
+    if np.dtype(dt).kind == "c":
+        x = x + 1j * rng.standard_normal(shape)
+    x = x.astype(dt)
+    Dl, d1, Dr, d2 = shape
+    M_ = x.reshape(Dl * d1, Dr * d2, order="F")
+    ctx.set_svd_method(method)
+    try:
+        for maxdim in (4, 100):
+            al, C, ar, eps = mpsgb.svd_trunc(mpsgb.DeviceTensor.from_numpy(ctx, "ac2", x), maxdim,
+                                             0.0, normalize=False)
+            U, s, Vh, e = P.svd_trunc(M_, maxdim, 0.0)
+            k = s.size
+            assert abs(eps - e) < 1e-9
+            rec = np.einsum("asm,mn,ntb->asbt", al.numpy(), C.numpy(), ar.numpy())
+            ref = (U * s) @ Vh
+            assert np.allclose(rec.reshape(Dl * d1, Dr * d2, order="F"), ref, atol=1e-10)
+            A = al.numpy().reshape(Dl * d1, k, order="F")
+            B = ar.numpy().reshape(k, d2 * Dr, order="F")
+            assert np.allclose(A.conj().T @ A, np.eye(k), atol=1e-12)
+            assert np.allclose(B @ B.conj().T, np.eye(k), atol=1e-12)
+    finally:
+        ctx.set_svd_method("gesvd")
