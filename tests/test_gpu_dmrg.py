@@ -87,7 +87,7 @@ def test_dmrg2_split_precision_energy(ctx):
 def test_dmrg2_split_precision_gram_svd_vs_oracle(ctx):
     """The chosen form (bf16x3 contractions, Gram SVD, FP64 Lanczos) against the FP64
     oracle on the same seeded problem: relative energy error below 1e-9."""
-    L_, D = 16, 24
+    L_, D = 12, 64
     terms = M.heisenberg_terms(L_, dtype=np.float64)
     As = P.random_initial_tensors(L_, 2, D, 77, np.float64)
     oH = M.finite_mpo_hamiltonian(L_, 2, terms, dtype=np.float64)
