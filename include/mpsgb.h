@@ -197,6 +197,20 @@ int gb_left_orth(gb_ctx* ctx, const gb_tensor* AC, gb_tensor** AL, gb_tensor** C
 /* right_gauge(AC): AC = C * AR (src/states/orthoview.jl:334-338); outputs created. */
 int gb_right_orth(gb_ctx* ctx, const gb_tensor* AC, gb_tensor** C, gb_tensor** AR);
 
+/* ---------------------------------------------------------------- allocation-free variant */
+/* y = GL . x . GR (the bond operator of GB_HEFF_C) on caller-owned DEVICE buffers in the
+ * device layouts above (GL (a, a', w), GR (b', w, b), x and y (l, r)), launched on
+ * `stream` (a cudaStream_t; NULL = legacy default stream) of the current device.
+ * No counterpart in the reference: it exists for callers that cannot allocate device
+ * memory (an external Krylov solver whose arrays all come from its own pool, or launches
+ * recorded into a CUDA graph).  It allocates nothing: the intermediate x . GR
+ * (Dl*w*Dr elements) lives in a 64 MiB file-scope device array shared by all calls, so
+ * larger problems are rejected with GB_ERR_ARG and calls that overlap on the GPU race.
+ * The first call on a device looks up the array's address; make it before any stream
+ * capture. */
+int gb_c_apply_noalloc(const void* GL, const void* GR, const void* x, void* y, int64_t Dl,
+                       int64_t Dr, int64_t w, int dtype, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -365,6 +365,27 @@ void gemm_fp64(gb_ctx* ctx, int dtype, char opA, char opB, int64_t M, int64_t N,
   count_launch(ctx);
 }
 
+// Same SIMT GEMM launched on a caller-provided stream, without a context (no scratch,
+// no allocation, no launch counter); used by the allocation-free entry point.
+cudaError_t gemm_fp64_on_stream(cudaStream_t stream, int dtype, char opA, char opB, int64_t M,
+                                int64_t N, int64_t K, cplx alpha, const void* A, int64_t lda,
+                                const void* B, int64_t ldb, cplx beta, void* C, int64_t ldc) {
+  if (M == 0 || N == 0) return cudaSuccess;
+  if ((N + GBN - 1) / GBN > 65535 || K <= 0) return cudaErrorInvalidValue;
+  dim3 grid((unsigned)((M + GBM - 1) / GBM), (unsigned)((N + GBN - 1) / GBN), 1);
+  bool use_beta = (beta.re != 0.0 || beta.im != 0.0);
+  if (is_cplx(dtype)) {
+    gemm_simt_kernel<dcx><<<grid, 256, 0, stream>>>(
+        opA, opB, M, N, K, mk(alpha.re, alpha.im), (const dcx*)A, lda, 0, (const dcx*)B, ldb, 0,
+        mk(beta.re, beta.im), use_beta, (dcx*)C, ldc, 0);
+  } else {
+    gemm_simt_kernel<double><<<grid, 256, 0, stream>>>(opA, opB, M, N, K, alpha.re,
+                                                       (const double*)A, lda, 0, (const double*)B,
+                                                       ldb, 0, beta.re, use_beta, (double*)C, ldc, 0);
+  }
+  return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ BLAS-1
 void fill_zero(gb_ctx* ctx, void* p, size_t bytes) {
   if (bytes == 0) return;

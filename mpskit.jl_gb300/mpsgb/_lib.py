@@ -98,6 +98,7 @@ _SIGS = {
     "gb_svd_trunc": ([P, P, I64, D, INT, ctypes.POINTER(P), ctypes.POINTER(P), ctypes.POINTER(P), PD], INT),
     "gb_left_orth": ([P, P, ctypes.POINTER(P), ctypes.POINTER(P)], INT),
     "gb_right_orth": ([P, P, ctypes.POINTER(P), ctypes.POINTER(P)], INT),
+    "gb_c_apply_noalloc": ([P, P, P, P, I64, I64, I64, INT, P], INT),
 }
 
 
