@@ -344,7 +344,14 @@ def run_ours(args):
     launches0 = ctx.kernel_launches()
     barrier(pg)
     ctx.synchronize()
+    try:
+        import torch
+        nvtx = torch.cuda.nvtx
+    except Exception:
+        nvtx = None
     with ClockSampler(local) as clocks:
+        if nvtx:
+            nvtx.range_push("timed")
         ctx.profile_begin()
         t0 = time.perf_counter()
         for _ in range(args.steps):
@@ -352,6 +359,8 @@ def run_ours(args):
         ctx.synchronize()
         t_wall = time.perf_counter() - t0
         prof = ctx.profile_end()
+        if nvtx:
+            nvtx.range_pop()
     barrier(pg)
     launches = ctx.kernel_launches() - launches0
     t_dev = prof["region_ms"] / 1e3          # CUDA-event time of the region on the stream
