@@ -95,7 +95,7 @@ int gb_ctx_kernel_launches(gb_ctx* ctx, int64_t* out);
 /* device status word written by bounded waits inside kernels (0 = clean); cleared on read */
 int gb_ctx_device_status(gb_ctx* ctx, int32_t* out);
 /* arithmetic of the auxiliary state contractions of this context (gb_mps_ac2,
- * gb_mps_mul_front, gb_mps_mul_tail); GB_PREC_FP64 by default */
+ * gb_mps_mul_front, gb_mps_mul_tail, gb_project_complement); GB_PREC_FP64 by default */
 int gb_ctx_set_precision(gb_ctx* ctx, int precision);
 /* Tracing of the tensor-core GEMM (the dominant kernel): between profile_begin and
  * profile_end every split-precision GEMM launch is bracketed by CUDA events on the

@@ -1181,10 +1181,12 @@ int gb_project_complement(gb_ctx* ctx, gb_tensor* Y, const gb_tensor* X) {
   DevGuard g(ctx->device);
   const size_t es = elem_size(Y->dtype);
   void* T = scratch(ctx, SLOT_TMP, (size_t)k * cols * es);
-  gemm(ctx, GB_PREC_FP64, Y->dtype, 'C', 'N', k, cols, rows, 1.0, X->data, rows, 0, Y->data, rows,
-       0, 0.0, T, k, 0);
-  gemm(ctx, GB_PREC_FP64, Y->dtype, 'N', 'N', rows, cols, k, -1.0, X->data, rows, 0, T, k, 0, 1.0,
-       Y->data, rows, 0);
+  // the auxiliary precision of the context: in split mode Y is itself the output of a
+  // split-precision operator, so FP64 here would not add accuracy
+  gemm(ctx, ctx->aux_prec, Y->dtype, 'C', 'N', k, cols, rows, 1.0, X->data, rows, 0, Y->data,
+       rows, 0, 0.0, T, k, 0);
+  gemm(ctx, ctx->aux_prec, Y->dtype, 'N', 'N', rows, cols, k, -1.0, X->data, rows, 0, T, k, 0,
+       1.0, Y->data, rows, 0);
   API_END
 }
 

@@ -12,7 +12,8 @@ from .operators import (FiniteMPOHamiltonian, InfiniteMPOHamiltonian, MPOHamilto
                         heisenberg_XXX, j1j2_cylinder, transverse_field_ising, xxz)
 from .states import (FiniteEnvironments, FiniteMPS, ac2_from, left_orth, mul_front, mul_tail,
                      project_complement_, right_orth, svd_trunc)
-from .algorithms import DMRG, DMRG2, AdaptiveKrylov, expectation_value, find_groundstate
+from .algorithms import (DMRG, DMRG2, TDVP, AdaptiveKrylov, expectation_value,
+                         find_groundstate, timestep)
 
 __all__ = [
     "Context", "DeviceTensor", "context", "AC2_hamiltonian", "AC_hamiltonian", "C_hamiltonian",
@@ -21,4 +22,5 @@ __all__ = [
     "j1j2_cylinder", "transverse_field_ising", "xxz", "FiniteEnvironments", "FiniteMPS",
     "ac2_from", "left_orth", "mul_front", "mul_tail", "project_complement_", "right_orth",
     "svd_trunc", "DMRG", "DMRG2", "AdaptiveKrylov", "expectation_value", "find_groundstate",
+    "TDVP", "timestep",
 ]

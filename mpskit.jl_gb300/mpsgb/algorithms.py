@@ -11,7 +11,8 @@ import time
 import numpy as np
 
 from . import _lib as L
-from .derivatives import (AC2_hamiltonian, AC_hamiltonian, GB300Backend, Lanczos, fixedpoint)
+from .derivatives import (AC2_hamiltonian, AC_hamiltonian, C_hamiltonian, GB300Backend, Lanczos,
+                          exponentiate, fixedpoint)
 from .states import (FiniteEnvironments, ac2_from, left_orth, project_complement_, right_orth,
                      svd_trunc)
 
@@ -208,3 +209,53 @@ def _sweep_dmrg1(psi, H, alg, envs, maxsweeps, callback):
         if eps_global <= alg.tol:
             break
     return psi, envs, eps_global, hist
+
+
+# ---------------------------------------------------------------- TDVP
+
+class TDVP:
+    """Single-site TDVP (src/algorithms/timestep/tdvp.jl:30-60) with the KrylovKit
+    Lanczos exponentiator of Defaults.alg_expsolve (krylovdim 30, tol 1e-10)."""
+
+    def __init__(self, integrator=None, backend=None):
+        self.integrator = integrator or Lanczos(krylovdim=30, maxiter=200, tol=1e-10)
+        self.backend = backend or GB300Backend()
+
+
+def timestep(psi, H, t, dt, alg, envs=None, imaginary_evolution=False):
+    """timestep!(psi::FiniteMPS, H, t, dt, TDVP()) (tdvp.jl:135-211) on the device:
+    forward half-step sweep with backward bond evolutions, the right edge, the mirrored
+    backward sweep and the left edge.  Returns (psi, envs)."""
+    envs = envs or FiniteEnvironments(psi, H)
+    envs.precision = alg.backend.code
+    n = len(psi)
+
+    def integ(op, y, d):
+        tt = -d if imaginary_evolution else -1j * d
+        out, info = exponentiate(op, tt, y, alg.integrator)
+        return out
+
+    psi.ac_site = None
+    for i in range(n - 1):
+        AC = integ(AC_hamiltonian(i, psi, H, envs, alg.backend), psi.ac(i), dt / 2)
+        q, R = left_orth(AC)
+        psi.AL[i] = q
+        psi.C[i + 1] = R
+        psi.center = i + 1
+        psi.ac_site = None
+        Hc = C_hamiltonian(i, psi, H, envs, alg.backend)
+        psi.C[i + 1] = integ(Hc, psi.C[i + 1], -dt / 2)
+    psi.ac_tensor = integ(AC_hamiltonian(n - 1, psi, H, envs, alg.backend), psi.ac(n - 1), dt / 2)
+    psi.ac_site = n - 1
+    for i in range(n - 1, 0, -1):
+        AC = integ(AC_hamiltonian(i, psi, H, envs, alg.backend), psi.ac(i), dt / 2)
+        Lm, q = right_orth(AC)
+        psi.AR[i] = q
+        psi.C[i] = Lm
+        psi.center = i
+        psi.ac_site = None
+        Hc = C_hamiltonian(i - 1, psi, H, envs, alg.backend)
+        psi.C[i] = integ(Hc, psi.C[i], -dt / 2)
+    psi.ac_tensor = integ(AC_hamiltonian(0, psi, H, envs, alg.backend), psi.ac(0), dt / 2)
+    psi.ac_site = 0
+    return psi, envs

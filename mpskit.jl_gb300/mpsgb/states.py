@@ -150,6 +150,9 @@ class FiniteMPS:
         return self
 
     def ac(self, i):
+        """AC[i] for a centre bond at i or i+1, or the explicitly stored AC of site i."""
+        if getattr(self, "ac_site", None) == i:
+            return self.ac_tensor
         if self.center == i:
             return mul_front(self.C[i], self.AR[i])
         if self.center == i + 1:

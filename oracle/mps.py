@@ -75,7 +75,10 @@ class FiniteMPS:
         return FiniteMPS(cp(self.AL), cp(self.AR), cp(self.C), self.center)
 
     def ac(self, i):
-        """The centre-site tensor AC[i] for a centre bond at i or i+1."""
+        """The centre-site tensor AC[i] for a centre bond at i or i+1 (or an explicitly
+        stored AC, as `psi.AC[i] = ...` leaves it in the reference)."""
+        if getattr(self, "ac_site", None) == i:
+            return self.ac_tensor
         if self.center == i:
             return self.AC(i)
         if self.center == i + 1:
@@ -430,3 +433,45 @@ def find_groundstate_dmrg(psi, H, alg, envs=None, maxsweeps=None):
         if eps_global <= alg.tol:
             break
     return psi, envs, eps_global, hist
+
+
+# ---------------------------------------------------------------- TDVP (finite, 1-site)
+
+def tdvp_timestep(psi, H, envs, t, dt, krylovdim=30, tol=1e-10, imaginary=False):
+    """_timestep_finite! (tdvp.jl:147-211): left-to-right half-step sweep with backward bond
+    evolutions, the right edge, the mirrored right-to-left sweep and the left edge.
+    integrate(H, y, t, dt) = exp(-i dt H) y (exp(-dt H) in imaginary time), integrators.jl:44-53."""
+    from .krylov import lanczos_exponentiate
+
+    def integ(op, y, d):
+        tt = -d if imaginary else -1j * d
+        out, _ = lanczos_exponentiate(op, tt, y, krylovdim=krylovdim, tol=tol)
+        return out
+
+    L = len(psi)
+    psi.ac_site = None
+    for i in range(L - 1):
+        AC = integ(AC_hamiltonian(i, psi, H, envs), psi.ac(i), dt / 2)
+        Dl, d, Dr = AC.shape
+        Q, R = qr_pos(AC.reshape(Dl * d, Dr, order="F"))
+        psi.AL[i] = Q.reshape(Dl, d, -1, order="F")
+        psi.C[i + 1] = R
+        psi.center = i + 1
+        psi.ac_site = None
+        Hc = dv.CHam(envs.leftenv(i + 1, psi), envs.rightenv(i, psi))
+        psi.C[i + 1] = integ(Hc, psi.C[i + 1], -dt / 2)
+    psi.ac_tensor = integ(AC_hamiltonian(L - 1, psi, H, envs), psi.ac(L - 1), dt / 2)
+    psi.ac_site = L - 1
+    for i in range(L - 1, 0, -1):
+        AC = integ(AC_hamiltonian(i, psi, H, envs), psi.ac(i), dt / 2)
+        Dl, d, Dr = AC.shape
+        Lm, Q = lq_pos(AC.reshape(Dl, d * Dr, order="F"))
+        psi.AR[i] = Q.reshape(-1, d, Dr, order="F")
+        psi.C[i] = Lm
+        psi.center = i
+        psi.ac_site = None
+        Hc = dv.CHam(envs.leftenv(i, psi), envs.rightenv(i - 1, psi))
+        psi.C[i] = integ(Hc, psi.C[i], -dt / 2)
+    psi.ac_tensor = integ(AC_hamiltonian(0, psi, H, envs), psi.ac(0), dt / 2)
+    psi.ac_site = 0
+    return psi, envs
