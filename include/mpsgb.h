@@ -166,6 +166,12 @@ int gb_env_transfer_right(gb_ctx* ctx, const gb_tensor* GR, const gb_tensor* W,
 int gb_env_regularize(gb_ctx* ctx, gb_tensor* env, int64_t chan, const gb_tensor* lvec,
                       const gb_tensor* rvec);
 
+/* Copy the channel slice [src_c0, src_c0 + nchan) of one environment into the slice
+ * [dst_c0, dst_c0 + nchan) of another of the same kind and bond dimensions (the block
+ * assignment GL[site][i] = ... of src/environments/infinite_envs.jl:230-260) */
+int gb_env_channel_copy(gb_ctx* ctx, gb_tensor* dst, int64_t dst_c0, const gb_tensor* src,
+                        int64_t src_c0, int64_t nchan);
+
 /* ---------------------------------------------------------------- state manipulation */
 /* AC2 = A * _transpose_tail(B)   (src/states/finitemps.jl:376-385) */
 int gb_mps_ac2(gb_ctx* ctx, const gb_tensor* A, const gb_tensor* B, gb_tensor* AC2);
@@ -173,6 +179,8 @@ int gb_mps_ac2(gb_ctx* ctx, const gb_tensor* A, const gb_tensor* B, gb_tensor* A
 int gb_mps_mul_front(gb_ctx* ctx, const gb_tensor* C, const gb_tensor* A, gb_tensor* out);
 /* out = A * C   (mul_tail) */
 int gb_mps_mul_tail(gb_ctx* ctx, const gb_tensor* A, const gb_tensor* C, gb_tensor* out);
+/* out = C' (TensorKit `adjoint` of a bond tensor, used by regauge!, src/states/ortho.jl:178-184) */
+int gb_tensor_adjoint(gb_ctx* ctx, const gb_tensor* C, gb_tensor* out);
 /* Y <- (1 - X X') Y on the first two legs of Y (project_complement!, src/utility/utility.jl:22) */
 int gb_project_complement(gb_ctx* ctx, gb_tensor* Y, const gb_tensor* X);
 /* contract_mpo_expval-style scalar <x|y> after a heff apply is gb_tensor_dot. */

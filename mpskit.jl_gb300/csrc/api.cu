@@ -1120,6 +1120,51 @@ int gb_env_regularize(gb_ctx* ctx, gb_tensor* env, int64_t chan, const gb_tensor
   API_END
 }
 
+int gb_env_channel_copy(gb_ctx* ctx, gb_tensor* dst, int64_t dst_c0, const gb_tensor* src,
+                        int64_t src_c0, int64_t nchan) {
+  API_BEGIN
+  check_ctx(dst, ctx);
+  check_ctx(src, ctx);
+  GB_REQUIRE(dst->kind == src->kind && (dst->kind == GB_KIND_GL || dst->kind == GB_KIND_GR),
+             "channel_copy: both tensors must be environments of the same kind");
+  GB_REQUIRE(dst->dtype == src->dtype, "channel_copy: dtypes");
+  GB_REQUIRE(dst->dims[0] == src->dims[0] && dst->dims[2] == src->dims[2],
+             "channel_copy: bond dimensions differ");
+  GB_REQUIRE(nchan >= 0 && src_c0 >= 0 && dst_c0 >= 0 && src_c0 + nchan <= src->dims[1] &&
+                 dst_c0 + nchan <= dst->dims[1],
+             "channel_copy: channel range out of bounds");
+  if (nchan == 0) return GB_OK;
+  DevGuard g(ctx->device);
+  const size_t es = elem_size(dst->dtype);
+  const int64_t D0 = dst->dims[0], D2 = dst->dims[2];
+  if (dst->kind == GB_KIND_GL) {  // device (a, a', w): a channel slice is contiguous
+    GB_CHECK_CUDA(cudaMemcpyAsync((char*)dst->data + (size_t)D0 * D2 * dst_c0 * es,
+                                  (const char*)src->data + (size_t)D0 * D2 * src_c0 * es,
+                                  (size_t)D0 * D2 * nchan * es, cudaMemcpyDeviceToDevice,
+                                  ctx->stream));
+  } else {  // device (b', w, b): D0*nchan contiguous elements per b
+    GB_CHECK_CUDA(cudaMemcpy2DAsync((char*)dst->data + (size_t)D0 * dst_c0 * es,
+                                    (size_t)D0 * dst->dims[1] * es,
+                                    (const char*)src->data + (size_t)D0 * src_c0 * es,
+                                    (size_t)D0 * src->dims[1] * es, (size_t)D0 * nchan * es, D2,
+                                    cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  API_END
+}
+
+int gb_tensor_adjoint(gb_ctx* ctx, const gb_tensor* C, gb_tensor* out) {
+  API_BEGIN
+  check_ctx(C, ctx);
+  check_ctx(out, ctx);
+  GB_REQUIRE(C->kind == GB_KIND_BOND && out->kind == GB_KIND_BOND, "adjoint: bond tensors only");
+  GB_REQUIRE(C->dtype == out->dtype, "adjoint: dtypes");
+  GB_REQUIRE(out->dims[0] == C->dims[1] && out->dims[1] == C->dims[0], "adjoint: output shape");
+  DevGuard g(ctx->device);
+  conj_transpose(ctx, C->dtype, C->dims[0], C->dims[1], C->data, C->dims[0], out->data,
+                 C->dims[1]);
+  API_END
+}
+
 // ---------------------------------------------------------------- state manipulation
 int gb_mps_ac2(gb_ctx* ctx, const gb_tensor* A, const gb_tensor* B, gb_tensor* AC2) {
   API_BEGIN

@@ -14,6 +14,7 @@ from .states import (FiniteEnvironments, FiniteMPS, ac2_from, left_orth, mul_fro
                      project_complement_, right_orth, svd_trunc)
 from .algorithms import (DMRG, DMRG2, TDVP, AdaptiveKrylov, expectation_value,
                          find_groundstate, timestep)
+from .infinite import (VUMPS, InfiniteEnvironments, InfiniteMPS, find_groundstate_vumps)
 
 __all__ = [
     "Context", "DeviceTensor", "context", "AC2_hamiltonian", "AC_hamiltonian", "C_hamiltonian",
@@ -22,5 +23,5 @@ __all__ = [
     "j1j2_cylinder", "transverse_field_ising", "xxz", "FiniteEnvironments", "FiniteMPS",
     "ac2_from", "left_orth", "mul_front", "mul_tail", "project_complement_", "right_orth",
     "svd_trunc", "DMRG", "DMRG2", "AdaptiveKrylov", "expectation_value", "find_groundstate",
-    "TDVP", "timestep",
+    "TDVP", "timestep", "VUMPS", "InfiniteEnvironments", "InfiniteMPS", "find_groundstate_vumps",
 ]

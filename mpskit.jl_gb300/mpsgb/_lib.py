@@ -91,6 +91,8 @@ _SIGS = {
     "gb_env_transfer_left": ([P, P, P, P, P, INT, P], INT),
     "gb_env_transfer_right": ([P, P, P, P, P, INT, P], INT),
     "gb_env_regularize": ([P, P, I64, P, P], INT),
+    "gb_env_channel_copy": ([P, P, I64, P, I64, I64], INT),
+    "gb_tensor_adjoint": ([P, P, P], INT),
     "gb_mps_ac2": ([P, P, P, P], INT),
     "gb_mps_mul_front": ([P, P, P, P], INT),
     "gb_mps_mul_tail": ([P, P, P, P], INT),

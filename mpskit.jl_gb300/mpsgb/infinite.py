@@ -1,0 +1,369 @@
+"""VUMPS on a one-site unit cell, with InfiniteMPOHamiltonian environments, on the device.
+
+  InfiniteMPS gauge fixing (uniform_leftorth!/rightorth!) -- src/states/ortho.jl:210-340
+  regauge!(AC, C)                                          -- src/states/ortho.jl:178-184
+  InfiniteEnvironments for an InfiniteMPOHamiltonian      -- src/environments/infinite_envs.jl:177-346
+  VUMPS                                                    -- src/algorithms/groundstate/vumps.jl:62-192
+
+The environments are solved level by level (channel block by channel block of the MPO,
+which is upper triangular): the inhomogeneous term is a sum of transfers of the lower
+levels, and each level solves x - x T_ii = b by GMRES (regularised on identity levels).
+The GMRES loop runs on the host over device vectors; every transfer, dot and update is a
+libmpsgb call.  The Arnoldi acceleration of the gauge iterations (ortho.jl, after 10
+iterations) is not used: the QR/LQ iterations converge to the same fixed point.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib as L
+from .core import DeviceTensor, context
+from .derivatives import GB300Backend, Lanczos, fixedpoint, DerivativeOperator
+from .states import left_orth, mul_front, mul_tail, project_complement_, right_orth
+
+
+def _dyn_tol(eps, it, factor, tmin=1e-14, tmax=1e-4):
+    """DynamicTol with the Defaults bounds (src/utility/dynamictols.jl:86-89)."""
+    return min(max(factor * eps / np.sqrt(max(it, 1)), tmin), tmax)
+
+
+def _as_mps(C):
+    """A bond tensor C[l; r] viewed as an MPS tensor with a trivial physical leg."""
+    t = DeviceTensor(C.ctx, L.GB_KIND_MPS, C.dtype, (C.dims[0], 1, C.dims[1]))
+    L.check(L.lib().gb_tensor_copy(t.handle, C.handle))
+    return t
+
+
+def _as_bond(A):
+    t = DeviceTensor(A.ctx, L.GB_KIND_BOND, A.dtype, (A.dims[0], A.dims[2]))
+    L.check(L.lib().gb_tensor_copy(t.handle, A.handle))
+    return t
+
+
+def adjoint(C):
+    out = DeviceTensor(C.ctx, L.GB_KIND_BOND, C.dtype, (C.dims[1], C.dims[0]))
+    L.check(L.lib().gb_tensor_adjoint(C.ctx.handle, C.handle, out.handle))
+    return out
+
+
+def _bond_mul(A, B):
+    """A B for bond tensors."""
+    return _as_bond(mul_tail(_as_mps(A), B))
+
+
+def _diff_norm(a, b):
+    t = a.copy()
+    t.axpy_(-1.0, b)
+    return t.norm()
+
+
+class InfiniteMPS:
+    """One-site unit cell on the device: AL C = C AR = AC."""
+
+    def __init__(self, AL, AR, C):
+        self.AL, self.AR, self.C = AL, AR, C
+
+    @property
+    def ctx(self):
+        return self.C.ctx
+
+    @property
+    def dtype(self):
+        return self.C.dtype
+
+    @property
+    def AC(self):
+        return mul_tail(self.AL, self.C)
+
+    @classmethod
+    def from_tensor(cls, A, ctx=None, tol=1e-14, maxiter=200):
+        """InfiniteMPS(A): left then right uniform gauge fixing (order :LR)."""
+        ctx = ctx or context()
+        A = DeviceTensor.from_numpy(ctx, L.GB_KIND_MPS, A)
+        D = A.dims[0]
+        C0 = DeviceTensor.from_numpy(ctx, L.GB_KIND_BOND, np.eye(D, dtype=A.dtype))
+        AL, C = uniform_leftorth(A, C0, tol, maxiter)
+        AR, C = uniform_rightorth(AL, C, tol, maxiter)
+        return cls(AL, AR, C)
+
+    def to_numpy(self):
+        return self.AL.numpy(), self.AR.numpy(), self.C.numpy()
+
+
+def uniform_leftorth(A, C0, tol=1e-14, maxiter=200):
+    C = C0.copy().normalize_()
+    AL = None
+    for _ in range(maxiter):
+        AL, R = left_orth(mul_front(C, A))
+        R.normalize_()
+        err = _diff_norm(C, R)
+        C = R
+        if err < tol:
+            break
+    return AL, C
+
+
+def uniform_rightorth(A, C0, tol=1e-14, maxiter=200):
+    C = C0.copy().normalize_()
+    AR = None
+    for _ in range(maxiter):
+        Lm, AR = right_orth(mul_tail(A, C))
+        Lm.normalize_()
+        err = _diff_norm(C, Lm)
+        C = Lm
+        if err < tol:
+            break
+    return AR, C
+
+
+def regauge(AC, C):
+    """AL = Q_AC Q_C' from positive QRs of AC and C."""
+    qac, _ = left_orth(AC)
+    qc, _ = left_orth(_as_mps(C))
+    return mul_tail(qac, adjoint(_as_bond(qc)))
+
+
+# ---------------------------------------------------------------- environments
+
+def _levels(chans):
+    off = np.concatenate([[0], np.cumsum(chans)]).astype(int)
+    return [(int(off[i]), int(chans[i])) for i in range(len(chans))]
+
+
+def _is_identity_block(B):
+    n, d = B.shape[0], B.shape[1]
+    ref = np.einsum("ab,st->astb", np.eye(n), np.eye(d))
+    return B.shape == ref.shape and np.array_equal(B, ref)
+
+
+class _Blocks:
+    """Device copies of the nonzero MPO channel blocks W[level_j, :, :, level_i]."""
+
+    def __init__(self, ctx, W, chans, dtype):
+        self.lv = _levels(chans)
+        self.W = W
+        self.blk = {}
+        for j, (oj, nj) in enumerate(self.lv):
+            for i, (oi, ni) in enumerate(self.lv):
+                b = W[oj:oj + nj, :, :, oi:oi + ni]
+                if np.any(b != 0):
+                    self.blk[(j, i)] = DeviceTensor.from_numpy(ctx, L.GB_KIND_MPO,
+                                                               np.ascontiguousarray(b), dtype)
+
+    def diag_kind(self, i):
+        oi, ni = self.lv[i]
+        d = self.W[oi:oi + ni, :, :, oi:oi + ni]
+        if i == 0 or i == len(self.lv) - 1 or _is_identity_block(d):
+            return "identity"
+        return "diag" if (i, i) in self.blk else "empty"
+
+
+def _transfer(side, ctx, env, Wb, A, prec):
+    D = A.dims[2] if side == "L" else A.dims[0]
+    out_w = Wb.dims[3] if side == "L" else Wb.dims[0]
+    kind = L.GB_KIND_GL if side == "L" else L.GB_KIND_GR
+    out = DeviceTensor(ctx, kind, env.dtype, (D, out_w, D))
+    f = L.lib().gb_env_transfer_left if side == "L" else L.lib().gb_env_transfer_right
+    L.check(f(ctx.handle, env.handle, Wb.handle, A.handle, A.handle, prec, out.handle))
+    return out
+
+
+def _regularize(ctx, x, lvec, rvec):
+    """x -= tr(lvec x) rvec on every channel of the level block."""
+    for c in range(x.dims[1]):
+        L.check(L.lib().gb_env_regularize(ctx.handle, x.handle, c, lvec.handle, rvec.handle))
+    return x
+
+
+def gmres(op, b, x0, krylovdim=30, maxiter=200, tol=1e-12):
+    """Restarted GMRES for x - op(x) = b (KrylovKit linsolve(op, b, x0, GMRES, 1, -1));
+    the Krylov vectors live on the device, the Hessenberg least squares on the host.
+    Returns (x, converged, normres)."""
+    x = x0.copy()
+    res = np.inf
+    for _ in range(maxiter):
+        r = b.copy()
+        r.axpy_(-1.0, x)
+        r.axpy_(1.0, op(x))
+        beta = r.norm()
+        if beta <= tol:
+            return x, True, beta
+        V = [r.scale_(1.0 / beta)]
+        Hm = np.zeros((krylovdim + 1, krylovdim), dtype=np.complex128)
+        y = None
+        k = 0
+        for j in range(krylovdim):
+            w = V[j].copy()
+            w.axpy_(-1.0, op(V[j]))
+            for _pass in range(2):
+                for i in range(j + 1):
+                    h = V[i].dot(w)
+                    Hm[i, j] += h
+                    w.axpy_(-h, V[i])
+            hn = w.norm()
+            Hm[j + 1, j] = hn
+            k = j + 1
+            e = np.zeros(k + 1, dtype=np.complex128)
+            e[0] = beta
+            y = np.linalg.lstsq(Hm[:k + 1, :k], e, rcond=None)[0]
+            res = float(np.linalg.norm(e - Hm[:k + 1, :k] @ y))
+            if res <= tol or hn < 1e-300:
+                break
+            V.append(w.scale_(1.0 / hn))
+        for i in range(k):
+            coef = y[i] if x.dtype.kind == "c" else y[i].real
+            x.axpy_(coef, V[i])
+        if res <= tol:
+            return x, True, res
+    return x, False, res
+
+
+class InfiniteEnvironments:
+    """Fixed-point GL/GR of a one-site-cell InfiniteMPOHamiltonian on the device."""
+
+    def __init__(self, psi, H, precision=L.GB_PREC_FP64):
+        self.ctx = psi.ctx
+        self.H = H
+        self.dtype = np.result_type(psi.dtype, H.dtype)
+        self.precision = precision
+        self.blocks = _Blocks(self.ctx, H.W[0], H.chans[0], self.dtype)
+        self.GLl = None  # per-level blocks (previous solutions are GMRES starting points)
+        self.GRl = None
+        self.GL = self.GR = None
+
+    def recalculate(self, psi, tol=1e-12, krylovdim=30, maxiter=200):
+        ctx, B, prec = self.ctx, self.blocks, self.precision
+        lv = B.lv
+        n = len(lv)
+        D = psi.AL.dims[0]
+        kd = min(D * D, krylovdim)
+        eye = DeviceTensor.from_numpy(ctx, L.GB_KIND_BOND, np.eye(D, dtype=self.dtype))
+        zero = lambda ni, kind: DeviceTensor.from_numpy(ctx, kind, np.zeros((D, ni, D), self.dtype))
+        one = lambda kind: DeviceTensor.from_numpy(ctx, kind, np.eye(D, dtype=self.dtype)[:, None, :])
+        r_LL = _bond_mul(psi.C, adjoint(psi.C))
+        l_RR = _bond_mul(adjoint(psi.C), psi.C)
+        prevL = self.GLl or [None] * n
+        prevR = self.GRl or [None] * n
+        # left levels, ascending
+        GL = [one(L.GB_KIND_GL)] + [None] * (n - 1)
+        for i in range(1, n):
+            b = zero(lv[i][1], L.GB_KIND_GL)
+            for j in range(i):
+                if (j, i) in B.blk:
+                    b.axpy_(1.0, _transfer("L", ctx, GL[j], B.blk[(j, i)], psi.AL, prec))
+            x0 = prevL[i] if prevL[i] is not None else zero(lv[i][1], L.GB_KIND_GL)
+            kind = B.diag_kind(i)
+            if kind == "identity":
+                Wd = B.blk[(i, i)]
+                op = lambda v: _regularize(ctx, _transfer("L", ctx, v, Wd, psi.AL, prec), r_LL, eye)
+                x, conv, nr = gmres(op, b, x0, kd, maxiter, tol)
+                _regularize(ctx, x, r_LL, eye)
+            elif kind == "diag":
+                Wd = B.blk[(i, i)]
+                op = lambda v: _transfer("L", ctx, v, Wd, psi.AL, prec)
+                x, conv, nr = gmres(op, b, x0, kd, maxiter, tol)
+            else:
+                x = b
+            GL[i] = x
+        # right levels, descending
+        GR = [None] * (n - 1) + [one(L.GB_KIND_GR)]
+        for i in range(n - 2, -1, -1):
+            b = zero(lv[i][1], L.GB_KIND_GR)
+            for j in range(i + 1, n):
+                if (i, j) in B.blk:
+                    b.axpy_(1.0, _transfer("R", ctx, GR[j], B.blk[(i, j)], psi.AR, prec))
+            x0 = prevR[i] if prevR[i] is not None else zero(lv[i][1], L.GB_KIND_GR)
+            kind = B.diag_kind(i)
+            if kind == "identity":
+                Wd = B.blk[(i, i)]
+                op = lambda v: _regularize(ctx, _transfer("R", ctx, v, Wd, psi.AR, prec), l_RR, eye)
+                x, conv, nr = gmres(op, b, x0, kd, maxiter, tol)
+                _regularize(ctx, x, l_RR, eye)
+            elif kind == "diag":
+                Wd = B.blk[(i, i)]
+                op = lambda v: _transfer("R", ctx, v, Wd, psi.AR, prec)
+                x, conv, nr = gmres(op, b, x0, kd, maxiter, tol)
+            else:
+                x = b
+            GR[i] = x
+        self.GLl, self.GRl = GL, GR
+        w = sum(ni for _, ni in lv)
+        self.GL = DeviceTensor(ctx, L.GB_KIND_GL, self.dtype, (D, w, D))
+        self.GR = DeviceTensor(ctx, L.GB_KIND_GR, self.dtype, (D, w, D))
+        for i, (oi, ni) in enumerate(lv):
+            L.check(L.lib().gb_env_channel_copy(ctx.handle, self.GL.handle, oi, GL[i].handle, 0, ni))
+            L.check(L.lib().gb_env_channel_copy(ctx.handle, self.GR.handle, oi, GR[i].handle, 0, ni))
+        return self
+
+
+def _heff_ac(envs, backend):
+    W = envs.H.device(envs.ctx, envs.dtype)[0]
+    return DerivativeOperator(envs.ctx, L.GB_HEFF_AC, envs.GL, W, None, envs.GR, backend)
+
+
+def _heff_c(envs, backend):
+    return DerivativeOperator(envs.ctx, L.GB_HEFF_C, envs.GL, None, None, envs.GR, backend)
+
+
+def energy_density(psi, envs, backend=None):
+    """expectation_value(::InfiniteMPS, ::InfiniteMPOHamiltonian) (expval.jl:150-161):
+    <AC| GL . W[:, :, :, end] . GR[end] |AC>."""
+    ctx = envs.ctx
+    W = envs.H.W[0]
+    wl = W.shape[0]
+    Wl = DeviceTensor.from_numpy(ctx, L.GB_KIND_MPO, np.ascontiguousarray(W[:, :, :, -1:]),
+                                 envs.dtype)
+    D = envs.GR.dims[0]
+    GRl = DeviceTensor(ctx, L.GB_KIND_GR, envs.dtype, (D, 1, D))
+    L.check(L.lib().gb_env_channel_copy(ctx.handle, GRl.handle, 0, envs.GR.handle,
+                                        envs.GR.dims[1] - 1, 1))
+    op = DerivativeOperator(ctx, L.GB_HEFF_AC, envs.GL, Wl, None, GRl, backend or GB300Backend())
+    ac = psi.AC
+    return float(np.real(ac.dot(op(ac))))
+
+
+def galerkin(psi, envs, backend=None):
+    """calc_galerkin (toolbox.jl:63-70): |(1 - AL AL') normalize(H_AC(AC))|."""
+    y = _heff_ac(envs, backend or GB300Backend())(psi.AC)
+    y.normalize_()
+    project_complement_(y, psi.AL)
+    return y.norm()
+
+
+class VUMPS:
+    """VUMPS defaults (vumps.jl:19-43): tol 1e-10, maxiter 200, DynamicTol-adapted
+    eigensolver (factor 1e-3), environment (1e-4) and gauge (1e-6) tolerances."""
+
+    def __init__(self, tol=1e-10, maxiter=200, backend=None, verbosity=0):
+        self.tol, self.maxiter = tol, maxiter
+        self.backend = backend or GB300Backend()
+        self.verbosity = verbosity
+
+
+def find_groundstate_vumps(psi, H, alg, envs=None):
+    """find_groundstate(::InfiniteMPS, H, VUMPS()) for a one-site cell.
+    Returns (psi, envs, eps, history)."""
+    envs = envs or InfiniteEnvironments(psi, H, alg.backend.code)
+    it = 0
+    envs.recalculate(psi, tol=1e-10)
+    eps = galerkin(psi, envs, alg.backend)
+    envs.recalculate(psi, tol=_dyn_tol(eps, it, 1e-4))
+    hist = []
+    while True:
+        et = _dyn_tol(eps, it, 1e-3)
+        solver = Lanczos(krylovdim=30, maxiter=200, tol=et, eager=True)
+        _, AC, _ = fixedpoint(_heff_ac(envs, alg.backend), psi.AC, "SR", solver)
+        _, C, _ = fixedpoint(_heff_c(envs, alg.backend), psi.C, "SR", solver)
+        AL = regauge(AC, C)
+        AR, C = uniform_rightorth(AL, psi.C, tol=_dyn_tol(eps, it, 1e-6))
+        psi = InfiniteMPS(AL, AR, C)
+        envs.recalculate(psi, tol=_dyn_tol(eps, it, 1e-4))
+        eps = galerkin(psi, envs, alg.backend)
+        it += 1
+        e = energy_density(psi, envs, alg.backend)
+        hist.append({"iter": it, "energy": e, "eps": eps})
+        if alg.verbosity:
+            print(f"VUMPS {it}: e = {e:.14f}  eps = {eps:.3e}")
+        if eps <= alg.tol or it >= alg.maxiter:
+            break
+    return psi, envs, eps, hist

@@ -55,9 +55,12 @@ def split_two_site(op, atol=None):
 class MPOHamiltonian:
     """Dense Jordan-form MPO.  `W[i]` has shape (wl, d, d, wr)."""
 
-    def __init__(self, W, finite=True):
+    def __init__(self, W, finite=True, chans=None):
         self.W = list(W)
         self.finite = finite
+        # chans[i]: dimensions of the channel blocks (sum-space components) of the bond
+        # left of site i; the blocks are the "levels" of the infinite environments
+        self.chans = chans
         self._dev = {}
 
     def __len__(self):
@@ -170,7 +173,7 @@ def FiniteMPOHamiltonian(nsites, d, terms, dtype=np.complex128):
         chans[i + 1] = V
     W = [_fill(keys[i], ops[i], chans[i], chans[i + 1], d, np.dtype(dtype), True)
          for i in range(nsites)]
-    return MPOHamiltonian(W, finite=True)
+    return MPOHamiltonian(W, finite=True, chans=chans)
 
 
 def InfiniteMPOHamiltonian(ncell, d, terms, dtype=np.complex128):
@@ -206,7 +209,7 @@ def InfiniteMPOHamiltonian(ncell, d, terms, dtype=np.complex128):
                     changed = True
     V = [[1 if x is None else x for x in v] for v in V]
     W = [_fill(keys[i], ops[i], V[i - 1], V[i], d, np.dtype(dtype), True) for i in range(ncell)]
-    return MPOHamiltonian(W, finite=False)
+    return MPOHamiltonian(W, finite=False, chans=[V[i - 1] for i in range(ncell)] + [V[ncell - 1]])
 
 
 # ------------------------------------------------------------------ models

@@ -160,3 +160,14 @@ def test_transfer_environment_energy_consistency():
         psi.center = i + 1
         ei = P.expectation_value(psi, H, envs, i + 1)
         assert abs(ei - e0) < 1e-11
+
+
+def test_oracle_vumps_tfim_closed_form():
+    """VUMPS on the infinite TFIM (g = 0.5) reaches the free-fermion energy density."""
+    from oracle import vumps as V
+    H = M.infinite_mpo_hamiltonian(1, 2, M.tfim_terms(1, g=0.5, periodic=True))
+    rng = np.random.default_rng(1)
+    A = rng.standard_normal((12, 2, 12)) + 1j * rng.standard_normal((12, 2, 12))
+    psi, GL, GR, eps, hist = V.vumps(V.infinite_mps(A), H, tol=1e-10, maxiter=100)
+    assert eps <= 1e-10
+    assert abs(hist[-1][1] - M.tfim_infinite_energy_density(0.5)) < 1e-12
