@@ -184,6 +184,10 @@ size_t packed_bytes(int64_t rows, int64_t K, bool cplx, int role, int64_t batch)
 void pack_operand(gb_ctx* ctx, int dtype, int role, char op, int64_t M_or_N, int64_t K,
                   const void* src, int64_t ld, int64_t stride, int64_t batch, Packed& out,
                   void* dst);
+// leg mix whose output is written directly as the packed B operand of the next GEMM
+// (kJ[J]: contraction-index offset of output row J, mJ[J] + n*mn: output column index)
+void mixpack_run(gb_ctx* ctx, const MixDev& m, const int64_t* kJ, const int64_t* mJ, int64_t mn,
+                 int dtype, const void* x, Packed& out, int64_t Klog, int64_t Nlog);
 void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_t M,
                 int64_t N, double alpha, double beta, void* C, int64_t ldc, int64_t sC);
 bool tc_available(gb_ctx* ctx);

@@ -157,11 +157,89 @@ void pack_operand(gb_ctx* ctx, int dtype, int role, char op, int64_t R, int64_t 
   out.batch = batch;
   out.cplx = cx;
   out.bytes = packed_bytes(R, K, cx, role, batch);
-  GB_CHECK_CUDA(cudaMemsetAsync(dst, 0, out.bytes, ctx->stream));
+  // no memset: the kernel writes every (row, k < Kh) entry, zeros included for k >= K
   GB_REQUIRE(batch <= 65535 && (R + 31) / 32 <= 65535, "pack: grid too large");
   dim3 grid((unsigned)((p.Kh + 31) / 32), (unsigned)((R + 31) / 32), (unsigned)batch);
   pack_kernel<<<grid, dim3(32, 8), 0, ctx->stream>>>(p, (const double*)src,
                                                       (__nv_bfloat16*)dst);
+  GB_CHECK_CUDA(cudaGetLastError());
+  count_launch(ctx);
+}
+
+// ------------------------------------------------------------------ fused leg mix + pack
+// y[a + out_off[J] + n*yn] = sum_e val[e] x[a + in_off[col[e]] + n*xn] written directly as
+// the packed B operand of the following GEMM: logical B element (k, m) with
+// k = a + kJ[J] (contraction index) and m = mJ[J] + n*mn (output column index).
+template <bool CPLX>
+__global__ void mixpack_kernel(int64_t A, int64_t N, int64_t xn, const int64_t* __restrict__ in_off,
+                               const int64_t* __restrict__ kJ, const int64_t* __restrict__ mJ,
+                               int64_t mn, const int* __restrict__ row_ptr,
+                               const int* __restrict__ col, const double* __restrict__ val,
+                               const double* __restrict__ x, __nv_bfloat16* __restrict__ hi,
+                               int64_t Nlog, int64_t Kp, int64_t Kh, int64_t plane) {
+  const int J = blockIdx.y;
+  const int e0 = row_ptr[J], e1 = row_ptr[J + 1];
+  __nv_bfloat16* lo = hi + plane;
+  auto put = [&](int64_t row, int64_t c, double v) {
+    __nv_bfloat16 h = __double2bfloat16(v);
+    hi[row * Kp + c] = h;
+    lo[row * Kp + c] = __double2bfloat16(v - (double)__bfloat162float(h));
+  };
+  for (int64_t n = blockIdx.z; n < N; n += gridDim.z) {
+    const int64_t m = mJ[J] + n * mn;
+    for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < A;
+         a += (int64_t)gridDim.x * blockDim.x) {
+      const int64_t k = a + kJ[J];
+      if (CPLX) {
+        double re = 0.0, im = 0.0;
+        for (int e = e0; e < e1; ++e) {
+          const double* xv = x + 2 * (a + in_off[col[e]] + n * xn);
+          double vr = val[2 * e], vi = val[2 * e + 1];
+          re = fma(vr, xv[0], fma(-vi, xv[1], re));
+          im = fma(vr, xv[1], fma(vi, xv[0], im));
+        }
+        put(m, k, re);
+        put(m, Kh + k, -im);
+        put(Nlog + m, k, im);
+        put(Nlog + m, Kh + k, re);
+      } else {
+        double acc = 0.0;
+        for (int e = e0; e < e1; ++e) acc = fma(val[e], x[a + in_off[col[e]] + n * xn], acc);
+        put(m, k, acc);
+      }
+    }
+  }
+}
+
+void mixpack_run(gb_ctx* ctx, const MixDev& m, const int64_t* kJ, const int64_t* mJ, int64_t mn,
+                 int dtype, const void* x, Packed& out, int64_t Klog, int64_t Nlog) {
+  const bool cx = is_cplx(dtype);
+  GB_REQUIRE(m.nJ <= 65535, "mixpack: too many output rows");
+  GB_REQUIRE(m.xa == 1, "mixpack: unit input stride required");
+  // zero the K padding of every row once (entries k >= Klog are never produced by the mix)
+  if (out.Kh > Klog) {
+    __nv_bfloat16* base = (__nv_bfloat16*)out.data;
+    const int64_t planes = 2 * out.batch;
+    for (int64_t p = 0; p < planes; ++p) {
+      char* pb = (char*)(base + p * out.rows * out.Kp);
+      GB_CHECK_CUDA(cudaMemset2DAsync(pb + Klog * 2, out.Kp * 2, 0, (out.Kh - Klog) * 2, out.rows,
+                                      ctx->stream));
+      if (cx)
+        GB_CHECK_CUDA(cudaMemset2DAsync(pb + (out.Kh + Klog) * 2, out.Kp * 2, 0,
+                                        (out.Kh - Klog) * 2, out.rows, ctx->stream));
+    }
+  }
+  dim3 grid((unsigned)std::min<int64_t>((m.A + 127) / 128, 64), (unsigned)m.nJ,
+            (unsigned)std::min<int64_t>(m.N, 65535));
+  const int64_t plane = out.rows * out.Kp;
+  if (cx)
+    mixpack_kernel<true><<<grid, 128, 0, ctx->stream>>>(
+        m.A, m.N, m.xn, m.in_off, kJ, mJ, mn, m.row_ptr, m.col, m.val, (const double*)x,
+        (__nv_bfloat16*)out.data, Nlog, out.Kp, out.Kh, plane);
+  else
+    mixpack_kernel<false><<<grid, 128, 0, ctx->stream>>>(
+        m.A, m.N, m.xn, m.in_off, kJ, mJ, mn, m.row_ptr, m.col, m.val, (const double*)x,
+        (__nv_bfloat16*)out.data, Nlog, out.Kp, out.Kh, plane);
   GB_CHECK_CUDA(cudaGetLastError());
   count_launch(ctx);
 }

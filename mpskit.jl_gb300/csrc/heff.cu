@@ -47,6 +47,10 @@ struct Step {
   int src = S_X;
   MixDev mix;
   std::string name;
+  // the continuing-channel chain: the middle mix produces T2, the next GEMM consumes it;
+  // in split precision the mix writes T2 directly as that GEMM's packed B operand
+  bool t2_producer = false;
+  bool t2_consumer = false;
 };
 
 struct Cx {
@@ -125,6 +129,12 @@ struct gb_heff {
   bool y_zero_first = false;  // y must be zeroed before the steps (no step overwrites it)
   void* t1 = nullptr;
   void* t2 = nullptr;
+  // packed-T2 path (split precision): output-row offsets of the mix in the packed B operand
+  std::vector<int64_t> kJ, mJ;
+  int64_t mn = 0, t2K = 0, t2N = 0;
+  void* kmJ_dev = nullptr;
+  Packed t2p;
+  bool t2p_ready = false;
 };
 
 namespace gb {
@@ -145,11 +155,35 @@ static void add_gemm_flops(gb_heff* h, const Step& s) {
 }
 
 // Pre-pack constant GEMM operands for the split path.
+static void prepare_t2p(gb_heff* h) {
+  if (h->prec == GB_PREC_FP64 || h->t2p_ready || h->kJ.empty()) return;
+  const bool cx = is_cplx(h->dtype);
+  size_t nJ = h->kJ.size();
+  h->kmJ_dev = dalloc(h, 2 * nJ * sizeof(int64_t));
+  std::vector<int64_t> tab(h->kJ);
+  tab.insert(tab.end(), h->mJ.begin(), h->mJ.end());
+  GB_CHECK_CUDA(cudaMemcpyAsync(h->kmJ_dev, tab.data(), tab.size() * sizeof(int64_t),
+                                cudaMemcpyHostToDevice, h->ctx->stream));
+  GB_CHECK_CUDA(cudaStreamSynchronize(h->ctx->stream));
+  size_t bytes = packed_bytes(h->t2N, h->t2K, cx, PACK_AS_B, 1);
+  Packed& p = h->t2p;
+  p.data = dalloc(h, bytes);
+  p.bytes = bytes;
+  p.K = h->t2K;
+  p.Kh = (h->t2K + 63) / 64 * 64;
+  p.Kp = cx ? 2 * p.Kh : p.Kh;
+  p.rows = cx ? 2 * h->t2N : h->t2N;
+  p.batch = 1;
+  p.cplx = cx;
+  h->t2p_ready = true;
+}
+
 static void prepack(gb_heff* h, Step& s) {
   if (h->prec == GB_PREC_FP64) {
     s.hasPA = s.hasPB = false;
     return;
   }
+  prepare_t2p(h);
   gb_ctx* ctx = h->ctx;
   if (s.srcA == S_CONST && !s.hasPA) {
     void* dst = dalloc(h, packed_bytes(s.M, s.K, is_cplx(h->dtype), PACK_AS_A, 1));
@@ -377,8 +411,22 @@ static void build_ac2(gb_heff* h, const gb_tensor* GL, const gb_tensor* W1,
     s2.mix = mix_upload(ctx, make_plan(cf, cx, Dl, Dr, 1, Dl * d1 * d2 * chc, 1,
                                        Dl * chr * d1 * d2, io, oo));
     s2.accumulate = false;
+    s2.t2_producer = true;
     steps.push_back(s2);
     h->t2_elems = std::max(h->t2_elems, Dl * chr * d1 * d2 * Dr);
+    // T2 as the B operand of step 3: k = l' + Dl*c, column = (s1 + d1*s2) + d1*d2*r
+    h->kJ.resize(chr * d1 * d2);
+    h->mJ.resize(chr * d1 * d2);
+    for (int64_t c = 0; c < chr; ++c)
+      for (int64_t sa = 0; sa < d1; ++sa)
+        for (int64_t sb = 0; sb < d2; ++sb) {
+          int64_t J = c + chr * (sa + d1 * sb);
+          h->kJ[J] = Dl * c;
+          h->mJ[J] = sa + d1 * sb;
+        }
+    h->mn = d1 * d2;
+    h->t2K = Dl * chr;
+    h->t2N = d1 * d2 * Dr;
     // step 3: Y[l, (s1 s2 r)] (+)= GLc[l, (l' c)] . T2[(l' c), (s1 s2 r)]
     Step s3;
     s3.name = "AA3";
@@ -392,6 +440,7 @@ static void build_ac2(gb_heff* h, const gb_tensor* GL, const gb_tensor* W1,
     s3.M = Dl;
     s3.N = d1 * d2 * Dr;
     s3.K = Dl * chr;
+    s3.t2_consumer = true;
     push_gemm(s3);
     names.push_back("AA");
   }
@@ -790,8 +839,19 @@ static void build_ac(gb_heff* h, const gb_tensor* GL, const gb_tensor* W, const 
     s2.dst = S_T2;
     s2.mix = mix_upload(ctx, make_plan(cf, cx, Dl, Dr, 1, Dl * d * chc, 1, Dl * chr * d, io, oo));
     s2.accumulate = false;
+    s2.t2_producer = true;
     steps.push_back(s2);
     h->t2_elems = std::max(h->t2_elems, Dl * chr * d * Dr);
+    h->kJ.resize(chr * d);
+    h->mJ.resize(chr * d);
+    for (int64_t c = 0; c < chr; ++c)
+      for (int64_t sa = 0; sa < d; ++sa) {
+        h->kJ[c + chr * sa] = Dl * c;
+        h->mJ[c + chr * sa] = sa;
+      }
+    h->mn = d;
+    h->t2K = Dl * chr;
+    h->t2N = d * Dr;
     Step s3;
     s3.name = "A3";
     s3.srcA = S_CONST;
@@ -804,6 +864,7 @@ static void build_ac(gb_heff* h, const gb_tensor* GL, const gb_tensor* W, const 
     s3.M = Dl;
     s3.N = d * Dr;
     s3.K = Dl * chr;
+    s3.t2_consumer = true;
     push_gemm(s3);
     names.push_back("A");
   }
@@ -1029,7 +1090,9 @@ gb_heff* heff_build(gb_ctx* ctx, int kind, const gb_tensor* GL, const gb_tensor*
     }
     size_t es = elem_size(h->dtype);
     if (h->t1_elems) h->t1 = dalloc(h, (size_t)h->t1_elems * es);
-    if (h->t2_elems) h->t2 = dalloc(h, (size_t)h->t2_elems * es);
+    // the FP64 T2 buffer is only needed when T2 is not written packed (split precision)
+    if (h->t2_elems && (h->prec == GB_PREC_FP64 || h->kJ.empty()))
+      h->t2 = dalloc(h, (size_t)h->t2_elems * es);
     for (auto& s : h->steps)
       if (s.is_gemm) prepack(h, s);
     GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -1068,13 +1131,21 @@ void heff_apply_raw(gb_heff* h, const void* x, void* y) {
     }
     return nullptr;
   };
+  const bool fused_t2 = h->prec != GB_PREC_FP64 && h->t2p_ready;
+  if (!fused_t2 && h->t2_elems && !h->t2)
+    h->t2 = dalloc(h, (size_t)h->t2_elems * elem_size(h->dtype));
   for (const Step& s : h->steps) {
     if (s.is_gemm) {
       void* C = (void*)ptr(s.dst, nullptr);
       double beta = s.accumulate ? 1.0 : 0.0;
+      const Packed* pB = s.hasPB ? &s.pB : nullptr;
+      if (fused_t2 && s.t2_consumer) pB = &h->t2p;
       gemm(ctx, h->prec, h->dtype, s.opA, s.opB, s.M, s.N, s.K, 1.0, ptr(s.srcA, s.cA), s.lda, 0,
-           ptr(s.srcB, s.cB), s.ldb, 0, beta, C, s.ldc, 0, 1, s.hasPA ? &s.pA : nullptr,
-           s.hasPB ? &s.pB : nullptr);
+           ptr(s.srcB, s.cB), s.ldb, 0, beta, C, s.ldc, 0, 1, s.hasPA ? &s.pA : nullptr, pB);
+    } else if (fused_t2 && s.t2_producer) {
+      const int64_t* kJ = (const int64_t*)h->kmJ_dev;
+      mixpack_run(ctx, s.mix, kJ, kJ + h->kJ.size(), h->mn, h->dtype, ptr(s.src, nullptr), h->t2p,
+                  h->t2K, h->t2N);
     } else {
       mix_run(ctx, s.mix, h->dtype, ptr(s.src, nullptr), (void*)ptr(s.dst, nullptr),
               s.accumulate ? 1.0 : 0.0);
