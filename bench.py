@@ -49,8 +49,11 @@ def parse():
     ap.add_argument("--precision", default="bf16x3", choices=["bf16x3", "fp64"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--seed", type=int, default=1234 + 5)
     ap.add_argument("--svd", default="gram", choices=["gesvd", "gesvdp", "gram"])
+    ap.add_argument("--symmetry", default="u1", choices=["u1", "none"],
+                    help="u1: U(1) (total Sz = 0) block-sparse state and MPO; none: dense")
     return ap.parse_args()
 
 
@@ -287,14 +290,20 @@ def run_ours(args):
     ctx.set_precision(prec)
     ctx.set_svd_method(args.svd)
     backend = mpsgb.GB300Backend(prec, local)
-    H = mpsgb.j1j2_cylinder(args.Lx, args.Ly, dtype=np.float64)
+    u1 = args.symmetry == "u1"
+    H = mpsgb.j1j2_cylinder(args.Lx, args.Ly, dtype=np.float64, u1=u1)
     n = len(H)
     pos = n // 2 - 1
     D = args.D
     t_setup = time.perf_counter()
-    As = mpsgb.states.random_tensors(n, 2, D, args.seed + rank, np.float64)
-    log(f"random tensors ready (L={n}, D={D})")
-    psi = mpsgb.FiniteMPS.from_tensors(As, ctx, center=pos + 1)
+    charges = None
+    if u1:
+        As, qb = mpsgb.u1.random_u1_tensors(n, D, args.seed + rank, 0, np.float64)
+        charges = (qb, mpsgb.operators.SPIN_HALF_CHARGES)
+    else:
+        As = mpsgb.states.random_tensors(n, 2, D, args.seed + rank, np.float64)
+    log(f"random tensors ready (L={n}, D={D}, symmetry {args.symmetry})")
+    psi = mpsgb.FiniteMPS.from_tensors(As, ctx, center=pos + 1, charges=charges)
     del As
     ctx.synchronize()
     log("canonical MPS built on the device")
@@ -349,6 +358,7 @@ def run_ours(args):
         nvtx = torch.cuda.nvtx
     except Exception:
         nvtx = None
+    ctx.read_work(reset=True)
     with ClockSampler(local) as clocks:
         if nvtx:
             nvtx.range_push("timed")
@@ -363,24 +373,38 @@ def run_ours(args):
             nvtx.range_pop()
     barrier(pg)
     launches = ctx.kernel_launches() - launches0
+    tile_flops_timed = ctx.read_work(reset=True)["tile_flops"]
     t_dev = prof["region_ms"] / 1e3          # CUDA-event time of the region on the stream
     t_step = max(t_wall, t_dev)
     t_max = allmax(pg, t_step)
-    flops_tot = allsum(pg, stats.heff_flops)
-    value = flops_tot / t_max / 1e12
     ms_per_step = 1e3 * t_max / args.steps
+    # flop accounting (untimed): one H_eff matvec at the same bond with the nonzero-product
+    # counters on -- the block-sparse algorithmic count of the U(1) workload (equal to the
+    # dense GEMM count when nothing is zero) and the tile work the tensor pipe executes
+    count = heff_count_pass(ctx, psi, H, envs, backend, pos) if prec == "bf16x3" else None
+    if count:
+        heff_alg = count["nonzero_flops"] * stats.matvecs
+        rho = count["nonzero_flops"] / max(1.0, count["tile_flops"])
+    else:
+        heff_alg, rho = stats.heff_flops, 1.0
+    value = allsum(pg, heff_alg) / t_max / 1e12
 
     pk = peaks() or {}
     peak_bf16 = pk.get("bf16_tflops_sustained")
     peak_src = "measured (sustained)" if peak_bf16 else "fallback"
     peak_bf16 = peak_bf16 or 1700.0
     split = 3.0 if prec == "bf16x3" else 1.0
-    gemm_alg = prof["gemm_flops"] / (prof["gemm_ms"] / 1e3) / 1e12 if prof["gemm_ms"] > 0 else 0.0
+    gemm_s = prof["gemm_ms"] / 1e3
+    # algorithmic GEMM flops of the timed region: executed tile work x (nonzero / tile) of
+    # the counted matvec (the dense case has rho ~ 1, below 1 only by partial-tile padding)
+    gemm_alg = rho * tile_flops_timed / gemm_s / 1e12 if gemm_s > 0 else 0.0
     achieved = split * gemm_alg
     roofline = {
-        "bound": "tensor", "kernel": "gemm_bf16x3_kernel", "achieved": achieved,
+        "bound": "tensor", "kernel": "gemm_bf16x3_persistent", "achieved": achieved,
         "peak": peak_bf16, "unit": "TFLOP/s", "frac": achieved / peak_bf16,
         "peak_source": peak_src, "algorithmic_tflops": gemm_alg,
+        "executed_tile_tflops_per_product": tile_flops_timed / max(gemm_s, 1e-12) / 1e12,
+        "executed_frac": split * tile_flops_timed / max(gemm_s, 1e-12) / 1e12 / peak_bf16,
         "launches": prof["gemm_launches"], "kernel_ms": prof["gemm_ms"],
         "kernel_share_of_step": prof["gemm_ms"] / max(1e-9, prof["region_ms"]),
         "traffic": None,
@@ -390,8 +414,15 @@ def run_ours(args):
     log(f"timed region done: {t_wall:.3f}s wall, {t_dev:.3f}s device; status {ctx.device_status()}")
     e2e = None
     if not args.no_e2e:
-        e2e = run_e2e(args, ctx, psi, H, envs, alg, pos, state, pg)
+        e2e = run_e2e(args, ctx, psi, H, envs, alg, pos, state, pg,
+                      count["nonzero_flops"] if count else None)
         log("e2e done")
+
+    fp64 = None
+    if prec != "fp64" and not args.no_fp64_compare:
+        fp64 = fp64_compare(ctx, psi, H, envs, backend, pos, Wd, GR_next, stats, args.steps,
+                            ms_per_step / 1e3)
+        log(f"plain FP64 GPU comparison done: {fp64}")
 
     cpu = None
     if not args.no_cpu_baseline and rank == 0 and world == 1:
@@ -416,7 +447,9 @@ def run_ours(args):
             "data": "synthetic",
             "config": {
                 "workload": f"J1-J2 Heisenberg {args.Ly}x{args.Lx} cylinder ({n} sites), DMRG2 "
-                            f"local update + env step at bond {pos}, D={D}, dense Float64",
+                            f"local update + env step at bond {pos}, D={D}, Float64, "
+                            + ("U(1) total Sz = 0, block-sparse" if u1 else "dense, no symmetry"),
+                "symmetry": args.symmetry,
                 "model": "J1=1, J2=0.5, snake order", "D": D, "L": n,
                 "mpo_width_at_bond": int(H.W[pos].shape[3]), "precision": prec,
                 "svd": args.svd,
@@ -424,12 +457,17 @@ def run_ours(args):
             },
             "gpu_launches": launches,
             "sweep_s_estimate": ms_per_step / 1e3 * (2 * n - 3),
-            "heff_flops_per_step": stats.heff_flops / args.steps,
+            "heff_flops_per_step": heff_alg / args.steps,
+            "heff_flops_per_matvec": {
+                "nonzero_products": count["nonzero_flops"] if count else None,
+                "tile_executed_per_product": count["tile_flops"] if count else None,
+                "dense_equivalent": stats.heff_flops / max(1, stats.matvecs)},
             "matvecs_per_step": stats.matvecs / args.steps,
             "phase_s_per_step": {k: v / args.steps for k, v in stats.t.items()},
             "local_energy": state.get("val"), "eps_trunc": state.get("eps_trunc"),
             "setup_s": t_setup,
             "roofline": roofline,
+            "fp64_gpu": fp64,
             "clocks": clocks.summary(),
             "e2e": e2e,
             "cpu_baseline": cpu,
@@ -439,7 +477,56 @@ def run_ours(args):
         pg.destroy_process_group()
 
 
-def run_e2e(args, ctx, psi, H, envs, alg, pos, state, pg):
+def heff_count_pass(ctx, psi, H, envs, backend, pos):
+    """One AC2 matvec with the GEMM work counters on: nonzero-product flops (block-sparse
+    algorithmic count) and tile flops executed per split product."""
+    import mpsgb
+    ctx.read_work(reset=True)
+    ctx.set_counting(True)
+    try:
+        Heff = mpsgb.AC2_hamiltonian(pos, psi, H, envs, backend)
+        x = mpsgb.ac2_from(psi.AL[pos], psi.ac(pos + 1))
+        Heff(x)
+        ctx.synchronize()
+        return ctx.read_work(reset=True)
+    finally:
+        ctx.set_counting(False)
+
+
+def fp64_compare(ctx, psi, H, envs, backend, pos, Wd, GR_next, stats, steps, t_step_split):
+    """The plain FP64 GPU path on the same bond: one AC2 matvec and one environment step timed
+    at FP64 (same kernels' FP64 variants, CUDA-event region on the library stream), composed
+    with the step's measured matvec count and its FP64 gauge time into a per-step figure."""
+    import mpsgb
+    from mpsgb import _lib as L
+    Heff = mpsgb.AC2_hamiltonian(pos, psi, H, envs, mpsgb.GB300Backend("fp64", backend.device))
+    x = mpsgb.ac2_from(psi.AL[pos], psi.ac(pos + 1))
+    y = Heff.new_vector()
+    Heff(x, out=y)                       # warm-up (plans, pool)
+    ctx.synchronize()
+    ctx.profile_begin()
+    Heff(x, out=y)
+    ctx.synchronize()
+    t_mv = ctx.profile_end()["region_ms"] / 1e3
+    A = psi.AR[pos + 1]
+    ctx.profile_begin()
+    L.check(L.lib().gb_env_transfer_right(ctx.handle, envs.rightenv(pos + 1, psi).handle,
+                                          Wd[pos + 1].handle, A.handle, A.handle,
+                                          L.GB_PREC_FP64, GR_next.handle))
+    ctx.synchronize()
+    t_env = ctx.profile_end()["region_ms"] / 1e3
+    del Heff, y
+    mv = stats.matvecs / steps
+    gauge = stats.t["gauge"] / steps
+    est = mv * t_mv + gauge + t_env
+    return {"matvec_s": t_mv, "env_step_s": t_env, "matvecs_per_step": mv,
+            "gauge_s": gauge, "step_s_estimate": est,
+            "split_speedup_per_step": est / t_step_split,
+            "how": "FP64 matvec and env step timed once each on the device; step = "
+                   "matvecs x matvec + gauge (FP64 in both paths) + env step"}
+
+
+def run_e2e(args, ctx, psi, H, envs, alg, pos, state, pg, flops_per_matvec=None):
     """Local updates driven through the C ABI with host buffers: x0 uploaded from pinned
     host memory, eigensolve + truncated SVD on the device, AL/S/AR downloaded."""
     import ctypes
@@ -457,11 +544,11 @@ def run_e2e(args, ctx, psi, H, envs, alg, pos, state, pg):
     x_host = pin(ac2.dims)
     L.check(L.lib().gb_tensor_download(ac2.handle, host_ptr(x_host), ac2.size * 8))
     Heff = mpsgb.AC2_hamiltonian(pos, psi, H, envs, alg.backend)
-    flops = Heff.flops
+    flops = flops_per_matvec or Heff.flops
     outs = {}
 
     def one():
-        x = mpsgb.DeviceTensor(ctx, L.GB_KIND_AC2, np.float64, ac2.dims)
+        x = mpsgb.DeviceTensor(ctx, L.GB_KIND_AC2, np.float64, ac2.dims, charges=ac2.charges)
         L.check(L.lib().gb_tensor_upload(x.handle, host_ptr(x_host), x.size * 8))
         solver = alg.alg_eigsolve.adapt(state["decay"], state["eps_local"], state["eps_local"],
                                         state["eps_trunc"])

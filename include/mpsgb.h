@@ -107,6 +107,29 @@ int gb_ctx_profile_begin(gb_ctx* ctx);
 int gb_ctx_profile_end(gb_ctx* ctx, double* gemm_ms, int64_t* gemm_launches,
                        double* gemm_flops, double* region_ms);
 
+/* Schedule of the split-precision tensor-core GEMM (the choice TensorOperations leaves to
+ * its contraction backend, `backend::AbstractBackend` carried by every derivative operator,
+ * src/algorithms/derivatives/mpo_derivatives.jl:10-16).  tile_n = output tile width along
+ * N (128 or 256; 0 = chosen per GEMM shape). */
+enum {
+  GB_SCHED_PERSISTENT = 0,       /* one CTA per SM over a tile counter, accumulator double-
+                                    buffered in TMEM; k-blocks whose packed A and B tiles
+                                    are both zero are skipped (block-sparse operands stored
+                                    densely with charge-sorted legs); the default         */
+  GB_SCHED_PERSISTENT_DENSE = 1, /* the same kernel over every k-block                    */
+  GB_SCHED_TILE = 2              /* one CTA per output tile, single accumulator          */
+};
+int gb_ctx_set_gemm_schedule(gb_ctx* ctx, int schedule, int tile_n);
+/* Work counters of the split-precision GEMMs (the flop accounting of the block-sparse
+ * measurement; the reference's TimerOutputs sections, src/algorithms/groundstate/dmrg.jl:
+ * 289-292, count time only).  tile_flops: flops the tensor pipe executes per split product,
+ * summed over the k-blocks every output tile runs (accumulated while profiling or counting).
+ * nonzero_flops: 2 x the number of nonzero scalar products sum_k nnz(A[:,k]) nnz(B[k,:]) of
+ * every split GEMM while counting is on -- the block-sparse algorithmic count; counting adds
+ * a pass over each packed operand, so keep it off inside timed regions. */
+int gb_ctx_set_counting(gb_ctx* ctx, int on);
+int gb_ctx_read_work(gb_ctx* ctx, double* tile_flops, double* nonzero_flops, int reset);
+
 /* ---------------------------------------------------------------- tensors */
 /* Storage of TensorMap blocks (TensorKit `TensorMap{T,S,N1,N2}` with Trivial sectors). */
 int gb_tensor_create(gb_ctx* ctx, int kind, int dtype, int ndim, const int64_t* dims,
@@ -204,6 +227,32 @@ int gb_svd_trunc(gb_ctx* ctx, const gb_tensor* AC2, int64_t maxdim, double atol,
 int gb_left_orth(gb_ctx* ctx, const gb_tensor* AC, gb_tensor** AL, gb_tensor** C);
 /* right_gauge(AC): AC = C * AR (src/states/orthoview.jl:334-338); outputs created. */
 int gb_right_orth(gb_ctx* ctx, const gb_tensor* AC, gb_tensor** C, gb_tensor** AR);
+
+/* ---------------------------------------------------------------- U(1) symmetry */
+/* U(1)-symmetric tensors are stored densely with every leg sorted by charge; entries
+ * outside the charge-conserving blocks are exactly zero (for A[l s; r]: q_l + q_s = q_r;
+ * for AC2[l s1; r s2]: q_l + q_s1 + q_s2 = q_r).  Contractions need no extra argument: the
+ * split-precision GEMM skips zero tiles (GB_SCHED_PERSISTENT).  The factorisations below act
+ * per charge block, as TensorKit's do on a symmetric TensorMap (MatrixAlgebraKit called on
+ * each block), so that no rounding leaks between sectors.  Charges are host int32 arrays per
+ * leg; q_k receives the charges of the new bond (ascending; capacity min of the two fused
+ * dimensions) and k its dimension.  Inputs with weight outside their blocks are rejected. */
+/* left_gauge(AC) (src/states/orthoview.jl:322-326) block by block: AC = AL * C */
+int gb_u1_left_orth(gb_ctx* ctx, const gb_tensor* AC, const int32_t* q_l, const int32_t* q_s,
+                    const int32_t* q_r, gb_tensor** AL, gb_tensor** C, int32_t* q_k,
+                    int64_t* k);
+/* right_gauge(AC) (src/states/orthoview.jl:334-338) block by block: AC = C * AR */
+int gb_u1_right_orth(gb_ctx* ctx, const gb_tensor* AC, const int32_t* q_l, const int32_t* q_s,
+                     const int32_t* q_r, gb_tensor** C, gb_tensor** AR, int32_t* q_k,
+                     int64_t* k);
+/* gauge2! with svd_trunc (src/states/orthoview.jl:401-420) on a symmetric two-site tensor:
+ * per-block factorisation (method of gb_ctx_set_svd_method), truncation by truncrank(maxdim)
+ * & trunctol(atol) over the singular values of all blocks together (ties broken by charge,
+ * then by position).  Charges in reference leg order (l, s1, r, s2). */
+int gb_u1_svd_trunc(gb_ctx* ctx, const gb_tensor* AC2, const int32_t* q_l, const int32_t* q_s1,
+                    const int32_t* q_r, const int32_t* q_s2, int64_t maxdim, double atol,
+                    int normalize, gb_tensor** AL, gb_tensor** S, gb_tensor** AR, int32_t* q_k,
+                    int64_t* k, double* eps);
 
 /* ---------------------------------------------------------------- allocation-free variant */
 /* y = GL . x . GR (the bond operator of GB_HEFF_C) on caller-owned DEVICE buffers in the

@@ -670,6 +670,34 @@ void check_ctx(const gb_tensor* t, gb_ctx* ctx) {
 
 }  // namespace
 
+// external-linkage access to the gauge helpers above (used by u1.cu)
+namespace gb {
+gb_tensor* gauge_new_tensor(gb_ctx* ctx, int kind, int dtype, int ndim, const int64_t* dims) {
+  return new_tensor(ctx, kind, dtype, ndim, dims);
+}
+void gauge_free_tensor(gb_tensor* t) { free_tensor(t); }
+void gauge_qr_pos(gb_ctx* ctx, int dtype, int64_t m, int64_t n, const void* M, void* Q, void* R) {
+  qr_pos(ctx, dtype, m, n, M, Q, R);
+}
+void gauge_svd_tall(gb_ctx* ctx, int dtype, int64_t m, int64_t n, void* A, void* U, double* S,
+                    void* VT) {
+  svd_tall(ctx, dtype, m, n, A, U, S, VT);
+}
+void gauge_conj_transpose(gb_ctx* ctx, int dtype, int64_t m, int64_t n, const void* A,
+                          int64_t lda, void* B, int64_t ldb) {
+  conj_transpose(ctx, dtype, m, n, A, lda, B, ldb);
+}
+void* gauge_solver(gb_ctx* ctx) { return (void*)solver(ctx); }
+void u1_left_orth(gb_ctx* ctx, const gb_tensor* AC, const int32_t* ql, const int32_t* qs,
+                  const int32_t* qr, gb_tensor** AL, gb_tensor** C, int32_t* qk, int64_t* k);
+void u1_right_orth(gb_ctx* ctx, const gb_tensor* AC, const int32_t* ql, const int32_t* qs,
+                   const int32_t* qr, gb_tensor** C, gb_tensor** AR, int32_t* qk, int64_t* k);
+void u1_svd_trunc(gb_ctx* ctx, const gb_tensor* AC2, const int32_t* ql, const int32_t* qs1,
+                  const int32_t* qs2, const int32_t* qr, int64_t maxdim, double atol,
+                  int normalize, gb_tensor** AL, gb_tensor** S, gb_tensor** AR, int32_t* qk,
+                  int64_t* k, double* eps);
+}  // namespace gb
+
 // ================================================================== C ABI
 extern "C" {
 
@@ -690,6 +718,8 @@ int gb_ctx_create(int device, uint32_t flags, gb_ctx** out) {
   GB_CHECK_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   GB_CHECK_CUDA(cudaMalloc(&c->d_status, 256));
   GB_CHECK_CUDA(cudaMemset(c->d_status, 0, 256));
+  c->d_tile_counter = (unsigned int*)((char*)c->d_status + 128);
+  c->d_work = (double*)((char*)c->d_status + 192);
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
   cudaMemPool_t pool;
   if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
@@ -761,6 +791,38 @@ int gb_ctx_set_svd_method(gb_ctx* ctx, int method) {
   GB_REQUIRE(method == GB_SVD_GESVD || method == GB_SVD_GESVDP || method == GB_SVD_GRAM,
              "unknown SVD method");
   ctx->svd_method = method;
+  API_END
+}
+
+int gb_ctx_set_gemm_schedule(gb_ctx* ctx, int schedule, int tile_n) {
+  API_BEGIN
+  GB_REQUIRE(ctx, "null context");
+  GB_REQUIRE(schedule == GB_SCHED_PERSISTENT || schedule == GB_SCHED_PERSISTENT_DENSE ||
+                 schedule == GB_SCHED_TILE,
+             "unknown GEMM schedule");
+  GB_REQUIRE(tile_n == 0 || tile_n == 128 || tile_n == 256, "tile_n must be 0, 128 or 256");
+  ctx->gemm_schedule = schedule;
+  ctx->gemm_bn = tile_n;
+  API_END
+}
+
+int gb_ctx_set_counting(gb_ctx* ctx, int on) {
+  API_BEGIN
+  GB_REQUIRE(ctx, "null context");
+  ctx->counting = on != 0;
+  API_END
+}
+
+int gb_ctx_read_work(gb_ctx* ctx, double* tile_flops, double* nonzero_flops, int reset) {
+  API_BEGIN
+  GB_REQUIRE(ctx, "null context");
+  DevGuard g(ctx->device);
+  double w[2] = {0.0, 0.0};
+  GB_CHECK_CUDA(cudaMemcpyAsync(w, ctx->d_work, sizeof(w), cudaMemcpyDeviceToHost, ctx->stream));
+  GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (tile_flops) *tile_flops = w[0];
+  if (nonzero_flops) *nonzero_flops = w[1];
+  if (reset) GB_CHECK_CUDA(cudaMemsetAsync(ctx->d_work, 0, sizeof(w), ctx->stream));
   API_END
 }
 
@@ -1352,6 +1414,44 @@ int gb_right_orth(gb_ctx* ctx, const gb_tensor* AC, gb_tensor** C, gb_tensor** A
   GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
   *C = l;
   *AR = q;
+  API_END
+}
+
+int gb_u1_left_orth(gb_ctx* ctx, const gb_tensor* AC, const int32_t* q_l, const int32_t* q_s,
+                    const int32_t* q_r, gb_tensor** AL, gb_tensor** C, int32_t* q_k,
+                    int64_t* k) {
+  API_BEGIN
+  check_ctx(AC, ctx);
+  GB_REQUIRE(AL && C && q_k && k && q_l && q_s && q_r, "null argument");
+  GB_REQUIRE(AC->kind == GB_KIND_MPS, "u1_left_orth: input must be an MPS tensor");
+  DevGuard g(ctx->device);
+  gb::u1_left_orth(ctx, AC, q_l, q_s, q_r, AL, C, q_k, k);
+  API_END
+}
+
+int gb_u1_right_orth(gb_ctx* ctx, const gb_tensor* AC, const int32_t* q_l, const int32_t* q_s,
+                     const int32_t* q_r, gb_tensor** C, gb_tensor** AR, int32_t* q_k,
+                     int64_t* k) {
+  API_BEGIN
+  check_ctx(AC, ctx);
+  GB_REQUIRE(AR && C && q_k && k && q_l && q_s && q_r, "null argument");
+  GB_REQUIRE(AC->kind == GB_KIND_MPS, "u1_right_orth: input must be an MPS tensor");
+  DevGuard g(ctx->device);
+  gb::u1_right_orth(ctx, AC, q_l, q_s, q_r, C, AR, q_k, k);
+  API_END
+}
+
+int gb_u1_svd_trunc(gb_ctx* ctx, const gb_tensor* AC2, const int32_t* q_l, const int32_t* q_s1,
+                    const int32_t* q_r, const int32_t* q_s2, int64_t maxdim, double atol,
+                    int normalize, gb_tensor** AL, gb_tensor** S, gb_tensor** AR, int32_t* q_k,
+                    int64_t* k, double* eps) {
+  API_BEGIN
+  check_ctx(AC2, ctx);
+  GB_REQUIRE(AL && S && AR && q_k && k && q_l && q_s1 && q_s2 && q_r, "null argument");
+  GB_REQUIRE(AC2->kind == GB_KIND_AC2, "u1_svd_trunc: input must be a two-site tensor");
+  DevGuard g(ctx->device);
+  gb::u1_svd_trunc(ctx, AC2, q_l, q_s1, q_s2, q_r, maxdim, atol, normalize, AL, S, AR, q_k, k,
+                   eps);
   API_END
 }
 

@@ -76,6 +76,14 @@ struct gb_ctx {
   int num_sms = 0;
   int aux_prec = GB_PREC_FP64;   // precision of auxiliary state contractions
   int svd_method = 0;            // GB_SVD_* of gb_svd_trunc
+  // split-precision GEMM schedule (GB_SCHED_*) and output tile width (0 = chosen per shape)
+  int gemm_schedule = 0;
+  int gemm_bn = 0;
+  unsigned int* d_tile_counter = nullptr;  // work counter of the persistent GEMM
+  // work counters (device doubles): [0] flops the tensor pipe executes per split product
+  // (tile granularity), [1] algorithmic flops of the nonzero products (block-sparse count)
+  double* d_work = nullptr;
+  bool counting = false;  // count nonzero products of every split GEMM (extra passes)
   // tracing of the tensor-core GEMM launches
   bool profiling = false;
   std::vector<cudaEvent_t> prof_events;  // pairs (start, stop) per launch
@@ -169,6 +177,13 @@ bool all_finite(gb_ctx* ctx, int dtype, int64_t n, const void* x);
 // ------------------------------------------------------------------ split precision
 // Operand packed for the tcgen05 BF16 GEMM: K-major rows, two planes (hi, lo),
 // realified when complex (see gemm_tc.cu).
+//
+// Each packed operand carries a nonzero map: one bit per (128-row tile, 64-wide k-block),
+// [batch][ceil(rows/128)][kw] 32-bit words stored after the planes.  A bit is set when any
+// entry of that tile is nonzero; the persistent GEMM skips k-blocks whose A and B bits are
+// not both set, which is how block-sparse (charge-conserving) operands stored densely with
+// charge-sorted legs run only their nonzero blocks.
+constexpr int64_t MASK_ROWS = 128;
 struct Packed {
   void* data = nullptr;  // [batch][2 planes][rows][Kp] bf16
   int64_t rows = 0, Kp = 0, batch = 1;
@@ -177,10 +192,18 @@ struct Packed {
   bool cplx = false;
   bool owned = false;
   size_t bytes = 0;
+  uint32_t* mask = nullptr;  // nonzero map (see above)
+  int64_t mrows = 0;         // ceil(rows / 128)
+  int kw = 0;                // 32-bit words per mask row: ceil(Kp / 64 / 32)
+  uint32_t* cnt = nullptr;   // [batch][Kp] nonzero rows per packed k (filled when counting)
+  bool cnt_valid = false;
 };
 // which operand of C = op(A) op(B) is being packed
 enum PackRole { PACK_AS_A = 0, PACK_AS_B = 1 };
 size_t packed_bytes(int64_t rows, int64_t K, bool cplx, int role, int64_t batch);
+// fills every field of out for a buffer of packed_bytes(...) at data
+void packed_layout(Packed& out, void* data, int64_t R, int64_t K, bool cplx, int role,
+                   int64_t batch);
 void pack_operand(gb_ctx* ctx, int dtype, int role, char op, int64_t M_or_N, int64_t K,
                   const void* src, int64_t ld, int64_t stride, int64_t batch, Packed& out,
                   void* dst);

@@ -75,7 +75,8 @@ __device__ inline void load_elem(const PackArgs& p, const double* src, int64_t r
 
 // 32 x 32 tile transpose through shared memory; block = 32 x 8 threads.
 __global__ void pack_kernel(PackArgs p, const double* __restrict__ src,
-                            __nv_bfloat16* __restrict__ dst) {
+                            __nv_bfloat16* __restrict__ dst, uint32_t* __restrict__ mask,
+                            int kw, int64_t mrows) {
   __shared__ double tre[32][33];
   __shared__ double tim[32][33];
   const int64_t b = blockIdx.z;
@@ -103,10 +104,12 @@ __global__ void pack_kernel(PackArgs p, const double* __restrict__ src,
   }
   __syncthreads();
   // store: k fastest
+  int nz = 0;
   for (int j = ty; j < 32; j += 8) {
     int64_t r = r0 + j, k = k0 + tx;
-    if (r >= p.R || k >= p.Kh) continue;  // pads were zeroed by memset
+    if (r >= p.R || k >= p.Kh) continue;  // entries k >= K were loaded as zeros
     double re = tre[j][tx], im = tim[j][tx];
+    nz |= (re != 0.0 || im != 0.0);
     auto put = [&](int64_t row, int64_t col, double v) {
       __nv_bfloat16 h = __double2bfloat16(v);
       __nv_bfloat16 l = __double2bfloat16(v - (double)__bfloat162float(h));
@@ -125,13 +128,101 @@ __global__ void pack_kernel(PackArgs p, const double* __restrict__ src,
       put(p.R + r, p.Kh + k, re);
     }
   }
+  // nonzero map: this 32 x 32 block lies in one 128-row tile and one 64-wide k-block
+  // (complex operands also touch the imaginary half; marked conservatively)
+  if (__syncthreads_or(nz) && tx == 0 && ty == 0) {
+    uint32_t* mb = mask + b * mrows * kw;
+    auto mark = [&](int64_t row, int64_t col) {
+      int64_t kb = col / KALIGN;
+      atomicOr(&mb[(row / MASK_ROWS) * kw + kb / 32], 1u << (kb % 32));
+    };
+    const int64_t rlast = std::min<int64_t>(r0 + 31, p.R - 1);
+    mark(r0, k0);
+    if (p.cplx) {
+      mark(r0, p.Kh + k0);
+      if (p.role == 1) {
+        mark(p.R + r0, k0);
+        mark(p.R + r0, p.Kh + k0);
+        mark(p.R + rlast, k0);
+        mark(p.R + rlast, p.Kh + k0);
+      }
+    }
+  }
 }
+
+static size_t plane_bytes(int64_t prow, int64_t Kp, int64_t batch) {
+  return (size_t)round_up((int64_t)batch * 2 * prow * Kp * 2, 256);
+}
+static int mask_words(int64_t Kp) { return (int)((Kp / KALIGN + 31) / 32); }
 
 size_t packed_bytes(int64_t rows, int64_t K, bool cplx, int role, int64_t batch) {
   int64_t Kh = round_up(std::max<int64_t>(K, 1), KALIGN);
   int64_t Kp = cplx ? 2 * Kh : Kh;
   int64_t prow = (cplx && role == PACK_AS_B) ? 2 * rows : rows;
-  return (size_t)batch * 2 * prow * Kp * 2;
+  int64_t mrows = (prow + MASK_ROWS - 1) / MASK_ROWS;
+  return plane_bytes(prow, Kp, batch) + (size_t)batch * mrows * mask_words(Kp) * 4 +
+         (size_t)batch * Kp * 4;
+}
+
+void packed_layout(Packed& out, void* data, int64_t R, int64_t K, bool cx, int role,
+                   int64_t batch) {
+  out.data = data;
+  out.K = K;
+  out.Kh = round_up(std::max<int64_t>(K, 1), KALIGN);
+  out.Kp = cx ? 2 * out.Kh : out.Kh;
+  out.rows = (cx && role == PACK_AS_B) ? 2 * R : R;
+  out.batch = batch;
+  out.cplx = cx;
+  out.bytes = packed_bytes(R, K, cx, role, batch);
+  out.mrows = (out.rows + MASK_ROWS - 1) / MASK_ROWS;
+  out.kw = mask_words(out.Kp);
+  out.mask = (uint32_t*)((char*)data + plane_bytes(out.rows, out.Kp, batch));
+  out.cnt = out.mask + (size_t)batch * out.mrows * out.kw;
+  out.cnt_valid = false;
+}
+
+// nonzero rows per packed k (both planes), rows split in chunks of 256 with one atomic each
+__global__ void count_cols_kernel(const __nv_bfloat16* __restrict__ planes, int64_t rows,
+                                  int64_t Kp, uint32_t* __restrict__ cnt) {
+  const int64_t b = blockIdx.z;
+  const __nv_bfloat16* hi = planes + b * 2 * rows * Kp;
+  const __nv_bfloat16* lo = hi + rows * Kp;
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= Kp) return;
+  const int64_t r0 = (int64_t)blockIdx.y * 256, r1 = std::min<int64_t>(r0 + 256, rows);
+  uint32_t c = 0;
+  for (int64_t r = r0; r < r1; ++r)
+    c += (__bfloat162float(hi[r * Kp + k]) != 0.f || __bfloat162float(lo[r * Kp + k]) != 0.f);
+  if (c) atomicAdd(&cnt[b * Kp + k], c);
+}
+
+static void count_cols(gb_ctx* ctx, Packed& p) {
+  GB_CHECK_CUDA(cudaMemsetAsync(p.cnt, 0, (size_t)p.batch * p.Kp * 4, ctx->stream));
+  dim3 grid((unsigned)((p.Kp + 255) / 256), (unsigned)((p.rows + 255) / 256), (unsigned)p.batch);
+  GB_REQUIRE(grid.y <= 65535 && grid.z <= 65535, "count: grid too large");
+  count_cols_kernel<<<grid, 256, 0, ctx->stream>>>((const __nv_bfloat16*)p.data, p.rows, p.Kp,
+                                                   p.cnt);
+  GB_CHECK_CUDA(cudaGetLastError());
+  count_launch(ctx);
+  p.cnt_valid = true;
+}
+
+// work[1] += 2 sum_z sum_k cntA[z][k] cntB[z][k]
+__global__ void nonzero_products_kernel(const uint32_t* __restrict__ ca, const uint32_t* __restrict__ cb,
+                                        int64_t Kp, int64_t batch, int sa, int sb,
+                                        double* __restrict__ work) {
+  double acc = 0.0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < Kp * batch;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t z = e / Kp, k = e % Kp;
+    acc += (double)ca[(sa ? z : 0) * Kp + k] * (double)cb[(sb ? z : 0) * Kp + k];
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0 && acc != 0.0) atomicAdd(&work[1], 2.0 * acc);
+}
+
+static void clear_mask(gb_ctx* ctx, const Packed& p) {
+  GB_CHECK_CUDA(cudaMemsetAsync(p.mask, 0, (size_t)p.batch * p.mrows * p.kw * 4, ctx->stream));
 }
 
 void pack_operand(gb_ctx* ctx, int dtype, int role, char op, int64_t R, int64_t K,
@@ -149,21 +240,18 @@ void pack_operand(gb_ctx* ctx, int dtype, int role, char op, int64_t R, int64_t 
   p.rows = (cx && role == PACK_AS_B) ? 2 * R : R;
   p.ld = ld;
   p.stride = stride;
-  out.data = dst;
-  out.rows = p.rows;
-  out.Kp = p.Kp;
-  out.K = K;
-  out.Kh = p.Kh;
-  out.batch = batch;
-  out.cplx = cx;
-  out.bytes = packed_bytes(R, K, cx, role, batch);
-  // no memset: the kernel writes every (row, k < Kh) entry, zeros included for k >= K
+  packed_layout(out, dst, R, K, cx, role, batch);
+  // the planes need no memset: the kernel writes every (row, k < Kh) entry, zeros
+  // included for k >= K; only the nonzero map starts cleared
+  clear_mask(ctx, out);
   GB_REQUIRE(batch <= 65535 && (R + 31) / 32 <= 65535, "pack: grid too large");
   dim3 grid((unsigned)((p.Kh + 31) / 32), (unsigned)((R + 31) / 32), (unsigned)batch);
   pack_kernel<<<grid, dim3(32, 8), 0, ctx->stream>>>(p, (const double*)src,
-                                                      (__nv_bfloat16*)dst);
+                                                      (__nv_bfloat16*)dst, out.mask, out.kw,
+                                                      out.mrows);
   GB_CHECK_CUDA(cudaGetLastError());
   count_launch(ctx);
+  if (ctx->counting) count_cols(ctx, out);
 }
 
 // ------------------------------------------------------------------ fused leg mix + pack
@@ -176,36 +264,61 @@ __global__ void mixpack_kernel(int64_t A, int64_t N, int64_t xn, const int64_t* 
                                int64_t mn, const int* __restrict__ row_ptr,
                                const int* __restrict__ col, const double* __restrict__ val,
                                const double* __restrict__ x, __nv_bfloat16* __restrict__ hi,
-                               int64_t Nlog, int64_t Kp, int64_t Kh, int64_t plane) {
+                               int64_t Nlog, int64_t Kp, int64_t Kh, int64_t plane,
+                               uint32_t* __restrict__ mask, int kw) {
   const int J = blockIdx.y;
   const int e0 = row_ptr[J], e1 = row_ptr[J + 1];
+  const int lane = threadIdx.x % 32;
   __nv_bfloat16* lo = hi + plane;
   auto put = [&](int64_t row, int64_t c, double v) {
     __nv_bfloat16 h = __double2bfloat16(v);
     hi[row * Kp + c] = h;
     lo[row * Kp + c] = __double2bfloat16(v - (double)__bfloat162float(h));
   };
+  auto mark = [&](int64_t row, int64_t kb) {
+    atomicOr(&mask[(row / MASK_ROWS) * kw + kb / 32], 1u << (kb % 32));
+  };
   for (int64_t n = blockIdx.z; n < N; n += gridDim.z) {
     const int64_t m = mJ[J] + n * mn;
-    for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < A;
-         a += (int64_t)gridDim.x * blockDim.x) {
+    // every thread of the block runs the same number of iterations (warp-wide votes below)
+    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < A;
+         base += (int64_t)gridDim.x * blockDim.x) {
+      const int64_t a = base + threadIdx.x;
+      const bool valid = a < A;
       const int64_t k = a + kJ[J];
-      if (CPLX) {
-        double re = 0.0, im = 0.0;
-        for (int e = e0; e < e1; ++e) {
-          const double* xv = x + 2 * (a + in_off[col[e]] + n * xn);
-          double vr = val[2 * e], vi = val[2 * e + 1];
-          re = fma(vr, xv[0], fma(-vi, xv[1], re));
-          im = fma(vr, xv[1], fma(vi, xv[0], im));
+      bool nz = false;
+      if (valid) {
+        if (CPLX) {
+          double re = 0.0, im = 0.0;
+          for (int e = e0; e < e1; ++e) {
+            const double* xv = x + 2 * (a + in_off[col[e]] + n * xn);
+            double vr = val[2 * e], vi = val[2 * e + 1];
+            re = fma(vr, xv[0], fma(-vi, xv[1], re));
+            im = fma(vr, xv[1], fma(vi, xv[0], im));
+          }
+          put(m, k, re);
+          put(m, Kh + k, -im);
+          put(Nlog + m, k, im);
+          put(Nlog + m, Kh + k, re);
+          nz = (re != 0.0 || im != 0.0);
+        } else {
+          double acc = 0.0;
+          for (int e = e0; e < e1; ++e) acc = fma(val[e], x[a + in_off[col[e]] + n * xn], acc);
+          put(m, k, acc);
+          nz = acc != 0.0;
         }
-        put(m, k, re);
-        put(m, Kh + k, -im);
-        put(Nlog + m, k, im);
-        put(Nlog + m, Kh + k, re);
-      } else {
-        double acc = 0.0;
-        for (int e = e0; e < e1; ++e) acc = fma(val[e], x[a + in_off[col[e]] + n * xn], acc);
-        put(m, k, acc);
+      }
+      // one atomic per (k-block, warp): the first lane with a nonzero value in its group
+      const int64_t kb = valid ? k / KALIGN : -1;
+      const unsigned grp = __match_any_sync(0xffffffffu, kb);
+      const unsigned nzb = __ballot_sync(0xffffffffu, nz);
+      if (nz && lane == __ffs(grp & nzb) - 1) {
+        mark(m, kb);
+        if (CPLX) {
+          mark(m, kb + Kh / KALIGN);
+          mark(Nlog + m, kb);
+          mark(Nlog + m, kb + Kh / KALIGN);
+        }
       }
     }
   }
@@ -229,19 +342,23 @@ void mixpack_run(gb_ctx* ctx, const MixDev& m, const int64_t* kJ, const int64_t*
                                         (out.Kh - Klog) * 2, out.rows, ctx->stream));
     }
   }
+  GB_REQUIRE(out.batch == 1 && out.mask, "mixpack: single packed operand with a map");
+  clear_mask(ctx, out);
   dim3 grid((unsigned)std::min<int64_t>((m.A + 127) / 128, 64), (unsigned)m.nJ,
             (unsigned)std::min<int64_t>(m.N, 65535));
   const int64_t plane = out.rows * out.Kp;
   if (cx)
     mixpack_kernel<true><<<grid, 128, 0, ctx->stream>>>(
         m.A, m.N, m.xn, m.in_off, kJ, mJ, mn, m.row_ptr, m.col, m.val, (const double*)x,
-        (__nv_bfloat16*)out.data, Nlog, out.Kp, out.Kh, plane);
+        (__nv_bfloat16*)out.data, Nlog, out.Kp, out.Kh, plane, out.mask, out.kw);
   else
     mixpack_kernel<false><<<grid, 128, 0, ctx->stream>>>(
         m.A, m.N, m.xn, m.in_off, kJ, mJ, mn, m.row_ptr, m.col, m.val, (const double*)x,
-        (__nv_bfloat16*)out.data, Nlog, out.Kp, out.Kh, plane);
+        (__nv_bfloat16*)out.data, Nlog, out.Kp, out.Kh, plane, out.mask, out.kw);
   GB_CHECK_CUDA(cudaGetLastError());
   count_launch(ctx);
+  out.cnt_valid = false;
+  if (ctx->counting) count_cols(ctx, out);
 }
 
 // ------------------------------------------------------------------ PTX helpers
@@ -476,6 +593,302 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   }
 }
 
+// ------------------------------------------------------------------ persistent kernel
+// One CTA per SM walks output tiles handed out by a global counter.  The producer warp
+// fetches a tile, computes its k-block list (all k-blocks, or those whose A-tile and B-tile
+// nonzero bits are both set) and publishes (tile, count) through a small ring in shared
+// memory to the MMA warp and the four epilogue warps.  The accumulator is double-buffered
+// in TMEM (2 x BN columns): the epilogue drains tile i while the MMAs of tile i+1 run.
+struct PArgs {
+  int64_t M, N, Nlog;  // N = packed B rows (2N when complex)
+  int cplx;
+  int kblocks;         // Kp / 64
+  int mt, nt;          // output tiles along M (128) and N (BN)
+  int ntiles;          // mt * nt * batch
+  int batchA, batchB;
+  double alpha, beta;
+  double* C;
+  int64_t ldc, sC;
+  const uint32_t* maskA;  // null: every k-block
+  const uint32_t* maskB;
+  int kw;
+  int64_t mskA_b, mskB_b;  // words per batch entry
+  int64_t mrowsB;
+  unsigned int* counter;
+  int* status;
+  double* work;  // when set: += tensor-pipe flops per split product of every tile
+};
+
+constexpr int PS_RING = 4;
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+template <int BN>
+struct TileMasks {
+  const uint32_t* a;
+  const uint32_t* b;
+  int nb;  // mask rows of B covered by this tile
+  __device__ __forceinline__ uint32_t word(int w, int kw) const {
+    uint32_t bw = 0;
+    for (int q = 0; q < nb; ++q) bw |= b[q * kw + w];
+    return a[w] & bw;
+  }
+};
+
+template <int BN>
+__device__ __forceinline__ TileMasks<BN> tile_masks(const PArgs& p, int mi, int ni, int z) {
+  TileMasks<BN> t;
+  t.a = p.maskA + (p.batchA > 1 ? z : 0) * p.mskA_b + (int64_t)mi * p.kw;
+  int64_t r0 = (int64_t)ni * (BN / MASK_ROWS);
+  t.b = p.maskB + (p.batchB > 1 ? z : 0) * p.mskB_b + r0 * p.kw;
+  t.nb = (int)std::min<int64_t>(BN / MASK_ROWS, p.mrowsB - r0);
+  return t;
+}
+
+template <int BN, int STAGES>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    gemm_bf16x3_persistent(const __grid_constant__ CUtensorMap mapA,
+                           const __grid_constant__ CUtensorMap mapB, PArgs args) {
+  constexpr int A_BYTES = TC_BM * TC_BK * 2;
+  constexpr int B_BYTES = BN * TC_BK * 2;
+  constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* bars = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+  uint64_t* full = bars;                        // [STAGES]  TMA -> MMA
+  uint64_t* empty = full + STAGES;              // [STAGES]  MMA -> TMA
+  uint64_t* tfull = empty + STAGES;             // [2]       MMA -> epilogue
+  uint64_t* tempty = tfull + 2;                 // [2]       epilogue -> MMA
+  uint64_t* sfull = tempty + 2;                 // [RING]    producer -> consumers
+  uint64_t* sempty = sfull + PS_RING;           // [RING]    consumers -> producer
+  uint64_t* done = sempty + PS_RING;            // [1]       all MMAs retired
+  int* stile = (int*)(done + 1);                // [RING]
+  int* snk = stile + PS_RING;                   // [RING]
+  uint32_t* tmem_slot = (uint32_t*)(snk + PS_RING);
+
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int mn = args.mt * args.nt;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(smem_u32(&full[s]), 1);
+      mbar_init(smem_u32(&empty[s]), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(smem_u32(&tfull[b]), 1);
+      mbar_init(smem_u32(&tempty[b]), 4);
+    }
+    for (int r = 0; r < PS_RING; ++r) {
+      mbar_init(smem_u32(&sfull[r]), 1);
+      mbar_init(smem_u32(&sempty[r]), 5);  // MMA thread + 4 epilogue warps
+    }
+    mbar_init(smem_u32(done), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)&mapA) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)&mapB) : "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(2 * BN));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    // ---------------- scheduler + TMA producer
+    uint32_t g = 0, issued = 0;
+    bool ok = true;
+    for (int j = 0; ok; ++j) {
+      int t = -1, nk = 0, mi = 0, ni = 0, z = 0;
+      for (;;) {
+        int c = (int)atomicAdd(args.counter, 1u);
+        if (c >= args.ntiles) break;
+        z = c / mn;
+        int r = c - z * mn;
+        ni = r / args.mt;
+        mi = r - ni * args.mt;
+        if (args.maskA) {
+          TileMasks<BN> tm = tile_masks<BN>(args, mi, ni, z);
+          nk = 0;
+          for (int w = 0; w < args.kw; ++w) nk += __popc(tm.word(w, args.kw));
+        } else {
+          nk = args.kblocks;
+        }
+        if (nk > 0 || args.beta != 1.0) {
+          t = c;
+          break;
+        }
+      }
+      const int slot = j % PS_RING;
+      ok = mbar_wait_bounded(smem_u32(&sempty[slot]), ((j / PS_RING) & 1) ^ 1, args.status);
+      if (!ok) break;
+      stile[slot] = t;
+      snk[slot] = nk;
+      mbar_arrive(smem_u32(&sfull[slot]));
+      if (t < 0) break;
+      if (nk == 0) continue;
+      if (args.work) atomicAdd(args.work, (double)nk * (2.0 * TC_BM * BN * TC_BK));
+      const int64_t m0 = (int64_t)mi * TC_BM, n0 = (int64_t)ni * BN;
+      const int za0 = (args.batchA > 1 ? z : 0) * 2, zb0 = (args.batchB > 1 ? z : 0) * 2;
+      TileMasks<BN> tm;
+      if (args.maskA) tm = tile_masks<BN>(args, mi, ni, z);
+      for (int pair = 0; pair < 3 && ok; ++pair) {
+        const int planeA = (pair == 2) ? 1 : 0, planeB = (pair == 1) ? 1 : 0;
+        for (int w = 0; w < (args.maskA ? args.kw : 1) && ok; ++w) {
+          uint32_t bits = args.maskA ? tm.word(w, args.kw) : 0u;
+          int kb = args.maskA ? -1 : 0;
+          for (;;) {
+            if (args.maskA) {
+              if (!bits) break;
+              kb = w * 32 + __ffs(bits) - 1;
+              bits &= bits - 1;
+            } else if (kb >= args.kblocks) {
+              break;
+            }
+            const int s = g % STAGES;
+            ok = mbar_wait_bounded(smem_u32(&empty[s]), ((g / STAGES) & 1) ^ 1, args.status);
+            if (!ok) break;
+            const uint32_t sa = smem_u32(smem + s * STAGE_BYTES);
+            const uint32_t fb = smem_u32(&full[s]);
+            mbar_expect_tx(fb, STAGE_BYTES);
+            tma_load_3d(sa, &mapA, fb, kb * TC_BK, (int)m0, za0 + planeA);
+            tma_load_3d(sa + A_BYTES, &mapB, fb, kb * TC_BK, (int)n0, zb0 + planeB);
+            ++g;
+            ++issued;
+            if (!args.maskA) ++kb;
+          }
+        }
+      }
+    }
+    if (!ok) {
+      // drain copies still in flight before this CTA may exit
+      for (uint32_t it = issued > (uint32_t)STAGES ? issued - STAGES : 0; it < issued; ++it) {
+        const int s = it % STAGES;
+        mbar_wait_bounded(smem_u32(&full[s]), (it / STAGES) & 1, args.status);
+      }
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---------------- MMA issuer
+    const uint32_t idesc = idesc_bf16(TC_BM, BN);
+    uint32_t g = 0, acc = 0;
+    bool ok = true;
+    for (int j = 0; ok; ++j) {
+      const int slot = j % PS_RING;
+      ok = mbar_wait_bounded(smem_u32(&sfull[slot]), (j / PS_RING) & 1, args.status);
+      if (!ok) break;
+      const int t = stile[slot], nk = snk[slot];
+      mbar_arrive(smem_u32(&sempty[slot]));
+      if (t < 0) break;
+      if (nk == 0) continue;
+      const uint32_t buf = acc & 1;
+      ok = mbar_wait_bounded(smem_u32(&tempty[buf]), ((acc >> 1) & 1) ^ 1, args.status);
+      if (!ok) break;
+      tc_fence_after();
+      const uint32_t d = tmem + buf * BN;
+      const int total = 3 * nk;
+      for (int it = 0; it < total; ++it) {
+        const int s = g % STAGES;
+        ok = mbar_wait_bounded(smem_u32(&full[s]), (g / STAGES) & 1, args.status);
+        if (!ok) break;
+        tc_fence_after();
+        const uint32_t sa = smem_u32(smem + s * STAGE_BYTES);
+        const uint64_t da = smem_desc_sw128(sa), db = smem_desc_sw128(sa + A_BYTES);
+#pragma unroll
+        for (int k = 0; k < TC_BK / 16; ++k)
+          mma_bf16(d, da + (uint64_t)(2 * k), db + (uint64_t)(2 * k), idesc,
+                   (it > 0 || k > 0) ? 1u : 0u);
+        mma_commit(smem_u32(&empty[s]));
+        ++g;
+      }
+      if (!ok) break;
+      mma_commit(smem_u32(&tfull[buf]));
+      ++acc;
+    }
+    // every MMA issued by this thread has retired once `done` completes
+    mma_commit(smem_u32(done));
+    mbar_wait_bounded(smem_u32(done), 0, args.status);
+  } else if (warp >= 2) {
+    // ---------------- epilogue: TMEM -> registers -> FP64 global
+    const int q = warp % 4;  // TMEM lane quarter accessible by this warp
+    uint32_t acc = 0;
+    for (int j = 0;; ++j) {
+      const int slot = j % PS_RING;
+      bool ok = mbar_wait_bounded(smem_u32(&sfull[slot]), (j / PS_RING) & 1, args.status);
+      ok = __all_sync(0xffffffffu, ok);
+      const int t = ok ? stile[slot] : -1, nk = ok ? snk[slot] : 0;
+      __syncwarp();
+      if (ok && lane == 0) mbar_arrive(smem_u32(&sempty[slot]));
+      if (t < 0) break;
+      const int z = t / mn;
+      const int r = t - z * mn;
+      const int ni = r / args.mt, mi = r - ni * args.mt;
+      const int64_t m = (int64_t)mi * TC_BM + 32 * q + lane;
+      const int64_t n0 = (int64_t)ni * BN;
+      double* C = args.C + (int64_t)z * args.sC * (args.cplx ? 2 : 1);
+      auto out = [&](int64_t n) -> double* {
+        if (args.cplx) {
+          const int64_t nn = n < args.Nlog ? n : n - args.Nlog;
+          return C + 2 * (m + args.ldc * nn) + (n < args.Nlog ? 0 : 1);
+        }
+        return C + m + args.ldc * n;
+      };
+      if (nk == 0) {
+        // no contributing k-block: C = beta * C
+        if (m < args.M)
+          for (int64_t n = n0; n < n0 + BN && n < args.N; ++n) {
+            double* p = out(n);
+            *p = args.beta != 0.0 ? args.beta * *p : 0.0;
+          }
+        continue;
+      }
+      const uint32_t buf = acc & 1;
+      ok = mbar_wait_bounded(smem_u32(&tfull[buf]), (acc >> 1) & 1, args.status);
+      ok = __all_sync(0xffffffffu, ok);
+      if (!ok) break;
+      tc_fence_after();
+#pragma unroll 1
+      for (int c0 = 0; c0 < BN; c0 += 32) {
+        uint32_t v[32];
+        const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + buf * BN + (uint32_t)c0;
+        TMEM_LD32(taddr, v);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (m >= args.M) continue;
+#pragma unroll
+        for (int jj = 0; jj < 32; ++jj) {
+          const int64_t n = n0 + c0 + jj;
+          if (n >= args.N) break;
+          double val = args.alpha * (double)__uint_as_float(v[jj]);
+          double* p = out(n);
+          if (args.beta != 0.0) val = fma(args.beta, *p, val);
+          *p = val;
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(smem_u32(&tempty[buf]));
+      ++acc;
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(2 * BN));
+  }
+}
+
+template <int BN, int STAGES>
+constexpr int persistent_smem() {
+  return STAGES * (TC_BM * TC_BK * 2 + BN * TC_BK * 2) + 1024 + 512;
+}
+
 // ------------------------------------------------------------------ host side
 static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 static std::once_flag g_encode_once;
@@ -546,9 +959,6 @@ void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_
   a.sC = sC;
   a.status = ctx->d_status;
   GB_REQUIRE(M <= (int64_t)INT32_MAX && Npk <= (int64_t)INT32_MAX, "gemm_split: size");
-  dim3 grid((unsigned)((M + TC_BM - 1) / TC_BM), (unsigned)((Npk + TC_BN - 1) / TC_BN),
-            (unsigned)batch);
-  GB_REQUIRE(grid.y <= 65535 && grid.z <= 65535, "gemm_split: grid too large");
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   if (ctx->profiling) {
     if (ctx->prof_used + 2 > ctx->prof_events.size()) {
@@ -563,10 +973,74 @@ void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_
     ctx->prof_flops += (A.cplx ? 8.0 : 2.0) * (double)M * (double)N * (double)A.K;
     GB_CHECK_CUDA(cudaEventRecord(ev0, ctx->stream));
   }
-  gemm_bf16x3_kernel<<<grid, TC_THREADS, TC_SMEM_BYTES, ctx->stream>>>(ma, mb, a);
+  if (ctx->gemm_schedule == GB_SCHED_TILE) {
+    dim3 grid((unsigned)((M + TC_BM - 1) / TC_BM), (unsigned)((Npk + TC_BN - 1) / TC_BN),
+              (unsigned)batch);
+    GB_REQUIRE(grid.y <= 65535 && grid.z <= 65535, "gemm_split: grid too large");
+    gemm_bf16x3_kernel<<<grid, TC_THREADS, TC_SMEM_BYTES, ctx->stream>>>(ma, mb, a);
+  } else {
+    const int bn = ctx->gemm_bn ? ctx->gemm_bn : (Npk <= 128 ? 128 : 256);
+    if (bn == 128) mb = make_map(B, 128);
+    PArgs p;
+    p.M = M;
+    p.N = Npk;
+    p.Nlog = N;
+    p.cplx = A.cplx;
+    p.kblocks = (int)(A.Kp / TC_BK);
+    p.mt = (int)((M + TC_BM - 1) / TC_BM);
+    p.nt = (int)((Npk + bn - 1) / bn);
+    const int64_t ntiles = (int64_t)p.mt * p.nt * batch;
+    GB_REQUIRE(ntiles < (int64_t)INT32_MAX / 2, "gemm_split: too many tiles");
+    p.ntiles = (int)ntiles;
+    p.batchA = (int)A.batch;
+    p.batchB = (int)B.batch;
+    p.alpha = alpha;
+    p.beta = beta;
+    p.C = (double*)C;
+    p.ldc = ldc;
+    p.sC = sC;
+    const bool masked = ctx->gemm_schedule == GB_SCHED_PERSISTENT && A.mask && B.mask;
+    GB_REQUIRE(!masked || A.kw == B.kw, "gemm_split: nonzero maps differ in width");
+    p.maskA = masked ? A.mask : nullptr;
+    p.maskB = masked ? B.mask : nullptr;
+    p.kw = A.kw;
+    p.mskA_b = A.mrows * A.kw;
+    p.mskB_b = B.mrows * B.kw;
+    p.mrowsB = B.mrows;
+    p.counter = ctx->d_tile_counter;
+    p.status = ctx->d_status;
+    p.work = (ctx->profiling || ctx->counting) ? ctx->d_work : nullptr;
+    GB_CHECK_CUDA(cudaMemsetAsync(ctx->d_tile_counter, 0, sizeof(unsigned int), ctx->stream));
+    const unsigned grid = (unsigned)std::min<int64_t>(ntiles, std::max(1, ctx->num_sms));
+    if (bn == 128) {
+      constexpr int SM = persistent_smem<128, 6>();
+      static bool set128 = false;
+      if (!set128) {
+        GB_CHECK_CUDA(cudaFuncSetAttribute(gemm_bf16x3_persistent<128, 6>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
+        set128 = true;
+      }
+      gemm_bf16x3_persistent<128, 6><<<grid, TC_THREADS, SM, ctx->stream>>>(ma, mb, p);
+    } else {
+      constexpr int SM = persistent_smem<256, 4>();
+      static bool set256 = false;
+      if (!set256) {
+        GB_CHECK_CUDA(cudaFuncSetAttribute(gemm_bf16x3_persistent<256, 4>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
+        set256 = true;
+      }
+      gemm_bf16x3_persistent<256, 4><<<grid, TC_THREADS, SM, ctx->stream>>>(ma, mb, p);
+    }
+  }
   GB_CHECK_CUDA(cudaGetLastError());
   if (ev1) GB_CHECK_CUDA(cudaEventRecord(ev1, ctx->stream));
   count_launch(ctx);
+  if (ctx->counting && A.cnt_valid && B.cnt_valid) {
+    nonzero_products_kernel<<<256, 256, 0, ctx->stream>>>(A.cnt, B.cnt, A.Kp, batch,
+                                                          A.batch > 1, B.batch > 1, ctx->d_work);
+    GB_CHECK_CUDA(cudaGetLastError());
+    count_launch(ctx);
+  }
 }
 
 // ------------------------------------------------------------------ unified entry

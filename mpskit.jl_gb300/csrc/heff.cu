@@ -166,15 +166,7 @@ static void prepare_t2p(gb_heff* h) {
                                 cudaMemcpyHostToDevice, h->ctx->stream));
   GB_CHECK_CUDA(cudaStreamSynchronize(h->ctx->stream));
   size_t bytes = packed_bytes(h->t2N, h->t2K, cx, PACK_AS_B, 1);
-  Packed& p = h->t2p;
-  p.data = dalloc(h, bytes);
-  p.bytes = bytes;
-  p.K = h->t2K;
-  p.Kh = (h->t2K + 63) / 64 * 64;
-  p.Kp = cx ? 2 * p.Kh : p.Kh;
-  p.rows = cx ? 2 * h->t2N : h->t2N;
-  p.batch = 1;
-  p.cplx = cx;
+  packed_layout(h->t2p, dalloc(h, bytes), h->t2N, h->t2K, cx, PACK_AS_B, 1);
   h->t2p_ready = true;
 }
 

@@ -35,6 +35,7 @@ struct Ops<double> {
   static __device__ double mul(double a, double b) { return a * b; }
   static __device__ double add(double a, double b) { return a + b; }
   static __device__ double from(cplx c) { return c.re; }
+  static __device__ bool is_zero(double a) { return a == 0.0; }
 };
 template <>
 struct Ops<dcx> {
@@ -44,6 +45,7 @@ struct Ops<dcx> {
   static __device__ dcx mul(dcx a, dcx b) { return cmul(a, b); }
   static __device__ dcx add(dcx a, dcx b) { return cadd(a, b); }
   static __device__ dcx from(cplx c) { return mk(c.re, c.im); }
+  static __device__ bool is_zero(dcx a) { return a.re == 0.0 && a.im == 0.0; }
 };
 
 static inline unsigned nblocks(int64_t n, int bs, int64_t cap = 1 << 20) {
@@ -256,12 +258,40 @@ __device__ inline T load_op(const T* __restrict__ P, int64_t ld, char op, int64_
   return op == 'C' ? Ops<T>::conj(v) : v;
 }
 
+// Nonzero map of op(P) (R x Cn) at 64 x 64 granularity: bit (r / 64, c / 64) of
+// mask[(tile) * kw + word] where the tile index runs along `tile_dim` (0: rows, 1: cols) and
+// the 64-wide block index along the other dimension.  One CTA per 64 x 64 region.
+template <typename T>
+__global__ void zero_map_kernel(char op, const T* __restrict__ P, int64_t ld, int64_t stride,
+                                int64_t R, int64_t Cn, int tile_dim, uint32_t* __restrict__ mask,
+                                int kw, int64_t mstride) {
+  const int64_t b = blockIdx.z;
+  P += b * stride;
+  const int64_t r0 = (int64_t)blockIdx.x * 64, c0 = (int64_t)blockIdx.y * 64;
+  const bool rowfast = (op == 'N');
+  int nz = 0;
+  for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) {
+    const int fast = e % 64, slow = e / 64;
+    const int64_t r = r0 + (rowfast ? fast : slow), c = c0 + (rowfast ? slow : fast);
+    if (r < R && c < Cn) {
+      const T v = rowfast ? P[r + ld * c] : P[c + ld * r];
+      nz |= !Ops<T>::is_zero(v);
+    }
+  }
+  if (__syncthreads_or(nz) && threadIdx.x == 0) {
+    const int64_t tile = tile_dim == 0 ? blockIdx.x : blockIdx.y;
+    const int64_t kb = tile_dim == 0 ? blockIdx.y : blockIdx.x;
+    atomicOr(&mask[b * mstride + tile * kw + kb / 32], 1u << (kb % 32));
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256)
     gemm_simt_kernel(char opA, char opB, int64_t M, int64_t N, int64_t K, T alpha,
                      const T* __restrict__ A, int64_t lda, int64_t sA, const T* __restrict__ B,
                      int64_t ldb, int64_t sB, T beta, bool use_beta, T* __restrict__ C,
-                     int64_t ldc, int64_t sC) {
+                     int64_t ldc, int64_t sC, const uint32_t* __restrict__ mA,
+                     const uint32_t* __restrict__ mB, int kw, int64_t mAb, int64_t mBb) {
   __shared__ T As[GBK][GBM + 1];
   __shared__ T Bs[GBK][GBN + 1];
   const int64_t bz = blockIdx.z;
@@ -271,12 +301,22 @@ __global__ void __launch_bounds__(256)
   const int64_t m0 = (int64_t)blockIdx.x * GBM, n0 = (int64_t)blockIdx.y * GBN;
   const int tid = threadIdx.x;
   const int tm = (tid % 16) * 4, tn = (tid / 16) * 4;
+  // zero-tile skipping: 64-wide k-blocks in which this A row tile or B column tile is zero
+  const uint32_t* ma = mA ? mA + (sA ? bz : 0) * mAb + (int64_t)blockIdx.x * kw : nullptr;
+  const uint32_t* mb = mB ? mB + (sB ? bz : 0) * mBb + (int64_t)blockIdx.y * kw : nullptr;
   T acc[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j] = Ops<T>::zero();
   for (int64_t k0 = 0; k0 < K; k0 += GBK) {
+    if (ma) {
+      const int64_t kb = k0 / 64;
+      if (!((ma[kb / 32] & mb[kb / 32]) >> (kb % 32) & 1u)) {
+        k0 = (kb + 1) * 64 - GBK;  // the loop increment lands on the next 64-block
+        continue;
+      }
+    }
     // A tile: GBM x GBK = 1024 elements, 4 per thread
 #pragma unroll
     for (int l = 0; l < 4; ++l) {
@@ -352,17 +392,48 @@ void gemm_fp64(gb_ctx* ctx, int dtype, char opA, char opB, int64_t M, int64_t N,
     }
     return;
   }
+  // large products skip zero 64 x 64 x 64 blocks (block-sparse operands stored densely)
+  uint32_t* masks = nullptr;
+  const int kw = (int)((K + 64 * 32 - 1) / (64 * 32));
+  const int64_t mt = grid.x, nt = grid.y;
+  const int64_t bA = sA ? batch : 1, bB = sB ? batch : 1;
+  const bool skip = ctx->gemm_schedule == GB_SCHED_PERSISTENT &&
+                    (double)M * (double)N * (double)K >= 1.3e8 && (K + 63) / 64 <= 65535;
+  if (skip) {
+    const size_t words = (size_t)(bA * mt + bB * nt) * kw;
+    GB_CHECK_CUDA(cudaMallocAsync((void**)&masks, words * 4, ctx->stream));
+    GB_CHECK_CUDA(cudaMemsetAsync(masks, 0, words * 4, ctx->stream));
+    const int64_t kb = (K + 63) / 64;
+    dim3 ga((unsigned)mt, (unsigned)kb, (unsigned)bA), gb_((unsigned)kb, (unsigned)nt, (unsigned)bB);
+    uint32_t* mB = masks + bA * mt * kw;
+    if (is_cplx(dtype)) {
+      zero_map_kernel<dcx><<<ga, 256, 0, ctx->stream>>>(opA, (const dcx*)A, lda, sA, M, K, 0,
+                                                        masks, kw, mt * kw);
+      zero_map_kernel<dcx><<<gb_, 256, 0, ctx->stream>>>(opB, (const dcx*)B,
+                                                         ldb, sB, K, N, 1, mB, kw, nt * kw);
+    } else {
+      zero_map_kernel<double><<<ga, 256, 0, ctx->stream>>>(opA, (const double*)A, lda, sA, M, K,
+                                                           0, masks, kw, mt * kw);
+      zero_map_kernel<double><<<gb_, 256, 0, ctx->stream>>>(opB, (const double*)B, ldb, sB, K,
+                                                            N, 1, mB, kw, nt * kw);
+    }
+    LAUNCH_CHECK();
+    count_launch(ctx, 2);
+  }
+  const uint32_t* mA_ = masks;
+  const uint32_t* mB_ = masks ? masks + bA * mt * kw : nullptr;
   if (is_cplx(dtype)) {
     gemm_simt_kernel<dcx><<<grid, 256, 0, ctx->stream>>>(
         opA, opB, M, N, K, mk(alpha.re, alpha.im), (const dcx*)A, lda, sA, (const dcx*)B, ldb,
-        sB, mk(beta.re, beta.im), use_beta, (dcx*)C, ldc, sC);
+        sB, mk(beta.re, beta.im), use_beta, (dcx*)C, ldc, sC, mA_, mB_, kw, mt * kw, nt * kw);
   } else {
     gemm_simt_kernel<double><<<grid, 256, 0, ctx->stream>>>(
         opA, opB, M, N, K, alpha.re, (const double*)A, lda, sA, (const double*)B, ldb, sB,
-        beta.re, use_beta, (double*)C, ldc, sC);
+        beta.re, use_beta, (double*)C, ldc, sC, mA_, mB_, kw, mt * kw, nt * kw);
   }
   LAUNCH_CHECK();
   count_launch(ctx);
+  if (masks) GB_CHECK_CUDA(cudaFreeAsync(masks, ctx->stream));
 }
 
 // Same SIMT GEMM launched on a caller-provided stream, without a context (no scratch,
@@ -377,11 +448,12 @@ cudaError_t gemm_fp64_on_stream(cudaStream_t stream, int dtype, char opA, char o
   if (is_cplx(dtype)) {
     gemm_simt_kernel<dcx><<<grid, 256, 0, stream>>>(
         opA, opB, M, N, K, mk(alpha.re, alpha.im), (const dcx*)A, lda, 0, (const dcx*)B, ldb, 0,
-        mk(beta.re, beta.im), use_beta, (dcx*)C, ldc, 0);
+        mk(beta.re, beta.im), use_beta, (dcx*)C, ldc, 0, nullptr, nullptr, 0, 0, 0);
   } else {
     gemm_simt_kernel<double><<<grid, 256, 0, stream>>>(opA, opB, M, N, K, alpha.re,
                                                        (const double*)A, lda, 0, (const double*)B,
-                                                       ldb, 0, beta.re, use_beta, (double*)C, ldc, 0);
+                                                       ldb, 0, beta.re, use_beta, (double*)C, ldc, 0,
+                                                       nullptr, nullptr, 0, 0, 0);
   }
   return cudaGetLastError();
 }

@@ -82,6 +82,15 @@ free(h) = ccall((:gb_tensor_free, libmpsgb), Cint, (Ptr{Cvoid},), h)
 densempo(W::JordanMPOTensor) = convert(Array, TensorMap(W))
 denseenv(G) = convert(Array, G isa TensorMap ? G : TensorMap(G))
 
+# Symmetric tensors cross the boundary as their dense embedding.  For U1Irrep spaces
+# TensorKit iterates the sectors of a leg in sorted charge order, so convert(Array, t) is
+# the charge-sorted layout libmpsgb's U(1) path expects (zeros outside the blocks); the
+# way back is the projecting constructor TensorMap(array, space).
+fromdense(a::AbstractArray, V) = TensorMap(a, V)
+# per-index charges of a U1 leg (2q, so spin-1/2 charges are odd integers), as the
+# gb_u1_* factorisations take them
+leg_charges(V) = Int32[Int32(2 * c.charge) for c in sectors(V) for _ in 1:dim(V, c)]
+
 """
     GB300Derivative <: DerivativeOperator
 
@@ -147,10 +156,10 @@ function (op::GB300Derivative{T})(x::AbstractTensorMap) where {T}
     hy = upload(op.ctx, xkind(op), zeros(T, size(convert(Array, x))))
     check(ccall((:gb_heff_apply, libmpsgb), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}),
                 op.h, hx, hy))
-    y = similar(x)
-    download!(reshape(y.data, size(convert(Array, x))), hy)
+    a = zeros(T, size(convert(Array, x)))
+    download!(a, hy)
     free(hx); free(hy)
-    return y
+    return fromdense(a, space(x))
 end
 
 # fixedpoint.jl:15-18: the whole Lanczos eigensolve on the device
@@ -166,8 +175,7 @@ function fixedpoint(op::GB300Derivative{T}, x₀, which::Symbol, alg::Lanczos) w
                 λ, info))
     download!(a, hx)
     free(hx)
-    x = similar(x₀)
-    copyto!(x.data, vec(a))
+    x = fromdense(a, space(x₀))
     i = info[]
     return λ[], x, (; converged = i.converged, numops = i.numops, numiter = i.numiter,
                     normres = (i.normres,))

@@ -15,6 +15,7 @@ from .states import (FiniteEnvironments, FiniteMPS, ac2_from, left_orth, mul_fro
 from .algorithms import (DMRG, DMRG2, TDVP, AdaptiveKrylov, expectation_value,
                          find_groundstate, timestep)
 from .infinite import (VUMPS, InfiniteEnvironments, InfiniteMPS, find_groundstate_vumps)
+from . import u1
 
 __all__ = [
     "Context", "DeviceTensor", "context", "AC2_hamiltonian", "AC_hamiltonian", "C_hamiltonian",
@@ -23,5 +24,5 @@ __all__ = [
     "j1j2_cylinder", "transverse_field_ising", "xxz", "FiniteEnvironments", "FiniteMPS",
     "ac2_from", "left_orth", "mul_front", "mul_tail", "project_complement_", "right_orth",
     "svd_trunc", "DMRG", "DMRG2", "AdaptiveKrylov", "expectation_value", "find_groundstate",
-    "TDVP", "timestep", "VUMPS", "InfiniteEnvironments", "InfiniteMPS", "find_groundstate_vumps",
+    "TDVP", "timestep", "VUMPS", "InfiniteEnvironments", "InfiniteMPS", "find_groundstate_vumps", "u1",
 ]

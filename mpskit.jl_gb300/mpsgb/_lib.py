@@ -35,6 +35,9 @@ GB_HEFF_AC2 = 2
 
 GB_PREC_FP64 = 0
 GB_PREC_BF16X3 = 1
+GB_SCHED_PERSISTENT = 0
+GB_SCHED_PERSISTENT_DENSE = 1
+GB_SCHED_TILE = 2
 
 
 class KrylovInfo(ctypes.Structure):
@@ -53,6 +56,7 @@ _lib = None
 P = ctypes.c_void_p
 I64 = ctypes.c_int64
 PI64 = ctypes.POINTER(ctypes.c_int64)
+PI32 = ctypes.POINTER(ctypes.c_int32)
 D = ctypes.c_double
 PD = ctypes.POINTER(ctypes.c_double)
 INT = ctypes.c_int
@@ -69,6 +73,9 @@ _SIGS = {
     "gb_ctx_set_precision": ([P, INT], INT),
     "gb_ctx_profile_begin": ([P], INT),
     "gb_ctx_set_svd_method": ([P, INT], INT),
+    "gb_ctx_set_gemm_schedule": ([P, INT, INT], INT),
+    "gb_ctx_set_counting": ([P, INT], INT),
+    "gb_ctx_read_work": ([P, PD, PD, INT], INT),
     "gb_ctx_profile_end": ([P, PD, PI64, PD, PD], INT),
     "gb_tensor_create": ([P, INT, INT, INT, PI64, ctypes.POINTER(P)], INT),
     "gb_tensor_free": ([P], INT),
@@ -98,6 +105,10 @@ _SIGS = {
     "gb_mps_mul_tail": ([P, P, P, P], INT),
     "gb_project_complement": ([P, P, P], INT),
     "gb_svd_trunc": ([P, P, I64, D, INT, ctypes.POINTER(P), ctypes.POINTER(P), ctypes.POINTER(P), PD], INT),
+    "gb_u1_left_orth": ([P, P, PI32, PI32, PI32, ctypes.POINTER(P), ctypes.POINTER(P), PI32, PI64], INT),
+    "gb_u1_right_orth": ([P, P, PI32, PI32, PI32, ctypes.POINTER(P), ctypes.POINTER(P), PI32, PI64], INT),
+    "gb_u1_svd_trunc": ([P, P, PI32, PI32, PI32, PI32, I64, D, INT, ctypes.POINTER(P), ctypes.POINTER(P),
+                         ctypes.POINTER(P), PI32, PI64, PD], INT),
     "gb_left_orth": ([P, P, ctypes.POINTER(P), ctypes.POINTER(P)], INT),
     "gb_right_orth": ([P, P, ctypes.POINTER(P), ctypes.POINTER(P)], INT),
     "gb_c_apply_noalloc": ([P, P, P, P, I64, I64, I64, INT, P], INT),

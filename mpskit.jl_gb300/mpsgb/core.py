@@ -39,6 +39,25 @@ class Context:
         code = {"fp64": L.GB_PREC_FP64, "bf16x3": L.GB_PREC_BF16X3}[precision]
         L.check(L.lib().gb_ctx_set_precision(self.handle, code))
 
+    def set_gemm_schedule(self, schedule="persistent", tile_n=0):
+        """Split-precision GEMM schedule: "persistent" (tile-skipping, default),
+        "persistent_dense" or "tile"; tile_n in (0 = per shape, 128, 256)."""
+        code = {"persistent": L.GB_SCHED_PERSISTENT,
+                "persistent_dense": L.GB_SCHED_PERSISTENT_DENSE,
+                "tile": L.GB_SCHED_TILE}[schedule]
+        L.check(L.lib().gb_ctx_set_gemm_schedule(self.handle, code, int(tile_n)))
+
+    def set_counting(self, on=True):
+        """Count the nonzero products of every split GEMM (block-sparse flop accounting)."""
+        L.check(L.lib().gb_ctx_set_counting(self.handle, int(bool(on))))
+
+    def read_work(self, reset=True):
+        """-> dict(tile_flops, nonzero_flops) accumulated since the last reset."""
+        t, z = ctypes.c_double(), ctypes.c_double()
+        L.check(L.lib().gb_ctx_read_work(self.handle, ctypes.byref(t), ctypes.byref(z),
+                                         int(bool(reset))))
+        return {"tile_flops": t.value, "nonzero_flops": z.value}
+
     def set_svd_method(self, method):
         """'gesvd' (default), 'gesvdp' or 'gram' for gb_svd_trunc."""
         code = {"gesvd": 0, "gesvdp": 1, "gram": 2}[method]
@@ -81,12 +100,17 @@ def _dtype_code(dtype):
 
 
 class DeviceTensor:
-    """A dense TensorMap block resident on the GPU."""
+    """A dense TensorMap block resident on the GPU.
 
-    __slots__ = ("ctx", "handle", "kind", "dtype", "dims", "__weakref__")
+    `charges` (optional) makes it a U(1)-symmetric tensor: one int32 array of charges per
+    leg, in reference leg order, every virtual leg sorted by charge, entries outside the
+    charge-conserving blocks exactly zero (see mpsgb.u1)."""
 
-    def __init__(self, ctx, kind, dtype, dims, handle=None):
+    __slots__ = ("ctx", "handle", "kind", "dtype", "dims", "charges", "__weakref__")
+
+    def __init__(self, ctx, kind, dtype, dims, handle=None, charges=None):
         self.ctx = ctx
+        self.charges = charges
         self.kind = _KIND_NAMES[kind] if isinstance(kind, str) else kind
         self.dtype = np.dtype(dtype)
         self.dims = tuple(int(x) for x in dims)
@@ -134,7 +158,7 @@ class DeviceTensor:
 
     # ------------------------------------------------ VectorInterface-style operations
     def similar(self):
-        return DeviceTensor(self.ctx, self.kind, self.dtype, self.dims)
+        return DeviceTensor(self.ctx, self.kind, self.dtype, self.dims, charges=self.charges)
 
     def copy(self):
         t = self.similar()

@@ -40,15 +40,46 @@ def _as(a, dtype):
     return np.ascontiguousarray(a, dtype=np.complex128)
 
 
-def split_two_site(op, atol=None):
-    """op[s1,s2,s1',s2'] = sum_k L[s1,s1',k] R[k,s2,s2'] with an isometric left factor."""
+def split_two_site(op, atol=None, qphys=None):
+    """op[s1,s2,s1',s2'] = sum_k L[s1,s1',k] R[k,s2,s2'] with an isometric left factor.
+
+    With physical charges `qphys` (U(1)), the split is done per charge transfer
+    delta = q(s1) - q(s1'), so that every channel carries a definite charge (the channel
+    spaces of a symmetric MPO, src/operators/mpohamiltonian.jl:439-519, are graded the same
+    way); `op` must conserve charge."""
     d1, d2 = op.shape[0], op.shape[1]
     atol = np.finfo(np.float64).eps ** 0.75 if atol is None else atol
     M = op.transpose(0, 2, 1, 3).reshape(d1 * d1, d2 * d2)
-    U, S, Vh = np.linalg.svd(M, full_matrices=False)
-    r = int((S > atol).sum())
-    left = U[:, :r].reshape(d1, d1, r)
-    right = (S[:r, None] * Vh[:r]).reshape(r, d2, d2)
+    if qphys is None:
+        U, S, Vh = np.linalg.svd(M, full_matrices=False)
+        r = int((S > atol).sum())
+        left = U[:, :r].reshape(d1, d1, r)
+        right = (S[:r, None] * Vh[:r]).reshape(r, d2, d2)
+        return left.astype(op.dtype), right.astype(op.dtype)
+    q = np.asarray(qphys)
+    dqr = (q[:d1, None] - q[None, :d1]).reshape(-1)   # row s1*d1 + s1'
+    dqc = (q[:d2, None] - q[None, :d2]).reshape(-1)   # col s2*d2 + s2'
+    lefts, rights = [], []
+    rest = M.copy()
+    for delta in sorted(set(dqr.tolist())):
+        rows = np.nonzero(dqr == delta)[0]
+        cols = np.nonzero(dqc == -delta)[0]
+        if rows.size == 0 or cols.size == 0:
+            continue
+        blk = M[np.ix_(rows, cols)]
+        rest[np.ix_(rows, cols)] = 0
+        U, S, Vh = np.linalg.svd(blk, full_matrices=False)
+        for k in range(int((S > atol).sum())):
+            lv = np.zeros(d1 * d1, dtype=M.dtype)
+            rv = np.zeros(d2 * d2, dtype=M.dtype)
+            lv[rows] = U[:, k]
+            rv[cols] = S[k] * Vh[k]
+            lefts.append(lv)
+            rights.append(rv)
+    if np.abs(rest).max(initial=0.0) > atol:
+        raise ValueError("two-site operator does not conserve the given charges")
+    left = np.stack(lefts, axis=1).reshape(d1, d1, len(lefts))
+    right = np.stack(rights, axis=0).reshape(len(rights), d2, d2)
     return left.astype(op.dtype), right.astype(op.dtype)
 
 
@@ -85,15 +116,15 @@ class MPOHamiltonian:
         return self._dev[key]
 
 
-def _site_pieces(sites, op):
+def _site_pieces(sites, op, qphys=None):
     if len(sites) == 1:
         return [op.reshape(1, op.shape[0], op.shape[1], 1)]
-    a, b = split_two_site(op)
+    a, b = split_two_site(op, qphys=qphys)
     return [a.reshape(1, a.shape[0], a.shape[1], a.shape[2]),
             b.reshape(b.shape[0], b.shape[1], b.shape[2], 1)]
 
 
-def _normalize_terms(terms, dtype):
+def _normalize_terms(terms, dtype, qphys=None):
     out = []
     for sites, op in terms:
         sites = tuple(int(s) for s in sites)
@@ -103,7 +134,7 @@ def _normalize_terms(terms, dtype):
             op = op.transpose(1, 0, 3, 2)
         if len(sites) == 2 and sites[0] == sites[1]:
             raise ValueError("a two-site term needs two distinct sites")
-        pieces = _site_pieces(sites, op)
+        pieces = _site_pieces(sites, op, qphys)
         span = list(range(sites[0], sites[-1] + 1))
         chain = []
         it = iter(pieces)
@@ -158,9 +189,10 @@ def _fill(keys_s, ops_s, cl, cr, d, dtype, identity_corners):
     return W
 
 
-def FiniteMPOHamiltonian(nsites, d, terms, dtype=np.complex128):
-    """Jordan-form MPO of sum(terms) on an open chain of `nsites` sites of dimension d."""
-    terms = _normalize_terms(terms, dtype)
+def FiniteMPOHamiltonian(nsites, d, terms, dtype=np.complex128, qphys=None):
+    """Jordan-form MPO of sum(terms) on an open chain of `nsites` sites of dimension d
+    (`qphys`: U(1) charges of the physical basis, for charge-definite channels)."""
+    terms = _normalize_terms(terms, dtype, qphys)
     keys, ops = _assign(terms, nsites, wrap=False)
     chans = [[1] for _ in range(nsites + 1)]
     for i in range(nsites - 1):
@@ -176,9 +208,9 @@ def FiniteMPOHamiltonian(nsites, d, terms, dtype=np.complex128):
     return MPOHamiltonian(W, finite=True, chans=chans)
 
 
-def InfiniteMPOHamiltonian(ncell, d, terms, dtype=np.complex128):
+def InfiniteMPOHamiltonian(ncell, d, terms, dtype=np.complex128, qphys=None):
     """Jordan-form MPO of a translation-invariant sum of terms with unit cell `ncell`."""
-    terms = _normalize_terms(terms, dtype)
+    terms = _normalize_terms(terms, dtype, qphys)
     keys, ops = _assign(terms, ncell, wrap=True)
     n = max(max([k[1] for k in K] + [1]) + 1 for K in keys)
     V = [[None] * n for _ in range(ncell)]   # V[i] = channels right of site i
@@ -214,16 +246,21 @@ def InfiniteMPOHamiltonian(ncell, d, terms, dtype=np.complex128):
 
 # ------------------------------------------------------------------ models
 
-def heisenberg_XXX(L, J=1.0, dtype=np.complex128, infinite=False):
-    """J sum S_i . S_{i+1} for spin 1/2."""
+# U(1) charges (2 Sz) of the spin-1/2 basis |up>, |down>
+SPIN_HALF_CHARGES = np.array([1, -1], dtype=np.int32)
+
+
+def heisenberg_XXX(L, J=1.0, dtype=np.complex128, infinite=False, u1=False):
+    """J sum S_i . S_{i+1} for spin 1/2 (`u1`: channels of definite Sz transfer)."""
     sx, sy, sz = spin_half()
     h = J * (kron2(sx, sx) + kron2(sy, sy) + kron2(sz, sz))
+    q = SPIN_HALF_CHARGES if u1 else None
     if infinite:
-        return InfiniteMPOHamiltonian(L, 2, [((i, i + 1), h) for i in range(L)], dtype)
-    return FiniteMPOHamiltonian(L, 2, [((i, i + 1), h) for i in range(L - 1)], dtype)
+        return InfiniteMPOHamiltonian(L, 2, [((i, i + 1), h) for i in range(L)], dtype, q)
+    return FiniteMPOHamiltonian(L, 2, [((i, i + 1), h) for i in range(L - 1)], dtype, q)
 
 
-def xxz(L, Jxy=1.0, Jz=1.0, hz=0.0, dtype=np.complex128, infinite=False):
+def xxz(L, Jxy=1.0, Jz=1.0, hz=0.0, dtype=np.complex128, infinite=False, u1=False):
     sx, sy, sz = spin_half()
     h = Jxy * (kron2(sx, sx) + kron2(sy, sy)) + Jz * kron2(sz, sz)
     nb = L if infinite else L - 1
@@ -231,7 +268,7 @@ def xxz(L, Jxy=1.0, Jz=1.0, hz=0.0, dtype=np.complex128, infinite=False):
     if hz:
         terms += [((i,), -hz * sz) for i in range(L)]
     build = InfiniteMPOHamiltonian if infinite else FiniteMPOHamiltonian
-    return build(L, 2, terms, dtype)
+    return build(L, 2, terms, dtype, SPIN_HALF_CHARGES if u1 else None)
 
 
 def transverse_field_ising(L, g=1.0, J=1.0, dtype=np.complex128, infinite=False):
@@ -244,7 +281,7 @@ def transverse_field_ising(L, g=1.0, J=1.0, dtype=np.complex128, infinite=False)
     return build(L, 2, terms, dtype)
 
 
-def j1j2_cylinder(Lx, Ly, J1=1.0, J2=0.5, dtype=np.float64):
+def j1j2_cylinder(Lx, Ly, J1=1.0, J2=0.5, dtype=np.float64, u1=False):
     """J1-J2 Heisenberg on an Lx x Ly cylinder (periodic in y, open in x), snake-ordered."""
     def site(x, y):
         y %= Ly
@@ -268,4 +305,4 @@ def j1j2_cylinder(Lx, Ly, J1=1.0, J2=0.5, dtype=np.float64):
                 add(site(x, y), site(x + 1, y + 1), J2)
                 add(site(x, y), site(x + 1, y - 1), J2)
     terms = [((a, b), J * h) for (a, b), J in sorted(bonds.items())]
-    return FiniteMPOHamiltonian(Lx * Ly, 2, terms, dtype)
+    return FiniteMPOHamiltonian(Lx * Ly, 2, terms, dtype, SPIN_HALF_CHARGES if u1 else None)

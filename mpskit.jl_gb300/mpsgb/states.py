@@ -21,24 +21,67 @@ def _wrap_out(ctx, *handles):
     return [DeviceTensor.wrap(ctx, h) for h in handles]
 
 
+def _q(q):
+    a = np.ascontiguousarray(q, dtype=np.int32)
+    return a, a.ctypes.data_as(L.PI32)
+
+
 def left_orth(AC):
-    """AC = AL * C with a positive-diagonal QR (Householder(positive = true))."""
+    """AC = AL * C with a positive-diagonal QR (Householder(positive = true)); block by
+    block when AC carries U(1) charges."""
     a, c = ctypes.c_void_p(), ctypes.c_void_p()
+    if AC.charges is not None:
+        (ql, pl), (qs, ps), (qr, pr) = (_q(x) for x in AC.charges)
+        qk = np.zeros(min(AC.dims[0] * AC.dims[1], AC.dims[2]), dtype=np.int32)
+        k = ctypes.c_int64()
+        L.check(L.lib().gb_u1_left_orth(AC.ctx.handle, AC.handle, pl, ps, pr, ctypes.byref(a),
+                                        ctypes.byref(c), qk.ctypes.data_as(L.PI32),
+                                        ctypes.byref(k)))
+        al, cc = _wrap_out(AC.ctx, a, c)
+        qk = qk[:k.value].copy()
+        al.charges, cc.charges = (ql, qs, qk), (qk, qr)
+        return al, cc
     L.check(L.lib().gb_left_orth(AC.ctx.handle, AC.handle, ctypes.byref(a), ctypes.byref(c)))
     return tuple(_wrap_out(AC.ctx, a, c))
 
 
 def right_orth(AC):
-    """AC = C * AR with a positive-diagonal LQ."""
+    """AC = C * AR with a positive-diagonal LQ (block by block for U(1) tensors)."""
     c, a = ctypes.c_void_p(), ctypes.c_void_p()
+    if AC.charges is not None:
+        (ql, pl), (qs, ps), (qr, pr) = (_q(x) for x in AC.charges)
+        qk = np.zeros(min(AC.dims[0], AC.dims[1] * AC.dims[2]), dtype=np.int32)
+        k = ctypes.c_int64()
+        L.check(L.lib().gb_u1_right_orth(AC.ctx.handle, AC.handle, pl, ps, pr, ctypes.byref(c),
+                                         ctypes.byref(a), qk.ctypes.data_as(L.PI32),
+                                         ctypes.byref(k)))
+        cc, ar = _wrap_out(AC.ctx, c, a)
+        qk = qk[:k.value].copy()
+        cc.charges, ar.charges = (ql, qk), (qk, qs, qr)
+        return cc, ar
     L.check(L.lib().gb_right_orth(AC.ctx.handle, AC.handle, ctypes.byref(c), ctypes.byref(a)))
     return tuple(_wrap_out(AC.ctx, c, a))
 
 
 def svd_trunc(AC2, maxdim=None, atol=0.0, normalize=True):
-    """Truncated SVD of a two-site tensor -> (AL, S, AR, eps)."""
+    """Truncated SVD of a two-site tensor -> (AL, S, AR, eps); per charge block, with the
+    truncation global over blocks, for U(1) tensors."""
     a, s, r = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
     eps = ctypes.c_double()
+    if AC2.charges is not None:
+        (ql, pl), (qs1, p1), (qr, pr), (qs2, p2) = (_q(x) for x in AC2.charges)
+        Dl, d1, Dr, d2 = AC2.dims
+        qk = np.zeros(min(Dl * d1, d2 * Dr), dtype=np.int32)
+        k = ctypes.c_int64()
+        L.check(L.lib().gb_u1_svd_trunc(AC2.ctx.handle, AC2.handle, pl, p1, pr, p2,
+                                        int(maxdim or 0), float(atol), int(bool(normalize)),
+                                        ctypes.byref(a), ctypes.byref(s), ctypes.byref(r),
+                                        qk.ctypes.data_as(L.PI32), ctypes.byref(k),
+                                        ctypes.byref(eps)))
+        al, S, ar = _wrap_out(AC2.ctx, a, s, r)
+        qk = qk[:k.value].copy()
+        al.charges, S.charges, ar.charges = (ql, qs1, qk), (qk, qk), (qk, qs2, qr)
+        return al, S, ar, eps.value
     L.check(L.lib().gb_svd_trunc(AC2.ctx.handle, AC2.handle, int(maxdim or 0), float(atol),
                                  int(bool(normalize)), ctypes.byref(a), ctypes.byref(s),
                                  ctypes.byref(r), ctypes.byref(eps)))
@@ -46,15 +89,23 @@ def svd_trunc(AC2, maxdim=None, atol=0.0, normalize=True):
     return al, S, ar, eps.value
 
 
+def _both(x, y):
+    return x.charges is not None and y.charges is not None
+
+
 def mul_front(C, A):
     out = DeviceTensor(A.ctx, L.GB_KIND_MPS, A.dtype, (C.dims[0], A.dims[1], A.dims[2]))
     L.check(L.lib().gb_mps_mul_front(A.ctx.handle, C.handle, A.handle, out.handle))
+    if _both(C, A):
+        out.charges = (C.charges[0], A.charges[1], A.charges[2])
     return out
 
 
 def mul_tail(A, C):
     out = DeviceTensor(A.ctx, L.GB_KIND_MPS, A.dtype, (A.dims[0], A.dims[1], C.dims[1]))
     L.check(L.lib().gb_mps_mul_tail(A.ctx.handle, A.handle, C.handle, out.handle))
+    if _both(A, C):
+        out.charges = (A.charges[0], A.charges[1], C.charges[1])
     return out
 
 
@@ -62,6 +113,8 @@ def ac2_from(A, B):
     """AC2[l s1; r s2] = A[l s1; m] B[m s2; r]."""
     out = DeviceTensor(A.ctx, L.GB_KIND_AC2, A.dtype, (A.dims[0], A.dims[1], B.dims[2], B.dims[1]))
     L.check(L.lib().gb_mps_ac2(A.ctx.handle, A.handle, B.handle, out.handle))
+    if _both(A, B):
+        out.charges = (A.charges[0], A.charges[1], B.charges[2], B.charges[1])
     return out
 
 
@@ -112,12 +165,19 @@ class FiniteMPS:
         return self.C[self.center].dtype
 
     @classmethod
-    def from_tensors(cls, As, ctx=None, normalize=True, center=0):
+    def from_tensors(cls, As, ctx=None, normalize=True, center=0, charges=None):
         """FiniteMPS(As; normalize): positive-QR sweep left to right on the device, then
-        LQ moves right to left down to the centre bond `center`."""
+        LQ moves right to left down to the centre bond `center`.  `charges` =
+        (bond charges [L+1 arrays], physical charges) makes it a U(1)-symmetric state
+        (mpsgb.u1): the gauge steps then act per charge block."""
         ctx = ctx or context()
         n = len(As)
         A = [DeviceTensor.from_numpy(ctx, L.GB_KIND_MPS, a) for a in As]
+        if charges is not None:
+            qb, qp = charges
+            for i, a in enumerate(A):
+                a.charges = (np.asarray(qb[i], np.int32), np.asarray(qp, np.int32),
+                             np.asarray(qb[i + 1], np.int32))
         AL = [None] * n
         C = [None] * (n + 1)
         R = None

@@ -61,18 +61,22 @@ class FiniteMPS:
     """AL/AR/C storage with an explicit centre bond: AL[i] is valid for i < center,
     AR[i] for i >= center, C[center] is the current centre matrix."""
 
-    def __init__(self, AL, AR, C, center=0):
+    def __init__(self, AL, AR, C, center=0, qb=None, qp=None):
         self.AL = AL
         self.AR = AR
         self.C = C
         self.center = center
+        # U(1): charges of every bond (qb[b] between sites b-1 and b) and of the physical leg
+        self.qb = qb
+        self.qp = qp
 
     def __len__(self):
         return len(self.AL)
 
     def copy(self):
         cp = lambda xs: [None if x is None else x.copy() for x in xs]
-        return FiniteMPS(cp(self.AL), cp(self.AR), cp(self.C), self.center)
+        return FiniteMPS(cp(self.AL), cp(self.AR), cp(self.C), self.center,
+                         None if self.qb is None else cp(self.qb), self.qp)
 
     def ac(self, i):
         """The centre-site tensor AC[i] for a centre bond at i or i+1 (or an explicitly
@@ -92,7 +96,12 @@ class FiniteMPS:
             return self.AL[i]
         ac = self.ac(i)
         Dl, d, Dr = ac.shape
-        Q, _ = qr_pos(ac.reshape(Dl * d, Dr, order="F"))
+        if self.qb is not None:
+            from .u1 import fuse, left_orth_u1
+            Q, _, _ = left_orth_u1(ac.reshape(Dl * d, Dr, order="F"), fuse(self.qb[i], self.qp),
+                                   self.qb[i + 1])
+        else:
+            Q, _ = qr_pos(ac.reshape(Dl * d, Dr, order="F"))
         return Q.reshape(Dl, d, Q.shape[1], order="F")
 
     def AC(self, i):
@@ -135,38 +144,57 @@ def random_initial_tensors(L, d, D, seed, dtype=np.complex128):
     return As
 
 
-def finite_mps_from_tensors(As, normalize=True):
+def finite_mps_from_tensors(As, normalize=True, charges=None):
     """FiniteMPS(As; normalize) (finitemps.jl:229-250): positive-QR sweep left->right,
     then an LQ sweep right->left to build the AR gauge (what the reference does lazily
-    on first access of `psi.AR`)."""
+    on first access of `psi.AR`).  `charges` = (bond charges, physical charges) gives a
+    U(1)-symmetric state whose factorisations act per charge block (oracle.u1)."""
+    from .u1 import fuse, left_orth_u1
     L = len(As)
     As = [a.copy() for a in As]
     AL = [None] * L
     C = [None] * (L + 1)
+    qb = qp = None
+    if charges is not None:
+        qb = [np.asarray(q, np.int32) for q in charges[0]]
+        qp = np.asarray(charges[1], np.int32)
     for i in range(L):
         Dl, d, Dr = As[i].shape
         M = As[i].reshape(Dl * d, Dr, order="F")
-        Q, R = qr_pos(M)
+        if qb is not None:
+            Q, R, qb[i + 1] = left_orth_u1(M, fuse(qb[i], qp), qb[i + 1])
+        else:
+            Q, R = qr_pos(M)
         AL[i] = Q.reshape(Dl, d, Q.shape[1], order="F")
         if normalize:
             R = R / np.linalg.norm(R)
         if i < L - 1:
             As[i + 1] = np.einsum("ab,bsc->asc", R, As[i + 1])
     C[L] = R
-    psi = FiniteMPS(AL, [None] * L, C, center=L)
+    psi = FiniteMPS(AL, [None] * L, C, center=L, qb=qb, qp=qp)
     right_canonicalize(psi)
     return psi
 
 
+def _col_charges(qp, qr):
+    """Charges of the fused column (s, r) of A[l; s r]: q[s + d*r] = q_r - q_s."""
+    return (np.asarray(qr)[None, :] - np.asarray(qp)[:, None]).reshape(-1, order="F")
+
+
 def right_canonicalize(psi):
     """Build AR[i] and C[i] from the centre at bond L by positive LQ moves."""
+    from .u1 import right_orth_u1
     L = len(psi)
     X = psi.C[L]
     for i in range(L - 1, -1, -1):
         A = np.einsum("asb,bc->asc", psi.AL[i], X)
         Dl, d, Dr = A.shape
         M = A.reshape(Dl, d * Dr, order="F")
-        Lm, Q = lq_pos(M)
+        if psi.qb is not None:
+            Lm, Q, qk = right_orth_u1(M, psi.qb[i], _col_charges(psi.qp, psi.qb[i + 1]))
+            assert np.array_equal(qk, psi.qb[i]), "LQ sweep changed a bond space"
+        else:
+            Lm, Q = lq_pos(M)
         psi.AR[i] = Q.reshape(Q.shape[0], d, Dr, order="F")
         X = Lm
         psi.C[i] = Lm
@@ -320,7 +348,16 @@ def dmrg2_local_update(pos, right, psi, H, alg, envs, eps_global, eps_trunc, dec
     # gauge2! with truncated SVD (orthoview.jl:401-420)
     Dl, d1, Dr, d2 = new.shape
     M = new.reshape(Dl * d1, Dr * d2, order="F")
-    U, S, Vh, eps_tr = svd_trunc(M, alg.maxdim, alg.cutoff)
+    if psi.qb is not None:
+        from .u1 import fuse, svd_trunc_u1
+        # columns (r, s2): q = q_r - q_s2
+        qcol = (np.asarray(psi.qb[pos + 2])[:, None] - np.asarray(psi.qp)[None, :]).reshape(
+            -1, order="F")
+        U, S, Vh, qk, eps_tr = svd_trunc_u1(M, fuse(psi.qb[pos], psi.qp), qcol, alg.maxdim,
+                                            alg.cutoff)
+        psi.qb[pos + 1] = qk
+    else:
+        U, S, Vh, eps_tr = svd_trunc(M, alg.maxdim, alg.cutoff)
     S = S / np.linalg.norm(S)
     k = S.size
     al = U.reshape(Dl, d1, k, order="F")
@@ -392,13 +429,25 @@ def dmrg1_local_update(pos, right, psi, H, alg, envs, eps_global, eps_trunc, dec
                                       eager=alg.alg_eigsolve.eager)
     stats["matvecs"] += info.numops
     if right:
-        Q, R = qr_pos(new.reshape(Dl * d, Dr, order="F"))
+        if psi.qb is not None:
+            from .u1 import fuse, left_orth_u1
+            Q, R, qk = left_orth_u1(new.reshape(Dl * d, Dr, order="F"), fuse(psi.qb[pos], psi.qp),
+                                    psi.qb[pos + 1])
+            assert np.array_equal(qk, psi.qb[pos + 1]), "QR changed a bond space"
+        else:
+            Q, R = qr_pos(new.reshape(Dl * d, Dr, order="F"))
         R = R / np.linalg.norm(R)
         psi.AL[pos] = Q.reshape(Dl, d, Dr, order="F")
         psi.C[pos + 1] = R
         psi.center = pos + 1
     else:
-        Lm, Q = lq_pos(new.reshape(Dl, d * Dr, order="F"))
+        if psi.qb is not None:
+            from .u1 import right_orth_u1
+            Lm, Q, qk = right_orth_u1(new.reshape(Dl, d * Dr, order="F"), psi.qb[pos],
+                                      _col_charges(psi.qp, psi.qb[pos + 1]))
+            assert np.array_equal(qk, psi.qb[pos]), "LQ changed a bond space"
+        else:
+            Lm, Q = lq_pos(new.reshape(Dl, d * Dr, order="F"))
         Lm = Lm / np.linalg.norm(Lm)
         psi.AR[pos] = Q.reshape(Dl, d, Dr, order="F")
         psi.C[pos] = Lm

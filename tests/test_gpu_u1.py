@@ -1,0 +1,158 @@
+"""U(1) symmetry on the device: block-wise gauge factorisations against the oracle, the
+tile-skipping GEMM schedule against the dense one on block-sparse operators, and U(1) DMRG2
+against the oracle."""
+import numpy as np
+import pytest
+
+import mpsgb
+from mpsgb import _lib as L
+from mpsgb import u1 as HU
+from mpsgb.operators import SPIN_HALF_CHARGES as QP
+from oracle import mps as P
+from oracle import u1 as U
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = mpsgb.context(0)
+    yield c
+    c.set_gemm_schedule("persistent", 0)
+    c.set_svd_method("gesvd")
+
+
+def _sym(rng, ql, qs, qr, dtype):
+    a = rng.standard_normal((len(ql), len(qs), len(qr)))
+    if np.dtype(dtype).kind == "c":
+        a = a + 1j * rng.standard_normal(a.shape)
+    return (a * HU.block_mask(ql, qs, qr)).astype(dtype)
+
+
+def _charges(rng, n, lo=-3, hi=3):
+    return np.sort(rng.integers(lo, hi + 1, size=n)).astype(np.int32)
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex128])
+def test_u1_left_right_orth_match_oracle(ctx, dt):
+    rng = np.random.default_rng(1)
+    ql, qr = _charges(rng, 30), _charges(rng, 41)
+    A = _sym(rng, ql, QP, qr, dt)
+    t = mpsgb.DeviceTensor.from_numpy(ctx, "mps", A)
+    t.charges = (ql, QP, qr)
+    al, c = mpsgb.left_orth(t)
+    Q, R, qk = U.left_orth_u1(A.reshape(-1, A.shape[2], order="F"), U.fuse(ql, QP), qr)
+    assert np.array_equal(al.charges[2], qk)
+    assert np.abs(al.numpy().reshape(Q.shape, order="F") - Q).max() < 1e-12
+    assert np.abs(c.numpy() - R).max() < 1e-12
+    # exact zeros outside the blocks
+    assert np.all(al.numpy()[~HU.block_mask(ql, QP, qk)] == 0)
+    cc, ar = mpsgb.right_orth(t)
+    qcol = (qr[None, :] - QP[:, None]).reshape(-1, order="F")
+    Lm, Q2, qk2 = U.right_orth_u1(A.reshape(A.shape[0], -1, order="F"), ql, qcol)
+    assert np.array_equal(ar.charges[0], qk2)
+    assert np.abs(ar.numpy().reshape(Q2.shape, order="F") - Q2).max() < 1e-12
+    assert np.abs(cc.numpy() - Lm).max() < 1e-12
+    assert np.all(ar.numpy()[~HU.block_mask(qk2, QP, qr)] == 0)
+
+
+@pytest.mark.parametrize("method", ["gesvd", "gram"])
+@pytest.mark.parametrize("dt", [np.float64, np.complex128])
+def test_u1_svd_trunc_matches_oracle(ctx, method, dt):
+    rng = np.random.default_rng(2)
+    ql, qr = _charges(rng, 24, -2, 2), _charges(rng, 28, -2, 2)
+    # AC2[l s1; r s2] with q_l + q_s1 + q_s2 = q_r
+    a = rng.standard_normal((len(ql), 2, len(qr), 2))
+    if np.dtype(dt).kind == "c":
+        a = a + 1j * rng.standard_normal(a.shape)
+    mask = HU.block_mask(ql, QP, qr, QP, signs=[1, 1, -1, 1])
+    AC2 = (a * mask).astype(dt)
+    ctx.set_svd_method(method)
+    t = mpsgb.DeviceTensor.from_numpy(ctx, "ac2", AC2)
+    t.charges = (ql, QP, qr, QP)
+    for maxdim in (None, 17):
+        al, S, ar, eps = mpsgb.svd_trunc(t, maxdim, 0.0, normalize=False)
+        M_ = AC2.reshape(len(ql) * 2, -1, order="F")
+        qcol = (qr[:, None] - QP[None, :]).reshape(-1, order="F")
+        Uu, Sv, Vh, qk, oeps = U.svd_trunc_u1(M_, U.fuse(ql, QP), qcol, maxdim)
+        assert np.array_equal(al.charges[2], qk)
+        assert abs(eps - oeps) < 1e-10 * max(1.0, oeps)
+        # same truncated matrix: AL C AR == U S Vh
+        k = qk.size
+        dev = np.einsum("lsk,km,mtr->lsrt", al.numpy(), S.numpy(), ar.numpy())
+        ref = ((Uu * Sv) @ Vh).reshape(AC2.shape, order="F")
+        assert np.abs(dev - ref).max() < 1e-10 * np.abs(ref).max()
+        assert np.allclose(np.einsum("lsk,lsm->km", al.numpy().conj(), al.numpy()), np.eye(k),
+                           atol=1e-11)
+        assert np.all(al.numpy()[~HU.block_mask(ql, QP, qk)] == 0)
+        assert np.all(ar.numpy()[~HU.block_mask(qk, QP, qr)] == 0)
+    ctx.set_svd_method("gesvd")
+
+
+def _u1_operator(ctx, L_=10, D=48, pos=4, seed=9, dtype=np.float64):
+    H = mpsgb.heisenberg_XXX(L_, dtype=dtype, u1=True)
+    As, qb = HU.random_u1_tensors(L_, D, seed, 0, dtype)
+    psi = mpsgb.FiniteMPS.from_tensors(As, ctx, center=pos + 1, charges=(qb, QP))
+    envs = mpsgb.FiniteEnvironments(psi, H)
+    return psi, H, envs
+
+
+def test_tile_skipping_equals_dense_schedule_on_u1_operator(ctx):
+    """Skipping k-blocks whose packed A and B tiles are zero changes nothing: the skipped
+    products are exact zeros."""
+    psi, H, envs = _u1_operator(ctx, L_=12, D=160, pos=5)
+    be = mpsgb.GB300Backend("bf16x3")
+    ac2 = mpsgb.ac2_from(psi.AL[5], psi.ac(6))
+    outs = {}
+    for sched, bn in (("persistent", 0), ("persistent_dense", 0), ("persistent", 128),
+                      ("tile", 0)):
+        ctx.set_gemm_schedule(sched, bn)
+        Heff = mpsgb.AC2_hamiltonian(5, psi, H, envs, be)
+        outs[(sched, bn)] = Heff(ac2).numpy()
+    ctx.set_gemm_schedule("persistent", 0)
+    ref = mpsgb.AC2_hamiltonian(5, psi, H, envs, mpsgb.GB300Backend("fp64"))(ac2).numpy()
+    assert np.array_equal(outs[("persistent", 0)], outs[("persistent_dense", 0)])
+    for v in outs.values():
+        assert np.linalg.norm(v - ref) < 1e-4 * np.linalg.norm(ref)
+    # H_eff preserves the block structure
+    mask = HU.block_mask(psi.AL[5].charges[0], QP, psi.AR[6].charges[2], QP,
+                         signs=[1, 1, -1, 1])
+    assert np.all(ref[~mask] == 0)
+
+
+def test_u1_dmrg2_matches_oracle(ctx):
+    L_, D = 12, 32
+    H = mpsgb.heisenberg_XXX(L_, dtype=np.float64, u1=True)
+    As, qb = HU.random_u1_tensors(L_, D, 21, 0, np.float64)
+    opsi = P.finite_mps_from_tensors(As, charges=(qb, QP))
+    _, _, _, ohist = P.find_groundstate_dmrg2(opsi, H, P.DMRG2(maxdim=D, cutoff=1e-10),
+                                              maxsweeps=5)
+    psi = mpsgb.FiniteMPS.from_tensors(As, ctx, charges=(qb, QP))
+    psi, envs, eps, hist = mpsgb.find_groundstate(psi, H, mpsgb.DMRG2(maxdim=D, cutoff=1e-10),
+                                                  maxsweeps=5)
+    for a, b in zip(hist, ohist):
+        assert abs(a["energy"] - b[1]) < 1e-10 * abs(b[1]), (a, b)
+
+
+def test_u1_dmrg2_split_precision_gram(ctx):
+    """Split-precision contractions + Gram factorisation per block reach the FP64 oracle
+    energy of the same U(1) run to 1e-9."""
+    L_, D = 16, 48
+    H = mpsgb.heisenberg_XXX(L_, dtype=np.float64, u1=True)
+    As, qb = HU.random_u1_tensors(L_, D, 23, 0, np.float64)
+    opsi = P.finite_mps_from_tensors(As, charges=(qb, QP))
+    _, _, _, ohist = P.find_groundstate_dmrg2(opsi, H, P.DMRG2(maxdim=D, cutoff=1e-12),
+                                              maxsweeps=8)
+    ctx.set_svd_method("gram")
+    ctx.set_precision("bf16x3")
+    try:
+        psi = mpsgb.FiniteMPS.from_tensors(As, ctx, charges=(qb, QP))
+        alg = mpsgb.DMRG2(maxdim=D, cutoff=1e-12, backend=mpsgb.GB300Backend("bf16x3"))
+        psi, envs, eps, hist = mpsgb.find_groundstate(psi, H, alg, maxsweeps=8)
+        # the FP64 refinement step: energy from FP64 environments of the converged state
+        e = mpsgb.expectation_value(psi, H, mpsgb.FiniteEnvironments(psi, H), 0)
+    finally:
+        ctx.set_svd_method("gesvd")
+        ctx.set_precision("fp64")
+    e_ref = ohist[-1][1]
+    assert abs(e - e_ref) < 1e-9 * abs(e_ref), (e, e_ref)
