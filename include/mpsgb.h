@@ -62,9 +62,11 @@ enum { GB_HEFF_C = 0, GB_HEFF_AC = 1, GB_HEFF_AC2 = 2 };
 /* arithmetic of the bulk contractions */
 enum {
   GB_PREC_FP64 = 0,    /* plain FP64 (CUDA-core FMA)                                 */
-  GB_PREC_BF16X3 = 1   /* split precision: hi/lo BF16 operands, 3 products
+  GB_PREC_BF16X3 = 1,  /* split precision: hi/lo BF16 operands, 3 products
                           (hi*hi + hi*lo + lo*hi), FP32 accumulate in TMEM
                           (tcgen05), FP64 output                                      */
+  GB_PREC_TF32X3 = 2   /* the same scheme with hi/lo TF32 operands (22 significant bits
+                          against 16; tcgen05 kind::tf32 runs at half the BF16 rate)   */
 };
 
 typedef struct gb_ctx gb_ctx;

@@ -780,7 +780,9 @@ int gb_ctx_device_status(gb_ctx* ctx, int32_t* out) {
 int gb_ctx_set_precision(gb_ctx* ctx, int precision) {
   API_BEGIN
   GB_REQUIRE(ctx, "null context");
-  GB_REQUIRE(precision == GB_PREC_FP64 || precision == GB_PREC_BF16X3, "unknown precision");
+  GB_REQUIRE(precision == GB_PREC_FP64 || precision == GB_PREC_BF16X3 ||
+                 precision == GB_PREC_TF32X3,
+             "unknown precision");
   ctx->aux_prec = precision;
   API_END
 }

@@ -197,28 +197,52 @@ struct Packed {
   int kw = 0;                // 32-bit words per mask row: ceil(Kp / 64 / 32)
   uint32_t* cnt = nullptr;   // [batch][Kp] nonzero rows per packed k (filled when counting)
   bool cnt_valid = false;
+  int esz = 2;               // plane element bytes: 2 (BF16 planes) or 4 (TF32 planes)
+  int bk = 64;               // k-block (elements per 128-byte swizzle row): 64 or 32
 };
 // which operand of C = op(A) op(B) is being packed
 enum PackRole { PACK_AS_A = 0, PACK_AS_B = 1 };
-size_t packed_bytes(int64_t rows, int64_t K, bool cplx, int role, int64_t batch);
+// prec: GB_PREC_BF16X3 (BF16 planes) or GB_PREC_TF32X3 (TF32 planes in 32-bit words)
+size_t packed_bytes(int64_t rows, int64_t K, bool cplx, int role, int64_t batch,
+                    int prec = GB_PREC_BF16X3);
 // fills every field of out for a buffer of packed_bytes(...) at data
 void packed_layout(Packed& out, void* data, int64_t R, int64_t K, bool cplx, int role,
-                   int64_t batch);
+                   int64_t batch, int prec = GB_PREC_BF16X3);
 void pack_operand(gb_ctx* ctx, int dtype, int role, char op, int64_t M_or_N, int64_t K,
                   const void* src, int64_t ld, int64_t stride, int64_t batch, Packed& out,
-                  void* dst);
+                  void* dst, int prec = GB_PREC_BF16X3);
+// Skipping structurally zero work in mixpack_run: x is the output of a GEMM with an output
+// map (xmap, onc columns of 128 per row tile of 128); input i of the mix at (a, n) sits at
+// row a + roff[i], column coff[i] + n*xnM of that matrix.  prev: scratch of the packed
+// output's map size that receives the previous map (the planes must have been zeroed when
+// allocated, and the K padding is then never touched again).
+struct MixSkipDev {
+  const uint32_t* xmap = nullptr;
+  int64_t onc = 0;
+  const int64_t* roff = nullptr;
+  const int64_t* coff = nullptr;
+  int64_t xnM = 0;
+  uint32_t* prev = nullptr;
+};
 // leg mix whose output is written directly as the packed B operand of the next GEMM
 // (kJ[J]: contraction-index offset of output row J, mJ[J] + n*mn: output column index)
 void mixpack_run(gb_ctx* ctx, const MixDev& m, const int64_t* kJ, const int64_t* mJ, int64_t mn,
-                 int dtype, const void* x, Packed& out, int64_t Klog, int64_t Nlog);
+                 int dtype, const void* x, Packed& out, int64_t Klog, int64_t Nlog,
+                 const MixSkipDev* skip = nullptr);
+// outmap (optional, batch 1, split precision only): bit (m/128)*ceil(N/128) + n/128 is set
+// for every 128 x 128 region of C that receives a contribution; for real data the regions
+// that receive none are then not written (the consumer must read C only where set)
+size_t outmap_bytes(int64_t M, int64_t N);
 void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_t M,
-                int64_t N, double alpha, double beta, void* C, int64_t ldc, int64_t sC);
+                int64_t N, double alpha, double beta, void* C, int64_t ldc, int64_t sC,
+                uint32_t* outmap = nullptr);
 bool tc_available(gb_ctx* ctx);
 
 // Unified GEMM: dispatches on precision; optional pre-packed operands.
 void gemm(gb_ctx* ctx, int prec, int dtype, char opA, char opB, int64_t M, int64_t N,
           int64_t K, double alpha, const void* A, int64_t lda, int64_t sA, const void* B,
           int64_t ldb, int64_t sB, double beta, void* C, int64_t ldc, int64_t sC,
-          int64_t batch = 1, const Packed* pA = nullptr, const Packed* pB = nullptr);
+          int64_t batch = 1, const Packed* pA = nullptr, const Packed* pB = nullptr,
+          uint32_t* outmap = nullptr);
 
 }  // namespace gb

@@ -5,6 +5,8 @@
 // Computations", ARITH 2019): every FP64 operand x is split into hi = bf16(x) and
 // lo = bf16(x - hi); the product is hi*hi + hi*lo + lo*hi accumulated in FP32.  The
 // three products are one K-loop over (pair, k-block) that re-reads the hi/lo planes.
+// "tf32x3" is the same scheme with TF32 planes (hi = tf32(x), lo = tf32(x - hi), each held
+// in a 32-bit word, tcgen05 kind::tf32): 22 significant bits per operand instead of 16.
 //
 // Complex operands are realified: A' = [Re A | Im A] along K and
 // B' = [[Re B; -Im B] | [Im B; Re B]] along N, so C' = A' B'^T = [Re C | Im C].
@@ -41,6 +43,33 @@ constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s bound on any wait
 
 static inline int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
 
+// ------------------------------------------------------------------ plane element types
+// BF16 planes (bf16x3) or TF32 values in 32-bit words (tf32x3).  A k-block is one 128-byte
+// swizzle row: 64 BF16 or 32 TF32 elements.
+template <typename E>
+constexpr int bk_of() {
+  return 128 / (int)sizeof(E);
+}
+__device__ __forceinline__ float tf32_rna(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+__device__ __forceinline__ void split_put(__nv_bfloat16* hi, __nv_bfloat16* lo, int64_t i,
+                                          double v) {
+  const __nv_bfloat16 h = __double2bfloat16(v);
+  hi[i] = h;
+  lo[i] = __double2bfloat16(v - (double)__bfloat162float(h));
+}
+__device__ __forceinline__ void split_put(float* hi, float* lo, int64_t i, double v) {
+  const float h = tf32_rna((float)v);
+  hi[i] = h;
+  lo[i] = tf32_rna((float)(v - (double)h));
+}
+__device__ __forceinline__ bool plane_nz(__nv_bfloat16 a) { return __bfloat162float(a) != 0.f; }
+__device__ __forceinline__ bool plane_nz(float a) { return a != 0.f; }
+static inline bool is_tf32(int prec) { return prec == GB_PREC_TF32X3; }
+
 // ------------------------------------------------------------------ packing
 // out layout: [batch][plane(2)][rows][Kp] bf16 ; rows = M (A) or N / 2N (B, complex)
 struct PackArgs {
@@ -74,15 +103,15 @@ __device__ inline void load_elem(const PackArgs& p, const double* src, int64_t r
 }
 
 // 32 x 32 tile transpose through shared memory; block = 32 x 8 threads.
-__global__ void pack_kernel(PackArgs p, const double* __restrict__ src,
-                            __nv_bfloat16* __restrict__ dst, uint32_t* __restrict__ mask,
-                            int kw, int64_t mrows) {
+template <typename E>
+__global__ void pack_kernel(PackArgs p, const double* __restrict__ src, E* __restrict__ dst,
+                            uint32_t* __restrict__ mask, int kw, int64_t mrows) {
   __shared__ double tre[32][33];
   __shared__ double tim[32][33];
   const int64_t b = blockIdx.z;
   src += b * p.stride * (p.cplx ? 2 : 1);
-  __nv_bfloat16* hi = dst + b * 2 * p.rows * p.Kp;
-  __nv_bfloat16* lo = hi + p.rows * p.Kp;
+  E* hi = dst + b * 2 * p.rows * p.Kp;
+  E* lo = hi + p.rows * p.Kp;
   const int64_t r0 = (int64_t)blockIdx.y * 32, k0 = (int64_t)blockIdx.x * 32;
   const int tx = threadIdx.x, ty = threadIdx.y;
   bool rowfast = (p.role == 0) ? (p.op == 'N') : (p.op != 'N');
@@ -110,12 +139,7 @@ __global__ void pack_kernel(PackArgs p, const double* __restrict__ src,
     if (r >= p.R || k >= p.Kh) continue;  // entries k >= K were loaded as zeros
     double re = tre[j][tx], im = tim[j][tx];
     nz |= (re != 0.0 || im != 0.0);
-    auto put = [&](int64_t row, int64_t col, double v) {
-      __nv_bfloat16 h = __double2bfloat16(v);
-      __nv_bfloat16 l = __double2bfloat16(v - (double)__bfloat162float(h));
-      hi[row * p.Kp + col] = h;
-      lo[row * p.Kp + col] = l;
-    };
+    auto put = [&](int64_t row, int64_t col, double v) { split_put(hi, lo, row * p.Kp + col, v); };
     if (!p.cplx) {
       put(r, k, re);
     } else if (p.role == 0) {
@@ -128,12 +152,12 @@ __global__ void pack_kernel(PackArgs p, const double* __restrict__ src,
       put(p.R + r, p.Kh + k, re);
     }
   }
-  // nonzero map: this 32 x 32 block lies in one 128-row tile and one 64-wide k-block
+  // nonzero map: this 32 x 32 block lies in one 128-row tile and one k-block
   // (complex operands also touch the imaginary half; marked conservatively)
   if (__syncthreads_or(nz) && tx == 0 && ty == 0) {
     uint32_t* mb = mask + b * mrows * kw;
     auto mark = [&](int64_t row, int64_t col) {
-      int64_t kb = col / KALIGN;
+      int64_t kb = col / bk_of<E>();
       atomicOr(&mb[(row / MASK_ROWS) * kw + kb / 32], 1u << (kb % 32));
     };
     const int64_t rlast = std::min<int64_t>(r0 + 31, p.R - 1);
@@ -150,22 +174,25 @@ __global__ void pack_kernel(PackArgs p, const double* __restrict__ src,
   }
 }
 
-static size_t plane_bytes(int64_t prow, int64_t Kp, int64_t batch) {
-  return (size_t)round_up((int64_t)batch * 2 * prow * Kp * 2, 256);
+static size_t plane_bytes(int64_t prow, int64_t Kp, int64_t batch, int esz) {
+  return (size_t)round_up((int64_t)batch * 2 * prow * Kp * esz, 256);
 }
-static int mask_words(int64_t Kp) { return (int)((Kp / KALIGN + 31) / 32); }
+static int mask_words(int64_t Kp, int bk) { return (int)((Kp / bk + 31) / 32); }
 
-size_t packed_bytes(int64_t rows, int64_t K, bool cplx, int role, int64_t batch) {
+size_t packed_bytes(int64_t rows, int64_t K, bool cplx, int role, int64_t batch, int prec) {
+  const int esz = is_tf32(prec) ? 4 : 2, bk = 128 / esz;
   int64_t Kh = round_up(std::max<int64_t>(K, 1), KALIGN);
   int64_t Kp = cplx ? 2 * Kh : Kh;
   int64_t prow = (cplx && role == PACK_AS_B) ? 2 * rows : rows;
   int64_t mrows = (prow + MASK_ROWS - 1) / MASK_ROWS;
-  return plane_bytes(prow, Kp, batch) + (size_t)batch * mrows * mask_words(Kp) * 4 +
+  return plane_bytes(prow, Kp, batch, esz) + (size_t)batch * mrows * mask_words(Kp, bk) * 4 +
          (size_t)batch * Kp * 4;
 }
 
 void packed_layout(Packed& out, void* data, int64_t R, int64_t K, bool cx, int role,
-                   int64_t batch) {
+                   int64_t batch, int prec) {
+  out.esz = is_tf32(prec) ? 4 : 2;
+  out.bk = 128 / out.esz;
   out.data = data;
   out.K = K;
   out.Kh = round_up(std::max<int64_t>(K, 1), KALIGN);
@@ -173,26 +200,27 @@ void packed_layout(Packed& out, void* data, int64_t R, int64_t K, bool cx, int r
   out.rows = (cx && role == PACK_AS_B) ? 2 * R : R;
   out.batch = batch;
   out.cplx = cx;
-  out.bytes = packed_bytes(R, K, cx, role, batch);
+  out.bytes = packed_bytes(R, K, cx, role, batch, prec);
   out.mrows = (out.rows + MASK_ROWS - 1) / MASK_ROWS;
-  out.kw = mask_words(out.Kp);
-  out.mask = (uint32_t*)((char*)data + plane_bytes(out.rows, out.Kp, batch));
+  out.kw = mask_words(out.Kp, out.bk);
+  out.mask = (uint32_t*)((char*)data + plane_bytes(out.rows, out.Kp, batch, out.esz));
   out.cnt = out.mask + (size_t)batch * out.mrows * out.kw;
   out.cnt_valid = false;
 }
 
 // nonzero rows per packed k (both planes), rows split in chunks of 256 with one atomic each
-__global__ void count_cols_kernel(const __nv_bfloat16* __restrict__ planes, int64_t rows,
-                                  int64_t Kp, uint32_t* __restrict__ cnt) {
+template <typename E>
+__global__ void count_cols_kernel(const E* __restrict__ planes, int64_t rows, int64_t Kp,
+                                  uint32_t* __restrict__ cnt) {
   const int64_t b = blockIdx.z;
-  const __nv_bfloat16* hi = planes + b * 2 * rows * Kp;
-  const __nv_bfloat16* lo = hi + rows * Kp;
+  const E* hi = planes + b * 2 * rows * Kp;
+  const E* lo = hi + rows * Kp;
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (k >= Kp) return;
   const int64_t r0 = (int64_t)blockIdx.y * 256, r1 = std::min<int64_t>(r0 + 256, rows);
   uint32_t c = 0;
   for (int64_t r = r0; r < r1; ++r)
-    c += (__bfloat162float(hi[r * Kp + k]) != 0.f || __bfloat162float(lo[r * Kp + k]) != 0.f);
+    c += (plane_nz(hi[r * Kp + k]) || plane_nz(lo[r * Kp + k]));
   if (c) atomicAdd(&cnt[b * Kp + k], c);
 }
 
@@ -200,8 +228,12 @@ static void count_cols(gb_ctx* ctx, Packed& p) {
   GB_CHECK_CUDA(cudaMemsetAsync(p.cnt, 0, (size_t)p.batch * p.Kp * 4, ctx->stream));
   dim3 grid((unsigned)((p.Kp + 255) / 256), (unsigned)((p.rows + 255) / 256), (unsigned)p.batch);
   GB_REQUIRE(grid.y <= 65535 && grid.z <= 65535, "count: grid too large");
-  count_cols_kernel<<<grid, 256, 0, ctx->stream>>>((const __nv_bfloat16*)p.data, p.rows, p.Kp,
-                                                   p.cnt);
+  if (p.esz == 4)
+    count_cols_kernel<float><<<grid, 256, 0, ctx->stream>>>((const float*)p.data, p.rows, p.Kp,
+                                                            p.cnt);
+  else
+    count_cols_kernel<__nv_bfloat16><<<grid, 256, 0, ctx->stream>>>(
+        (const __nv_bfloat16*)p.data, p.rows, p.Kp, p.cnt);
   GB_CHECK_CUDA(cudaGetLastError());
   count_launch(ctx);
   p.cnt_valid = true;
@@ -227,7 +259,7 @@ static void clear_mask(gb_ctx* ctx, const Packed& p) {
 
 void pack_operand(gb_ctx* ctx, int dtype, int role, char op, int64_t R, int64_t K,
                   const void* src, int64_t ld, int64_t stride, int64_t batch, Packed& out,
-                  void* dst) {
+                  void* dst, int prec) {
   bool cx = is_cplx(dtype);
   PackArgs p;
   p.role = role;
@@ -240,15 +272,18 @@ void pack_operand(gb_ctx* ctx, int dtype, int role, char op, int64_t R, int64_t 
   p.rows = (cx && role == PACK_AS_B) ? 2 * R : R;
   p.ld = ld;
   p.stride = stride;
-  packed_layout(out, dst, R, K, cx, role, batch);
+  packed_layout(out, dst, R, K, cx, role, batch, prec);
   // the planes need no memset: the kernel writes every (row, k < Kh) entry, zeros
   // included for k >= K; only the nonzero map starts cleared
   clear_mask(ctx, out);
   GB_REQUIRE(batch <= 65535 && (R + 31) / 32 <= 65535, "pack: grid too large");
   dim3 grid((unsigned)((p.Kh + 31) / 32), (unsigned)((R + 31) / 32), (unsigned)batch);
-  pack_kernel<<<grid, dim3(32, 8), 0, ctx->stream>>>(p, (const double*)src,
-                                                      (__nv_bfloat16*)dst, out.mask, out.kw,
-                                                      out.mrows);
+  if (out.esz == 4)
+    pack_kernel<float><<<grid, dim3(32, 8), 0, ctx->stream>>>(p, (const double*)src, (float*)dst,
+                                                              out.mask, out.kw, out.mrows);
+  else
+    pack_kernel<__nv_bfloat16><<<grid, dim3(32, 8), 0, ctx->stream>>>(
+        p, (const double*)src, (__nv_bfloat16*)dst, out.mask, out.kw, out.mrows);
   GB_CHECK_CUDA(cudaGetLastError());
   count_launch(ctx);
   if (ctx->counting) count_cols(ctx, out);
@@ -258,23 +293,20 @@ void pack_operand(gb_ctx* ctx, int dtype, int role, char op, int64_t R, int64_t 
 // y[a + out_off[J] + n*yn] = sum_e val[e] x[a + in_off[col[e]] + n*xn] written directly as
 // the packed B operand of the following GEMM: logical B element (k, m) with
 // k = a + kJ[J] (contraction index) and m = mJ[J] + n*mn (output column index).
-template <bool CPLX>
+template <bool CPLX, typename E>
 __global__ void mixpack_kernel(int64_t A, int64_t N, int64_t xn, const int64_t* __restrict__ in_off,
                                const int64_t* __restrict__ kJ, const int64_t* __restrict__ mJ,
                                int64_t mn, const int* __restrict__ row_ptr,
                                const int* __restrict__ col, const double* __restrict__ val,
-                               const double* __restrict__ x, __nv_bfloat16* __restrict__ hi,
-                               int64_t Nlog, int64_t Kp, int64_t Kh, int64_t plane,
-                               uint32_t* __restrict__ mask, int kw) {
+                               const double* __restrict__ x, E* __restrict__ hi, int64_t Nlog,
+                               int64_t Kp, int64_t Kh, int64_t plane, uint32_t* __restrict__ mask,
+                               int kw, MixSkipDev sk) {
+  constexpr int BK = bk_of<E>();
   const int J = blockIdx.y;
   const int e0 = row_ptr[J], e1 = row_ptr[J + 1];
   const int lane = threadIdx.x % 32;
-  __nv_bfloat16* lo = hi + plane;
-  auto put = [&](int64_t row, int64_t c, double v) {
-    __nv_bfloat16 h = __double2bfloat16(v);
-    hi[row * Kp + c] = h;
-    lo[row * Kp + c] = __double2bfloat16(v - (double)__bfloat162float(h));
-  };
+  E* lo = hi + plane;
+  auto put = [&](int64_t row, int64_t c, double v) { split_put(hi, lo, row * Kp + c, v); };
   auto mark = [&](int64_t row, int64_t kb) {
     atomicOr(&mask[(row / MASK_ROWS) * kw + kb / 32], 1u << (kb % 32));
   };
@@ -284,9 +316,32 @@ __global__ void mixpack_kernel(int64_t A, int64_t N, int64_t xn, const int64_t* 
     for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < A;
          base += (int64_t)gridDim.x * blockDim.x) {
       const int64_t a = base + threadIdx.x;
-      const bool valid = a < A;
+      bool valid = a < A;
       const int64_t k = a + kJ[J];
       bool nz = false;
+      if (valid && sk.xmap) {
+        // all inputs in regions of x that its producer left unwritten (no contribution):
+        // the value is zero; it is written only where the previous apply marked its box
+        bool any = false;
+        for (int e = e0; e < e1 && !any; ++e) {
+          const int i = col[e];
+          const int64_t bit = ((a + sk.roff[i]) >> 7) * sk.onc + ((sk.coff[i] + n * sk.xnM) >> 7);
+          any = (sk.xmap[bit >> 5] >> (bit & 31)) & 1u;
+        }
+        if (!any) {
+          const int64_t kb0 = k / BK;
+          auto prev = [&](int64_t row, int64_t kb) {
+            return (sk.prev[(row / MASK_ROWS) * kw + kb / 32] >> (kb % 32)) & 1u;
+          };
+          if (prev(m, kb0)) put(m, k, 0.0);
+          if (CPLX) {
+            if (prev(m, kb0 + Kh / BK)) put(m, Kh + k, 0.0);
+            if (prev(Nlog + m, kb0)) put(Nlog + m, k, 0.0);
+            if (prev(Nlog + m, kb0 + Kh / BK)) put(Nlog + m, Kh + k, 0.0);
+          }
+          valid = false;  // nothing to compute or mark
+        }
+      }
       if (valid) {
         if (CPLX) {
           double re = 0.0, im = 0.0;
@@ -309,15 +364,15 @@ __global__ void mixpack_kernel(int64_t A, int64_t N, int64_t xn, const int64_t* 
         }
       }
       // one atomic per (k-block, warp): the first lane with a nonzero value in its group
-      const int64_t kb = valid ? k / KALIGN : -1;
+      const int64_t kb = valid ? k / BK : -1;
       const unsigned grp = __match_any_sync(0xffffffffu, kb);
       const unsigned nzb = __ballot_sync(0xffffffffu, nz);
       if (nz && lane == __ffs(grp & nzb) - 1) {
         mark(m, kb);
         if (CPLX) {
-          mark(m, kb + Kh / KALIGN);
+          mark(m, kb + Kh / BK);
           mark(Nlog + m, kb);
-          mark(Nlog + m, kb + Kh / KALIGN);
+          mark(Nlog + m, kb + Kh / BK);
         }
       }
     }
@@ -325,36 +380,50 @@ __global__ void mixpack_kernel(int64_t A, int64_t N, int64_t xn, const int64_t* 
 }
 
 void mixpack_run(gb_ctx* ctx, const MixDev& m, const int64_t* kJ, const int64_t* mJ, int64_t mn,
-                 int dtype, const void* x, Packed& out, int64_t Klog, int64_t Nlog) {
+                 int dtype, const void* x, Packed& out, int64_t Klog, int64_t Nlog,
+                 const MixSkipDev* skip) {
   const bool cx = is_cplx(dtype);
   GB_REQUIRE(m.nJ <= 65535, "mixpack: too many output rows");
   GB_REQUIRE(m.xa == 1, "mixpack: unit input stride required");
-  // zero the K padding of every row once (entries k >= Klog are never produced by the mix)
-  if (out.Kh > Klog) {
-    __nv_bfloat16* base = (__nv_bfloat16*)out.data;
+  // zero the K padding of every row (entries k >= Klog are never produced by the mix); with
+  // skipping, the planes were zeroed at allocation and the padding is never written
+  if (out.Kh > Klog && !(skip && skip->xmap)) {
+    const int64_t es = out.esz;
     const int64_t planes = 2 * out.batch;
     for (int64_t p = 0; p < planes; ++p) {
-      char* pb = (char*)(base + p * out.rows * out.Kp);
-      GB_CHECK_CUDA(cudaMemset2DAsync(pb + Klog * 2, out.Kp * 2, 0, (out.Kh - Klog) * 2, out.rows,
-                                      ctx->stream));
+      char* pb = (char*)out.data + p * out.rows * out.Kp * es;
+      GB_CHECK_CUDA(cudaMemset2DAsync(pb + Klog * es, out.Kp * es, 0, (out.Kh - Klog) * es,
+                                      out.rows, ctx->stream));
       if (cx)
-        GB_CHECK_CUDA(cudaMemset2DAsync(pb + (out.Kh + Klog) * 2, out.Kp * 2, 0,
-                                        (out.Kh - Klog) * 2, out.rows, ctx->stream));
+        GB_CHECK_CUDA(cudaMemset2DAsync(pb + (out.Kh + Klog) * es, out.Kp * es, 0,
+                                        (out.Kh - Klog) * es, out.rows, ctx->stream));
     }
   }
   GB_REQUIRE(out.batch == 1 && out.mask, "mixpack: single packed operand with a map");
+  MixSkipDev sk{};
+  if (skip && skip->xmap) {
+    // the planes were zeroed at allocation and entries are skipped only where they are
+    // known zero: keep the previous map to know which boxes may hold stale nonzeros
+    sk = *skip;
+    GB_CHECK_CUDA(cudaMemcpyAsync(sk.prev, out.mask, (size_t)out.mrows * out.kw * 4,
+                                  cudaMemcpyDeviceToDevice, ctx->stream));
+  }
   clear_mask(ctx, out);
   dim3 grid((unsigned)std::min<int64_t>((m.A + 127) / 128, 64), (unsigned)m.nJ,
             (unsigned)std::min<int64_t>(m.N, 65535));
   const int64_t plane = out.rows * out.Kp;
-  if (cx)
-    mixpack_kernel<true><<<grid, 128, 0, ctx->stream>>>(
-        m.A, m.N, m.xn, m.in_off, kJ, mJ, mn, m.row_ptr, m.col, m.val, (const double*)x,
-        (__nv_bfloat16*)out.data, Nlog, out.Kp, out.Kh, plane, out.mask, out.kw);
-  else
-    mixpack_kernel<false><<<grid, 128, 0, ctx->stream>>>(
-        m.A, m.N, m.xn, m.in_off, kJ, mJ, mn, m.row_ptr, m.col, m.val, (const double*)x,
-        (__nv_bfloat16*)out.data, Nlog, out.Kp, out.Kh, plane, out.mask, out.kw);
+#define GB_MIXPACK(C, E)                                                                      \
+  mixpack_kernel<C, E><<<grid, 128, 0, ctx->stream>>>(                                        \
+      m.A, m.N, m.xn, m.in_off, kJ, mJ, mn, m.row_ptr, m.col, m.val, (const double*)x,        \
+      (E*)out.data, Nlog, out.Kp, out.Kh, plane, out.mask, out.kw, sk)
+  if (out.esz == 4) {
+    if (cx) GB_MIXPACK(true, float);
+    else GB_MIXPACK(false, float);
+  } else {
+    if (cx) GB_MIXPACK(true, __nv_bfloat16);
+    else GB_MIXPACK(false, __nv_bfloat16);
+  }
+#undef GB_MIXPACK
   GB_CHECK_CUDA(cudaGetLastError());
   count_launch(ctx);
   out.cnt_valid = false;
@@ -428,6 +497,19 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+// kind::tf32 instruction descriptor: TF32 x TF32 -> F32, both K-major
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                         uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
       "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
@@ -617,6 +699,12 @@ struct PArgs {
   unsigned int* counter;
   int* status;
   double* work;  // when set: += tensor-pipe flops per split product of every tile
+  // optional output map: bit (m / 128) * onc + (logical column / 128) is set for every
+  // output tile that receives a contribution; with skip_zero_out, tiles that receive none
+  // are not written at all (the consumer reads C only where the map is set)
+  uint32_t* outmap;
+  int64_t onc;
+  int skip_zero_out;
 };
 
 constexpr int PS_RING = 4;
@@ -647,12 +735,13 @@ __device__ __forceinline__ TileMasks<BN> tile_masks(const PArgs& p, int mi, int 
   return t;
 }
 
-template <int BN, int STAGES>
+template <int BN, int STAGES, bool TF32>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     gemm_bf16x3_persistent(const __grid_constant__ CUtensorMap mapA,
                            const __grid_constant__ CUtensorMap mapB, PArgs args) {
-  constexpr int A_BYTES = TC_BM * TC_BK * 2;
-  constexpr int B_BYTES = BN * TC_BK * 2;
+  constexpr int BKE = TF32 ? 32 : 64;  // k elements per stage (one 128-byte swizzle row)
+  constexpr int A_BYTES = TC_BM * 128;
+  constexpr int B_BYTES = BN * 128;
   constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -720,7 +809,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         } else {
           nk = args.kblocks;
         }
-        if (nk > 0 || args.beta != 1.0) {
+        if (nk > 0 || (args.beta != 1.0 && !args.skip_zero_out)) {
           t = c;
           break;
         }
@@ -733,7 +822,23 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       mbar_arrive(smem_u32(&sfull[slot]));
       if (t < 0) break;
       if (nk == 0) continue;
-      if (args.work) atomicAdd(args.work, (double)nk * (2.0 * TC_BM * BN * TC_BK));
+      if (args.work) atomicAdd(args.work, (double)nk * (2.0 * TC_BM * BN * BKE));
+      if (args.outmap) {
+        // logical column groups of this tile (complex: real and imaginary halves)
+        const int64_t n0 = (int64_t)ni * BN, n1 = std::min<int64_t>(n0 + BN, args.N);
+        auto set_range = [&](int64_t c0, int64_t c1) {
+          for (int64_t g = c0 / 128; g <= (c1 - 1) / 128; ++g) {
+            const int64_t bit = (int64_t)mi * args.onc + g;
+            atomicOr(&args.outmap[bit >> 5], 1u << (bit & 31));
+          }
+        };
+        if (!args.cplx) {
+          set_range(n0, n1);
+        } else {
+          if (n0 < args.Nlog) set_range(n0, std::min(n1, args.Nlog));
+          if (n1 > args.Nlog) set_range(std::max(n0, args.Nlog) - args.Nlog, n1 - args.Nlog);
+        }
+      }
       const int64_t m0 = (int64_t)mi * TC_BM, n0 = (int64_t)ni * BN;
       const int za0 = (args.batchA > 1 ? z : 0) * 2, zb0 = (args.batchB > 1 ? z : 0) * 2;
       TileMasks<BN> tm;
@@ -757,8 +862,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const uint32_t sa = smem_u32(smem + s * STAGE_BYTES);
             const uint32_t fb = smem_u32(&full[s]);
             mbar_expect_tx(fb, STAGE_BYTES);
-            tma_load_3d(sa, &mapA, fb, kb * TC_BK, (int)m0, za0 + planeA);
-            tma_load_3d(sa + A_BYTES, &mapB, fb, kb * TC_BK, (int)n0, zb0 + planeB);
+            tma_load_3d(sa, &mapA, fb, kb * BKE, (int)m0, za0 + planeA);
+            tma_load_3d(sa + A_BYTES, &mapB, fb, kb * BKE, (int)n0, zb0 + planeB);
             ++g;
             ++issued;
             if (!args.maskA) ++kb;
@@ -775,7 +880,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
   } else if (warp == 1 && lane == 0) {
     // ---------------- MMA issuer
-    const uint32_t idesc = idesc_bf16(TC_BM, BN);
+    const uint32_t idesc = TF32 ? idesc_tf32(TC_BM, BN) : idesc_bf16(TC_BM, BN);
     uint32_t g = 0, acc = 0;
     bool ok = true;
     for (int j = 0; ok; ++j) {
@@ -799,10 +904,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         tc_fence_after();
         const uint32_t sa = smem_u32(smem + s * STAGE_BYTES);
         const uint64_t da = smem_desc_sw128(sa), db = smem_desc_sw128(sa + A_BYTES);
+        // four MMAs of 32 bytes of K each (16 BF16 or 8 TF32): +2 in 16-byte units
 #pragma unroll
-        for (int k = 0; k < TC_BK / 16; ++k)
-          mma_bf16(d, da + (uint64_t)(2 * k), db + (uint64_t)(2 * k), idesc,
-                   (it > 0 || k > 0) ? 1u : 0u);
+        for (int k = 0; k < 4; ++k) {
+          if (TF32)
+            mma_tf32(d, da + (uint64_t)(2 * k), db + (uint64_t)(2 * k), idesc,
+                     (it > 0 || k > 0) ? 1u : 0u);
+          else
+            mma_bf16(d, da + (uint64_t)(2 * k), db + (uint64_t)(2 * k), idesc,
+                     (it > 0 || k > 0) ? 1u : 0u);
+        }
         mma_commit(smem_u32(&empty[s]));
         ++g;
       }
@@ -886,7 +997,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
 template <int BN, int STAGES>
 constexpr int persistent_smem() {
-  return STAGES * (TC_BM * TC_BK * 2 + BN * TC_BK * 2) + 1024 + 512;
+  return STAGES * (TC_BM * 128 + BN * 128) + 1024 + 512;
 }
 
 // ------------------------------------------------------------------ host side
@@ -907,11 +1018,14 @@ static void load_encode() {
 
 static CUtensorMap make_map(const Packed& P, int box_rows) {
   CUtensorMap m;
+  const cuuint64_t es = (cuuint64_t)P.esz;
   cuuint64_t dims[3] = {(cuuint64_t)P.Kp, (cuuint64_t)P.rows, (cuuint64_t)(2 * P.batch)};
-  cuuint64_t strides[2] = {(cuuint64_t)P.Kp * 2, (cuuint64_t)P.Kp * P.rows * 2};
-  cuuint32_t box[3] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows, 1};
+  cuuint64_t strides[2] = {(cuuint64_t)P.Kp * es, (cuuint64_t)P.Kp * P.rows * es};
+  cuuint32_t box[3] = {(cuuint32_t)P.bk, (cuuint32_t)box_rows, 1};
   cuuint32_t estr[3] = {1, 1, 1};
-  CUresult r = g_encode(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, P.data, dims, strides, box,
+  CUresult r = g_encode(&m, P.esz == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                       : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
+                        3, P.data, dims, strides, box,
                         estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) throw Error(GB_ERR_CUDA, "cuTensorMapEncodeTiled failed");
@@ -926,10 +1040,13 @@ bool tc_available(gb_ctx* ctx) {
 }
 
 void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_t M,
-                int64_t N, double alpha, double beta, void* C, int64_t ldc, int64_t sC) {
+                int64_t N, double alpha, double beta, void* C, int64_t ldc, int64_t sC,
+                uint32_t* outmap) {
   GB_REQUIRE(tc_available(ctx), "split-precision GEMM needs an sm_103 device");
-  GB_REQUIRE(A.Kp == B.Kp && A.cplx == B.cplx, "gemm_split: operand packing mismatch");
-  GB_REQUIRE(A.Kp % TC_BK == 0, "gemm_split: Kp alignment");
+  GB_REQUIRE(A.Kp == B.Kp && A.cplx == B.cplx && A.esz == B.esz,
+             "gemm_split: operand packing mismatch");
+  GB_REQUIRE(A.Kp % A.bk == 0, "gemm_split: Kp alignment");
+  const bool tf32 = A.esz == 4;
   load_encode();
   static bool attr_set = false;
   if (!attr_set) {
@@ -973,7 +1090,8 @@ void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_
     ctx->prof_flops += (A.cplx ? 8.0 : 2.0) * (double)M * (double)N * (double)A.K;
     GB_CHECK_CUDA(cudaEventRecord(ev0, ctx->stream));
   }
-  if (ctx->gemm_schedule == GB_SCHED_TILE) {
+  if (outmap) GB_REQUIRE(std::max(A.batch, B.batch) == 1, "gemm_split: output map needs batch 1");
+  if (ctx->gemm_schedule == GB_SCHED_TILE && !tf32 && !outmap) {
     dim3 grid((unsigned)((M + TC_BM - 1) / TC_BM), (unsigned)((Npk + TC_BN - 1) / TC_BN),
               (unsigned)batch);
     GB_REQUIRE(grid.y <= 65535 && grid.z <= 65535, "gemm_split: grid too large");
@@ -986,7 +1104,7 @@ void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_
     p.N = Npk;
     p.Nlog = N;
     p.cplx = A.cplx;
-    p.kblocks = (int)(A.Kp / TC_BK);
+    p.kblocks = (int)(A.Kp / A.bk);
     p.mt = (int)((M + TC_BM - 1) / TC_BM);
     p.nt = (int)((Npk + bn - 1) / bn);
     const int64_t ntiles = (int64_t)p.mt * p.nt * batch;
@@ -999,7 +1117,7 @@ void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_
     p.C = (double*)C;
     p.ldc = ldc;
     p.sC = sC;
-    const bool masked = ctx->gemm_schedule == GB_SCHED_PERSISTENT && A.mask && B.mask;
+    const bool masked = ctx->gemm_schedule != GB_SCHED_PERSISTENT_DENSE && A.mask && B.mask;
     GB_REQUIRE(!masked || A.kw == B.kw, "gemm_split: nonzero maps differ in width");
     p.maskA = masked ? A.mask : nullptr;
     p.maskB = masked ? B.mask : nullptr;
@@ -1010,27 +1128,32 @@ void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_
     p.counter = ctx->d_tile_counter;
     p.status = ctx->d_status;
     p.work = (ctx->profiling || ctx->counting) ? ctx->d_work : nullptr;
+    p.outmap = outmap;
+    p.onc = (N + 127) / 128;
+    p.skip_zero_out = (outmap && !A.cplx) ? 1 : 0;
+    if (outmap)
+      GB_CHECK_CUDA(cudaMemsetAsync(outmap, 0, outmap_bytes(M, N), ctx->stream));
     GB_CHECK_CUDA(cudaMemsetAsync(ctx->d_tile_counter, 0, sizeof(unsigned int), ctx->stream));
     const unsigned grid = (unsigned)std::min<int64_t>(ntiles, std::max(1, ctx->num_sms));
+#define GB_PERSISTENT(BN_, ST_, TF_)                                                          \
+  do {                                                                                        \
+    constexpr int SM = persistent_smem<BN_, ST_>();                                           \
+    static bool set = false;                                                                  \
+    if (!set) {                                                                               \
+      GB_CHECK_CUDA(cudaFuncSetAttribute(gemm_bf16x3_persistent<BN_, ST_, TF_>,               \
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, SM));   \
+      set = true;                                                                             \
+    }                                                                                         \
+    gemm_bf16x3_persistent<BN_, ST_, TF_><<<grid, TC_THREADS, SM, ctx->stream>>>(ma, mb, p); \
+  } while (0)
     if (bn == 128) {
-      constexpr int SM = persistent_smem<128, 6>();
-      static bool set128 = false;
-      if (!set128) {
-        GB_CHECK_CUDA(cudaFuncSetAttribute(gemm_bf16x3_persistent<128, 6>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
-        set128 = true;
-      }
-      gemm_bf16x3_persistent<128, 6><<<grid, TC_THREADS, SM, ctx->stream>>>(ma, mb, p);
+      if (tf32) GB_PERSISTENT(128, 6, true);
+      else GB_PERSISTENT(128, 6, false);
     } else {
-      constexpr int SM = persistent_smem<256, 4>();
-      static bool set256 = false;
-      if (!set256) {
-        GB_CHECK_CUDA(cudaFuncSetAttribute(gemm_bf16x3_persistent<256, 4>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
-        set256 = true;
-      }
-      gemm_bf16x3_persistent<256, 4><<<grid, TC_THREADS, SM, ctx->stream>>>(ma, mb, p);
+      if (tf32) GB_PERSISTENT(256, 4, true);
+      else GB_PERSISTENT(256, 4, false);
     }
+#undef GB_PERSISTENT
   }
   GB_CHECK_CUDA(cudaGetLastError());
   if (ev1) GB_CHECK_CUDA(cudaEventRecord(ev1, ctx->stream));
@@ -1043,15 +1166,22 @@ void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_
   }
 }
 
+size_t outmap_bytes(int64_t M, int64_t N) {
+  const int64_t bits = ((M + 127) / 128) * ((N + 127) / 128);
+  return (size_t)((bits + 31) / 32) * 4;
+}
+
 // ------------------------------------------------------------------ unified entry
 void gemm(gb_ctx* ctx, int prec, int dtype, char opA, char opB, int64_t M, int64_t N,
           int64_t K, double alpha, const void* A, int64_t lda, int64_t sA, const void* B,
           int64_t ldb, int64_t sB, double beta, void* C, int64_t ldc, int64_t sC,
-          int64_t batch, const Packed* pA, const Packed* pB) {
+          int64_t batch, const Packed* pA, const Packed* pB, uint32_t* outmap) {
   if (M == 0 || N == 0 || batch == 0) return;
   if (prec == GB_PREC_FP64 || K == 0) {
     gemm_fp64(ctx, dtype, opA, opB, M, N, K, cplx{alpha, 0}, A, lda, sA, B, ldb, sB,
               cplx{beta, 0}, C, ldc, sC, batch);
+    // every region written: a full output map
+    if (outmap) GB_CHECK_CUDA(cudaMemsetAsync(outmap, 0xff, outmap_bytes(M, N), ctx->stream));
     return;
   }
   Packed a, b;
@@ -1059,17 +1189,19 @@ void gemm(gb_ctx* ctx, int prec, int dtype, char opA, char opB, int64_t M, int64
     a = *pA;
   } else {
     int64_t bA = (sA == 0) ? 1 : batch;
-    void* dst = scratch(ctx, SLOT_PACK_A, packed_bytes(M, K, is_cplx(dtype), PACK_AS_A, bA));
-    pack_operand(ctx, dtype, PACK_AS_A, opA, M, K, A, lda, sA, bA, a, dst);
+    void* dst =
+        scratch(ctx, SLOT_PACK_A, packed_bytes(M, K, is_cplx(dtype), PACK_AS_A, bA, prec));
+    pack_operand(ctx, dtype, PACK_AS_A, opA, M, K, A, lda, sA, bA, a, dst, prec);
   }
   if (pB) {
     b = *pB;
   } else {
     int64_t bB = (sB == 0) ? 1 : batch;
-    void* dst = scratch(ctx, SLOT_PACK_B, packed_bytes(N, K, is_cplx(dtype), PACK_AS_B, bB));
-    pack_operand(ctx, dtype, PACK_AS_B, opB, N, K, B, ldb, sB, bB, b, dst);
+    void* dst =
+        scratch(ctx, SLOT_PACK_B, packed_bytes(N, K, is_cplx(dtype), PACK_AS_B, bB, prec));
+    pack_operand(ctx, dtype, PACK_AS_B, opB, N, K, B, ldb, sB, bB, b, dst, prec);
   }
-  gemm_split(ctx, dtype, a, b, M, N, alpha, beta, C, ldc, sC);
+  gemm_split(ctx, dtype, a, b, M, N, alpha, beta, C, ldc, sC, outmap);
 }
 
 }  // namespace gb

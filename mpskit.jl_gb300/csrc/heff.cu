@@ -135,6 +135,14 @@ struct gb_heff {
   void* kmJ_dev = nullptr;
   Packed t2p;
   bool t2p_ready = false;
+  // structurally zero regions of the AA chain (split precision): the T1 GEMM records which
+  // 128 x 128 regions of T1 it wrote (t1map), and the fused mix reads only those; input i
+  // of the mix at (a, n) is T1[a + t1roff[i], t1coff[i] + n * t1xnM]
+  int64_t t1M = 0, t1N = 0, t1xnM = 0;
+  std::vector<int64_t> t1roff, t1coff;
+  uint32_t* t1map = nullptr;
+  int64_t* t1rc_dev = nullptr;
+  uint32_t* t2prev = nullptr;
 };
 
 namespace gb {
@@ -148,6 +156,21 @@ static void* dalloc(gb_heff* h, size_t bytes) {
   if (e != cudaSuccess) throw Error(GB_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
   h->owned.push_back(p);
   return p;
+}
+
+// T1 is an M x N column-major matrix; the mix input i starts at offset io[i] and advances
+// by M * xnM per output column n
+static void record_t1_geometry(gb_heff* h, int64_t M, int64_t N, const std::vector<int64_t>& io,
+                               int64_t xnM) {
+  h->t1M = M;
+  h->t1N = N;
+  h->t1xnM = xnM;
+  h->t1roff.resize(io.size());
+  h->t1coff.resize(io.size());
+  for (size_t i = 0; i < io.size(); ++i) {
+    h->t1roff[i] = io[i] % M;
+    h->t1coff[i] = io[i] / M;
+  }
 }
 
 static void add_gemm_flops(gb_heff* h, const Step& s) {
@@ -165,8 +188,21 @@ static void prepare_t2p(gb_heff* h) {
   GB_CHECK_CUDA(cudaMemcpyAsync(h->kmJ_dev, tab.data(), tab.size() * sizeof(int64_t),
                                 cudaMemcpyHostToDevice, h->ctx->stream));
   GB_CHECK_CUDA(cudaStreamSynchronize(h->ctx->stream));
-  size_t bytes = packed_bytes(h->t2N, h->t2K, cx, PACK_AS_B, 1);
-  packed_layout(h->t2p, dalloc(h, bytes), h->t2N, h->t2K, cx, PACK_AS_B, 1);
+  size_t bytes = packed_bytes(h->t2N, h->t2K, cx, PACK_AS_B, 1, h->prec);
+  packed_layout(h->t2p, dalloc(h, bytes), h->t2N, h->t2K, cx, PACK_AS_B, 1, h->prec);
+  // zeroed once: the fused mix then writes only entries that may be nonzero (see MixSkipDev)
+  GB_CHECK_CUDA(cudaMemsetAsync(h->t2p.data, 0, bytes, h->ctx->stream));
+  if (h->t1M > 0) {
+    h->t1map = (uint32_t*)dalloc(h, outmap_bytes(h->t1M, h->t1N));
+    h->t2prev = (uint32_t*)dalloc(h, (size_t)h->t2p.mrows * h->t2p.kw * 4);
+    const size_t ni = h->t1roff.size();
+    h->t1rc_dev = (int64_t*)dalloc(h, 2 * ni * sizeof(int64_t));
+    std::vector<int64_t> rc(h->t1roff);
+    rc.insert(rc.end(), h->t1coff.begin(), h->t1coff.end());
+    GB_CHECK_CUDA(cudaMemcpyAsync(h->t1rc_dev, rc.data(), rc.size() * sizeof(int64_t),
+                                  cudaMemcpyHostToDevice, h->ctx->stream));
+    GB_CHECK_CUDA(cudaStreamSynchronize(h->ctx->stream));
+  }
   h->t2p_ready = true;
 }
 
@@ -178,13 +214,15 @@ static void prepack(gb_heff* h, Step& s) {
   prepare_t2p(h);
   gb_ctx* ctx = h->ctx;
   if (s.srcA == S_CONST && !s.hasPA) {
-    void* dst = dalloc(h, packed_bytes(s.M, s.K, is_cplx(h->dtype), PACK_AS_A, 1));
-    pack_operand(ctx, h->dtype, PACK_AS_A, s.opA, s.M, s.K, s.cA, s.lda, 0, 1, s.pA, dst);
+    void* dst = dalloc(h, packed_bytes(s.M, s.K, is_cplx(h->dtype), PACK_AS_A, 1, h->prec));
+    pack_operand(ctx, h->dtype, PACK_AS_A, s.opA, s.M, s.K, s.cA, s.lda, 0, 1, s.pA, dst,
+                 h->prec);
     s.hasPA = true;
   }
   if (s.srcB == S_CONST && !s.hasPB) {
-    void* dst = dalloc(h, packed_bytes(s.N, s.K, is_cplx(h->dtype), PACK_AS_B, 1));
-    pack_operand(ctx, h->dtype, PACK_AS_B, s.opB, s.N, s.K, s.cB, s.ldb, 0, 1, s.pB, dst);
+    void* dst = dalloc(h, packed_bytes(s.N, s.K, is_cplx(h->dtype), PACK_AS_B, 1, h->prec));
+    pack_operand(ctx, h->dtype, PACK_AS_B, s.opB, s.N, s.K, s.cB, s.ldb, 0, 1, s.pB, dst,
+                 h->prec);
     s.hasPB = true;
   }
 }
@@ -395,6 +433,7 @@ static void build_ac2(gb_heff* h, const gb_tensor* GL, const gb_tensor* W1,
     std::vector<int64_t> io(d1 * d2 * chc), oo(chr * d1 * d2);
     for (int64_t i = 0; i < (int64_t)io.size(); ++i) io[i] = Dl * i;
     for (int64_t j = 0; j < (int64_t)oo.size(); ++j) oo[j] = Dl * j;
+    record_t1_geometry(h, s1.M, s1.N, io, chc);
     Step s2;
     s2.is_gemm = false;
     s2.name = "AA2";
@@ -824,6 +863,7 @@ static void build_ac(gb_heff* h, const gb_tensor* GL, const gb_tensor* W, const 
     std::vector<int64_t> io(d * chc), oo(chr * d);
     for (int64_t i = 0; i < (int64_t)io.size(); ++i) io[i] = Dl * i;
     for (int64_t j = 0; j < (int64_t)oo.size(); ++j) oo[j] = Dl * j;
+    record_t1_geometry(h, s1.M, s1.N, io, chc);
     Step s2;
     s2.is_gemm = false;
     s2.name = "A2";
@@ -1055,7 +1095,8 @@ gb_heff* heff_build(gb_ctx* ctx, int kind, const gb_tensor* GL, const gb_tensor*
   GB_REQUIRE(GL && GR, "heff: GL and GR are required");
   GB_REQUIRE(GL->kind == GB_KIND_GL && GR->kind == GB_KIND_GR, "heff: env kinds");
   GB_REQUIRE(GL->dtype == GR->dtype, "heff: GL/GR dtype mismatch");
-  GB_REQUIRE(prec == GB_PREC_FP64 || prec == GB_PREC_BF16X3, "heff: precision");
+  GB_REQUIRE(prec == GB_PREC_FP64 || prec == GB_PREC_BF16X3 || prec == GB_PREC_TF32X3,
+             "heff: precision");
   for (const gb_tensor* W : {W1, W2}) {
     if (!W) continue;
     GB_REQUIRE(W->kind == GB_KIND_MPO, "heff: W must be an MPO tensor");
@@ -1103,7 +1144,14 @@ void heff_free(gb_heff* h) {
 }
 
 void heff_set_precision(gb_heff* h, int prec) {
-  GB_REQUIRE(prec == GB_PREC_FP64 || prec == GB_PREC_BF16X3, "heff: precision");
+  GB_REQUIRE(prec == GB_PREC_FP64 || prec == GB_PREC_BF16X3 || prec == GB_PREC_TF32X3,
+             "heff: precision");
+  if (prec != h->prec) {
+    // packed constants and the packed T2 follow the plane type; repack on change (the old
+    // buffers stay owned by the operator until it is freed)
+    for (auto& s : h->steps) s.hasPA = s.hasPB = false;
+    h->t2p_ready = false;
+  }
   h->prec = prec;
   for (auto& s : h->steps)
     if (s.is_gemm) prepack(h, s);
@@ -1132,12 +1180,23 @@ void heff_apply_raw(gb_heff* h, const void* x, void* y) {
       double beta = s.accumulate ? 1.0 : 0.0;
       const Packed* pB = s.hasPB ? &s.pB : nullptr;
       if (fused_t2 && s.t2_consumer) pB = &h->t2p;
+      uint32_t* omap = (fused_t2 && s.dst == S_T1 && h->t1map) ? h->t1map : nullptr;
       gemm(ctx, h->prec, h->dtype, s.opA, s.opB, s.M, s.N, s.K, 1.0, ptr(s.srcA, s.cA), s.lda, 0,
-           ptr(s.srcB, s.cB), s.ldb, 0, beta, C, s.ldc, 0, 1, s.hasPA ? &s.pA : nullptr, pB);
+           ptr(s.srcB, s.cB), s.ldb, 0, beta, C, s.ldc, 0, 1, s.hasPA ? &s.pA : nullptr, pB,
+           omap);
     } else if (fused_t2 && s.t2_producer) {
       const int64_t* kJ = (const int64_t*)h->kmJ_dev;
+      MixSkipDev sk;
+      if (h->t1map && s.src == S_T1) {
+        sk.xmap = h->t1map;
+        sk.onc = (h->t1N + 127) / 128;
+        sk.roff = h->t1rc_dev;
+        sk.coff = h->t1rc_dev + h->t1roff.size();
+        sk.xnM = h->t1xnM;
+        sk.prev = h->t2prev;
+      }
       mixpack_run(ctx, s.mix, kJ, kJ + h->kJ.size(), h->mn, h->dtype, ptr(s.src, nullptr), h->t2p,
-                  h->t2K, h->t2N);
+                  h->t2K, h->t2N, sk.xmap ? &sk : nullptr);
     } else {
       mix_run(ctx, s.mix, h->dtype, ptr(s.src, nullptr), (void*)ptr(s.dst, nullptr),
               s.accumulate ? 1.0 : 0.0);

@@ -35,14 +35,16 @@ end
     GB300Backend(precision = :fp64; device = 0)
 
 `TensorOperations.AbstractBackend` selecting the GB300 engine.  `precision` is `:fp64`
-(plain) or `:bf16x3` (split-precision tensor-core contractions, FP64 Krylov and gauge).
+(plain), `:bf16x3` or `:tf32x3` (split-precision tensor-core contractions with BF16 or TF32
+hi/lo operands, FP64 Krylov and gauge).
 """
 struct GB300Backend <: AbstractBackend
     precision::Cint
     device::Cint
 end
+const PRECISION_CODES = Dict(:fp64 => Cint(0), :bf16x3 => Cint(1), :tf32x3 => Cint(2))
 GB300Backend(p::Symbol = :fp64; device::Integer = 0) =
-    GB300Backend(p === :bf16x3 ? Cint(1) : Cint(0), Cint(device))
+    GB300Backend(PRECISION_CODES[p], Cint(device))
 
 check(code) = code == GB_OK ? nothing :
     error("libmpsgb: ", unsafe_string(ccall((:gb_last_error, libmpsgb), Cstring, ())))

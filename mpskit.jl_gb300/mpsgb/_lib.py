@@ -35,6 +35,8 @@ GB_HEFF_AC2 = 2
 
 GB_PREC_FP64 = 0
 GB_PREC_BF16X3 = 1
+GB_PREC_TF32X3 = 2
+PRECISIONS = {"fp64": GB_PREC_FP64, "bf16x3": GB_PREC_BF16X3, "tf32x3": GB_PREC_TF32X3}
 GB_SCHED_PERSISTENT = 0
 GB_SCHED_PERSISTENT_DENSE = 1
 GB_SCHED_TILE = 2

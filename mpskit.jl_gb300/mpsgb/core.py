@@ -36,7 +36,7 @@ class Context:
         return v.value
 
     def set_precision(self, precision):
-        code = {"fp64": L.GB_PREC_FP64, "bf16x3": L.GB_PREC_BF16X3}[precision]
+        code = L.PRECISIONS[precision]
         L.check(L.lib().gb_ctx_set_precision(self.handle, code))
 
     def set_gemm_schedule(self, schedule="persistent", tile_n=0):

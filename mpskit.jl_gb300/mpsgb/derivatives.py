@@ -23,14 +23,14 @@ class GB300Backend:
     """Contraction backend selecting the GB300 engine (the `backend` seam of
     DMRG/DMRG2/VUMPS/TDVP, src/algorithms/groundstate/dmrg.jl:86-87).
 
-    precision: "fp64" (plain) or "bf16x3" (split-precision tensor-core contractions with
-    FP64 Krylov/gauge steps)."""
+    precision: "fp64" (plain), "bf16x3" or "tf32x3" (split-precision tensor-core
+    contractions with BF16 or TF32 hi/lo operands, FP64 Krylov/gauge steps)."""
     precision: str = "fp64"
     device: int = 0
 
     @property
     def code(self):
-        return {"fp64": L.GB_PREC_FP64, "bf16x3": L.GB_PREC_BF16X3}[self.precision]
+        return L.PRECISIONS[self.precision]
 
 
 @dataclass
@@ -79,7 +79,7 @@ class DerivativeOperator:
         return v.value
 
     def set_precision(self, precision):
-        code = {"fp64": L.GB_PREC_FP64, "bf16x3": L.GB_PREC_BF16X3}[precision]
+        code = L.PRECISIONS[precision]
         L.check(L.lib().gb_heff_set_precision(self.handle, code))
 
     def new_vector(self):

@@ -23,14 +23,14 @@ def _rel(a, b):
 
 
 @pytest.mark.parametrize("dt", [np.float64, np.complex128])
-@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("bf16x3", 1e-4)])
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("bf16x3", 1e-4), ("tf32x3", 4e-6)])
 def test_transfers(ctx, dt, prec, tol):
     L_ = 10
     H = M.finite_mpo_hamiltonian(L_, 2, M.j1j2_cylinder_terms(5, 2) if dt == np.float64
                                  else M.heisenberg_terms(L_), dtype=dt)
     psi = P.finite_mps_from_tensors(P.random_initial_tensors(L_, 2, 24, 31, dt))
     envs = P.FiniteEnvironments(psi, H)
-    code = L.GB_PREC_FP64 if prec == "fp64" else L.GB_PREC_BF16X3
+    code = L.PRECISIONS[prec]
     for j in (0, 3, 7):
         GL = envs.leftenv(j, psi)
         A = psi.AL[j]

@@ -14,6 +14,7 @@ pytestmark = pytest.mark.gpu
 HERE = os.path.dirname(os.path.abspath(__file__))
 FP64_TOL = 1e-12      # relative, plain FP64 path
 SPLIT_TOL = 1e-4      # relative, bf16x3 split path (hi/lo BF16 operands, FP32 accumulate)
+TF32_TOL = 4e-6       # relative, tf32x3 split path (hi/lo TF32 operands, FP32 accumulate)
 
 
 @pytest.fixture(scope="module")
@@ -119,6 +120,31 @@ def test_split_precision_apply(ctx, model):
     y = op(mpsgb.DeviceTensor.from_numpy(ctx, "ac2", x)).numpy()
     err = _rel(y, dv.JordanAC2(GL, H[pos], H[pos + 1], GR)(x))
     assert err < SPLIT_TOL, err
+    assert ctx.device_status() == 0
+
+
+@pytest.mark.parametrize("model", ["heis_c", "j1j2_r"])
+def test_tf32_split_precision_apply(ctx, model):
+    """hi/lo TF32 operands: products exact in FP32, so the error left is the FP32
+    accumulation of the tensor pipe (~1e-6 here) -- below the BF16 split error, which adds
+    a 2^-16 representation error per operand."""
+    L_, terms, dt = MODELS[model]()
+    H, psi, envs = _envs(L_, terms, dt, 32, 24)
+    rng = np.random.default_rng(9)
+    pos = L_ // 2 - 1
+    GL, GR = envs.leftenv(pos, psi), envs.rightenv(pos + 1, psi)
+    x = _rand(rng, (GL.shape[0], 2, GR.shape[0], 2), dt)
+    ref = dv.JordanAC2(GL, H[pos], H[pos + 1], GR)(x)
+    errs = {}
+    for prec in ("bf16x3", "tf32x3"):
+        op = dev_op(ctx, L.GB_HEFF_AC2, GL, H[pos], H[pos + 1], GR, prec)
+        errs[prec] = _rel(op(mpsgb.DeviceTensor.from_numpy(ctx, "ac2", x)).numpy(), ref)
+    assert errs["tf32x3"] < TF32_TOL, errs
+    assert errs["tf32x3"] < errs["bf16x3"], errs
+    # switching an existing operator's precision repacks its constant operands
+    op.set_precision("bf16x3")
+    e = _rel(op(mpsgb.DeviceTensor.from_numpy(ctx, "ac2", x)).numpy(), ref)
+    assert abs(e - errs["bf16x3"]) < 1e-3 * errs["bf16x3"] + 1e-15
     assert ctx.device_status() == 0
 
 
