@@ -3,20 +3,26 @@
 
 Workload (the configuration the headline metric is quoted at, D = 2048): two-site DMRG
 on the spin-1/2 J1-J2 Heisenberg model (J1 = 1, J2 = 0.5) on a width-6 cylinder of
-length 24, snake-ordered into a 144-site chain, MPO from the channel-assignment builder,
-Float64, seeded random initial MPS at D = 2048, split-precision (bf16x3) contractions
-with FP64 Lanczos / SVD.  U(1) block sparsity is not exploited: every contraction is
-computed densely, which is strictly more work than the block-sparse form.
+length 24, snake-ordered into a 144-site chain, MPO from the channel-assignment builder
+with charge-definite channels, Float64, U(1) symmetric (total Sz = 0) seeded random
+initial MPS at D = 2048 (`--symmetry none`: dense, no symmetry), split-precision (bf16x3)
+contractions with FP64 Lanczos / gauge.
 
 One step = one DMRG2 local update (dmrg.jl:211-244) at the central bond -- H_eff build
-and prepare, the Galerkin matvec, the adaptive Lanczos eigensolve, the truncated SVD --
-plus the environment step the next bond of a sweep needs.
+and prepare, the Galerkin matvec, the adaptive Lanczos eigensolve, the truncated
+(per-charge-block) factorisation -- plus the environment step the next bond of a sweep
+needs.
 
-value  = H_eff algorithmic flops executed per second of step time (TFLOP/s);
+value  = H_eff algorithmic flops per second of step time (TFLOP/s); algorithmic = the
+         nonzero scalar products of the block-sparse contractions (counted on one matvec);
 e2e    = the same, driven through the C ABI with host buffers (x0 uploaded from pinned
          host memory, the new AL / S / AR downloaded every step);
-roofline = the tcgen05 split GEMM (dominant kernel), timed with CUDA events on the
-         library's stream, against the measured dense BF16 peak.
+roofline = the persistent tcgen05 split GEMM (dominant contraction kernel), timed with
+         CUDA events on the library's stream, against the measured sustained BF16 peak;
+fp64_gpu = the plain FP64 GPU path on the same bond.
+
+`--workload vumps-sweep` times a different configuration: 64 independent TFIM chains
+(one-site VUMPS, g in [0.1, 2.0], D in {64, 128, 192, 256}) solved concurrently.
 """
 import argparse
 import json
@@ -46,7 +52,7 @@ def parse():
     ap.add_argument("--D", type=int, default=2048)
     ap.add_argument("--Lx", type=int, default=24)
     ap.add_argument("--Ly", type=int, default=6)
-    ap.add_argument("--precision", default="bf16x3", choices=["bf16x3", "fp64"])
+    ap.add_argument("--precision", default="bf16x3", choices=["bf16x3", "tf32x3", "fp64"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true")
@@ -54,6 +60,13 @@ def parse():
     ap.add_argument("--svd", default="gram", choices=["gesvd", "gesvdp", "gram"])
     ap.add_argument("--symmetry", default="u1", choices=["u1", "none"],
                     help="u1: U(1) (total Sz = 0) block-sparse state and MPO; none: dense")
+    ap.add_argument("--workload", default="dmrg2", choices=["dmrg2", "vumps-sweep"],
+                    help="dmrg2: the headline DMRG2 step; vumps-sweep: 64 independent TFIM "
+                         "chains (VUMPS, g in [0.1, 2], D in {64..256}) solved concurrently")
+    ap.add_argument("--tile-n", type=int, default=0, choices=[0, 128, 256],
+                    help="output tile width of the split GEMM (0: chosen per GEMM shape)")
+    ap.add_argument("--workers", type=int, default=16)
+    ap.add_argument("--vumps-iters", type=int, default=6)
     return ap.parse_args()
 
 
@@ -289,6 +302,7 @@ def run_ours(args):
     prec = args.precision
     ctx.set_precision(prec)
     ctx.set_svd_method(args.svd)
+    ctx.set_gemm_schedule("persistent", args.tile_n)
     backend = mpsgb.GB300Backend(prec, local)
     u1 = args.symmetry == "u1"
     H = mpsgb.j1j2_cylinder(args.Lx, args.Ly, dtype=np.float64, u1=u1)
@@ -381,7 +395,7 @@ def run_ours(args):
     # flop accounting (untimed): one H_eff matvec at the same bond with the nonzero-product
     # counters on -- the block-sparse algorithmic count of the U(1) workload (equal to the
     # dense GEMM count when nothing is zero) and the tile work the tensor pipe executes
-    count = heff_count_pass(ctx, psi, H, envs, backend, pos) if prec == "bf16x3" else None
+    count = heff_count_pass(ctx, psi, H, envs, backend, pos) if prec != "fp64" else None
     if count:
         heff_alg = count["nonzero_flops"] * stats.matvecs
         rho = count["nonzero_flops"] / max(1.0, count["tile_flops"])
@@ -393,7 +407,7 @@ def run_ours(args):
     peak_bf16 = pk.get("bf16_tflops_sustained")
     peak_src = "measured (sustained)" if peak_bf16 else "fallback"
     peak_bf16 = peak_bf16 or 1700.0
-    split = 3.0 if prec == "bf16x3" else 1.0
+    split = 1.0 if prec == "fp64" else 3.0
     gemm_s = prof["gemm_ms"] / 1e3
     # algorithmic GEMM flops of the timed region: executed tile work x (nonzero / tile) of
     # the counted matvec (the dense case has rho ~ 1, below 1 only by partial-tile padding)
@@ -452,7 +466,7 @@ def run_ours(args):
                 "symmetry": args.symmetry,
                 "model": "J1=1, J2=0.5, snake order", "D": D, "L": n,
                 "mpo_width_at_bond": int(H.W[pos].shape[3]), "precision": prec,
-                "svd": args.svd,
+                "svd": args.svd, "tile_n": args.tile_n or "per shape",
                 "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (GL/GR/T1 >> 129 MB)",
             },
             "gpu_launches": launches,
@@ -585,10 +599,54 @@ def run_e2e(args, ctx, psi, H, envs, alg, pos, state, pg, flops_per_matvec=None)
             "path": "gb_tensor_upload -> gb_heff_eigsolve -> gb_svd_trunc -> gb_tensor_download"}
 
 
+def run_vumps_sweep(args):
+    """64 TFIM chains (J = 1, g uniformly in [0.1, 2.0], D drawn from {64, 128, 192, 256},
+    ComplexF64), a fixed number of VUMPS iterations each, solved by `--workers` concurrent
+    contexts; the same sweep solved one instance at a time is timed beside it."""
+    import mpsgb
+    from mpsgb import batched as B
+    from oracle import models as M
+    prec = args.precision
+    alg = mpsgb.VUMPS(tol=1e-10, maxiter=args.vumps_iters, backend=mpsgb.GB300Backend(prec))
+    ctxs = [mpsgb.Context(0) for _ in range(max(1, args.workers))]
+    B.solve_vumps_batched(B.tfim_sweep(n=4, dims=(64,)), alg, contexts=ctxs[:4])  # warm-up
+    log("vumps sweep warm-up done")
+    res = {}
+    for label, cs in (("concurrent", ctxs), ("sequential", ctxs[:1])):
+        inst = B.tfim_sweep()
+        for c in cs:
+            c.synchronize()
+        t0 = time.perf_counter()
+        B.solve_vumps_batched(inst, alg, contexts=cs)
+        t = time.perf_counter() - t0
+        its = sum(i.iterations for i in inst)
+        err = max(abs(i.energy - M.tfim_infinite_energy_density(i.label["g"])) for i in inst)
+        res[label] = {"seconds": t, "iterations": its, "iter_per_s": its / t,
+                      "max_energy_error_vs_exact": err}
+        log(f"vumps sweep {label}: {t:.2f} s, {its} iterations")
+    c = res["concurrent"]
+    line = {
+        "metric": "VUMPS iterations/s, 64-chain TFIM coupling sweep", "value": c["iter_per_s"],
+        "unit": "VUMPS iterations/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+        "ms_per_step": 1e3 * c["seconds"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c128" if prec == "fp64" else f"c128 ({prec} split contractions)",
+        "data": "synthetic",
+        "config": {"workload": "64 TFIM chains, J=1, g uniform in [0.1, 2.0], one-site VUMPS, "
+                               "D drawn from {64,128,192,256} (seed 1238), ComplexF64",
+                   "vumps_iterations_per_instance": args.vumps_iters, "workers": len(ctxs),
+                   "precision": prec},
+        "concurrent": c, "sequential": res["sequential"],
+        "speedup_concurrent_vs_sequential": res["sequential"]["seconds"] / c["seconds"],
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "vumps-sweep":
+        run_vumps_sweep(args)
     else:
         run_ours(args)
 

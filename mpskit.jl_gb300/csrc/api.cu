@@ -5,11 +5,13 @@
 #include <cusolverDn.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
 
 #include "gb_common.h"
 
@@ -688,6 +690,56 @@ void gauge_conj_transpose(gb_ctx* ctx, int dtype, int64_t m, int64_t n, const vo
   conj_transpose(ctx, dtype, m, n, A, lda, B, ldb);
 }
 void* gauge_solver(gb_ctx* ctx) { return (void*)solver(ctx); }
+
+void run_on_lanes(gb_ctx* ctx, int64_t n, const std::function<void(gb_ctx*, int64_t)>& fn) {
+  const int K = (int)std::min<int64_t>(n, 8);
+  if (K <= 1) {
+    for (int64_t i = 0; i < n; ++i) fn(ctx, i);
+    return;
+  }
+  while ((int)ctx->lanes.size() < K) {
+    gb_ctx* l = nullptr;
+    const int rc = gb_ctx_create(ctx->device, 0, &l);
+    if (rc != GB_OK) throw Error(rc, "lane context: " + std::string(gb_last_error()));
+    ctx->lanes.push_back(l);
+  }
+  std::vector<int64_t> before(K);
+  for (int k = 0; k < K; ++k) {
+    gb_ctx* l = ctx->lanes[k];
+    l->svd_method = ctx->svd_method;
+    l->aux_prec = ctx->aux_prec;
+    l->gemm_schedule = ctx->gemm_schedule;
+    l->gemm_bn = ctx->gemm_bn;
+    before[k] = l->launches;
+  }
+  GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::atomic<int64_t> next{0};
+  std::exception_ptr err;
+  std::mutex mu;
+  std::vector<std::thread> th;
+  th.reserve(K);
+  for (int k = 0; k < K; ++k)
+    th.emplace_back([&, k] {
+      gb_ctx* l = ctx->lanes[k];
+      try {
+        GB_CHECK_CUDA(cudaSetDevice(l->device));
+        for (int64_t i; (i = next++) < n;) {
+          {
+            std::lock_guard<std::mutex> g(mu);
+            if (err) break;
+          }
+          fn(l, i);
+        }
+        GB_CHECK_CUDA(cudaStreamSynchronize(l->stream));
+      } catch (...) {
+        std::lock_guard<std::mutex> g(mu);
+        if (!err) err = std::current_exception();
+      }
+    });
+  for (auto& t : th) t.join();
+  for (int k = 0; k < K; ++k) ctx->launches += ctx->lanes[k]->launches - before[k];
+  if (err) std::rethrow_exception(err);
+}
 void u1_left_orth(gb_ctx* ctx, const gb_tensor* AC, const int32_t* ql, const int32_t* qs,
                   const int32_t* qr, gb_tensor** AL, gb_tensor** C, int32_t* qk, int64_t* k);
 void u1_right_orth(gb_ctx* ctx, const gb_tensor* AC, const int32_t* ql, const int32_t* qs,
@@ -734,6 +786,8 @@ int gb_ctx_destroy(gb_ctx* ctx) {
   API_BEGIN
   if (!ctx) return GB_OK;
   DevGuard g(ctx->device);
+  for (gb_ctx* l : ctx->lanes) gb_ctx_destroy(l);
+  ctx->lanes.clear();
   cudaStreamSynchronize(ctx->stream);
   for (auto& s : ctx->scratch)
     if (s.ptr) cudaFree(s.ptr);

@@ -8,6 +8,7 @@
 #include <cstring>
 #include <stdexcept>
 #include <string>
+#include <functional>
 #include <vector>
 
 #include "../../include/mpsgb.h"
@@ -84,6 +85,9 @@ struct gb_ctx {
   // (tile granularity), [1] algorithmic flops of the nonzero products (block-sparse count)
   double* d_work = nullptr;
   bool counting = false;  // count nonzero products of every split GEMM (extra passes)
+  // auxiliary contexts (own stream, scratch and solver handle) for many small independent
+  // work items, e.g. the charge sectors of a U(1) factorisation (see run_on_lanes)
+  std::vector<gb_ctx*> lanes;
   // tracing of the tensor-core GEMM launches
   bool profiling = false;
   std::vector<cudaEvent_t> prof_events;  // pairs (start, stop) per launch
@@ -114,6 +118,10 @@ inline int64_t numel(const gb_tensor* t) {
 inline bool is_cplx(int dtype) { return dtype == GB_C128; }
 
 void* scratch(gb_ctx* ctx, int slot, size_t bytes);
+// fn(lane, i) for i < n on up to 8 lane contexts, one host thread per lane: the parent's
+// stream is synchronised first, every lane's stream at the end; the first exception thrown
+// by any item is rethrown after all lanes stopped
+void run_on_lanes(gb_ctx* ctx, int64_t n, const std::function<void(gb_ctx*, int64_t)>& fn);
 inline void count_launch(gb_ctx* ctx, int n = 1) { ctx->launches += n; }
 
 // ------------------------------------------------------------------ kernel launchers

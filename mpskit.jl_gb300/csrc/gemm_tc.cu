@@ -1048,13 +1048,12 @@ void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_
   GB_REQUIRE(A.Kp % A.bk == 0, "gemm_split: Kp alignment");
   const bool tf32 = A.esz == 4;
   load_encode();
-  static bool attr_set = false;
-  if (!attr_set) {
+  static std::once_flag attr_once;  // contexts may launch from several host threads
+  std::call_once(attr_once, [] {
     GB_CHECK_CUDA(cudaFuncSetAttribute(gemm_bf16x3_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        TC_SMEM_BYTES));
-    attr_set = true;
-  }
+  });
   CUtensorMap ma = make_map(A, TC_BM);
   CUtensorMap mb = make_map(B, TC_BN);
   int64_t batch = std::max(A.batch, B.batch);
@@ -1138,12 +1137,11 @@ void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_
 #define GB_PERSISTENT(BN_, ST_, TF_)                                                          \
   do {                                                                                        \
     constexpr int SM = persistent_smem<BN_, ST_>();                                           \
-    static bool set = false;                                                                  \
-    if (!set) {                                                                               \
+    static std::once_flag once;                                                               \
+    std::call_once(once, [] {                                                                 \
       GB_CHECK_CUDA(cudaFuncSetAttribute(gemm_bf16x3_persistent<BN_, ST_, TF_>,               \
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, SM));   \
-      set = true;                                                                             \
-    }                                                                                         \
+    });                                                                                       \
     gemm_bf16x3_persistent<BN_, ST_, TF_><<<grid, TC_THREADS, SM, ctx->stream>>>(ma, mb, p); \
   } while (0)
     if (bn == 128) {

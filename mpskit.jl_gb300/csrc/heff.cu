@@ -1143,6 +1143,8 @@ void heff_free(gb_heff* h) {
   delete h;
 }
 
+int heff_precision(const gb_heff* h) { return h->prec; }
+
 void heff_set_precision(gb_heff* h, int prec) {
   GB_REQUIRE(prec == GB_PREC_FP64 || prec == GB_PREC_BF16X3 || prec == GB_PREC_TF32X3,
              "heff: precision");

@@ -25,6 +25,7 @@
 namespace gb {
 
 void heff_apply_raw(gb_heff* h, const void* x, void* y);
+int heff_precision(const gb_heff* h);
 
 // Cyclic Jacobi eigen-decomposition of a small real symmetric matrix (row-major n x n).
 // D ascending; U[:, j] (row-major U[i*n + j]) the eigenvector of D[j].
@@ -125,6 +126,12 @@ int heff_eigsolve_raw(gb_ctx* ctx, gb_heff* h, int64_t n, int dtype, void* x, in
   double beta = 0.0;
   std::vector<double> D, U;
   std::vector<double> f;
+  // With split-precision contractions the residual cannot fall below the operator's own
+  // accuracy (~1e-6 relative); a restart that no longer reduces it by 10% ends the solve
+  // (reported as not converged, as when maxiter runs out) instead of spending the remaining
+  // restarts on rounding noise.  FP64 operators keep KrylovKit's plain maxiter rule.
+  const bool split = heff_precision(h) != GB_PREC_FP64;
+  double last_res = INFINITY;
   while (true) {
     heff_apply_raw(h, vec(K), w);
     ++numops;
@@ -154,6 +161,11 @@ int heff_eigsolve_raw(gb_ctx* ctx, gb_heff* h, int64_t n, int dtype, void* x, in
       continue;
     }
     if (numiter == maxiter) break;
+    if (split) {
+      const double res = std::fabs(f[0]);
+      if (res > 0.9 * last_res) break;
+      last_res = res;
+    }
     // thick restart: V[:keep] <- V[:K] U[:, :keep]
     int keep = (3 * kd + 2 * howmany) / 5;
     keep = std::max(1, std::min(keep, K - 1));

@@ -239,25 +239,33 @@ void scale_rows_(gb_ctx* ctx, int64_t m, int64_t n, void* A, const double* f, bo
   count_launch(ctx);
 }
 
-// Hermitian eigendecomposition G = V diag(lam) V^H (ascending), G overwritten by V
-void syevd(gb_ctx* ctx, int dtype, int64_t g, void* G, double* lam) {
-  cusolverDnHandle_t h = (cusolverDnHandle_t)gauge_solver(ctx);
-  cudaDataType t = is_cplx(dtype) ? CUDA_C_64F : CUDA_R_64F;
+
+// Gram route of one sector on a lane: E (g x g) = eigenvectors of the smaller-side Gram
+// matrix of M (ni x nj) in descending order, W (g) = its eigenvalues ascending, *info set
+void gram_eig_sector(gb_ctx* L, int dt, int64_t ni, int64_t nj, const void* M, void* E, double* W,
+                     int* info) {
+  const size_t es = elem_size(dt);
+  const int64_t g = std::min(ni, nj);
+  cusolverDnHandle_t h = (cusolverDnHandle_t)gauge_solver(L);
+  const cudaDataType t = is_cplx(dt) ? CUDA_C_64F : CUDA_R_64F;
+  DevBuf G(L, (size_t)g * g * es + 256);
+  if (ni >= nj)
+    gemm_fp64(L, dt, 'C', 'N', g, g, ni, cplx{1, 0}, M, ni, 0, M, ni, 0, cplx{0, 0}, G.p, g, 0, 1);
+  else
+    gemm_fp64(L, dt, 'N', 'C', g, g, nj, cplx{1, 0}, M, ni, 0, M, ni, 0, cplx{0, 0}, G.p, g, 0, 1);
   size_t dws = 0, hws = 0;
-  CUSOLVER_CHECK_U1(cusolverDnXsyevd_bufferSize(h, (cusolverDnParams_t)ctx->solver_params,
+  CUSOLVER_CHECK_U1(cusolverDnXsyevd_bufferSize(h, (cusolverDnParams_t)L->solver_params,
                                                 CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
-                                                g, t, G, g, CUDA_R_64F, lam, t, &dws, &hws));
-  DevBuf dw(ctx, dws + 256);
-  int* dinfo = (int*)((char*)dw.p + ((dws + 127) & ~size_t(127)));
+                                                g, t, G.p, g, CUDA_R_64F, W, t, &dws, &hws));
+  DevBuf dw(L, dws + 256);
   std::vector<char> hw(hws + 1);
-  CUSOLVER_CHECK_U1(cusolverDnXsyevd(h, (cusolverDnParams_t)ctx->solver_params,
-                                     CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, g, t, G, g,
-                                     CUDA_R_64F, lam, t, dw.p, dws, hw.data(), hws, dinfo));
-  count_launch(ctx);
-  int hinfo = 0;
-  GB_CHECK_CUDA(cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
-  if (hinfo != 0) throw Error(GB_ERR_CUDA, "syevd info = " + std::to_string(hinfo));
+  CUSOLVER_CHECK_U1(cusolverDnXsyevd(h, (cusolverDnParams_t)L->solver_params,
+                                     CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, g, t, G.p,
+                                     g, CUDA_R_64F, W, t, dw.p, dws, hw.data(), hws, info));
+  count_launch(L);
+  int64_t dims[2] = {g, g}, ins[2] = {1, -g}, outs[2] = {1, g};
+  permute(L, dt, 2, dims, G.as<char>() + (size_t)(g - 1) * g * es, ins, E, outs);
+  GB_CHECK_CUDA(cudaStreamSynchronize(L->stream));  // hw and the buffers end with this scope
 }
 
 }  // namespace
@@ -274,11 +282,8 @@ void u1_left_orth(gb_ctx* ctx, const gb_tensor* AC, const int32_t* ql, const int
   for (int64_t s = 0; s < d; ++s)
     for (int64_t l = 0; l < Dl; ++l) qrow[l + Dl * s] = ql[l] + qs[s];
   std::vector<Sector> ss = make_sectors(qrow, qcol);
-  int64_t k = 0, maxblk = 0;
-  for (auto& s : ss) {
-    k += std::min<int64_t>(s.rows.size(), s.cols.size());
-    maxblk = std::max<int64_t>(maxblk, (int64_t)(s.rows.size() * s.cols.size()));
-  }
+  int64_t k = 0;
+  for (auto& s : ss) k += std::min<int64_t>(s.rows.size(), s.cols.size());
   GB_REQUIRE(k > 0, "U(1) left_orth: no charge sector is shared by rows and columns");
   IndexTable tab(ctx, ss);
   Iota iota(ctx, std::max(k, Dr));
@@ -287,20 +292,28 @@ void u1_left_orth(gb_ctx* ctx, const gb_tensor* AC, const int32_t* ql, const int
   gb_tensor* cc = gauge_new_tensor(ctx, GB_KIND_BOND, dt, 2, dc);
   fill_zero(ctx, al->data, al->bytes);
   fill_zero(ctx, cc->data, cc->bytes);
-  DevBuf Mb(ctx, maxblk * es), Qb(ctx, maxblk * es), Rb(ctx, maxblk * es);
+  std::vector<int64_t> kof(ss.size());
   int64_t ko = 0;
-  double blocks_sq = 0.0;
-  for (auto& s : ss) {
-    const int64_t ni = s.rows.size(), nj = s.cols.size(), kc = std::min(ni, nj);
-    copy_block(ctx, false, ni, nj, tab.rows(s), tab.cols(s), AC->data, m, Mb.p, cx);
-    const double nb = nrm2(ctx, dt, ni * nj, Mb.p);
-    blocks_sq += nb * nb;
-    gauge_qr_pos(ctx, dt, ni, nj, Mb.p, Qb.p, Rb.p);
-    copy_block(ctx, true, ni, kc, tab.rows(s), iota.at(ko), al->data, m, Qb.p, cx);
-    copy_block(ctx, true, kc, nj, iota.at(ko), tab.cols(s), cc->data, k, Rb.p, cx);
-    for (int64_t i = 0; i < kc; ++i) qk[ko + i] = s.q;
+  for (size_t c = 0; c < ss.size(); ++c) {
+    const int64_t kc = std::min<int64_t>(ss[c].rows.size(), ss[c].cols.size());
+    kof[c] = ko;
+    for (int64_t i = 0; i < kc; ++i) qk[ko + i] = ss[c].q;
     ko += kc;
   }
+  std::vector<double> nrm(ss.size(), 0.0);
+  // sectors are independent: one per lane at a time
+  run_on_lanes(ctx, (int64_t)ss.size(), [&](gb_ctx* L, int64_t c) {
+    const Sector& s = ss[c];
+    const int64_t ni = s.rows.size(), nj = s.cols.size(), kc = std::min(ni, nj);
+    DevBuf Mb(L, ni * nj * es + 256), Qb(L, ni * kc * es + 256), Rb(L, kc * nj * es + 256);
+    copy_block(L, false, ni, nj, tab.rows(s), tab.cols(s), AC->data, m, Mb.p, cx);
+    nrm[c] = nrm2(L, dt, ni * nj, Mb.p);
+    gauge_qr_pos(L, dt, ni, nj, Mb.p, Qb.p, Rb.p);
+    copy_block(L, true, ni, kc, tab.rows(s), iota.at(kof[c]), al->data, m, Qb.p, cx);
+    copy_block(L, true, kc, nj, iota.at(kof[c]), tab.cols(s), cc->data, k, Rb.p, cx);
+  });
+  double blocks_sq = 0.0;
+  for (double v : nrm) blocks_sq += v * v;
   check_blocks_norm(ctx, dt, m * Dr, AC->data, blocks_sq);
   GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
   *AL = al;
@@ -320,11 +333,8 @@ void u1_right_orth(gb_ctx* ctx, const gb_tensor* AC, const int32_t* ql, const in
   for (int64_t r = 0; r < Dr; ++r)
     for (int64_t s = 0; s < d; ++s) qcol[s + d * r] = qr[r] - qs[s];
   std::vector<Sector> ss = make_sectors(qrow, qcol);
-  int64_t k = 0, maxblk = 0;
-  for (auto& s : ss) {
-    k += std::min<int64_t>(s.rows.size(), s.cols.size());
-    maxblk = std::max<int64_t>(maxblk, (int64_t)(s.rows.size() * s.cols.size()));
-  }
+  int64_t k = 0;
+  for (auto& s : ss) k += std::min<int64_t>(s.rows.size(), s.cols.size());
   GB_REQUIRE(k > 0, "U(1) right_orth: no charge sector is shared by rows and columns");
   IndexTable tab(ctx, ss);
   Iota iota(ctx, std::max(k, Dl));
@@ -333,25 +343,32 @@ void u1_right_orth(gb_ctx* ctx, const gb_tensor* AC, const int32_t* ql, const in
   gb_tensor* ar = gauge_new_tensor(ctx, GB_KIND_MPS, dt, 3, dr);
   fill_zero(ctx, ar->data, ar->bytes);
   fill_zero(ctx, cc->data, cc->bytes);
-  DevBuf Mb(ctx, maxblk * es), Mh(ctx, maxblk * es), Qb(ctx, maxblk * es), Rb(ctx, maxblk * es),
-      Tb(ctx, maxblk * es);
+  std::vector<int64_t> kof(ss.size());
   int64_t ko = 0;
-  double blocks_sq = 0.0;
-  for (auto& s : ss) {
-    const int64_t ni = s.rows.size(), nj = s.cols.size(), kc = std::min(ni, nj);
-    copy_block(ctx, false, ni, nj, tab.rows(s), tab.cols(s), AC->data, Dl, Mb.p, cx);
-    const double nb = nrm2(ctx, dt, ni * nj, Mb.p);
-    blocks_sq += nb * nb;
-    // LQ through the positive QR of the adjoint: M^H = Q' R' -> M = R'^H Q'^H
-    gauge_conj_transpose(ctx, dt, ni, nj, Mb.p, ni, Mh.p, nj);
-    gauge_qr_pos(ctx, dt, nj, ni, Mh.p, Qb.p, Rb.p);    // Q' nj x kc, R' kc x ni
-    gauge_conj_transpose(ctx, dt, nj, kc, Qb.p, nj, Tb.p, kc);  // AR block kc x nj
-    copy_block(ctx, true, kc, nj, iota.at(ko), tab.cols(s), ar->data, k, Tb.p, cx);
-    gauge_conj_transpose(ctx, dt, kc, ni, Rb.p, kc, Tb.p, ni);  // C block ni x kc
-    copy_block(ctx, true, ni, kc, tab.rows(s), iota.at(ko), cc->data, Dl, Tb.p, cx);
-    for (int64_t i = 0; i < kc; ++i) qk[ko + i] = s.q;
+  for (size_t c = 0; c < ss.size(); ++c) {
+    const int64_t kc = std::min<int64_t>(ss[c].rows.size(), ss[c].cols.size());
+    kof[c] = ko;
+    for (int64_t i = 0; i < kc; ++i) qk[ko + i] = ss[c].q;
     ko += kc;
   }
+  std::vector<double> nrm(ss.size(), 0.0);
+  run_on_lanes(ctx, (int64_t)ss.size(), [&](gb_ctx* L, int64_t c) {
+    const Sector& s = ss[c];
+    const int64_t ni = s.rows.size(), nj = s.cols.size(), kc = std::min(ni, nj);
+    const size_t blk = ni * nj * es + 256;
+    DevBuf Mb(L, blk), Mh(L, blk), Qb(L, blk), Rb(L, blk), Tb(L, blk);
+    copy_block(L, false, ni, nj, tab.rows(s), tab.cols(s), AC->data, Dl, Mb.p, cx);
+    nrm[c] = nrm2(L, dt, ni * nj, Mb.p);
+    // LQ through the positive QR of the adjoint: M^H = Q' R' -> M = R'^H Q'^H
+    gauge_conj_transpose(L, dt, ni, nj, Mb.p, ni, Mh.p, nj);
+    gauge_qr_pos(L, dt, nj, ni, Mh.p, Qb.p, Rb.p);            // Q' nj x kc, R' kc x ni
+    gauge_conj_transpose(L, dt, nj, kc, Qb.p, nj, Tb.p, kc);  // AR block kc x nj
+    copy_block(L, true, kc, nj, iota.at(kof[c]), tab.cols(s), ar->data, k, Tb.p, cx);
+    gauge_conj_transpose(L, dt, kc, ni, Rb.p, kc, Tb.p, ni);  // C block ni x kc
+    copy_block(L, true, ni, kc, tab.rows(s), iota.at(kof[c]), cc->data, Dl, Tb.p, cx);
+  });
+  double blocks_sq = 0.0;
+  for (double v : nrm) blocks_sq += v * v;
   check_blocks_norm(ctx, dt, Dl * n, AC->data, blocks_sq);
   GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
   *C = cc;
@@ -386,13 +403,17 @@ void u1_svd_trunc(gb_ctx* ctx, const gb_tensor* AC2, const int32_t* ql, const in
   };
   std::vector<Fac> fs(ss.size());
   size_t arena = 0, nsig = 0;
-  for (size_t c = 0; c < ss.size(); ++c) {
+  for (size_t c = 0; c < ss.size(); ++c) {  // the gathered blocks first, contiguous
     Fac& f = fs[c];
     f.ni = ss[c].rows.size();
     f.nj = ss[c].cols.size();
     f.g = std::min(f.ni, f.nj);
     f.oM = arena;
     arena += f.ni * f.nj;
+  }
+  const size_t blocks_elems = arena;
+  for (size_t c = 0; c < ss.size(); ++c) {
+    Fac& f = fs[c];
     f.oU = arena;
     arena += gram ? f.g * f.g : f.ni * f.g;
     f.oV = arena;
@@ -400,54 +421,59 @@ void u1_svd_trunc(gb_ctx* ctx, const gb_tensor* AC2, const int32_t* ql, const in
     f.oS = nsig;
     nsig += f.g;
   }
-  DevBuf ar_(ctx, arena * es + 256), sig(ctx, nsig * sizeof(double) + 256),
-      lam(ctx, nsig * sizeof(double) + 256);
+  DevBuf ar_(ctx, arena * es + 256), sig(ctx, nsig * sizeof(double) + 256);
   char* base = ar_.as<char>();
   auto at = [&](size_t off) { return (void*)(base + off * es); };
-  int64_t maxblk = 0;
-  for (auto& f : fs) maxblk = std::max<int64_t>(maxblk, f.ni * f.nj);
-  DevBuf W1(ctx, maxblk * es + 256), W2(ctx, maxblk * es + 256), W3(ctx, maxblk * es + 256);
   double blocks_sq = 0.0;
-  for (size_t c = 0; c < ss.size(); ++c) {
-    Fac& f = fs[c];
+  for (size_t c = 0; c < ss.size(); ++c)
+    copy_block(ctx, false, fs[c].ni, fs[c].nj, tab.rows(ss[c]), tab.cols(ss[c]), AC2->data, m,
+               at(fs[c].oM), cx);
+  {
+    const double nb = nrm2(ctx, dt, (int64_t)blocks_elems, at(0));
+    blocks_sq = nb * nb;
+  }
+  DevBuf W(ctx, nsig * sizeof(double) + 256), info(ctx, ss.size() * sizeof(int) + 256);
+  // sectors are independent: one per lane at a time
+  run_on_lanes(ctx, (int64_t)ss.size(), [&](gb_ctx* L, int64_t c) {
+    const Fac& f = fs[c];
     void* Mc = at(f.oM);
-    copy_block(ctx, false, f.ni, f.nj, tab.rows(ss[c]), tab.cols(ss[c]), AC2->data, m, Mc, cx);
-    const double nb = nrm2(ctx, dt, f.ni * f.nj, Mc);
-    blocks_sq += nb * nb;
     double* sc = sig.as<double>() + f.oS;
     if (gram) {
-      // Gram matrix of the smaller side, eigenvectors in descending order of sigma
-      void* G = W1.p;
-      if (f.ni >= f.nj)
-        gemm_fp64(ctx, dt, 'C', 'N', f.nj, f.nj, f.ni, cplx{1, 0}, Mc, f.ni, 0, Mc, f.ni, 0,
-                  cplx{0, 0}, G, f.nj, 0, 1);
-      else
-        gemm_fp64(ctx, dt, 'N', 'C', f.ni, f.ni, f.nj, cplx{1, 0}, Mc, f.ni, 0, Mc, f.ni, 0,
-                  cplx{0, 0}, G, f.ni, 0, 1);
-      double* lc = lam.as<double>() + f.oS;
-      syevd(ctx, dt, f.g, G, lc);
-      // reverse order: E[:, j] = V[:, g-1-j], sigma_j = sqrt(max(lam_{g-1-j}, 0))
-      int64_t dims[2] = {f.g, f.g}, ins[2] = {1, -f.g}, outs[2] = {1, f.g};
-      permute(ctx, dt, 2, dims, (char*)G + (size_t)(f.g - 1) * f.g * es, ins, at(f.oU), outs);
-      std::vector<double> hl(f.g), hsig(f.g);
-      GB_CHECK_CUDA(cudaMemcpyAsync(hl.data(), lc, f.g * sizeof(double), cudaMemcpyDeviceToHost,
-                                    ctx->stream));
-      GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
-      for (int64_t j = 0; j < f.g; ++j) hsig[j] = std::sqrt(std::max(hl[f.g - 1 - j], 0.0));
-      GB_CHECK_CUDA(cudaMemcpyAsync(sc, hsig.data(), f.g * sizeof(double),
-                                    cudaMemcpyHostToDevice, ctx->stream));
-      GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
-    } else if (f.ni >= f.nj) {
+      gram_eig_sector(L, dt, f.ni, f.nj, Mc, at(f.oU), W.as<double>() + f.oS, info.as<int>() + c);
+      return;
+    }
+    const size_t blk = f.ni * f.nj * es + 256;
+    DevBuf W1(L, blk), W2(L, blk), W3(L, blk);
+    if (f.ni >= f.nj) {
       GB_CHECK_CUDA(cudaMemcpyAsync(W1.p, Mc, f.ni * f.nj * es, cudaMemcpyDeviceToDevice,
-                                    ctx->stream));
-      gauge_svd_tall(ctx, dt, f.ni, f.nj, W1.p, at(f.oU), sc, at(f.oV));
+                                    L->stream));
+      gauge_svd_tall(L, dt, f.ni, f.nj, W1.p, at(f.oU), sc, at(f.oV));
     } else {
       // SVD of M^H (tall): M^H = U' S VT' -> M = VT'^H S U'^H
-      gauge_conj_transpose(ctx, dt, f.ni, f.nj, Mc, f.ni, W1.p, f.nj);
-      gauge_svd_tall(ctx, dt, f.nj, f.ni, W1.p, W2.p, sc, W3.p);  // U' nj x g, VT' g x ni
-      gauge_conj_transpose(ctx, dt, f.g, f.ni, W3.p, f.g, at(f.oU), f.ni);  // U = VT'^H
-      gauge_conj_transpose(ctx, dt, f.nj, f.g, W2.p, f.nj, at(f.oV), f.g);  // VT = U'^H
+      gauge_conj_transpose(L, dt, f.ni, f.nj, Mc, f.ni, W1.p, f.nj);
+      gauge_svd_tall(L, dt, f.nj, f.ni, W1.p, W2.p, sc, W3.p);  // U' nj x g, VT' g x ni
+      gauge_conj_transpose(L, dt, f.g, f.ni, W3.p, f.g, at(f.oU), f.ni);  // U = VT'^H
+      gauge_conj_transpose(L, dt, f.nj, f.g, W2.p, f.nj, at(f.oV), f.g);  // VT = U'^H
     }
+    GB_CHECK_CUDA(cudaStreamSynchronize(L->stream));
+  });
+  if (gram) {
+    // singular values from the Gram eigenvalues (ascending per sector), descending
+    std::vector<int> hinfo(ss.size());
+    std::vector<double> hW(nsig), hsig(nsig);
+    GB_CHECK_CUDA(cudaMemcpyAsync(hinfo.data(), info.p, ss.size() * sizeof(int),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    GB_CHECK_CUDA(cudaMemcpyAsync(hW.data(), W.p, nsig * sizeof(double), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (size_t c = 0; c < ss.size(); ++c) {
+      if (hinfo[c] != 0) throw Error(GB_ERR_CUDA, "syevd info = " + std::to_string(hinfo[c]));
+      const Fac& f = fs[c];
+      for (int64_t q = 0; q < f.g; ++q)
+        hsig[f.oS + q] = std::sqrt(std::max(hW[f.oS + f.g - 1 - q], 0.0));
+    }
+    GB_CHECK_CUDA(cudaMemcpyAsync(sig.p, hsig.data(), nsig * sizeof(double),
+                                  cudaMemcpyHostToDevice, ctx->stream));
   }
   check_blocks_norm(ctx, dt, m * n, AC2->data, blocks_sq);
   // phase 2: global truncation (truncrank & trunctol over all sectors)
@@ -490,53 +516,61 @@ void u1_svd_trunc(gb_ctx* ctx, const gb_tensor* AC2, const int32_t* ql, const in
   fill_zero(ctx, ar->data, ar->bytes);
   fill_zero(ctx, cc->data, cc->bytes);
   Iota iota(ctx, k);
+  std::vector<int64_t> kof(ss.size(), 0), kept;
   int64_t ko = 0;
   for (size_t c = 0; c < ss.size(); ++c) {
+    kof[c] = ko;
+    if (kc[c] == 0) continue;
+    kept.push_back((int64_t)c);
+    for (int64_t i = 0; i < kc[c]; ++i) qk[ko + i] = ss[c].q;
+    ko += kc[c];
+  }
+  run_on_lanes(ctx, (int64_t)kept.size(), [&](gb_ctx* L, int64_t idx) {
+    const size_t c = (size_t)kept[idx];
     const Fac& f = fs[c];
-    const int64_t kk = kc[c];
-    if (kk == 0) continue;
+    const int64_t kk = kc[c], o = kof[c];
     const Sector& s = ss[c];
-    double* sc = sig.as<double>() + f.oS;
+    const double* sc = sig.as<double>() + f.oS;
+    const size_t blk = std::max(f.ni, f.nj) * std::max<int64_t>(kk, f.g) * es + 256;
+    DevBuf W1(L, blk), W2(L, blk), W3(L, blk);
     if (!gram) {
-      copy_block(ctx, true, f.ni, kk, tab.rows(s), iota.at(ko), al->data, m, at(f.oU), cx);
+      copy_block(L, true, f.ni, kk, tab.rows(s), iota.at(o), al->data, m, at(f.oU), cx);
       // rows 0..kk-1 of VT (g x nj, ld g): gather them contiguously first
-      gauge_conj_transpose(ctx, dt, f.g, f.nj, at(f.oV), f.g, W1.p, f.nj);   // V  nj x g
-      gauge_conj_transpose(ctx, dt, f.nj, kk, W1.p, f.nj, W2.p, kk);        // VT_k kk x nj
-      copy_block(ctx, true, kk, f.nj, iota.at(ko), tab.cols(s), ar->data, k, W2.p, cx);
-      put_diag_kernel<<<blocks_for(kk), 256, 0, ctx->stream>>>(k, ko, kk, sc, (double*)cc->data,
-                                                               cx);
+      gauge_conj_transpose(L, dt, f.g, f.nj, at(f.oV), f.g, W1.p, f.nj);  // V  nj x g
+      gauge_conj_transpose(L, dt, f.nj, kk, W1.p, f.nj, W2.p, kk);       // VT_k kk x nj
+      copy_block(L, true, kk, f.nj, iota.at(o), tab.cols(s), ar->data, k, W2.p, cx);
+      put_diag_kernel<<<blocks_for(kk), 256, 0, L->stream>>>(k, o, kk, sc, (double*)cc->data, cx);
       GB_CHECK_CUDA(cudaGetLastError());
-      count_launch(ctx);
+      count_launch(L);
     } else if (f.ni >= f.nj) {
       // E (nj x kk) eigenvectors; U = M E / sigma -> Q R; AL = Q, C = R Sigma, AR = E^H
       void* E = at(f.oU);
-      gemm_fp64(ctx, dt, 'N', 'N', f.ni, kk, f.nj, cplx{1, 0}, at(f.oM), f.ni, 0, E, f.nj, 0,
+      gemm_fp64(L, dt, 'N', 'N', f.ni, kk, f.nj, cplx{1, 0}, at(f.oM), f.ni, 0, E, f.nj, 0,
                 cplx{0, 0}, W1.p, f.ni, 0, 1);
-      scale_cols(ctx, f.ni, kk, W1.p, sc, true, cx);
-      gauge_qr_pos(ctx, dt, f.ni, kk, W1.p, W2.p, W3.p);  // Q ni x kk, R kk x kk
-      scale_cols(ctx, kk, kk, W3.p, sc, false, cx);       // R Sigma
-      copy_block(ctx, true, f.ni, kk, tab.rows(s), iota.at(ko), al->data, m, W2.p, cx);
-      copy_block(ctx, true, kk, kk, iota.at(ko), iota.at(ko), cc->data, k, W3.p, cx);
-      gauge_conj_transpose(ctx, dt, f.nj, kk, E, f.nj, W1.p, kk);  // E^H kk x nj
-      copy_block(ctx, true, kk, f.nj, iota.at(ko), tab.cols(s), ar->data, k, W1.p, cx);
+      scale_cols(L, f.ni, kk, W1.p, sc, true, cx);
+      gauge_qr_pos(L, dt, f.ni, kk, W1.p, W2.p, W3.p);  // Q ni x kk, R kk x kk
+      scale_cols(L, kk, kk, W3.p, sc, false, cx);       // R Sigma
+      copy_block(L, true, f.ni, kk, tab.rows(s), iota.at(o), al->data, m, W2.p, cx);
+      copy_block(L, true, kk, kk, iota.at(o), iota.at(o), cc->data, k, W3.p, cx);
+      gauge_conj_transpose(L, dt, f.nj, kk, E, f.nj, W1.p, kk);  // E^H kk x nj
+      copy_block(L, true, kk, f.nj, iota.at(o), tab.cols(s), ar->data, k, W1.p, cx);
     } else {
       // E (ni x kk); AL = E; W = Sigma^-1 E^H M -> L Q; AR = Q, C = Sigma L
       void* E = at(f.oU);
-      copy_block(ctx, true, f.ni, kk, tab.rows(s), iota.at(ko), al->data, m, E, cx);
-      gemm_fp64(ctx, dt, 'C', 'N', kk, f.nj, f.ni, cplx{1, 0}, E, f.ni, 0, at(f.oM), f.ni, 0,
+      copy_block(L, true, f.ni, kk, tab.rows(s), iota.at(o), al->data, m, E, cx);
+      gemm_fp64(L, dt, 'C', 'N', kk, f.nj, f.ni, cplx{1, 0}, E, f.ni, 0, at(f.oM), f.ni, 0,
                 cplx{0, 0}, W1.p, kk, 0, 1);
-      scale_rows_(ctx, kk, f.nj, W1.p, sc, true, cx);
-      gauge_conj_transpose(ctx, dt, kk, f.nj, W1.p, kk, W2.p, f.nj);  // W^H nj x kk
-      gauge_qr_pos(ctx, dt, f.nj, kk, W2.p, W3.p, W1.p);               // Q' nj x kk, R' kk x kk
-      gauge_conj_transpose(ctx, dt, f.nj, kk, W3.p, f.nj, W2.p, kk);  // AR block = Q'^H
-      copy_block(ctx, true, kk, f.nj, iota.at(ko), tab.cols(s), ar->data, k, W2.p, cx);
-      gauge_conj_transpose(ctx, dt, kk, kk, W1.p, kk, W3.p, kk);      // L = R'^H
-      scale_rows_(ctx, kk, kk, W3.p, sc, false, cx);                   // Sigma L
-      copy_block(ctx, true, kk, kk, iota.at(ko), iota.at(ko), cc->data, k, W3.p, cx);
+      scale_rows_(L, kk, f.nj, W1.p, sc, true, cx);
+      gauge_conj_transpose(L, dt, kk, f.nj, W1.p, kk, W2.p, f.nj);  // W^H nj x kk
+      gauge_qr_pos(L, dt, f.nj, kk, W2.p, W3.p, W1.p);               // Q' nj x kk, R' kk x kk
+      gauge_conj_transpose(L, dt, f.nj, kk, W3.p, f.nj, W2.p, kk);  // AR block = Q'^H
+      copy_block(L, true, kk, f.nj, iota.at(o), tab.cols(s), ar->data, k, W2.p, cx);
+      gauge_conj_transpose(L, dt, kk, kk, W1.p, kk, W3.p, kk);      // L = R'^H
+      scale_rows_(L, kk, kk, W3.p, sc, false, cx);                   // Sigma L
+      copy_block(L, true, kk, kk, iota.at(o), iota.at(o), cc->data, k, W3.p, cx);
     }
-    for (int64_t i = 0; i < kk; ++i) qk[ko + i] = s.q;
-    ko += kk;
-  }
+    GB_CHECK_CUDA(cudaStreamSynchronize(L->stream));
+  });
   if (normalize) {
     const double nc = nrm2(ctx, dt, k * k, cc->data);
     scale(ctx, dt, k * k, cplx{1.0 / nc, 0}, cc->data);

@@ -14,8 +14,10 @@ from .states import (FiniteEnvironments, FiniteMPS, ac2_from, left_orth, mul_fro
                      project_complement_, right_orth, svd_trunc)
 from .algorithms import (DMRG, DMRG2, TDVP, AdaptiveKrylov, expectation_value,
                          find_groundstate, timestep)
-from .infinite import (VUMPS, InfiniteEnvironments, InfiniteMPS, find_groundstate_vumps)
+from .infinite import (VUMPS, InfiniteEnvironments, InfiniteMPS, find_groundstate_vumps,
+                       timestep_infinite)
 from . import u1
+from . import batched
 
 __all__ = [
     "Context", "DeviceTensor", "context", "AC2_hamiltonian", "AC_hamiltonian", "C_hamiltonian",
@@ -24,5 +26,5 @@ __all__ = [
     "j1j2_cylinder", "transverse_field_ising", "xxz", "FiniteEnvironments", "FiniteMPS",
     "ac2_from", "left_orth", "mul_front", "mul_tail", "project_complement_", "right_orth",
     "svd_trunc", "DMRG", "DMRG2", "AdaptiveKrylov", "expectation_value", "find_groundstate",
-    "TDVP", "timestep", "VUMPS", "InfiniteEnvironments", "InfiniteMPS", "find_groundstate_vumps", "u1",
+    "TDVP", "timestep", "VUMPS", "InfiniteEnvironments", "InfiniteMPS", "find_groundstate_vumps", "timestep_infinite", "u1", "batched",
 ]

@@ -18,7 +18,7 @@ import numpy as np
 
 from . import _lib as L
 from .core import DeviceTensor, context
-from .derivatives import GB300Backend, Lanczos, fixedpoint, DerivativeOperator
+from .derivatives import GB300Backend, Lanczos, fixedpoint, integrate, DerivativeOperator
 from .states import left_orth, mul_front, mul_tail, project_complement_, right_orth
 
 
@@ -175,12 +175,15 @@ def _regularize(ctx, x, lvec, rvec):
     return x
 
 
-def gmres(op, b, x0, krylovdim=30, maxiter=200, tol=1e-12):
+def gmres(op, b, x0, krylovdim=30, maxiter=200, tol=1e-12, stagnation=False):
     """Restarted GMRES for x - op(x) = b (KrylovKit linsolve(op, b, x0, GMRES, 1, -1));
     the Krylov vectors live on the device, the Hessenberg least squares on the host.
+    With `stagnation` (split-precision operators, whose residual cannot fall below their
+    own accuracy) a restart that reduces the true residual by less than 10% ends the solve.
     Returns (x, converged, normres)."""
     x = x0.copy()
     res = np.inf
+    last = np.inf
     for _ in range(maxiter):
         r = b.copy()
         r.axpy_(-1.0, x)
@@ -188,6 +191,9 @@ def gmres(op, b, x0, krylovdim=30, maxiter=200, tol=1e-12):
         beta = r.norm()
         if beta <= tol:
             return x, True, beta
+        if stagnation and beta > 0.9 * last:
+            return x, False, beta
+        last = beta
         V = [r.scale_(1.0 / beta)]
         Hm = np.zeros((krylovdim + 1, krylovdim), dtype=np.complex128)
         y = None
@@ -233,6 +239,7 @@ class InfiniteEnvironments:
 
     def recalculate(self, psi, tol=1e-12, krylovdim=30, maxiter=200):
         ctx, B, prec = self.ctx, self.blocks, self.precision
+        stag = prec != L.GB_PREC_FP64
         lv = B.lv
         n = len(lv)
         D = psi.AL.dims[0]
@@ -256,12 +263,12 @@ class InfiniteEnvironments:
             if kind == "identity":
                 Wd = B.blk[(i, i)]
                 op = lambda v: _regularize(ctx, _transfer("L", ctx, v, Wd, psi.AL, prec), r_LL, eye)
-                x, conv, nr = gmres(op, b, x0, kd, maxiter, tol)
+                x, conv, nr = gmres(op, b, x0, kd, maxiter, tol, stag)
                 _regularize(ctx, x, r_LL, eye)
             elif kind == "diag":
                 Wd = B.blk[(i, i)]
                 op = lambda v: _transfer("L", ctx, v, Wd, psi.AL, prec)
-                x, conv, nr = gmres(op, b, x0, kd, maxiter, tol)
+                x, conv, nr = gmres(op, b, x0, kd, maxiter, tol, stag)
             else:
                 x = b
             GL[i] = x
@@ -277,12 +284,12 @@ class InfiniteEnvironments:
             if kind == "identity":
                 Wd = B.blk[(i, i)]
                 op = lambda v: _regularize(ctx, _transfer("R", ctx, v, Wd, psi.AR, prec), l_RR, eye)
-                x, conv, nr = gmres(op, b, x0, kd, maxiter, tol)
+                x, conv, nr = gmres(op, b, x0, kd, maxiter, tol, stag)
                 _regularize(ctx, x, l_RR, eye)
             elif kind == "diag":
                 Wd = B.blk[(i, i)]
                 op = lambda v: _transfer("R", ctx, v, Wd, psi.AR, prec)
-                x, conv, nr = gmres(op, b, x0, kd, maxiter, tol)
+                x, conv, nr = gmres(op, b, x0, kd, maxiter, tol, stag)
             else:
                 x = b
             GR[i] = x
@@ -367,3 +374,27 @@ def find_groundstate_vumps(psi, H, alg, envs=None):
         if eps <= alg.tol or it >= alg.maxiter:
             break
     return psi, envs, eps, hist
+
+
+def timestep_infinite(psi, H, t, dt, alg=None, envs=None, imaginary_evolution=False,
+                      tolgauge=1e-14):
+    """timestep(::InfiniteMPS, H, t, dt, TDVP()) for a one-site cell (tdvp.jl:72-133,
+    leftorthflag = true): AC and C are integrated with the same environments, AL =
+    regauge(AC, C), the state is rebuilt by the uniform right gauge from AL (old C as the
+    starting point) and the environments are recalculated.  Returns (psi, envs)."""
+    from .algorithms import TDVP
+    alg = alg or TDVP()
+    if psi.dtype.kind != "c" and not imaginary_evolution:
+        raise TypeError("real-time evolution needs a complex InfiniteMPS")
+    if envs is None:
+        envs = InfiniteEnvironments(psi, H, alg.backend.code)
+    if envs.GL is None:
+        envs.recalculate(psi)
+    AC = integrate(_heff_ac(envs, alg.backend), psi.AC, t, dt, alg.integrator,
+                   imaginary_evolution)
+    C = integrate(_heff_c(envs, alg.backend), psi.C, t, dt, alg.integrator, imaginary_evolution)
+    AL = regauge(AC, C)
+    AR, C = uniform_rightorth(AL, psi.C, tol=tolgauge)
+    psi = InfiniteMPS(AL, AR, C)
+    envs.recalculate(psi)
+    return psi, envs

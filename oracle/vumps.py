@@ -14,6 +14,9 @@ Restates:
         -- src/utility/dynamictols.jl:86-89, src/utility/defaults.jl:22-93
   * expectation_value(InfiniteMPS, InfiniteMPOHamiltonian) -- src/algorithms/expval.jl:150-161
   * l_LL = 1, r_LL = C C', l_RR = C' C, r_RR = 1 -- src/states/infinitemps.jl:349-408
+  * timestep(::InfiniteMPS, H, t, dt, TDVP()) for a one-site cell -- integrate AC and C with
+    the same environments, regauge, uniform gauge, recalculate
+        -- src/algorithms/timestep/tdvp.jl:72-133
 
 The Arnoldi acceleration of the gauge iterations (after eig_miniter = 10 steps) is not
 restated; the QR/LQ iterations converge to the same fixed point.
@@ -21,7 +24,7 @@ restated; the QR/LQ iterations converge to the same fixed point.
 import numpy as np
 
 from . import derivatives as dv
-from .krylov import gmres_solve, lanczos_eigsolve
+from .krylov import gmres_solve, lanczos_eigsolve, lanczos_exponentiate
 from .mps import lq_pos, qr_pos
 
 
@@ -211,3 +214,24 @@ def vumps(psi, H, tol=1e-10, maxiter=200, verbose=False):
         if eps <= tol or it >= maxiter:
             break
     return psi, GL, GR, eps, hist
+
+
+def tdvp_timestep_infinite(psi, H, dt, GL=None, GR=None, imaginary=False, tol=1e-12):
+    """One TDVP step of a one-site InfiniteMPS (tdvp.jl:91-133, leftorthflag = true):
+    AC' = exp(-i dt H_AC) AC and C' = exp(-i dt H_C) C with the environments of psi
+    (-dt instead of -i dt for imaginary time), AL = regauge(AC', C'), then the uniform
+    right gauge from AL with the old C as starting point.  Returns (psi', GL, GR) with the
+    environments of psi'."""
+    W = H[0]
+    chans = H.chans[0]
+    if GL is None:
+        GL, GR = infinite_envs(psi, W, chans, tol=tol)
+    tt = -dt if imaginary else -1j * dt
+    AC, _ = lanczos_exponentiate(dv.JordanAC(GL, W, GR), tt, psi.AC, krylovdim=30, tol=tol)
+    C, _ = lanczos_exponentiate(dv.CHam(GL, GR), tt, psi.C.astype(np.complex128), krylovdim=30,
+                                tol=tol)
+    AL = regauge(AC, C)
+    AR, C2 = uniform_rightorth(AL, psi.C, tol=1e-14)
+    psi2 = InfiniteMPS1(AL, AR, C2)
+    GL, GR = infinite_envs(psi2, W, chans, GL, GR, tol=tol)
+    return psi2, GL, GR

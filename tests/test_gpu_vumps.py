@@ -56,3 +56,40 @@ def test_vumps_tfim_reaches_closed_form(ctx):
     psi, envs, eps, hist = mpsgb.find_groundstate_vumps(psi, H, mpsgb.VUMPS(tol=1e-10, maxiter=100))
     assert eps <= 1e-10
     assert abs(hist[-1]["energy"] - M.tfim_infinite_energy_density(g)) < 1e-11
+
+
+@pytest.mark.parametrize("imaginary", [False, True])
+def test_infinite_tdvp_matches_oracle(ctx, imaginary):
+    """Three one-site TDVP steps of an InfiniteMPS (real and imaginary time) against the
+    oracle: the same gauge-fixed tensors and energy density."""
+    g = 0.8
+    terms = M.tfim_terms(1, g=g, periodic=True)
+    oH = M.infinite_mpo_hamiltonian(1, 2, terms)
+    H = mpsgb.transverse_field_ising(1, g=g, infinite=True)
+    A = _A(8, 5)
+    opsi = V.infinite_mps(A)
+    psi = mpsgb.InfiniteMPS.from_tensor(A, ctx)
+    alg = mpsgb.TDVP(integrator=mpsgb.Lanczos(krylovdim=30, maxiter=200, tol=1e-12))
+    GL = GR = None
+    envs = None
+    for _ in range(3):
+        opsi, GL, GR = V.tdvp_timestep_infinite(opsi, oH, 0.05, GL, GR, imaginary=imaginary)
+        psi, envs = mpsgb.timestep_infinite(psi, H, 0.0, 0.05, alg, envs,
+                                            imaginary_evolution=imaginary)
+    AL, AR, C = psi.to_numpy()
+    assert np.allclose(AL, opsi.AL, atol=1e-8)
+    assert np.allclose(C, opsi.C, atol=1e-8)
+    e = mpsgb.infinite.energy_density(psi, envs)
+    assert abs(e - V.energy_density(opsi, oH[0], GL, GR)) < 1e-9
+
+
+def test_infinite_imaginary_time_approaches_ground_state(ctx):
+    g = 0.5
+    H = mpsgb.transverse_field_ising(1, g=g, infinite=True)
+    psi = mpsgb.InfiniteMPS.from_tensor(_A(8, 6), ctx)
+    alg = mpsgb.TDVP(integrator=mpsgb.Lanczos(krylovdim=30, maxiter=200, tol=1e-12))
+    envs = None
+    for _ in range(60):
+        psi, envs = mpsgb.timestep_infinite(psi, H, 0.0, 0.2, alg, envs, imaginary_evolution=True)
+    e = mpsgb.infinite.energy_density(psi, envs)
+    assert abs(e - M.tfim_infinite_energy_density(g)) < 1e-7

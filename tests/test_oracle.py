@@ -171,3 +171,26 @@ def test_oracle_vumps_tfim_closed_form():
     psi, GL, GR, eps, hist = V.vumps(V.infinite_mps(A), H, tol=1e-10, maxiter=100)
     assert eps <= 1e-10
     assert abs(hist[-1][1] - M.tfim_infinite_energy_density(0.5)) < 1e-12
+
+
+def test_oracle_infinite_tdvp_imaginary_and_real_time():
+    """One-site infinite TDVP (tdvp.jl:91-133): imaginary time reaches the TFIM closed form,
+    real time conserves the energy density."""
+    from oracle import vumps as V
+    g = 0.5
+    oH = M.infinite_mpo_hamiltonian(1, 2, M.tfim_terms(1, g=g, periodic=True))
+    rng = np.random.default_rng(6)
+    A = rng.standard_normal((8, 2, 8)) + 1j * rng.standard_normal((8, 2, 8))
+    psi = V.infinite_mps(A)
+    GL = GR = None
+    for _ in range(60):
+        psi, GL, GR = V.tdvp_timestep_infinite(psi, oH, 0.2, GL, GR, imaginary=True)
+    e0 = V.energy_density(psi, oH[0], GL, GR)
+    assert abs(e0 - M.tfim_infinite_energy_density(g)) < 1e-10
+    # quench to g = 0.8 and evolve in real time: the energy density is conserved
+    oH2 = M.infinite_mpo_hamiltonian(1, 2, M.tfim_terms(1, g=0.8, periodic=True))
+    GL, GR = V.infinite_envs(psi, oH2[0], oH2.chans[0])
+    e1 = V.energy_density(psi, oH2[0], GL, GR)
+    for _ in range(5):
+        psi, GL, GR = V.tdvp_timestep_infinite(psi, oH2, 0.05, GL, GR)
+    assert abs(V.energy_density(psi, oH2[0], GL, GR) - e1) < 1e-6
