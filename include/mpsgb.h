@@ -186,6 +186,16 @@ int gb_env_transfer_left(gb_ctx* ctx, const gb_tensor* GL, const gb_tensor* W,
 int gb_env_transfer_right(gb_ctx* ctx, const gb_tensor* GR, const gb_tensor* W,
                           const gb_tensor* A, const gb_tensor* Abar, int precision,
                           gb_tensor* GR_out);
+/* x - T(x) = b for one level of an infinite environment: KrylovKit
+ * linsolve(T, b, x0, GMRES(krylovdim, maxiter, tol), 1, -1) as compute_leftenvs! /
+ * compute_rightenvs! call it (src/environments/infinite_envs.jl:236, 252, 307, 322).
+ * side 0: T(v) = transfer_left(v, W, A, A); side 1: transfer_right.  With lvec/rvec
+ * (GB_KIND_BOND) every channel of T(v) is regularised as by gb_env_regularize (the
+ * identity levels).  x holds x0 on entry and the solution on exit; info as in eigsolve.
+ * Split-precision transfers stop when a restart no longer reduces the residual. */
+int gb_env_linsolve(gb_ctx* ctx, int side, const gb_tensor* W, const gb_tensor* A, int precision,
+                    const gb_tensor* lvec, const gb_tensor* rvec, const gb_tensor* b,
+                    gb_tensor* x, int krylovdim, int maxiter, double tol, gb_krylov_info* info);
 /* regularize!(v, lvec, rvec): v -= tr(lvec * v) * rvec on the channel slice `chan` of an
  * environment (src/transfermatrix/transfermatrix.jl:231-237) */
 int gb_env_regularize(gb_ctx* ctx, gb_tensor* env, int64_t chan, const gb_tensor* lvec,

@@ -44,6 +44,9 @@ gb_heff* heff_build(gb_ctx* ctx, int kind, const gb_tensor* GL, const gb_tensor*
 void heff_free(gb_heff* h);
 void heff_set_precision(gb_heff* h, int prec);
 void heff_apply_raw(gb_heff* h, const void* x, void* y);
+int env_linsolve_raw(gb_ctx* ctx, int side, const gb_tensor* W, const gb_tensor* A, int prec,
+                     const gb_tensor* lvec, const gb_tensor* rvec, const gb_tensor* b,
+                     gb_tensor* x, int krylovdim, int maxiter, double tol, gb_krylov_info* info);
 int heff_eigsolve_raw(gb_ctx* ctx, gb_heff* h, int64_t n, int dtype, void* x, int krylovdim,
                       int maxiter, double tol, bool eager, double* lambda, gb_krylov_info* info);
 int heff_exponentiate_raw(gb_ctx* ctx, gb_heff* h, int64_t n, int dtype, void* x, double t_re,
@@ -1197,6 +1200,29 @@ int gb_env_transfer_right(gb_ctx* ctx, const gb_tensor* GR, const gb_tensor* W, 
   // GR'[(a w), b] = T2[(a w), (s r)] conj(Abar[b, (s r)])^T
   gemm(ctx, prec, dt, 'N', 'C', Dk * wl, Db, d * Dbra, 1.0, T2, Dk * wl, 0, Abar->data, Db, 0, 0.0,
        GR_out->data, Dk * wl, 0);
+  API_END
+}
+
+int gb_env_linsolve(gb_ctx* ctx, int side, const gb_tensor* W, const gb_tensor* A, int precision,
+                    const gb_tensor* lvec, const gb_tensor* rvec, const gb_tensor* b,
+                    gb_tensor* x, int krylovdim, int maxiter, double tol, gb_krylov_info* info) {
+  API_BEGIN
+  check_ctx(b, ctx);
+  check_ctx(x, ctx);
+  GB_REQUIRE(W && A, "null argument");
+  GB_REQUIRE(side == 0 || side == 1, "linsolve: side must be 0 (left) or 1 (right)");
+  GB_REQUIRE(b->kind == (side == 0 ? GB_KIND_GL : GB_KIND_GR) && x->kind == b->kind,
+             "linsolve: b and x must be environments of the side");
+  GB_REQUIRE(b->dtype == x->dtype && b->ndim == 3 && x->ndim == 3 &&
+                 std::equal(b->dims, b->dims + 3, x->dims),
+             "linsolve: b and x must have the same shape");
+  GB_REQUIRE((lvec == nullptr) == (rvec == nullptr), "linsolve: give both lvec and rvec or none");
+  GB_REQUIRE(precision == GB_PREC_FP64 || precision == GB_PREC_BF16X3 ||
+                 precision == GB_PREC_TF32X3,
+             "linsolve: precision");
+  DevGuard g(ctx->device);
+  gb::env_linsolve_raw(ctx, side, W, A, precision, lvec, rvec, b, x, krylovdim, maxiter, tol,
+                       info);
   API_END
 }
 

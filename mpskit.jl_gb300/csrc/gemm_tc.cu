@@ -409,8 +409,10 @@ void mixpack_run(gb_ctx* ctx, const MixDev& m, const int64_t* kJ, const int64_t*
                                   cudaMemcpyDeviceToDevice, ctx->stream));
   }
   clear_mask(ctx, out);
+  // a block walks N / gridDim.z output columns: long-lived blocks, since with structural
+  // skipping most of a block's work is a map test
   dim3 grid((unsigned)std::min<int64_t>((m.A + 127) / 128, 64), (unsigned)m.nJ,
-            (unsigned)std::min<int64_t>(m.N, 65535));
+            (unsigned)std::min<int64_t>(m.N, 32));
   const int64_t plane = out.rows * out.Kp;
 #define GB_MIXPACK(C, E)                                                                      \
   mixpack_kernel<C, E><<<grid, 128, 0, ctx->stream>>>(                                        \

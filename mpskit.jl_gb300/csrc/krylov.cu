@@ -284,4 +284,147 @@ int heff_exponentiate_raw(gb_ctx* ctx, gb_heff* h, int64_t n, int dtype, void* x
   return GB_OK;
 }
 
+
+// ------------------------------------------------------------------ environment linsolve
+// x - T(x) = b on one level of an infinite environment (KrylovKit linsolve(T, b, x0,
+// GMRES(krylovdim, maxiter, tol), 1, -1) as compute_leftenvs!/compute_rightenvs! call it,
+// src/environments/infinite_envs.jl:236, 252, 307, 322): T(v) = transfer(v, W, A, A) (left
+// or right), followed, when lvec is given, by the regularisation v_c -= tr(lvec v_c) rvec on
+// every channel c (the identity levels).  Restarted GMRES with Givens rotations on the host;
+// the Krylov vectors stay on the device and are orthogonalised in two batched CGS passes.
+// With a split-precision transfer a restart that reduces the true residual by less than 10%
+// ends the solve (the operator is accurate to ~1e-6; see heff_eigsolve_raw).
+int env_linsolve_raw(gb_ctx* ctx, int side, const gb_tensor* W, const gb_tensor* A, int prec,
+                     const gb_tensor* lvec, const gb_tensor* rvec, const gb_tensor* b,
+                     gb_tensor* x, int krylovdim, int maxiter, double tol, gb_krylov_info* info) {
+  using zc = std::complex<double>;
+  const int dt = b->dtype;
+  const size_t es = elem_size(dt);
+  int64_t n = 1;
+  for (int i = 0; i < b->ndim; ++i) n *= b->dims[i];
+  const int kd = std::max(1, std::min(krylovdim, 64));
+  char* V = (char*)scratch(ctx, SLOT_KRYLOV, (size_t)(kd + 2) * n * es);
+  void* w = scratch(ctx, SLOT_KRYLOV_W, (size_t)n * es);
+  auto vec = [&](int j) { return (void*)(V + (size_t)j * n * es); };
+  void* Tv = vec(kd + 1);
+  auto wrap = [&](void* p) {
+    gb_tensor t;
+    t.ctx = ctx;
+    t.kind = b->kind;
+    t.dtype = dt;
+    t.ndim = b->ndim;
+    for (int i = 0; i < 6; ++i) t.dims[i] = b->dims[i];
+    t.data = p;
+    t.bytes = (size_t)n * es;
+    return t;
+  };
+  auto check = [](int rc) {
+    if (rc != GB_OK) throw Error(rc, gb_last_error());
+  };
+  int numops = 0;
+  // out <- v - T(v)
+  auto apply = [&](const void* v, void* out) {
+    gb_tensor tin = wrap((void*)v), tout = wrap(Tv);
+    if (side == 0)
+      check(gb_env_transfer_left(ctx, &tin, W, A, A, prec, &tout));
+    else
+      check(gb_env_transfer_right(ctx, &tin, W, A, A, prec, &tout));
+    if (lvec)
+      for (int64_t c = 0; c < b->dims[1]; ++c) check(gb_env_regularize(ctx, &tout, c, lvec, rvec));
+    GB_CHECK_CUDA(cudaMemcpyAsync(out, v, (size_t)n * es, cudaMemcpyDeviceToDevice, ctx->stream));
+    axpy(ctx, dt, n, cplx{-1.0, 0.0}, Tv, out);
+    ++numops;
+  };
+  const bool split = prec != GB_PREC_FP64;
+  const bool cx = is_cplx(dt);
+  double res = INFINITY, last = INFINITY;
+  int it = 0, converged = 0;
+  for (it = 0; it < std::max(1, maxiter); ++it) {
+    // r = b - (x - T x)
+    apply(x->data, w);
+    axpy(ctx, dt, n, cplx{-1.0, 0.0}, b->data, w);  // w = (x - T x) - b
+    const double beta = nrm2(ctx, dt, n, w);
+    res = beta;
+    if (beta <= tol) {
+      converged = 1;
+      break;
+    }
+    if (split && beta > 0.9 * last) break;
+    last = beta;
+    GB_CHECK_CUDA(cudaMemcpyAsync(vec(0), w, (size_t)n * es, cudaMemcpyDeviceToDevice,
+                                  ctx->stream));
+    scale(ctx, dt, n, cplx{-1.0 / beta, 0.0}, vec(0));  // V0 = r / beta
+    std::vector<std::vector<zc>> R;                       // rotated Hessenberg columns
+    std::vector<double> cs;
+    std::vector<zc> sn, g(1, zc(beta, 0.0));
+    int k = 0;
+    for (int j = 0; j < kd; ++j) {
+      apply(vec(j), w);
+      std::vector<cplx> hc;
+      orthogonalize(ctx, dt, n, j + 1, V, w, hc);
+      const double hn = nrm2(ctx, dt, n, w);
+      std::vector<zc> h(j + 2);
+      for (int i = 0; i <= j; ++i) h[i] = zc(hc[i].re, cx ? hc[i].im : 0.0);
+      h[j + 1] = zc(hn, 0.0);
+      for (int i = 0; i < j; ++i) {  // previous rotations
+        const zc t = cs[i] * h[i] + sn[i] * h[i + 1];
+        h[i + 1] = -std::conj(sn[i]) * h[i] + cs[i] * h[i + 1];
+        h[i] = t;
+      }
+      const double a = std::abs(h[j]);
+      double c;
+      zc s;
+      if (a == 0.0) {
+        c = 0.0;
+        s = zc(1.0, 0.0);
+        h[j] = h[j + 1];
+      } else {
+        const double r = std::hypot(a, hn);
+        c = a / r;
+        s = (h[j] / a) * (hn / r);
+        h[j] = (h[j] / a) * r;
+      }
+      h[j + 1] = 0.0;
+      cs.push_back(c);
+      sn.push_back(s);
+      g.push_back(-std::conj(s) * g[j]);
+      g[j] = c * g[j];
+      R.push_back(h);
+      k = j + 1;
+      res = std::abs(g[j + 1]);
+      if (res <= tol || hn < 1e-300) break;
+      if (j + 1 < kd) {
+        GB_CHECK_CUDA(cudaMemcpyAsync(vec(j + 1), w, (size_t)n * es, cudaMemcpyDeviceToDevice,
+                                      ctx->stream));
+        scale(ctx, dt, n, cplx{1.0 / hn, 0.0}, vec(j + 1));
+      }
+    }
+    // R y = g (upper triangular, columns R[j][0..j]); x += sum_i y_i V_i
+    std::vector<zc> y(k);
+    for (int i = k - 1; i >= 0; --i) {
+      zc acc = g[i];
+      for (int jj = i + 1; jj < k; ++jj) acc -= R[jj][i] * y[jj];
+      y[i] = acc / R[i][i];
+    }
+    std::vector<cplx> coef(k);
+    for (int i = 0; i < k; ++i) coef[i] = cplx{y[i].real(), cx ? y[i].imag() : 0.0};
+    multi_axpy(ctx, dt, n, k, V, n, coef.data(), x->data);
+  }
+  if (!converged && it >= std::max(1, maxiter)) {
+    // report the true residual of the final iterate
+    apply(x->data, w);
+    axpy(ctx, dt, n, cplx{-1.0, 0.0}, b->data, w);
+    res = nrm2(ctx, dt, n, w);
+    converged = res <= tol;
+  }
+  if (info) {
+    info->converged = converged;
+    info->numops = numops;
+    info->numiter = it;
+    info->normres = res;
+  }
+  GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  return GB_OK;
+}
+
 }  // namespace gb

@@ -97,6 +97,8 @@ _SIGS = {
     "gb_heff_apply": ([P, P, P], INT),
     "gb_heff_eigsolve": ([P, P, INT, INT, D, INT, PD, ctypes.POINTER(KrylovInfo)], INT),
     "gb_heff_exponentiate": ([P, P, D, D, INT, INT, D, ctypes.POINTER(KrylovInfo)], INT),
+    "gb_env_linsolve": ([P, INT, P, P, INT, P, P, P, P, INT, INT, D, ctypes.POINTER(KrylovInfo)],
+                        INT),
     "gb_env_transfer_left": ([P, P, P, P, P, INT, P], INT),
     "gb_env_transfer_right": ([P, P, P, P, P, INT, P], INT),
     "gb_env_regularize": ([P, P, I64, P, P], INT),

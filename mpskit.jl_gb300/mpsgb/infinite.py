@@ -175,53 +175,18 @@ def _regularize(ctx, x, lvec, rvec):
     return x
 
 
-def gmres(op, b, x0, krylovdim=30, maxiter=200, tol=1e-12, stagnation=False):
-    """Restarted GMRES for x - op(x) = b (KrylovKit linsolve(op, b, x0, GMRES, 1, -1));
-    the Krylov vectors live on the device, the Hessenberg least squares on the host.
-    With `stagnation` (split-precision operators, whose residual cannot fall below their
-    own accuracy) a restart that reduces the true residual by less than 10% ends the solve.
-    Returns (x, converged, normres)."""
+def _linsolve(side, ctx, b, x0, Wd, A, prec, reg, kd, maxiter, tol):
+    """x - T(x) = b for one environment level on the device (gb_env_linsolve: KrylovKit
+    linsolve(T, b, x0, GMRES, 1, -1), infinite_envs.jl:236-322); `reg` = (lvec, rvec) adds
+    the regularisation of the identity levels.  Returns (x, converged, normres)."""
     x = x0.copy()
-    res = np.inf
-    last = np.inf
-    for _ in range(maxiter):
-        r = b.copy()
-        r.axpy_(-1.0, x)
-        r.axpy_(1.0, op(x))
-        beta = r.norm()
-        if beta <= tol:
-            return x, True, beta
-        if stagnation and beta > 0.9 * last:
-            return x, False, beta
-        last = beta
-        V = [r.scale_(1.0 / beta)]
-        Hm = np.zeros((krylovdim + 1, krylovdim), dtype=np.complex128)
-        y = None
-        k = 0
-        for j in range(krylovdim):
-            w = V[j].copy()
-            w.axpy_(-1.0, op(V[j]))
-            for _pass in range(2):
-                for i in range(j + 1):
-                    h = V[i].dot(w)
-                    Hm[i, j] += h
-                    w.axpy_(-h, V[i])
-            hn = w.norm()
-            Hm[j + 1, j] = hn
-            k = j + 1
-            e = np.zeros(k + 1, dtype=np.complex128)
-            e[0] = beta
-            y = np.linalg.lstsq(Hm[:k + 1, :k], e, rcond=None)[0]
-            res = float(np.linalg.norm(e - Hm[:k + 1, :k] @ y))
-            if res <= tol or hn < 1e-300:
-                break
-            V.append(w.scale_(1.0 / hn))
-        for i in range(k):
-            coef = y[i] if x.dtype.kind == "c" else y[i].real
-            x.axpy_(coef, V[i])
-        if res <= tol:
-            return x, True, res
-    return x, False, res
+    ki = L.KrylovInfo()
+    lv, rv = reg if reg is not None else (None, None)
+    L.check(L.lib().gb_env_linsolve(ctx.handle, 0 if side == "L" else 1, Wd.handle, A.handle,
+                                    prec, lv.handle if lv is not None else None,
+                                    rv.handle if rv is not None else None, b.handle, x.handle,
+                                    int(kd), int(maxiter), float(tol), ctypes.byref(ki)))
+    return x, bool(ki.converged), ki.normres
 
 
 class InfiniteEnvironments:
@@ -239,7 +204,6 @@ class InfiniteEnvironments:
 
     def recalculate(self, psi, tol=1e-12, krylovdim=30, maxiter=200):
         ctx, B, prec = self.ctx, self.blocks, self.precision
-        stag = prec != L.GB_PREC_FP64
         lv = B.lv
         n = len(lv)
         D = psi.AL.dims[0]
@@ -262,13 +226,12 @@ class InfiniteEnvironments:
             kind = B.diag_kind(i)
             if kind == "identity":
                 Wd = B.blk[(i, i)]
-                op = lambda v: _regularize(ctx, _transfer("L", ctx, v, Wd, psi.AL, prec), r_LL, eye)
-                x, conv, nr = gmres(op, b, x0, kd, maxiter, tol, stag)
+                x, conv, nr = _linsolve("L", ctx, b, x0, Wd, psi.AL, prec, (r_LL, eye), kd,
+                                        maxiter, tol)
                 _regularize(ctx, x, r_LL, eye)
             elif kind == "diag":
                 Wd = B.blk[(i, i)]
-                op = lambda v: _transfer("L", ctx, v, Wd, psi.AL, prec)
-                x, conv, nr = gmres(op, b, x0, kd, maxiter, tol, stag)
+                x, conv, nr = _linsolve("L", ctx, b, x0, Wd, psi.AL, prec, None, kd, maxiter, tol)
             else:
                 x = b
             GL[i] = x
@@ -283,13 +246,12 @@ class InfiniteEnvironments:
             kind = B.diag_kind(i)
             if kind == "identity":
                 Wd = B.blk[(i, i)]
-                op = lambda v: _regularize(ctx, _transfer("R", ctx, v, Wd, psi.AR, prec), l_RR, eye)
-                x, conv, nr = gmres(op, b, x0, kd, maxiter, tol, stag)
+                x, conv, nr = _linsolve("R", ctx, b, x0, Wd, psi.AR, prec, (l_RR, eye), kd,
+                                        maxiter, tol)
                 _regularize(ctx, x, l_RR, eye)
             elif kind == "diag":
                 Wd = B.blk[(i, i)]
-                op = lambda v: _transfer("R", ctx, v, Wd, psi.AR, prec)
-                x, conv, nr = gmres(op, b, x0, kd, maxiter, tol, stag)
+                x, conv, nr = _linsolve("R", ctx, b, x0, Wd, psi.AR, prec, None, kd, maxiter, tol)
             else:
                 x = b
             GR[i] = x
