@@ -56,6 +56,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true")
+    ap.add_argument("--trace", action="store_true",
+                    help="after the timed steps, trace one more step: time per issuing "
+                         "source site (gb_ctx_trace_begin/end)")
     ap.add_argument("--seed", type=int, default=1234 + 5)
     ap.add_argument("--svd", default="gram", choices=["gesvd", "gesvdp", "gram"])
     ap.add_argument("--symmetry", default="u1", choices=["u1", "none"],
@@ -63,7 +66,8 @@ def parse():
     ap.add_argument("--workload", default="dmrg2", choices=["dmrg2", "vumps-sweep", "vumps-xxz"],
                     help="dmrg2: the headline DMRG2 step; vumps-sweep: 64 independent TFIM "
                          "chains (VUMPS, g in [0.1, 2], D in {64..256}) solved concurrently; "
-                         "vumps-xxz: one-site VUMPS of the XXZ chain (Jz = 1.5) at D = 256, "
+                         "vumps-xxz: one-site VUMPS of the XXZ chain (Jz = 1.5, sublattice-"
+                         "rotated) at D = 256, "
                          "plain FP64 against the split precision")
     ap.add_argument("--tile-n", type=int, default=0, choices=[0, 128, 256],
                     help="output tile width of the split GEMM (0: chosen per GEMM shape)")
@@ -399,6 +403,18 @@ def run_ours(args):
     # counters on -- the block-sparse algorithmic count of the U(1) workload (equal to the
     # dense GEMM count when nothing is zero) and the tile work the tensor pipe executes
     count = heff_count_pass(ctx, psi, H, envs, backend, pos) if prec != "fp64" else None
+    trace = None
+    if args.trace:
+        # one more (untimed) step under the launch trace: time per issuing source site
+        ctx.trace_begin()
+        tstats = SweepStats(sync=True)
+        step(tstats)
+        span, sites = ctx.trace_end()
+        trace = {"span_ms": span, "matvecs": tstats.matvecs,
+                 "sites": [[nm, round(ms, 3), ev] for nm, ms, ev in sites[:24]]}
+        log(f"launch trace: {span:.1f} ms over {sum(ev for _, _, ev in sites)} events")
+        for nm, ms, ev in sites[:24]:
+            log(f"  {nm:28s} {ms:9.3f} ms {ev:6d} events")
     if count:
         heff_alg = count["nonzero_flops"] * stats.matvecs
         rho = count["nonzero_flops"] / max(1.0, count["tile_flops"])
@@ -485,6 +501,7 @@ def run_ours(args):
             "local_energy": state.get("val"), "eps_trunc": state.get("eps_trunc"),
             "setup_s": t_setup,
             "roofline": roofline,
+            "launch_trace": trace,
             "fp64_gpu": fp64,
             "clocks": clocks.summary(),
             "e2e": e2e,
@@ -646,14 +663,23 @@ def run_vumps_sweep(args):
 
 
 def run_vumps_xxz(args):
-    """XXZ chain (Jxy = 1, Jz = 1.5, hz = 0), one-site VUMPS, D = 256, ComplexF64 seeded
-    random InfiniteMPS: the same iteration budget in plain FP64 and in split precision
-    (tf32x3 unless --precision names another split mode); energies from FP64 environments."""
+    """XXZ chain Jxy = 1, Jz = 1.5, hz = 0 (Neel phase) after a rotation by pi about x on
+    every other site -- Jxy (SxSx - SySy) - Jz SzSz per bond, the same spectrum, one-site
+    translation invariant -- one-site VUMPS, D = 256, ComplexF64 seeded random InfiniteMPS:
+    the same iteration budget in plain FP64 and in split precision (tf32x3 unless
+    --precision names another split mode); energies from FP64 environments of the final
+    state, compared with the Bethe-ansatz energy density."""
     import mpsgb
     from mpsgb import _lib as L
     D = 256
     ctx = mpsgb.context(0)
-    H = mpsgb.xxz(1, 1.0, 1.5, 0.0, dtype=np.complex128, infinite=True)
+    delta = 1.5
+    H = mpsgb.xxz(1, 1.0, delta, 0.0, dtype=np.complex128, infinite=True, rotated=True)
+    # Bethe ansatz for Delta = cosh(phi) > 1 (Yang and Yang 1966):
+    # e = Delta/4 - sinh(phi) (1/2 + 2 sum_n 1/(exp(2 n phi) + 1))
+    phi = np.arccosh(delta)
+    n = np.arange(1, 2000)
+    exact = delta / 4 - np.sinh(phi) * (0.5 + 2 * np.sum(1 / (np.exp(np.minimum(2 * n * phi, 700)) + 1)))
     rng = np.random.default_rng(args.seed)
     A = (rng.standard_normal((D, 2, D)) + 1j * rng.standard_normal((D, 2, D))).astype(np.complex128)
     split = args.precision if args.precision != "bf16x3" else "tf32x3"
@@ -670,15 +696,17 @@ def run_vumps_xxz(args):
         env64.recalculate(psi, tol=1e-12)
         e = mpsgb.infinite.energy_density(psi, env64)
         res[prec] = {"seconds": t, "iterations": len(hist), "s_per_iteration": t / len(hist),
-                     "energy_density": e, "galerkin_eps": eps}
-        log(f"vumps xxz {prec}: {t:.2f} s, {len(hist)} iterations, e = {e:.12f}, eps = {eps:.2e}")
+                     "energy_density": e, "error_vs_exact": e - exact, "galerkin_eps": eps}
+        log(f"vumps xxz {prec}: {t:.2f} s, {len(hist)} iterations, e = {e:.12f} "
+            f"(exact {exact:.12f}), eps = {eps:.2e}")
     line = {
-        "metric": "VUMPS s per iteration, XXZ (Jz = 1.5) one-site cell, D = 256",
+        "metric": "VUMPS s per iteration, XXZ (Jz = 1.5, sublattice-rotated) one-site cell, D = 256",
         "value": res[split]["s_per_iteration"], "unit": "s/iteration", "n_gpus": 1,
         "steps": args.vumps_iters, "warmup": 0, "ms_per_step": 1e3 * res[split]["s_per_iteration"],
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": f"c128 ({split} split contractions)", "data": "synthetic",
-        "config": {"workload": "XXZ Jxy=1, Jz=1.5, hz=0, one-site VUMPS, D=256, ComplexF64 "
+        "config": {"workload": "XXZ Jxy=1, Jz=1.5, hz=0 rotated by pi about x on odd sites, "
+                               "one-site VUMPS, D=256, ComplexF64 "
                                f"random InfiniteMPS (seed {args.seed})",
                    "vumps_iterations": args.vumps_iters},
         "fp64": res["fp64"], "split": res[split],

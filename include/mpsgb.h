@@ -109,6 +109,19 @@ int gb_ctx_profile_begin(gb_ctx* ctx);
 int gb_ctx_profile_end(gb_ctx* ctx, double* gemm_ms, int64_t* gemm_launches,
                        double* gemm_flops, double* region_ms);
 
+/* Launch trace of the context's stream: between trace_begin and trace_end every kernel the
+ * library launches (and every traced library call) records an event tagged with its source
+ * site; trace_end charges the time between consecutive events to the later site (its work
+ * plus any idle gap before it -- host latency shows up there) and returns the number of
+ * distinct sites and the traced span (ms).  gb_ctx_trace_site reads site i: its
+ * "file.cu:line" name, ms and event count.  Work on auxiliary lane streams appears as time
+ * of the next main-stream site.  (The per-section TimerOutputs of dmrg.jl:289-292 and
+ * vumps.jl, at kernel granularity.) */
+int gb_ctx_trace_begin(gb_ctx* ctx);
+int gb_ctx_trace_end(gb_ctx* ctx, int64_t* n_sites, double* total_ms);
+int gb_ctx_trace_site(gb_ctx* ctx, int64_t i, char* name, size_t name_len, double* ms,
+                      int64_t* events);
+
 /* Schedule of the split-precision tensor-core GEMM (the choice TensorOperations leaves to
  * its contraction backend, `backend::AbstractBackend` carried by every derivative operator,
  * src/algorithms/derivatives/mpo_derivatives.jl:10-16).  tile_n = output tile width along
@@ -143,6 +156,7 @@ int gb_tensor_download(const gb_tensor* t, void* host, size_t bytes);
 
 /* VectorInterface operations used by the Krylov solvers (KrylovKit over TensorMaps) */
 int gb_tensor_copy(gb_tensor* dst, const gb_tensor* src);
+/* t *= (re + i im); a zero factor writes zeros whatever t held (zerovector!) */
 int gb_tensor_scale(gb_tensor* t, double re, double im);
 int gb_tensor_axpy(gb_tensor* y, double re, double im, const gb_tensor* x);
 int gb_tensor_dot(const gb_tensor* x, const gb_tensor* y, double* re, double* im);
@@ -216,6 +230,12 @@ int gb_mps_mul_front(gb_ctx* ctx, const gb_tensor* C, const gb_tensor* A, gb_ten
 int gb_mps_mul_tail(gb_ctx* ctx, const gb_tensor* A, const gb_tensor* C, gb_tensor* out);
 /* out = C' (TensorKit `adjoint` of a bond tensor, used by regauge!, src/states/ortho.jl:178-184) */
 int gb_tensor_adjoint(gb_ctx* ctx, const gb_tensor* C, gb_tensor* out);
+/* Mixed transfer maps of a bond matrix, the operators whose dominant eigenvectors the
+ * uniform gauge fixing accelerates with (flip(TransferMatrix(A, AL)) and
+ * TransferMatrix(A, AR) in gauge_eigsolve_step!, src/states/ortho.jl:254-263, 315-324):
+ * side 0: out = sum_s B[s]' X A[s];  side 1: out = sum_s A[s] X B[s]'. */
+int gb_mps_transfer_bond(gb_ctx* ctx, int side, const gb_tensor* A, const gb_tensor* B,
+                         const gb_tensor* X, gb_tensor* out);
 /* Y <- (1 - X X') Y on the first two legs of Y (project_complement!, src/utility/utility.jl:22) */
 int gb_project_complement(gb_ctx* ctx, gb_tensor* Y, const gb_tensor* X);
 /* contract_mpo_expval-style scalar <x|y> after a heff apply is gb_tensor_dot. */

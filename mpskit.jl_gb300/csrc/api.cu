@@ -39,6 +39,37 @@ void* scratch(gb_ctx* ctx, int slot, size_t bytes) {
   return s.ptr;
 }
 
+// source sites of traced launches ("file.cu:line"), shared by every context
+static std::mutex g_site_mu;
+static std::vector<std::string> g_site_names;
+static std::map<std::pair<const char*, int>, int> g_site_ids;
+
+void trace_point(gb_ctx* ctx, const char* file, int line) {
+  int id;
+  {
+    std::lock_guard<std::mutex> lk(g_site_mu);
+    auto it = g_site_ids.find({file, line});
+    if (it == g_site_ids.end()) {
+      std::string f(file);
+      size_t sl = f.find_last_of('/');
+      if (sl != std::string::npos) f = f.substr(sl + 1);
+      id = (int)g_site_names.size();
+      g_site_names.push_back(f + ":" + std::to_string(line));
+      g_site_ids.emplace(std::make_pair(file, line), id);
+    } else {
+      id = it->second;
+    }
+  }
+  if (ctx->trace_used == ctx->trace_ev.size()) {
+    cudaEvent_t e;
+    GB_CHECK_CUDA(cudaEventCreate(&e));
+    ctx->trace_ev.push_back(e);
+    ctx->trace_site.push_back(-1);
+  }
+  GB_CHECK_CUDA(cudaEventRecord(ctx->trace_ev[ctx->trace_used], ctx->stream));
+  ctx->trace_site[ctx->trace_used++] = id;
+}
+
 gb_heff* heff_build(gb_ctx* ctx, int kind, const gb_tensor* GL, const gb_tensor* W1,
                     const gb_tensor* W2, const gb_tensor* GR, int prec);
 void heff_free(gb_heff* h);
@@ -350,6 +381,7 @@ void svd_tall(gb_ctx* ctx, int dtype, int64_t m, int64_t n, void* A, void* U, do
     CUSOLVER_CHECK(cusolverDnXgesvdp(h, (cusolverDnParams_t)ctx->solver_params,
                                      CUSOLVER_EIG_MODE_VECTOR, 1, m, n, t, A, m, CUDA_R_64F, S, t,
                                      U, m, t, V, n, t, dw, dws, hw.data(), hws, dinfo, &herr));
+    GB_TRACE(ctx);
     count_launch(ctx);
     int hinfo = 0;
     GB_CHECK_CUDA(cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -367,6 +399,7 @@ void svd_tall(gb_ctx* ctx, int dtype, int64_t m, int64_t n, void* A, void* U, do
   CUSOLVER_CHECK(cusolverDnXgesvd(h, (cusolverDnParams_t)ctx->solver_params, 'S', 'S', m, n, t,
                                   A, m, CUDA_R_64F, S, t, U, m, t, VT, n, t, dw, dws, hw.data(),
                                   hws, dinfo));
+  GB_TRACE(ctx);
   int hinfo = 0;
   GB_CHECK_CUDA(cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -415,6 +448,7 @@ void qr_pos(gb_ctx* ctx, int dtype, int64_t m, int64_t n, const void* M, void* Q
   std::vector<char> hw(hws + 1);
   CUSOLVER_CHECK(cusolverDnXgeqrf(h, (cusolverDnParams_t)ctx->solver_params, m, n, t, A, m, t,
                                   tau, t, dw, dws, hw.data(), hws, dinfo));
+  GB_TRACE(ctx);
   count_launch(ctx);
   // R = upper(A[:k, :])
   extract_upper_kernel<<<256, 256, 0, ctx->stream>>>(k, n, (const double*)A, m, (double*)R, cx);
@@ -428,12 +462,14 @@ void qr_pos(gb_ctx* ctx, int dtype, int64_t m, int64_t n, const void* M, void* Q
     char* wk = (char*)scratch(ctx, SLOT_TMP, (size_t)lwork * es + 256);
     CUSOLVER_CHECK(cusolverDnZungqr(h, (int)m, (int)k, (int)k, (cuDoubleComplex*)A, (int)m,
                                     (cuDoubleComplex*)tau, (cuDoubleComplex*)wk, lwork, dinfo));
+    GB_TRACE(ctx);
   } else {
     CUSOLVER_CHECK(cusolverDnDorgqr_bufferSize(h, (int)m, (int)k, (int)k, (double*)A, (int)m,
                                                (double*)tau, &lwork));
     char* wk = (char*)scratch(ctx, SLOT_TMP, (size_t)lwork * es + 256);
     CUSOLVER_CHECK(cusolverDnDorgqr(h, (int)m, (int)k, (int)k, (double*)A, (int)m, (double*)tau,
                                     (double*)wk, lwork, dinfo));
+    GB_TRACE(ctx);
   }
   count_launch(ctx);
   GB_CHECK_CUDA(cudaMemcpyAsync(Q, A, (size_t)m * k * es, cudaMemcpyDeviceToDevice, ctx->stream));
@@ -482,6 +518,7 @@ void svd_trunc_gram(gb_ctx* ctx, const gb_tensor* AC2, int64_t maxdim, double at
   CUSOLVER_CHECK(cusolverDnXsyevd(h, (cusolverDnParams_t)ctx->solver_params,
                                   CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, g, t, G, g,
                                   CUDA_R_64F, lam, t, dw, dws, hw.data(), hws, dinfo));
+  GB_TRACE(ctx);
   count_launch(ctx);
   sqrt_reverse_kernel<<<64, 256, 0, ctx->stream>>>(g, lam, sig);
   GB_CHECK_CUDA(cudaGetLastError());
@@ -740,6 +777,7 @@ void run_on_lanes(gb_ctx* ctx, int64_t n, const std::function<void(gb_ctx*, int6
       }
     });
   for (auto& t : th) t.join();
+  GB_TRACE(ctx);  // marks the end of the lanes' work on the (idle) main stream
   for (int k = 0; k < K; ++k) ctx->launches += ctx->lanes[k]->launches - before[k];
   if (err) std::rethrow_exception(err);
 }
@@ -800,6 +838,8 @@ int gb_ctx_destroy(gb_ctx* ctx) {
   }
   if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
   for (auto e : ctx->prof_events) cudaEventDestroy(e);
+  for (auto e : ctx->trace_ev) cudaEventDestroy(e);
+  if (ctx->trace_start) cudaEventDestroy(ctx->trace_start);
   for (auto e : ctx->prof_region)
     if (e) cudaEventDestroy(e);
   cudaFree(ctx->d_status);
@@ -882,6 +922,67 @@ int gb_ctx_read_work(gb_ctx* ctx, double* tile_flops, double* nonzero_flops, int
   if (tile_flops) *tile_flops = w[0];
   if (nonzero_flops) *nonzero_flops = w[1];
   if (reset) GB_CHECK_CUDA(cudaMemsetAsync(ctx->d_work, 0, sizeof(w), ctx->stream));
+  API_END
+}
+
+int gb_ctx_trace_begin(gb_ctx* ctx) {
+  API_BEGIN
+  GB_REQUIRE(ctx, "null context");
+  DevGuard g(ctx->device);
+  if (!ctx->trace_start) GB_CHECK_CUDA(cudaEventCreate(&ctx->trace_start));
+  ctx->trace_used = 0;
+  ctx->tracing = true;
+  GB_CHECK_CUDA(cudaEventRecord(ctx->trace_start, ctx->stream));
+  API_END
+}
+
+int gb_ctx_trace_end(gb_ctx* ctx, int64_t* n_sites, double* total_ms) {
+  API_BEGIN
+  GB_REQUIRE(ctx && n_sites, "null argument");
+  GB_REQUIRE(ctx->tracing, "trace_end without trace_begin");
+  DevGuard g(ctx->device);
+  ctx->tracing = false;
+  GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::map<int, std::pair<double, int64_t>> acc;
+  cudaEvent_t prev = ctx->trace_start;
+  for (size_t i = 0; i < ctx->trace_used; ++i) {
+    float ms = 0.f;
+    GB_CHECK_CUDA(cudaEventElapsedTime(&ms, prev, ctx->trace_ev[i]));
+    auto& a = acc[ctx->trace_site[i]];
+    a.first += ms;
+    a.second += 1;
+    prev = ctx->trace_ev[i];
+  }
+  if (total_ms) {
+    float ms = 0.f;
+    if (ctx->trace_used) GB_CHECK_CUDA(cudaEventElapsedTime(&ms, ctx->trace_start, prev));
+    *total_ms = ms;
+  }
+  ctx->trace_res_site.clear();
+  ctx->trace_res_ms.clear();
+  ctx->trace_res_n.clear();
+  for (auto& kv : acc) {
+    ctx->trace_res_site.push_back(kv.first);
+    ctx->trace_res_ms.push_back(kv.second.first);
+    ctx->trace_res_n.push_back(kv.second.second);
+  }
+  *n_sites = (int64_t)acc.size();
+  API_END
+}
+
+int gb_ctx_trace_site(gb_ctx* ctx, int64_t i, char* name, size_t name_len, double* ms,
+                      int64_t* events) {
+  API_BEGIN
+  GB_REQUIRE(ctx && name && name_len > 0 && ms && events, "null argument");
+  GB_REQUIRE(i >= 0 && i < (int64_t)ctx->trace_res_site.size(), "trace_site: index out of range");
+  std::string nm;
+  {
+    std::lock_guard<std::mutex> lk(g_site_mu);
+    nm = g_site_names[ctx->trace_res_site[i]];
+  }
+  std::snprintf(name, name_len, "%s", nm.c_str());
+  *ms = ctx->trace_res_ms[i];
+  *events = ctx->trace_res_n[i];
   API_END
 }
 
@@ -1354,6 +1455,45 @@ int gb_mps_mul_tail(gb_ctx* ctx, const gb_tensor* A, const gb_tensor* C, gb_tens
   DevGuard g(ctx->device);
   gemm(ctx, ctx->aux_prec, A->dtype, 'N', 'N', l * d, r, m, 1.0, A->data, l * d, 0, C->data, m, 0,
        0.0, out->data, l * d, 0);
+  API_END
+}
+
+int gb_mps_transfer_bond(gb_ctx* ctx, int side, const gb_tensor* A, const gb_tensor* B,
+                         const gb_tensor* X, gb_tensor* out) {
+  API_BEGIN
+  for (const gb_tensor* t : {A, B, X, (const gb_tensor*)out}) check_ctx(t, ctx);
+  GB_REQUIRE(A->kind == GB_KIND_MPS && B->kind == GB_KIND_MPS && X->kind == GB_KIND_BOND &&
+                 out->kind == GB_KIND_BOND,
+             "transfer_bond: kinds");
+  GB_REQUIRE(A->dtype == B->dtype && X->dtype == A->dtype && out->dtype == A->dtype,
+             "transfer_bond: dtypes");
+  GB_REQUIRE(side == 0 || side == 1, "transfer_bond: side must be 0 (left) or 1 (right)");
+  const int dt = A->dtype;
+  const int64_t d = A->dims[1];
+  GB_REQUIRE(B->dims[1] == d, "transfer_bond: physical dimensions differ");
+  DevGuard g(ctx->device);
+  const size_t es = elem_size(dt);
+  if (side == 0) {
+    // out[b, a] = sum_{l l' s} conj(B[l, s, b]) X[l, l'] A[l', s, a]
+    const int64_t lB = B->dims[0], lA = A->dims[0], rB = B->dims[2], rA = A->dims[2];
+    GB_REQUIRE(X->dims[0] == lB && X->dims[1] == lA && out->dims[0] == rB && out->dims[1] == rA,
+               "transfer_bond: shapes");
+    void* T = scratch(ctx, SLOT_TMP, (size_t)lB * d * rA * es);
+    gemm(ctx, ctx->aux_prec, dt, 'N', 'N', lB, d * rA, lA, 1.0, X->data, lB, 0, A->data, lA, 0,
+         0.0, T, lB, 0);  // T = X A : (lB, s, rA)
+    gemm(ctx, ctx->aux_prec, dt, 'C', 'N', rB, rA, lB * d, 1.0, B->data, lB * d, 0, T, lB * d, 0,
+         0.0, out->data, rB, 0);
+  } else {
+    // out[a, b] = sum_{s r r'} A[a, s, r] X[r, r'] conj(B[b, s, r'])
+    const int64_t lA = A->dims[0], lB = B->dims[0], rA = A->dims[2], rB = B->dims[2];
+    GB_REQUIRE(X->dims[0] == rA && X->dims[1] == rB && out->dims[0] == lA && out->dims[1] == lB,
+               "transfer_bond: shapes");
+    void* T = scratch(ctx, SLOT_TMP, (size_t)lA * d * rB * es);
+    gemm(ctx, ctx->aux_prec, dt, 'N', 'N', lA * d, rB, rA, 1.0, A->data, lA * d, 0, X->data, rA,
+         0, 0.0, T, lA * d, 0);  // T = A X : (lA, s, rB)
+    gemm(ctx, ctx->aux_prec, dt, 'N', 'C', lA, lB, d * rB, 1.0, T, lA, 0, B->data, lB, 0, 0.0,
+         out->data, lA, 0);
+  }
   API_END
 }
 

@@ -94,6 +94,17 @@ struct gb_ctx {
   size_t prof_used = 0;
   double prof_flops = 0.0;
   cudaEvent_t prof_region[2] = {nullptr, nullptr};
+  // launch trace: an event after every counted launch (and every trace point), tagged with
+  // the source site that issued it; the time between consecutive events is charged to the
+  // later site (its kernel plus any idle gap before it)
+  bool tracing = false;
+  std::vector<cudaEvent_t> trace_ev;
+  std::vector<int> trace_site;
+  size_t trace_used = 0;
+  cudaEvent_t trace_start = nullptr;
+  std::vector<int> trace_res_site;  // per site after gb_ctx_trace_end: id, ms, launches
+  std::vector<double> trace_res_ms;
+  std::vector<int64_t> trace_res_n;
 };
 
 struct gb_tensor {
@@ -122,7 +133,19 @@ void* scratch(gb_ctx* ctx, int slot, size_t bytes);
 // stream is synchronised first, every lane's stream at the end; the first exception thrown
 // by any item is rethrown after all lanes stopped
 void run_on_lanes(gb_ctx* ctx, int64_t n, const std::function<void(gb_ctx*, int64_t)>& fn);
-inline void count_launch(gb_ctx* ctx, int n = 1) { ctx->launches += n; }
+// launch accounting (and, while tracing, an event tagged with the issuing source line)
+void trace_point(gb_ctx* ctx, const char* file, int line);
+inline void count_launch_at(gb_ctx* ctx, int n, const char* file, int line) {
+  ctx->launches += n;
+  if (ctx->tracing) trace_point(ctx, file, line);
+}
+#define count_launch(ctx) ::gb::count_launch_at((ctx), 1, __FILE__, __LINE__)
+#define count_launch_n(ctx, n) ::gb::count_launch_at((ctx), (n), __FILE__, __LINE__)
+// a trace point after work that is not a counted kernel (library calls, copies)
+#define GB_TRACE(ctx) \
+  do {                                                             \
+    if ((ctx)->tracing) ::gb::trace_point((ctx), __FILE__, __LINE__); \
+  } while (0)
 
 // ------------------------------------------------------------------ kernel launchers
 // All operate on ctx->stream and count their launches.
@@ -236,14 +259,15 @@ struct MixSkipDev {
 // (kJ[J]: contraction-index offset of output row J, mJ[J] + n*mn: output column index)
 void mixpack_run(gb_ctx* ctx, const MixDev& m, const int64_t* kJ, const int64_t* mJ, int64_t mn,
                  int dtype, const void* x, Packed& out, int64_t Klog, int64_t Nlog,
-                 const MixSkipDev* skip = nullptr);
+                 const MixSkipDev* skip = nullptr, bool x_f32 = false);
 // outmap (optional, batch 1, split precision only): bit (m/128)*ceil(N/128) + n/128 is set
 // for every 128 x 128 region of C that receives a contribution; for real data the regions
 // that receive none are then not written (the consumer must read C only where set)
 size_t outmap_bytes(int64_t M, int64_t N);
+// c_f32: C is stored in FP32 (exact for alpha = 1, beta = 0: the FP32 accumulator itself)
 void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_t M,
                 int64_t N, double alpha, double beta, void* C, int64_t ldc, int64_t sC,
-                uint32_t* outmap = nullptr);
+                uint32_t* outmap = nullptr, bool c_f32 = false);
 bool tc_available(gb_ctx* ctx);
 
 // Unified GEMM: dispatches on precision; optional pre-packed operands.
@@ -251,6 +275,6 @@ void gemm(gb_ctx* ctx, int prec, int dtype, char opA, char opB, int64_t M, int64
           int64_t K, double alpha, const void* A, int64_t lda, int64_t sA, const void* B,
           int64_t ldb, int64_t sB, double beta, void* C, int64_t ldc, int64_t sC,
           int64_t batch = 1, const Packed* pA = nullptr, const Packed* pB = nullptr,
-          uint32_t* outmap = nullptr);
+          uint32_t* outmap = nullptr, bool c_f32 = false);
 
 }  // namespace gb

@@ -293,12 +293,12 @@ void pack_operand(gb_ctx* ctx, int dtype, int role, char op, int64_t R, int64_t 
 // y[a + out_off[J] + n*yn] = sum_e val[e] x[a + in_off[col[e]] + n*xn] written directly as
 // the packed B operand of the following GEMM: logical B element (k, m) with
 // k = a + kJ[J] (contraction index) and m = mJ[J] + n*mn (output column index).
-template <bool CPLX, typename E>
+template <bool CPLX, typename E, typename TX>
 __global__ void mixpack_kernel(int64_t A, int64_t N, int64_t xn, const int64_t* __restrict__ in_off,
                                const int64_t* __restrict__ kJ, const int64_t* __restrict__ mJ,
                                int64_t mn, const int* __restrict__ row_ptr,
                                const int* __restrict__ col, const double* __restrict__ val,
-                               const double* __restrict__ x, E* __restrict__ hi, int64_t Nlog,
+                               const TX* __restrict__ x, E* __restrict__ hi, int64_t Nlog,
                                int64_t Kp, int64_t Kh, int64_t plane, uint32_t* __restrict__ mask,
                                int kw, MixSkipDev sk) {
   constexpr int BK = bk_of<E>();
@@ -346,10 +346,11 @@ __global__ void mixpack_kernel(int64_t A, int64_t N, int64_t xn, const int64_t* 
         if (CPLX) {
           double re = 0.0, im = 0.0;
           for (int e = e0; e < e1; ++e) {
-            const double* xv = x + 2 * (a + in_off[col[e]] + n * xn);
+            const TX* xv = x + 2 * (a + in_off[col[e]] + n * xn);
+            const double xr = xv[0], xi = xv[1];
             double vr = val[2 * e], vi = val[2 * e + 1];
-            re = fma(vr, xv[0], fma(-vi, xv[1], re));
-            im = fma(vr, xv[1], fma(vi, xv[0], im));
+            re = fma(vr, xr, fma(-vi, xi, re));
+            im = fma(vr, xi, fma(vi, xr, im));
           }
           put(m, k, re);
           put(m, Kh + k, -im);
@@ -358,7 +359,8 @@ __global__ void mixpack_kernel(int64_t A, int64_t N, int64_t xn, const int64_t* 
           nz = (re != 0.0 || im != 0.0);
         } else {
           double acc = 0.0;
-          for (int e = e0; e < e1; ++e) acc = fma(val[e], x[a + in_off[col[e]] + n * xn], acc);
+          for (int e = e0; e < e1; ++e)
+            acc = fma(val[e], (double)x[a + in_off[col[e]] + n * xn], acc);
           put(m, k, acc);
           nz = acc != 0.0;
         }
@@ -381,7 +383,7 @@ __global__ void mixpack_kernel(int64_t A, int64_t N, int64_t xn, const int64_t* 
 
 void mixpack_run(gb_ctx* ctx, const MixDev& m, const int64_t* kJ, const int64_t* mJ, int64_t mn,
                  int dtype, const void* x, Packed& out, int64_t Klog, int64_t Nlog,
-                 const MixSkipDev* skip) {
+                 const MixSkipDev* skip, bool x_f32) {
   const bool cx = is_cplx(dtype);
   GB_REQUIRE(m.nJ <= 65535, "mixpack: too many output rows");
   GB_REQUIRE(m.xa == 1, "mixpack: unit input stride required");
@@ -414,17 +416,23 @@ void mixpack_run(gb_ctx* ctx, const MixDev& m, const int64_t* kJ, const int64_t*
   dim3 grid((unsigned)std::min<int64_t>((m.A + 127) / 128, 64), (unsigned)m.nJ,
             (unsigned)std::min<int64_t>(m.N, 32));
   const int64_t plane = out.rows * out.Kp;
-#define GB_MIXPACK(C, E)                                                                      \
-  mixpack_kernel<C, E><<<grid, 128, 0, ctx->stream>>>(                                        \
-      m.A, m.N, m.xn, m.in_off, kJ, mJ, mn, m.row_ptr, m.col, m.val, (const double*)x,        \
+#define GB_MIXPACK(C, E, TX)                                                                  \
+  mixpack_kernel<C, E, TX><<<grid, 128, 0, ctx->stream>>>(                                    \
+      m.A, m.N, m.xn, m.in_off, kJ, mJ, mn, m.row_ptr, m.col, m.val, (const TX*)x,            \
       (E*)out.data, Nlog, out.Kp, out.Kh, plane, out.mask, out.kw, sk)
+#define GB_MIXPACK_X(C, E)          \
+  do {                              \
+    if (x_f32) GB_MIXPACK(C, E, float); \
+    else GB_MIXPACK(C, E, double);  \
+  } while (0)
   if (out.esz == 4) {
-    if (cx) GB_MIXPACK(true, float);
-    else GB_MIXPACK(false, float);
+    if (cx) GB_MIXPACK_X(true, float);
+    else GB_MIXPACK_X(false, float);
   } else {
-    if (cx) GB_MIXPACK(true, __nv_bfloat16);
-    else GB_MIXPACK(false, __nv_bfloat16);
+    if (cx) GB_MIXPACK_X(true, __nv_bfloat16);
+    else GB_MIXPACK_X(false, __nv_bfloat16);
   }
+#undef GB_MIXPACK_X
 #undef GB_MIXPACK
   GB_CHECK_CUDA(cudaGetLastError());
   count_launch(ctx);
@@ -707,6 +715,7 @@ struct PArgs {
   uint32_t* outmap;
   int64_t onc;
   int skip_zero_out;
+  int c_f32;  // C is stored in FP32 (exact when alpha = 1 and beta = 0: C is the accumulator)
 };
 
 constexpr int PS_RING = 4;
@@ -943,21 +952,30 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const int ni = r / args.mt, mi = r - ni * args.mt;
       const int64_t m = (int64_t)mi * TC_BM + 32 * q + lane;
       const int64_t n0 = (int64_t)ni * BN;
-      double* C = args.C + (int64_t)z * args.sC * (args.cplx ? 2 : 1);
-      auto out = [&](int64_t n) -> double* {
+      // element offset of C[m, n] (complex: interleaved real / imaginary parts)
+      const int64_t cz = (int64_t)z * args.sC * (args.cplx ? 2 : 1);
+      auto off = [&](int64_t n) -> int64_t {
         if (args.cplx) {
           const int64_t nn = n < args.Nlog ? n : n - args.Nlog;
-          return C + 2 * (m + args.ldc * nn) + (n < args.Nlog ? 0 : 1);
+          return cz + 2 * (m + args.ldc * nn) + (n < args.Nlog ? 0 : 1);
         }
-        return C + m + args.ldc * n;
+        return cz + m + args.ldc * n;
+      };
+      auto store = [&](int64_t e, double val) {
+        if (args.c_f32) {
+          float* p = (float*)args.C + e;
+          if (args.beta != 0.0) val = fma(args.beta, (double)*p, val);
+          *p = (float)val;
+        } else {
+          double* p = args.C + e;
+          if (args.beta != 0.0) val = fma(args.beta, *p, val);
+          *p = val;
+        }
       };
       if (nk == 0) {
         // no contributing k-block: C = beta * C
         if (m < args.M)
-          for (int64_t n = n0; n < n0 + BN && n < args.N; ++n) {
-            double* p = out(n);
-            *p = args.beta != 0.0 ? args.beta * *p : 0.0;
-          }
+          for (int64_t n = n0; n < n0 + BN && n < args.N; ++n) store(off(n), 0.0);
         continue;
       }
       const uint32_t buf = acc & 1;
@@ -976,10 +994,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         for (int jj = 0; jj < 32; ++jj) {
           const int64_t n = n0 + c0 + jj;
           if (n >= args.N) break;
-          double val = args.alpha * (double)__uint_as_float(v[jj]);
-          double* p = out(n);
-          if (args.beta != 0.0) val = fma(args.beta, *p, val);
-          *p = val;
+          store(off(n), args.alpha * (double)__uint_as_float(v[jj]));
         }
       }
       tc_fence_before();
@@ -1043,7 +1058,7 @@ bool tc_available(gb_ctx* ctx) {
 
 void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_t M,
                 int64_t N, double alpha, double beta, void* C, int64_t ldc, int64_t sC,
-                uint32_t* outmap) {
+                uint32_t* outmap, bool c_f32) {
   GB_REQUIRE(tc_available(ctx), "split-precision GEMM needs an sm_103 device");
   GB_REQUIRE(A.Kp == B.Kp && A.cplx == B.cplx && A.esz == B.esz,
              "gemm_split: operand packing mismatch");
@@ -1092,7 +1107,7 @@ void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_
     GB_CHECK_CUDA(cudaEventRecord(ev0, ctx->stream));
   }
   if (outmap) GB_REQUIRE(std::max(A.batch, B.batch) == 1, "gemm_split: output map needs batch 1");
-  if (ctx->gemm_schedule == GB_SCHED_TILE && !tf32 && !outmap) {
+  if (ctx->gemm_schedule == GB_SCHED_TILE && !tf32 && !outmap && !c_f32) {
     dim3 grid((unsigned)((M + TC_BM - 1) / TC_BM), (unsigned)((Npk + TC_BN - 1) / TC_BN),
               (unsigned)batch);
     GB_REQUIRE(grid.y <= 65535 && grid.z <= 65535, "gemm_split: grid too large");
@@ -1132,6 +1147,7 @@ void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_
     p.outmap = outmap;
     p.onc = (N + 127) / 128;
     p.skip_zero_out = (outmap && !A.cplx) ? 1 : 0;
+    p.c_f32 = c_f32 ? 1 : 0;
     if (outmap)
       GB_CHECK_CUDA(cudaMemsetAsync(outmap, 0, outmap_bytes(M, N), ctx->stream));
     GB_CHECK_CUDA(cudaMemsetAsync(ctx->d_tile_counter, 0, sizeof(unsigned int), ctx->stream));
@@ -1175,8 +1191,9 @@ size_t outmap_bytes(int64_t M, int64_t N) {
 void gemm(gb_ctx* ctx, int prec, int dtype, char opA, char opB, int64_t M, int64_t N,
           int64_t K, double alpha, const void* A, int64_t lda, int64_t sA, const void* B,
           int64_t ldb, int64_t sB, double beta, void* C, int64_t ldc, int64_t sC,
-          int64_t batch, const Packed* pA, const Packed* pB, uint32_t* outmap) {
+          int64_t batch, const Packed* pA, const Packed* pB, uint32_t* outmap, bool c_f32) {
   if (M == 0 || N == 0 || batch == 0) return;
+  GB_REQUIRE(!c_f32 || (prec != GB_PREC_FP64 && K > 0), "gemm: FP32 output only in split mode");
   if (prec == GB_PREC_FP64 || K == 0) {
     gemm_fp64(ctx, dtype, opA, opB, M, N, K, cplx{alpha, 0}, A, lda, sA, B, ldb, sB,
               cplx{beta, 0}, C, ldc, sC, batch);
@@ -1201,7 +1218,7 @@ void gemm(gb_ctx* ctx, int prec, int dtype, char opA, char opB, int64_t M, int64
         scratch(ctx, SLOT_PACK_B, packed_bytes(N, K, is_cplx(dtype), PACK_AS_B, bB, prec));
     pack_operand(ctx, dtype, PACK_AS_B, opB, N, K, B, ldb, sB, bB, b, dst, prec);
   }
-  gemm_split(ctx, dtype, a, b, M, N, alpha, beta, C, ldc, sC, outmap);
+  gemm_split(ctx, dtype, a, b, M, N, alpha, beta, C, ldc, sC, outmap, c_f32);
 }
 
 }  // namespace gb

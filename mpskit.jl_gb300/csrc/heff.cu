@@ -143,6 +143,7 @@ struct gb_heff {
   uint32_t* t1map = nullptr;
   int64_t* t1rc_dev = nullptr;
   uint32_t* t2prev = nullptr;
+  bool t1_f32 = false;  // T1 currently holds FP32 values (fused split chain)
 };
 
 namespace gb {
@@ -1183,9 +1184,14 @@ void heff_apply_raw(gb_heff* h, const void* x, void* y) {
       const Packed* pB = s.hasPB ? &s.pB : nullptr;
       if (fused_t2 && s.t2_consumer) pB = &h->t2p;
       uint32_t* omap = (fused_t2 && s.dst == S_T1 && h->t1map) ? h->t1map : nullptr;
+      // T1 of the fused chain is written as the FP32 accumulator itself (exact: alpha = 1,
+      // beta = 0) and read back by the fused mix: half the traffic of the largest
+      // intermediate
+      const bool f32 = omap != nullptr && !s.accumulate;
       gemm(ctx, h->prec, h->dtype, s.opA, s.opB, s.M, s.N, s.K, 1.0, ptr(s.srcA, s.cA), s.lda, 0,
            ptr(s.srcB, s.cB), s.ldb, 0, beta, C, s.ldc, 0, 1, s.hasPA ? &s.pA : nullptr, pB,
-           omap);
+           omap, f32);
+      if (omap) h->t1_f32 = f32;
     } else if (fused_t2 && s.t2_producer) {
       const int64_t* kJ = (const int64_t*)h->kmJ_dev;
       MixSkipDev sk;
@@ -1198,7 +1204,7 @@ void heff_apply_raw(gb_heff* h, const void* x, void* y) {
         sk.prev = h->t2prev;
       }
       mixpack_run(ctx, s.mix, kJ, kJ + h->kJ.size(), h->mn, h->dtype, ptr(s.src, nullptr), h->t2p,
-                  h->t2K, h->t2N, sk.xmap ? &sk : nullptr);
+                  h->t2K, h->t2N, sk.xmap ? &sk : nullptr, sk.xmap && h->t1_f32);
     } else {
       mix_run(ctx, s.mix, h->dtype, ptr(s.src, nullptr), (void*)ptr(s.dst, nullptr),
               s.accumulate ? 1.0 : 0.0);

@@ -418,7 +418,7 @@ void gemm_fp64(gb_ctx* ctx, int dtype, char opA, char opB, int64_t M, int64_t N,
                                                             N, 1, mB, kw, nt * kw);
     }
     LAUNCH_CHECK();
-    count_launch(ctx, 2);
+    count_launch_n(ctx, 2);
   }
   const uint32_t* mA_ = masks;
   const uint32_t* mB_ = masks ? masks + bA * mt * kw : nullptr;
@@ -490,6 +490,12 @@ void axpy(gb_ctx* ctx, int dtype, int64_t n, cplx a, const void* x, void* y) {
 
 void scale(gb_ctx* ctx, int dtype, int64_t n, cplx a, void* x) {
   if (n == 0) return;
+  if (a.re == 0.0 && a.im == 0.0) {
+    // scaling by zero writes zeros (VectorInterface.zerovector!): the contents of a fresh
+    // allocation, NaN bit patterns included, do not survive
+    GB_CHECK_CUDA(cudaMemsetAsync(x, 0, (size_t)n * elem_size(dtype), ctx->stream));
+    return;
+  }
   unsigned nb = nblocks(n, 256, 152 * 16);
   if (is_cplx(dtype))
     scale_kernel<dcx><<<nb, 256, 0, ctx->stream>>>(n, mk(a.re, a.im), (dcx*)x);

@@ -14,8 +14,8 @@ from .states import (FiniteEnvironments, FiniteMPS, ac2_from, left_orth, mul_fro
                      project_complement_, right_orth, svd_trunc)
 from .algorithms import (DMRG, DMRG2, TDVP, AdaptiveKrylov, expectation_value,
                          find_groundstate, timestep)
-from .infinite import (VUMPS, InfiniteEnvironments, InfiniteMPS, find_groundstate_vumps,
-                       timestep_infinite)
+from .infinite import (IDMRG, VUMPS, InfiniteEnvironments, InfiniteMPS,
+                       find_groundstate_idmrg, find_groundstate_vumps, timestep_infinite)
 from . import u1
 from . import batched
 
@@ -26,5 +26,6 @@ __all__ = [
     "j1j2_cylinder", "transverse_field_ising", "xxz", "FiniteEnvironments", "FiniteMPS",
     "ac2_from", "left_orth", "mul_front", "mul_tail", "project_complement_", "right_orth",
     "svd_trunc", "DMRG", "DMRG2", "AdaptiveKrylov", "expectation_value", "find_groundstate",
-    "TDVP", "timestep", "VUMPS", "InfiniteEnvironments", "InfiniteMPS", "find_groundstate_vumps", "timestep_infinite", "u1", "batched",
+    "TDVP", "timestep", "VUMPS", "IDMRG", "InfiniteEnvironments", "InfiniteMPS",
+    "find_groundstate_vumps", "find_groundstate_idmrg", "timestep_infinite", "u1", "batched",
 ]

@@ -79,6 +79,9 @@ _SIGS = {
     "gb_ctx_set_counting": ([P, INT], INT),
     "gb_ctx_read_work": ([P, PD, PD, INT], INT),
     "gb_ctx_profile_end": ([P, PD, PI64, PD, PD], INT),
+    "gb_ctx_trace_begin": ([P], INT),
+    "gb_ctx_trace_end": ([P, PI64, PD], INT),
+    "gb_ctx_trace_site": ([P, ctypes.c_int64, ctypes.c_char_p, SZ, PD, PI64], INT),
     "gb_tensor_create": ([P, INT, INT, INT, PI64, ctypes.POINTER(P)], INT),
     "gb_tensor_free": ([P], INT),
     "gb_tensor_shape": ([P, ctypes.POINTER(INT), ctypes.POINTER(INT), ctypes.POINTER(INT), PI64], INT),
@@ -97,6 +100,7 @@ _SIGS = {
     "gb_heff_apply": ([P, P, P], INT),
     "gb_heff_eigsolve": ([P, P, INT, INT, D, INT, PD, ctypes.POINTER(KrylovInfo)], INT),
     "gb_heff_exponentiate": ([P, P, D, D, INT, INT, D, ctypes.POINTER(KrylovInfo)], INT),
+    "gb_mps_transfer_bond": ([P, INT, P, P, P, P], INT),
     "gb_env_linsolve": ([P, INT, P, P, INT, P, P, P, P, INT, INT, D, ctypes.POINTER(KrylovInfo)],
                         INT),
     "gb_env_transfer_left": ([P, P, P, P, P, INT, P], INT),

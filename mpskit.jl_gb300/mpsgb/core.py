@@ -75,6 +75,25 @@ class Context:
         return {"gemm_ms": ms.value, "gemm_launches": n.value, "gemm_flops": fl.value,
                 "region_ms": rms.value}
 
+    def trace_begin(self):
+        """Start a launch trace of this context's stream (gb_ctx_trace_begin)."""
+        L.check(L.lib().gb_ctx_trace_begin(self.handle))
+
+    def trace_end(self):
+        """-> (total_ms, [(site, ms, events)] sorted by ms): the traced span and the time
+        charged to each issuing source site (kernel plus the idle gap before it)."""
+        n, tot = ctypes.c_int64(), ctypes.c_double()
+        L.check(L.lib().gb_ctx_trace_end(self.handle, ctypes.byref(n), ctypes.byref(tot)))
+        out = []
+        buf = ctypes.create_string_buffer(256)
+        for i in range(n.value):
+            ms, ev = ctypes.c_double(), ctypes.c_int64()
+            L.check(L.lib().gb_ctx_trace_site(self.handle, i, buf, 256, ctypes.byref(ms),
+                                              ctypes.byref(ev)))
+            out.append((buf.value.decode(), ms.value, ev.value))
+        out.sort(key=lambda t: -t[1])
+        return tot.value, out
+
     def device_status(self):
         v = ctypes.c_int32()
         L.check(L.lib().gb_ctx_device_status(self.handle, ctypes.byref(v)))

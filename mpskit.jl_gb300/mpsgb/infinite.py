@@ -76,10 +76,14 @@ class InfiniteMPS:
         return mul_tail(self.AL, self.C)
 
     @classmethod
-    def from_tensor(cls, A, ctx=None, tol=1e-14, maxiter=200):
-        """InfiniteMPS(A): left then right uniform gauge fixing (order :LR)."""
-        ctx = ctx or context()
-        A = DeviceTensor.from_numpy(ctx, L.GB_KIND_MPS, A)
+    def from_tensor(cls, A, ctx=None, tol=1e-13, maxiter=200):
+        """InfiniteMPS(A): left then right uniform gauge fixing (order :LR); A is a host
+        array or a device MPS tensor."""
+        if isinstance(A, DeviceTensor):
+            ctx = A.ctx
+        else:
+            ctx = ctx or context()
+            A = DeviceTensor.from_numpy(ctx, L.GB_KIND_MPS, A)
         D = A.dims[0]
         C0 = DeviceTensor.from_numpy(ctx, L.GB_KIND_BOND, np.eye(D, dtype=A.dtype))
         AL, C = uniform_leftorth(A, C0, tol, maxiter)
@@ -90,10 +94,68 @@ class InfiniteMPS:
         return self.AL.numpy(), self.AR.numpy(), self.C.numpy()
 
 
-def uniform_leftorth(A, C0, tol=1e-14, maxiter=200):
+def _transfer_bond(side, A, B, X):
+    """side 0: sum_s B[s]' X A[s]; side 1: sum_s A[s] X B[s]' (gb_mps_transfer_bond)."""
+    shape = (B.dims[2], A.dims[2]) if side == 0 else (A.dims[0], B.dims[0])
+    out = DeviceTensor(X.ctx, L.GB_KIND_BOND, X.dtype, shape)
+    L.check(L.lib().gb_mps_transfer_bond(X.ctx.handle, side, A.handle, B.handle, X.handle,
+                                         out.handle))
+    return out
+
+
+def _arnoldi_dominant(op, x0, tol, krylovdim=30, maxiter=200):
+    """Eigenvector of the largest-magnitude eigenvalue of `op` (KrylovKit Arnoldi, :LM, eager;
+    explicit restarts from the Ritz vector), device vectors, Hessenberg on the host."""
+    real = x0.dtype.kind != "c"
+    x = x0.copy().normalize_()
+    for _ in range(maxiter):
+        V = [x]
+        Hm = np.zeros((krylovdim + 1, krylovdim), dtype=np.complex128)
+        y = np.ones(1)
+        for j in range(krylovdim):
+            w = op(V[j])
+            for _pass in range(2):
+                for i in range(j + 1):
+                    h = V[i].dot(w)
+                    Hm[i, j] += h
+                    w.axpy_(-h, V[i])
+            hn = w.norm()
+            Hm[j + 1, j] = hn
+            k = j + 1
+            ev, U = np.linalg.eig(Hm[:k, :k])
+            i = int(np.argmax(np.abs(ev)))
+            y = U[:, i] / np.linalg.norm(U[:, i])
+            # an invariant subspace (hn at rounding level of H) ends the expansion
+            breakdown = hn <= 1e-14 * max(1.0, np.linalg.norm(Hm[:k, :k]))
+            if abs(hn * y[-1]) <= tol or breakdown:
+                break
+            V.append(w.scale_(1.0 / hn))
+        if real:
+            y = y.real * np.sign(y.real[np.argmax(np.abs(y.real))])
+        x = V[0].similar()
+        L.check(L.lib().gb_tensor_scale(x.handle, 0.0, 0.0))
+        for i in range(len(y)):
+            x.axpy_(complex(y[i]) if not real else float(y[i]), V[i])
+        x.normalize_()
+        if abs(hn * y[-1]) <= tol or breakdown:
+            break
+    return x
+
+
+def uniform_leftorth(A, C0, tol=1e-13, maxiter=200, eig_miniter=10):
+    """uniform_leftorth! (src/states/ortho.jl:215-277): positive-QR iterations C A = AL C';
+    from iteration eig_miniter on, C is first replaced by the dominant eigenvector of
+    X -> sum_s AL[s]' X A[s] (Arnoldi, tolerance clamp(err^2, 1e-14, 1e-4)), made upper
+    triangular by a positive QR -- the acceleration of gauge_eigsolve_step!."""
     C = C0.copy().normalize_()
     AL = None
-    for _ in range(maxiter):
+    err = np.inf
+    for it in range(maxiter):
+        if it >= eig_miniter and AL is not None:
+            t = min(max(err * err, 1e-14), 1e-4)
+            vec = _arnoldi_dominant(lambda X: _transfer_bond(0, A, AL, X), C, t)
+            _, C = left_orth(_as_mps(vec))
+            C.normalize_()
         AL, R = left_orth(mul_front(C, A))
         R.normalize_()
         err = _diff_norm(C, R)
@@ -103,10 +165,19 @@ def uniform_leftorth(A, C0, tol=1e-14, maxiter=200):
     return AL, C
 
 
-def uniform_rightorth(A, C0, tol=1e-14, maxiter=200):
+def uniform_rightorth(A, C0, tol=1e-13, maxiter=200, eig_miniter=10):
+    """uniform_rightorth! (src/states/ortho.jl:279-340): positive-LQ iterations A C = C' AR,
+    accelerated from iteration eig_miniter on by the dominant eigenvector of
+    X -> sum_s A[s] X AR[s]' (made lower triangular by a positive LQ)."""
     C = C0.copy().normalize_()
     AR = None
-    for _ in range(maxiter):
+    err = np.inf
+    for it in range(maxiter):
+        if it >= eig_miniter and AR is not None:
+            t = min(max(err * err, 1e-14), 1e-4)
+            vec = _arnoldi_dominant(lambda X: _transfer_bond(1, A, AR, X), C, t)
+            C, _ = right_orth(_as_mps(vec))
+            C.normalize_()
         Lm, AR = right_orth(mul_tail(A, C))
         Lm.normalize_()
         err = _diff_norm(C, Lm)
@@ -335,6 +406,54 @@ def find_groundstate_vumps(psi, H, alg, envs=None):
             print(f"VUMPS {it}: e = {e:.14f}  eps = {eps:.3e}")
         if eps <= alg.tol or it >= alg.maxiter:
             break
+    return psi, envs, eps, hist
+
+
+class IDMRG:
+    """IDMRG defaults (idmrg.jl:14-31): tol 1e-10, maxiter 200, DynamicTol-adapted
+    eigensolver (factor 1e-3) and gauge (factor 1e-6) tolerances."""
+
+    def __init__(self, tol=1e-10, maxiter=200, backend=None, verbosity=0):
+        self.tol, self.maxiter = tol, maxiter
+        self.backend = backend or GB300Backend()
+        self.verbosity = verbosity
+
+
+def find_groundstate_idmrg(psi, H, alg, envs=None):
+    """find_groundstate(::InfiniteMPS, H, IDMRG()) for a one-site cell (idmrg.jl:85-216).
+    Per iteration: AC eigensolve, positive QR AC = AL C, GL <- GL T(AL) (un-normalised,
+    transfer_leftenv!, infinite_envs.jl:359-363); AC eigensolve again, positive LQ
+    AC = C AR, GR <- T(AR) GR; error |C - C_old|.  The result is InfiniteMPS(AR) with the
+    DynamicTol gauge tolerance and recalculated environments.  Returns (psi, envs, eps,
+    history); history entries carry the energy change per site (E - E_old) / 2."""
+    envs = envs or InfiniteEnvironments(psi, H, alg.backend.code)
+    ctx = psi.ctx
+    envs.recalculate(psi, tol=1e-10)  # environments(psi, H): GMRES at Defaults.tol
+    eps = galerkin(psi, envs, alg.backend)
+    E_old = energy_density(psi, envs, alg.backend)
+    W = H.device(ctx, envs.dtype)[0]
+    AC, C, AR = psi.AC, psi.C, psi.AR
+    it = 0
+    hist = []
+    while True:
+        solver = Lanczos(krylovdim=30, maxiter=200, tol=_dyn_tol(eps, it, 1e-3), eager=True)
+        C_old = C
+        _, AC, _ = fixedpoint(_heff_ac(envs, alg.backend), AC, "SR", solver)
+        AL, _ = left_orth(AC)
+        envs.GL = _transfer("L", ctx, envs.GL, W, AL, envs.precision)
+        E, AC, _ = fixedpoint(_heff_ac(envs, alg.backend), AC, "SR", solver)
+        C, AR = right_orth(AC)
+        envs.GR = _transfer("R", ctx, envs.GR, W, AR, envs.precision)
+        eps = _diff_norm(C, C_old)
+        it += 1
+        hist.append({"iter": it, "energy_change": (E - E_old) / 2, "eps": eps})
+        E_old = E
+        if alg.verbosity:
+            print(f"IDMRG {it}: dE = {hist[-1]['energy_change']:.14f}  eps = {eps:.3e}")
+        if eps <= alg.tol or it >= alg.maxiter:
+            break
+    psi = InfiniteMPS.from_tensor(AR, tol=_dyn_tol(eps, it, 1e-6), maxiter=200)
+    envs.recalculate(psi, tol=1e-10)
     return psi, envs, eps, hist
 
 

@@ -260,9 +260,18 @@ def heisenberg_XXX(L, J=1.0, dtype=np.complex128, infinite=False, u1=False):
     return FiniteMPOHamiltonian(L, 2, [((i, i + 1), h) for i in range(L - 1)], dtype, q)
 
 
-def xxz(L, Jxy=1.0, Jz=1.0, hz=0.0, dtype=np.complex128, infinite=False, u1=False):
+def xxz(L, Jxy=1.0, Jz=1.0, hz=0.0, dtype=np.complex128, infinite=False, u1=False,
+        rotated=False):
+    """sum Jxy (SxSx + SySy) + Jz SzSz - hz sum Sz.  rotated=True applies a rotation by pi
+    about x on every other site (same spectrum; hz = 0 only): Jxy (SxSx - SySy) - Jz SzSz per
+    bond, one-site translation invariant in the Neel phase.  It does not conserve Sz."""
     sx, sy, sz = spin_half()
-    h = Jxy * (kron2(sx, sx) + kron2(sy, sy)) + Jz * kron2(sz, sz)
+    if rotated:
+        if hz or u1:
+            raise ValueError("rotated XXZ: no field and no U(1) charges")
+        h = Jxy * (kron2(sx, sx) - kron2(sy, sy)) - Jz * kron2(sz, sz)
+    else:
+        h = Jxy * (kron2(sx, sx) + kron2(sy, sy)) + Jz * kron2(sz, sz)
     nb = L if infinite else L - 1
     terms = [((i, i + 1), h) for i in range(nb)]
     if hz:

@@ -299,10 +299,18 @@ def heisenberg_terms(L, J=1.0, dtype=np.complex128, periodic=False):
     return [((i, i + 1), _cast(h, dtype)) for i in range(n)]
 
 
-def xxz_terms(L, Jxy=1.0, Jz=1.0, hz=0.0, dtype=np.complex128, periodic=False):
-    """H = sum Jxy (SxSx + SySy) + Jz SzSz - hz sum Sz."""
+def xxz_terms(L, Jxy=1.0, Jz=1.0, hz=0.0, dtype=np.complex128, periodic=False, rotated=False):
+    """H = sum Jxy (SxSx + SySy) + Jz SzSz - hz sum Sz.  rotated=True: the same chain after a
+    rotation by pi about x on every other site (Sy, Sz -> -Sy, -Sz there), which keeps the
+    spectrum and makes the Neel phase (Jz > Jxy > 0) one-site translation invariant:
+    Jxy (SxSx - SySy) - Jz SzSz per bond (only for hz = 0)."""
     sx, sy, sz = spin_ops()
-    h = Jxy * (two_site(sx, sx) + two_site(sy, sy)) + Jz * two_site(sz, sz)
+    if rotated:
+        if hz != 0.0:
+            raise ValueError("the sublattice rotation turns a uniform field into a staggered one")
+        h = Jxy * (two_site(sx, sx) - two_site(sy, sy)) - Jz * two_site(sz, sz)
+    else:
+        h = Jxy * (two_site(sx, sx) + two_site(sy, sy)) + Jz * two_site(sz, sz)
     n = L if periodic else L - 1
     terms = [((i, i + 1), _cast(h, dtype)) for i in range(n)]
     if hz != 0.0:
@@ -424,3 +432,19 @@ def tfim_infinite_energy_density(g, J=1.0, n=200001):
     k = np.linspace(0, np.pi, n)
     f = np.sqrt(J * J + g * g + 2 * J * g * np.cos(k))
     return -float(np.trapezoid(f, k) / np.pi)
+
+
+def xxz_infinite_energy_density(Jz, Jxy=1.0):
+    """Bethe-ansatz ground-state energy per site of sum Jxy (SxSx + SySy) + Jz SzSz (S = sigma/2)
+    for Delta = Jz / Jxy >= 1 (Yang and Yang 1966; des Cloizeaux and Gaudin 1966):
+    Delta = cosh(phi), e = Jxy [Delta/4 - sinh(phi) (1/2 + 2 sum_{n>=1} 1/(exp(2 n phi) + 1))],
+    which tends to Jxy (1/4 - ln 2) at Delta = 1."""
+    delta = Jz / Jxy
+    if delta < 1.0:
+        raise ValueError("closed form restated for Delta >= 1 only")
+    if delta == 1.0:
+        return Jxy * (0.25 - np.log(2.0))
+    phi = np.arccosh(delta)
+    n = np.arange(1, int(min(1e7, 40.0 / phi + 100)) + 1)  # terms below e^-80 dropped
+    s = np.sum(1.0 / (np.exp(np.minimum(2.0 * n * phi, 700.0)) + 1.0))
+    return float(Jxy * (delta / 4.0 - np.sinh(phi) * (0.5 + 2.0 * s)))

@@ -17,6 +17,10 @@ Restates:
   * timestep(::InfiniteMPS, H, t, dt, TDVP()) for a one-site cell -- integrate AC and C with
     the same environments, regauge, uniform gauge, recalculate
         -- src/algorithms/timestep/tdvp.jl:72-133
+  * find_groundstate(::InfiniteMPS, H, IDMRG()) for a one-site cell -- left and right
+    eigensolve of AC with positive QR / LQ and un-normalised environment transfers, the
+    change of C as the error, InfiniteMPS(AR) and recalculated environments at the end
+        -- src/algorithms/groundstate/idmrg.jl:85-216, src/environments/infinite_envs.jl:359-369
 
 The Arnoldi acceleration of the gauge iterations (after eig_miniter = 10 steps) is not
 restated; the QR/LQ iterations converge to the same fixed point.
@@ -235,3 +239,50 @@ def tdvp_timestep_infinite(psi, H, dt, GL=None, GR=None, imaginary=False, tol=1e
     psi2 = InfiniteMPS1(AL, AR, C2)
     GL, GR = infinite_envs(psi2, W, chans, GL, GR, tol=tol)
     return psi2, GL, GR
+
+
+def idmrg(psi, H, tol=1e-10, maxiter=200):
+    """find_groundstate(::InfiniteMPS, H, IDMRG()) for a one-site cell.  Each iteration
+    (idmrg.jl:194-228): AC eigensolve (:SR, DynamicTol factor 1e-3), AL C = AC (positive
+    QR), GL <- GL T(AL) without normalisation (transfer_leftenv!, infinite_envs.jl:359-363);
+    AC eigensolve from the previous AC, C AR = AC (positive LQ), GR <- T(AR) GR; the error
+    is |C - C_old| (idmrg.jl:150-159).  The result is InfiniteMPS(AR) gauge-fixed with the
+    DynamicTol gauge tolerance and recalculated environments (idmrg.jl:131-135).
+    Returns (psi, GL, GR, eps, history) with history entries (iteration, dE, eps), dE the
+    energy change per site (idmrg.jl:162)."""
+    W = H[0]
+    chans = H.chans[0]
+    D, d, _ = psi.AL.shape
+    GL, GR = infinite_envs(psi, W, chans, tol=1e-10)
+    eps = galerkin(psi, W, GL, GR)
+    E_old = energy_density(psi, W, GL, GR)
+    AC, C = psi.AC, psi.C
+    AR = psi.AR
+    it = 0
+    hist = []
+    while True:
+        et = dyn_tol(eps, it, 1e-3)
+        C_old = C
+        _, AC, _ = lanczos_eigsolve(dv.JordanAC(GL, W, GR), AC, krylovdim=30, maxiter=200,
+                                    tol=et, eager=True)
+        Q, C = qr_pos(AC.reshape(D * d, D, order="F"))
+        AL = Q.reshape(D, d, D, order="F")
+        GL = dv.transfer_left(GL, W, AL, AL)
+        E, AC, _ = lanczos_eigsolve(dv.JordanAC(GL, W, GR), AC, krylovdim=30, maxiter=200,
+                                    tol=et, eager=True)
+        C, Q = lq_pos(AC.reshape(D, d * D, order="F"))
+        AR = Q.reshape(D, d, D, order="F")
+        GR = dv.transfer_right(GR, W, AR, AR)
+        eps = float(np.linalg.norm(C - C_old))
+        it += 1
+        hist.append((it, (E - E_old) / 2, eps))
+        E_old = E
+        if eps <= tol or it >= maxiter:
+            break
+    D0 = AR.shape[0]
+    gtol = dyn_tol(eps, it, 1e-6)
+    AL2, C2 = uniform_leftorth(AR, np.eye(D0, dtype=AR.dtype), gtol)
+    AR2, C2 = uniform_rightorth(AL2, C2, gtol)
+    psi2 = InfiniteMPS1(AL2, AR2, C2)
+    GL, GR = infinite_envs(psi2, W, chans, GL, GR, tol=1e-10)
+    return psi2, GL, GR, eps, hist

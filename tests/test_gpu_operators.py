@@ -187,3 +187,26 @@ def test_errors_are_reported_not_crashing(ctx):
     with pytest.raises(L.GBError) as e:
         op(wrong)
     assert e.value.code == L.GB_ERR_ARG
+
+
+def test_launch_trace_accounts_every_launch(ctx):
+    """gb_ctx_trace_begin/end: one event per launch site visit (a site may issue two
+    kernels), charged to named source sites; the per-site times add up to the span."""
+    L_, terms, dt = MODELS["heis_c"]()
+    H, psi, envs = _envs(L_, terms, dt, 16, 26)
+    pos = 3
+    GL, GR = envs.leftenv(pos, psi), envs.rightenv(pos + 1, psi)
+    op = dev_op(ctx, L.GB_HEFF_AC2, GL, H[pos], H[pos + 1], GR, "bf16x3")
+    x = mpsgb.DeviceTensor.from_numpy(ctx, "ac2", _rand(np.random.default_rng(3),
+                                                        (GL.shape[0], 2, GR.shape[0], 2), dt))
+    op(x)
+    ctx.synchronize()
+    n0 = ctx.kernel_launches()
+    ctx.trace_begin()
+    op(x)
+    span, sites = ctx.trace_end()
+    launches = ctx.kernel_launches() - n0
+    assert launches > 0 and sites
+    assert 0 < sum(ev for _, _, ev in sites) <= launches
+    assert all(":" in nm and nm.split(":")[0].endswith(".cu") for nm, _, _ in sites)
+    assert abs(sum(ms for _, ms, _ in sites) - span) <= 1e-3 * max(span, 1.0) + 1e-3

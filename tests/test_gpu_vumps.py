@@ -93,3 +93,51 @@ def test_infinite_imaginary_time_approaches_ground_state(ctx):
         psi, envs = mpsgb.timestep_infinite(psi, H, 0.0, 0.2, alg, envs, imaginary_evolution=True)
     e = mpsgb.infinite.energy_density(psi, envs)
     assert abs(e - M.tfim_infinite_energy_density(g)) < 1e-7
+
+
+def test_vumps_rotated_xxz_neel_phase(ctx):
+    """XXZ with Jxy = 1, Jz = 1.5 after the sublattice rotation: one-site VUMPS on the
+    device converges to the oracle's state energy and sits just above the Bethe-ansatz
+    energy density (D = 24)."""
+    delta = 1.5
+    terms = M.xxz_terms(1, 1.0, delta, periodic=True, rotated=True)
+    oH = M.infinite_mpo_hamiltonian(1, 2, terms)
+    H = mpsgb.xxz(1, 1.0, delta, 0.0, infinite=True, rotated=True)
+    A = _A(24, 7)
+    _, _, _, oeps, ohist = V.vumps(V.infinite_mps(A), oH, tol=1e-10, maxiter=100)
+    psi = mpsgb.InfiniteMPS.from_tensor(A, ctx)
+    psi, envs, eps, hist = mpsgb.find_groundstate_vumps(psi, H, mpsgb.VUMPS(tol=1e-10,
+                                                                            maxiter=100))
+    assert eps <= 1e-9 and oeps <= 1e-9
+    e = hist[-1]["energy"]
+    assert abs(e - ohist[-1][1]) < 1e-10
+    de = e - M.xxz_infinite_energy_density(delta)
+    assert 0.0 <= de < 1e-6
+
+
+@pytest.mark.parametrize("model", ["tfim", "xxz_rotated"])
+def test_idmrg_matches_oracle(ctx, model):
+    """One-site IDMRG (idmrg.jl:194-228) on the device against the oracle from the same
+    initial state: the same iteration count, converged energy density and gauge tensors."""
+    if model == "tfim":
+        terms = M.tfim_terms(1, g=0.5, periodic=True)
+        H = mpsgb.transverse_field_ising(1, g=0.5, infinite=True)
+        exact, maxiter = M.tfim_infinite_energy_density(0.5), 200
+    else:
+        terms = M.xxz_terms(1, 1.0, 3.0, periodic=True, rotated=True)
+        H = mpsgb.xxz(1, 1.0, 3.0, 0.0, infinite=True, rotated=True)
+        exact, maxiter = M.xxz_infinite_energy_density(3.0), 30
+    oH = M.infinite_mpo_hamiltonian(1, 2, terms)
+    A = _A(12, 1)
+    opsi, GL, GR, oeps, ohist = V.idmrg(V.infinite_mps(A), oH, tol=1e-10, maxiter=maxiter)
+    oe = V.energy_density(opsi, oH[0], GL, GR)
+    psi = mpsgb.InfiniteMPS.from_tensor(A, ctx)
+    psi, envs, eps, hist = mpsgb.find_groundstate_idmrg(psi, H, mpsgb.IDMRG(tol=1e-10,
+                                                                            maxiter=maxiter))
+    e = mpsgb.infinite.energy_density(psi, envs)
+    assert abs(e - oe) < 1e-10
+    assert 0.0 <= e - exact < 1e-7
+    if model == "tfim":
+        assert eps <= 1e-10 and len(hist) == len(ohist)
+        AL, AR, C = psi.to_numpy()
+        assert np.allclose(C, opsi.C, atol=1e-8)

@@ -194,3 +194,47 @@ def test_oracle_infinite_tdvp_imaginary_and_real_time():
     for _ in range(5):
         psi, GL, GR = V.tdvp_timestep_infinite(psi, oH2, 0.05, GL, GR)
     assert abs(V.energy_density(psi, oH2[0], GL, GR) - e1) < 1e-6
+
+
+def test_rotated_xxz_is_unitarily_equivalent():
+    """The sublattice rotation (pi about x on every other site) maps the XXZ bond term
+    Jxy (SxSx + SySy) + Jz SzSz onto Jxy (SxSx - SySy) - Jz SzSz: same spectrum, and the
+    open-chain ground energies agree (ED, L = 8)."""
+    sx, sy, sz = M.spin_ops()
+    h = (M.two_site(sx, sx) + M.two_site(sy, sy) + 1.5 * M.two_site(sz, sz)).reshape(4, 4)
+    hr = (M.two_site(sx, sx) - M.two_site(sy, sy) - 1.5 * M.two_site(sz, sz)).reshape(4, 4)
+    U = np.kron(np.eye(2), 2 * sx)
+    assert np.allclose(U @ h @ U.conj().T, hr, atol=1e-15)
+    e = M.ed_ground_energy(8, 2, M.xxz_terms(8, 1.0, 1.5))[0]
+    er = M.ed_ground_energy(8, 2, M.xxz_terms(8, 1.0, 1.5, rotated=True))[0]
+    assert abs(e - er) < 1e-12
+
+
+def test_oracle_vumps_rotated_xxz_bethe_ansatz():
+    """One-site VUMPS on the rotated XXZ chain in the Neel phase (Delta = 3) approaches the
+    Bethe-ansatz energy density from above (variational, D = 12)."""
+    from oracle import vumps as V
+    delta = 3.0
+    H = M.infinite_mpo_hamiltonian(1, 2, M.xxz_terms(1, 1.0, delta, periodic=True,
+                                                     rotated=True))
+    rng = np.random.default_rng(7)
+    A = rng.standard_normal((12, 2, 12)) + 1j * rng.standard_normal((12, 2, 12))
+    psi, GL, GR, eps, hist = V.vumps(V.infinite_mps(A), H, tol=1e-10, maxiter=40)
+    de = hist[-1][1] - M.xxz_infinite_energy_density(delta)
+    assert 0.0 <= de < 2e-8
+    # the closed form at Delta = 1 is 1/4 - ln 2, and it is continuous there
+    assert abs(M.xxz_infinite_energy_density(1.0 + 1e-9) - (0.25 - np.log(2.0))) < 1e-6
+
+
+def test_oracle_idmrg_tfim_closed_form():
+    """One-site IDMRG (idmrg.jl:194-228) on the infinite TFIM (g = 0.5) reaches the
+    free-fermion energy density, and its last energy change per site agrees with it."""
+    from oracle import vumps as V
+    H = M.infinite_mpo_hamiltonian(1, 2, M.tfim_terms(1, g=0.5, periodic=True))
+    rng = np.random.default_rng(1)
+    A = rng.standard_normal((12, 2, 12)) + 1j * rng.standard_normal((12, 2, 12))
+    psi, GL, GR, eps, hist = V.idmrg(V.infinite_mps(A), H, tol=1e-10, maxiter=100)
+    exact = M.tfim_infinite_energy_density(0.5)
+    assert eps <= 1e-10
+    assert abs(V.energy_density(psi, H[0], GL, GR) - exact) < 1e-12
+    assert abs(hist[-1][1] - exact) < 1e-10
