@@ -179,6 +179,16 @@ int gb_heff_terms(const gb_heff* h, char* buf, size_t len);
 /* algorithmic flops of one application (unsplit shapes; 2 flops/real MAC, 8/complex MAC) */
 int gb_heff_flops(const gb_heff* h, double* flops);
 int gb_heff_set_precision(gb_heff* h, int precision);
+/* U(1) sectors of the operator's vector space: x[l, s1, r, s2] (AC2) or x[l, s, r] (AC) is
+ * allowed where q_left[l] + q_phys1[s1] (+ q_phys2[s2]) = q_right[r], with q_left sorted
+ * ascending (the charge-sorted dense embedding).  The continuing-channel charges are read off
+ * the left environment; the fused AA chain then computes only the charge-allowed entries of
+ * its intermediate -- the others are exact zeros -- instead of the whole dense embedding.
+ * Optional: results are unchanged.  (TensorKit's block structure of the same contraction,
+ * src/algorithms/derivatives/hamiltonian_derivatives.jl:243-369.)  GB_ERR_ARG if the
+ * environment does not conserve the given charges. */
+int gb_heff_set_sectors(gb_heff* h, const int32_t* q_left, const int32_t* q_phys1,
+                        const int32_t* q_phys2, const int32_t* q_right);
 /* y = H(x)   (hamiltonian_derivatives.jl:472-500; mpo_derivatives.jl:85-98) */
 int gb_heff_apply(gb_heff* h, const gb_tensor* x, gb_tensor* y);
 /* fixedpoint(H, x0, :SR, Lanczos(krylovdim, maxiter, tol, eager)) run entirely on the

@@ -74,6 +74,8 @@ gb_heff* heff_build(gb_ctx* ctx, int kind, const gb_tensor* GL, const gb_tensor*
                     const gb_tensor* W2, const gb_tensor* GR, int prec);
 void heff_free(gb_heff* h);
 void heff_set_precision(gb_heff* h, int prec);
+void heff_set_sectors(gb_heff* h, const int32_t* ql, const int32_t* qp1, const int32_t* qp2,
+                      const int32_t* qr);
 void heff_apply_raw(gb_heff* h, const void* x, void* y);
 int env_linsolve_raw(gb_ctx* ctx, int side, const gb_tensor* W, const gb_tensor* A, int prec,
                      const gb_tensor* lvec, const gb_tensor* rvec, const gb_tensor* b,
@@ -1183,6 +1185,18 @@ int gb_heff_set_precision(gb_heff* h, int precision) {
   API_BEGIN
   GB_REQUIRE(h, "null operator");
   heff_set_precision(h, precision);
+  API_END
+}
+
+int gb_heff_set_sectors(gb_heff* h, const int32_t* q_left, const int32_t* q_phys1,
+                        const int32_t* q_phys2, const int32_t* q_right) {
+  API_BEGIN
+  GB_REQUIRE(h && q_left && q_phys1 && q_right, "null argument");
+  HeffInfo hi = heff_info(h);
+  GB_REQUIRE(hi.kind != GB_HEFF_C, "set_sectors: AC or AC2 operators only");
+  GB_REQUIRE(hi.kind != GB_HEFF_AC2 || q_phys2, "set_sectors: AC2 needs both physical legs");
+  DevGuard g(hi.ctx->device);
+  heff_set_sectors(h, q_left, q_phys1, q_phys2, q_right);
   API_END
 }
 

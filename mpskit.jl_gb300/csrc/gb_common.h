@@ -254,6 +254,10 @@ struct MixSkipDev {
   const int64_t* coff = nullptr;
   int64_t xnM = 0;
   uint32_t* prev = nullptr;
+  // U(1) sectors (optional): output (a, J, n) is structurally zero outside
+  // a in [arange[J + nJ*n].x, .y); those entries are never written (they stay zero)
+  const int2* arange = nullptr;
+  int64_t arange_max = 0;
 };
 // leg mix whose output is written directly as the packed B operand of the next GEMM
 // (kJ[J]: contraction-index offset of output row J, mJ[J] + n*mn: output column index)
@@ -261,8 +265,11 @@ void mixpack_run(gb_ctx* ctx, const MixDev& m, const int64_t* kJ, const int64_t*
                  int dtype, const void* x, Packed& out, int64_t Klog, int64_t Nlog,
                  const MixSkipDev* skip = nullptr, bool x_f32 = false);
 // outmap (optional, batch 1, split precision only): bit (m/128)*ceil(N/128) + n/128 is set
-// for every 128 x 128 region of C that receives a contribution; for real data the regions
-// that receive none are then not written (the consumer must read C only where set)
+// for every 128 x 128 region of C that receives a contribution.  For real data the regions
+// that receive none are not written, except where the previous call with the same map wrote
+// them: those are overwritten with zeros.  The buffer holds two maps (2 * outmap_bytes): the
+// current one and, behind it, the previous call's; started at zero together with C, every
+// region outside the current map then holds zeros.
 size_t outmap_bytes(int64_t M, int64_t N);
 // c_f32: C is stored in FP32 (exact for alpha = 1, beta = 0: the FP32 accumulator itself)
 void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_t M,

@@ -312,32 +312,53 @@ __global__ void mixpack_kernel(int64_t A, int64_t N, int64_t xn, const int64_t* 
   };
   for (int64_t n = blockIdx.z; n < N; n += gridDim.z) {
     const int64_t m = mJ[J] + n * mn;
+    // U(1): only the l' sector of (J, n) can be nonzero; every entry of it is written on
+    // every call, and the rest of the operand stays zero from its allocation
+    int64_t lo = 0, hi = A;
+    if (sk.arange) {
+      const int2 r = sk.arange[n * gridDim.y + J];
+      lo = r.x;
+      hi = r.y;
+    }
     // every thread of the block runs the same number of iterations (warp-wide votes below)
-    for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < A;
+    for (int64_t base = lo + blockIdx.x * (int64_t)blockDim.x; base < hi;
          base += (int64_t)gridDim.x * blockDim.x) {
       const int64_t a = base + threadIdx.x;
-      bool valid = a < A;
+      bool valid = a < hi;
       const int64_t k = a + kJ[J];
       bool nz = false;
-      if (valid && sk.xmap) {
-        // all inputs in regions of x that its producer left unwritten (no contribution):
-        // the value is zero; it is written only where the previous apply marked its box
-        bool any = false;
-        for (int e = e0; e < e1 && !any; ++e) {
-          const int i = col[e];
-          const int64_t bit = ((a + sk.roff[i]) >> 7) * sk.onc + ((sk.coff[i] + n * sk.xnM) >> 7);
-          any = (sk.xmap[bit >> 5] >> (bit & 31)) & 1u;
-        }
-        if (!any) {
-          const int64_t kb0 = k / BK;
-          auto prev = [&](int64_t row, int64_t kb) {
-            return (sk.prev[(row / MASK_ROWS) * kw + kb / 32] >> (kb % 32)) & 1u;
-          };
-          if (prev(m, kb0)) put(m, k, 0.0);
-          if (CPLX) {
-            if (prev(m, kb0 + Kh / BK)) put(m, Kh + k, 0.0);
-            if (prev(Nlog + m, kb0)) put(Nlog + m, k, 0.0);
-            if (prev(Nlog + m, kb0 + Kh / BK)) put(Nlog + m, Kh + k, 0.0);
+      // input e of element (a, n) lies in box (row, column) of x's written-region map; the
+      // producer keeps every region outside the map at zero
+      auto box_set = [&](int i, int64_t row) {
+        const int64_t bit = ((row + sk.roff[i]) >> 7) * sk.onc + ((sk.coff[i] + n * sk.xnM) >> 7);
+        return ((sk.xmap[bit >> 5] >> (bit & 31)) & 1u) != 0u;
+      };
+      if (sk.xmap && !sk.arange) {
+        // warp-wide test first: the warp's 32 rows span at most two row boxes per input, so
+        // one pass of the lanes over the inputs decides whether anything is there to read
+        const int64_t wa0 = base + (threadIdx.x & ~31);
+        const int64_t wa1 = (wa0 + 31 < A ? wa0 + 31 : A - 1);
+        bool hit = false;
+        if (wa0 < A)
+          for (int e = e0 + lane; e < e1 && !hit; e += 32) {
+            const int i = col[e];
+            hit = box_set(i, wa0) || box_set(i, wa1);
+          }
+        hit = __any_sync(0xffffffffu, hit);
+        if (!hit) {
+          // nothing to read: the output is zero; it is written only where the previous
+          // apply marked its box (the planes hold zeros everywhere else)
+          if (valid) {
+            const int64_t kb0 = k / BK;
+            auto prev = [&](int64_t row, int64_t kb) {
+              return (sk.prev[(row / MASK_ROWS) * kw + kb / 32] >> (kb % 32)) & 1u;
+            };
+            if (prev(m, kb0)) put(m, k, 0.0);
+            if (CPLX) {
+              if (prev(m, kb0 + Kh / BK)) put(m, Kh + k, 0.0);
+              if (prev(Nlog + m, kb0)) put(Nlog + m, k, 0.0);
+              if (prev(Nlog + m, kb0 + Kh / BK)) put(Nlog + m, Kh + k, 0.0);
+            }
           }
           valid = false;  // nothing to compute or mark
         }
@@ -413,7 +434,8 @@ void mixpack_run(gb_ctx* ctx, const MixDev& m, const int64_t* kJ, const int64_t*
   clear_mask(ctx, out);
   // a block walks N / gridDim.z output columns: long-lived blocks, since with structural
   // skipping most of a block's work is a map test
-  dim3 grid((unsigned)std::min<int64_t>((m.A + 127) / 128, 64), (unsigned)m.nJ,
+  const int64_t span = sk.arange ? std::max<int64_t>(sk.arange_max, 1) : m.A;
+  dim3 grid((unsigned)std::min<int64_t>((span + 127) / 128, 64), (unsigned)m.nJ,
             (unsigned)std::min<int64_t>(m.N, 32));
   const int64_t plane = out.rows * out.Kp;
 #define GB_MIXPACK(C, E, TX)                                                                  \
@@ -713,6 +735,7 @@ struct PArgs {
   // output tile that receives a contribution; with skip_zero_out, tiles that receive none
   // are not written at all (the consumer reads C only where the map is set)
   uint32_t* outmap;
+  const uint32_t* prevmap;  // the previous call's map: its tiles are zeroed if not rewritten
   int64_t onc;
   int skip_zero_out;
   int c_f32;  // C is stored in FP32 (exact when alpha = 1 and beta = 0: C is the accumulator)
@@ -823,6 +846,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         if (nk > 0 || (args.beta != 1.0 && !args.skip_zero_out)) {
           t = c;
           break;
+        }
+        if (args.prevmap && args.beta == 0.0) {
+          // written by the previous call, nothing this time: overwrite with zeros
+          const int64_t n0 = (int64_t)ni * BN, n1 = std::min<int64_t>(n0 + BN, args.N);
+          bool stale = false;
+          for (int64_t g = n0 / 128; g <= (n1 - 1) / 128 && !stale; ++g) {
+            const int64_t bit = (int64_t)mi * args.onc + g;
+            stale = (args.prevmap[bit >> 5] >> (bit & 31)) & 1u;
+          }
+          if (stale) {
+            t = c;
+            break;
+          }
         }
       }
       const int slot = j % PS_RING;
@@ -1145,11 +1181,20 @@ void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_
     p.status = ctx->d_status;
     p.work = (ctx->profiling || ctx->counting) ? ctx->d_work : nullptr;
     p.outmap = outmap;
+    p.prevmap = nullptr;
     p.onc = (N + 127) / 128;
     p.skip_zero_out = (outmap && !A.cplx) ? 1 : 0;
     p.c_f32 = c_f32 ? 1 : 0;
-    if (outmap)
-      GB_CHECK_CUDA(cudaMemsetAsync(outmap, 0, outmap_bytes(M, N), ctx->stream));
+    if (outmap) {
+      const size_t mb = outmap_bytes(M, N);
+      if (p.skip_zero_out) {
+        uint32_t* prev = outmap + mb / 4;
+        GB_CHECK_CUDA(
+            cudaMemcpyAsync(prev, outmap, mb, cudaMemcpyDeviceToDevice, ctx->stream));
+        p.prevmap = prev;
+      }
+      GB_CHECK_CUDA(cudaMemsetAsync(outmap, 0, mb, ctx->stream));
+    }
     GB_CHECK_CUDA(cudaMemsetAsync(ctx->d_tile_counter, 0, sizeof(unsigned int), ctx->stream));
     const unsigned grid = (unsigned)std::min<int64_t>(ntiles, std::max(1, ctx->num_sms));
 #define GB_PERSISTENT(BN_, ST_, TF_)                                                          \

@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <sstream>
 
@@ -144,6 +145,14 @@ struct gb_heff {
   int64_t* t1rc_dev = nullptr;
   uint32_t* t2prev = nullptr;
   bool t1_f32 = false;  // T1 currently holds FP32 values (fused split chain)
+  // U(1) sectors of the fused chain (gb_heff_set_sectors): output row J of the mix is
+  // (continuing channel Jc[J], fused physical index Jp[J]); element (a, J, n) may be nonzero
+  // only for a in arange[J + nJ * n] -- the l' sector of charge q_r(n) - dq_c - q_p
+  const void* aa_glc = nullptr;  // GL's continuing channels (l, l', c)
+  int64_t aa_chr = 0, aa_Dl = 0, aa_Dr = 0, aa_np = 0;
+  std::vector<int64_t> Jc, Jp;
+  int2* arange = nullptr;
+  int64_t arange_max = 0;
 };
 
 namespace gb {
@@ -194,7 +203,15 @@ static void prepare_t2p(gb_heff* h) {
   // zeroed once: the fused mix then writes only entries that may be nonzero (see MixSkipDev)
   GB_CHECK_CUDA(cudaMemsetAsync(h->t2p.data, 0, bytes, h->ctx->stream));
   if (h->t1M > 0) {
-    h->t1map = (uint32_t*)dalloc(h, outmap_bytes(h->t1M, h->t1N));
+    // current and previous output maps of the T1 GEMM, and T1 itself, start at zero: the
+    // regions outside the current map then always hold zeros (the GEMM re-zeroes regions
+    // the previous apply wrote), so the fused mix may read any input without testing it
+    const size_t mb = outmap_bytes(h->t1M, h->t1N);
+    h->t1map = (uint32_t*)dalloc(h, 2 * mb);
+    GB_CHECK_CUDA(cudaMemsetAsync(h->t1map, 0, 2 * mb, h->ctx->stream));
+    GB_REQUIRE(h->t1, "heff: T1 buffer missing");
+    GB_CHECK_CUDA(cudaMemsetAsync(h->t1, 0, (size_t)h->t1M * h->t1N * sizeof(float),
+                                  h->ctx->stream));
     h->t2prev = (uint32_t*)dalloc(h, (size_t)h->t2p.mrows * h->t2p.kw * 4);
     const size_t ni = h->t1roff.size();
     h->t1rc_dev = (int64_t*)dalloc(h, 2 * ni * sizeof(int64_t));
@@ -459,6 +476,17 @@ static void build_ac2(gb_heff* h, const gb_tensor* GL, const gb_tensor* W1,
     h->mn = d1 * d2;
     h->t2K = Dl * chr;
     h->t2N = d1 * d2 * Dr;
+    h->aa_glc = glc;
+    h->aa_chr = chr;
+    h->aa_Dl = Dl;
+    h->aa_Dr = Dr;
+    h->aa_np = d1 * d2;
+    h->Jc.resize(chr * d1 * d2);
+    h->Jp.resize(chr * d1 * d2);
+    for (int64_t J = 0; J < chr * d1 * d2; ++J) {
+      h->Jc[J] = J % chr;
+      h->Jp[J] = J / chr;  // sa + d1 * sb
+    }
     // step 3: Y[l, (s1 s2 r)] (+)= GLc[l, (l' c)] . T2[(l' c), (s1 s2 r)]
     Step s3;
     s3.name = "AA3";
@@ -885,6 +913,17 @@ static void build_ac(gb_heff* h, const gb_tensor* GL, const gb_tensor* W, const 
     h->mn = d;
     h->t2K = Dl * chr;
     h->t2N = d * Dr;
+    h->aa_glc = glc;
+    h->aa_chr = chr;
+    h->aa_Dl = Dl;
+    h->aa_Dr = Dr;
+    h->aa_np = d;
+    h->Jc.resize(chr * d);
+    h->Jp.resize(chr * d);
+    for (int64_t J = 0; J < chr * d; ++J) {
+      h->Jc[J] = J % chr;
+      h->Jp[J] = J / chr;
+    }
     Step s3;
     s3.name = "A3";
     s3.srcA = S_CONST;
@@ -1146,6 +1185,90 @@ void heff_free(gb_heff* h) {
 
 int heff_precision(const gb_heff* h) { return h->prec; }
 
+// dq[c] = q_l(l) - q_l(l') over the nonzero entries of GL's continuing channel c (one
+// value per channel when GL conserves charge; INT_MIN: the channel is zero)
+__global__ void channel_charge_kernel(const double* __restrict__ glc, int64_t Dl, int64_t chr,
+                                      int cplx, const int* __restrict__ ql, int* dq, int* bad) {
+  const int64_t n = Dl * Dl * chr;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const bool nz = cplx ? (glc[2 * i] != 0.0 || glc[2 * i + 1] != 0.0) : glc[i] != 0.0;
+    if (!nz) continue;
+    const int64_t l = i % Dl, lp = (i / Dl) % Dl, c = i / (Dl * Dl);
+    const int v = ql[l] - ql[lp];
+    const int old = atomicCAS(&dq[c], INT_MIN, v);
+    if (old != INT_MIN && old != v) atomicExch(bad, 1);
+  }
+}
+
+void heff_set_sectors(gb_heff* h, const int32_t* ql, const int32_t* qp1, const int32_t* qp2,
+                      const int32_t* qr) {
+  gb_ctx* ctx = h->ctx;
+  const int64_t Dl = h->xdims[0], Dr = h->xdims[2];  // x: (l, s1, r, s2) or (l, s, r)
+  for (int64_t i = 1; i < Dl; ++i)
+    GB_REQUIRE(ql[i - 1] <= ql[i], "set_sectors: left charges must be sorted ascending");
+  if (!h->aa_glc || h->kJ.empty()) return;  // no fused chain: nothing to restrict
+  GB_REQUIRE(h->aa_Dl == Dl && h->aa_Dr == Dr, "set_sectors: bond dimensions");
+  const int64_t chr = h->aa_chr;
+  // fused physical charges of the mix rows
+  std::vector<int> qp(h->aa_np);
+  if (h->kind == GB_HEFF_AC2) {
+    const int64_t d1 = h->xdims[1], d2 = h->xdims[3];
+    GB_REQUIRE(qp2, "set_sectors: two physical legs expected");
+    for (int64_t sb = 0; sb < d2; ++sb)
+      for (int64_t sa = 0; sa < d1; ++sa) qp[sa + d1 * sb] = qp1[sa] + qp2[sb];
+  } else {
+    for (int64_t s = 0; s < h->aa_np; ++s) qp[s] = qp1[s];
+  }
+  // channel charges from GL itself
+  int* dev = nullptr;
+  GB_CHECK_CUDA(cudaMallocAsync(&dev, (Dl + chr + 1) * sizeof(int), ctx->stream));
+  std::vector<int> init(chr + 1, INT_MIN);
+  init[chr] = 0;
+  GB_CHECK_CUDA(cudaMemcpyAsync(dev, ql, Dl * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  GB_CHECK_CUDA(cudaMemcpyAsync(dev + Dl, init.data(), (chr + 1) * sizeof(int),
+                                cudaMemcpyHostToDevice, ctx->stream));
+  channel_charge_kernel<<<(unsigned)std::min<int64_t>((Dl * Dl * chr + 255) / 256, 152 * 16),
+                          256, 0, ctx->stream>>>((const double*)h->aa_glc, Dl, chr,
+                                                 is_cplx(h->dtype) ? 1 : 0, dev, dev + Dl,
+                                                 dev + Dl + chr);
+  GB_CHECK_CUDA(cudaGetLastError());
+  count_launch(ctx);
+  std::vector<int> dq(chr + 1);
+  GB_CHECK_CUDA(cudaMemcpyAsync(dq.data(), dev + Dl, (chr + 1) * sizeof(int),
+                                cudaMemcpyDeviceToHost, ctx->stream));
+  GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  GB_CHECK_CUDA(cudaFreeAsync(dev, ctx->stream));
+  GB_REQUIRE(dq[chr] == 0, "set_sectors: the left environment does not conserve these charges");
+  // sector table of the (sorted) left charges, indexed by charge - ql[0]
+  const int64_t qmin = ql[0], qspan = (int64_t)ql[Dl - 1] - qmin + 1;
+  std::vector<int2> sec((size_t)qspan, int2{0, 0});
+  for (int64_t i = 0; i < Dl; ++i) {
+    int2& r = sec[(size_t)(ql[i] - qmin)];
+    if (r.y == 0) r.x = (int)i;
+    r.y = (int)i + 1;
+  }
+  const int64_t nJ = (int64_t)h->kJ.size();
+  std::vector<int2> tab((size_t)nJ * Dr);
+  int64_t mx = 0;
+  for (int64_t n = 0; n < Dr; ++n)
+    for (int64_t J = 0; J < nJ; ++J) {
+      int2 r{0, 0};
+      const int d = dq[h->Jc[J]];
+      if (d != INT_MIN) {
+        const int64_t t = (int64_t)qr[n] - d - qp[h->Jp[J]] - qmin;
+        if (t >= 0 && t < qspan) r = sec[(size_t)t];
+      }
+      tab[(size_t)n * nJ + J] = r;
+      mx = std::max<int64_t>(mx, r.y - r.x);
+    }
+  if (!h->arange) h->arange = (int2*)dalloc(h, tab.size() * sizeof(int2));
+  GB_CHECK_CUDA(cudaMemcpyAsync(h->arange, tab.data(), tab.size() * sizeof(int2),
+                                cudaMemcpyHostToDevice, ctx->stream));
+  GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  h->arange_max = mx;
+}
+
 void heff_set_precision(gb_heff* h, int prec) {
   GB_REQUIRE(prec == GB_PREC_FP64 || prec == GB_PREC_BF16X3 || prec == GB_PREC_TF32X3,
              "heff: precision");
@@ -1202,6 +1325,10 @@ void heff_apply_raw(gb_heff* h, const void* x, void* y) {
         sk.coff = h->t1rc_dev + h->t1roff.size();
         sk.xnM = h->t1xnM;
         sk.prev = h->t2prev;
+      }
+      if (h->arange && s.src == S_T1) {
+        sk.arange = h->arange;
+        sk.arange_max = h->arange_max;
       }
       mixpack_run(ctx, s.mix, kJ, kJ + h->kJ.size(), h->mn, h->dtype, ptr(s.src, nullptr), h->t2p,
                   h->t2K, h->t2N, sk.xmap ? &sk : nullptr, sk.xmap && h->t1_f32);

@@ -97,6 +97,7 @@ _SIGS = {
     "gb_heff_terms": ([P, ctypes.c_char_p, SZ], INT),
     "gb_heff_flops": ([P, PD], INT),
     "gb_heff_set_precision": ([P, INT], INT),
+    "gb_heff_set_sectors": ([P, PI32, PI32, PI32, PI32], INT),
     "gb_heff_apply": ([P, P, P], INT),
     "gb_heff_eigsolve": ([P, P, INT, INT, D, INT, PD, ctypes.POINTER(KrylovInfo)], INT),
     "gb_heff_exponentiate": ([P, P, D, D, INT, INT, D, ctypes.POINTER(KrylovInfo)], INT),

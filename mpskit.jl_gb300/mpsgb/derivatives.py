@@ -57,6 +57,7 @@ class DerivativeOperator:
         self.handle = h
         # keep the environments alive: the operator references their device storage
         self._keep = (GL, GR, W1, W2)
+        self._sectors = None
         self.dtype = GL.dtype
         Dl, Dr = GL.dims[0], GR.dims[0]
         if kind == L.GB_HEFF_AC2:
@@ -82,10 +83,27 @@ class DerivativeOperator:
         code = L.PRECISIONS[precision]
         L.check(L.lib().gb_heff_set_precision(self.handle, code))
 
+    def set_sectors(self, x):
+        """Hand the U(1) leg charges of x (AC: (l, s, r); AC2: (l, s1, r, s2)) to the
+        operator once (gb_heff_set_sectors): its fused chain then skips the exact zeros of
+        the charge-sorted embedding.  No-op for dense vectors and C operators."""
+        if self._sectors is not None or x.charges is None or self.kind == L.GB_HEFF_C:
+            return
+        q = [np.ascontiguousarray(c, dtype=np.int32) for c in x.charges]
+        p = lambda a: a.ctypes.data_as(L.PI32)
+        if self.kind == L.GB_HEFF_AC2:
+            ql, qs1, qr, qs2 = q
+            L.check(L.lib().gb_heff_set_sectors(self.handle, p(ql), p(qs1), p(qs2), p(qr)))
+        else:
+            ql, qs, qr = q
+            L.check(L.lib().gb_heff_set_sectors(self.handle, p(ql), p(qs), None, p(qr)))
+        self._sectors = q
+
     def new_vector(self):
         return DeviceTensor(self.ctx, self.xkind, self.dtype, self.xdims)
 
     def __call__(self, x, out=None):
+        self.set_sectors(x)
         y = out if out is not None else x.similar()
         L.check(L.lib().gb_heff_apply(self.handle, x.handle, y.handle))
         return y
@@ -143,6 +161,7 @@ def fixedpoint(A, x0, which="SR", alg=None):
     if which != "SR":
         raise NotImplementedError("only :SR eigensolves run on the device")
     alg = alg or Lanczos()
+    A.set_sectors(x0)
     x = x0.copy()
     lam = ctypes.c_double()
     ki = L.KrylovInfo()
@@ -155,6 +174,7 @@ def fixedpoint(A, x0, which="SR", alg=None):
 def exponentiate(A, t, x0, alg=None):
     """exp(t A) x0 (KrylovKit.exponentiate); returns (y, info)."""
     alg = alg or Lanczos(tol=1e-12)
+    A.set_sectors(x0)
     t = complex(t)
     y = x0.copy()
     ki = L.KrylovInfo()

@@ -157,3 +157,41 @@ def test_u1_dmrg2_split_precision_gram(ctx):
         ctx.set_precision("fp64")
     e_ref = ohist[-1][1]
     assert abs(e - e_ref) < 1e-9 * abs(e_ref), (e, e_ref)
+
+
+@pytest.mark.parametrize("prec", ["bf16x3", "tf32x3"])
+def test_sector_restricted_chain_is_exact(ctx, prec):
+    """gb_heff_set_sectors: the fused AA chain of a U(1) J1-J2 operator computes only the
+    charge-allowed entries of its intermediate; the result is bit-for-bit the one of the
+    same operator without sectors (AC2 and one-site AC, two applications each)."""
+    L_, pos = 12, 5
+    H = mpsgb.j1j2_cylinder(4, 3, u1=True)
+    As, qb = HU.random_u1_tensors(L_, 96, 13, 0, np.float64)
+    psi = mpsgb.FiniteMPS.from_tensors(As, ctx, center=pos + 1, charges=(qb, QP))
+    envs = mpsgb.FiniteEnvironments(psi, H)
+    be = mpsgb.GB300Backend(prec)
+    ac2 = mpsgb.ac2_from(psi.AL[pos], psi.ac(pos + 1))
+    plain = ac2.copy()
+    plain.charges = None  # the same vector without its leg charges: no sectors
+    Hs = mpsgb.AC2_hamiltonian(pos, psi, H, envs, be)
+    assert "AA" in Hs.terms
+    ys = [Hs(ac2).numpy() for _ in range(2)]
+    assert Hs._sectors is not None
+    yd = mpsgb.AC2_hamiltonian(pos, psi, H, envs, be)(plain).numpy()
+    assert np.array_equal(ys[0], yd) and np.array_equal(ys[1], yd)
+    ac = psi.ac(pos + 1)
+    Hs1 = mpsgb.AC_hamiltonian(pos + 1, psi, H, envs, be)
+    y1 = Hs1(ac).numpy()
+    assert Hs1._sectors is not None
+    ac_plain = ac.copy()
+    ac_plain.charges = None
+    y1d = mpsgb.AC_hamiltonian(pos + 1, psi, H, envs, be)(ac_plain).numpy()
+    assert np.array_equal(y1, y1d)
+    # unsorted left charges are refused
+    bad = mpsgb.AC2_hamiltonian(pos, psi, H, envs, be)
+    q = [np.ascontiguousarray(c, dtype=np.int32) for c in ac2.charges]
+    q0 = q[0][::-1].copy()
+    if np.any(np.diff(q0) < 0):
+        p = lambda a: a.ctypes.data_as(L.PI32)
+        with pytest.raises(RuntimeError):
+            L.check(L.lib().gb_heff_set_sectors(bad.handle, p(q0), p(q[1]), p(q[3]), p(q[2])))
