@@ -133,6 +133,17 @@ void* scratch(gb_ctx* ctx, int slot, size_t bytes);
 // stream is synchronised first, every lane's stream at the end; the first exception thrown
 // by any item is rethrown after all lanes stopped
 void run_on_lanes(gb_ctx* ctx, int64_t n, const std::function<void(gb_ctx*, int64_t)>& fn);
+// U(1) operators (after gb_heff_set_sectors): the Krylov solvers keep only the n allowed
+// entries of their vectors; xcomp is an operator-owned compact vector
+struct HeffCompact {
+  int64_t n = 0;
+  void* xcomp = nullptr;
+};
+bool heff_compact(gb_heff* h, HeffCompact* c);
+void heff_gather(gb_heff* h, const void* dense, void* compact);
+void heff_scatter(gb_heff* h, const void* compact, void* dense);  // zero-fills dense first
+void heff_apply_compact(gb_heff* h, const void* x, void* y);
+
 // launch accounting (and, while tracing, an event tagged with the issuing source line)
 void trace_point(gb_ctx* ctx, const char* file, int line);
 inline void count_launch_at(gb_ctx* ctx, int n, const char* file, int line) {

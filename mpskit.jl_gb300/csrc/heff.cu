@@ -153,6 +153,13 @@ struct gb_heff {
   std::vector<int64_t> Jc, Jp;
   int2* arange = nullptr;
   int64_t arange_max = 0;
+  // U(1) sectors of x itself: column j of the device layout (l fastest) holds its allowed
+  // entries in one run of l; runs[3j..3j+2] = (compact offset, dense offset, length)
+  int64_t* runs = nullptr;
+  int64_t nruns = 0, ncompact = 0;
+  void* xfull = nullptr;  // dense staging of the Krylov solvers (zero outside the runs)
+  void* yfull = nullptr;
+  void* xcomp = nullptr;  // a compact state vector (exponentiate)
 };
 
 namespace gb {
@@ -1201,13 +1208,109 @@ __global__ void channel_charge_kernel(const double* __restrict__ glc, int64_t Dl
   }
 }
 
+void heff_apply_raw(gb_heff* h, const void* x, void* y);
+
+template <typename T>
+__global__ void runs_copy_kernel(const int64_t* __restrict__ runs, int64_t nruns,
+                                 const T* __restrict__ src, T* __restrict__ dst, int scatter) {
+  for (int64_t c = blockIdx.x; c < nruns; c += gridDim.x) {
+    const int64_t co = runs[3 * c], dof = runs[3 * c + 1], len = runs[3 * c + 2];
+    for (int64_t i = threadIdx.x; i < len; i += blockDim.x) {
+      if (scatter) dst[dof + i] = src[co + i];
+      else dst[co + i] = src[dof + i];
+    }
+  }
+}
+
+// compact <-> dense copies of the allowed entries (scatter = 1: compact -> dense)
+static void runs_copy(gb_heff* h, const void* src, void* dst, int scatter) {
+  gb_ctx* ctx = h->ctx;
+  const unsigned grid = (unsigned)std::min<int64_t>(h->nruns, 152 * 8);
+  if (grid == 0) return;
+  if (is_cplx(h->dtype))
+    runs_copy_kernel<double2><<<grid, 256, 0, ctx->stream>>>(h->runs, h->nruns,
+                                                             (const double2*)src, (double2*)dst,
+                                                             scatter);
+  else
+    runs_copy_kernel<double><<<grid, 256, 0, ctx->stream>>>(h->runs, h->nruns,
+                                                            (const double*)src, (double*)dst,
+                                                            scatter);
+  GB_CHECK_CUDA(cudaGetLastError());
+  count_launch(ctx);
+}
+
+bool heff_compact(gb_heff* h, HeffCompact* c) {
+  if (!h->runs) return false;
+  const size_t es = elem_size(h->dtype);
+  if (!h->xfull) {
+    h->xfull = dalloc(h, (size_t)h->xnumel * es);
+    GB_CHECK_CUDA(cudaMemsetAsync(h->xfull, 0, (size_t)h->xnumel * es, h->ctx->stream));
+    h->yfull = dalloc(h, (size_t)h->xnumel * es);
+    h->xcomp = dalloc(h, (size_t)std::max<int64_t>(h->ncompact, 1) * es);
+  }
+  c->n = h->ncompact;
+  c->xcomp = h->xcomp;
+  return true;
+}
+
+void heff_gather(gb_heff* h, const void* dense, void* compact) { runs_copy(h, dense, compact, 0); }
+
+void heff_scatter(gb_heff* h, const void* compact, void* dense) {
+  fill_zero(h->ctx, dense, (size_t)h->xnumel * elem_size(h->dtype));
+  runs_copy(h, compact, dense, 1);
+}
+
+// y = H x on compact vectors: scatter into the zero-padded staging vector, apply, gather
+void heff_apply_compact(gb_heff* h, const void* x, void* y) {
+  runs_copy(h, x, h->xfull, 1);
+  heff_apply_raw(h, h->xfull, h->yfull);
+  runs_copy(h, h->yfull, y, 0);
+}
+
 void heff_set_sectors(gb_heff* h, const int32_t* ql, const int32_t* qp1, const int32_t* qp2,
                       const int32_t* qr) {
   gb_ctx* ctx = h->ctx;
   const int64_t Dl = h->xdims[0], Dr = h->xdims[2];  // x: (l, s1, r, s2) or (l, s, r)
   for (int64_t i = 1; i < Dl; ++i)
     GB_REQUIRE(ql[i - 1] <= ql[i], "set_sectors: left charges must be sorted ascending");
-  if (!h->aa_glc || h->kJ.empty()) return;  // no fused chain: nothing to restrict
+  // sector table of the (sorted) left charges, indexed by charge - ql[0]
+  const int64_t qmin = ql[0], qspan = (int64_t)ql[Dl - 1] - qmin + 1;
+  std::vector<int2> sec((size_t)qspan, int2{0, 0});
+  for (int64_t i = 0; i < Dl; ++i) {
+    int2& r = sec[(size_t)(ql[i] - qmin)];
+    if (r.y == 0) r.x = (int)i;
+    r.y = (int)i + 1;
+  }
+  auto sector = [&](int64_t q) {
+    const int64_t t = q - qmin;
+    return (t >= 0 && t < qspan) ? sec[(size_t)t] : int2{0, 0};
+  };
+  // runs of x: device layout (l, s1, s2, r) or (l, s, r), l fastest
+  if (!h->runs) {
+    const bool two = h->kind == GB_HEFF_AC2;
+    const int64_t d1 = h->xdims[1], d2 = two ? h->xdims[3] : 1;
+    std::vector<int64_t> runs;
+    int64_t off = 0;
+    for (int64_t r = 0; r < Dr; ++r)
+      for (int64_t s2 = 0; s2 < d2; ++s2)
+        for (int64_t s1 = 0; s1 < d1; ++s1) {
+          const int64_t col = s1 + d1 * (s2 + d2 * r);
+          const int2 lr = sector((int64_t)qr[r] - qp1[s1] - (two ? qp2[s2] : 0));
+          if (lr.y <= lr.x) continue;
+          runs.push_back(off);
+          runs.push_back(col * Dl + lr.x);
+          runs.push_back(lr.y - lr.x);
+          off += lr.y - lr.x;
+        }
+    GB_REQUIRE(off > 0, "set_sectors: no allowed entry (charges inconsistent with the vector)");
+    h->nruns = (int64_t)runs.size() / 3;
+    h->ncompact = off;
+    h->runs = (int64_t*)dalloc(h, runs.size() * sizeof(int64_t));
+    GB_CHECK_CUDA(cudaMemcpyAsync(h->runs, runs.data(), runs.size() * sizeof(int64_t),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  if (!h->aa_glc || h->kJ.empty()) return;  // no fused chain: nothing more to restrict
   GB_REQUIRE(h->aa_Dl == Dl && h->aa_Dr == Dr, "set_sectors: bond dimensions");
   const int64_t chr = h->aa_chr;
   // fused physical charges of the mix rows
@@ -1240,14 +1343,6 @@ void heff_set_sectors(gb_heff* h, const int32_t* ql, const int32_t* qp1, const i
   GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
   GB_CHECK_CUDA(cudaFreeAsync(dev, ctx->stream));
   GB_REQUIRE(dq[chr] == 0, "set_sectors: the left environment does not conserve these charges");
-  // sector table of the (sorted) left charges, indexed by charge - ql[0]
-  const int64_t qmin = ql[0], qspan = (int64_t)ql[Dl - 1] - qmin + 1;
-  std::vector<int2> sec((size_t)qspan, int2{0, 0});
-  for (int64_t i = 0; i < Dl; ++i) {
-    int2& r = sec[(size_t)(ql[i] - qmin)];
-    if (r.y == 0) r.x = (int)i;
-    r.y = (int)i + 1;
-  }
   const int64_t nJ = (int64_t)h->kJ.size();
   std::vector<int2> tab((size_t)nJ * Dr);
   int64_t mx = 0;
@@ -1255,10 +1350,7 @@ void heff_set_sectors(gb_heff* h, const int32_t* ql, const int32_t* qp1, const i
     for (int64_t J = 0; J < nJ; ++J) {
       int2 r{0, 0};
       const int d = dq[h->Jc[J]];
-      if (d != INT_MIN) {
-        const int64_t t = (int64_t)qr[n] - d - qp[h->Jp[J]] - qmin;
-        if (t >= 0 && t < qspan) r = sec[(size_t)t];
-      }
+      if (d != INT_MIN) r = sector((int64_t)qr[n] - d - qp[h->Jp[J]]);
       tab[(size_t)n * nJ + J] = r;
       mx = std::max<int64_t>(mx, r.y - r.x);
     }

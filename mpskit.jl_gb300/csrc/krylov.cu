@@ -107,17 +107,50 @@ static void combine(gb_ctx* ctx, int dtype, int64_t n, int k, const void* V,
   multi_axpy(ctx, dtype, n, k, V, n, coef.data(), x);
 }
 
-int heff_eigsolve_raw(gb_ctx* ctx, gb_heff* h, int64_t n, int dtype, void* x, int krylovdim,
-                      int maxiter, double tol, bool eager, double* lambda, gb_krylov_info* info) {
+// The vector space of a solve: the dense vectors of the operator, or -- for a U(1)
+// operator whose sectors are known -- only their charge-allowed entries (the rest of the
+// charge-sorted embedding is exactly zero and stays so under H), which cuts the traffic of
+// the re-orthogonalisation and of every vector operation by the sector fraction.
+struct KrylovSpace {
+  gb_heff* h;
+  bool compact;
+  int64_t n;  // length of the solver's vectors
+  KrylovSpace(gb_heff* h_, int64_t dense_n) : h(h_) {
+    HeffCompact c;
+    compact = heff_compact(h, &c);
+    n = compact ? c.n : dense_n;
+  }
+  void apply(const void* x, void* y) const {
+    if (compact) heff_apply_compact(h, x, y);
+    else heff_apply_raw(h, x, y);
+  }
+  // solver vector <- dense x, and back (the back copy zero-fills the rest of x)
+  void load(gb_ctx* ctx, int dtype, const void* dense, void* v) const {
+    if (compact) heff_gather(h, dense, v);
+    else GB_CHECK_CUDA(cudaMemcpyAsync(v, dense, (size_t)n * elem_size(dtype),
+                                       cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  void store(gb_ctx* ctx, int dtype, const void* v, void* dense) const {
+    if (compact) heff_scatter(h, v, dense);
+    else GB_CHECK_CUDA(cudaMemcpyAsync(dense, v, (size_t)n * elem_size(dtype),
+                                       cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+};
+
+int heff_eigsolve_raw(gb_ctx* ctx, gb_heff* h, int64_t n_dense, int dtype, void* x,
+                      int krylovdim, int maxiter, double tol, bool eager, double* lambda,
+                      gb_krylov_info* info) {
   GB_REQUIRE(krylovdim >= 1 && krylovdim <= 64 && maxiter >= 1, "eigsolve: krylovdim/maxiter");
+  const KrylovSpace sp(h, n_dense);
+  const int64_t n = sp.n;
   const size_t es = elem_size(dtype);
   const int kd = krylovdim;
   char* V = (char*)scratch(ctx, SLOT_KRYLOV, (size_t)(kd + 1) * n * es);
   void* w = scratch(ctx, SLOT_KRYLOV_W, (size_t)n * es);
   auto vec = [&](int j) { return (void*)(V + (size_t)j * n * es); };
-  double nx = nrm2(ctx, dtype, n, x);
+  sp.load(ctx, dtype, x, vec(0));
+  double nx = nrm2(ctx, dtype, n, vec(0));
   GB_REQUIRE(nx > 0 && std::isfinite(nx), "eigsolve: initial vector has zero or non-finite norm");
-  GB_CHECK_CUDA(cudaMemcpyAsync(vec(0), x, n * es, cudaMemcpyDeviceToDevice, ctx->stream));
   scale(ctx, dtype, n, cplx{1.0 / nx, 0}, vec(0));
   const int howmany = 1;
   std::vector<double> H((size_t)(kd + 1) * (kd + 1), 0.0);  // row-major, stride kd+1
@@ -133,7 +166,7 @@ int heff_eigsolve_raw(gb_ctx* ctx, gb_heff* h, int64_t n, int dtype, void* x, in
   const bool split = heff_precision(h) != GB_PREC_FP64;
   double last_res = INFINITY;
   while (true) {
-    heff_apply_raw(h, vec(K), w);
+    sp.apply(vec(K), w);
     ++numops;
     std::vector<cplx> hc;
     orthogonalize(ctx, dtype, n, K + 1, V, w, hc);
@@ -190,9 +223,10 @@ int heff_eigsolve_raw(gb_ctx* ctx, gb_heff* h, int64_t n, int dtype, void* x, in
   }
   std::vector<cplx> coef(K);
   for (int i = 0; i < K; ++i) coef[i] = cplx{U[i * K + 0], 0.0};
-  combine(ctx, dtype, n, K, V, coef, x);
-  double nn = nrm2(ctx, dtype, n, x);
-  scale(ctx, dtype, n, cplx{1.0 / nn, 0}, x);
+  combine(ctx, dtype, n, K, V, coef, w);
+  double nn = nrm2(ctx, dtype, n, w);
+  scale(ctx, dtype, n, cplx{1.0 / nn, 0}, w);
+  sp.store(ctx, dtype, w, x);
   *lambda = D[0];
   if (info) {
     info->converged = converged;
@@ -204,11 +238,21 @@ int heff_eigsolve_raw(gb_ctx* ctx, gb_heff* h, int64_t n, int dtype, void* x, in
   return GB_OK;
 }
 
-int heff_exponentiate_raw(gb_ctx* ctx, gb_heff* h, int64_t n, int dtype, void* x, double t_re,
-                          double t_im, int krylovdim, int maxiter, double tol,
+int heff_exponentiate_raw(gb_ctx* ctx, gb_heff* h, int64_t n_dense, int dtype, void* x_dense,
+                          double t_re, double t_im, int krylovdim, int maxiter, double tol,
                           gb_krylov_info* info) {
   GB_REQUIRE(krylovdim >= 1 && krylovdim <= 64, "exponentiate: krylovdim");
   GB_REQUIRE(is_cplx(dtype) || t_im == 0.0, "exponentiate: complex time needs complex storage");
+  const KrylovSpace sp(h, n_dense);
+  const int64_t n = sp.n;
+  // the evolving state in the solver's space (compact: an operator-owned vector)
+  void* x = x_dense;
+  if (sp.compact) {
+    HeffCompact c;
+    heff_compact(h, &c);
+    x = c.xcomp;
+    sp.load(ctx, dtype, x_dense, x);
+  }
   const size_t es = elem_size(dtype);
   const int kd = krylovdim;
   char* V = (char*)scratch(ctx, SLOT_KRYLOV, (size_t)(kd + 1) * n * es);
@@ -228,7 +272,7 @@ int heff_exponentiate_raw(gb_ctx* ctx, gb_heff* h, int64_t n, int dtype, void* x
     int K = 0;
     bool happy = false;
     for (int j = 0; j < kd; ++j) {
-      heff_apply_raw(h, vec(j), w);
+      sp.apply(vec(j), w);
       ++numops;
       std::vector<cplx> hc;
       orthogonalize(ctx, dtype, n, j + 1, V, w, hc);
@@ -274,6 +318,7 @@ int heff_exponentiate_raw(gb_ctx* ctx, gb_heff* h, int64_t n, int dtype, void* x
     if (tau_left < 1e-15) tau_left = 0.0;
     tau = std::min(2 * tau, 1.0);
   }
+  if (sp.compact) sp.store(ctx, dtype, x, x_dense);
   if (info) {
     info->converged = tau_left == 0.0 ? 1 : 0;
     info->numops = numops;
