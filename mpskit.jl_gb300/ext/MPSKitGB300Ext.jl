@@ -118,6 +118,15 @@ function build(kind, ctx, GL, Ws, GR, xspace, T, backend::GB300Backend)
                 (Ptr{Cvoid}, Cint, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint,
                  Ptr{Ptr{Cvoid}}), ctx, kind, hGL, w1, w2, hGR, backend.precision, r))
     N = kind == GB_HEFF_AC2 ? 4 : kind == GB_HEFF_AC ? 3 : 2
+    if kind != GB_HEFF_C && sectortype(xspace) === U1Irrep
+        # the vectors' U(1) sectors: x[l s1; r s2] allowed where q_l + q_s1 + q_s2 = q_r
+        ql, qs1 = leg_charges(codomain(xspace)[1]), leg_charges(codomain(xspace)[2])
+        qr = leg_charges(domain(xspace)[1])
+        qs2 = kind == GB_HEFF_AC2 ? leg_charges(dual(domain(xspace)[2])) : C_NULL
+        check(ccall((:gb_heff_set_sectors, libmpsgb), Cint,
+                    (Ptr{Cvoid}, Ptr{Int32}, Ptr{Int32}, Ptr{Int32}, Ptr{Int32}),
+                    r[], ql, qs1, qs2, qr))
+    end
     op = GB300Derivative{T, N}(r[], ctx, kind, xspace, [hGL; hGR; hW])
     finalizer(op) do o
         ccall((:gb_heff_free, libmpsgb), Cint, (Ptr{Cvoid},), o.h)
