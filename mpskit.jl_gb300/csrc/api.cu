@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <condition_variable>
 #include <cstdio>
 #include <map>
 #include <mutex>
@@ -733,6 +734,63 @@ void gauge_conj_transpose(gb_ctx* ctx, int dtype, int64_t m, int64_t n, const vo
 }
 void* gauge_solver(gb_ctx* ctx) { return (void*)solver(ctx); }
 
+// One host thread per lane, started with the first parallel call and kept until the context
+// is destroyed (thread start-up stays off the per-call path).  A call hands every worker the
+// same job and waits until all of them have finished it.
+struct LanePool {
+  std::vector<std::thread> threads;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  uint64_t gen = 0;
+  int busy = 0;
+  bool stop = false;
+  std::function<void(int)> job;
+
+  void start(int count, int device) {
+    while ((int)threads.size() < count) {
+      const int k = (int)threads.size();
+      threads.emplace_back([this, k, device] {
+        cudaSetDevice(device);
+        uint64_t seen = 0;
+        for (;;) {
+          std::function<void(int)> f;
+          {
+            std::unique_lock<std::mutex> lk(mu);
+            cv_work.wait(lk, [&] { return stop || gen != seen; });
+            if (stop) return;
+            seen = gen;
+            f = job;
+          }
+          f(k);
+          {
+            std::lock_guard<std::mutex> lk(mu);
+            if (--busy == 0) cv_done.notify_all();
+          }
+        }
+      });
+    }
+  }
+  void run(const std::function<void(int)>& f) {
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      job = f;
+      busy = (int)threads.size();
+      ++gen;
+    }
+    cv_work.notify_all();
+    std::unique_lock<std::mutex> lk(mu);
+    cv_done.wait(lk, [&] { return busy == 0; });
+  }
+  ~LanePool() {
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      stop = true;
+    }
+    cv_work.notify_all();
+    for (auto& t : threads) t.join();
+  }
+};
+
 void run_on_lanes(gb_ctx* ctx, int64_t n, const std::function<void(gb_ctx*, int64_t)>& fn) {
   const int K = (int)std::min<int64_t>(n, 8);
   if (K <= 1) {
@@ -754,31 +812,29 @@ void run_on_lanes(gb_ctx* ctx, int64_t n, const std::function<void(gb_ctx*, int6
     l->gemm_bn = ctx->gemm_bn;
     before[k] = l->launches;
   }
+  if (!ctx->lane_pool) ctx->lane_pool = new LanePool();
+  ctx->lane_pool->start(K, ctx->device);
   GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
   std::atomic<int64_t> next{0};
   std::exception_ptr err;
   std::mutex mu;
-  std::vector<std::thread> th;
-  th.reserve(K);
-  for (int k = 0; k < K; ++k)
-    th.emplace_back([&, k] {
-      gb_ctx* l = ctx->lanes[k];
-      try {
-        GB_CHECK_CUDA(cudaSetDevice(l->device));
-        for (int64_t i; (i = next++) < n;) {
-          {
-            std::lock_guard<std::mutex> g(mu);
-            if (err) break;
-          }
-          fn(l, i);
+  ctx->lane_pool->run([&](int k) {
+    if (k >= K) return;
+    gb_ctx* l = ctx->lanes[k];
+    try {
+      for (int64_t i; (i = next++) < n;) {
+        {
+          std::lock_guard<std::mutex> g(mu);
+          if (err) break;
         }
-        GB_CHECK_CUDA(cudaStreamSynchronize(l->stream));
-      } catch (...) {
-        std::lock_guard<std::mutex> g(mu);
-        if (!err) err = std::current_exception();
+        fn(l, i);
       }
-    });
-  for (auto& t : th) t.join();
+      GB_CHECK_CUDA(cudaStreamSynchronize(l->stream));
+    } catch (...) {
+      std::lock_guard<std::mutex> g(mu);
+      if (!err) err = std::current_exception();
+    }
+  });
   GB_TRACE(ctx);  // marks the end of the lanes' work on the (idle) main stream
   for (int k = 0; k < K; ++k) ctx->launches += ctx->lanes[k]->launches - before[k];
   if (err) std::rethrow_exception(err);
@@ -829,6 +885,8 @@ int gb_ctx_destroy(gb_ctx* ctx) {
   API_BEGIN
   if (!ctx) return GB_OK;
   DevGuard g(ctx->device);
+  delete ctx->lane_pool;  // joins the lane threads (idle between calls)
+  ctx->lane_pool = nullptr;
   for (gb_ctx* l : ctx->lanes) gb_ctx_destroy(l);
   ctx->lanes.clear();
   cudaStreamSynchronize(ctx->stream);

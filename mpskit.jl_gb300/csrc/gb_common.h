@@ -62,6 +62,8 @@ enum ScratchSlot {
   SLOT_COUNT
 };
 
+struct LanePool;
+
 }  // namespace gb
 
 struct gb_ctx {
@@ -88,6 +90,7 @@ struct gb_ctx {
   // auxiliary contexts (own stream, scratch and solver handle) for many small independent
   // work items, e.g. the charge sectors of a U(1) factorisation (see run_on_lanes)
   std::vector<gb_ctx*> lanes;
+  gb::LanePool* lane_pool = nullptr;  // persistent host threads driving the lanes
   // tracing of the tensor-core GEMM launches
   bool profiling = false;
   std::vector<cudaEvent_t> prof_events;  // pairs (start, stop) per launch
