@@ -1291,8 +1291,9 @@ void heff_set_sectors(gb_heff* h, const int32_t* ql, const int32_t* qp1, const i
     const int64_t t = q - qmin;
     return (t >= 0 && t < qspan) ? sec[(size_t)t] : int2{0, 0};
   };
-  // runs of x: device layout (l, s1, s2, r) or (l, s, r), l fastest
-  if (!h->runs) {
+  // runs of x: device layout (l, s1, s2, r) or (l, s, r), l fastest (a later call with
+  // other charges replaces them; the staging vector is then cleared again)
+  {
     const bool two = h->kind == GB_HEFF_AC2;
     const int64_t d1 = h->xdims[1], d2 = two ? h->xdims[3] : 1;
     std::vector<int64_t> runs;
@@ -1314,6 +1315,11 @@ void heff_set_sectors(gb_heff* h, const int32_t* ql, const int32_t* qp1, const i
     h->runs = (int64_t*)dalloc(h, runs.size() * sizeof(int64_t));
     GB_CHECK_CUDA(cudaMemcpyAsync(h->runs, runs.data(), runs.size() * sizeof(int64_t),
                                   cudaMemcpyHostToDevice, ctx->stream));
+    if (h->xfull) {
+      const size_t es = elem_size(h->dtype);
+      GB_CHECK_CUDA(cudaMemsetAsync(h->xfull, 0, (size_t)h->xnumel * es, ctx->stream));
+      h->xcomp = dalloc(h, (size_t)h->ncompact * es);  // follows the new compact length
+    }
     GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
   }
   if (!h->aa_glc || h->kJ.empty()) return;  // no fused chain: nothing more to restrict
