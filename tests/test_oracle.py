@@ -238,3 +238,59 @@ def test_oracle_idmrg_tfim_closed_form():
     assert eps <= 1e-10
     assert abs(V.energy_density(psi, H[0], GL, GR) - exact) < 1e-12
     assert abs(hist[-1][1] - exact) < 1e-10
+
+
+def test_oracle_cell_of_one_site_equals_one_site_vumps():
+    """The unit-cell restatement (oracle/cell.py) with L = 1 takes the one-site VUMPS path
+    step for step: same iterations, energies and tensors."""
+    from oracle import cell as Ce
+    from oracle import vumps as V
+    H = M.infinite_mpo_hamiltonian(1, 2, M.tfim_terms(1, g=0.5, periodic=True))
+    rng = np.random.default_rng(1)
+    A = rng.standard_normal((12, 2, 12)) + 1j * rng.standard_normal((12, 2, 12))
+    p1, _, _, e1, h1 = V.vumps(V.infinite_mps(A), H, tol=1e-10, maxiter=100)
+    pc, _, _, ec, hc = Ce.vumps(Ce.infinite_mps([A]), H, tol=1e-10, maxiter=100)
+    assert len(h1) == len(hc)
+    assert abs(h1[-1][1] - hc[-1][1]) < 1e-13
+    assert np.allclose(p1.AL, pc.AL[0], atol=1e-12)
+
+
+def test_oracle_two_site_cell_vumps():
+    """VUMPS on a two-site cell: the TFIM reaches the free-fermion energy density, and the
+    Neel-ordered XXZ chain (Delta = 3, no sublattice rotation) approaches the Bethe ansatz
+    from above."""
+    from oracle import cell as Ce
+    rng = np.random.default_rng(3)
+    H = M.infinite_mpo_hamiltonian(2, 2, M.tfim_terms(2, g=0.5, periodic=True))
+    As = [rng.standard_normal((10, 2, 10)) + 1j * rng.standard_normal((10, 2, 10))
+          for _ in range(2)]
+    _, _, _, eps, hist = Ce.vumps(Ce.infinite_mps(As), H, tol=1e-10, maxiter=100)
+    assert eps <= 1e-10
+    assert abs(hist[-1][1] - M.tfim_infinite_energy_density(0.5)) < 1e-12
+    Hx = M.infinite_mpo_hamiltonian(2, 2, M.xxz_terms(2, 1.0, 3.0, periodic=True))
+    As = [rng.standard_normal((12, 2, 12)) + 1j * rng.standard_normal((12, 2, 12))
+          for _ in range(2)]
+    _, _, _, _, hist = Ce.vumps(Ce.infinite_mps(As), Hx, tol=1e-10, maxiter=30)
+    de = hist[-1][1] - M.xxz_infinite_energy_density(3.0)
+    assert 0.0 <= de < 2e-8
+
+
+def test_oracle_idmrg2_tfim():
+    """IDMRG2 (idmrg.jl:230-338) on a two-site cell grows the bond from D = 4 under
+    truncrank(16) and reaches the TFIM energy density; its energy change per cycle is the
+    energy of one unit cell."""
+    from oracle import cell as Ce
+    rng = np.random.default_rng(3)
+    H = M.infinite_mpo_hamiltonian(2, 2, M.tfim_terms(2, g=0.5, periodic=True))
+    As = [rng.standard_normal((4, 2, 4)) + 1j * rng.standard_normal((4, 2, 4))
+          for _ in range(2)]
+    psi, GL, GR, eps, hist = Ce.idmrg2(Ce.infinite_mps(As), H, maxdim=16, atol=1e-12,
+                                       tol=1e-10, maxiter=100)
+    exact = M.tfim_infinite_energy_density(0.5)
+    assert eps <= 1e-10
+    assert psi.AL[0].shape[0] > 4
+    assert abs(Ce.energy(psi, H, GL, GR) / 2 - exact) < 1e-10
+    assert abs(hist[-1][1] - 2 * exact) < 1e-8
+    with pytest.raises(ValueError):
+        Ce.idmrg2(Ce.infinite_mps(As[:1]), M.infinite_mpo_hamiltonian(
+            1, 2, M.tfim_terms(1, g=0.5, periodic=True)), maxdim=8)
