@@ -18,6 +18,7 @@ from .infinite import (IDMRG, VUMPS, InfiniteEnvironments, InfiniteMPS,
                        find_groundstate_idmrg, find_groundstate_vumps, timestep_infinite)
 from . import u1
 from . import batched
+from . import cell
 
 __all__ = [
     "Context", "DeviceTensor", "context", "AC2_hamiltonian", "AC_hamiltonian", "C_hamiltonian",
@@ -28,4 +29,5 @@ __all__ = [
     "svd_trunc", "DMRG", "DMRG2", "AdaptiveKrylov", "expectation_value", "find_groundstate",
     "TDVP", "timestep", "VUMPS", "IDMRG", "InfiniteEnvironments", "InfiniteMPS",
     "find_groundstate_vumps", "find_groundstate_idmrg", "timestep_infinite", "u1", "batched",
+    "cell",
 ]

@@ -8,9 +8,10 @@
 The environments are solved level by level (channel block by channel block of the MPO,
 which is upper triangular): the inhomogeneous term is a sum of transfers of the lower
 levels, and each level solves x - x T_ii = b by GMRES (regularised on identity levels).
-The GMRES loop runs on the host over device vectors; every transfer, dot and update is a
-libmpsgb call.  The Arnoldi acceleration of the gauge iterations (ortho.jl, after 10
-iterations) is not used: the QR/LQ iterations converge to the same fixed point.
+Each level is one gb_env_linsolve call (restarted GMRES on the device).  The uniform gauge
+iterations use the reference's acceleration (gauge_eigsolve_step!, ortho.jl:258-263,
+322-324): from iteration 10 on, the boundary C is replaced by the dominant eigenvector of the
+mixed transfer map before the QR/LQ step.
 """
 import ctypes
 
