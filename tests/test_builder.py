@@ -47,3 +47,15 @@ def test_mpo_reproduces_ed_spectrum():
     Hd = T.transpose(perm).reshape(2 ** L, 2 ** L)
     e = np.linalg.eigvalsh(Hd)[0]
     assert abs(e - M.ed_ground_energy(L, 2, M.xxz_terms(L, 1.0, 0.7, 0.2))[0]) < 1e-12
+
+
+@pytest.mark.parametrize("cell", [1, 2])
+def test_infinite_rotated_xxz(cell):
+    """The sublattice-rotated XXZ chain (one-site invariant form of the Neel phase) builds the
+    same MPO as the oracle; a field is refused (it would become staggered)."""
+    a = mpsgb.xxz(cell, 1.0, 1.5, infinite=True, rotated=True)
+    b = M.infinite_mpo_hamiltonian(cell, 2, M.xxz_terms(cell, 1.0, 1.5, periodic=True,
+                                                        rotated=True))
+    assert all(np.allclose(x, y, atol=1e-15) for x, y in zip(a.W, b.W))
+    with pytest.raises(ValueError):
+        mpsgb.xxz(cell, 1.0, 1.5, hz=0.1, infinite=True, rotated=True)
