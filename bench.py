@@ -579,6 +579,9 @@ def run_e2e(args, ctx, psi, H, envs, alg, pos, state, pg, flops_per_matvec=None)
     x_host = pin(ac2.dims)
     L.check(L.lib().gb_tensor_download(ac2.handle, host_ptr(x_host), ac2.size * 8))
     Heff = mpsgb.AC2_hamiltonian(pos, psi, H, envs, alg.backend)
+    # U(1): the vectors' sectors, as a C-ABI caller passes them after gb_heff_build
+    # (gb_heff_set_sectors; a no-op for dense vectors)
+    Heff.set_sectors(ac2)
     flops = flops_per_matvec or Heff.flops
     outs = {}
 
@@ -617,7 +620,8 @@ def run_e2e(args, ctx, psi, H, envs, alg, pos, state, pg, flops_per_matvec=None)
     fl = allsum(pg, flops * nops)
     return {"value": fl / t / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": ac2.size * 8,
             "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * t / args.steps,
-            "path": "gb_tensor_upload -> gb_heff_eigsolve -> gb_svd_trunc -> gb_tensor_download"}
+            "path": "gb_heff_set_sectors once; gb_tensor_upload -> gb_heff_eigsolve -> "
+                    "gb_svd_trunc -> gb_tensor_download"}
 
 
 def run_vumps_sweep(args):
