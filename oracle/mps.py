@@ -308,10 +308,71 @@ class DMRG2:
 
 
 class DMRG:
-    def __init__(self, tol=1e-10, maxiter=200, alg_eigsolve=None):
+    def __init__(self, tol=1e-10, maxiter=200, alg_eigsolve=None, alg_gauge=None):
         self.tol = tol
         self.maxiter = maxiter
         self.alg_eigsolve = alg_eigsolve or AdaptiveKrylov()
+        # None: the positive QR/LQ gauge; a DMRG3S: the perturbed, truncated gauge
+        self.alg_gauge = alg_gauge
+
+
+class DMRG3S:
+    """DMRG3S(noise, ExponentialDecay(decay_rate)) with the truncated SVD DMRG fills in
+    (post_expand/dmrg3s.jl:83-153; trunc = truncrank(maxdim) & trunctol(atol)): the noise
+    at outer iteration `it` is noise * decay_rate^it (ExponentialDecay, dmrg3s.jl:36-56)."""
+
+    def __init__(self, noise, decay_rate, maxdim, atol=0.0):
+        self.noise, self.decay_rate = noise, decay_rate
+        self.maxdim, self.atol = maxdim, atol
+
+    def noise_at(self, it):
+        return self.noise * self.decay_rate ** it
+
+
+def dmrg3s_gauge(pos, right, psi, H, envs, AC, noise, maxdim, atol):
+    """gauge!(psi, pos, dir, H, envs, AC, ::DMRG3S) (dmrg3s.jl:155-221).  Right: the
+    perturbation noise * GL[pos] W[pos] AC with the right bond and the MPO leg fused
+    (r fastest) is appended to AC along its right bond, the truncated SVD gives AL[pos] and
+    C = S Vh, and AR[pos+1] gets zero rows for the new directions.  Left: the mirror image,
+    with the perturbation GR[pos]-side and zero columns appended to AL[pos-1].  Returns the
+    truncation error."""
+    W = H[pos]
+    Dl, d, Dr = AC.shape
+    if right:
+        wr = W.shape[3]
+        comb = np.zeros((Dr, wr, Dr * wr), dtype=AC.dtype)   # GR-like: [in, w, out]
+        for w in range(wr):
+            comb[np.arange(Dr), w, w * Dr + np.arange(Dr)] = 1
+        pert = noise * dv.mpo_ac_apply(envs.leftenv(pos, psi), W, comb, AC)
+        ACe = np.concatenate([AC, pert], axis=2)
+        U, S, Vh, eps = svd_trunc(ACe.reshape(Dl * d, -1, order="F"), maxdim, atol)
+        k = S.size
+        C = S[:, None] * Vh
+        C = C / np.linalg.norm(C)
+        B = psi.AR[pos + 1]
+        psi.AL[pos] = np.ascontiguousarray(U.reshape(Dl, d, k, order="F"))
+        psi.AR[pos + 1] = np.concatenate(
+            [B, np.zeros((Dr * wr,) + B.shape[1:], dtype=B.dtype)], axis=0)
+        psi.C[pos + 1] = C
+        psi.center = pos + 1
+    else:
+        wl = W.shape[0]
+        comb = np.zeros((Dl * wl, wl, Dl), dtype=AC.dtype)   # GL-like: [out, w, in]
+        for w in range(wl):
+            comb[w * Dl + np.arange(Dl), w, np.arange(Dl)] = 1
+        pert = noise * dv.mpo_ac_apply(comb, W, envs.rightenv(pos, psi), AC)
+        ACe = np.concatenate([AC, pert], axis=0)
+        U, S, Vh, eps = svd_trunc(ACe.reshape(ACe.shape[0], d * Dr, order="F"), maxdim, atol)
+        k = S.size
+        C = U * S[None, :]
+        C = C / np.linalg.norm(C)
+        B = psi.AL[pos - 1]
+        psi.AR[pos] = np.ascontiguousarray(Vh.reshape(k, d, Dr, order="F"))
+        psi.AL[pos - 1] = np.concatenate(
+            [B, np.zeros(B.shape[:2] + (Dl * wl,), dtype=B.dtype)], axis=2)
+        psi.C[pos] = C
+        psi.center = pos
+    return eps
 
 
 def _as_mat(x, nl):
@@ -428,6 +489,14 @@ def dmrg1_local_update(pos, right, psi, H, alg, envs, eps_global, eps_trunc, dec
     val, new, info = lanczos_eigsolve(Heff, ac, krylovdim=kd, maxiter=mi, tol=tol,
                                       eager=alg.alg_eigsolve.eager)
     stats["matvecs"] += info.numops
+    g = getattr(alg, "alg_gauge", None)
+    if g is not None:
+        noise = g.noise_at(stats.get("iter", 0))
+        if noise != 0.0:
+            eps_tr = dmrg3s_gauge(pos, right, psi, H, envs, new, noise, g.maxdim, g.atol)
+            decay = min(max((info.normres / eps_local) ** (1 / max(1, info.numops)), 1e-3),
+                        0.999) if eps_local > 0 else 0.999
+            return eps_local, eps_tr, decay, val
     if right:
         if psi.qb is not None:
             from .u1 import fuse, left_orth_u1
@@ -469,6 +538,7 @@ def find_groundstate_dmrg(psi, H, alg, envs=None, maxsweeps=None):
     hist = []
     niter = alg.maxiter if maxsweeps is None else maxsweeps
     for it in range(niter):
+        stats["iter"] = it
         for pos in range(0, L - 1):
             eps_locals[pos], _, decays[pos], val = dmrg1_local_update(
                 pos, True, psi, H, alg, envs, eps_global, 0.0, decays[pos], stats)

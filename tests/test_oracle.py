@@ -294,3 +294,20 @@ def test_oracle_idmrg2_tfim():
     with pytest.raises(ValueError):
         Ce.idmrg2(Ce.infinite_mps(As[:1]), M.infinite_mpo_hamiltonian(
             1, 2, M.tfim_terms(1, g=0.5, periodic=True)), maxdim=8)
+
+
+def test_oracle_dmrg3s_escapes_a_small_bond():
+    """Single-site DMRG cannot grow the bond of a D = 2 start and stalls far above the ground
+    state; with the DMRG3S gauge (post_expand/dmrg3s.jl:155-221, noise 0.1, decay 0.8,
+    truncrank(16)) the perturbation opens new directions and the energy reaches exact
+    diagonalisation -- the mechanism of the reference's 'DMRG3S escapes local minimum' test
+    (test/algorithms/groundstate.jl:151-175)."""
+    L_ = 10
+    H = M.finite_mpo_hamiltonian(L_, 2, M.heisenberg_terms(L_))
+    e_ed = M.ed_ground_energy(L_, 2, M.heisenberg_terms(L_))[0]
+    psi0 = P.finite_mps_from_tensors(P.random_initial_tensors(L_, 2, 2, 5))
+    _, _, _, h_plain = P.find_groundstate_dmrg(psi0, H, P.DMRG(tol=1e-10, maxiter=12))
+    alg = P.DMRG(tol=1e-10, maxiter=12, alg_gauge=P.DMRG3S(0.1, 0.8, 16, 1e-12))
+    _, _, _, h_3s = P.find_groundstate_dmrg(psi0, H, alg)
+    assert h_plain[-1][1] - e_ed > 0.1
+    assert 0.0 <= h_3s[-1][1] - e_ed < 1e-7
