@@ -308,12 +308,86 @@ class DMRG2:
 
 
 class DMRG:
-    def __init__(self, tol=1e-10, maxiter=200, alg_eigsolve=None, alg_gauge=None):
+    def __init__(self, tol=1e-10, maxiter=200, alg_eigsolve=None, alg_gauge=None,
+                 alg_expand=None):
         self.tol = tol
         self.maxiter = maxiter
         self.alg_eigsolve = alg_eigsolve or AdaptiveKrylov()
         # None: the positive QR/LQ gauge; a DMRG3S: the perturbed, truncated gauge
         self.alg_gauge = alg_gauge
+        # None, or an OptimalExpand run ahead of every local update (dmrg.jl:128-134)
+        self.alg_expand = alg_expand
+
+
+class OptimalExpand:
+    """OptimalExpand(; trunc = truncrank(add)) (changebonds/optimalexpand.jl:36-47): at
+    most `add` directions are added to a bond per expansion."""
+
+    def __init__(self, add):
+        self.add = add
+
+
+def _left_null(M):
+    """Orthonormal basis of the complement of the column space of M (m x n, m >= n)."""
+    Q, _ = np.linalg.qr(M, mode="complete")
+    return Q[:, M.shape[1]:]
+
+
+def _ac2_matrix(ac2):
+    """AC2[l s1; r s2] as the matrix (l s1) x (s2 r)."""
+    Dl, d1, Dr, d2 = ac2.shape
+    return np.transpose(ac2, (0, 1, 3, 2)).reshape(Dl * d1, d2 * Dr, order="F")
+
+
+def optimal_expand(pos, right, psi, H, envs, alg):
+    """changebond!(site, dir, psi, H, ::OptimalExpand, envs) (optimalexpand.jl:122-187):
+    the two-site update H_AC2 (AC2) projected onto the complements of the two sites
+    (left_null / right_null), its `add` dominant directions appended to the bond -- with
+    zero weight, so the state is unchanged -- and the sites regauged."""
+    eps34 = np.finfo(np.float64).eps ** 0.75
+    if right:
+        left, rt = psi.ac(pos), psi.AR[pos + 1]
+        Dl, d, Dr = left.shape
+        Dn = rt.shape[2]
+        lmat = left.reshape(Dl * d, Dr, order="F")
+        RT = rt.reshape(Dr, d * Dn, order="F")
+        NL = _left_null(lmat)
+        NR = _left_null(RT.conj().T).conj().T
+        ac2 = np.einsum("asm,mtb->asbt", left, rt)
+        g2 = NL.conj().T @ _ac2_matrix(AC2_hamiltonian(pos, psi, H, envs)(ac2)) @ NR.conj().T
+        nrm = np.linalg.norm(g2)
+        if nrm <= eps34 or g2.size == 0:
+            return
+        _, _, Vh, _ = svd_trunc(g2 / nrm, alg.add, 0.0)
+        k = Vh.shape[0]
+        nal, nc = qr_pos(np.concatenate([lmat, np.zeros((Dl * d, k), dtype=lmat.dtype)], axis=1))
+        nar = np.concatenate([RT, Vh @ NR], axis=0)
+        psi.AL[pos] = nal.reshape(Dl, d, nal.shape[1], order="F")
+        psi.C[pos + 1] = nc / np.linalg.norm(nc)
+        psi.AR[pos + 1] = nar.reshape(Dr + k, d, Dn, order="F")
+        psi.center = pos + 1
+    else:
+        lf, rgt = psi.AL[pos - 1], psi.ac(pos)
+        Dp, d, Dl = lf.shape
+        Dr = rgt.shape[2]
+        lmat = lf.reshape(Dp * d, Dl, order="F")
+        RT = rgt.reshape(Dl, d * Dr, order="F")
+        NL = _left_null(lmat)
+        NR = _left_null(RT.conj().T).conj().T
+        ac2 = np.einsum("asm,mtb->asbt", lf, rgt)
+        g2 = (NL.conj().T @ _ac2_matrix(AC2_hamiltonian(pos - 1, psi, H, envs)(ac2))
+              @ NR.conj().T)
+        nrm = np.linalg.norm(g2)
+        if nrm <= eps34 or g2.size == 0:
+            return
+        U, _, _, _ = svd_trunc(g2 / nrm, alg.add, 0.0)
+        k = U.shape[1]
+        nc, Qr = lq_pos(np.concatenate([RT, np.zeros((k, d * Dr), dtype=RT.dtype)], axis=0))
+        psi.AR[pos] = Qr.reshape(Qr.shape[0], d, Dr, order="F")
+        psi.C[pos] = nc / np.linalg.norm(nc)
+        psi.AL[pos - 1] = np.concatenate([lmat, NL @ U], axis=1).reshape(Dp, d, Dl + k,
+                                                                          order="F")
+        psi.center = pos
 
 
 class DMRG3S:
@@ -483,8 +557,13 @@ def dmrg1_local_update(pos, right, psi, H, alg, envs, eps_global, eps_trunc, dec
     stats["matvecs"] += 1
     y = y / np.linalg.norm(y)
     # the galerkin error uses the AL of the current centre site
-    Dl, d, Dr = ac.shape
     eps_local = float(np.linalg.norm(project_complement(y, psi.al(pos))))
+    if getattr(alg, "alg_expand", None) is not None:
+        # 1. expand (dmrg.jl:128-134), then the update from the expanded tensor
+        optimal_expand(pos, right, psi, H, envs, alg.alg_expand)
+        ac = psi.ac(pos)
+        Heff = AC_hamiltonian(pos, psi, H, envs)
+    Dl, d, Dr = ac.shape
     kd, mi, tol = alg.alg_eigsolve.adapt(decay_rate, eps_local, eps_global, eps_trunc)
     val, new, info = lanczos_eigsolve(Heff, ac, krylovdim=kd, maxiter=mi, tol=tol,
                                       eager=alg.alg_eigsolve.eager)

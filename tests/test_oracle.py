@@ -311,3 +311,41 @@ def test_oracle_dmrg3s_escapes_a_small_bond():
     _, _, _, h_3s = P.find_groundstate_dmrg(psi0, H, alg)
     assert h_plain[-1][1] - e_ed > 0.1
     assert 0.0 <= h_3s[-1][1] - e_ed < 1e-7
+
+
+def _mps_vector(psi):
+    """The state vector of a small finite MPS with its centre bond at psi.center."""
+    c = psi.center
+    ts = [psi.AL[i] for i in range(c)] + [psi.AC(c)] + [psi.AR[i] for i in range(c + 1, len(psi))]
+    v = ts[0]
+    for t in ts[1:]:
+        v = np.tensordot(v, t, axes=([v.ndim - 1], [0]))
+    return v.reshape(-1)
+
+
+def test_oracle_optimal_expand_preserves_the_state_and_reaches_ed():
+    """OptimalExpand (changebonds/optimalexpand.jl:122-187) adds directions with zero
+    weight: one expansion leaves the state vector unchanged while the bond grows; ahead of
+    every single-site update (dmrg.jl:128-134) it lets DMRG from a D = 2 start reach the
+    exact-diagonalisation energy."""
+    L_ = 8
+    H = M.finite_mpo_hamiltonian(L_, 2, M.heisenberg_terms(L_))
+    psi = P.finite_mps_from_tensors(P.random_initial_tensors(L_, 2, 2, 6))
+    assert psi.center == 0
+    ac = psi.AC(0)
+    Q, R = P.qr_pos(ac.reshape(-1, ac.shape[2], order="F"))
+    psi.AL[0], psi.C[1], psi.center = Q.reshape(ac.shape, order="F"), R, 1
+    v0 = _mps_vector(psi)
+    D0 = psi.AR[2].shape[0]
+    P.optimal_expand(1, True, psi, H, P.FiniteEnvironments(psi, H), P.OptimalExpand(3))
+    assert psi.center == 2 and psi.AR[2].shape[0] > D0
+    v1 = _mps_vector(psi)
+    assert np.linalg.norm(v1 / np.linalg.norm(v1) - v0 / np.linalg.norm(v0)) < 1e-12
+    L_ = 10
+    H = M.finite_mpo_hamiltonian(L_, 2, M.heisenberg_terms(L_))
+    e_ed = M.ed_ground_energy(L_, 2, M.heisenberg_terms(L_))[0]
+    psi0 = P.finite_mps_from_tensors(P.random_initial_tensors(L_, 2, 2, 5))
+    alg = P.DMRG(tol=1e-10, maxiter=12, alg_expand=P.OptimalExpand(4))
+    _, _, eps, hist = P.find_groundstate_dmrg(psi0, H, alg)
+    assert eps <= 1e-10
+    assert abs(hist[-1][1] - e_ed) < 1e-10
