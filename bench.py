@@ -63,14 +63,33 @@ def parse():
     ap.add_argument("--svd", default="gram", choices=["gesvd", "gesvdp", "gram"])
     ap.add_argument("--symmetry", default="u1", choices=["u1", "none"],
                     help="u1: U(1) (total Sz = 0) block-sparse state and MPO; none: dense")
-    ap.add_argument("--workload", default="dmrg2", choices=["dmrg2", "vumps-sweep", "vumps-xxz"],
-                    help="dmrg2: the headline DMRG2 step; vumps-sweep: 64 independent TFIM "
+    ap.add_argument("--workload", default="dmrg2",
+                    choices=["dmrg2", "dmrg2-sweep", "matvec", "vumps-sweep", "vumps-xxz"],
+                    help="dmrg2: the headline DMRG2 step; dmrg2-sweep: full DMRG2 sweeps of "
+                         "the same state (checkpointed environments); matvec: repeated H_eff "
+                         "applications at the central bond (a small case for profiling); "
+                         "vumps-sweep: 64 "
+                         "independent TFIM "
                          "chains (VUMPS, g in [0.1, 2], D in {64..256}) solved concurrently; "
                          "vumps-xxz: one-site VUMPS of the XXZ chain (Jz = 1.5, sublattice-"
                          "rotated) at D = 256, "
                          "plain FP64 against the split precision")
+    ap.add_argument("--schedule", default="grouped",
+                    choices=["grouped", "persistent", "persistent_dense", "tile"],
+                    help="split GEMM schedule: grouped (one launch per contraction over its "
+                         "U(1) charge blocks; the default) or the dense-embedding schedules")
     ap.add_argument("--tile-n", type=int, default=0, choices=[0, 128, 256],
                     help="output tile width of the split GEMM (0: chosen per GEMM shape)")
+    ap.add_argument("--window", type=int, default=8,
+                    help="bonds of the measured sweep window (split and plain FP64 from the "
+                         "same state); 0 skips it")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the split-vs-FP64 eigensolve comparison at the bench bond")
+    ap.add_argument("--sweeps", type=int, default=1, help="sweeps of --workload dmrg2-sweep")
+    ap.add_argument("--checkpoint", type=int, default=12,
+                    help="dmrg2-sweep: environments kept resident every this many sites")
+    ap.add_argument("--ref-budget", type=float, default=90.0,
+                    help="seconds of timed CPU steps in --impl reference (bounded sample)")
     ap.add_argument("--workers", type=int, default=16)
     ap.add_argument("--vumps-iters", type=int, default=6)
     return ap.parse_args()
@@ -185,117 +204,95 @@ def allsum(pg, v):
 
 # ---------------------------------------------------------------- oracle timing (CPU)
 
-def oracle_sample(GL, W1, W2, GR, dtype, reps, min_total_s=0.0):
-    """Time the oracle's JordanAC2 matvec (the reference algorithm restated in numpy) on
-    the host cores, `reps` times and at least until `min_total_s` seconds of work.
-    Returns (seconds per matvec, threads, matvecs timed)."""
-    from oracle import derivatives as odv
+def oracle_threads():
     try:
         from threadpoolctl import threadpool_info
-        threads = max([i.get("num_threads", 1) for i in threadpool_info()] + [1])
+        return max([i.get("num_threads", 1) for i in threadpool_info()] + [1])
     except Exception:
-        threads = os.cpu_count() or 1
-    op = odv.JordanAC2(GL, W1, W2, GR)
-    rng = np.random.default_rng(0)
-    x = rng.standard_normal((GL.shape[0], W1.shape[1], GR.shape[0], W2.shape[1])).astype(dtype)
-    times = []
-    while len(times) < reps or sum(times) < min_total_s:
-        t0 = time.perf_counter()
-        op(x)
-        times.append(time.perf_counter() - t0)
-    return sum(times) / len(times), threads, len(times)
-
-
-def cpu_sample_D(W1, W2, D_target, budget_s=20.0):
-    """Largest D <= D_target (halving) whose oracle matvec is predicted to fit in the
-    budget, predicted from a D=256 probe with the D^3 cost law."""
-    rng = np.random.default_rng(1)
-    D0 = min(256, D_target)
-    GL = rng.standard_normal((D0, W1.shape[0], D0))
-    GR = rng.standard_normal((D0, W2.shape[3], D0))
-    t0, _, _ = oracle_sample(GL, W1, W2, GR, np.float64, 1)
-    D = D_target
-    while D > D0 and t0 * (D / D0) ** 3 > budget_s:
-        D //= 2
-    return D
+        return os.cpu_count() or 1
 
 
 def run_reference(args):
-    """--impl reference: the oracle port on the host cores, one matvec per step, at the
-    workload's central-bond shapes with seeded synthetic environments."""
+    """--impl reference: the same workload on the host cores with the oracle's block-sparse
+    U(1) restatement (oracle/blocksparse.py: TensorKit-style blockwise contractions), from
+    the same seeded state: blockwise canonical form, environments to the central bond, then
+    per step one DMRG2 local update at that bond (Galerkin matvec, adaptive Lanczos on the
+    charge-allowed entries, blockwise truncated SVD) plus the environment step the next bond
+    needs.  H_eff flops are counted as in the GPU arm: 2 x the multiply-adds of the charge
+    blocks of every contraction.  The CPU needs no warm-up beyond one step; timed steps stop
+    after --ref-budget seconds (a bounded sample of the requested steps)."""
     world, rank, local, pg = dist_setup(args)
     if rank != 0:
         return
     import mpsgb
-    H = mpsgb.j1j2_cylinder(args.Lx, args.Ly, dtype=np.float64)
+    from mpsgb.operators import SPIN_HALF_CHARGES as QP
+    from oracle import blocksparse as B
+    from oracle import mps as P
+    if args.symmetry != "u1":
+        print(json.dumps({"impl": "reference", "unavailable":
+                          "the CPU arm restates the U(1) workload only"}), flush=True)
+        return
+    t_setup = time.perf_counter()
+    H = mpsgb.j1j2_cylinder(args.Lx, args.Ly, dtype=np.float64, u1=True)
     n = len(H)
     pos = n // 2 - 1
-    W1, W2 = H.W[pos], H.W[pos + 1]
-    D = cpu_sample_D(W1, W2, args.D)
-    rng = np.random.default_rng(args.seed)
-    GL = rng.standard_normal((D, W1.shape[0], D))
-    GR = rng.standard_normal((D, W2.shape[3], D))
-    flops = heff_ac2_flops(GL.shape, GR.shape, W1, W2, False)
-    for _ in range(args.warmup):
-        oracle_sample(GL, W1, W2, GR, np.float64, 1)
+    D = args.D
+    As, qb = mpsgb.u1.random_u1_tensors(n, D, args.seed, 0, np.float64)
+    psi = B.canonical_u1(As, qb, QP, pos + 1)
+    del As
+    log("reference: canonical form done")
+    envs = B.FiniteEnvironmentsU1(psi, H, keep_newest=True)
+    envs.leftenv(pos, psi)
+    envs.rightenv(pos + 1, psi)
+    t_setup = time.perf_counter() - t_setup
+    log(f"reference: environments at bond {pos} done ({t_setup:.1f} s setup)")
+    alg = P.DMRG2(maxdim=D, cutoff=1e-10)
+    state = {"eps_local": 1.0, "eps_trunc": 0.0, "decay": 0.0}
+
+    def step(stats):
+        el, et, dec, val = B.dmrg2_local_update(pos, False, psi, H, alg, envs, state["eps_local"],
+                                                state["eps_trunc"], state["decay"], stats)
+        state.update(eps_local=el, eps_trunc=et, decay=dec, val=val)
+        A = psi.AR[pos + 1]
+        B.transfer_right(envs.rightenv(pos + 1, psi), H.W[pos + 1], A, psi.qb[pos + 1], QP,
+                         psi.qb[pos + 2], envs.dq[pos + 1])
+
+    for i in range(min(args.warmup, 1)):
+        step({"matvecs": 0})
+        log(f"reference: warm-up step {i} done")
+    stats = {"matvecs": 0}
     ts = []
-    threads = 1
-    for _ in range(args.steps):
-        t, threads, _ = oracle_sample(GL, W1, W2, GR, np.float64, 1)
-        ts.append(t)
+    for i in range(args.steps):
+        t0 = time.perf_counter()
+        step(stats)
+        ts.append(time.perf_counter() - t0)
+        log(f"reference: step {i}: {ts[-1]:.2f} s")
+        if sum(ts) > args.ref_budget:
+            break
     tot = sum(ts)
-    value = flops * len(ts) / tot / 1e12
+    value = stats["block_flops"] / tot / 1e12
+    threads = oracle_threads()
+    sample = (f"{len(ts)} of the {args.steps} requested steps (timed steps stop after {args.ref_budget:.0f} s);"
+              f" one step = DMRG2 local update at bond {pos} + environment step, oracle "
+              f"block-sparse (numpy/BLAS, {threads} threads), {stats['matvecs'] / len(ts):.1f} "
+              f"matvecs per step")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "n_gpus": args.gpus, "steps": len(ts), "warmup": min(args.warmup, 1),
         "ms_per_step": 1e3 * tot / len(ts), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"J1-J2 {args.Ly}x{args.Lx} cylinder DMRG2 H_eff matvec at the "
-                               f"central bond, D={D}, dense Float64", "D": D,
-                   "sample": f"one AC2 H_eff application per step at D={D} (oracle port, numpy; "
-                             f"D halved from {args.D} until one matvec fits ~20 s)"},
-        "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": threads, "kind": "port",
-                         "sample": f"one JordanAC2 matvec of the workload's central bond at D={D} "
-                                   "per step"},
+        "config": {"workload": f"J1-J2 Heisenberg {args.Ly}x{args.Lx} cylinder ({n} sites), DMRG2 "
+                               f"local update + env step at bond {pos}, D={D}, Float64, U(1) "
+                               f"total Sz = 0, block-sparse", "symmetry": "u1", "D": D, "L": n,
+                   "mpo_width_at_bond": int(H.W[pos].shape[3]), "sample": sample,
+                   "setup_s": t_setup},
+        "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": threads,
+                         "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
+        "local_energy": state.get("val"),
     }
     print(json.dumps(line), flush=True)
-
-
-def heff_ac2_flops(GL_shape, GR_shape, W1, W2, cplx):
-    """Algorithmic flops of one AC2 application in the form libmpsgb executes it:
-    the GEMMs left after prepare folding and channel pruning (2 flops / real MAC)."""
-    Dl, wl, _ = GL_shape
-    Dr, wr, _ = GR_shape
-    d1, d2 = W1.shape[1], W2.shape[1]
-    wm = W1.shape[3]
-    nz = lambda a: a.size > 0 and np.any(a != 0)
-    A1, A2 = W1[1:-1, :, :, 1:-1], W2[1:-1, :, :, 1:-1]
-    B1, B2 = W1[1:-1, :, :, -1], W2[1:-1, :, :, -1]
-    C1, C2 = W1[0, :, :, 1:-1], W2[0, :, :, 1:-1]
-    CA = nz(C1) and nz(A2)
-    AB = nz(A1) and nz(B2)
-    IC = nz(C2) and not CA
-    BE = nz(B1) and not AB
-    macs = 0.0
-    if nz(A1) and nz(A2):
-        f1 = np.any(A1 != 0, axis=(1, 2))
-        f2 = np.any(A2 != 0, axis=(1, 2))
-        both = f1.any(0) & f2.any(1)
-        if both.any():
-            chr_ = int(f1[:, both].any(1).sum())
-            chc = int(f2[both, :].any(0).sum())
-            macs += Dl * d1 * d2 * chc * Dr * Dr + Dl * d1 * d2 * Dr * Dl * chr_
-    if CA:
-        macs += Dl * (d1 * d2 * Dr) ** 2
-    if AB:
-        macs += (Dl * d1 * d2) ** 2 * Dr
-    if IC:
-        macs += Dl * d1 * (d2 * Dr) ** 2
-    if BE:
-        macs += (Dl * d1) ** 2 * d2 * Dr
-    return (8.0 if cplx else 2.0) * macs
 
 
 # ---------------------------------------------------------------- our arm
@@ -309,7 +306,7 @@ def run_ours(args):
     prec = args.precision
     ctx.set_precision(prec)
     ctx.set_svd_method(args.svd)
-    ctx.set_gemm_schedule("persistent", args.tile_n)
+    ctx.set_gemm_schedule(args.schedule, args.tile_n)
     backend = mpsgb.GB300Backend(prec, local)
     u1 = args.symmetry == "u1"
     H = mpsgb.j1j2_cylinder(args.Lx, args.Ly, dtype=np.float64, u1=u1)
@@ -328,7 +325,9 @@ def run_ours(args):
     del As
     ctx.synchronize()
     log("canonical MPS built on the device")
-    envs = mpsgb.FiniteEnvironments(psi, H, resident=False)
+    # the right environments of the measured window stay resident (2 GB each at D = 2048)
+    envs = mpsgb.FiniteEnvironments(psi, H, resident=False, keep_left={pos},
+                                    keep_right=set(range(pos + 1, pos + args.window + 2)))
     envs.precision = backend.code
     envs.leftenv(pos, psi)
     ctx.synchronize()
@@ -399,10 +398,11 @@ def run_ours(args):
     t_step = max(t_wall, t_dev)
     t_max = allmax(pg, t_step)
     ms_per_step = 1e3 * t_max / args.steps
-    # flop accounting (untimed): one H_eff matvec at the same bond with the nonzero-product
-    # counters on -- the block-sparse algorithmic count of the U(1) workload (equal to the
-    # dense GEMM count when nothing is zero) and the tile work the tensor pipe executes
-    count = heff_count_pass(ctx, psi, H, envs, backend, pos) if prec != "fp64" else None
+    # flop accounting (untimed): one H_eff matvec at the same bond -- the charge-block flops
+    # of its contractions (2 sum_g M_g N_g K_g over the blocks of every GEMM, the work a
+    # blockwise library does; the dense GEMM count without symmetry), the nonzero products
+    # (sum_k nnz(A[:, k]) nnz(B[k, :])) and the tile work the tensor pipe executes
+    count = heff_count_pass(ctx, psi, H, envs, backend, pos, u1) if prec != "fp64" else None
     trace = None
     if args.trace:
         # one more (untimed) step under the launch trace: time per issuing source site
@@ -416,7 +416,7 @@ def run_ours(args):
         for nm, ms, ev in sites[:24]:
             log(f"  {nm:28s} {ms:9.3f} ms {ev:6d} events")
     if count:
-        heff_alg = count["nonzero_flops"] * stats.matvecs
+        heff_alg = count["block_flops"] * stats.matvecs
         rho = count["nonzero_flops"] / max(1.0, count["tile_flops"])
     else:
         heff_alg, rho = stats.heff_flops, 1.0
@@ -427,19 +427,29 @@ def run_ours(args):
     peak_src = "measured (sustained)" if peak_bf16 else "fallback"
     peak_bf16 = peak_bf16 or 1700.0
     split = 1.0 if prec == "fp64" else 3.0
-    gemm_s = prof["gemm_ms"] / 1e3
-    # algorithmic GEMM flops of the timed region: executed tile work x (nonzero / tile) of
-    # the counted matvec (the dense case has rho ~ 1, below 1 only by partial-tile padding)
-    gemm_alg = rho * tile_flops_timed / gemm_s / 1e12 if gemm_s > 0 else 0.0
+    grouped = prof["grouped"]["launches"] > 0
+    if grouped:
+        # the grouped sector-block GEMM: its charge-block flops over its own kernel time
+        kms = prof["grouped"]["ms"]
+        gemm_alg = prof["grouped"]["flops"] / (kms / 1e3) / 1e12 if kms > 0 else 0.0
+        kernel, klaunch = "gemm_grouped_kernel", prof["grouped"]["launches"]
+    else:
+        # the dense-embedding GEMM: executed tile work x (nonzero / tile) of the counted
+        # matvec (the dense case has rho ~ 1, below 1 only by partial-tile padding)
+        kms = prof["persistent"]["ms"]
+        gemm_alg = rho * tile_flops_timed / (kms / 1e3) / 1e12 if kms > 0 else 0.0
+        kernel, klaunch = "gemm_bf16x3_persistent", prof["persistent"]["launches"]
     achieved = split * gemm_alg
     roofline = {
-        "bound": "tensor", "kernel": "gemm_bf16x3_persistent", "achieved": achieved,
+        "bound": "tensor", "kernel": kernel, "achieved": achieved,
         "peak": peak_bf16, "unit": "TFLOP/s", "frac": achieved / peak_bf16,
         "peak_source": peak_src, "algorithmic_tflops": gemm_alg,
-        "executed_tile_tflops_per_product": tile_flops_timed / max(gemm_s, 1e-12) / 1e12,
-        "executed_frac": split * tile_flops_timed / max(gemm_s, 1e-12) / 1e12 / peak_bf16,
-        "launches": prof["gemm_launches"], "kernel_ms": prof["gemm_ms"],
-        "kernel_share_of_step": prof["gemm_ms"] / max(1e-9, prof["region_ms"]),
+        "executed_tile_tflops_per_product": tile_flops_timed / max(prof["gemm_ms"] / 1e3, 1e-12) / 1e12,
+        "launches": klaunch, "kernel_ms": kms,
+        "kernel_share_of_step": kms / max(1e-9, prof["region_ms"]),
+        "other_split_gemm": {"kernel": "gemm_bf16x3_persistent (environment step)",
+                             "ms": prof["persistent"]["ms"],
+                             "launches": prof["persistent"]["launches"]} if grouped else None,
         "traffic": None,
     }
 
@@ -448,29 +458,23 @@ def run_ours(args):
     e2e = None
     if not args.no_e2e:
         e2e = run_e2e(args, ctx, psi, H, envs, alg, pos, state, pg,
-                      count["nonzero_flops"] if count else None)
+                      count["block_flops"] if count else None)
         log("e2e done")
 
-    fp64 = None
-    if prec != "fp64" and not args.no_fp64_compare:
-        fp64 = fp64_compare(ctx, psi, H, envs, backend, pos, Wd, GR_next, stats, args.steps,
-                            ms_per_step / 1e3)
-        log(f"plain FP64 GPU comparison done: {fp64}")
+    accuracy = None
+    if prec != "fp64" and not args.no_accuracy:
+        accuracy = accuracy_compare(ctx, psi, H, envs, backend, pos)
+        log(f"accuracy at bond {pos}: {accuracy}")
+    window = None
+    if prec != "fp64" and not args.no_fp64_compare and args.window > 0:
+        window = window_compare(ctx, psi, H, envs, pos, args.window, prec, D, state)
+        log(f"window of {args.window} bonds: split {window['split']['s_per_bond']:.3f} s/bond, "
+            f"fp64 {window['fp64']['s_per_bond']:.3f} s/bond")
 
     cpu = None
-    if not args.no_cpu_baseline and rank == 0 and world == 1:
-        Dc = cpu_sample_D(H.W[pos], H.W[pos + 1], D)
-        GL = envs.leftenv(pos, psi).numpy()[:Dc, :, :Dc]
-        GR = envs.rightenv(pos + 1, psi).numpy()[:Dc, :, :Dc]
-        f1 = heff_ac2_flops(GL.shape, GR.shape, H.W[pos], H.W[pos + 1], False)
-        log(f"cpu baseline sample starting (D={Dc})")
-        t, threads, nrep = oracle_sample(GL, H.W[pos], H.W[pos + 1], GR, np.float64, 1, 10.0)
-        log("cpu baseline sample done")
-        cpu = {"value": f1 / t / 1e12, "unit": "TFLOP/s", "cores": threads, "kind": "port",
-               "sample": f"{nrep} JordanAC2 matvecs (oracle, numpy/BLAS, dense arithmetic) at "
-                         f"the workload's central bond restricted to D={Dc} (the leading block "
-                         f"of the device-built environments), {t:.2f} s each; flops counted "
-                         f"dense, the rate a block-sparse CPU contraction would also run at"}
+    if not args.no_cpu_baseline and rank == 0 and world == 1 and u1:
+        cpu = cpu_baseline_sample(psi, H, envs, pos, stats.matvecs / args.steps)
+        log(f"cpu baseline done: {cpu['value']:.4f} TFLOP/s")
 
     if rank == 0:
         line = {
@@ -490,7 +494,6 @@ def run_ours(args):
                 "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (GL/GR/T1 >> 129 MB)",
             },
             "gpu_launches": launches,
-            "sweep_s_estimate": ms_per_step / 1e3 * (2 * n - 3),
             "heff_flops_per_step": heff_alg / args.steps,
             "heff_flops_per_matvec": {
                 "nonzero_products": count["nonzero_flops"] if count else None,
@@ -502,7 +505,8 @@ def run_ours(args):
             "setup_s": t_setup,
             "roofline": roofline,
             "launch_trace": trace,
-            "fp64_gpu": fp64,
+            "accuracy_vs_fp64": accuracy,
+            "sweep_window": window,
             "clocks": clocks.summary(),
             "e2e": e2e,
             "cpu_baseline": cpu,
@@ -512,53 +516,149 @@ def run_ours(args):
         pg.destroy_process_group()
 
 
-def heff_count_pass(ctx, psi, H, envs, backend, pos):
-    """One AC2 matvec with the GEMM work counters on: nonzero-product flops (block-sparse
-    algorithmic count) and tile flops executed per split product."""
+def heff_count_pass(ctx, psi, H, envs, backend, pos, u1):
+    """One AC2 matvec with the GEMM work counters on: charge-block flops (the grouped GEMMs'
+    2 sum_g M_g N_g K_g; without symmetry the dense GEMM flops), nonzero-product flops and
+    tile flops executed per split product."""
     import mpsgb
     ctx.read_work(reset=True)
     ctx.set_counting(True)
     try:
         Heff = mpsgb.AC2_hamiltonian(pos, psi, H, envs, backend)
         x = mpsgb.ac2_from(psi.AL[pos], psi.ac(pos + 1))
-        Heff(x)
+        Heff.set_sectors(x)
         ctx.synchronize()
-        return ctx.read_work(reset=True)
+        ctx.read_work(reset=True)
+        ctx.profile_begin()
+        Heff(x)
+        prof = ctx.profile_end()
+        out = ctx.read_work(reset=True)
     finally:
         ctx.set_counting(False)
+    if prof["grouped"]["launches"] > 0:
+        out["block_flops"] = prof["grouped"]["flops"]
+    else:
+        out["block_flops"] = out["nonzero_flops"] if u1 else prof["gemm_flops"]
+    return out
 
 
-def fp64_compare(ctx, psi, H, envs, backend, pos, Wd, GR_next, stats, steps, t_step_split):
-    """The plain FP64 GPU path on the same bond: one AC2 matvec and one environment step timed
-    at FP64 (same kernels' FP64 variants, CUDA-event region on the library stream), composed
-    with the step's measured matvec count and its FP64 gauge time into a per-step figure."""
+def cpu_baseline_sample(psi, H, envs, pos, matvecs):
+    """The oracle's block-sparse operator (oracle/blocksparse.py) on the host cores, on the
+    environments and state of the GPU run at the bench bond: the operator build plus as many
+    matvecs as one GPU local update took (a bounded sample of one local update; the block SVD
+    is left out).  Rate = charge-block flops / time, as in the GPU arm."""
+    from mpsgb.operators import SPIN_HALF_CHARGES as QP
+    from oracle import blocksparse as B
+    GL = envs.leftenv(pos, psi).numpy()
+    GR = envs.rightenv(pos + 1, psi).numpy()
+    x = __import__("mpsgb").ac2_from(psi.AL[pos], psi.ac(pos + 1))
+    ql, _, qr, _ = x.charges
+    x = x.numpy()
+    dq = B.mpo_channel_charges([H.W[i] for i in range(len(H))], QP)
+    k = max(1, int(round(matvecs)))
+    t0 = time.perf_counter()
+    op = B.JordanAC2U1(GL, H.W[pos], H.W[pos + 1], GR, ql, QP, qr, dq[pos], dq[pos + 2])
+    t_build = time.perf_counter() - t0
+    for _ in range(k):
+        x = op(x)
+        x /= np.linalg.norm(x)
+    t = time.perf_counter() - t0
+    threads = oracle_threads()
+    return {"value": op.block_flops() * k / t / 1e12, "unit": "TFLOP/s", "cores": threads,
+            "kind": "port",
+            "sample": f"oracle block-sparse JordanAC2 at bond {pos} on the device-built "
+                      f"environments: operator build ({t_build:.1f} s) + {k} matvecs (the "
+                      f"matvec count of one GPU local update), {t:.1f} s; numpy/BLAS with "
+                      f"{threads} threads; the block SVD and the environment step left out"}
+
+
+def accuracy_compare(ctx, psi, H, envs, backend, pos, fp64_maxiter=4):
+    """The precision condition of the metric at the bench bond: from the same state,
+    environments and start vector, the split-precision Lanczos solve followed by its FP64
+    refinement step (one FP64 matvec: Rayleigh quotient and residual of the split solution
+    with the FP64 operator) against the FP64 Lanczos solve of the same local problem."""
     import mpsgb
-    from mpsgb import _lib as L
-    Heff = mpsgb.AC2_hamiltonian(pos, psi, H, envs, mpsgb.GB300Backend("fp64", backend.device))
-    x = mpsgb.ac2_from(psi.AL[pos], psi.ac(pos + 1))
-    y = Heff.new_vector()
-    Heff(x, out=y)                       # warm-up (plans, pool)
-    ctx.synchronize()
-    ctx.profile_begin()
-    Heff(x, out=y)
-    ctx.synchronize()
-    t_mv = ctx.profile_end()["region_ms"] / 1e3
-    A = psi.AR[pos + 1]
-    ctx.profile_begin()
-    L.check(L.lib().gb_env_transfer_right(ctx.handle, envs.rightenv(pos + 1, psi).handle,
-                                          Wd[pos + 1].handle, A.handle, A.handle,
-                                          L.GB_PREC_FP64, GR_next.handle))
-    ctx.synchronize()
-    t_env = ctx.profile_end()["region_ms"] / 1e3
-    del Heff, y
-    mv = stats.matvecs / steps
-    gauge = stats.t["gauge"] / steps
-    est = mv * t_mv + gauge + t_env
-    return {"matvec_s": t_mv, "env_step_s": t_env, "matvecs_per_step": mv,
-            "gauge_s": gauge, "step_s_estimate": est,
-            "split_speedup_per_step": est / t_step_split,
-            "how": "FP64 matvec and env step timed once each on the device; step = "
-                   "matvecs x matvec + gauge (FP64 in both paths) + env step"}
+    fp64 = mpsgb.GB300Backend("fp64", backend.device)
+    x0 = mpsgb.ac2_from(psi.AL[pos], psi.ac(pos + 1))
+    H64 = mpsgb.AC2_hamiltonian(pos, psi, H, envs, fp64)
+    Hs = mpsgb.AC2_hamiltonian(pos, psi, H, envs, backend)
+
+    def refine(x):
+        y = H64(x)
+        nx2 = x.dot(x).real
+        e = float(np.real(x.dot(y))) / nx2
+        y.axpy_(-e, x)
+        return e, y.norm() / np.sqrt(nx2)
+
+    out = {}
+    for label, op, tol, mi in (("split", Hs, 1e-10, 12), ("fp64", H64, 1e-11, fp64_maxiter)):
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        lam, x, info = mpsgb.fixedpoint(op, x0, "SR", mpsgb.Lanczos(krylovdim=30, maxiter=mi,
+                                                                   tol=tol, eager=False))
+        ctx.synchronize()
+        t = time.perf_counter() - t0
+        e, r = refine(x)
+        out[label] = {"eigsolve_s": t, "matvecs": info.numops, "converged": info.converged,
+                      "ritz_value": lam, "energy_fp64": e, "residual_fp64": r}
+    e_s, e_d = out["split"]["energy_fp64"], out["fp64"]["energy_fp64"]
+    out["delta_e_rel"] = abs(e_s - e_d) / abs(e_d)
+    out["ritz_delta_rel"] = abs(out["split"]["ritz_value"] - e_d) / abs(e_d)
+    out["how"] = ("same bond, state, environments and x0; split Lanczos (tol 1e-10, stops at "
+                  "its noise floor) then one FP64 matvec: energy = FP64 Rayleigh quotient, "
+                  "residual = |H x - E x| / |x| with the FP64 operator; against the FP64 "
+                  "Lanczos solve (tol 1e-11)")
+    return out
+
+
+def window_compare(ctx, psi, H, envs, pos, nb, prec, D, state):
+    """A sweep window measured in both precisions from the same state: `nb` consecutive
+    two-site updates moving right from the bench bond (local update + the left environment
+    the next bond needs), split precision first, then plain FP64 from the restored state.
+    Per bond: Ritz value, matvecs; per window: seconds (device-synchronised)."""
+    import mpsgb
+    from mpsgb.algorithms import SweepStats, dmrg2_local_update
+    sites = range(pos, pos + nb + 2)
+    saved = ({i: psi.AL[i] for i in sites}, {i: psi.AR[i] for i in sites},
+             {i: psi.C[i] for i in sites}, psi.center)
+
+    def restore():
+        for i in sites:
+            psi.AL[i], psi.AR[i], psi.C[i] = saved[0][i], saved[1][i], saved[2][i]
+        psi.center = saved[3]
+
+    res = {}
+    for label, p in (("split", prec), ("fp64", "fp64")):
+        restore()
+        be = mpsgb.GB300Backend(p)
+        envs.precision = be.code
+        alg = mpsgb.DMRG2(maxdim=D, cutoff=1e-10, backend=be)
+        envs.leftenv(pos, psi)
+        envs.rightenv(pos + 1, psi)
+        ctx.synchronize()
+        stats = SweepStats(sync=True)
+        ritz, et, dec = [], state["eps_trunc"], state["decay"]
+        t0 = time.perf_counter()
+        for k in range(nb):
+            el, et, dec, val = dmrg2_local_update(pos + k, True, psi, H, alg, envs,
+                                                  state["eps_local"], et, dec, stats)
+            envs.leftenv(pos + k + 1, psi)  # the next bond's left environment
+            ritz.append(val)
+        ctx.synchronize()
+        t = time.perf_counter() - t0
+        res[label] = {"seconds": t, "s_per_bond": t / nb, "matvecs": stats.matvecs,
+                      "phase_s": {k: v for k, v in stats.t.items()}, "ritz_values": ritz}
+    restore()
+    envs.precision = mpsgb.GB300Backend(prec).code
+    res["bonds"] = [pos, pos + nb - 1]
+    res["split_speedup_per_bond"] = res["fp64"]["s_per_bond"] / res["split"]["s_per_bond"]
+    res["max_ritz_delta_rel"] = max(abs(a - b) / abs(b) for a, b in
+                                    zip(res["split"]["ritz_values"], res["fp64"]["ritz_values"]))
+    res["how"] = ("measured: the same right-moving window of two-site updates run in split "
+                  "precision and in plain FP64 from the same state, each with its own Krylov "
+                  "budget (AdaptiveKrylov), SVD truncation and left-environment steps; Ritz "
+                  "values are those of each precision's own operator")
+    return res
 
 
 def run_e2e(args, ctx, psi, H, envs, alg, pos, state, pg, flops_per_matvec=None):
@@ -622,6 +722,103 @@ def run_e2e(args, ctx, psi, H, envs, alg, pos, state, pg, flops_per_matvec=None)
             "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * t / args.steps,
             "path": "gb_heff_set_sectors once; gb_tensor_upload -> gb_heff_eigsolve -> "
                     "gb_svd_trunc -> gb_tensor_download"}
+
+
+def run_matvec(args):
+    """Repeated applications of the two-site operator at the central bond of the headline
+    model (U(1), seeded random state, D = --D): the dominant contractions alone, for
+    profiling at a size whose operands fit a few GB.  Reports charge-block TFLOP/s."""
+    import mpsgb
+    ctx = mpsgb.context(0)
+    ctx.set_gemm_schedule(args.schedule, args.tile_n)
+    backend = mpsgb.GB300Backend(args.precision, 0)
+    H = mpsgb.j1j2_cylinder(args.Lx, args.Ly, dtype=np.float64, u1=True)
+    n, D = len(H), args.D
+    pos = n // 2 - 1
+    As, qb = mpsgb.u1.random_u1_tensors(n, D, args.seed, 0, np.float64)
+    psi = mpsgb.FiniteMPS.from_tensors(As, ctx, center=pos + 1,
+                                       charges=(qb, mpsgb.operators.SPIN_HALF_CHARGES))
+    envs = mpsgb.FiniteEnvironments(psi, H, resident=False)
+    envs.precision = backend.code
+    Heff = mpsgb.AC2_hamiltonian(pos, psi, H, envs, backend)
+    x = mpsgb.ac2_from(psi.AL[pos], psi.ac(pos + 1))
+    Heff.set_sectors(x)
+    y = Heff.new_vector()
+    y.charges = x.charges
+    for _ in range(max(args.warmup, 1)):
+        Heff(x, out=y)
+    ctx.synchronize()
+    ctx.profile_begin()
+    for _ in range(args.steps):
+        Heff(x, out=y)
+    prof = ctx.profile_end()
+    t = prof["region_ms"] / 1e3
+    g = prof["grouped"]
+    per = g["flops"] / max(1, args.steps)
+    line = {
+        "metric": "H_eff TFLOP/s (charge blocks), two-site operator at the central bond",
+        "value": g["flops"] / t / 1e12 if t > 0 else 0.0, "unit": "TFLOP/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": f"f64 ({args.precision} split contractions)", "data": "synthetic",
+        "config": {"workload": f"J1-J2 {args.Ly}x{args.Lx} cylinder AC2 apply at bond {pos}, "
+                               f"D={D}, U(1)", "terms": Heff.terms},
+        "block_flops_per_matvec": per,
+        "grouped_gemm": {"ms": g["ms"], "launches": g["launches"],
+                         "tflops": g["flops"] / (g["ms"] / 1e3) / 1e12 if g["ms"] > 0 else 0.0},
+        "gpu_launches": ctx.kernel_launches(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_dmrg2_sweep(args):
+    """Full DMRG2 sweeps (dmrg.jl:286-354: L-1 bond updates left to right, L-2 back) of the
+    headline workload from its seeded random state, measured end to end: every local update
+    (operator build, Galerkin matvec, adaptive Lanczos, blockwise truncated SVD) and every
+    environment step.  Environments at D = 2048 are 2 GB each, so only every `checkpoint`-th
+    one (and the newest per side) stays resident; the others are recomputed from the nearest
+    checkpoint, whose cost is part of the measured sweep."""
+    import mpsgb
+    ctx = mpsgb.context(0)
+    prec = args.precision
+    ctx.set_precision(prec)
+    ctx.set_svd_method(args.svd)
+    ctx.set_gemm_schedule(args.schedule, args.tile_n)
+    backend = mpsgb.GB300Backend(prec, 0)
+    H = mpsgb.j1j2_cylinder(args.Lx, args.Ly, dtype=np.float64, u1=True)
+    n, D = len(H), args.D
+    As, qb = mpsgb.u1.random_u1_tensors(n, D, args.seed, 0, np.float64)
+    psi = mpsgb.FiniteMPS.from_tensors(As, ctx, center=0,
+                                       charges=(qb, mpsgb.operators.SPIN_HALF_CHARGES))
+    del As
+    K = max(1, args.checkpoint)
+    envs = mpsgb.FiniteEnvironments(psi, H, resident=False, keep_left=set(range(0, n + 1, K)),
+                                    keep_right=set(range(0, n, K)))
+    envs.precision = backend.code
+    envs.rightenv(0, psi)
+    ctx.synchronize()
+    log("sweep workload: state and right environments ready")
+    alg = mpsgb.DMRG2(maxdim=D, cutoff=1e-10, backend=backend)
+    with ClockSampler(0) as clocks:
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        psi, envs, eps, hist = mpsgb.find_groundstate(psi, H, alg, envs=envs, maxsweeps=args.sweeps)
+        ctx.synchronize()
+        t = time.perf_counter() - t0
+    per = [{"sweep": h["sweep"], "seconds": h["time"], "energy": h["energy"], "eps": h["eps"],
+            "matvecs": h["matvecs"]} for h in hist]
+    line = {
+        "metric": "DMRG2 sweep seconds at D=2048 (J1-J2 6x24 cylinder, U(1))",
+        "value": t / len(hist), "unit": "s/sweep", "n_gpus": 1, "steps": len(hist), "warmup": 0,
+        "ms_per_step": 1e3 * t / len(hist), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": f"f64 ({prec} split contractions)", "data": "synthetic",
+        "config": {"workload": f"J1-J2 Heisenberg {args.Ly}x{args.Lx} cylinder ({n} sites), full "
+                               f"DMRG2 sweeps from the seeded random U(1) state (Sz = 0), "
+                               f"D={D}, Float64", "checkpoint": K, "precision": prec},
+        "sweeps": per, "clocks": clocks.summary(),
+        "gpu_launches": ctx.kernel_launches(),
+    }
+    print(json.dumps(line), flush=True)
 
 
 def run_vumps_sweep(args):
@@ -726,6 +923,10 @@ def main():
         run_reference(args)
     elif args.workload == "vumps-sweep":
         run_vumps_sweep(args)
+    elif args.workload == "matvec":
+        run_matvec(args)
+    elif args.workload == "dmrg2-sweep":
+        run_dmrg2_sweep(args)
     elif args.workload == "vumps-xxz":
         run_vumps_xxz(args)
     else:

@@ -96,6 +96,13 @@ int gb_ctx_synchronize(gb_ctx* ctx);
 int gb_ctx_kernel_launches(gb_ctx* ctx, int64_t* out);
 /* device status word written by bounded waits inside kernels (0 = clean); cleared on read */
 int gb_ctx_device_status(gb_ctx* ctx, int32_t* out);
+/* Bound (seconds, default 2) on every pipeline wait of the tensor-core kernels launched
+ * through this context.  A wait that runs out records GB_ERR_TIMEOUT in the status word
+ * (gb_ctx_device_status); the kernel then waits (with the default bound) for the copies
+ * and MMAs it has already issued, releases its tensor memory and returns, so the context
+ * stays usable.  No counterpart in the reference (it has no device code); it is the
+ * failure-detection knob of this library, and tests shorten it to exercise that path. */
+int gb_ctx_set_wait_bound(gb_ctx* ctx, double seconds);
 /* arithmetic of the auxiliary state contractions of this context (gb_mps_ac2,
  * gb_mps_mul_front, gb_mps_mul_tail, gb_project_complement); GB_PREC_FP64 by default */
 int gb_ctx_set_precision(gb_ctx* ctx, int precision);
@@ -108,6 +115,13 @@ int gb_ctx_set_precision(gb_ctx* ctx, int precision);
 int gb_ctx_profile_begin(gb_ctx* ctx);
 int gb_ctx_profile_end(gb_ctx* ctx, double* gemm_ms, int64_t* gemm_launches,
                        double* gemm_flops, double* region_ms);
+/* The same region split by kernel family (valid after gb_ctx_profile_end): summed kernel
+ * time (ms), launches and flops.  GB_PROF_PERSISTENT: the split GEMMs over dense-embedded
+ * operands (flops of their full shapes); GB_PROF_GROUPED: the grouped sector-block GEMMs
+ * (flops of their charge blocks, 2 sum_g M_g N_g K_g -- the work a blockwise library does). */
+enum { GB_PROF_PERSISTENT = 0, GB_PROF_GROUPED = 1 };
+int gb_ctx_profile_kernel(gb_ctx* ctx, int kernel, double* ms, int64_t* launches,
+                          double* flops);
 
 /* Launch trace of the context's stream: between trace_begin and trace_end every kernel the
  * library launches (and every traced library call) records an event tagged with its source
@@ -130,9 +144,17 @@ enum {
   GB_SCHED_PERSISTENT = 0,       /* one CTA per SM over a tile counter, accumulator double-
                                     buffered in TMEM; k-blocks whose packed A and B tiles
                                     are both zero are skipped (block-sparse operands stored
-                                    densely with charge-sorted legs); the default         */
+                                    densely with charge-sorted legs)                      */
   GB_SCHED_PERSISTENT_DENSE = 1, /* the same kernel over every k-block                    */
-  GB_SCHED_TILE = 2              /* one CTA per output tile, single accumulator          */
+  GB_SCHED_TILE = 2,             /* one CTA per output tile, single accumulator          */
+  GB_SCHED_GROUPED = 3           /* the default: operators whose U(1) sectors are known
+                                    (gb_heff_set_sectors; real data, split precision) run
+                                    every GEMM as one persistent launch over its charge
+                                    blocks only -- operands packed block by block, tiles
+                                    sized to each block, as TensorKit contracts a symmetric
+                                    TensorMap blockwise; every other GEMM runs as
+                                    GB_SCHED_PERSISTENT.  The schedule is read when an
+                                    operator is built. */
 };
 int gb_ctx_set_gemm_schedule(gb_ctx* ctx, int schedule, int tile_n);
 /* Work counters of the split-precision GEMMs (the flop accounting of the block-sparse
@@ -255,12 +277,19 @@ int gb_project_complement(gb_ctx* ctx, gb_tensor* Y, const gb_tensor* X);
 enum {
   GB_SVD_GESVD = 0,   /* cuSOLVER QR-iteration SVD (default)                          */
   GB_SVD_GESVDP = 1,  /* cuSOLVER polar-decomposition SVD                             */
-  GB_SVD_GRAM = 2     /* eigendecomposition of the Gram matrix (FP64 syevd); singular
-                         values below ~1e-7 of the largest lose relative accuracy     */
+  GB_SVD_GRAM = 2     /* eigendecomposition of the Gram matrix of the smaller side
+                         (FP64 syevd; per charge block for U(1)).  Its singular values
+                         are rounding noise below ~1e-7 of the largest (of the block):
+                         when a kept value or the first discarded one is that small, the
+                         call falls back to the SVD (GB_SVD_GESVD) for that
+                         factorisation.  The bond factor S it returns is triangular
+                         (R Sigma or Sigma L, making AL and AR exact isometries), not
+                         diagonal; the truncated state AL S AR is the same.           */
 };
 int gb_ctx_set_svd_method(gb_ctx* ctx, int method);
 /* Truncated SVD of a two-site tensor, gauge2! (src/states/orthoview.jl:401-420) with
- * truncrank(maxdim) & trunctol(atol): AL[l s1; k], S (diagonal, GB_KIND_BOND k x k),
+ * truncrank(maxdim) & trunctol(atol): AL[l s1; k], S (GB_KIND_BOND k x k: diagonal, or
+ * triangular under GB_SVD_GRAM),
  * AR[k s2; r].  Returns the discarded-weight norm eps.  Outputs are newly created. */
 int gb_svd_trunc(gb_ctx* ctx, const gb_tensor* AC2, int64_t maxdim, double atol,
                  int normalize, gb_tensor** AL, gb_tensor** S, gb_tensor** AR, double* eps);
@@ -306,7 +335,9 @@ int gb_u1_svd_trunc(gb_ctx* ctx, const gb_tensor* AC2, const int32_t* q_l, const
  * (Dl*w*Dr elements) lives in a 64 MiB file-scope device array shared by all calls, so
  * larger problems are rejected with GB_ERR_ARG and calls that overlap on the GPU race.
  * The first call on a device looks up the array's address; make it before any stream
- * capture. */
+ * capture.  The address is cached for the life of the process and cudaDeviceReset unloads
+ * the array: after a reset of a device, do not call this entry point on that device again
+ * in the same process. */
 int gb_c_apply_noalloc(const void* GL, const void* GR, const void* x, void* y, int64_t Dl,
                        int64_t Dr, int64_t w, int dtype, void* stream);
 

@@ -492,7 +492,12 @@ void qr_pos(gb_ctx* ctx, int dtype, int64_t m, int64_t n, const void* M, void* Q
 // the other factor (M V / sigma, or sigma^-1 U^H M) is made exactly isometric by a positive
 // QR / LQ, whose triangular factor is absorbed into the bond matrix C = R Sigma (or Sigma L).
 // The state AL C AR equals U Sigma V^H of the truncated SVD; C is triangular, not diagonal.
-void svd_trunc_gram(gb_ctx* ctx, const gb_tensor* AC2, int64_t maxdim, double atol, int normalize,
+// Singular values from Gram eigenvalues carry an absolute error of about eps_mach * s_max^2 /
+// s, so values below GRAM_FLOOR * s_max are rounding noise: when a kept value or the first
+// discarded one lies below that floor, the rank and the discarded weight cannot be decided
+// from them, and the function returns false without output (the caller then runs the SVD).
+constexpr double GRAM_FLOOR = 1e-7;
+bool svd_trunc_gram(gb_ctx* ctx, const gb_tensor* AC2, int64_t maxdim, double atol, int normalize,
                     gb_tensor** AL, gb_tensor** S, gb_tensor** AR, double* eps) {
   cusolverDnHandle_t h = solver(ctx);
   const int dt = AC2->dtype;
@@ -538,6 +543,8 @@ void svd_trunc_gram(gb_ctx* ctx, const gb_tensor* AC2, int64_t maxdim, double at
     if (hs[i] > atol) ++keep;
   if (maxdim > 0) keep = std::min(keep, maxdim);
   keep = std::max<int64_t>(keep, 1);
+  const double floor = GRAM_FLOOR * hs[0];
+  if (!(hs[keep - 1] >= floor && (keep == g || hs[keep] >= floor))) return false;
   double e2 = 0.0;
   for (int64_t i = keep; i < g; ++i) e2 += hs[i] * hs[i];
   if (eps) *eps = std::sqrt(e2);
@@ -597,6 +604,7 @@ void svd_trunc_gram(gb_ctx* ctx, const gb_tensor* AC2, int64_t maxdim, double at
   *AL = al;
   *AR = ar;
   *S = cc;
+  return true;
 }
 
 // env-transfer mix plans cached per (W, side, dims)
@@ -810,6 +818,7 @@ void run_on_lanes(gb_ctx* ctx, int64_t n, const std::function<void(gb_ctx*, int6
     l->aux_prec = ctx->aux_prec;
     l->gemm_schedule = ctx->gemm_schedule;
     l->gemm_bn = ctx->gemm_bn;
+    l->wait_ns = ctx->wait_ns;
     before[k] = l->launches;
   }
   if (!ctx->lane_pool) ctx->lane_pool = new LanePool();
@@ -957,11 +966,19 @@ int gb_ctx_set_gemm_schedule(gb_ctx* ctx, int schedule, int tile_n) {
   API_BEGIN
   GB_REQUIRE(ctx, "null context");
   GB_REQUIRE(schedule == GB_SCHED_PERSISTENT || schedule == GB_SCHED_PERSISTENT_DENSE ||
-                 schedule == GB_SCHED_TILE,
+                 schedule == GB_SCHED_TILE || schedule == GB_SCHED_GROUPED,
              "unknown GEMM schedule");
   GB_REQUIRE(tile_n == 0 || tile_n == 128 || tile_n == 256, "tile_n must be 0, 128 or 256");
   ctx->gemm_schedule = schedule;
   ctx->gemm_bn = tile_n;
+  API_END
+}
+
+int gb_ctx_set_wait_bound(gb_ctx* ctx, double seconds) {
+  API_BEGIN
+  GB_REQUIRE(ctx, "null context");
+  GB_REQUIRE(seconds >= 0.0 && seconds <= 60.0, "wait bound must lie in [0, 60] s");
+  ctx->wait_ns = (unsigned long long)(seconds * 1e9);
   API_END
 }
 
@@ -1055,6 +1072,8 @@ int gb_ctx_profile_begin(gb_ctx* ctx) {
   ctx->profiling = true;
   ctx->prof_used = 0;
   ctx->prof_flops = 0.0;
+  ctx->prof_kind.clear();
+  for (int k = 0; k < 2; ++k) ctx->prof_kind_flops[k] = 0.0;
   GB_CHECK_CUDA(cudaEventRecord(ctx->prof_region[0], ctx->stream));
   API_END
 }
@@ -1068,10 +1087,18 @@ int gb_ctx_profile_end(gb_ctx* ctx, double* gemm_ms, int64_t* gemm_launches, dou
   GB_CHECK_CUDA(cudaEventRecord(ctx->prof_region[1], ctx->stream));
   GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
   double tot = 0.0;
+  for (int k = 0; k < 2; ++k) {
+    ctx->prof_res_ms[k] = 0.0;
+    ctx->prof_res_n[k] = 0;
+    ctx->prof_res_flops[k] = ctx->prof_kind_flops[k];
+  }
   for (size_t i = 0; i + 1 < ctx->prof_used; i += 2) {
     float ms = 0.f;
     GB_CHECK_CUDA(cudaEventElapsedTime(&ms, ctx->prof_events[i], ctx->prof_events[i + 1]));
     tot += ms;
+    const int k = (i / 2 < ctx->prof_kind.size()) ? ctx->prof_kind[i / 2] : 0;
+    ctx->prof_res_ms[k] += ms;
+    ctx->prof_res_n[k] += 1;
   }
   float rms = 0.f;
   GB_CHECK_CUDA(cudaEventElapsedTime(&rms, ctx->prof_region[0], ctx->prof_region[1]));
@@ -1081,6 +1108,17 @@ int gb_ctx_profile_end(gb_ctx* ctx, double* gemm_ms, int64_t* gemm_launches, dou
   if (region_ms) *region_ms = rms;
   ctx->profiling = false;
   ctx->prof_used = 0;
+  API_END
+}
+
+int gb_ctx_profile_kernel(gb_ctx* ctx, int kernel, double* ms, int64_t* launches,
+                          double* flops) {
+  API_BEGIN
+  GB_REQUIRE(ctx, "null context");
+  GB_REQUIRE(kernel == GB_PROF_PERSISTENT || kernel == GB_PROF_GROUPED, "unknown kernel family");
+  if (ms) *ms = ctx->prof_res_ms[kernel];
+  if (launches) *launches = ctx->prof_res_n[kernel];
+  if (flops) *flops = ctx->prof_res_flops[kernel];
   API_END
 }
 
@@ -1599,10 +1637,10 @@ int gb_svd_trunc(gb_ctx* ctx, const gb_tensor* AC2, int64_t maxdim, double atol,
   GB_REQUIRE(AL && S && AR, "null output");
   GB_REQUIRE(AC2->kind == GB_KIND_AC2, "svd_trunc: input must be a two-site tensor");
   DevGuard g(ctx->device);
-  if (ctx->svd_method == GB_SVD_GRAM) {
-    svd_trunc_gram(ctx, AC2, maxdim, atol, normalize, AL, S, AR, eps);
+  // the Gram route when its singular values decide the truncation, else the SVD below
+  if (ctx->svd_method == GB_SVD_GRAM &&
+      svd_trunc_gram(ctx, AC2, maxdim, atol, normalize, AL, S, AR, eps))
     return GB_OK;
-  }
   const int dt = AC2->dtype;
   const size_t es = elem_size(dt);
   const int64_t Dl = AC2->dims[0], d1 = AC2->dims[1], Dr = AC2->dims[2], d2 = AC2->dims[3];

@@ -71,6 +71,9 @@ struct gb_ctx {
   cudaStream_t stream = nullptr;
   int64_t launches = 0;
   int32_t* d_status = nullptr;   // device status word (bounded waits)
+  // bound on every pipeline wait inside the tensor-core kernels (gb_ctx_set_wait_bound);
+  // on expiry a kernel records GB_ERR_TIMEOUT, drains its copies and exits
+  unsigned long long wait_ns = 2000000000ull;
   void* solver = nullptr;        // cusolverDnHandle_t
   void* solver_params = nullptr; // cusolverDnParams_t
   gb::Scratch scratch[gb::SLOT_COUNT];
@@ -80,7 +83,7 @@ struct gb_ctx {
   int aux_prec = GB_PREC_FP64;   // precision of auxiliary state contractions
   int svd_method = 0;            // GB_SVD_* of gb_svd_trunc
   // split-precision GEMM schedule (GB_SCHED_*) and output tile width (0 = chosen per shape)
-  int gemm_schedule = 0;
+  int gemm_schedule = GB_SCHED_GROUPED;
   int gemm_bn = 0;
   unsigned int* d_tile_counter = nullptr;  // work counter of the persistent GEMM
   // work counters (device doubles): [0] flops the tensor pipe executes per split product
@@ -96,6 +99,13 @@ struct gb_ctx {
   std::vector<cudaEvent_t> prof_events;  // pairs (start, stop) per launch
   size_t prof_used = 0;
   double prof_flops = 0.0;
+  // per kernel family (0: dense-embedding split GEMM, 1: grouped sector-block GEMM): the
+  // family of every event pair, the flops issued, and after profile_end the summed results
+  std::vector<int> prof_kind;
+  double prof_kind_flops[2] = {0.0, 0.0};
+  double prof_res_ms[2] = {0.0, 0.0};
+  int64_t prof_res_n[2] = {0, 0};
+  double prof_res_flops[2] = {0.0, 0.0};
   cudaEvent_t prof_region[2] = {nullptr, nullptr};
   // launch trace: an event after every counted launch (and every trace point), tagged with
   // the source site that issued it; the time between consecutive events is charged to the

@@ -26,6 +26,7 @@
 #include <mutex>
 
 #include "gb_common.h"
+#include "tc_ptx.cuh"
 
 namespace gb {
 
@@ -39,36 +40,8 @@ constexpr int TC_B_BYTES = TC_BN * TC_BK * 2;
 constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
 constexpr int TC_SMEM_BYTES = TC_STAGES * TC_STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 constexpr int64_t KALIGN = TC_BK;
-constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s bound on any wait
 
 static inline int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
-
-// ------------------------------------------------------------------ plane element types
-// BF16 planes (bf16x3) or TF32 values in 32-bit words (tf32x3).  A k-block is one 128-byte
-// swizzle row: 64 BF16 or 32 TF32 elements.
-template <typename E>
-constexpr int bk_of() {
-  return 128 / (int)sizeof(E);
-}
-__device__ __forceinline__ float tf32_rna(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return __uint_as_float(r);
-}
-__device__ __forceinline__ void split_put(__nv_bfloat16* hi, __nv_bfloat16* lo, int64_t i,
-                                          double v) {
-  const __nv_bfloat16 h = __double2bfloat16(v);
-  hi[i] = h;
-  lo[i] = __double2bfloat16(v - (double)__bfloat162float(h));
-}
-__device__ __forceinline__ void split_put(float* hi, float* lo, int64_t i, double v) {
-  const float h = tf32_rna((float)v);
-  hi[i] = h;
-  lo[i] = tf32_rna((float)(v - (double)h));
-}
-__device__ __forceinline__ bool plane_nz(__nv_bfloat16 a) { return __bfloat162float(a) != 0.f; }
-__device__ __forceinline__ bool plane_nz(float a) { return a != 0.f; }
-static inline bool is_tf32(int prec) { return prec == GB_PREC_TF32X3; }
 
 // ------------------------------------------------------------------ packing
 // out layout: [batch][plane(2)][rows][Kp] bf16 ; rows = M (A) or N / 2N (B, complex)
@@ -462,111 +435,6 @@ void mixpack_run(gb_ctx* ctx, const MixDev& m, const int64_t* kJ, const int64_t*
   if (ctx->counting) count_cols(ctx, out);
 }
 
-// ------------------------------------------------------------------ PTX helpers
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ unsigned long long globaltimer() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
-  return t;
-}
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// bounded wait: returns false (and records a timeout) when the bound expires
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, int* status) {
-  if (mbar_try_wait(bar, parity)) return true;
-  unsigned long long t0 = globaltimer();
-  while (!mbar_try_wait(bar, parity)) {
-    if (globaltimer() - t0 > WAIT_NS) {
-      atomicExch(status, GB_ERR_TIMEOUT);
-      return false;
-    }
-  }
-  return true;
-}
-__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, uint32_t bar,
-                                            int x, int y, int z) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(dst),
-      "l"((unsigned long long)map), "r"(bar), "r"(x), "r"(y), "r"(z)
-      : "memory");
-}
-__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((saddr >> 4) & 0x3FFF);        // start address
-  d |= (uint64_t)1 << 16;                        // leading byte offset (unused for SW128 K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;              // stride byte offset: 8 rows x 128 B
-  d |= (uint64_t)1 << 46;                        // descriptor version (sm_100 family)
-  d |= (uint64_t)2 << 61;                        // 128-byte swizzle
-  return d;
-}
-// kind::f16 instruction descriptor: BF16 x BF16 -> F32, both K-major
-__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
-         ((uint32_t)(M >> 4) << 24);
-}
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
-                                         uint32_t idesc, uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
-}
-// kind::tf32 instruction descriptor: TF32 x TF32 -> F32, both K-major
-__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
-  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) |
-         ((uint32_t)(M >> 4) << 24);
-}
-__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
-                                         uint32_t idesc, uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
-}
-__device__ __forceinline__ void mma_commit(uint32_t bar) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-      : "memory");
-}
-__device__ __forceinline__ void tc_fence_before() {
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void tc_fence_after() {
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-
-#define TMEM_LD32(taddr, r)                                                                   \
-  asm volatile(                                                                               \
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13," \
-      "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"      \
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),  \
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),           \
-        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),        \
-        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),        \
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),        \
-        "=r"(r[31])                                                                           \
-      : "r"(taddr))
 
 struct TcArgs {
   int64_t M, N;        // logical output (N = packed B rows, i.e. 2N when complex)
@@ -578,6 +446,7 @@ struct TcArgs {
   double* C;
   int64_t ldc, sC;
   int* status;
+  unsigned long long wait_ns;  // bound on every pipeline wait (drains use DRAIN_WAIT_NS)
 };
 
 __global__ void __launch_bounds__(TC_THREADS, 1)
@@ -625,7 +494,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     for (int it = 0; it < total && ok; ++it) {
       int s = it % TC_STAGES;
       uint32_t round = it / TC_STAGES;
-      ok = mbar_wait_bounded(smem_u32(&empty[s]), (round & 1) ^ 1, args.status);
+      ok = mbar_wait_bounded(smem_u32(&empty[s]), (round & 1) ^ 1, args.status, args.wait_ns);
       if (!ok) break;
       int pair = it / args.kblocks, kb = it % args.kblocks;
       int planeA = (pair == 2) ? 1 : 0, planeB = (pair == 1) ? 1 : 0;
@@ -643,7 +512,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       // drain copies still in flight before this CTA may exit
       for (int it = std::max(0, issued - TC_STAGES); it < issued; ++it) {
         int s = it % TC_STAGES;
-        mbar_wait_bounded(smem_u32(&full[s]), (it / TC_STAGES) & 1, args.status);
+        mbar_wait_bounded(smem_u32(&full[s]), (it / TC_STAGES) & 1, args.status, DRAIN_WAIT_NS);
       }
     }
   } else if (warp == 1 && lane == 0) {
@@ -652,7 +521,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     bool ok = true;
     for (int it = 0; it < total; ++it) {
       int s = it % TC_STAGES;
-      ok = mbar_wait_bounded(smem_u32(&full[s]), (it / TC_STAGES) & 1, args.status);
+      ok = mbar_wait_bounded(smem_u32(&full[s]), (it / TC_STAGES) & 1, args.status, args.wait_ns);
       if (!ok) break;
       tc_fence_after();
       uint32_t sa = smem_u32(smem + s * TC_STAGE_BYTES);
@@ -667,10 +536,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       mma_commit(smem_u32(&empty[s]));
     }
     mma_commit(smem_u32(accum));
+    // every MMA issued by this thread has retired before TMEM is released
+    mbar_wait_bounded(smem_u32(accum), 0, args.status, DRAIN_WAIT_NS);
   } else if (warp >= 2) {
     // ---------------- epilogue: TMEM -> registers -> FP64 global
     const int g = warp % 4;  // TMEM lane quarter accessible by this warp
-    bool ok = mbar_wait_bounded(smem_u32(accum), 0, args.status);
+    bool ok = mbar_wait_bounded(smem_u32(accum), 0, args.status, args.wait_ns);
     tc_fence_after();
     const int64_t m = m0 + 32 * g + lane;
     double* C = args.C + (int64_t)bz * args.sC * (args.cplx ? 2 : 1);
@@ -730,6 +601,7 @@ struct PArgs {
   int64_t mrowsB;
   unsigned int* counter;
   int* status;
+  unsigned long long wait_ns;  // bound on every pipeline wait (drains use DRAIN_WAIT_NS)
   double* work;  // when set: += tensor-pipe flops per split product of every tile
   // optional output map: bit (m / 128) * onc + (logical column / 128) is set for every
   // output tile that receives a contribution; with skip_zero_out, tiles that receive none
@@ -743,9 +615,6 @@ struct PArgs {
 
 constexpr int PS_RING = 4;
 
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
-}
 
 template <int BN>
 struct TileMasks {
@@ -862,7 +731,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
       }
       const int slot = j % PS_RING;
-      ok = mbar_wait_bounded(smem_u32(&sempty[slot]), ((j / PS_RING) & 1) ^ 1, args.status);
+      ok = mbar_wait_bounded(smem_u32(&sempty[slot]), ((j / PS_RING) & 1) ^ 1, args.status, args.wait_ns);
       if (!ok) break;
       stile[slot] = t;
       snk[slot] = nk;
@@ -904,7 +773,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
               break;
             }
             const int s = g % STAGES;
-            ok = mbar_wait_bounded(smem_u32(&empty[s]), ((g / STAGES) & 1) ^ 1, args.status);
+            ok = mbar_wait_bounded(smem_u32(&empty[s]), ((g / STAGES) & 1) ^ 1, args.status, args.wait_ns);
             if (!ok) break;
             const uint32_t sa = smem_u32(smem + s * STAGE_BYTES);
             const uint32_t fb = smem_u32(&full[s]);
@@ -922,7 +791,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       // drain copies still in flight before this CTA may exit
       for (uint32_t it = issued > (uint32_t)STAGES ? issued - STAGES : 0; it < issued; ++it) {
         const int s = it % STAGES;
-        mbar_wait_bounded(smem_u32(&full[s]), (it / STAGES) & 1, args.status);
+        mbar_wait_bounded(smem_u32(&full[s]), (it / STAGES) & 1, args.status, DRAIN_WAIT_NS);
       }
     }
   } else if (warp == 1 && lane == 0) {
@@ -932,21 +801,21 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     bool ok = true;
     for (int j = 0; ok; ++j) {
       const int slot = j % PS_RING;
-      ok = mbar_wait_bounded(smem_u32(&sfull[slot]), (j / PS_RING) & 1, args.status);
+      ok = mbar_wait_bounded(smem_u32(&sfull[slot]), (j / PS_RING) & 1, args.status, args.wait_ns);
       if (!ok) break;
       const int t = stile[slot], nk = snk[slot];
       mbar_arrive(smem_u32(&sempty[slot]));
       if (t < 0) break;
       if (nk == 0) continue;
       const uint32_t buf = acc & 1;
-      ok = mbar_wait_bounded(smem_u32(&tempty[buf]), ((acc >> 1) & 1) ^ 1, args.status);
+      ok = mbar_wait_bounded(smem_u32(&tempty[buf]), ((acc >> 1) & 1) ^ 1, args.status, args.wait_ns);
       if (!ok) break;
       tc_fence_after();
       const uint32_t d = tmem + buf * BN;
       const int total = 3 * nk;
       for (int it = 0; it < total; ++it) {
         const int s = g % STAGES;
-        ok = mbar_wait_bounded(smem_u32(&full[s]), (g / STAGES) & 1, args.status);
+        ok = mbar_wait_bounded(smem_u32(&full[s]), (g / STAGES) & 1, args.status, args.wait_ns);
         if (!ok) break;
         tc_fence_after();
         const uint32_t sa = smem_u32(smem + s * STAGE_BYTES);
@@ -970,14 +839,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
     // every MMA issued by this thread has retired once `done` completes
     mma_commit(smem_u32(done));
-    mbar_wait_bounded(smem_u32(done), 0, args.status);
+    mbar_wait_bounded(smem_u32(done), 0, args.status, DRAIN_WAIT_NS);
   } else if (warp >= 2) {
     // ---------------- epilogue: TMEM -> registers -> FP64 global
     const int q = warp % 4;  // TMEM lane quarter accessible by this warp
     uint32_t acc = 0;
     for (int j = 0;; ++j) {
       const int slot = j % PS_RING;
-      bool ok = mbar_wait_bounded(smem_u32(&sfull[slot]), (j / PS_RING) & 1, args.status);
+      bool ok = mbar_wait_bounded(smem_u32(&sfull[slot]), (j / PS_RING) & 1, args.status, args.wait_ns);
       ok = __all_sync(0xffffffffu, ok);
       const int t = ok ? stile[slot] : -1, nk = ok ? snk[slot] : 0;
       __syncwarp();
@@ -1015,7 +884,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         continue;
       }
       const uint32_t buf = acc & 1;
-      ok = mbar_wait_bounded(smem_u32(&tfull[buf]), (acc >> 1) & 1, args.status);
+      ok = mbar_wait_bounded(smem_u32(&tfull[buf]), (acc >> 1) & 1, args.status, args.wait_ns);
       ok = __all_sync(0xffffffffu, ok);
       if (!ok) break;
       tc_fence_after();
@@ -1085,6 +954,28 @@ static CUtensorMap make_map(const Packed& P, int box_rows) {
   return m;
 }
 
+// map over split planes [planes][rows][kdim] (K-major, 128-byte swizzle), box of one
+// 128-byte K row by box_rows rows; used by the grouped sector-block GEMM
+CUtensorMap make_plane_map(void* data, int esz, int64_t kdim, int64_t rows, int64_t planes,
+                           int box_rows) {
+  load_encode();
+  GB_REQUIRE((kdim * esz) % 128 == 0 && ((uintptr_t)data % 256) == 0,
+             "plane map: K rows must be whole 128-byte lines on an aligned buffer");
+  CUtensorMap m;
+  const cuuint64_t es = (cuuint64_t)esz;
+  cuuint64_t dims[3] = {(cuuint64_t)kdim, (cuuint64_t)rows, (cuuint64_t)planes};
+  cuuint64_t strides[2] = {(cuuint64_t)kdim * es, (cuuint64_t)kdim * rows * es};
+  cuuint32_t box[3] = {(cuuint32_t)(128 / esz), (cuuint32_t)box_rows, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = g_encode(&m, esz == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                     : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16,
+                        3, data, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw Error(GB_ERR_CUDA, "cuTensorMapEncodeTiled failed (plane map)");
+  return m;
+}
+
 bool tc_available(gb_ctx* ctx) {
   int major = 0, minor = 0;
   cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, ctx->device);
@@ -1127,6 +1018,7 @@ void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_
   a.ldc = ldc;
   a.sC = sC;
   a.status = ctx->d_status;
+  a.wait_ns = ctx->wait_ns;
   GB_REQUIRE(M <= (int64_t)INT32_MAX && Npk <= (int64_t)INT32_MAX, "gemm_split: size");
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   if (ctx->profiling) {
@@ -1139,7 +1031,10 @@ void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_
     }
     ev0 = ctx->prof_events[ctx->prof_used++];
     ev1 = ctx->prof_events[ctx->prof_used++];
-    ctx->prof_flops += (A.cplx ? 8.0 : 2.0) * (double)M * (double)N * (double)A.K;
+    const double fl = (A.cplx ? 8.0 : 2.0) * (double)M * (double)N * (double)A.K;
+    ctx->prof_flops += fl;
+    ctx->prof_kind.push_back(0);
+    ctx->prof_kind_flops[0] += fl;
     GB_CHECK_CUDA(cudaEventRecord(ev0, ctx->stream));
   }
   if (outmap) GB_REQUIRE(std::max(A.batch, B.batch) == 1, "gemm_split: output map needs batch 1");
@@ -1179,6 +1074,7 @@ void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_
     p.mrowsB = B.mrows;
     p.counter = ctx->d_tile_counter;
     p.status = ctx->d_status;
+    p.wait_ns = ctx->wait_ns;
     p.work = (ctx->profiling || ctx->counting) ? ctx->d_work : nullptr;
     p.outmap = outmap;
     p.prevmap = nullptr;

@@ -22,6 +22,7 @@
 #include <sstream>
 
 #include "gb_common.h"
+#include "grouped.h"
 
 using gb::cplx;
 using gb::MixDev;
@@ -52,6 +53,15 @@ struct Step {
   // in split precision the mix writes T2 directly as that GEMM's packed B operand
   bool t2_producer = false;
   bool t2_consumer = false;
+  // U(1) labels of the GEMM's index spaces (M, K, N) for the grouped sector-block GEMM:
+  // legs in the order of the dense index (first fastest)
+  std::vector<gb::LegSpec> lM, lK, lN;
+};
+
+// grouped sector-block form of one GEMM step (after gb_heff_set_sectors)
+struct GStep {
+  gb::GPlan plan;
+  gb::GOperand op[2];  // packed original A (side 0) and B (side 1)
 };
 
 struct Cx {
@@ -160,6 +170,19 @@ struct gb_heff {
   void* xfull = nullptr;  // dense staging of the Krylov solvers (zero outside the runs)
   void* yfull = nullptr;
   void* xcomp = nullptr;  // a compact state vector (exponentiate)
+  // grouped sector-block GEMMs (GB_SCHED_GROUPED, split precision, real data): one plan per
+  // GEMM step, the AA-chain mix written straight into the block-stacked T2 operand
+  int sched = 0;                 // GEMM schedule of the context at build time
+  const void* aa_grc = nullptr;  // GR's continuing channels (r', j, r)
+  int64_t aa_chc = 0;
+  std::vector<int32_t> q_l, q_r, q_p1, q_p2, dq_l, dq_r;  // charges (host)
+  std::vector<int2> arange_h;    // host copy of arange
+  std::vector<GStep> gsteps;     // index-aligned with steps
+  gb::GMixEntry* gmix = nullptr;
+  int t2_step = -1;              // the step that consumes T2
+  bool gp_ready = false;
+  bool prepacked = false;        // constants of the dense-embedding path packed
+  int gp_prec = -1;
 };
 
 namespace gb {
@@ -251,6 +274,8 @@ static void prepack(gb_heff* h, Step& s) {
     s.hasPB = true;
   }
 }
+
+static void ensure_prepacked(gb_heff* h);
 
 static void free_steps(gb_heff* h) {
   for (auto& s : h->steps)
@@ -485,6 +510,8 @@ static void build_ac2(gb_heff* h, const gb_tensor* GL, const gb_tensor* W1,
     h->t2N = d1 * d2 * Dr;
     h->aa_glc = glc;
     h->aa_chr = chr;
+    h->aa_grc = grc;
+    h->aa_chc = chc;
     h->aa_Dl = Dl;
     h->aa_Dr = Dr;
     h->aa_np = d1 * d2;
@@ -922,6 +949,8 @@ static void build_ac(gb_heff* h, const gb_tensor* GL, const gb_tensor* W, const 
     h->t2N = d * Dr;
     h->aa_glc = glc;
     h->aa_chr = chr;
+    h->aa_grc = grc;
+    h->aa_chc = chc;
     h->aa_Dl = Dl;
     h->aa_Dr = Dr;
     h->aa_np = d;
@@ -1155,6 +1184,7 @@ gb_heff* heff_build(gb_ctx* ctx, int kind, const gb_tensor* GL, const gb_tensor*
   h->kind = kind;
   h->dtype = GL->dtype;
   h->prec = prec;
+  h->sched = ctx->gemm_schedule;
   try {
     if (kind == GB_HEFF_AC2) {
       GB_REQUIRE(W1 && W2, "AC2 needs W1 and W2");
@@ -1173,8 +1203,12 @@ gb_heff* heff_build(gb_ctx* ctx, int kind, const gb_tensor* GL, const gb_tensor*
     // the FP64 T2 buffer is only needed when T2 is not written packed (split precision)
     if (h->t2_elems && (h->prec == GB_PREC_FP64 || h->kJ.empty()))
       h->t2 = dalloc(h, (size_t)h->t2_elems * es);
-    for (auto& s : h->steps)
-      if (s.is_gemm) prepack(h, s);
+    // with the grouped schedule a real split-precision operator packs its constants when
+    // its sectors arrive (gb_heff_set_sectors); the dense-embedding packing is then only
+    // made if the operator is applied without sectors
+    const bool deferred = h->sched == GB_SCHED_GROUPED && h->prec != GB_PREC_FP64 &&
+                          !is_cplx(h->dtype) && h->kind != GB_HEFF_C;
+    if (!deferred) ensure_prepacked(h);
     GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
   } catch (...) {
     free_steps(h);
@@ -1273,12 +1307,28 @@ void heff_apply_compact(gb_heff* h, const void* x, void* y) {
   runs_copy(h, h->yfull, y, 0);
 }
 
+static void grouped_prepare(gb_heff* h);
+
 void heff_set_sectors(gb_heff* h, const int32_t* ql, const int32_t* qp1, const int32_t* qp2,
                       const int32_t* qr) {
   gb_ctx* ctx = h->ctx;
   const int64_t Dl = h->xdims[0], Dr = h->xdims[2];  // x: (l, s1, r, s2) or (l, s, r)
   for (int64_t i = 1; i < Dl; ++i)
     GB_REQUIRE(ql[i - 1] <= ql[i], "set_sectors: left charges must be sorted ascending");
+  {
+    const bool two = h->kind == GB_HEFF_AC2;
+    h->q_l.assign(ql, ql + Dl);
+    h->q_r.assign(qr, qr + Dr);
+    h->q_p1.assign(qp1, qp1 + h->xdims[1]);
+    if (two) {
+      GB_REQUIRE(qp2, "set_sectors: two physical legs expected");
+      h->q_p2.assign(qp2, qp2 + h->xdims[3]);
+    } else {
+      h->q_p2.clear();
+    }
+    h->dq_l.clear();
+    h->arange_h.clear();
+  }
   // sector table of the (sorted) left charges, indexed by charge - ql[0]
   const int64_t qmin = ql[0], qspan = (int64_t)ql[Dl - 1] - qmin + 1;
   std::vector<int2> sec((size_t)qspan, int2{0, 0});
@@ -1322,7 +1372,10 @@ void heff_set_sectors(gb_heff* h, const int32_t* ql, const int32_t* qp1, const i
     }
     GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
   }
-  if (!h->aa_glc || h->kJ.empty()) return;  // no fused chain: nothing more to restrict
+  if (!h->aa_glc || h->kJ.empty()) {  // no fused chain: nothing more to restrict
+    grouped_prepare(h);
+    return;
+  }
   GB_REQUIRE(h->aa_Dl == Dl && h->aa_Dr == Dr, "set_sectors: bond dimensions");
   const int64_t chr = h->aa_chr;
   // fused physical charges of the mix rows
@@ -1371,6 +1424,245 @@ void heff_set_sectors(gb_heff* h, const int32_t* ql, const int32_t* qp1, const i
                                 cudaMemcpyHostToDevice, ctx->stream));
   GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
   h->arange_max = mx;
+  h->dq_l.assign(dq.begin(), dq.begin() + chr);
+  h->arange_h = std::move(tab);
+  grouped_prepare(h);
+}
+
+// ------------------------------------------------------------------ grouped sector blocks
+// dq[j] = q_r(r) - q_r(r') over the nonzero entries of GR's continuing channel j (layout
+// (r', j, r)); INT_MIN: the channel is zero
+__global__ void channel_charge_grc_kernel(const double* __restrict__ grc, int64_t Dr, int64_t chc,
+                                          const int* __restrict__ qr, int* dq, int* bad) {
+  const int64_t n = Dr * chc * Dr;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    if (grc[i] == 0.0) continue;
+    const int64_t rp = i % Dr, j = (i / Dr) % chc, r = i / (Dr * chc);
+    const int v = qr[r] - qr[rp];
+    int cur = *(volatile int*)&dq[j];
+    if (cur == INT_MIN) {
+      cur = atomicCAS(&dq[j], INT_MIN, v);
+      if (cur == INT_MIN) cur = v;
+    }
+    if (cur != v) atomicExch(bad, 1);
+  }
+}
+
+static gb::LegSpec leg(int64_t n, int which, int sign = 1) {
+  gb::LegSpec l;
+  l.n = n;
+  l.which = which;
+  l.sign = sign;
+  return l;
+}
+
+// charge labels of every GEMM step's M, K and N index (the vector x is allowed where
+// q_l + q_s1 (+ q_s2) = q_r; continuing channels carry the charge they add to the bond);
+// false when a step has no labelling (the grouped form is then not used)
+static bool assign_legs(gb_heff* h) {
+  using namespace gb;
+  const bool two = h->kind == GB_HEFF_AC2;
+  const int64_t Dl = h->xdims[0], d1 = h->xdims[1], Dr = h->xdims[2], d2 = two ? h->xdims[3] : 1;
+  const LegSpec L = leg(Dl, Q_L), R = leg(Dr, Q_R), P1 = leg(d1, Q_P1), P1m = leg(d1, Q_P1, -1),
+                P2 = leg(d2, Q_P2), P2m = leg(d2, Q_P2, -1);
+  const LegSpec CL = leg(h->aa_chr, Q_CL), CRm = leg(h->aa_chc, Q_CR, -1);
+  const std::vector<LegSpec> left = two ? std::vector<LegSpec>{L, P1, P2}
+                                        : std::vector<LegSpec>{L, P1};   // (l s1 s2)
+  const std::vector<LegSpec> right = two ? std::vector<LegSpec>{P1m, P2m, R}
+                                         : std::vector<LegSpec>{P1m, R};  // (s1 s2 r)
+  for (Step& st : h->steps) {
+    if (!st.is_gemm) continue;
+    const std::string& n = st.name;
+    if (n == "AA1" || n == "A1") {  // T1[(l' s'), (c' r)] = X[(l' s'), r'] GRc[r', (c' r)]
+      st.lM = left; st.lK = {R}; st.lN = {CRm, R};
+    } else if (n == "AA3" || n == "A3") {  // Y[l, (s r)] += GLc[l, (l' c)] T2[(l' c), (s r)]
+      st.lM = {L}; st.lK = {L, CL}; st.lN = right;
+    } else if (n == "CA" || n == "C") {  // Y[l, (s r)] += X[l, (s' r')] M[(s' r'), (s r)]
+      st.lM = {L}; st.lK = right; st.lN = right;
+    } else if (n == "AB" || n == "B") {  // Y[(l s), r] += M[(l s), (l' s')] X[(l' s'), r]
+      st.lM = left; st.lK = left; st.lN = {R};
+    } else if (n == "IC") {  // Y[(l s1), (s2 r)] += X[(l s1), (s2' r')] M
+      st.lM = {L, P1}; st.lK = {P2m, R}; st.lN = {P2m, R};
+    } else if (n == "BE") {  // Y[(l s1), (s2 r)] += M[(l s1), (l' s1')] X
+      st.lM = {L, P1}; st.lK = {L, P1}; st.lN = {P2m, R};
+    } else if (n == "II" || n == "I") {  // Y[(l s), r] += X[(l s), r'] GR[r', 0, r]
+      st.lM = left; st.lK = {R}; st.lN = {R};
+    } else if (n == "EE" || n == "E") {  // Y[l, (s r)] += GL[l, l', end] X[l', (s r)]
+      st.lM = {L}; st.lK = {L}; st.lN = right;
+    } else {
+      return false;
+    }
+  }
+  return true;
+}
+
+// Plans, packed constant operands and the mix table of the grouped form.  Every constant
+// operand is checked to lie inside its blocks (nonzero count of the packed blocks equal to
+// that of the dense operand): an operator that does not conserve the given charges is an
+// error, never silently truncated.
+static void grouped_prepare(gb_heff* h) {
+  using namespace gb;
+  gb_ctx* ctx = h->ctx;
+  h->gp_ready = false;
+  if (h->sched != GB_SCHED_GROUPED || h->prec == GB_PREC_FP64 || is_cplx(h->dtype) ||
+      !h->runs || h->kind == GB_HEFF_C)
+    return;
+  if (!assign_legs(h)) return;
+  const bool chain = h->aa_glc && !h->kJ.empty();
+  if (chain) {
+    GB_REQUIRE((int64_t)h->dq_l.size() == h->aa_chr && !h->arange_h.empty(),
+               "grouped: sectors of the fused chain missing");
+    // continuing-channel charges of GR, read off GR itself
+    const int64_t Dr = h->xdims[2], chc = h->aa_chc;
+    int* dev = nullptr;
+    GB_CHECK_CUDA(cudaMallocAsync(&dev, (Dr + chc + 1) * sizeof(int), ctx->stream));
+    std::vector<int> init(chc + 1, INT_MIN);
+    init[chc] = 0;
+    GB_CHECK_CUDA(cudaMemcpyAsync(dev, h->q_r.data(), Dr * sizeof(int), cudaMemcpyHostToDevice,
+                                  ctx->stream));
+    GB_CHECK_CUDA(cudaMemcpyAsync(dev + Dr, init.data(), (chc + 1) * sizeof(int),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    channel_charge_grc_kernel<<<(unsigned)std::min<int64_t>((Dr * chc * Dr + 255) / 256,
+                                                            152 * 16),
+                                256, 0, ctx->stream>>>((const double*)h->aa_grc, Dr, chc, dev,
+                                                       dev + Dr, dev + Dr + chc);
+    GB_CHECK_CUDA(cudaGetLastError());
+    count_launch(ctx);
+    std::vector<int> dq(chc + 1);
+    GB_CHECK_CUDA(cudaMemcpyAsync(dq.data(), dev + Dr, (chc + 1) * sizeof(int),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+    GB_CHECK_CUDA(cudaFreeAsync(dev, ctx->stream));
+    GB_REQUIRE(dq[chc] == 0, "grouped: the right environment does not conserve these charges");
+    h->dq_r.assign(dq.begin(), dq.begin() + chc);
+  }
+  std::vector<const int32_t*> q(Q_COUNT, nullptr);
+  q[Q_L] = h->q_l.data();
+  q[Q_R] = h->q_r.data();
+  q[Q_P1] = h->q_p1.data();
+  q[Q_P2] = h->q_p2.empty() ? nullptr : h->q_p2.data();
+  q[Q_CL] = h->dq_l.empty() ? nullptr : h->dq_l.data();
+  q[Q_CR] = h->dq_r.empty() ? nullptr : h->dq_r.data();
+  auto alloc = [h](size_t b) { return dalloc(h, b); };
+  h->gsteps.assign(h->steps.size(), GStep());
+  h->t2_step = -1;
+  for (size_t i = 0; i < h->steps.size(); ++i) {
+    const Step& st = h->steps[i];
+    if (!st.is_gemm) continue;
+    GB_REQUIRE(st.opA == 'N' && st.opB == 'N', "grouped: transposed operands");
+    const std::vector<int32_t> lM = leg_labels(st.lM, q), lK = leg_labels(st.lK, q),
+                               lN = leg_labels(st.lN, q);
+    GB_REQUIRE((int64_t)lM.size() == st.M && (int64_t)lK.size() == st.K &&
+                   (int64_t)lN.size() == st.N,
+               "grouped: labels do not match the GEMM shape of step " + st.name);
+    GStep& gs = h->gsteps[i];
+    gplan_build(gs.plan, lM, lK, lN, !st.accumulate, st.ldc);
+    gplan_upload(ctx, gs.plan, alloc);
+    for (int sd = 0; sd < 2; ++sd)
+      goperand_init(ctx, gs.op[sd], gs.plan, sd, dalloc(h, goperand_bytes(gs.plan, sd, h->prec)),
+                    h->prec);
+    // constants: original A(m, k) at m + lda k, original B(k, n) at k + ldb n.  A nonzero
+    // whose row and column labels differ would be dropped by the blocks: refuse it (entries
+    // of a conserved label that has no group on the other side of the GEMM meet only zeros
+    // of x and are dropped rightly)
+    if (st.srcA == S_CONST) {
+      GB_REQUIRE(label_violations(ctx, (const double*)st.cA, st.M, st.K, 1, st.lda, lM, lK) == 0,
+                 "grouped: operator term " + st.name + " does not conserve the given charges");
+      gpack(ctx, gs.plan, 0, (const double*)st.cA, 1, st.lda, gs.op[0]);
+    }
+    if (st.srcB == S_CONST) {
+      GB_REQUIRE(label_violations(ctx, (const double*)st.cB, st.N, st.K, st.ldb, 1, lN, lK) == 0,
+                 "grouped: operator term " + st.name + " does not conserve the given charges");
+      gpack(ctx, gs.plan, 1, (const double*)st.cB, st.ldb, 1, gs.op[1]);
+    }
+    if (st.t2_consumer) {
+      GB_REQUIRE(st.srcB == S_T2, "grouped: T2 is the B operand of its consumer");
+      h->t2_step = (int)i;
+    }
+  }
+  if (chain) {
+    GB_REQUIRE(h->t2_step >= 0, "grouped: the fused chain has no consumer");
+    const GPlan& P = h->gsteps[h->t2_step].plan;
+    // packed row of every dense N index, position of every dense K index within its group
+    std::vector<int32_t> posN(h->t2N, -1), kpos(h->t2K, -1), ngrp(h->t2N, -1), kgrp(h->t2K, -1);
+    for (int g = 0; g < P.G; ++g) {
+      for (int32_t r = P.side[1].gstart[g]; r < P.side[1].gstart[g + 1]; ++r) {
+        posN[P.side[1].dense[r]] = r;
+        ngrp[P.side[1].dense[r]] = g;
+      }
+      for (int32_t k = P.kstart[g]; k < P.kstart[g + 1]; ++k) {
+        kpos[P.kdense[k]] = k - P.kstart[g];
+        kgrp[P.kdense[k]] = g;
+      }
+    }
+    const int64_t nJ = (int64_t)h->kJ.size(), Dr = h->xdims[2];
+    std::vector<GMixEntry> ent((size_t)nJ * Dr);
+    for (int64_t n = 0; n < Dr; ++n)
+      for (int64_t J = 0; J < nJ; ++J) {
+        const int2 ar = h->arange_h[(size_t)n * nJ + J];
+        GMixEntry e{ar.x, ar.y, -1, 0};
+        if (ar.y > ar.x) {
+          const int64_t m = h->mJ[J] + n * h->mn;
+          const int64_t k0 = ar.x + h->kJ[J], k1 = ar.y - 1 + h->kJ[J];
+          // a row or contraction index outside every block of the consumer meets only
+          // zeros there (its charge has no partner on the other side): nothing to write
+          if (posN[m] >= 0 && kpos[k0] >= 0) {
+            e.row = posN[m];
+            e.kst = kpos[k0];
+            GB_REQUIRE(ngrp[m] == kgrp[k0] && kgrp[k1] == kgrp[k0] &&
+                           kpos[k1] == e.kst + (ar.y - 1 - ar.x),
+                       "grouped: the fused chain's sectors do not match its consumer's blocks");
+          }
+        }
+        ent[(size_t)n * nJ + J] = e;
+      }
+    h->gmix = (GMixEntry*)dalloc(h, ent.size() * sizeof(GMixEntry));
+    GB_CHECK_CUDA(cudaMemcpyAsync(h->gmix, ent.data(), ent.size() * sizeof(GMixEntry),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    // T1 is read only inside its blocks; the entries no block writes stay zero
+    GB_REQUIRE(h->t1, "grouped: T1 buffer missing");
+    GB_CHECK_CUDA(cudaMemsetAsync(h->t1, 0, (size_t)h->t1_elems * elem_size(h->dtype),
+                                  ctx->stream));
+    GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  h->gp_prec = h->prec;
+  h->gp_ready = true;
+}
+
+// y = H x through the grouped plans.  x: dense embedding, zero outside the sectors; every
+// allowed entry of y is written (the first GEMM into y overwrites, the rest accumulate);
+// entries outside the sectors are zeroed only when y is not the operator's own staging
+// vector (whose outside entries are never read).
+static void heff_apply_grouped(gb_heff* h, const void* x, void* y) {
+  using namespace gb;
+  gb_ctx* ctx = h->ctx;
+  if (h->y_zero_first || y != h->yfull) fill_zero(ctx, y, (size_t)h->xnumel * elem_size(h->dtype));
+  for (size_t i = 0; i < h->steps.size(); ++i) {
+    const Step& st = h->steps[i];
+    if (st.is_gemm) {
+      GStep& gs = h->gsteps[i];
+      if (st.srcA == S_X) gpack(ctx, gs.plan, 0, (const double*)x, 1, st.lda, gs.op[0]);
+      if (st.srcB == S_X) gpack(ctx, gs.plan, 1, (const double*)x, st.ldb, 1, gs.op[1]);
+      const bool t1 = st.dst == S_T1;
+      gemm_grouped(ctx, gs.plan, gs.op[0], gs.op[1], 1.0, st.accumulate ? 1.0 : 0.0,
+                   t1 ? h->t1 : y, t1);
+      if (ctx->counting) gcount_products(ctx, gs.plan, gs.op[0], gs.op[1]);
+    } else if (st.t2_producer) {
+      gmix_run(ctx, st.mix, h->gmix, h->arange_max, (const float*)h->t1,
+               h->gsteps[h->t2_step].op[1]);
+    } else {
+      GB_REQUIRE(st.src == S_X && st.dst == S_Y, "grouped: unexpected mix step");
+      mix_run(ctx, st.mix, h->dtype, x, y, st.accumulate ? 1.0 : 0.0);
+    }
+  }
+}
+
+static void ensure_prepacked(gb_heff* h) {
+  if (h->prepacked) return;
+  for (auto& st : h->steps)
+    if (st.is_gemm) prepack(h, st);
+  h->prepacked = true;
 }
 
 void heff_set_precision(gb_heff* h, int prec) {
@@ -1381,15 +1673,22 @@ void heff_set_precision(gb_heff* h, int prec) {
     // buffers stay owned by the operator until it is freed)
     for (auto& s : h->steps) s.hasPA = s.hasPB = false;
     h->t2p_ready = false;
+    h->prepacked = false;
+    h->prec = prec;
+    if (h->runs) grouped_prepare(h);  // the grouped form follows the plane type too
   }
   h->prec = prec;
-  for (auto& s : h->steps)
-    if (s.is_gemm) prepack(h, s);
+  if (!h->gp_ready) ensure_prepacked(h);
 }
 
 // y = H x (device pointers, device layout)
 void heff_apply_raw(gb_heff* h, const void* x, void* y) {
   gb_ctx* ctx = h->ctx;
+  if (h->gp_ready && h->gp_prec == h->prec) {
+    heff_apply_grouped(h, x, y);
+    return;
+  }
+  ensure_prepacked(h);
   if (h->y_zero_first) fill_zero(ctx, y, (size_t)h->xnumel * elem_size(h->dtype));
   auto ptr = [&](int src, const void* c) -> const void* {
     switch (src) {

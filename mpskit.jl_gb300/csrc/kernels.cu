@@ -397,7 +397,10 @@ void gemm_fp64(gb_ctx* ctx, int dtype, char opA, char opB, int64_t M, int64_t N,
   const int kw = (int)((K + 64 * 32 - 1) / (64 * 32));
   const int64_t mt = grid.x, nt = grid.y;
   const int64_t bA = sA ? batch : 1, bB = sB ? batch : 1;
-  const bool skip = ctx->gemm_schedule == GB_SCHED_PERSISTENT &&
+  // (the grouped schedule only changes split-precision operators with known sectors: the
+  // FP64 GEMM keeps its block skipping under it)
+  const bool skip = (ctx->gemm_schedule == GB_SCHED_PERSISTENT ||
+                     ctx->gemm_schedule == GB_SCHED_GROUPED) &&
                     (double)M * (double)N * (double)K >= 1.3e8 && (K + 63) / 64 <= 65535;
   if (skip) {
     const size_t words = (size_t)(bA * mt + bB * nt) * kw;

@@ -150,7 +150,8 @@ int heff_eigsolve_raw(gb_ctx* ctx, gb_heff* h, int64_t n_dense, int dtype, void*
   auto vec = [&](int j) { return (void*)(V + (size_t)j * n * es); };
   sp.load(ctx, dtype, x, vec(0));
   double nx = nrm2(ctx, dtype, n, vec(0));
-  GB_REQUIRE(nx > 0 && std::isfinite(nx), "eigsolve: initial vector has zero or non-finite norm");
+  if (!std::isfinite(nx)) throw Error(GB_ERR_NAN, "eigsolve: initial vector is not finite");
+  GB_REQUIRE(nx > 0, "eigsolve: initial vector has zero norm");
   scale(ctx, dtype, n, cplx{1.0 / nx, 0}, vec(0));
   const int howmany = 1;
   std::vector<double> H((size_t)(kd + 1) * (kd + 1), 0.0);  // row-major, stride kd+1
@@ -176,7 +177,8 @@ int heff_eigsolve_raw(gb_ctx* ctx, gb_heff* h, int64_t n_dense, int dtype, void*
     }
     ++K;
     beta = nrm2(ctx, dtype, n, w);
-    GB_REQUIRE(std::isfinite(beta), "eigsolve: non-finite residual (NaN in operator or vector)");
+    if (!std::isfinite(beta))
+      throw Error(GB_ERR_NAN, "eigsolve: non-finite residual (NaN or Inf in the operator)");
     if (K == kd || beta <= tol || (eager && K >= howmany)) {
       std::vector<double> Hk((size_t)K * K);
       for (int i = 0; i < K; ++i)

@@ -16,7 +16,10 @@
 //   * calls that overlap on the GPU (two streams, or two threads) race on the array;
 //   * the first call on a device looks up the array's device address
 //     (cudaGetSymbolAddress) with that device current -- make that first call before
-//     any stream capture begins.
+//     any stream capture begins;
+//   * the address is cached for the life of the process; cudaDeviceReset unloads the
+//     module and its array, so after a reset of a device this entry point must not be
+//     called on that device again in the same process.
 #include <cuda_runtime.h>
 
 #include <mutex>

@@ -500,6 +500,26 @@ void u1_svd_trunc(gb_ctx* ctx, const gb_tensor* AC2, const int32_t* ql, const in
     if (v.s > atol) ++keep;
   if (maxdim > 0) keep = std::min(keep, maxdim);
   keep = std::max<int64_t>(keep, 1);
+  if (gram) {
+    // Gram singular values carry an absolute error of about eps_mach * s_max^2 / s with
+    // s_max the largest value of their own block: below 1e-7 s_max they are rounding noise.
+    // When a kept value or the first discarded one is that small, the rank and the discarded
+    // weight cannot be read off them: factorise every block by its SVD instead.
+    auto resolved = [&](const SV& v) { return v.s >= 1e-7 * hs[fs[v.c].oS]; };
+    if (!resolved(all[keep - 1]) || (keep < (int64_t)all.size() && !resolved(all[keep]))) {
+      const int saved = ctx->svd_method;
+      ctx->svd_method = GB_SVD_GESVD;
+      try {
+        u1_svd_trunc(ctx, AC2, ql, qs1, qs2, qr, maxdim, atol, normalize, AL, S, AR, qk, kout,
+                     eps);
+      } catch (...) {
+        ctx->svd_method = saved;
+        throw;
+      }
+      ctx->svd_method = saved;
+      return;
+    }
+  }
   double e2 = 0.0;
   for (size_t i = keep; i < all.size(); ++i) e2 += all[i].s * all[i].s;
   if (eps) *eps = std::sqrt(e2);

@@ -40,6 +40,7 @@ PRECISIONS = {"fp64": GB_PREC_FP64, "bf16x3": GB_PREC_BF16X3, "tf32x3": GB_PREC_
 GB_SCHED_PERSISTENT = 0
 GB_SCHED_PERSISTENT_DENSE = 1
 GB_SCHED_TILE = 2
+GB_SCHED_GROUPED = 3
 
 
 class KrylovInfo(ctypes.Structure):
@@ -72,6 +73,7 @@ _SIGS = {
     "gb_ctx_synchronize": ([P], INT),
     "gb_ctx_kernel_launches": ([P, PI64], INT),
     "gb_ctx_device_status": ([P, ctypes.POINTER(ctypes.c_int32)], INT),
+    "gb_ctx_set_wait_bound": ([P, D], INT),
     "gb_ctx_set_precision": ([P, INT], INT),
     "gb_ctx_profile_begin": ([P], INT),
     "gb_ctx_set_svd_method": ([P, INT], INT),
@@ -79,6 +81,7 @@ _SIGS = {
     "gb_ctx_set_counting": ([P, INT], INT),
     "gb_ctx_read_work": ([P, PD, PD, INT], INT),
     "gb_ctx_profile_end": ([P, PD, PI64, PD, PD], INT),
+    "gb_ctx_profile_kernel": ([P, INT, PD, PI64, PD], INT),
     "gb_ctx_trace_begin": ([P], INT),
     "gb_ctx_trace_end": ([P, PI64, PD], INT),
     "gb_ctx_trace_site": ([P, ctypes.c_int64, ctypes.c_char_p, SZ, PD, PI64], INT),

@@ -7,7 +7,8 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(ROOT, "csrc")
 BUILD = os.path.join(ROOT, "_build")
-SOURCES = ["kernels.cu", "gemm_tc.cu", "heff.cu", "krylov.cu", "api.cu", "u1.cu", "noalloc.cu"]
+SOURCES = ["kernels.cu", "gemm_tc.cu", "grouped.cu", "heff.cu", "krylov.cu", "api.cu", "u1.cu",
+           "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

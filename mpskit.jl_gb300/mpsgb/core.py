@@ -39,13 +39,20 @@ class Context:
         code = L.PRECISIONS[precision]
         L.check(L.lib().gb_ctx_set_precision(self.handle, code))
 
-    def set_gemm_schedule(self, schedule="persistent", tile_n=0):
-        """Split-precision GEMM schedule: "persistent" (tile-skipping, default),
-        "persistent_dense" or "tile"; tile_n in (0 = per shape, 128, 256)."""
+    def set_gemm_schedule(self, schedule="grouped", tile_n=0):
+        """Split-precision GEMM schedule: "grouped" (the default: operators with known U(1)
+        sectors run one launch over their charge blocks; other GEMMs as "persistent"),
+        "persistent" (tile skipping over the dense embedding), "persistent_dense" or "tile";
+        tile_n in (0 = per shape, 128, 256).  Read when an operator is built."""
         code = {"persistent": L.GB_SCHED_PERSISTENT,
                 "persistent_dense": L.GB_SCHED_PERSISTENT_DENSE,
-                "tile": L.GB_SCHED_TILE}[schedule]
+                "tile": L.GB_SCHED_TILE,
+                "grouped": L.GB_SCHED_GROUPED}[schedule]
         L.check(L.lib().gb_ctx_set_gemm_schedule(self.handle, code, int(tile_n)))
+
+    def set_wait_bound(self, seconds=2.0):
+        """Bound on every pipeline wait of the tensor-core kernels (gb_ctx_set_wait_bound)."""
+        L.check(L.lib().gb_ctx_set_wait_bound(self.handle, float(seconds)))
 
     def set_counting(self, on=True):
         """Count the nonzero products of every split GEMM (block-sparse flop accounting)."""
@@ -72,8 +79,14 @@ class Context:
         n = ctypes.c_int64()
         L.check(L.lib().gb_ctx_profile_end(self.handle, ctypes.byref(ms), ctypes.byref(n),
                                            ctypes.byref(fl), ctypes.byref(rms)))
-        return {"gemm_ms": ms.value, "gemm_launches": n.value, "gemm_flops": fl.value,
-                "region_ms": rms.value}
+        out = {"gemm_ms": ms.value, "gemm_launches": n.value, "gemm_flops": fl.value,
+               "region_ms": rms.value}
+        for name, code in (("persistent", 0), ("grouped", 1)):
+            kms, kfl, kn = ctypes.c_double(), ctypes.c_double(), ctypes.c_int64()
+            L.check(L.lib().gb_ctx_profile_kernel(self.handle, code, ctypes.byref(kms),
+                                                  ctypes.byref(kn), ctypes.byref(kfl)))
+            out[name] = {"ms": kms.value, "launches": kn.value, "flops": kfl.value}
+        return out
 
     def trace_begin(self):
         """Start a launch trace of this context's stream (gb_ctx_trace_begin)."""
@@ -95,6 +108,8 @@ class Context:
         return tot.value, out
 
     def device_status(self):
+        """Status word of the bounded device waits (0 = clean; GB_ERR_TIMEOUT after a wait
+        ran out); cleared on read."""
         v = ctypes.c_int32()
         L.check(L.lib().gb_ctx_device_status(self.handle, ctypes.byref(v)))
         return v.value

@@ -235,10 +235,13 @@ class FiniteEnvironments:
     """Lazy GL/GR cache.  With `resident=False` only the most recently computed
     environment of each side stays in HBM (older ones are released and recomputed from
     the boundary when asked for again) -- the memory policy for large D x w, where all
-    L environments do not fit on one device."""
+    L environments do not fit on one device.  `keep_left` / `keep_right`: sites whose
+    environments are never released (e.g. the right environments of a window of bonds a
+    sweep is about to visit)."""
 
-    def __init__(self, psi, H, ctx=None, resident=True):
+    def __init__(self, psi, H, ctx=None, resident=True, keep_left=(), keep_right=()):
         self.resident = resident
+        self.keep_left, self.keep_right = set(keep_left), set(keep_right)
         self.ctx = ctx or psi.ctx
         self.H = H
         n = len(psi)
@@ -272,7 +275,7 @@ class FiniteEnvironments:
                                                  self.precision, out.handle))
             self.GL[j + 1] = out
             self.ldep[j] = A
-            if not self.resident and j >= 1:
+            if not self.resident and j >= 1 and j not in self.keep_left:
                 self.GL[j] = None
         return self.GL[i]
 
@@ -294,6 +297,6 @@ class FiniteEnvironments:
                                                   self.precision, out.handle))
             self.GR[j - 1] = out
             self.rdep[j] = A
-            if not self.resident and j <= n - 2:
+            if not self.resident and j <= n - 2 and j not in self.keep_right:
                 self.GR[j] = None
         return self.GR[i]

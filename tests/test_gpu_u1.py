@@ -18,7 +18,7 @@ pytestmark = pytest.mark.gpu
 def ctx():
     c = mpsgb.context(0)
     yield c
-    c.set_gemm_schedule("persistent", 0)
+    c.set_gemm_schedule("grouped", 0)
     c.set_svd_method("gesvd")
 
 
@@ -106,11 +106,11 @@ def test_tile_skipping_equals_dense_schedule_on_u1_operator(ctx, prec, tol):
     ac2 = mpsgb.ac2_from(psi.AL[5], psi.ac(6))
     outs = {}
     for sched, bn in (("persistent", 0), ("persistent_dense", 0), ("persistent", 128),
-                      ("tile", 0)):
+                      ("tile", 0), ("grouped", 0)):
         ctx.set_gemm_schedule(sched, bn)
         Heff = mpsgb.AC2_hamiltonian(5, psi, H, envs, be)
         outs[(sched, bn)] = Heff(ac2).numpy()
-    ctx.set_gemm_schedule("persistent", 0)
+    ctx.set_gemm_schedule("grouped", 0)
     ref = mpsgb.AC2_hamiltonian(5, psi, H, envs, mpsgb.GB300Backend("fp64"))(ac2).numpy()
     assert np.array_equal(outs[("persistent", 0)], outs[("persistent_dense", 0)])
     for v in outs.values():
@@ -170,6 +170,14 @@ def test_sector_restricted_chain_is_exact(ctx, prec):
     psi = mpsgb.FiniteMPS.from_tensors(As, ctx, center=pos + 1, charges=(qb, QP))
     envs = mpsgb.FiniteEnvironments(psi, H)
     be = mpsgb.GB300Backend(prec)
+    ctx.set_gemm_schedule("persistent", 0)  # the restricted chain of the dense-embedding path
+    try:
+        _restricted_chain_checks(ctx, psi, H, envs, be, pos)
+    finally:
+        ctx.set_gemm_schedule("grouped", 0)
+
+
+def _restricted_chain_checks(ctx, psi, H, envs, be, pos):
     ac2 = mpsgb.ac2_from(psi.AL[pos], psi.ac(pos + 1))
     plain = ac2.copy()
     plain.charges = None  # the same vector without its leg charges: no sectors
@@ -225,3 +233,91 @@ def test_compact_krylov_matches_dense_solves(ctx):
     ys = mpsgb.integrate(Hs, ac2, 0.0, 0.1, mpsgb.Lanczos(tol=1e-12)).numpy()
     yd = mpsgb.integrate(Hd, plain, 0.0, 0.1, mpsgb.Lanczos(tol=1e-12)).numpy()
     assert np.linalg.norm(ys - yd) < 1e-10 * np.linalg.norm(yd)
+
+
+def _grouped_vs_fp64(ctx, psi, H, envs, pos, prec, tol, two_site=True):
+    """One operator on the grouped schedule (default) and on the dense-embedding schedule,
+    against the FP64 operator: two applications each."""
+    be = mpsgb.GB300Backend(prec)
+    if two_site:
+        x = mpsgb.ac2_from(psi.AL[pos], psi.ac(pos + 1))
+        make = lambda b: mpsgb.AC2_hamiltonian(pos, psi, H, envs, b)
+    else:
+        x = psi.ac(pos)
+        make = lambda b: mpsgb.AC_hamiltonian(pos, psi, H, envs, b)
+    ref = make(mpsgb.GB300Backend("fp64"))(x).numpy()
+    ctx.set_gemm_schedule("grouped", 0)
+    Hg = make(be)
+    yg = [Hg(x).numpy() for _ in range(2)]
+    ctx.set_gemm_schedule("persistent", 0)
+    try:
+        yp = make(be)(x).numpy()
+    finally:
+        ctx.set_gemm_schedule("grouped", 0)
+    nref = np.linalg.norm(ref)
+    for y in yg + [yp]:
+        assert np.linalg.norm(y - ref) < tol * nref, (prec, np.linalg.norm(y - ref) / nref)
+    # the same result on every call (operands repacked, the mix output reused)
+    assert np.array_equal(yg[0], yg[1])
+    # exact zeros outside the charge blocks
+    assert np.all(yg[0][ref == 0] == 0)
+    return Hg
+
+
+@pytest.mark.parametrize("prec,tol", [("bf16x3", 1e-4), ("tf32x3", 4e-6)])
+@pytest.mark.parametrize("model", ["j1j2", "heisenberg"])
+def test_grouped_sector_gemm_matches_fp64(ctx, prec, tol, model):
+    """The grouped sector-block GEMMs (one launch per contraction over its charge blocks,
+    block-stacked operands, per-block tile widths): two-site and one-site operators of a
+    long-range (AA, CA, AB terms) and a nearest-neighbour (IC, BE terms) U(1) model agree
+    with the FP64 operator within the split-precision tolerance."""
+    L_, pos = 12, 5
+    if model == "j1j2":
+        H = mpsgb.j1j2_cylinder(4, 3, u1=True)
+        D = 96
+    else:
+        H = mpsgb.heisenberg_XXX(L_, dtype=np.float64, u1=True)
+        D = 160
+    As, qb = HU.random_u1_tensors(L_, D, 31, 0, np.float64)
+    psi = mpsgb.FiniteMPS.from_tensors(As, ctx, center=pos + 1, charges=(qb, QP))
+    envs = mpsgb.FiniteEnvironments(psi, H)
+    Hg = _grouped_vs_fp64(ctx, psi, H, envs, pos, prec, tol, two_site=True)
+    if model == "j1j2":
+        assert "AA" in Hg.terms
+    else:
+        assert "IC" in Hg.terms and "BE" in Hg.terms
+    _grouped_vs_fp64(ctx, psi, H, envs, pos + 1, prec, tol, two_site=False)
+
+
+def test_grouped_counts_the_same_nonzero_products(ctx):
+    """Counting mode: the grouped GEMMs report the same block-sparse product count as the
+    dense-embedding GEMMs, and execute far fewer tile products."""
+    L_, pos = 12, 5
+    H = mpsgb.j1j2_cylinder(4, 3, u1=True)
+    As, qb = HU.random_u1_tensors(L_, 128, 37, 0, np.float64)
+    psi = mpsgb.FiniteMPS.from_tensors(As, ctx, center=pos + 1, charges=(qb, QP))
+    envs = mpsgb.FiniteEnvironments(psi, H)
+    x = mpsgb.ac2_from(psi.AL[pos], psi.ac(pos + 1))
+    be = mpsgb.GB300Backend("bf16x3")
+    work = {}
+    try:
+        for sched in ("grouped", "persistent"):
+            ctx.set_gemm_schedule(sched, 0)
+            # counting on before the build: the dense-embedding path counts its constant
+            # operands when it packs them
+            ctx.set_counting(True)
+            Heff = mpsgb.AC2_hamiltonian(pos, psi, H, envs, be)
+            Heff.set_sectors(x)
+            ctx.synchronize()
+            ctx.read_work(reset=True)
+            Heff(x)
+            ctx.synchronize()
+            ctx.set_counting(False)
+            work[sched] = ctx.read_work(reset=True)
+    finally:
+        ctx.set_counting(False)
+        ctx.set_gemm_schedule("grouped", 0)
+    g, p = work["grouped"], work["persistent"]
+    assert g["nonzero_flops"] > 0
+    assert abs(g["nonzero_flops"] - p["nonzero_flops"]) <= 1e-9 * p["nonzero_flops"]
+    assert g["tile_flops"] < p["tile_flops"]
