@@ -799,7 +799,8 @@ struct LanePool {
   }
 };
 
-void run_on_lanes(gb_ctx* ctx, int64_t n, const std::function<void(gb_ctx*, int64_t)>& fn) {
+void run_on_lanes_at(gb_ctx* ctx, int64_t n, const char* file, int line,
+                     const std::function<void(gb_ctx*, int64_t)>& fn) {
   const int K = (int)std::min<int64_t>(n, 8);
   if (K <= 1) {
     for (int64_t i = 0; i < n; ++i) fn(ctx, i);
@@ -844,7 +845,8 @@ void run_on_lanes(gb_ctx* ctx, int64_t n, const std::function<void(gb_ctx*, int6
       if (!err) err = std::current_exception();
     }
   });
-  GB_TRACE(ctx);  // marks the end of the lanes' work on the (idle) main stream
+  // marks the end of the lanes' work on the (idle) main stream, charged to the caller
+  if (ctx->tracing) trace_point(ctx, file, line);
   for (int k = 0; k < K; ++k) ctx->launches += ctx->lanes[k]->launches - before[k];
   if (err) std::rethrow_exception(err);
 }

@@ -145,7 +145,11 @@ void* scratch(gb_ctx* ctx, int slot, size_t bytes);
 // fn(lane, i) for i < n on up to 8 lane contexts, one host thread per lane: the parent's
 // stream is synchronised first, every lane's stream at the end; the first exception thrown
 // by any item is rethrown after all lanes stopped
-void run_on_lanes(gb_ctx* ctx, int64_t n, const std::function<void(gb_ctx*, int64_t)>& fn);
+// (run_on_lanes: the launch trace charges the lanes' work to the calling source line)
+void run_on_lanes_at(gb_ctx* ctx, int64_t n, const char* file, int line,
+                     const std::function<void(gb_ctx*, int64_t)>& fn);
+#define run_on_lanes(ctx, n, ...) \
+  ::gb::run_on_lanes_at((ctx), (n), __FILE__, __LINE__, __VA_ARGS__)
 // U(1) operators (after gb_heff_set_sectors): the Krylov solvers keep only the n allowed
 // entries of their vectors; xcomp is an operator-owned compact vector
 struct HeffCompact {

@@ -545,6 +545,7 @@ void u1_svd_trunc(gb_ctx* ctx, const gb_tensor* AC2, const int32_t* ql, const in
     for (int64_t i = 0; i < kc[c]; ++i) qk[ko + i] = ss[c].q;
     ko += kc[c];
   }
+  GB_TRACE(ctx);  // host-side truncation and output set-up end here
   run_on_lanes(ctx, (int64_t)kept.size(), [&](gb_ctx* L, int64_t idx) {
     const size_t c = (size_t)kept[idx];
     const Fac& f = fs[c];
