@@ -86,6 +86,8 @@ def parse():
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the split-vs-FP64 eigensolve comparison at the bench bond")
     ap.add_argument("--sweeps", type=int, default=1, help="sweeps of --workload dmrg2-sweep")
+    ap.add_argument("--describe", action="store_true",
+                    help="--workload matvec: print the operator's contraction steps and plans")
     ap.add_argument("--checkpoint", type=int, default=12,
                     help="dmrg2-sweep: environments kept resident every this many sites")
     ap.add_argument("--ref-budget", type=float, default=90.0,
@@ -748,6 +750,8 @@ def run_matvec(args):
     for _ in range(max(args.warmup, 1)):
         Heff(x, out=y)
     ctx.synchronize()
+    if args.describe:
+        log("operator steps:\n" + Heff.describe())
     ctx.profile_begin()
     for _ in range(args.steps):
         Heff(x, out=y)

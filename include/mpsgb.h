@@ -57,7 +57,7 @@ enum {
 };
 
 /* derivative-operator kinds */
-enum { GB_HEFF_C = 0, GB_HEFF_AC = 1, GB_HEFF_AC2 = 2 };
+enum { GB_HEFF_C = 0, GB_HEFF_AC = 1, GB_HEFF_AC2 = 2, GB_HEFF_AC_MPO = 3, GB_HEFF_AC2_MPO = 4 };
 
 /* arithmetic of the bulk contractions */
 enum {
@@ -192,12 +192,20 @@ int gb_tensor_norm(const gb_tensor* x, double* out);
  *                (hamiltonian_derivatives.jl:44-157);  W2 must be NULL
  *   GB_HEFF_C  : MPO_C_Hamiltonian(GL, GR)  (src/algorithms/derivatives/mpo_derivatives.jl:37-45,
  *                92-98, 216-219);  W1 and W2 must be NULL
+ *   GB_HEFF_AC_MPO / GB_HEFF_AC2_MPO : MPO_AC_Hamiltonian(GL, W, GR) / MPO_AC2_Hamiltonian(GL,
+ *                W1, W2, GR) of an arbitrary MPO, no Jordan structure assumed
+ *                (mpo_derivatives.jl:46-66, 100-107, 144-153): every channel pair is
+ *                contracted; the operator then behaves as GB_HEFF_AC / GB_HEFF_AC2 (vector
+ *                kinds, sectors, solvers) and gb_heff_terms reports "A" / "AA"
  * GL/GR must be GB_KIND_GL/GB_KIND_GR tensors, W* GB_KIND_MPO. */
 int gb_heff_build(gb_ctx* ctx, int kind, const gb_tensor* GL, const gb_tensor* W1,
                   const gb_tensor* W2, const gb_tensor* GR, int precision, gb_heff** out);
 int gb_heff_free(gb_heff* h);
 /* comma-separated list of the terms left after prepare, e.g. "IC,BE" */
 int gb_heff_terms(const gb_heff* h, char* buf, size_t len);
+/* one text line per contraction step of the prepared operator (GEMM shapes; for a grouped
+ * sector-block GEMM its groups, tiles and K-blocks), for tuning and diagnostics */
+int gb_heff_describe(const gb_heff* h, char* buf, size_t len);
 /* algorithmic flops of one application (unsplit shapes; 2 flops/real MAC, 8/complex MAC) */
 int gb_heff_flops(const gb_heff* h, double* flops);
 int gb_heff_set_precision(gb_heff* h, int precision);
@@ -270,7 +278,37 @@ int gb_mps_transfer_bond(gb_ctx* ctx, int side, const gb_tensor* A, const gb_ten
                          const gb_tensor* X, gb_tensor* out);
 /* Y <- (1 - X X') Y on the first two legs of Y (project_complement!, src/utility/utility.jl:22) */
 int gb_project_complement(gb_ctx* ctx, gb_tensor* Y, const gb_tensor* X);
+/* Y <- Y (1 - X' X) on the last two legs of Y, X an MPS tensor with orthonormal rows
+ * (k x (s r)), e.g. a right-isometric AR: with gb_project_complement this gives
+ * NL NL' Y NR' NR, the two-site update projected onto the complements of both sites
+ * (left_null / right_null! of changebond!(::OptimalExpand),
+ * src/algorithms/changebonds/optimalexpand.jl:122-135, 148-161) without forming the null
+ * spaces: the right singular vectors of the projected Y are Vh * NR. */
+int gb_project_complement_right(gb_ctx* ctx, gb_tensor* Y, const gb_tensor* X);
 /* contract_mpo_expval-style scalar <x|y> after a heff apply is gb_tensor_dot. */
+
+/* ---------------------------------------------------------------- bond expansion */
+/* The DMRG3S perturbation MPO_AC_Hamiltonian(env, W, combiner) * AC
+ * (src/algorithms/post_expand/dmrg3s.jl:133-192), the combiner fusing the bond with the MPO
+ * channel (bond index fastest):
+ *   side 0 (env = GL of the site): out[l s; (r w)]  = GL[l w'; l'] AC[l' s'; r] W[w' s; s' w],
+ *                                  out dims (Dl_bra, d, Dr * wr)
+ *   side 1 (env = GR of the site): out[(l w) s; r]  = W[w s; s' w'] AC[l s'; r'] GR[r' w'; r],
+ *                                  out dims (Dl * wl, d, Dr_bra)
+ * `out` is caller-created (GB_KIND_MPS); precision as for the transfers. */
+int gb_mps_perturb(gb_ctx* ctx, int side, const gb_tensor* env, const gb_tensor* W,
+                   const gb_tensor* AC, int precision, gb_tensor* out);
+/* out = A (+) B along one virtual leg of MPS tensors (catdomain / catcodomain on the right
+ * (leg 2) or left (leg 0) bond, dmrg3s.jl:148-156, optimalexpand.jl:138-142); B = NULL
+ * appends zeros (zeros(T, Vpert <- domain(B)), dmrg3s.jl:153).  The other legs must agree;
+ * out (caller-created) has the summed dimension. */
+int gb_mps_cat(gb_ctx* ctx, const gb_tensor* A, const gb_tensor* B, int leg, gb_tensor* out);
+/* Relabel the kind and shape of an MPS, two-site, bond or generic tensor without moving
+ * data: the new shape reads the same device storage in its own device order (MPS (l, s, r),
+ * two-site (l, s1, s2, r), bond (l, r)).  E.g. an MPS tensor (l, s, r) is the two-site tensor
+ * (Dl, d, Dr, 1) or (Dl, 1, Dr, d), whose truncated SVD is left_gauge / right_gauge with a
+ * truncation (src/states/orthoview.jl:326-341).  The element count must not change. */
+int gb_tensor_reshape(gb_tensor* t, int kind, int ndim, const int64_t* dims);
 
 /* ---------------------------------------------------------------- gauge */
 /* factorisation used by gb_svd_trunc */

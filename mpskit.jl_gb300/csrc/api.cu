@@ -101,6 +101,7 @@ struct HeffInfo {
   const char* terms;
 };
 HeffInfo heff_info(const gb_heff* h);
+std::string heff_describe(const gb_heff* h);
 }  // namespace gb
 
 using namespace gb;
@@ -1272,6 +1273,13 @@ int gb_heff_terms(const gb_heff* h, char* buf, size_t len) {
   API_END
 }
 
+int gb_heff_describe(const gb_heff* h, char* buf, size_t len) {
+  API_BEGIN
+  GB_REQUIRE(h && buf && len > 0, "null argument");
+  snprintf(buf, len, "%s", heff_describe(h).c_str());
+  API_END
+}
+
 int gb_heff_flops(const gb_heff* h, double* flops) {
   API_BEGIN
   GB_REQUIRE(h && flops, "null argument");
@@ -1413,6 +1421,143 @@ int gb_env_transfer_right(gb_ctx* ctx, const gb_tensor* GR, const gb_tensor* W, 
   // GR'[(a w), b] = T2[(a w), (s r)] conj(Abar[b, (s r)])^T
   gemm(ctx, prec, dt, 'N', 'C', Dk * wl, Db, d * Dbra, 1.0, T2, Dk * wl, 0, Abar->data, Db, 0, 0.0,
        GR_out->data, Dk * wl, 0);
+  API_END
+}
+
+// ---------------------------------------------------------------- bond expansion
+int gb_mps_perturb(gb_ctx* ctx, int side, const gb_tensor* env, const gb_tensor* W,
+                   const gb_tensor* AC, int precision, gb_tensor* out) {
+  API_BEGIN
+  GB_REQUIRE(ctx && env && W && AC && out, "null argument");
+  for (const gb_tensor* t : {env, W, AC, (const gb_tensor*)out}) check_ctx(t, ctx);
+  GB_REQUIRE(side == 0 || side == 1, "perturb: side must be 0 (left env) or 1 (right env)");
+  GB_REQUIRE(W->kind == GB_KIND_MPO && AC->kind == GB_KIND_MPS && out->kind == GB_KIND_MPS,
+             "perturb: operand kinds");
+  const int dt = AC->dtype;
+  GB_REQUIRE(env->dtype == dt && out->dtype == dt, "perturb: dtypes");
+  GB_REQUIRE(!(is_cplx(W->dtype) && !is_cplx(dt)), "perturb: complex MPO on a real state");
+  const int64_t Dl = AC->dims[0], d = AC->dims[1], Dr = AC->dims[2];
+  const int64_t wl = W->dims[0], wr = W->dims[3];
+  GB_REQUIRE(W->dims[1] == d && W->dims[2] == d, "perturb: MPO physical legs");
+  DevGuard g(ctx->device);
+  const size_t es = elem_size(dt);
+  if (side == 0) {
+    // P[l, s, (r w')] = GL[l, l', w] AC[l', s', r] W[w, s, s', w']  -- the first two steps
+    // of transfer_left with the bra contraction left out
+    GB_REQUIRE(env->kind == GB_KIND_GL && env->dims[1] == wl && env->dims[2] == Dl,
+               "perturb: GL shape");
+    const int64_t Db = env->dims[0];
+    GB_REQUIRE(out->dims[0] == Db && out->dims[1] == d && out->dims[2] == Dr * wr,
+               "perturb: output shape (Dl, d, Dr * wr)");
+    void* T1 = scratch(ctx, SLOT_T1, (size_t)Db * d * Dr * wl * es);
+    gemm(ctx, precision, dt, 'N', 'N', Db, d * Dr, Dl, 1.0, env->data, Db, Db * Dl, AC->data,
+         Dl, 0, 0.0, T1, Db, Db * d * Dr, wl);
+    const MixDev& m = transfer_plan(ctx, W, 0, Db, Dr, 0, is_cplx(dt));
+    mix_run(ctx, m, dt, T1, out->data, 0.0);
+  } else {
+    // P[(l w), s, r] = W[w, s, s', w'] AC[l, s', r'] GR[r', w', r]  -- the first two steps of
+    // transfer_right without the bra
+    GB_REQUIRE(env->kind == GB_KIND_GR && env->dims[0] == Dr && env->dims[1] == wr,
+               "perturb: GR shape");
+    const int64_t Db = env->dims[2];
+    GB_REQUIRE(out->dims[0] == Dl * wl && out->dims[1] == d && out->dims[2] == Db,
+               "perturb: output shape (Dl * wl, d, Dr)");
+    void* T1 = scratch(ctx, SLOT_T1, (size_t)Dl * d * wr * Db * es);
+    gemm(ctx, precision, dt, 'N', 'N', Dl * d, wr * Db, Dr, 1.0, AC->data, Dl * d, 0, env->data,
+         Dr, 0, 0.0, T1, Dl * d, 0);
+    const MixDev& m = transfer_plan(ctx, W, 1, Dl, 0, Db, is_cplx(dt));
+    mix_run(ctx, m, dt, T1, out->data, 0.0);
+  }
+  API_END
+}
+
+int gb_mps_cat(gb_ctx* ctx, const gb_tensor* A, const gb_tensor* B, int leg, gb_tensor* out) {
+  API_BEGIN
+  GB_REQUIRE(ctx && A && out, "null argument");
+  check_ctx(A, ctx);
+  check_ctx(out, ctx);
+  if (B) check_ctx(B, ctx);
+  GB_REQUIRE(A->kind == GB_KIND_MPS && out->kind == GB_KIND_MPS && (!B || B->kind == GB_KIND_MPS),
+             "cat: MPS tensors only");
+  GB_REQUIRE(leg == 0 || leg == 2, "cat: leg must be 0 (left bond) or 2 (right bond)");
+  GB_REQUIRE(out->dtype == A->dtype && (!B || B->dtype == A->dtype), "cat: dtypes");
+  const int other = 2 - leg;
+  GB_REQUIRE(out->dims[1] == A->dims[1] && out->dims[other] == A->dims[other],
+             "cat: the legs not concatenated must agree");
+  const int64_t nb = out->dims[leg] - A->dims[leg];
+  GB_REQUIRE(nb >= 0, "cat: output smaller than the first operand");
+  if (B)
+    GB_REQUIRE(B->dims[1] == A->dims[1] && B->dims[other] == A->dims[other] && B->dims[leg] == nb,
+               "cat: second operand shape");
+  DevGuard g(ctx->device);
+  const size_t es = elem_size(A->dtype);
+  cudaStream_t st = ctx->stream;
+  if (!B) GB_CHECK_CUDA(cudaMemsetAsync(out->data, 0, out->bytes, st));
+  if (leg == 2) {  // right bond: slowest in (l, s, r) -- two contiguous pieces
+    if (A->bytes)
+      GB_CHECK_CUDA(cudaMemcpyAsync(out->data, A->data, A->bytes, cudaMemcpyDeviceToDevice, st));
+    if (B && B->bytes)
+      GB_CHECK_CUDA(cudaMemcpyAsync((char*)out->data + A->bytes, B->data, B->bytes,
+                                    cudaMemcpyDeviceToDevice, st));
+  } else {  // left bond: fastest -- row blocks of A->dims[0] and nb elements per (s, r)
+    const int64_t cols = A->dims[1] * A->dims[2], ld = out->dims[0];
+    if (A->dims[0] && cols)
+      GB_CHECK_CUDA(cudaMemcpy2DAsync(out->data, ld * es, A->data, A->dims[0] * es,
+                                      A->dims[0] * es, cols, cudaMemcpyDeviceToDevice, st));
+    if (B && nb && cols)
+      GB_CHECK_CUDA(cudaMemcpy2DAsync((char*)out->data + A->dims[0] * es, ld * es, B->data,
+                                      nb * es, nb * es, cols, cudaMemcpyDeviceToDevice, st));
+  }
+  API_END
+}
+
+int gb_tensor_reshape(gb_tensor* t, int kind, int ndim, const int64_t* dims) {
+  API_BEGIN
+  GB_REQUIRE(t && dims, "null argument");
+  auto plain = [](int k) {
+    return k == GB_KIND_MPS || k == GB_KIND_AC2 || k == GB_KIND_BOND || k == GB_KIND_GENERIC;
+  };
+  GB_REQUIRE(plain(t->kind) && plain(kind), "reshape: MPS, two-site, bond or generic tensors");
+  const int want = kind == GB_KIND_MPS ? 3 : kind == GB_KIND_AC2 ? 4 : kind == GB_KIND_BOND ? 2 : -1;
+  GB_REQUIRE(ndim >= 1 && ndim <= 6 && (want < 0 || ndim == want), "reshape: rank");
+  int64_t n = 1;
+  for (int i = 0; i < ndim; ++i) {
+    GB_REQUIRE(dims[i] >= 0, "reshape: negative dimension");
+    n *= dims[i];
+  }
+  GB_REQUIRE(n == numel(t), "reshape: element count");
+  t->kind = kind;
+  t->ndim = ndim;
+  for (int i = 0; i < 6; ++i) t->dims[i] = i < ndim ? dims[i] : 0;
+  API_END
+}
+
+int gb_project_complement_right(gb_ctx* ctx, gb_tensor* Y, const gb_tensor* X) {
+  API_BEGIN
+  check_ctx(Y, ctx);
+  check_ctx(X, ctx);
+  GB_REQUIRE(X->kind == GB_KIND_MPS, "project_complement_right: X must be an MPS tensor");
+  GB_REQUIRE(Y->kind == GB_KIND_MPS || Y->kind == GB_KIND_AC2,
+             "project_complement_right: Y kind");
+  GB_REQUIRE(X->dtype == Y->dtype, "project_complement_right: dtypes");
+  const int64_t k = X->dims[0], cols = X->dims[1] * X->dims[2];
+  GB_REQUIRE(cols > 0 && numel(Y) % cols == 0, "project_complement_right: trailing legs mismatch");
+  // the trailing legs of Y in device order must be X's (s, r)
+  if (Y->kind == GB_KIND_AC2)
+    GB_REQUIRE(Y->dims[3] == X->dims[1] && Y->dims[2] == X->dims[2],
+               "project_complement_right: trailing legs mismatch");
+  else
+    GB_REQUIRE(Y->dims[1] == X->dims[1] && Y->dims[2] == X->dims[2],
+               "project_complement_right: trailing legs mismatch");
+  const int64_t rows = numel(Y) / cols;
+  DevGuard g(ctx->device);
+  const size_t es = elem_size(Y->dtype);
+  void* T = scratch(ctx, SLOT_TMP, (size_t)rows * k * es);
+  // T = Y X^H (rows x k); Y -= T X
+  gemm(ctx, ctx->aux_prec, Y->dtype, 'N', 'C', rows, k, cols, 1.0, Y->data, rows, 0, X->data, k,
+       0, 0.0, T, rows, 0);
+  gemm(ctx, ctx->aux_prec, Y->dtype, 'N', 'N', rows, cols, k, -1.0, T, rows, 0, X->data, k, 0,
+       1.0, Y->data, rows, 0);
   API_END
 }
 

@@ -297,8 +297,11 @@ static HostW hostw(const gb_tensor* W) {
 }
 
 // ------------------------------------------------------------------ AC2
+// generic: MPO_AC2_Hamiltonian of an arbitrary MPO (mpo_derivatives.jl:56-66, 144-163):
+// every channel continues, no Jordan terms -- the whole operator is the x.GR -> (W1 W2) ->
+// GL.(.) chain over all channels (connected ones only)
 static void build_ac2(gb_heff* h, const gb_tensor* GL, const gb_tensor* W1,
-                      const gb_tensor* W2, const gb_tensor* GR) {
+                      const gb_tensor* W2, const gb_tensor* GR, bool generic = false) {
   gb_ctx* ctx = h->ctx;
   const bool cx = is_cplx(h->dtype);
   const size_t es = elem_size(h->dtype);
@@ -312,41 +315,45 @@ static void build_ac2(gb_heff* h, const gb_tensor* GL, const gb_tensor* W1,
   const double* gl = (const double*)GL->data;
   const double* gr = (const double*)GR->data;
 
-  // Jordan blocks (flat channel index; first = start, last = finished)
+  // Jordan blocks (flat channel index; first = start, last = finished); for a generic MPO
+  // the "continuing" block is the whole tensor (channel offset co = 0, all channels)
+  const int64_t co = generic ? 0 : 1, cut = generic ? 0 : 2;
   auto A1nz = [&](int64_t c, int64_t k) {  // A1[c, :, :, k] nonzero, c < wl-2, k < wm-2
     for (int64_t s = 0; s < d1; ++s)
       for (int64_t t = 0; t < d1; ++t)
-        if (w1.nz(1 + c, s, t, 1 + k)) return true;
+        if (w1.nz(co + c, s, t, co + k)) return true;
     return false;
   };
   auto A2nz = [&](int64_t k, int64_t m) {
     for (int64_t s = 0; s < d2; ++s)
       for (int64_t t = 0; t < d2; ++t)
-        if (w2.nz(1 + k, s, t, 1 + m)) return true;
+        if (w2.nz(co + k, s, t, co + m)) return true;
     return false;
   };
-  const int64_t nA1r = std::max<int64_t>(wl - 2, 0), nA1c = std::max<int64_t>(wm - 2, 0);
-  const int64_t nA2r = nA1c, nA2c = std::max<int64_t>(wr - 2, 0);
+  const int64_t nA1r = std::max<int64_t>(wl - cut, 0), nA1c = std::max<int64_t>(wm - cut, 0);
+  const int64_t nA2r = nA1c, nA2c = std::max<int64_t>(wr - cut, 0);
   bool nzA1 = false, nzA2 = false, nzB1 = false, nzB2 = false, nzC1 = false, nzC2 = false,
        nzD1 = false, nzD2 = false;
   for (int64_t c = 0; c < nA1r; ++c)
     for (int64_t k = 0; k < nA1c; ++k) nzA1 |= A1nz(c, k);
   for (int64_t k = 0; k < nA2r; ++k)
     for (int64_t m = 0; m < nA2c; ++m) nzA2 |= A2nz(k, m);
-  for (int64_t s = 0; s < d1; ++s)
-    for (int64_t t = 0; t < d1; ++t) {
-      for (int64_t c = 0; c < nA1r; ++c) nzB1 |= w1.nz(1 + c, s, t, wm - 1);
-      for (int64_t k = 0; k < nA1c; ++k) nzC1 |= w1.nz(0, s, t, 1 + k);
-      nzD1 |= w1.nz(0, s, t, wm - 1);
-    }
-  for (int64_t s = 0; s < d2; ++s)
-    for (int64_t t = 0; t < d2; ++t) {
-      for (int64_t k = 0; k < nA2r; ++k) nzB2 |= w2.nz(1 + k, s, t, wr - 1);
-      for (int64_t m = 0; m < nA2c; ++m) nzC2 |= w2.nz(0, s, t, 1 + m);
-      nzD2 |= w2.nz(0, s, t, wr - 1);
-    }
-  // term presence (hamiltonian_derivatives.jl:283-359)
-  bool II = wr > 1, EE = wl > 1, IC = nzC2, DE = nzD1, ID = nzD2;
+  if (!generic) {
+    for (int64_t s = 0; s < d1; ++s)
+      for (int64_t t = 0; t < d1; ++t) {
+        for (int64_t c = 0; c < nA1r; ++c) nzB1 |= w1.nz(1 + c, s, t, wm - 1);
+        for (int64_t k = 0; k < nA1c; ++k) nzC1 |= w1.nz(0, s, t, 1 + k);
+        nzD1 |= w1.nz(0, s, t, wm - 1);
+      }
+    for (int64_t s = 0; s < d2; ++s)
+      for (int64_t t = 0; t < d2; ++t) {
+        for (int64_t k = 0; k < nA2r; ++k) nzB2 |= w2.nz(1 + k, s, t, wr - 1);
+        for (int64_t m = 0; m < nA2c; ++m) nzC2 |= w2.nz(0, s, t, 1 + m);
+        nzD2 |= w2.nz(0, s, t, wr - 1);
+      }
+  }
+  // term presence (hamiltonian_derivatives.jl:283-359); none but the chain when generic
+  bool II = !generic && wr > 1, EE = !generic && wl > 1, IC = nzC2, DE = nzD1, ID = nzD2;
   bool CB = nzC1 && nzB2, CA = nzC1 && nzA2, AB = nzA1 && nzB2, BE = nzB1;
   // connected channels (:243-270)
   std::vector<int64_t> rows, mids, cols;
@@ -390,11 +397,11 @@ static void build_ac2(gb_heff* h, const gb_tensor* GL, const gb_tensor* W1,
   auto C1v = [&](int64_t s, int64_t t, int64_t k) { return w1.at(0, s, t, 1 + k); };
   auto D1v = [&](int64_t s, int64_t t) { return w1.at(0, s, t, wm - 1); };
   auto B1v = [&](int64_t c, int64_t s, int64_t t) { return w1.at(1 + c, s, t, wm - 1); };
-  auto A1v = [&](int64_t c, int64_t s, int64_t t, int64_t k) { return w1.at(1 + c, s, t, 1 + k); };
+  auto A1v = [&](int64_t c, int64_t s, int64_t t, int64_t k) { return w1.at(co + c, s, t, co + k); };
   auto C2v = [&](int64_t s, int64_t t, int64_t m) { return w2.at(0, s, t, 1 + m); };
   auto D2v = [&](int64_t s, int64_t t) { return w2.at(0, s, t, wr - 1); };
   auto B2v = [&](int64_t k, int64_t s, int64_t t) { return w2.at(1 + k, s, t, wr - 1); };
-  auto A2v = [&](int64_t k, int64_t s, int64_t t, int64_t m) { return w2.at(1 + k, s, t, 1 + m); };
+  auto A2v = [&](int64_t k, int64_t s, int64_t t, int64_t m) { return w2.at(co + k, s, t, co + m); };
   auto CBv = [&](int64_t s1, int64_t s2, int64_t u1, int64_t u2) {
     Cx acc;
     for (int64_t k = 0; k < nA1c; ++k) acc = cadd(acc, cmul(C1v(s1, u1, k), B2v(k, s2, u2)));
@@ -432,7 +439,7 @@ static void build_ac2(gb_heff* h, const gb_tensor* GL, const gb_tensor* W1,
       Coef cf(chc, wr);
       std::vector<int64_t> oo(chc);
       for (int64_t j = 0; j < chc; ++j) {
-        cf.at(j, 1 + cols[j]) = Cx{1, 0};
+        cf.at(j, co + cols[j]) = Cx{1, 0};
         oo[j] = Dr * j;
       }
       MixDev m = mix_upload(ctx, make_plan(cf, cx, Dr, Dr, 1, Dr * wr, 1, Dr * chc, gr_in, oo));
@@ -444,7 +451,7 @@ static void build_ac2(gb_heff* h, const gb_tensor* GL, const gb_tensor* W1,
       Coef cf(chr, wl);
       std::vector<int64_t> oo(chr);
       for (int64_t i = 0; i < chr; ++i) {
-        cf.at(i, 1 + rows[i]) = Cx{1, 0};
+        cf.at(i, co + rows[i]) = Cx{1, 0};
         oo[i] = Dl * Dl * i;
       }
       MixDev m = mix_upload(ctx, make_plan(cf, cx, Dl, Dl, 1, Dl, 1, Dl, gl_in, oo));
@@ -815,7 +822,10 @@ static void build_ac2(gb_heff* h, const gb_tensor* GL, const gb_tensor* W1,
 }
 
 // ------------------------------------------------------------------ AC
-static void build_ac(gb_heff* h, const gb_tensor* GL, const gb_tensor* W, const gb_tensor* GR) {
+// generic: MPO_AC_Hamiltonian of an arbitrary MPO (mpo_derivatives.jl:46-55, 127-142): no
+// Jordan terms, the whole operator is the x.GR -> W -> GL.(.) chain over all channels
+static void build_ac(gb_heff* h, const gb_tensor* GL, const gb_tensor* W, const gb_tensor* GR,
+                     bool generic = false) {
   gb_ctx* ctx = h->ctx;
   const bool cx = is_cplx(h->dtype);
   const size_t es = elem_size(h->dtype);
@@ -827,8 +837,9 @@ static void build_ac(gb_heff* h, const gb_tensor* GL, const gb_tensor* W, const 
   GB_REQUIRE(w.wl == wl && w.wr == wr && w.d1 == w.d2, "AC: MPO shape mismatch");
   const double* gl = (const double*)GL->data;
   const double* gr = (const double*)GR->data;
-  const int64_t nr = std::max<int64_t>(wl - 2, 0), nc = std::max<int64_t>(wr - 2, 0);
-  auto Av = [&](int64_t c, int64_t s, int64_t t, int64_t k) { return w.at(1 + c, s, t, 1 + k); };
+  const int64_t co = generic ? 0 : 1, cut = generic ? 0 : 2;
+  const int64_t nr = std::max<int64_t>(wl - cut, 0), nc = std::max<int64_t>(wr - cut, 0);
+  auto Av = [&](int64_t c, int64_t s, int64_t t, int64_t k) { return w.at(co + c, s, t, co + k); };
   auto Bv = [&](int64_t c, int64_t s, int64_t t) { return w.at(1 + c, s, t, wr - 1); };
   auto Cv = [&](int64_t s, int64_t t, int64_t k) { return w.at(0, s, t, 1 + k); };
   auto Dv = [&](int64_t s, int64_t t) { return w.at(0, s, t, wr - 1); };
@@ -838,16 +849,17 @@ static void build_ac(gb_heff* h, const gb_tensor* GL, const gb_tensor* W, const 
     for (int64_t t = 0; t < d; ++t) {
       for (int64_t c = 0; c < nr; ++c)
         for (int64_t k = 0; k < nc; ++k)
-          if (w.nz(1 + c, s, t, 1 + k)) {
+          if (w.nz(co + c, s, t, co + k)) {
             nzA = true;
             rowA[c] = 1;
             colA[k] = 1;
           }
+      if (generic) continue;
       for (int64_t c = 0; c < nr; ++c) nzB |= w.nz(1 + c, s, t, wr - 1);
       for (int64_t k = 0; k < nc; ++k) nzC |= w.nz(0, s, t, 1 + k);
       nzD |= w.nz(0, s, t, wr - 1);
     }
-  bool D = nzD, I = wr > 1, E = wl > 1, C = nzC, B = nzB, A = nzA;
+  bool D = nzD, I = !generic && wr > 1, E = !generic && wl > 1, C = nzC, B = nzB, A = nzA;
   enum { KEEP, INTO_C, INTO_B };
   int fD = KEEP, fI = KEEP, fE = KEEP;
   if (D) fD = C ? INTO_C : (B ? INTO_B : KEEP);
@@ -884,7 +896,7 @@ static void build_ac(gb_heff* h, const gb_tensor* GL, const gb_tensor* W, const 
       Coef cf(chc, wr);
       std::vector<int64_t> oo(chc);
       for (int64_t j = 0; j < chc; ++j) {
-        cf.at(j, 1 + cols[j]) = Cx{1, 0};
+        cf.at(j, co + cols[j]) = Cx{1, 0};
         oo[j] = Dr * j;
       }
       MixDev m = mix_upload(ctx, make_plan(cf, cx, Dr, Dr, 1, Dr * wr, 1, Dr * chc, gr_in, oo));
@@ -896,7 +908,7 @@ static void build_ac(gb_heff* h, const gb_tensor* GL, const gb_tensor* W, const 
       Coef cf(chr, wl);
       std::vector<int64_t> oo(chr);
       for (int64_t i = 0; i < chr; ++i) {
-        cf.at(i, 1 + rows[i]) = Cx{1, 0};
+        cf.at(i, co + rows[i]) = Cx{1, 0};
         oo[i] = Dl * Dl * i;
       }
       MixDev m = mix_upload(ctx, make_plan(cf, cx, Dl, Dl, 1, Dl, 1, Dl, gl_in, oo));
@@ -1185,13 +1197,17 @@ gb_heff* heff_build(gb_ctx* ctx, int kind, const gb_tensor* GL, const gb_tensor*
   h->dtype = GL->dtype;
   h->prec = prec;
   h->sched = ctx->gemm_schedule;
+  // the generic-MPO kinds are built and applied as the Jordan kinds with one term
+  const bool generic = kind == GB_HEFF_AC_MPO || kind == GB_HEFF_AC2_MPO;
+  if (kind == GB_HEFF_AC_MPO) h->kind = kind = GB_HEFF_AC;
+  if (kind == GB_HEFF_AC2_MPO) h->kind = kind = GB_HEFF_AC2;
   try {
     if (kind == GB_HEFF_AC2) {
       GB_REQUIRE(W1 && W2, "AC2 needs W1 and W2");
-      build_ac2(h, GL, W1, W2, GR);
+      build_ac2(h, GL, W1, W2, GR, generic);
     } else if (kind == GB_HEFF_AC) {
       GB_REQUIRE(W1 && !W2, "AC needs exactly W1");
-      build_ac(h, GL, W1, GR);
+      build_ac(h, GL, W1, GR, generic);
     } else if (kind == GB_HEFF_C) {
       GB_REQUIRE(!W1 && !W2, "C takes no MPO tensor");
       build_c(h, GL, GR);
@@ -1753,6 +1769,30 @@ struct HeffInfo {
   double flops;
   const char* terms;
 };
+// one line per contraction step: its shape and, for a grouped sector-block GEMM, the plan
+// (groups, tiles, K-blocks of the longest tile, tile work over nonzero block work)
+std::string heff_describe(const gb_heff* h) {
+  std::ostringstream os;
+  for (size_t i = 0; i < h->steps.size(); ++i) {
+    const Step& s = h->steps[i];
+    os << s.name << (s.is_gemm ? " gemm" : " mix");
+    if (s.is_gemm) os << " M=" << s.M << " N=" << s.N << " K=" << s.K;
+    if (i < h->gsteps.size() && !h->gsteps[i].plan.tiles.empty()) {
+      const GPlan& p = h->gsteps[i].plan;
+      int64_t maxkb = 0, kb = 0;
+      for (const GTile& t : p.tiles) {
+        maxkb = std::max<int64_t>(maxkb, t.nkb);
+        kb += t.nkb;
+      }
+      os << " grouped G=" << p.G << " tiles=" << p.tiles.size() << " kblocks=" << kb
+         << " max_tile_kblocks=" << maxkb << " trans=" << (p.trans ? 1 : 0)
+         << " block_gflop=" << p.block_flops * 1e-9 << " tile_gflop=" << p.tile_flops * 1e-9;
+    }
+    os << "\n";
+  }
+  return os.str();
+}
+
 HeffInfo heff_info(const gb_heff* h) {
   HeffInfo hi;
   hi.ctx = h->ctx;

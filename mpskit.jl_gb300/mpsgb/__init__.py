@@ -7,13 +7,14 @@ contraction runs in libmpsgb.so on the GPU.
 from . import _lib
 from .core import Context, DeviceTensor, context
 from .derivatives import (AC2_hamiltonian, AC_hamiltonian, C_hamiltonian, DerivativeOperator,
-                          GB300Backend, Lanczos, exponentiate, fixedpoint, integrate)
+                          GB300Backend, Lanczos, MPO_AC2_Hamiltonian, MPO_AC_Hamiltonian,
+                          exponentiate, fixedpoint, integrate)
 from .operators import (FiniteMPOHamiltonian, InfiniteMPOHamiltonian, MPOHamiltonian,
                         heisenberg_XXX, j1j2_cylinder, transverse_field_ising, xxz)
 from .states import (FiniteEnvironments, FiniteMPS, ac2_from, left_orth, mul_front, mul_tail,
                      project_complement_, right_orth, svd_trunc)
-from .algorithms import (DMRG, DMRG2, TDVP, AdaptiveKrylov, expectation_value,
-                         find_groundstate, timestep)
+from .algorithms import (DMRG, DMRG2, DMRG3S, TDVP, AdaptiveKrylov, OptimalExpand,
+                         expectation_value, find_groundstate, timestep)
 from .infinite import (IDMRG, VUMPS, InfiniteEnvironments, InfiniteMPS,
                        find_groundstate_idmrg, find_groundstate_vumps, timestep_infinite)
 from . import u1
@@ -23,10 +24,12 @@ from . import cell
 __all__ = [
     "Context", "DeviceTensor", "context", "AC2_hamiltonian", "AC_hamiltonian", "C_hamiltonian",
     "DerivativeOperator", "GB300Backend", "Lanczos", "exponentiate", "fixedpoint", "integrate",
+    "MPO_AC_Hamiltonian", "MPO_AC2_Hamiltonian",
     "FiniteMPOHamiltonian", "InfiniteMPOHamiltonian", "MPOHamiltonian", "heisenberg_XXX",
     "j1j2_cylinder", "transverse_field_ising", "xxz", "FiniteEnvironments", "FiniteMPS",
     "ac2_from", "left_orth", "mul_front", "mul_tail", "project_complement_", "right_orth",
-    "svd_trunc", "DMRG", "DMRG2", "AdaptiveKrylov", "expectation_value", "find_groundstate",
+    "svd_trunc", "DMRG", "DMRG2", "DMRG3S", "OptimalExpand", "AdaptiveKrylov",
+    "expectation_value", "find_groundstate",
     "TDVP", "timestep", "VUMPS", "IDMRG", "InfiniteEnvironments", "InfiniteMPS",
     "find_groundstate_vumps", "find_groundstate_idmrg", "timestep_infinite", "u1", "batched",
     "cell",

@@ -32,6 +32,8 @@ GB_KIND_MPO = 6
 GB_HEFF_C = 0
 GB_HEFF_AC = 1
 GB_HEFF_AC2 = 2
+GB_HEFF_AC_MPO = 3
+GB_HEFF_AC2_MPO = 4
 
 GB_PREC_FP64 = 0
 GB_PREC_BF16X3 = 1
@@ -116,6 +118,11 @@ _SIGS = {
     "gb_mps_mul_front": ([P, P, P, P], INT),
     "gb_mps_mul_tail": ([P, P, P, P], INT),
     "gb_project_complement": ([P, P, P], INT),
+    "gb_project_complement_right": ([P, P, P], INT),
+    "gb_heff_describe": ([P, ctypes.c_char_p, ctypes.c_size_t], INT),
+    "gb_mps_perturb": ([P, INT, P, P, P, INT, P], INT),
+    "gb_mps_cat": ([P, P, P, INT, P], INT),
+    "gb_tensor_reshape": ([P, INT, INT, PI64], INT),
     "gb_svd_trunc": ([P, P, I64, D, INT, ctypes.POINTER(P), ctypes.POINTER(P), ctypes.POINTER(P), PD], INT),
     "gb_u1_left_orth": ([P, P, PI32, PI32, PI32, ctypes.POINTER(P), ctypes.POINTER(P), PI32, PI64], INT),
     "gb_u1_right_orth": ([P, P, PI32, PI32, PI32, ctypes.POINTER(P), ctypes.POINTER(P), PI32, PI64], INT),

@@ -4,6 +4,8 @@
   AdaptiveKrylov / adapt_solver             -- src/utility/dynamictols.jl:182-235
   calc_galerkin                             -- src/algorithms/toolbox.jl:63-70
   expectation_value(FiniteMPS, H)           -- src/algorithms/expval.jl:136-141
+  OptimalExpand changebond!                 -- src/algorithms/changebonds/optimalexpand.jl:122-187
+  DMRG3S gauge!, ExponentialDecay           -- src/algorithms/post_expand/dmrg3s.jl:36-56, 133-192
 """
 import math
 import time
@@ -13,8 +15,11 @@ import numpy as np
 from . import _lib as L
 from .derivatives import (AC2_hamiltonian, AC_hamiltonian, C_hamiltonian, GB300Backend, Lanczos,
                           exponentiate, fixedpoint)
-from .states import (FiniteEnvironments, ac2_from, left_orth, project_complement_, right_orth,
+from .states import (FiniteEnvironments, ac2_from, left_orth, mps_cat, mul_front, mul_tail,
+                     perturb, project_complement_, project_complement_right_, right_orth,
                      svd_trunc)
+
+EPS34 = np.finfo(np.float64).eps ** 0.75
 
 
 class AdaptiveKrylov:
@@ -59,11 +64,132 @@ class DMRG2:
 
 
 class DMRG:
-    def __init__(self, tol=1e-10, maxiter=200, alg_eigsolve=None, backend=None, verbosity=0):
+    """Single-site DMRG (dmrg.jl:55-158).  alg_gauge = None: the positive QR/LQ gauge;
+    a DMRG3S: the perturbed, truncated gauge.  alg_expand = an OptimalExpand run ahead of
+    every local update (dmrg.jl:128-134)."""
+
+    def __init__(self, tol=1e-10, maxiter=200, alg_eigsolve=None, backend=None, verbosity=0,
+                 alg_gauge=None, alg_expand=None):
         self.tol, self.maxiter = tol, maxiter
         self.alg_eigsolve = alg_eigsolve or AdaptiveKrylov()
         self.backend = backend or GB300Backend()
         self.verbosity = verbosity
+        self.alg_gauge = alg_gauge
+        self.alg_expand = alg_expand
+
+
+class OptimalExpand:
+    """OptimalExpand(; trunc = truncrank(add)) (optimalexpand.jl:36-47): at most `add`
+    directions are added to a bond per expansion."""
+
+    def __init__(self, add):
+        self.add = add
+
+
+class DMRG3S:
+    """DMRG3S(noise, ExponentialDecay(decay_rate)) with the truncated SVD DMRG fills in
+    (dmrg3s.jl:83-131; trunc = truncrank(maxdim) & trunctol(atol)): the noise at outer
+    iteration `it` is noise * decay_rate^it."""
+
+    def __init__(self, noise, decay_rate, maxdim, atol=0.0):
+        self.noise, self.decay_rate = noise, decay_rate
+        self.maxdim, self.atol = maxdim, atol
+
+    def noise_at(self, it):
+        return self.noise * self.decay_rate ** it
+
+
+def _dense_only(psi, what):
+    if psi.C[psi.center].charges is not None:
+        raise NotImplementedError(f"{what} of a U(1)-symmetric state")
+
+
+def optimal_expand(pos, right, psi, H, envs, alg, backend=None):
+    """changebond!(site, dir, psi, H, ::OptimalExpand, envs) (optimalexpand.jl:122-187):
+    the two-site update AC2_projection projected onto the complements of both sites, its
+    `add` dominant right (left) singular directions appended to the bond with zero weight
+    -- the state is unchanged -- and the site regauged.  The complements are applied as
+    projectors (1 - AL AL') Y (1 - AR' AR) instead of null-space bases: the singular
+    vectors of the projected Y are those of NL' Y NR' mapped back by NL / NR.  Directions
+    whose singular value is below eps^(3/4) of the normalised Y (arbitrary in the
+    reference) are not added."""
+    _dense_only(psi, "OptimalExpand")
+    backend = backend or GB300Backend()
+    b = pos if right else pos - 1
+    if right:
+        left, rt = psi.ac(pos), psi.AR[pos + 1]
+        PL = psi.al(pos)
+    else:
+        left, rt = psi.AL[pos - 1], psi.ac(pos)
+        PL = left
+    # two-site update from the projected effective Hamiltonian (AC2_projection)
+    Y = AC2_hamiltonian(b, psi, H, envs, backend)(ac2_from(left, rt))
+    project_complement_(Y, PL)
+    if right:
+        project_complement_right_(Y, rt)
+    else:
+        # the right complement of AC[pos]: its row space is that of its LQ factor
+        _, q = right_orth(rt)
+        project_complement_right_(Y, q)
+    nrm = Y.norm()
+    if nrm <= EPS34:
+        return
+    Y.scale_(1.0 / nrm)
+    u, _, vh, _ = svd_trunc(Y, alg.add, EPS34, normalize=False)
+    if right:
+        k = vh.dims[0]
+        nar = mps_cat(rt, vh, 0)                         # AR[pos+1] with the new rows
+        nal, nc = left_orth(mps_cat(left, None, 2, nb=k))  # [AC | 0] regauged
+        nc.scale_(1.0 / nc.norm())
+        psi.AL[pos], psi.C[pos + 1], psi.AR[pos + 1] = nal, nc, nar
+        psi.center = pos + 1
+    else:
+        k = u.dims[2]
+        nal = mps_cat(left, u, 2)                        # AL[pos-1] with the new columns
+        nc, nar = right_orth(mps_cat(rt, None, 0, nb=k))  # [AC ; 0] regauged
+        nc.scale_(1.0 / nc.norm())
+        psi.AL[pos - 1], psi.C[pos], psi.AR[pos] = nal, nc, nar
+        psi.center = pos
+
+
+def dmrg3s_gauge(pos, right, psi, H, envs, AC, noise, maxdim, atol):
+    """gauge!(psi, pos, dir, H, envs, AC, ::DMRG3S) (dmrg3s.jl:133-192).  Right: the
+    perturbation noise * GL[pos] W[pos] AC with the right bond and the MPO channel fused
+    (bond index fastest) is appended to AC along its right bond, the truncated SVD gives
+    AL[pos] and C = S Vh, and AR[pos+1] gets zero rows for the new directions.  Left: the
+    mirror image with GR[pos], zero columns appended to AL[pos-1].  Returns the truncation
+    error."""
+    _dense_only(psi, "DMRG3S")
+    W = H.device(envs.ctx, envs.dtype)[pos]
+    Dl, d, Dr = AC.dims
+    if right:
+        P = perturb(envs.leftenv(pos, psi), W, AC, 0, envs.precision)
+        P.scale_(noise)
+        ACe = mps_cat(AC, P, 2)
+        ACe.reshape_(L.GB_KIND_AC2, (Dl, d, ACe.dims[2], 1))   # left_gauge as an SVD
+        al, S, vh, eps = svd_trunc(ACe, maxdim, atol, normalize=True)
+        k = S.dims[0]
+        C = mul_front(S, vh)
+        C.reshape_(L.GB_KIND_BOND, (k, C.dims[2]))
+        psi.AL[pos] = al
+        psi.AR[pos + 1] = mps_cat(psi.AR[pos + 1], None, 0, nb=P.dims[2])
+        psi.C[pos + 1] = C
+        psi.center = pos + 1
+    else:
+        P = perturb(envs.rightenv(pos, psi), W, AC, 1, envs.precision)
+        P.scale_(noise)
+        ACe = mps_cat(AC, P, 0)
+        Dl2 = ACe.dims[0]
+        ACe.reshape_(L.GB_KIND_AC2, (Dl2, 1, Dr, d))           # right_gauge as an SVD
+        u, S, ar, eps = svd_trunc(ACe, maxdim, atol, normalize=True)
+        k = S.dims[0]
+        C = mul_tail(u, S)
+        C.reshape_(L.GB_KIND_BOND, (Dl2, k))
+        psi.AR[pos] = ar
+        psi.AL[pos - 1] = mps_cat(psi.AL[pos - 1], None, 2, nb=P.dims[0])
+        psi.C[pos] = C
+        psi.center = pos
+    return eps
 
 
 def _decay(normres, eps_local, numops):
@@ -167,6 +293,41 @@ def _sweep_dmrg2(psi, H, alg, envs, maxsweeps, callback):
     return psi, envs, eps_global, hist
 
 
+def dmrg1_local_update(pos, right, psi, H, alg, envs, eps_global, decay_rate, it):
+    """local_update!(..., ::DMRG) (dmrg.jl:121-158): Galerkin error, optional expansion,
+    eigensolve, then the QR/LQ or the DMRG3S gauge."""
+    ac = psi.ac(pos)
+    Heff = AC_hamiltonian(pos, psi, H, envs, alg.backend)
+    y = Heff(ac)
+    y.normalize_()
+    project_complement_(y, psi.al(pos))
+    eps_local = y.norm()
+    if alg.alg_expand is not None:
+        optimal_expand(pos, right, psi, H, envs, alg.alg_expand, alg.backend)
+        ac = psi.ac(pos)
+        Heff = AC_hamiltonian(pos, psi, H, envs, alg.backend)
+    solver = alg.alg_eigsolve.adapt(decay_rate, eps_local, eps_global, 0.0)
+    val, new, info = fixedpoint(Heff, ac, "SR", solver)
+    decay = _decay(info.normres, eps_local, info.numops)
+    g = alg.alg_gauge
+    if g is not None and g.noise_at(it) != 0.0:
+        eps_tr = dmrg3s_gauge(pos, right, psi, H, envs, new, g.noise_at(it), g.maxdim, g.atol)
+        return eps_local, eps_tr, decay, val
+    if right:
+        q, R = left_orth(new)
+        R.scale_(1.0 / R.norm())
+        psi.AL[pos] = q
+        psi.C[pos + 1] = R
+        psi.center = pos + 1
+    else:
+        Lm, q = right_orth(new)
+        Lm.scale_(1.0 / Lm.norm())
+        psi.AR[pos] = q
+        psi.C[pos] = Lm
+        psi.center = pos
+    return eps_local, 0.0, decay, val
+
+
 def _sweep_dmrg1(psi, H, alg, envs, maxsweeps, callback):
     envs = envs or FiniteEnvironments(psi, H)
     envs.precision = alg.backend.code
@@ -180,28 +341,8 @@ def _sweep_dmrg1(psi, H, alg, envs, maxsweeps, callback):
     for it in range(niter):
         for right, rng in ((True, range(0, n - 1)), (False, range(n - 1, 0, -1))):
             for pos in rng:
-                ac = psi.ac(pos)
-                Heff = AC_hamiltonian(pos, psi, H, envs, alg.backend)
-                y = Heff(ac)
-                y.normalize_()
-                project_complement_(y, psi.al(pos))
-                eps_local = y.norm()
-                solver = alg.alg_eigsolve.adapt(decays[pos], eps_local, eps_global, 0.0)
-                val, new, info = fixedpoint(Heff, ac, "SR", solver)
-                if right:
-                    q, R = left_orth(new)
-                    R.scale_(1.0 / R.norm())
-                    psi.AL[pos] = q
-                    psi.C[pos + 1] = R
-                    psi.center = pos + 1
-                else:
-                    Lm, q = right_orth(new)
-                    Lm.scale_(1.0 / Lm.norm())
-                    psi.AR[pos] = q
-                    psi.C[pos] = Lm
-                    psi.center = pos
-                eps_locals[pos] = eps_local
-                decays[pos] = _decay(info.normres, eps_local, info.numops)
+                eps_locals[pos], _, decays[pos], val = dmrg1_local_update(
+                    pos, right, psi, H, alg, envs, eps_global, decays[pos], it)
                 eps_global = float(eps_locals.max())
         hist.append({"sweep": it, "energy": float(val), "eps": eps_global})
         if callback:

@@ -190,6 +190,15 @@ class DeviceTensor:
                                            out.nbytes))
         return out
 
+    def reshape_(self, kind, dims, charges=None):
+        """Relabel kind and shape in place over the same device storage (gb_tensor_reshape:
+        the new shape reads the storage in its own device order)."""
+        kind = _KIND_NAMES[kind] if isinstance(kind, str) else kind
+        arr = (ctypes.c_int64 * len(dims))(*[int(x) for x in dims])
+        L.check(L.lib().gb_tensor_reshape(self.handle, kind, len(dims), arr))
+        self.kind, self.dims, self.charges = kind, tuple(int(x) for x in dims), charges
+        return self
+
     # ------------------------------------------------ VectorInterface-style operations
     def similar(self):
         return DeviceTensor(self.ctx, self.kind, self.dtype, self.dims, charges=self.charges)

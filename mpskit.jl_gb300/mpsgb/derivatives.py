@@ -3,6 +3,8 @@
   AC2_hamiltonian / AC_hamiltonian / C_hamiltonian
       -- src/algorithms/derivatives/hamiltonian_derivatives.jl:44-55, 206-217,
          src/algorithms/derivatives/mpo_derivatives.jl:37-45
+  MPO_AC_Hamiltonian / MPO_AC2_Hamiltonian (an arbitrary MPO, no Jordan structure)
+      -- src/algorithms/derivatives/mpo_derivatives.jl:46-66
   fixedpoint(H, x0, :SR, Lanczos)       -- src/algorithms/fixedpoint.jl:15-18
   integrate(H, y0, t, dt, Lanczos)      -- src/algorithms/timestep/integrators.jl:44-53
 
@@ -47,7 +49,9 @@ class DerivativeOperator:
 
     def __init__(self, ctx, kind, GL, W1, W2, GR, backend):
         self.ctx = ctx
-        self.kind = kind
+        # the generic-MPO kinds act as the Jordan kinds of the same arity
+        self.kind = {L.GB_HEFF_AC_MPO: L.GB_HEFF_AC, L.GB_HEFF_AC2_MPO: L.GB_HEFF_AC2}.get(kind, kind)
+        self.generic = kind in (L.GB_HEFF_AC_MPO, L.GB_HEFF_AC2_MPO)
         self.backend = backend
         h = ctypes.c_void_p()
         L.check(L.lib().gb_heff_build(ctx.handle, kind, GL.handle,
@@ -60,9 +64,9 @@ class DerivativeOperator:
         self._sectors = None
         self.dtype = GL.dtype
         Dl, Dr = GL.dims[0], GR.dims[0]
-        if kind == L.GB_HEFF_AC2:
+        if self.kind == L.GB_HEFF_AC2:
             self.xkind, self.xdims = L.GB_KIND_AC2, (Dl, W1.dims[1], Dr, W2.dims[1])
-        elif kind == L.GB_HEFF_AC:
+        elif self.kind == L.GB_HEFF_AC:
             self.xkind, self.xdims = L.GB_KIND_MPS, (Dl, W1.dims[1], Dr)
         else:
             self.xkind, self.xdims = L.GB_KIND_BOND, (Dl, Dr)
@@ -72,6 +76,12 @@ class DerivativeOperator:
         buf = ctypes.create_string_buffer(256)
         L.check(L.lib().gb_heff_terms(self.handle, buf, 256))
         return tuple(t for t in buf.value.decode().split(",") if t)
+
+    def describe(self):
+        """Per-step contraction shapes and grouped sector-block plans (gb_heff_describe)."""
+        buf = ctypes.create_string_buffer(1 << 16)
+        L.check(L.lib().gb_heff_describe(self.handle, buf, 1 << 16))
+        return buf.value.decode()
 
     @property
     def flops(self):
@@ -135,6 +145,20 @@ def AC_hamiltonian(site, psi, H, envs, backend=None):
     W = H.device(ctx, envs.dtype)
     return DerivativeOperator(ctx, L.GB_HEFF_AC, envs.leftenv(site, psi), W[site], None,
                               envs.rightenv(site, psi), backend)
+
+
+def MPO_AC_Hamiltonian(GL, W, GR, backend=None):
+    """MPO_AC_Hamiltonian(GL, W, GR) of an arbitrary MPO tensor (mpo_derivatives.jl:46-55,
+    100-107): y = GL . x . W . GR over every channel pair."""
+    return DerivativeOperator(GL.ctx, L.GB_HEFF_AC_MPO, GL, W, None, GR,
+                              backend or GB300Backend())
+
+
+def MPO_AC2_Hamiltonian(GL, W1, W2, GR, backend=None):
+    """MPO_AC2_Hamiltonian(GL, W1, W2, GR) of an arbitrary MPO (mpo_derivatives.jl:56-66,
+    144-153)."""
+    return DerivativeOperator(GL.ctx, L.GB_HEFF_AC2_MPO, GL, W1, W2, GR,
+                              backend or GB300Backend())
 
 
 def C_hamiltonian(site, psi, H, envs, backend=None):

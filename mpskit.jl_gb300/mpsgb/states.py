@@ -123,6 +123,38 @@ def project_complement_(Y, X):
     return Y
 
 
+def project_complement_right_(Y, X):
+    """Y <- Y (1 - X' X) on the last two legs (X with orthonormal rows, e.g. AR)."""
+    L.check(L.lib().gb_project_complement_right(Y.ctx.handle, Y.handle, X.handle))
+    return Y
+
+
+def mps_cat(A, B, leg, nb=None):
+    """A (+) B along virtual leg 0 or 2 (catcodomain / catdomain); B = None appends `nb`
+    zero rows / columns."""
+    n = B.dims[leg] if B is not None else int(nb)
+    dims = list(A.dims)
+    dims[leg] += n
+    out = DeviceTensor(A.ctx, L.GB_KIND_MPS, A.dtype, dims)
+    L.check(L.lib().gb_mps_cat(A.ctx.handle, A.handle, B.handle if B is not None else None,
+                               leg, out.handle))
+    return out
+
+
+def perturb(env, W, AC, side, precision=L.GB_PREC_FP64):
+    """The DMRG3S perturbation (gb_mps_perturb): side 0 with GL -> (Dl, d, Dr * wr),
+    side 1 with GR -> (Dl * wl, d, Dr)."""
+    Dl, d, Dr = AC.dims
+    if side == 0:
+        dims = (env.dims[0], d, Dr * W.dims[3])
+    else:
+        dims = (Dl * W.dims[0], d, env.dims[2])
+    out = DeviceTensor(AC.ctx, L.GB_KIND_MPS, np.result_type(AC.dtype, env.dtype), dims)
+    L.check(L.lib().gb_mps_perturb(AC.ctx.handle, side, env.handle, W.handle, AC.handle,
+                                   precision, out.handle))
+    return out
+
+
 def bond_dims(L_, d, D):
     V = [1] * (L_ + 1)
     for k in range(1, L_):

@@ -321,13 +321,18 @@ class CHam:
 def transfer_left(GL, W, A, Ab):
     """transfer_left(x, O, A, Ab) (transfer.jl:125-127):
     y[-1 -2;-3] = x[1 2;4] A[4 5;-3] O[2 3;5 -2] conj(Ab[1 3;-1])."""
-    return np.einsum("pwq,qtb,wstv,psa->avb", GL, A, W, Ab.conj(), optimize=True)
+    # as three pairwise contractions (a four-operand einsum can fall back to a naive loop)
+    T1 = np.tensordot(GL, A, axes=([2], [0]))                # (p, w, t, b)
+    T2 = np.tensordot(T1, W, axes=([1, 2], [0, 2]))          # (p, b, s, v)
+    return np.tensordot(Ab.conj(), T2, axes=([0, 1], [0, 2])).transpose(0, 2, 1)  # (a, v, b)
 
 
 def transfer_right(GR, W, A, Ab):
     """transfer_right(v, O, A, Ab) (transfer.jl:128-130):
     v[-1 -2;-3] = A[-1 2;1] O[-2 4;2 3] conj(Ab[-3 4;5]) v[1 3;5]."""
-    return np.einsum("atq,wstv,bsr,qvr->awb", A, W, Ab.conj(), GR, optimize=True)
+    T1 = np.tensordot(A, GR, axes=([2], [0]))                # (a, t, v, r)
+    T2 = np.tensordot(T1, W, axes=([1, 2], [2, 3]))          # (a, r, w, s)
+    return np.tensordot(T2, Ab.conj(), axes=([3, 1], [1, 2]))  # (a, w, b)
 
 
 def contract_mpo_expval(AC, GL, W, GR):

@@ -210,3 +210,64 @@ def test_launch_trace_accounts_every_launch(ctx):
     assert 0 < sum(ev for _, _, ev in sites) <= launches
     assert all(":" in nm and nm.split(":")[0].endswith(".cu") for nm, _, _ in sites)
     assert abs(sum(ms for _, ms, _ in sites) - span) <= 1e-3 * max(span, 1.0) + 1e-3
+
+
+# ------------------------------------------------------------------ generic MPO operators
+# MPO_AC_Hamiltonian / MPO_AC2_Hamiltonian of an arbitrary MPO (mpo_derivatives.jl:46-66,
+# 100-107, 144-153): dense W with no Jordan structure, every channel pair contracted.
+
+def _generic_case(rng, dt, D=24, wl=3, wm=4, wr=3, d=2):
+    GL = _rand(rng, (D, wl, D), dt)
+    GR = _rand(rng, (D + 4, wr, D + 4), dt)
+    W1 = _rand(rng, (wl, d, d, wm), dt)
+    W2 = _rand(rng, (wm, d, d, wr), dt)
+    return GL, W1, W2, GR
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex128])
+@pytest.mark.parametrize("prec,tol", [("fp64", FP64_TOL), ("bf16x3", SPLIT_TOL)])
+def test_generic_mpo_ac2(ctx, dt, prec, tol):
+    if prec != "fp64" and dt == np.complex128:
+        pytest.skip("split precision contracts real data")
+    rng = np.random.default_rng(31)
+    GL, W1, W2, GR = _generic_case(rng, dt)
+    op = dev_op(ctx, L.GB_HEFF_AC2_MPO, GL, W1, W2, GR, prec)
+    assert op.terms == ("AA",)
+    x = _rand(rng, (GL.shape[0], 2, GR.shape[0], 2), dt)
+    y = op(mpsgb.DeviceTensor.from_numpy(ctx, "ac2", x)).numpy()
+    assert _rel(y, dv.mpo_ac2_apply(GL, W1, W2, GR, x)) < tol
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex128])
+@pytest.mark.parametrize("prec,tol", [("fp64", FP64_TOL), ("bf16x3", SPLIT_TOL)])
+def test_generic_mpo_ac(ctx, dt, prec, tol):
+    if prec != "fp64" and dt == np.complex128:
+        pytest.skip("split precision contracts real data")
+    rng = np.random.default_rng(32)
+    GL, W1, _, GR = _generic_case(rng, dt, wr=4)
+    op = dev_op(ctx, L.GB_HEFF_AC_MPO, GL, W1, None, GR, prec)
+    assert op.terms == ("A",)
+    x = _rand(rng, (GL.shape[0], 2, GR.shape[0]), dt)
+    y = op(mpsgb.DeviceTensor.from_numpy(ctx, "mps", x)).numpy()
+    assert _rel(y, dv.mpo_ac_apply(GL, W1, GR, x)) < tol
+
+
+def test_generic_form_of_a_hamiltonian_equals_the_jordan_form(ctx):
+    """On a Jordan-form Hamiltonian MPO the generic operator (all channel pairs) and the
+    prepared Jordan operator are the same linear map."""
+    L_, terms, dt = MODELS["j1j2_r"]()
+    H, psi, envs = _envs(L_, terms, dt, 12, 23)
+    rng = np.random.default_rng(7)
+    pos = 5
+    GL, GR = envs.leftenv(pos, psi), envs.rightenv(pos + 1, psi)
+    x = _rand(rng, (GL.shape[0], 2, GR.shape[0], 2), dt)
+    xd = mpsgb.DeviceTensor.from_numpy(ctx, "ac2", x)
+    yj = dev_op(ctx, L.GB_HEFF_AC2, GL, H[pos], H[pos + 1], GR)(xd).numpy()
+    yg = dev_op(ctx, L.GB_HEFF_AC2_MPO, GL, H[pos], H[pos + 1], GR)(xd).numpy()
+    assert _rel(yg, yj) < FP64_TOL
+    GR1 = envs.rightenv(pos, psi)
+    x1 = _rand(rng, (GL.shape[0], 2, GR1.shape[0]), dt)
+    x1d = mpsgb.DeviceTensor.from_numpy(ctx, "mps", x1)
+    yj = dev_op(ctx, L.GB_HEFF_AC, GL, H[pos], None, GR1)(x1d).numpy()
+    yg = dev_op(ctx, L.GB_HEFF_AC_MPO, GL, H[pos], None, GR1)(x1d).numpy()
+    assert _rel(yg, yj) < FP64_TOL
