@@ -61,6 +61,9 @@ def parse():
                          "source site (gb_ctx_trace_begin/end)")
     ap.add_argument("--seed", type=int, default=1234 + 5)
     ap.add_argument("--svd", default="gram", choices=["gesvd", "gesvdp", "gram"])
+    ap.add_argument("--eig", default="syevd", choices=["syevd", "syevj"],
+                    help="eigensolver of the Gram factorisations")
+    ap.add_argument("--lanes", type=int, default=8, help="host-thread lanes of the gauge step")
     ap.add_argument("--symmetry", default="u1", choices=["u1", "none"],
                     help="u1: U(1) (total Sz = 0) block-sparse state and MPO; none: dense")
     ap.add_argument("--workload", default="dmrg2",
@@ -308,6 +311,7 @@ def run_ours(args):
     prec = args.precision
     ctx.set_precision(prec)
     ctx.set_svd_method(args.svd)
+    ctx.set_gauge(args.eig, args.lanes)
     ctx.set_gemm_schedule(args.schedule, args.tile_n)
     backend = mpsgb.GB300Backend(prec, local)
     u1 = args.symmetry == "u1"
@@ -483,7 +487,7 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if prec == "fp64" else "f64 (bf16x3 split contractions)",
+            "dtype": "f64" if prec == "fp64" else f"f64 ({prec} split contractions)",
             "data": "synthetic",
             "config": {
                 "workload": f"J1-J2 Heisenberg {args.Ly}x{args.Lx} cylinder ({n} sites), DMRG2 "
@@ -492,7 +496,8 @@ def run_ours(args):
                 "symmetry": args.symmetry,
                 "model": "J1=1, J2=0.5, snake order", "D": D, "L": n,
                 "mpo_width_at_bond": int(H.W[pos].shape[3]), "precision": prec,
-                "svd": args.svd, "tile_n": args.tile_n or "per shape",
+                "svd": args.svd, "eig": args.eig, "lanes": args.lanes,
+                "tile_n": args.tile_n or "per shape",
                 "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (GL/GR/T1 >> 129 MB)",
             },
             "gpu_launches": launches,
@@ -787,6 +792,7 @@ def run_dmrg2_sweep(args):
     prec = args.precision
     ctx.set_precision(prec)
     ctx.set_svd_method(args.svd)
+    ctx.set_gauge(args.eig, args.lanes)
     ctx.set_gemm_schedule(args.schedule, args.tile_n)
     backend = mpsgb.GB300Backend(prec, 0)
     H = mpsgb.j1j2_cylinder(args.Lx, args.Ly, dtype=np.float64, u1=True)

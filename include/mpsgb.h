@@ -325,6 +325,18 @@ enum {
                          diagonal; the truncated state AL S AR is the same.           */
 };
 int gb_ctx_set_svd_method(gb_ctx* ctx, int method);
+/* Gauge-step options: the Hermitian eigensolver of the Gram route (GB_EIG_SYEVD: cuSOLVER
+ * divide and conquer, the default; GB_EIG_SYEVJ: cuSOLVER cyclic Jacobi at machine-accuracy
+ * tolerance, all on the device) and the number of host-thread lanes (1..32, default 8) over
+ * which the per-sector factorisations of a U(1) tensor are spread. */
+enum { GB_EIG_SYEVD = 0, GB_EIG_SYEVJ = 1 };
+int gb_ctx_set_gauge(gb_ctx* ctx, int eig_method, int lanes);
+/* Implementation switches that leave every result unchanged (for comparisons):
+ *   GB_OPT_STAGED_MIX (default 1): the U(1) chain mix of the grouped schedule stages the
+ *   inputs of each charge's rows through shared memory (0: one warp per output row and
+ *   column reading the intermediate directly); both sum in the same order. */
+enum { GB_OPT_STAGED_MIX = 0 };
+int gb_ctx_set_option(gb_ctx* ctx, int option, int64_t value);
 /* Truncated SVD of a two-site tensor, gauge2! (src/states/orthoview.jl:401-420) with
  * truncrank(maxdim) & trunctol(atol): AL[l s1; k], S (GB_KIND_BOND k x k: diagonal, or
  * triangular under GB_SVD_GRAM),

@@ -517,18 +517,11 @@ bool svd_trunc_gram(gb_ctx* ctx, const gb_tensor* AC2, int64_t maxdim, double at
     gemm_fp64(ctx, dt, 'N', 'C', m, m, n, cplx{1, 0}, M, m, 0, M, m, 0, cplx{0, 0}, G, m, 0, 1);
   double* lam = (double*)scratch(ctx, SLOT_KRYLOV_W, sizeof(double) * (2 * g + 64) + 4096);
   double* sig = lam + g + 32;
-  size_t dws = 0, hws = 0;
-  CUSOLVER_CHECK(cusolverDnXsyevd_bufferSize(h, (cusolverDnParams_t)ctx->solver_params,
-                                             CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, g, t,
-                                             G, g, CUDA_R_64F, lam, t, &dws, &hws));
-  char* dw = (char*)scratch(ctx, SLOT_TMP, dws + 512);
-  int* dinfo = (int*)(dw + ((dws + 255) & ~size_t(255)));
-  std::vector<char> hw(hws + 1);
-  CUSOLVER_CHECK(cusolverDnXsyevd(h, (cusolverDnParams_t)ctx->solver_params,
-                                  CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, g, t, G, g,
-                                  CUDA_R_64F, lam, t, dw, dws, hw.data(), hws, dinfo));
+  (void)h;
+  (void)t;
+  int* dinfo = (int*)scratch(ctx, SLOT_TMP2, 256);
+  sym_eig(ctx, dt, g, G, lam, dinfo);
   GB_TRACE(ctx);
-  count_launch(ctx);
   sqrt_reverse_kernel<<<64, 256, 0, ctx->stream>>>(g, lam, sig);
   GB_CHECK_CUDA(cudaGetLastError());
   count_launch(ctx);
@@ -802,7 +795,7 @@ struct LanePool {
 
 void run_on_lanes_at(gb_ctx* ctx, int64_t n, const char* file, int line,
                      const std::function<void(gb_ctx*, int64_t)>& fn) {
-  const int K = (int)std::min<int64_t>(n, 8);
+  const int K = (int)std::min<int64_t>(n, ctx->lane_max);
   if (K <= 1) {
     for (int64_t i = 0; i < n; ++i) fn(ctx, i);
     return;
@@ -817,6 +810,7 @@ void run_on_lanes_at(gb_ctx* ctx, int64_t n, const char* file, int line,
   for (int k = 0; k < K; ++k) {
     gb_ctx* l = ctx->lanes[k];
     l->svd_method = ctx->svd_method;
+    l->eig_method = ctx->eig_method;
     l->aux_prec = ctx->aux_prec;
     l->gemm_schedule = ctx->gemm_schedule;
     l->gemm_bn = ctx->gemm_bn;
@@ -962,6 +956,26 @@ int gb_ctx_set_svd_method(gb_ctx* ctx, int method) {
   GB_REQUIRE(method == GB_SVD_GESVD || method == GB_SVD_GESVDP || method == GB_SVD_GRAM,
              "unknown SVD method");
   ctx->svd_method = method;
+  API_END
+}
+
+int gb_ctx_set_option(gb_ctx* ctx, int option, int64_t value) {
+  API_BEGIN
+  GB_REQUIRE(ctx, "null context");
+  switch (option) {
+    case GB_OPT_STAGED_MIX: ctx->staged_mix = value != 0; break;
+    default: throw Error(GB_ERR_ARG, "unknown option");
+  }
+  API_END
+}
+
+int gb_ctx_set_gauge(gb_ctx* ctx, int eig_method, int lanes) {
+  API_BEGIN
+  GB_REQUIRE(ctx, "null context");
+  GB_REQUIRE(eig_method == GB_EIG_SYEVD || eig_method == GB_EIG_SYEVJ, "unknown eigensolver");
+  GB_REQUIRE(lanes >= 1 && lanes <= 32, "lanes must be in 1..32");
+  ctx->eig_method = eig_method;
+  ctx->lane_max = lanes;
   API_END
 }
 

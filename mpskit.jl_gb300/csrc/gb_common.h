@@ -82,6 +82,9 @@ struct gb_ctx {
   int num_sms = 0;
   int aux_prec = GB_PREC_FP64;   // precision of auxiliary state contractions
   int svd_method = 0;            // GB_SVD_* of gb_svd_trunc
+  int eig_method = 0;            // GB_EIG_* of the Gram eigenproblems
+  int lane_max = 8;              // host-thread lanes for per-sector work
+  bool staged_mix = true;        // the grouped chain mix staged through shared memory
   // split-precision GEMM schedule (GB_SCHED_*) and output tile width (0 = chosen per shape)
   int gemm_schedule = GB_SCHED_GROUPED;
   int gemm_bn = 0;
@@ -304,6 +307,11 @@ void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_
                 int64_t N, double alpha, double beta, void* C, int64_t ldc, int64_t sC,
                 uint32_t* outmap = nullptr, bool c_f32 = false);
 bool tc_available(gb_ctx* ctx);
+
+// Hermitian eigendecomposition of the g x g matrix G in place (eigenvectors overwrite G,
+// eigenvalues ascending in W), by the context's GB_EIG_* method; *info (device) is nonzero on
+// failure.  Synchronises the context's stream before returning.
+void sym_eig(gb_ctx* ctx, int dtype, int64_t g, void* G, double* W, int* info);
 
 // Unified GEMM: dispatches on precision; optional pre-packed operands.
 void gemm(gb_ctx* ctx, int prec, int dtype, char opA, char opB, int64_t M, int64_t N,

@@ -72,7 +72,7 @@ std::vector<int32_t> leg_labels(const std::vector<LegSpec>& legs,
 }
 
 void gplan_build(GPlan& p, const std::vector<int32_t>& labM, const std::vector<int32_t>& labK,
-                 const std::vector<int32_t>& labN, bool first_writer, int64_t ldc) {
+                 const std::vector<int32_t>& labN, bool first_writer, int64_t ldc, int sms) {
   p = GPlan();
   std::map<int32_t, int> cntM, cntN, cntK;
   for (int32_t v : labM)
@@ -144,10 +144,45 @@ void gplan_build(GPlan& p, const std::vector<int32_t>& labM, const std::vector<i
         t.mlim = p.side[sa].gstart[g + 1];
         t.nlim = p.side[sb].gstart[g + 1];
         t.g = g;
-        t.pad = 0;
+        t.kb0 = 0;
+        t.nsplit = 1;
+        t.sid = 0;
+        t.pslot = -1;
+        t.cslot = -1;
         p.tiles.push_back(t);
         p.tile_flops += 2.0 * G_BM * (double)t.nw * (double)p.kpad[g];
       }
+  }
+  // split K: a tile longer than the target runs as several units, so that the long tiles
+  // of a plan with few tiles still spread over every multiprocessor
+  {
+    int64_t total = 0;
+    for (const GTile& t : p.tiles) total += t.nkb;
+    const int64_t target = std::max<int64_t>(8, (total + 2 * sms - 1) / (2 * std::max(sms, 1)));
+    std::vector<GTile> units;
+    for (const GTile& t : p.tiles) {
+      if (t.nkb <= target + target / 2) {
+        units.push_back(t);
+        continue;
+      }
+      const int ns = (int)((t.nkb + target - 1) / target);
+      const int per = (t.nkb + ns - 1) / ns;
+      int kb = 0, sid = 0;
+      const int first = p.nslots;
+      for (; kb < t.nkb; kb += per, ++sid) {
+        GTile u = t;
+        u.kb0 = kb;
+        u.nkb = std::min(per, t.nkb - kb);
+        u.sid = sid;
+        u.pslot = first;
+        u.cslot = p.ncounters;
+        units.push_back(u);
+      }
+      for (size_t i = units.size() - sid; i < units.size(); ++i) units[i].nsplit = sid;
+      p.nslots += sid;
+      ++p.ncounters;
+    }
+    p.tiles.swap(units);
   }
   // longest tiles first: the persistent kernel hands them out in this order
   std::stable_sort(p.tiles.begin(), p.tiles.end(), [](const GTile& a, const GTile& b) {
@@ -202,6 +237,9 @@ void gplan_upload(gb_ctx* ctx, GPlan& p, const std::function<void*(size_t)>& all
   const size_t o_kd = b.add(p.kdense.data(), p.kdense.size() * 4);
   const size_t o_ks = b.add(p.kstart.data(), p.kstart.size() * 4);
   const size_t o_kl = b.add(klen.data(), klen.size() * 4);
+  const size_t arrive_bytes = (size_t)std::max(p.ncounters, 1) * sizeof(unsigned int);
+  const size_t o_cnt = (b.h.size() + 255) / 256 * 256;
+  b.h.resize(o_cnt + arrive_bytes, 0);  // zeroed: every counter starts at 0
   char* d = (char*)alloc(b.h.size());
   p.dev = d;
   GB_CHECK_CUDA(cudaMemcpyAsync(d, b.h.data(), b.h.size(), cudaMemcpyHostToDevice, ctx->stream));
@@ -218,6 +256,10 @@ void gplan_upload(gb_ctx* ctx, GPlan& p, const std::function<void*(size_t)>& all
   p.d_kdense = (int32_t*)(d + o_kd);
   p.d_kstart = (int32_t*)(d + o_ks);
   p.d_klen = (int32_t*)(d + o_kl);
+  p.d_arrive = (unsigned int*)(d + o_cnt);
+  p.d_partial = nullptr;
+  if (p.nslots > 0)
+    p.d_partial = (float*)alloc((size_t)p.nslots * G_BM * G_BN * sizeof(float));
 }
 
 size_t goperand_bytes(const GPlan& p, int side, int prec) {
@@ -278,15 +320,21 @@ __global__ void label_violation_kernel(const double* __restrict__ src, int64_t R
                                        const int32_t* __restrict__ labK,
                                        unsigned long long* bad) {
   unsigned long long c = 0;
-  const int64_t n = R * K;
-  // walk the operand in memory order: consecutive threads read consecutive addresses
+  // blocks over the slow index, threads over the fast one: consecutive threads read
+  // consecutive addresses, no index division
   const bool rfast = rs == 1;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r = rfast ? i % R : i / K, k = rfast ? i / R : i % K;
-    if (src[r * rs + k * ks] == 0.0) continue;
-    const int32_t a = labR[r], b = labK[k];
-    c += (a == NO_LABEL || b == NO_LABEL || a != b);
+  const int64_t F = rfast ? R : K, S = rfast ? K : R;
+  const int64_t fstr = rfast ? rs : ks, sstr = rfast ? ks : rs;
+  const int32_t* labF = rfast ? labR : labK;
+  const int32_t* labS = rfast ? labK : labR;
+  for (int64_t sl = blockIdx.x; sl < S; sl += gridDim.x) {
+    const int32_t b = labS[sl];
+    const double* col = src + sl * sstr;
+    for (int64_t f = threadIdx.x; f < F; f += blockDim.x) {
+      if (col[f * fstr] == 0.0) continue;
+      const int32_t a = labF[f];
+      c += (a == NO_LABEL || b == NO_LABEL || a != b);
+    }
   }
   for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
   if ((threadIdx.x & 31) == 0 && c) atomicAdd(bad, c);
@@ -350,7 +398,8 @@ int64_t label_violations(gb_ctx* ctx, const double* src, int64_t R, int64_t K, i
   GB_CHECK_CUDA(cudaMemcpyAsync(d + R, labK.data(), K * sizeof(int32_t), cudaMemcpyHostToDevice,
                                 ctx->stream));
   unsigned long long* cnt = nnz_counter(ctx);
-  const unsigned grid = (unsigned)std::min<int64_t>((R * K + 255) / 256, 152 * 16);
+  const int64_t slow = rs == 1 ? K : R;
+  const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(slow, 152 * 16));
   label_violation_kernel<<<grid, 256, 0, ctx->stream>>>(src, R, K, rs, ks, d, d + R, cnt);
   GB_CHECK_CUDA(cudaGetLastError());
   count_launch(ctx);
@@ -416,6 +465,72 @@ void gmix_run(gb_ctx* ctx, const MixDev& m, const GMixEntry* ent, int64_t span_m
   count_launch(ctx);
 }
 
+template <typename E>
+__global__ void gmix_staged_kernel(int NL, int64_t nJ, int64_t xn, const int64_t* __restrict__ in_off,
+                                   const int* __restrict__ row_ptr, const int* __restrict__ lcol,
+                                   const double* __restrict__ val, const float* __restrict__ x,
+                                   const GMixEntry* __restrict__ ent, const int2* __restrict__ rng,
+                                   const int* __restrict__ jlist, const int* __restrict__ jstart,
+                                   const int* __restrict__ ilist, const int* __restrict__ istart,
+                                   int chunk, E* __restrict__ hi, int64_t plane, int64_t kmax) {
+  extern __shared__ float stage[];
+  const int g = blockIdx.y;
+  const int64_t n = blockIdx.x;
+  const int2 r = rng[n * NL + g];
+  if (r.y <= r.x) return;
+  const int i0 = istart[g], ni = istart[g + 1] - i0;
+  const int j0 = jstart[g], nj = jstart[g + 1] - j0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  E* lo = hi + plane;
+  for (int a0 = r.x; a0 < r.y; a0 += chunk) {
+    const int w = min(chunk, r.y - a0);
+    for (int idx = threadIdx.x; idx < ni * w; idx += blockDim.x) {
+      const int i = idx / w, a = idx - i * w;
+      stage[idx] = x[(int64_t)(a0 + a) + in_off[ilist[i0 + i]] + n * xn];
+    }
+    __syncthreads();
+    for (int jj = warp; jj < nj; jj += nw) {
+      const int J = jlist[j0 + jj];
+      const GMixEntry en = ent[n * nJ + J];
+      if (en.row < 0) continue;
+      const int64_t base = (int64_t)en.row * kmax + en.kst - en.lo;
+      const int e0 = row_ptr[J], e1 = row_ptr[J + 1];
+      for (int a = lane; a < w; a += 32) {
+        double acc = 0.0;
+        for (int e = e0; e < e1; ++e) acc = fma(val[e], (double)stage[lcol[e] * w + a], acc);
+        split_put(hi, lo, base + a0 + a, acc);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+void gmix_staged_run(gb_ctx* ctx, const MixDev& m, const GMixStaged& g, const GMixEntry* ent,
+                     const float* t1, GOperand& out) {
+  GB_REQUIRE(!m.cplx && m.xa == 1, "grouped mix: real data with unit input stride");
+  GB_REQUIRE(g.NL <= 65535 && m.N <= 0x7fffffff, "grouped mix: grid too large");
+  dim3 grid((unsigned)m.N, (unsigned)g.NL);
+  const int64_t plane = out.rows * out.kmax;
+  static std::once_flag attr_once;
+  std::call_once(attr_once, [] {
+    cudaFuncSetAttribute(gmix_staged_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         96 * 1024);
+    cudaFuncSetAttribute(gmix_staged_kernel<__nv_bfloat16>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+  });
+  GB_REQUIRE(g.smem <= 96 * 1024, "grouped mix: staging buffer too large");
+  if (out.esz == 4)
+    gmix_staged_kernel<float><<<grid, 256, g.smem, ctx->stream>>>(
+        g.NL, m.nJ, m.xn, m.in_off, m.row_ptr, g.lcol, m.val, t1, ent, g.rng, g.jlist, g.jstart,
+        g.ilist, g.istart, g.chunk, (float*)out.data, plane, out.kmax);
+  else
+    gmix_staged_kernel<__nv_bfloat16><<<grid, 256, g.smem, ctx->stream>>>(
+        g.NL, m.nJ, m.xn, m.in_off, m.row_ptr, g.lcol, m.val, t1, ent, g.rng, g.jlist, g.jstart,
+        g.ilist, g.istart, g.chunk, (__nv_bfloat16*)out.data, plane, out.kmax);
+  GB_CHECK_CUDA(cudaGetLastError());
+  count_launch(ctx);
+}
+
 // ------------------------------------------------------------------ the grouped kernel
 struct GArgs {
   const GTile* tiles;
@@ -430,6 +545,8 @@ struct GArgs {
   int* status;
   unsigned long long wait_ns;
   double* work;
+  float* partial;         // split-K partial sums [slot][G_BN][128]
+  unsigned int* arrive;   // split-K arrival counters
 };
 
 template <int STAGES>
@@ -458,8 +575,11 @@ __global__ void __launch_bounds__(G_THREADS, 1)
   uint64_t* sfull = tempty + 2;          // [RING]    scheduler -> consumers
   uint64_t* sempty = sfull + G_RING;     // [RING]    consumers -> scheduler
   uint64_t* done = sempty + G_RING;      // [1]       all MMAs retired
-  int* stile = (int*)(done + 1);         // [RING]
+  uint64_t* ep1 = done + 1;              // [1]       split tile: 4 epilogue warps wrote
+  uint64_t* ep2 = ep1 + 1;               // [1]       split tile: arrival counted
+  int* stile = (int*)(ep2 + 1);          // [RING]
   uint32_t* tmem_slot = (uint32_t*)(stile + G_RING);
+  int* sflag = (int*)(tmem_slot + 1);    // split tile: units done before this one
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   if (threadIdx.x == 0) {
@@ -476,6 +596,8 @@ __global__ void __launch_bounds__(G_THREADS, 1)
       mbar_init(smem_u32(&sempty[r]), 5);  // MMA thread + 4 epilogue warps
     }
     mbar_init(smem_u32(done), 1);
+    mbar_init(smem_u32(ep1), 4);
+    mbar_init(smem_u32(ep2), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)&mapA) : "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"((unsigned long long)&mapB) : "memory");
@@ -521,10 +643,10 @@ __global__ void __launch_bounds__(G_THREADS, 1)
           const uint32_t sa = smem_u32(smem + s * STAGE_BYTES);
           const uint32_t fb = smem_u32(&full[s]);
           mbar_expect_tx(fb, bytes);
-          tma_load_3d(sa, &mapA, fb, kb * BKE, T.m0, planeA);
+          const int kx = (T.kb0 * KB_PER_PAD + kb) * BKE;
+          tma_load_3d(sa, &mapA, fb, kx, T.m0, planeA);
           for (int i = 0; i < nbox; ++i)
-            tma_load_3d(sa + A_BYTES + i * BOX_BYTES, &mapB, fb, kb * BKE, T.n0 + i * G_BOXN,
-                        planeB);
+            tma_load_3d(sa + A_BYTES + i * BOX_BYTES, &mapB, fb, kx, T.n0 + i * G_BOXN, planeB);
           ++g;
           ++issued;
         }
@@ -588,18 +710,16 @@ __global__ void __launch_bounds__(G_THREADS, 1)
     // ---------------- epilogue: TMEM -> registers -> C
     const int q = warp % 4;  // TMEM lane quarter accessible by this warp
     float* xb = xbuf + (warp - 2) * 32 * 33;
-    auto store = [&](int64_t e, double v) {
-      if (args.c_f32) {
-        float* p = (float*)args.C + e;
-        if (args.beta != 0.0) v = fma(args.beta, (double)*p, v);
-        *p = (float)v;
-      } else {
-        double* p = (double*)args.C + e;
-        if (args.beta != 0.0) v = fma(args.beta, *p, v);
-        *p = v;
-      }
+    const bool f32 = args.c_f32 != 0;
+    const double alpha = args.alpha, beta = args.beta;
+    auto loadC = [&](int64_t e) -> double {
+      return f32 ? (double)((const float*)args.C)[e] : ((const double*)args.C)[e];
     };
-    uint32_t acc = 0;
+    auto putC = [&](int64_t e, double v) {
+      if (f32) ((float*)args.C)[e] = (float)v;
+      else ((double*)args.C)[e] = v;
+    };
+    uint32_t acc = 0, nsp = 0;
     for (int j = 0;; ++j) {
       const int slot = j % G_RING;
       bool ok = mbar_wait_bounded(smem_u32(&sfull[slot]), (j / G_RING) & 1, args.status,
@@ -615,30 +735,33 @@ __global__ void __launch_bounds__(G_THREADS, 1)
       const bool rvalid = mr < T.mlim;
       const int64_t roff = rvalid ? args.rowoff[mr] : 0;
       const int64_t nend = std::min<int64_t>((int64_t)T.n0 + T.nw, T.nlim);
-      if (T.nkb == 0) {
-        // no K member in this group: C = beta * C over the tile
-        if (rvalid)
-          for (int64_t n = T.n0; n < nend; ++n) store(roff + args.coloff[n], 0.0);
-        continue;
-      }
-      const uint32_t buf = acc & 1;
-      ok = mbar_wait_bounded(smem_u32(&tfull[buf]), (acc >> 1) & 1, args.status, args.wait_ns);
-      ok = __all_sync(0xffffffffu, ok);
-      if (!ok) break;
-      tc_fence_after();
-#pragma unroll 1
-      for (int c0 = 0; c0 < T.nw; c0 += 32) {
-        uint32_t v[32];
-        const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + buf * G_BN + (uint32_t)c0;
-        TMEM_LD32(taddr, v);
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      // C (+)= alpha * v for 32 columns c0.. of this warp's 32 rows (v: lane = row); the
+      // beta * C terms are all loaded before any store, so their latencies overlap
+      auto store_chunk = [&](int c0, const uint32_t (&v)[32]) {
+        const int64_t nl = (int64_t)T.n0 + c0 + lane;
         if (!args.trans_store) {
-          if (rvalid) {
+          const int64_t myco = nl < nend ? args.coloff[nl] : 0;
 #pragma unroll
-            for (int jj = 0; jj < 32; ++jj) {
-              const int64_t n = (int64_t)T.n0 + c0 + jj;
-              if (n >= nend) break;
-              store(roff + args.coloff[n], args.alpha * (double)__uint_as_float(v[jj]));
+          for (int h = 0; h < 32; h += 16) {  // two halves: fewer live registers
+            int64_t co[16];
+            double val[16];
+#pragma unroll
+            for (int jj = 0; jj < 16; ++jj) {
+              co[jj] = __shfl_sync(0xffffffffu, myco, h + jj);
+              val[jj] = alpha * (double)__uint_as_float(v[h + jj]);
+            }
+            if (beta != 0.0 && rvalid) {
+              double cv[16];
+#pragma unroll
+              for (int jj = 0; jj < 16; ++jj)
+                cv[jj] = ((int64_t)T.n0 + c0 + h + jj < nend) ? loadC(roff + co[jj]) : 0.0;
+#pragma unroll
+              for (int jj = 0; jj < 16; ++jj) val[jj] = fma(beta, cv[jj], val[jj]);
+            }
+            if (rvalid) {
+#pragma unroll
+              for (int jj = 0; jj < 16; ++jj)
+                if ((int64_t)T.n0 + c0 + h + jj < nend) putC(roff + co[jj], val[jj]);
             }
           }
         } else {
@@ -647,17 +770,113 @@ __global__ void __launch_bounds__(G_THREADS, 1)
 #pragma unroll
           for (int jj = 0; jj < 32; ++jj) xb[lane * 33 + jj] = __uint_as_float(v[jj]);
           __syncwarp();
-          const int64_t n = (int64_t)T.n0 + c0 + lane;
-          const bool cvalid = n < nend;
-          const int64_t co = cvalid ? args.coloff[n] : 0;
-#pragma unroll 4
-          for (int i = 0; i < 32; ++i) {
-            const int64_t ro = __shfl_sync(0xffffffffu, roff, i);
-            if (cvalid && mrow0 + i < T.mlim)
-              store(ro + co, args.alpha * (double)xb[i * 33 + lane]);
+          const bool cvalid = nl < nend;
+          const int64_t co = cvalid ? args.coloff[nl] : 0;
+#pragma unroll
+          for (int h = 0; h < 32; h += 16) {
+            int64_t ro[16];
+            double val[16];
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+              ro[i] = __shfl_sync(0xffffffffu, roff, h + i);
+              val[i] = alpha * (double)xb[(h + i) * 33 + lane];
+            }
+            if (beta != 0.0 && cvalid) {
+              double cv[16];
+#pragma unroll
+              for (int i = 0; i < 16; ++i)
+                cv[i] = (mrow0 + h + i < T.mlim) ? loadC(ro[i] + co) : 0.0;
+#pragma unroll
+              for (int i = 0; i < 16; ++i) val[i] = fma(beta, cv[i], val[i]);
+            }
+            if (cvalid) {
+#pragma unroll
+              for (int i = 0; i < 16; ++i)
+                if (mrow0 + h + i < T.mlim) putC(ro[i] + co, val[i]);
+            }
           }
           __syncwarp();
         }
+      };
+      if (T.nkb == 0) {
+        // no K member in this group: C = beta * C over the tile
+        if (rvalid)
+          for (int64_t n = T.n0; n < nend; ++n) {
+            const int64_t e = roff + args.coloff[n];
+            putC(e, beta != 0.0 ? beta * loadC(e) : 0.0);
+          }
+        continue;
+      }
+      const uint32_t buf = acc & 1;
+      ok = mbar_wait_bounded(smem_u32(&tfull[buf]), (acc >> 1) & 1, args.status, args.wait_ns);
+      ok = __all_sync(0xffffffffu, ok);
+      if (!ok) break;
+      tc_fence_after();
+      if (T.nsplit > 1) {
+        // split K: every unit writes its partial sums to its slot ([column][row], lane = row);
+        // the last unit of the tile to finish adds all slots in unit order and stores
+        float* own = args.partial + (size_t)(T.pslot + T.sid) * (G_BM * G_BN);
+#pragma unroll 1
+        for (int c0 = 0; c0 < T.nw; c0 += 32) {
+          uint32_t v[32];
+          const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + buf * G_BN + (uint32_t)c0;
+          TMEM_LD32(taddr, v);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int jj = 0; jj < 32; ++jj)
+            own[(size_t)(c0 + jj) * G_BM + 32 * q + lane] = __uint_as_float(v[jj]);
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_u32(&tempty[buf]));
+        ++acc;
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_u32(ep1));
+        if (warp == 2 && lane == 0) {
+          bool w1 = mbar_wait_bounded(smem_u32(ep1), nsp & 1, args.status, args.wait_ns);
+          int before = -1;
+          if (w1) {
+            before = (int)atomicAdd(&args.arrive[T.cslot], 1u);
+            if (before == T.nsplit - 1) args.arrive[T.cslot] = 0;  // ready for the next launch
+            __threadfence();
+          }
+          *sflag = before;
+          mbar_arrive(smem_u32(ep2));
+        }
+        ok = mbar_wait_bounded(smem_u32(ep2), nsp & 1, args.status, args.wait_ns);
+        ok = __all_sync(0xffffffffu, ok);
+        ++nsp;
+        if (!ok) break;
+        const int before = *sflag;
+        if (before < 0) break;  // the arrival wait ran out: status already recorded
+        if (before != T.nsplit - 1) continue;
+        __threadfence();
+#pragma unroll 1
+        for (int c0 = 0; c0 < T.nw; c0 += 32) {
+          float sum[32];
+#pragma unroll
+          for (int jj = 0; jj < 32; ++jj) sum[jj] = 0.0f;
+          for (int u = 0; u < T.nsplit; ++u) {
+            const float* pu = args.partial + (size_t)(T.pslot + u) * (G_BM * G_BN) +
+                              (size_t)c0 * G_BM + 32 * q + lane;
+#pragma unroll
+            for (int jj = 0; jj < 32; ++jj) sum[jj] += __ldcg(pu + (size_t)jj * G_BM);
+          }
+          uint32_t v[32];
+#pragma unroll
+          for (int jj = 0; jj < 32; ++jj) v[jj] = __float_as_uint(sum[jj]);
+          store_chunk(c0, v);
+        }
+        continue;
+      }
+#pragma unroll 1
+      for (int c0 = 0; c0 < T.nw; c0 += 32) {
+        uint32_t v[32];
+        const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + buf * G_BN + (uint32_t)c0;
+        TMEM_LD32(taddr, v);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        store_chunk(c0, v);
       }
       tc_fence_before();
       __syncwarp();
@@ -700,6 +919,9 @@ void gemm_grouped(gb_ctx* ctx, const GPlan& p, const GOperand& A, const GOperand
   a.status = ctx->d_status;
   a.wait_ns = ctx->wait_ns;
   a.work = (ctx->profiling || ctx->counting) ? ctx->d_work : nullptr;
+  a.partial = p.d_partial;
+  a.arrive = p.d_arrive;
+  GB_REQUIRE(p.nslots == 0 || p.d_partial, "grouped GEMM: split-K buffers missing");
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   if (ctx->profiling) {
     if (ctx->prof_used + 2 > ctx->prof_events.size()) {
@@ -717,6 +939,11 @@ void gemm_grouped(gb_ctx* ctx, const GPlan& p, const GOperand& A, const GOperand
     GB_CHECK_CUDA(cudaEventRecord(ev0, ctx->stream));
   }
   GB_CHECK_CUDA(cudaMemsetAsync(ctx->d_tile_counter, 0, sizeof(unsigned int), ctx->stream));
+  // split-K arrival counters start at zero whatever an earlier (possibly cut short) launch
+  // left in them
+  if (p.ncounters > 0)
+    GB_CHECK_CUDA(cudaMemsetAsync(p.d_arrive, 0, (size_t)p.ncounters * sizeof(unsigned int),
+                                  ctx->stream));
   const unsigned grid = (unsigned)std::min<int64_t>((int64_t)p.tiles.size(),
                                                     std::max(1, ctx->num_sms));
 #define GB_GROUPED(ST_, TF_)                                                                  \

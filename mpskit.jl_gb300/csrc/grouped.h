@@ -34,10 +34,15 @@ std::vector<int32_t> leg_labels(const std::vector<LegSpec>& legs,
 
 struct GTile {
   int32_t m0, n0;      // first packed row of the tile in the kernel's A / B row space
-  int32_t nkb;         // K blocks of the tile's group (0: the tile only writes beta * C)
+  int32_t nkb;         // K blocks of this work unit (0: the tile only writes beta * C)
   int32_t nw;          // MMA N of the tile (multiple of 16, <= 256)
   int32_t mlim, nlim;  // end of the tile's group in the A / B row space (exclusive)
-  int32_t g, pad;
+  int32_t g;
+  int32_t kb0;         // first K block of the unit within its group
+  int32_t nsplit;      // units sharing the output tile (split K); 1: the whole K
+  int32_t sid;         // index of this unit among them
+  int32_t pslot;       // partial-sum slot of unit 0 of the tile (unit sid uses pslot + sid)
+  int32_t cslot;       // arrival counter of the tile
 };
 
 struct GPackTile {
@@ -74,6 +79,8 @@ struct GPlan {
   std::vector<GTile> tiles;
   double tile_flops = 0.0;      // tensor-pipe flops per split product (BF16 K-block count)
   double block_flops = 0.0;     // 2 sum_g M_g N_g K_g
+  int nslots = 0;               // partial-sum slots of the split-K units
+  int ncounters = 0;            // output tiles computed by more than one unit
   // device copies (one owned buffer)
   void* dev = nullptr;
   GTile* d_tiles = nullptr;
@@ -85,13 +92,19 @@ struct GPlan {
   int32_t* d_kdense = nullptr;
   int32_t* d_kstart = nullptr;
   int32_t* d_klen = nullptr;
+  float* d_partial = nullptr;       // [nslots][G_BN columns][128 rows] FP32 partial sums
+  unsigned int* d_arrive = nullptr; // [ncounters] units of a split tile done (reset to 0)
 };
 
 // Plan of C = A B with dense labels of M, K, N.  first_writer: the GEMM overwrites C
 // (beta = 0), so groups without K members still get tiles that write zeros.  ldc: leading
 // dimension of the column-major output (element offsets).
+// sms: multiprocessors of the device; a tile whose K is long against the plan's total work
+// per multiprocessor is split along K into units summed deterministically (in unit order)
+// by the last of them to finish.
 void gplan_build(GPlan& p, const std::vector<int32_t>& labM, const std::vector<int32_t>& labK,
-                 const std::vector<int32_t>& labN, bool first_writer, int64_t ldc);
+                 const std::vector<int32_t>& labN, bool first_writer, int64_t ldc,
+                 int sms = 152);
 // device buffers of the plan (allocated through alloc, one call)
 void gplan_upload(gb_ctx* ctx, GPlan& p, const std::function<void*(size_t)>& alloc);
 size_t goperand_bytes(const GPlan& p, int side, int prec);
@@ -116,6 +129,24 @@ struct GMixEntry {
 };
 void gmix_run(gb_ctx* ctx, const MixDev& m, const GMixEntry* ent, int64_t span_max,
               const float* t1, GOperand& out);
+// The same mix staged through shared memory.  The output rows J fall into groups whose
+// input range [lo, hi) is the same at every column n (rows of one charge); a block per
+// (column, group) loads the inputs its rows read -- once, coalesced -- and computes every
+// row of the group from shared memory, with the sums in the same order as gmix_run (the
+// results are identical).
+struct GMixStaged {
+  int NL = 0;              // row groups
+  int chunk = 0;           // input rows a staged per pass
+  size_t smem = 0;         // dynamic shared memory per block
+  const int2* rng = nullptr;    // [N][NL]: (lo, hi) of group g at column n
+  const int* jlist = nullptr;   // rows of group g: jlist[jstart[g] .. jstart[g + 1])
+  const int* jstart = nullptr;
+  const int* ilist = nullptr;   // inputs read by group g: ilist[istart[g] .. istart[g + 1])
+  const int* istart = nullptr;
+  const int* lcol = nullptr;    // per mix entry e: position of col[e] in its row's input list
+};
+void gmix_staged_run(gb_ctx* ctx, const MixDev& m, const GMixStaged& g, const GMixEntry* ent,
+                     const float* t1, GOperand& out);
 
 // C = alpha * (A B) + beta * C over the plan's tiles; c_f32: C holds FP32
 void gemm_grouped(gb_ctx* ctx, const GPlan& p, const GOperand& A, const GOperand& B,

@@ -19,6 +19,8 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstring>
+#include <map>
 #include <sstream>
 
 #include "gb_common.h"
@@ -48,6 +50,7 @@ struct Step {
   // MIX: dst (+)= mix(src)
   int src = S_X;
   MixDev mix;
+  MixPlan mixh;  // host copy of the plan (the chain mix only: its staged grouped form)
   std::string name;
   // the continuing-channel chain: the middle mix produces T2, the next GEMM consumes it;
   // in split precision the mix writes T2 directly as that GEMM's packed B operand
@@ -179,6 +182,8 @@ struct gb_heff {
   std::vector<int2> arange_h;    // host copy of arange
   std::vector<GStep> gsteps;     // index-aligned with steps
   gb::GMixEntry* gmix = nullptr;
+  gb::GMixStaged gmix_st;        // staged form of the same mix (gmix_st.NL > 0 when built)
+  std::vector<int64_t> lam_J;    // charge of every chain row J (INT64_MIN: channel absent)
   int t2_step = -1;              // the step that consumes T2
   bool gp_ready = false;
   bool prepacked = false;        // constants of the dense-embedding path packed
@@ -496,8 +501,8 @@ static void build_ac2(gb_heff* h, const gb_tensor* GL, const gb_tensor* W1,
     s2.name = "AA2";
     s2.src = S_T1;
     s2.dst = S_T2;
-    s2.mix = mix_upload(ctx, make_plan(cf, cx, Dl, Dr, 1, Dl * d1 * d2 * chc, 1,
-                                       Dl * chr * d1 * d2, io, oo));
+    s2.mixh = make_plan(cf, cx, Dl, Dr, 1, Dl * d1 * d2 * chc, 1, Dl * chr * d1 * d2, io, oo);
+    s2.mix = mix_upload(ctx, s2.mixh);
     s2.accumulate = false;
     s2.t2_producer = true;
     steps.push_back(s2);
@@ -944,7 +949,8 @@ static void build_ac(gb_heff* h, const gb_tensor* GL, const gb_tensor* W, const 
     s2.name = "A2";
     s2.src = S_T1;
     s2.dst = S_T2;
-    s2.mix = mix_upload(ctx, make_plan(cf, cx, Dl, Dr, 1, Dl * d * chc, 1, Dl * chr * d, io, oo));
+    s2.mixh = make_plan(cf, cx, Dl, Dr, 1, Dl * d * chc, 1, Dl * chr * d, io, oo);
+    s2.mix = mix_upload(ctx, s2.mixh);
     s2.accumulate = false;
     s2.t2_producer = true;
     steps.push_back(s2);
@@ -1323,6 +1329,7 @@ void heff_apply_compact(gb_heff* h, const void* x, void* y) {
   runs_copy(h, h->yfull, y, 0);
 }
 
+static void build_staged_mix(gb_heff* h, int64_t Dr);
 static void grouped_prepare(gb_heff* h);
 
 void heff_set_sectors(gb_heff* h, const int32_t* ql, const int32_t* qp1, const int32_t* qp2,
@@ -1440,6 +1447,9 @@ void heff_set_sectors(gb_heff* h, const int32_t* ql, const int32_t* qp1, const i
                                 cudaMemcpyHostToDevice, ctx->stream));
   GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
   h->arange_max = mx;
+  h->lam_J.assign(nJ, INT64_MIN);
+  for (int64_t J = 0; J < nJ; ++J)
+    if (dq[h->Jc[J]] != INT_MIN) h->lam_J[J] = (int64_t)dq[h->Jc[J]] + qp[h->Jp[J]];
   h->dq_l.assign(dq.begin(), dq.begin() + chr);
   h->arange_h = std::move(tab);
   grouped_prepare(h);
@@ -1573,7 +1583,7 @@ static void grouped_prepare(gb_heff* h) {
                    (int64_t)lN.size() == st.N,
                "grouped: labels do not match the GEMM shape of step " + st.name);
     GStep& gs = h->gsteps[i];
-    gplan_build(gs.plan, lM, lK, lN, !st.accumulate, st.ldc);
+    gplan_build(gs.plan, lM, lK, lN, !st.accumulate, st.ldc, std::max(1, ctx->num_sms));
     gplan_upload(ctx, gs.plan, alloc);
     for (int sd = 0; sd < 2; ++sd)
       goperand_init(ctx, gs.op[sd], gs.plan, sd, dalloc(h, goperand_bytes(gs.plan, sd, h->prec)),
@@ -1636,6 +1646,7 @@ static void grouped_prepare(gb_heff* h) {
     h->gmix = (GMixEntry*)dalloc(h, ent.size() * sizeof(GMixEntry));
     GB_CHECK_CUDA(cudaMemcpyAsync(h->gmix, ent.data(), ent.size() * sizeof(GMixEntry),
                                   cudaMemcpyHostToDevice, ctx->stream));
+    build_staged_mix(h, Dr);
     // T1 is read only inside its blocks; the entries no block writes stay zero
     GB_REQUIRE(h->t1, "grouped: T1 buffer missing");
     GB_CHECK_CUDA(cudaMemsetAsync(h->t1, 0, (size_t)h->t1_elems * elem_size(h->dtype),
@@ -1646,7 +1657,88 @@ static void grouped_prepare(gb_heff* h) {
   h->gp_ready = true;
 }
 
-// y = H x through the grouped plans.  x: dense embedding, zero outside the sectors; every
+// The staged form of the chain mix (gmix_staged_run): rows J of one charge form a group
+// whose input range is the same at every column; each group stages the inputs its rows
+// read.  Left unbuilt (the plain gmix_run is used) when a group's inputs do not fit the
+// staging buffer.
+static void build_staged_mix(gb_heff* h, int64_t Dr) {
+  using namespace gb;
+  h->gmix_st = GMixStaged();
+  const Step* mixstep = nullptr;
+  for (const Step& s : h->steps)
+    if (s.t2_producer) mixstep = &s;
+  if (!mixstep || h->lam_J.empty()) return;
+  const MixPlan& mp = mixstep->mixh;
+  const int64_t nJ = (int64_t)h->kJ.size();
+  if ((int64_t)mp.row_ptr.size() != nJ + 1 || (int64_t)h->lam_J.size() != nJ) return;
+  std::map<int64_t, std::vector<int>> byq;
+  for (int64_t J = 0; J < nJ; ++J)
+    if (h->lam_J[J] != INT64_MIN) byq[h->lam_J[J]].push_back((int)J);
+  const int NL = (int)byq.size();
+  if (NL == 0) return;
+  std::vector<int> jlist, jstart{0}, ilist, istart{0}, lcol(mp.col.size(), 0);
+  std::vector<int2> rng((size_t)Dr * NL);
+  int max_ni = 0;
+  int g = 0;
+  for (const auto& kv : byq) {
+    const std::vector<int>& Js = kv.second;
+    std::vector<int> ins;
+    for (int J : Js)
+      for (int e = mp.row_ptr[J]; e < mp.row_ptr[J + 1]; ++e) ins.push_back(mp.col[e]);
+    std::sort(ins.begin(), ins.end());
+    ins.erase(std::unique(ins.begin(), ins.end()), ins.end());
+    for (int J : Js)
+      for (int e = mp.row_ptr[J]; e < mp.row_ptr[J + 1]; ++e)
+        lcol[e] = (int)(std::lower_bound(ins.begin(), ins.end(), mp.col[e]) - ins.begin());
+    // one input range per (column, group): every row of the group must agree
+    for (int64_t n = 0; n < Dr; ++n) {
+      const int2 r0 = h->arange_h[(size_t)n * nJ + Js[0]];
+      for (int J : Js) {
+        const int2 r = h->arange_h[(size_t)n * nJ + J];
+        if (r.x != r0.x || r.y != r0.y) return;
+      }
+      rng[(size_t)n * NL + g] = r0;
+    }
+    jlist.insert(jlist.end(), Js.begin(), Js.end());
+    jstart.push_back((int)jlist.size());
+    ilist.insert(ilist.end(), ins.begin(), ins.end());
+    istart.push_back((int)ilist.size());
+    max_ni = std::max<int>(max_ni, (int)ins.size());
+    ++g;
+  }
+  const int64_t cap = 96 * 1024 / 4;  // floats of staging
+  int64_t chunk = std::min<int64_t>(std::max<int64_t>(h->arange_max, 1), cap / std::max(max_ni, 1));
+  if (chunk < 32 && chunk < h->arange_max) return;
+  chunk = std::max<int64_t>(chunk, 1);
+  // one device blob for the tables
+  std::vector<char> blob;
+  auto put = [&](const void* src, size_t bytes) {
+    const size_t off = (blob.size() + 255) / 256 * 256;
+    blob.resize(off + std::max<size_t>(bytes, 16), 0);
+    if (bytes) memcpy(blob.data() + off, src, bytes);
+    return off;
+  };
+  const size_t o_r = put(rng.data(), rng.size() * sizeof(int2));
+  const size_t o_jl = put(jlist.data(), jlist.size() * 4), o_js = put(jstart.data(), jstart.size() * 4);
+  const size_t o_il = put(ilist.data(), ilist.size() * 4), o_is = put(istart.data(), istart.size() * 4);
+  const size_t o_lc = put(lcol.data(), lcol.size() * 4);
+  char* d = (char*)dalloc(h, blob.size());
+  GB_CHECK_CUDA(cudaMemcpyAsync(d, blob.data(), blob.size(), cudaMemcpyHostToDevice,
+                                h->ctx->stream));
+  GB_CHECK_CUDA(cudaStreamSynchronize(h->ctx->stream));
+  GMixStaged& st = h->gmix_st;
+  st.rng = (const int2*)(d + o_r);
+  st.jlist = (const int*)(d + o_jl);
+  st.jstart = (const int*)(d + o_js);
+  st.ilist = (const int*)(d + o_il);
+  st.istart = (const int*)(d + o_is);
+  st.lcol = (const int*)(d + o_lc);
+  st.chunk = (int)chunk;
+  st.smem = (size_t)chunk * max_ni * 4;
+  st.NL = NL;
+}
+
+// y = H x through the grouped plans.// y = H x through the grouped plans.  x: dense embedding, zero outside the sectors; every
 // allowed entry of y is written (the first GEMM into y overwrites, the rest accumulate);
 // entries outside the sectors are zeroed only when y is not the operator's own staging
 // vector (whose outside entries are never read).
@@ -1665,8 +1757,12 @@ static void heff_apply_grouped(gb_heff* h, const void* x, void* y) {
                    t1 ? h->t1 : y, t1);
       if (ctx->counting) gcount_products(ctx, gs.plan, gs.op[0], gs.op[1]);
     } else if (st.t2_producer) {
-      gmix_run(ctx, st.mix, h->gmix, h->arange_max, (const float*)h->t1,
-               h->gsteps[h->t2_step].op[1]);
+      if (h->gmix_st.NL > 0 && ctx->staged_mix)
+        gmix_staged_run(ctx, st.mix, h->gmix_st, h->gmix, (const float*)h->t1,
+                        h->gsteps[h->t2_step].op[1]);
+      else
+        gmix_run(ctx, st.mix, h->gmix, h->arange_max, (const float*)h->t1,
+                 h->gsteps[h->t2_step].op[1]);
     } else {
       GB_REQUIRE(st.src == S_X && st.dst == S_Y, "grouped: unexpected mix step");
       mix_run(ctx, st.mix, h->dtype, x, y, st.accumulate ? 1.0 : 0.0);
@@ -1784,8 +1880,9 @@ std::string heff_describe(const gb_heff* h) {
         maxkb = std::max<int64_t>(maxkb, t.nkb);
         kb += t.nkb;
       }
-      os << " grouped G=" << p.G << " tiles=" << p.tiles.size() << " kblocks=" << kb
-         << " max_tile_kblocks=" << maxkb << " trans=" << (p.trans ? 1 : 0)
+      os << " grouped G=" << p.G << " units=" << p.tiles.size()
+         << " split_tiles=" << p.ncounters << " kblocks=" << kb
+         << " max_unit_kblocks=" << maxkb << " trans=" << (p.trans ? 1 : 0)
          << " block_gflop=" << p.block_flops * 1e-9 << " tile_gflop=" << p.tile_flops * 1e-9;
     }
     os << "\n";

@@ -253,22 +253,68 @@ void gram_eig_sector(gb_ctx* L, int dt, int64_t ni, int64_t nj, const void* M, v
     gemm_fp64(L, dt, 'C', 'N', g, g, ni, cplx{1, 0}, M, ni, 0, M, ni, 0, cplx{0, 0}, G.p, g, 0, 1);
   else
     gemm_fp64(L, dt, 'N', 'C', g, g, nj, cplx{1, 0}, M, ni, 0, M, ni, 0, cplx{0, 0}, G.p, g, 0, 1);
-  size_t dws = 0, hws = 0;
-  CUSOLVER_CHECK_U1(cusolverDnXsyevd_bufferSize(h, (cusolverDnParams_t)L->solver_params,
-                                                CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
-                                                g, t, G.p, g, CUDA_R_64F, W, t, &dws, &hws));
-  DevBuf dw(L, dws + 256);
-  std::vector<char> hw(hws + 1);
-  CUSOLVER_CHECK_U1(cusolverDnXsyevd(h, (cusolverDnParams_t)L->solver_params,
-                                     CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, g, t, G.p,
-                                     g, CUDA_R_64F, W, t, dw.p, dws, hw.data(), hws, info));
-  count_launch(L);
+  (void)h;
+  (void)t;
+  sym_eig(L, dt, g, G.p, W, info);
   int64_t dims[2] = {g, g}, ins[2] = {1, -g}, outs[2] = {1, g};
   permute(L, dt, 2, dims, G.as<char>() + (size_t)(g - 1) * g * es, ins, E, outs);
   GB_CHECK_CUDA(cudaStreamSynchronize(L->stream));  // hw and the buffers end with this scope
 }
 
 }  // namespace
+
+// ------------------------------------------------------------------ Hermitian eigensolver
+void sym_eig(gb_ctx* L, int dt, int64_t g, void* G, double* W, int* info) {
+  cusolverDnHandle_t h = (cusolverDnHandle_t)gauge_solver(L);
+  const bool cx = is_cplx(dt);
+  if (L->eig_method == GB_EIG_SYEVJ) {
+    // cyclic Jacobi, all on the device (no host stage): tolerance at machine accuracy,
+    // eigenvalues ascending like syevd
+    GB_REQUIRE(g < (int64_t)1 << 31, "syevj: matrix too large");
+    syevjInfo_t p = nullptr;
+    CUSOLVER_CHECK_U1(cusolverDnCreateSyevjInfo(&p));
+    int lwork = 0;
+    try {
+      CUSOLVER_CHECK_U1(cusolverDnXsyevjSetMaxSweeps(p, 100));
+      if (cx)
+        CUSOLVER_CHECK_U1(cusolverDnZheevj_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR,
+                                                      CUBLAS_FILL_MODE_LOWER, (int)g,
+                                                      (cuDoubleComplex*)G, (int)g, W, &lwork, p));
+      else
+        CUSOLVER_CHECK_U1(cusolverDnDsyevj_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR,
+                                                      CUBLAS_FILL_MODE_LOWER, (int)g, (double*)G,
+                                                      (int)g, W, &lwork, p));
+      DevBuf wk(L, (size_t)lwork * elem_size(dt) + 256);
+      if (cx)
+        CUSOLVER_CHECK_U1(cusolverDnZheevj(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+                                           (int)g, (cuDoubleComplex*)G, (int)g, W,
+                                           wk.as<cuDoubleComplex>(), lwork, info, p));
+      else
+        CUSOLVER_CHECK_U1(cusolverDnDsyevj(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+                                           (int)g, (double*)G, (int)g, W, wk.as<double>(), lwork,
+                                           info, p));
+      count_launch(L);
+      GB_CHECK_CUDA(cudaStreamSynchronize(L->stream));
+    } catch (...) {
+      cusolverDnDestroySyevjInfo(p);
+      throw;
+    }
+    cusolverDnDestroySyevjInfo(p);
+    return;
+  }
+  const cudaDataType t = cx ? CUDA_C_64F : CUDA_R_64F;
+  size_t dws = 0, hws = 0;
+  CUSOLVER_CHECK_U1(cusolverDnXsyevd_bufferSize(h, (cusolverDnParams_t)L->solver_params,
+                                                CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+                                                g, t, G, g, CUDA_R_64F, W, t, &dws, &hws));
+  DevBuf dw(L, dws + 256);
+  std::vector<char> hw(hws + 1);
+  CUSOLVER_CHECK_U1(cusolverDnXsyevd(h, (cusolverDnParams_t)L->solver_params,
+                                     CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, g, t, G, g,
+                                     CUDA_R_64F, W, t, dw.p, dws, hw.data(), hws, info));
+  count_launch(L);
+  GB_CHECK_CUDA(cudaStreamSynchronize(L->stream));  // hw and dw end with this scope
+}
 
 // ------------------------------------------------------------------ left_orth
 void u1_left_orth(gb_ctx* ctx, const gb_tensor* AC, const int32_t* ql, const int32_t* qs,

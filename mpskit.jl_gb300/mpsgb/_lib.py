@@ -120,6 +120,8 @@ _SIGS = {
     "gb_project_complement": ([P, P, P], INT),
     "gb_project_complement_right": ([P, P, P], INT),
     "gb_heff_describe": ([P, ctypes.c_char_p, ctypes.c_size_t], INT),
+    "gb_ctx_set_gauge": ([P, INT, INT], INT),
+    "gb_ctx_set_option": ([P, INT, ctypes.c_int64], INT),
     "gb_mps_perturb": ([P, INT, P, P, P, INT, P], INT),
     "gb_mps_cat": ([P, P, P, INT, P], INT),
     "gb_tensor_reshape": ([P, INT, INT, PI64], INT),

@@ -70,6 +70,16 @@ class Context:
         code = {"gesvd": 0, "gesvdp": 1, "gram": 2}[method]
         L.check(L.lib().gb_ctx_set_svd_method(self.handle, code))
 
+    def set_gauge(self, eig="syevd", lanes=8):
+        """Gauge-step options (gb_ctx_set_gauge): the Gram route's eigensolver ('syevd' or
+        'syevj') and the number of host-thread lanes for per-sector factorisations."""
+        L.check(L.lib().gb_ctx_set_gauge(self.handle, {"syevd": 0, "syevj": 1}[eig], int(lanes)))
+
+    def set_option(self, name, value):
+        """Implementation switches that leave results unchanged (gb_ctx_set_option):
+        'staged_mix'."""
+        L.check(L.lib().gb_ctx_set_option(self.handle, {"staged_mix": 0}[name], int(value)))
+
     def profile_begin(self):
         L.check(L.lib().gb_ctx_profile_begin(self.handle))
 

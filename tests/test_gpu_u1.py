@@ -321,3 +321,48 @@ def test_grouped_counts_the_same_nonzero_products(ctx):
     assert g["nonzero_flops"] > 0
     assert abs(g["nonzero_flops"] - p["nonzero_flops"]) <= 1e-9 * p["nonzero_flops"]
     assert g["tile_flops"] < p["tile_flops"]
+
+
+@pytest.mark.parametrize("prec", ["bf16x3", "tf32x3"])
+def test_staged_chain_mix_is_bitwise_the_plain_mix(ctx, prec):
+    """The grouped schedule's chain mix staged through shared memory (per column and charge
+    of the rows, GB_OPT_STAGED_MIX) sums in the same order as the plain per-row form: the
+    operator's output is bit-for-bit the same, AC2 and one-site AC."""
+    L_, pos = 12, 5
+    H = mpsgb.j1j2_cylinder(4, 3, u1=True)
+    As, qb = HU.random_u1_tensors(L_, 96, 13, 0, np.float64)
+    psi = mpsgb.FiniteMPS.from_tensors(As, ctx, center=pos + 1, charges=(qb, QP))
+    envs = mpsgb.FiniteEnvironments(psi, H)
+    be = mpsgb.GB300Backend(prec)
+    ac2 = mpsgb.ac2_from(psi.AL[pos], psi.ac(pos + 1))
+    ac = psi.ac(pos + 1)
+    out = {}
+    for staged in (1, 0):
+        ctx.set_option("staged_mix", staged)
+        try:
+            H2 = mpsgb.AC2_hamiltonian(pos, psi, H, envs, be)
+            H1 = mpsgb.AC_hamiltonian(pos + 1, psi, H, envs, be)
+            out[staged] = (H2(ac2).numpy(), H1(ac).numpy())
+        finally:
+            ctx.set_option("staged_mix", 1)
+    assert "AA" in H2.terms
+    assert np.array_equal(out[1][0], out[0][0]) and np.array_equal(out[1][1], out[0][1])
+
+
+def test_grouped_split_k_is_deterministic_and_accurate(ctx):
+    """Long-K sector blocks run as split-K units whose FP32 partial sums the last unit adds
+    in unit order: repeated applications are bit-for-bit identical, and the result agrees
+    with the FP64 operator to the split-precision tolerance."""
+    L_, pos = 18, 8
+    H = mpsgb.j1j2_cylinder(6, 3, u1=True)
+    As, qb = HU.random_u1_tensors(L_, 512, 43, 0, np.float64)
+    psi = mpsgb.FiniteMPS.from_tensors(As, ctx, center=pos + 1, charges=(qb, QP))
+    envs = mpsgb.FiniteEnvironments(psi, H)
+    x = mpsgb.ac2_from(psi.AL[pos], psi.ac(pos + 1))
+    op = mpsgb.AC2_hamiltonian(pos, psi, H, envs, mpsgb.GB300Backend("bf16x3"))
+    ys = [op(x).numpy() for _ in range(3)]
+    desc = op.describe()
+    assert any("split_tiles=" in l and "split_tiles=0" not in l for l in desc.splitlines()), desc
+    assert np.array_equal(ys[0], ys[1]) and np.array_equal(ys[0], ys[2])
+    ref = mpsgb.AC2_hamiltonian(pos, psi, H, envs, mpsgb.GB300Backend("fp64"))(x).numpy()
+    assert np.linalg.norm(ys[0] - ref) < 1e-4 * np.linalg.norm(ref)
