@@ -91,6 +91,9 @@ def parse():
     ap.add_argument("--sweeps", type=int, default=1, help="sweeps of --workload dmrg2-sweep")
     ap.add_argument("--describe", action="store_true",
                     help="--workload matvec: print the operator's contraction steps and plans")
+    ap.add_argument("--env-storage", default="packed", choices=["packed", "checkpoint"],
+                    help="dmrg2-sweep: every environment resident tile-packed, or every "
+                         "--checkpoint-th one dense with recomputation")
     ap.add_argument("--checkpoint", type=int, default=12,
                     help="dmrg2-sweep: environments kept resident every this many sites")
     ap.add_argument("--ref-budget", type=float, default=90.0,
@@ -784,9 +787,10 @@ def run_dmrg2_sweep(args):
     """Full DMRG2 sweeps (dmrg.jl:286-354: L-1 bond updates left to right, L-2 back) of the
     headline workload from its seeded random state, measured end to end: every local update
     (operator build, Galerkin matvec, adaptive Lanczos, blockwise truncated SVD) and every
-    environment step.  Environments at D = 2048 are 2 GB each, so only every `checkpoint`-th
-    one (and the newest per side) stays resident; the others are recomputed from the nearest
-    checkpoint, whose cost is part of the measured sweep."""
+    environment step.  Environments at D = 2048 are 2 GB each as dense embeddings: by default
+    every one stays resident tile-packed (about a tenth of that) and the two in use are
+    unpacked; with --env-storage checkpoint only every `checkpoint`-th one stays (dense) and
+    the others are recomputed from the nearest, inside the measured sweep."""
     import mpsgb
     ctx = mpsgb.context(0)
     prec = args.precision
@@ -802,8 +806,13 @@ def run_dmrg2_sweep(args):
                                        charges=(qb, mpsgb.operators.SPIN_HALF_CHARGES))
     del As
     K = max(1, args.checkpoint)
-    envs = mpsgb.FiniteEnvironments(psi, H, resident=False, keep_left=set(range(0, n + 1, K)),
-                                    keep_right=set(range(0, n, K)))
+    if args.env_storage == "packed":
+        # every environment resident, tile-packed but for the two in use
+        envs = mpsgb.FiniteEnvironments(psi, H, packed=True)
+    else:
+        envs = mpsgb.FiniteEnvironments(psi, H, resident=False,
+                                        keep_left=set(range(0, n + 1, K)),
+                                        keep_right=set(range(0, n, K)))
     envs.precision = backend.code
     envs.rightenv(0, psi)
     ctx.synchronize()
@@ -824,7 +833,9 @@ def run_dmrg2_sweep(args):
         "vs_baseline": None, "dtype": f"f64 ({prec} split contractions)", "data": "synthetic",
         "config": {"workload": f"J1-J2 Heisenberg {args.Ly}x{args.Lx} cylinder ({n} sites), full "
                                f"DMRG2 sweeps from the seeded random U(1) state (Sz = 0), "
-                               f"D={D}, Float64", "checkpoint": K, "precision": prec},
+                               f"D={D}, Float64", "env_storage": args.env_storage,
+                   "checkpoint": K if args.env_storage == "checkpoint" else None,
+                   "precision": prec},
         "sweeps": per, "clocks": clocks.summary(),
         "gpu_launches": ctx.kernel_launches(),
     }

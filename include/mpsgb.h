@@ -72,6 +72,7 @@ enum {
 typedef struct gb_ctx gb_ctx;
 typedef struct gb_tensor gb_tensor;
 typedef struct gb_heff gb_heff;
+typedef struct gb_packed gb_packed;
 
 /* KrylovKit ConvergenceInfo fields read by MPSKit (src/algorithms/groundstate/dmrg.jl:153,239,
  * src/algorithms/timestep/integrators.jl:27) */
@@ -172,6 +173,17 @@ int gb_ctx_read_work(gb_ctx* ctx, double* tile_flops, double* nonzero_flops, int
 int gb_tensor_create(gb_ctx* ctx, int kind, int dtype, int ndim, const int64_t* dims,
                      gb_tensor** out);
 int gb_tensor_free(gb_tensor* t);
+/* Tile-packed copy of a block-sparse tensor (e.g. a U(1) environment in its charge-sorted
+ * dense embedding): only the 64 x 64 tiles of its matrix view (rows = first device
+ * dimension) that hold a nonzero are kept.  gb_packed_unpack rebuilds the dense tensor
+ * exactly into `out` (same kind, dtype and shape; zeros elsewhere).  Lets the environment
+ * cache keep every GL/GR of a sweep resident (src/environments/finite_envs.jl:110-151).
+ * gb_packed_info: tiles kept / total and the bytes held. */
+int gb_tensor_pack(gb_ctx* ctx, const gb_tensor* t, gb_packed** out);
+int gb_packed_unpack(gb_ctx* ctx, const gb_packed* p, gb_tensor* out);
+int gb_packed_info(const gb_packed* p, int64_t* tiles_kept, int64_t* tiles_total,
+                   size_t* bytes);
+int gb_packed_free(gb_packed* p);
 int gb_tensor_shape(const gb_tensor* t, int* kind, int* dtype, int* ndim, int64_t* dims);
 int gb_tensor_upload(gb_tensor* t, const void* host, size_t bytes);
 int gb_tensor_download(const gb_tensor* t, void* host, size_t bytes);

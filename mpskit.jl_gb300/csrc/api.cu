@@ -1148,6 +1148,42 @@ int gb_tensor_create(gb_ctx* ctx, int kind, int dtype, int ndim, const int64_t* 
   API_END
 }
 
+int gb_tensor_pack(gb_ctx* ctx, const gb_tensor* t, gb_packed** out) {
+  API_BEGIN
+  GB_REQUIRE(ctx && out, "null argument");
+  check_ctx(t, ctx);
+  GB_REQUIRE(t->kind != GB_KIND_MPO, "pack: MPO tensors keep their host mirror; not packed");
+  DevGuard g(ctx->device);
+  *out = tensor_pack(ctx, t);
+  API_END
+}
+
+int gb_packed_unpack(gb_ctx* ctx, const gb_packed* p, gb_tensor* out) {
+  API_BEGIN
+  GB_REQUIRE(ctx && p, "null argument");
+  check_ctx(out, ctx);
+  GB_REQUIRE(packed_ctx(p) == ctx, "packed tensor belongs to another context");
+  DevGuard g(ctx->device);
+  packed_unpack(ctx, p, out);
+  API_END
+}
+
+int gb_packed_info(const gb_packed* p, int64_t* tiles_kept, int64_t* tiles_total,
+                   size_t* bytes) {
+  API_BEGIN
+  GB_REQUIRE(p, "null argument");
+  packed_info(p, tiles_kept, tiles_total, bytes);
+  API_END
+}
+
+int gb_packed_free(gb_packed* p) {
+  API_BEGIN
+  if (!p) return GB_OK;
+  DevGuard g(packed_ctx(p)->device);
+  packed_free(p);
+  API_END
+}
+
 int gb_tensor_free(gb_tensor* t) {
   API_BEGIN
   if (!t) return GB_OK;

@@ -308,6 +308,13 @@ void gemm_split(gb_ctx* ctx, int dtype, const Packed& A, const Packed& B, int64_
                 uint32_t* outmap = nullptr, bool c_f32 = false);
 bool tc_available(gb_ctx* ctx);
 
+// tile-packed copies of block-sparse tensors (packed.cu)
+gb_packed* tensor_pack(gb_ctx* ctx, const gb_tensor* t);
+void packed_unpack(gb_ctx* ctx, const gb_packed* p, gb_tensor* out);
+void packed_info(const gb_packed* p, int64_t* kept, int64_t* total, size_t* bytes);
+gb_ctx* packed_ctx(const gb_packed* p);
+void packed_free(gb_packed* p);
+
 // Hermitian eigendecomposition of the g x g matrix G in place (eigenvectors overwrite G,
 // eigenvalues ascending in W), by the context's GB_EIG_* method; *info (device) is nonzero on
 // failure.  Synchronises the context's stream before returning.

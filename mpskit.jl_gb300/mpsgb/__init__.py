@@ -19,6 +19,7 @@ from .infinite import (IDMRG, VUMPS, InfiniteEnvironments, InfiniteMPS,
                        find_groundstate_idmrg, find_groundstate_vumps, timestep_infinite)
 from . import u1
 from . import batched
+from . import io
 from . import cell
 
 __all__ = [
@@ -31,6 +32,6 @@ __all__ = [
     "svd_trunc", "DMRG", "DMRG2", "DMRG3S", "OptimalExpand", "AdaptiveKrylov",
     "expectation_value", "find_groundstate",
     "TDVP", "timestep", "VUMPS", "IDMRG", "InfiniteEnvironments", "InfiniteMPS",
-    "find_groundstate_vumps", "find_groundstate_idmrg", "timestep_infinite", "u1", "batched",
+    "find_groundstate_vumps", "find_groundstate_idmrg", "timestep_infinite", "u1", "batched", "io",
     "cell",
 ]

@@ -122,6 +122,10 @@ _SIGS = {
     "gb_heff_describe": ([P, ctypes.c_char_p, ctypes.c_size_t], INT),
     "gb_ctx_set_gauge": ([P, INT, INT], INT),
     "gb_ctx_set_option": ([P, INT, ctypes.c_int64], INT),
+    "gb_tensor_pack": ([P, P, ctypes.POINTER(P)], INT),
+    "gb_packed_unpack": ([P, P, P], INT),
+    "gb_packed_info": ([P, PI64, PI64, ctypes.POINTER(ctypes.c_size_t)], INT),
+    "gb_packed_free": ([P], INT),
     "gb_mps_perturb": ([P, INT, P, P, P, INT, P], INT),
     "gb_mps_cat": ([P, P, P, INT, P], INT),
     "gb_tensor_reshape": ([P, INT, INT, PI64], INT),

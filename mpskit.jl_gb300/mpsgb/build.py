@@ -8,7 +8,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(ROOT, "csrc")
 BUILD = os.path.join(ROOT, "_build")
 SOURCES = ["kernels.cu", "gemm_tc.cu", "grouped.cu", "heff.cu", "krylov.cu", "api.cu", "u1.cu",
-           "noalloc.cu"]
+           "noalloc.cu", "packed.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

@@ -257,3 +257,38 @@ class DeviceTensor:
 
     def __repr__(self):
         return f"DeviceTensor(kind={self.kind}, dtype={self.dtype}, dims={self.dims})"
+
+
+class PackedTensor:
+    """A tile-packed copy of a block-sparse device tensor (gb_tensor_pack): only the 64 x 64
+    tiles that hold a nonzero stay in HBM; unpack() rebuilds the dense tensor exactly."""
+
+    __slots__ = ("ctx", "handle", "kind", "dtype", "dims", "charges", "__weakref__")
+
+    def __init__(self, t):
+        self.ctx, self.kind, self.dtype, self.dims, self.charges = (t.ctx, t.kind, t.dtype,
+                                                                     t.dims, t.charges)
+        h = ctypes.c_void_p()
+        L.check(L.lib().gb_tensor_pack(t.ctx.handle, t.handle, ctypes.byref(h)))
+        self.handle = h
+
+    def unpack(self):
+        t = DeviceTensor(self.ctx, self.kind, self.dtype, self.dims, charges=self.charges)
+        L.check(L.lib().gb_packed_unpack(self.ctx.handle, self.handle, t.handle))
+        return t
+
+    def info(self):
+        """(tiles kept, tiles total, bytes held)."""
+        k, n, b = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_size_t()
+        L.check(L.lib().gb_packed_info(self.handle, ctypes.byref(k), ctypes.byref(n),
+                                       ctypes.byref(b)))
+        return k.value, n.value, b.value
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and L._lib is not None:
+            try:
+                L.lib().gb_packed_free(h)
+            except Exception:
+                pass
+            self.handle = None

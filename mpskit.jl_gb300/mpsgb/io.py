@@ -22,7 +22,7 @@ recomputation (they are taken as built from that state's AL / AR).
 import numpy as np
 
 from . import _lib as L
-from .core import DeviceTensor, context
+from .core import DeviceTensor, PackedTensor, context
 from .operators import MPOHamiltonian
 from .states import FiniteEnvironments, FiniteMPS
 
@@ -103,12 +103,13 @@ def load_state(path, ctx=None):
 
 def save_environments(path, envs):
     out = {"kind": np.array("finite_envs"), "nsites": np.array(len(envs.GR) - 1)}
+    host = lambda g: _f((g.unpack() if isinstance(g, PackedTensor) else g).numpy())
     for i, g in enumerate(envs.GL):
         if g is not None:
-            out[f"GL{i}"] = _f(g.numpy())
+            out[f"GL{i}"] = host(g)
     for i, g in enumerate(envs.GR):
         if g is not None:
-            out[f"GR{i}"] = _f(g.numpy())
+            out[f"GR{i}"] = host(g)
     np.savez(path, **out)
 
 

@@ -14,7 +14,7 @@ import ctypes
 import numpy as np
 
 from . import _lib as L
-from .core import DeviceTensor, context
+from .core import DeviceTensor, PackedTensor, context
 
 
 def _wrap_out(ctx, *handles):
@@ -269,10 +269,15 @@ class FiniteEnvironments:
     the boundary when asked for again) -- the memory policy for large D x w, where all
     L environments do not fit on one device.  `keep_left` / `keep_right`: sites whose
     environments are never released (e.g. the right environments of a window of bonds a
-    sweep is about to visit)."""
+    sweep is about to visit).  With `packed=True` every environment stays resident but only
+    the newest (or last requested) one of each side is held dense: the others are
+    tile-packed (gb_tensor_pack, exact), a tenth of the dense embedding of a U(1)
+    environment, and unpacked when asked for again."""
 
-    def __init__(self, psi, H, ctx=None, resident=True, keep_left=(), keep_right=()):
-        self.resident = resident
+    def __init__(self, psi, H, ctx=None, resident=True, keep_left=(), keep_right=(),
+                 packed=False):
+        self.packed = packed
+        self.resident = resident or packed
         self.keep_left, self.keep_right = set(keep_left), set(keep_right)
         self.ctx = ctx or psi.ctx
         self.H = H
@@ -290,15 +295,30 @@ class FiniteEnvironments:
     def _W(self):
         return self.H.device(self.ctx, self.dtype)
 
+    def _dense(self, lst, i):
+        """lst[i] as a dense tensor; with packing on, every other environment of that side
+        (but the boundary ones) is packed."""
+        t = lst[i]
+        if not self.packed:
+            return t
+        if isinstance(t, PackedTensor):
+            t = lst[i] = t.unpack()
+        last = len(lst) - 1
+        for k, o in enumerate(lst):
+            if k != i and isinstance(o, DeviceTensor) and 0 < k < last and min(o.dims) > 1:
+                lst[k] = PackedTensor(o)
+        return t
+
     def leftenv(self, i, psi):
         """GL of site i, recomputed from the nearest valid environment below when an AL
         it depends on changed (by identity) or when it was released."""
         first = next((j for j in range(i) if psi.AL[j] is not self.ldep[j]), i)
         if first == i and self.GL[i] is not None:
-            return self.GL[i]
+            return self._dense(self.GL, i)
         start = max(k for k in range(first + 1) if self.GL[k] is not None)
         W = self._W()
         for j in range(start, i):
+            self._dense(self.GL, j)
             A = psi.AL[j]
             out = DeviceTensor(self.ctx, L.GB_KIND_GL, self.dtype,
                                (A.dims[2], W[j].dims[3], A.dims[2]))
@@ -309,7 +329,7 @@ class FiniteEnvironments:
             self.ldep[j] = A
             if not self.resident and j >= 1 and j not in self.keep_left:
                 self.GL[j] = None
-        return self.GL[i]
+        return self._dense(self.GL, i)
 
     def rightenv(self, i, psi):
         """GR of site i (everything right of i), recomputed from the nearest valid
@@ -317,10 +337,11 @@ class FiniteEnvironments:
         n = len(psi)
         first = next((j for j in range(n - 1, i, -1) if psi.AR[j] is not self.rdep[j]), i)
         if first == i and self.GR[i] is not None:
-            return self.GR[i]
+            return self._dense(self.GR, i)
         start = min(k for k in range(first, n) if self.GR[k] is not None)
         W = self._W()
         for j in range(start, i, -1):
+            self._dense(self.GR, j)
             A = psi.AR[j]
             out = DeviceTensor(self.ctx, L.GB_KIND_GR, self.dtype,
                                (A.dims[0], W[j].dims[0], A.dims[0]))
@@ -331,4 +352,4 @@ class FiniteEnvironments:
             self.rdep[j] = A
             if not self.resident and j <= n - 2 and j not in self.keep_right:
                 self.GR[j] = None
-        return self.GR[i]
+        return self._dense(self.GR, i)
