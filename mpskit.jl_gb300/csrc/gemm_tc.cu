@@ -112,7 +112,9 @@ __global__ void pack_kernel(PackArgs p, const double* __restrict__ src, E* __res
     if (r >= p.R || k >= p.Kh) continue;  // entries k >= K were loaded as zeros
     double re = tre[j][tx], im = tim[j][tx];
     nz |= (re != 0.0 || im != 0.0);
-    auto put = [&](int64_t row, int64_t col, double v) { split_put(hi, lo, row * p.Kp + col, v); };
+    auto put = [&](int64_t row, int64_t col, double v) {
+      split_put_f(hi, lo, row * p.Kp + col, (float)v);
+    };
     if (!p.cplx) {
       put(r, k, re);
     } else if (p.role == 0) {
@@ -279,7 +281,7 @@ __global__ void mixpack_kernel(int64_t A, int64_t N, int64_t xn, const int64_t* 
   const int e0 = row_ptr[J], e1 = row_ptr[J + 1];
   const int lane = threadIdx.x % 32;
   E* lo = hi + plane;
-  auto put = [&](int64_t row, int64_t c, double v) { split_put(hi, lo, row * Kp + c, v); };
+  auto put = [&](int64_t row, int64_t c, double v) { split_put_f(hi, lo, row * Kp + c, (float)v); };
   auto mark = [&](int64_t row, int64_t kb) {
     atomicOr(&mask[(row / MASK_ROWS) * kw + kb / 32], 1u << (kb % 32));
   };

@@ -31,6 +31,7 @@
 #include <map>
 #include <mutex>
 #include <numeric>
+#include <type_traits>
 
 #include "grouped.h"
 #include "tc_ptx.cuh"
@@ -285,27 +286,28 @@ __global__ void gpack_kernel(const GPackTile* __restrict__ tiles, const int32_t*
                              const int32_t* __restrict__ klen, const double* __restrict__ src,
                              int64_t rs, int64_t ks, int rowfast, E* __restrict__ hi,
                              int64_t plane, int64_t kmax, unsigned long long* nnz) {
-  __shared__ double t[32][33];
+  __shared__ float t[32][33];
   const GPackTile T = tiles[blockIdx.x];
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int32_t kl = klen[T.g], k0 = kstart[T.g];
-  // load with the source's contiguous index on threadIdx.x
+  // load with the source's contiguous index on threadIdx.x; the planes keep at most 22 bits,
+  // so the value is rounded to FP32 once and split there
   for (int j = ty; j < 32; j += 8) {
     const int i = rowfast ? tx : j;    // row within the block
     const int kk = rowfast ? j : tx;   // column within the block
     const int kp = T.kp0 + kk;
-    double v = 0.0;
+    float v = 0.0f;
     if (i < T.nr && kp < kl)
-      v = src[(int64_t)rdense[T.rp0 + i] * rs + (int64_t)kdense[k0 + kp] * ks];
+      v = (float)src[(int64_t)rdense[T.rp0 + i] * rs + (int64_t)kdense[k0 + kp] * ks];
     t[i][kk] = v;
   }
   __syncthreads();
   E* lo = hi + plane;
   int nz = 0;
   for (int i = ty; i < T.nr; i += 8) {
-    const double v = t[i][tx];
-    nz += (v != 0.0);
-    split_put(hi, lo, (int64_t)(T.rp0 + i) * kmax + T.kp0 + tx, v);
+    const float v = t[i][tx];
+    nz += (v != 0.0f);
+    split_put_f(hi, lo, (int64_t)(T.rp0 + i) * kmax + T.kp0 + tx, v);
   }
   if (nnz) {
     for (int o = 16; o > 0; o >>= 1) nz += __shfl_down_sync(0xffffffffu, nz, o);
@@ -438,9 +440,23 @@ __global__ void gmix_kernel(int64_t nJ, int64_t N, int64_t xn, const int64_t* __
     if (en.hi <= en.lo || en.row < 0) continue;
     const int64_t base = (int64_t)en.row * kmax + en.kst - en.lo;
     for (int64_t a = en.lo + lane; a < en.hi; a += 32) {
-      double acc = 0.0;
-      for (int e = e0; e < e1; ++e) acc = fma(val[e], (double)x[a + in_off[col[e]] + n * xn], acc);
-      split_put(hi, lo, base + a, acc);
+      // the arithmetic of gmix_staged_kernel, term for term (identical results)
+      float s = 0.0f, c = 0.0f;
+      for (int e = e0; e < e1; ++e) {
+        const float xv = x[a + in_off[col[e]] + n * xn];
+        const float vh = (float)val[e];
+        if (std::is_same<E, float>::value) {
+          const float vl = (float)(val[e] - (double)vh);
+          const float p = vh * xv;
+          const float pe = fmaf(vh, xv, -p) + vl * xv;
+          const float t = s + p, z = t - s;
+          c += ((s - (t - z)) + (p - z)) + pe;
+          s = t;
+        } else {
+          s = fmaf(vh, xv, s);
+        }
+      }
+      split_put_f(hi, lo, base + a, s + c);
     }
   }
 }
@@ -468,7 +484,8 @@ void gmix_run(gb_ctx* ctx, const MixDev& m, const GMixEntry* ent, int64_t span_m
 template <typename E>
 __global__ void gmix_staged_kernel(int NL, int64_t nJ, int64_t xn, const int64_t* __restrict__ in_off,
                                    const int* __restrict__ row_ptr, const int* __restrict__ lcol,
-                                   const double* __restrict__ val, const float* __restrict__ x,
+                                   const float* __restrict__ vhi, const float* __restrict__ vlo,
+                                   const float* __restrict__ x,
                                    const GMixEntry* __restrict__ ent, const int2* __restrict__ rng,
                                    const int* __restrict__ jlist, const int* __restrict__ jstart,
                                    const int* __restrict__ ilist, const int* __restrict__ istart,
@@ -496,9 +513,23 @@ __global__ void gmix_staged_kernel(int NL, int64_t nJ, int64_t xn, const int64_t
       const int64_t base = (int64_t)en.row * kmax + en.kst - en.lo;
       const int e0 = row_ptr[J], e1 = row_ptr[J + 1];
       for (int a = lane; a < w; a += 32) {
-        double acc = 0.0;
-        for (int e = e0; e < e1; ++e) acc = fma(val[e], (double)stage[lcol[e] * w + a], acc);
-        split_put(hi, lo, base + a0 + a, acc);
+        // FP32 arithmetic (GB300's FP64 rate is a small fraction of it): a plain sum for the
+        // 16 bits of BF16 planes; for the 22 bits of TF32 planes a compensated one (exact
+        // product and sum errors carried in a second word, coefficients as two floats)
+        float s = 0.0f, c = 0.0f;
+        for (int e = e0; e < e1; ++e) {
+          const float xv = stage[lcol[e] * w + a];
+          if (std::is_same<E, float>::value) {
+            const float p = vhi[e] * xv;
+            const float pe = fmaf(vhi[e], xv, -p) + vlo[e] * xv;
+            const float t = s + p, z = t - s;
+            c += ((s - (t - z)) + (p - z)) + pe;
+            s = t;
+          } else {
+            s = fmaf(vhi[e], xv, s);
+          }
+        }
+        split_put_f(hi, lo, base + a0 + a, s + c);
       }
     }
     __syncthreads();
@@ -521,12 +552,12 @@ void gmix_staged_run(gb_ctx* ctx, const MixDev& m, const GMixStaged& g, const GM
   GB_REQUIRE(g.smem <= 96 * 1024, "grouped mix: staging buffer too large");
   if (out.esz == 4)
     gmix_staged_kernel<float><<<grid, 256, g.smem, ctx->stream>>>(
-        g.NL, m.nJ, m.xn, m.in_off, m.row_ptr, g.lcol, m.val, t1, ent, g.rng, g.jlist, g.jstart,
-        g.ilist, g.istart, g.chunk, (float*)out.data, plane, out.kmax);
+        g.NL, m.nJ, m.xn, m.in_off, m.row_ptr, g.lcol, g.vhi, g.vlo, t1, ent, g.rng, g.jlist,
+        g.jstart, g.ilist, g.istart, g.chunk, (float*)out.data, plane, out.kmax);
   else
     gmix_staged_kernel<__nv_bfloat16><<<grid, 256, g.smem, ctx->stream>>>(
-        g.NL, m.nJ, m.xn, m.in_off, m.row_ptr, g.lcol, m.val, t1, ent, g.rng, g.jlist, g.jstart,
-        g.ilist, g.istart, g.chunk, (__nv_bfloat16*)out.data, plane, out.kmax);
+        g.NL, m.nJ, m.xn, m.in_off, m.row_ptr, g.lcol, g.vhi, g.vlo, t1, ent, g.rng, g.jlist,
+        g.jstart, g.ilist, g.istart, g.chunk, (__nv_bfloat16*)out.data, plane, out.kmax);
   GB_CHECK_CUDA(cudaGetLastError());
   count_launch(ctx);
 }
@@ -712,6 +743,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
     float* xb = xbuf + (warp - 2) * 32 * 33;
     const bool f32 = args.c_f32 != 0;
     const double alpha = args.alpha, beta = args.beta;
+    const bool copy_f32 = f32 && alpha == 1.0 && beta == 0.0;
     auto loadC = [&](int64_t e) -> double {
       return f32 ? (double)((const float*)args.C)[e] : ((const double*)args.C)[e];
     };
@@ -739,6 +771,17 @@ __global__ void __launch_bounds__(G_THREADS, 1)
       // beta * C terms are all loaded before any store, so their latencies overlap
       auto store_chunk = [&](int c0, const uint32_t (&v)[32]) {
         const int64_t nl = (int64_t)T.n0 + c0 + lane;
+        if (copy_f32 && !args.trans_store) {
+          // FP32 output that is the accumulator itself: no FP64 arithmetic
+          const int64_t myco = nl < nend ? args.coloff[nl] : 0;
+#pragma unroll
+          for (int jj = 0; jj < 32; ++jj) {
+            const int64_t co = __shfl_sync(0xffffffffu, myco, jj);
+            if (rvalid && (int64_t)T.n0 + c0 + jj < nend)
+              ((float*)args.C)[roff + co] = __uint_as_float(v[jj]);
+          }
+          return;
+        }
         if (!args.trans_store) {
           const int64_t myco = nl < nend ? args.coloff[nl] : 0;
 #pragma unroll

@@ -144,6 +144,8 @@ struct GMixStaged {
   const int* ilist = nullptr;   // inputs read by group g: ilist[istart[g] .. istart[g + 1])
   const int* istart = nullptr;
   const int* lcol = nullptr;    // per mix entry e: position of col[e] in its row's input list
+  const float* vhi = nullptr;   // mix coefficient of entry e as hi + lo floats
+  const float* vlo = nullptr;
 };
 void gmix_staged_run(gb_ctx* ctx, const MixDev& m, const GMixStaged& g, const GMixEntry* ent,
                      const float* t1, GOperand& out);

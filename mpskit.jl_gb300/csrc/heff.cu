@@ -1722,6 +1722,12 @@ static void build_staged_mix(gb_heff* h, int64_t Dr) {
   const size_t o_jl = put(jlist.data(), jlist.size() * 4), o_js = put(jstart.data(), jstart.size() * 4);
   const size_t o_il = put(ilist.data(), ilist.size() * 4), o_is = put(istart.data(), istart.size() * 4);
   const size_t o_lc = put(lcol.data(), lcol.size() * 4);
+  std::vector<float> vhi(mp.val.size()), vlo(mp.val.size());
+  for (size_t e = 0; e < mp.val.size(); ++e) {
+    vhi[e] = (float)mp.val[e];
+    vlo[e] = (float)(mp.val[e] - (double)vhi[e]);
+  }
+  const size_t o_vh = put(vhi.data(), vhi.size() * 4), o_vl = put(vlo.data(), vlo.size() * 4);
   char* d = (char*)dalloc(h, blob.size());
   GB_CHECK_CUDA(cudaMemcpyAsync(d, blob.data(), blob.size(), cudaMemcpyHostToDevice,
                                 h->ctx->stream));
@@ -1733,6 +1739,8 @@ static void build_staged_mix(gb_heff* h, int64_t Dr) {
   st.ilist = (const int*)(d + o_il);
   st.istart = (const int*)(d + o_is);
   st.lcol = (const int*)(d + o_lc);
+  st.vhi = (const float*)(d + o_vh);
+  st.vlo = (const float*)(d + o_vl);
   st.chunk = (int)chunk;
   st.smem = (size_t)chunk * max_ni * 4;
   st.NL = NL;

@@ -27,16 +27,19 @@ __device__ __forceinline__ float tf32_rna(float x) {
   asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
   return __uint_as_float(r);
 }
-__device__ __forceinline__ void split_put(__nv_bfloat16* hi, __nv_bfloat16* lo, int64_t i,
-                                          double v) {
-  const __nv_bfloat16 h = __double2bfloat16(v);
+// hi/lo split of a value rounded to FP32: its 24 bits hold the 16 (BF16) or 22 (TF32) bits
+// the two planes keep, and the split needs no FP64 arithmetic (GB300's FP64 rate is a small
+// fraction of its FP32 rate)
+__device__ __forceinline__ void split_put_f(__nv_bfloat16* hi, __nv_bfloat16* lo, int64_t i,
+                                            float v) {
+  const __nv_bfloat16 h = __float2bfloat16_rn(v);
   hi[i] = h;
-  lo[i] = __double2bfloat16(v - (double)__bfloat162float(h));
+  lo[i] = __float2bfloat16_rn(v - __bfloat162float(h));
 }
-__device__ __forceinline__ void split_put(float* hi, float* lo, int64_t i, double v) {
-  const float h = tf32_rna((float)v);
+__device__ __forceinline__ void split_put_f(float* hi, float* lo, int64_t i, float v) {
+  const float h = tf32_rna(v);
   hi[i] = h;
-  lo[i] = tf32_rna((float)(v - (double)h));
+  lo[i] = tf32_rna(v - h);
 }
 __device__ __forceinline__ bool plane_nz(__nv_bfloat16 a) { return __bfloat162float(a) != 0.f; }
 __device__ __forceinline__ bool plane_nz(float a) { return a != 0.f; }

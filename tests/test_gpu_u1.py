@@ -376,13 +376,13 @@ def test_packed_environments_are_exact_and_small(ctx):
     """gb_tensor_pack keeps only the nonzero 64 x 64 tiles of a U(1) environment's dense
     embedding and gb_packed_unpack restores it bit for bit; FiniteEnvironments(packed=True)
     serves the same environments as the dense cache."""
-    L_, pos = 14, 6
+    L_, pos = 24, 11
     H = mpsgb.heisenberg_XXX(L_, dtype=np.float64, u1=True)
-    As, qb = HU.random_u1_tensors(L_, 256, 47, 0, np.float64)
+    As, qb = HU.random_u1_tensors(L_, 1024, 47, 0, np.float64)
     psi = mpsgb.FiniteMPS.from_tensors(As, ctx, center=pos + 1, charges=(qb, QP))
     dense = mpsgb.FiniteEnvironments(psi, H)
     packed = mpsgb.FiniteEnvironments(psi, H, packed=True)
-    for i in range(1, pos + 1):
+    for i in range(pos - 2, pos + 1):
         a = dense.leftenv(i, psi).numpy()
         b = packed.leftenv(i, psi).numpy()
         assert np.array_equal(a, b)
@@ -392,6 +392,8 @@ def test_packed_environments_are_exact_and_small(ctx):
     assert kept < total and nbytes < 0.5 * GL.numpy().nbytes
     assert np.array_equal(p.unpack().numpy(), GL.numpy())
     # every environment but the requested one is held packed
-    assert sum(isinstance(g, mpsgb.core.PackedTensor) for g in packed.GL) >= pos - 2
-    for i in range(L_ - 2, pos, -1):
+    assert sum(isinstance(g, mpsgb.core.PackedTensor) for g in packed.GL) >= pos - 1
+    for i in (pos + 3, pos + 2, pos + 1):
         assert np.array_equal(dense.rightenv(i, psi).numpy(), packed.rightenv(i, psi).numpy())
+    # an environment asked for again comes back from its packed copy
+    assert np.array_equal(dense.leftenv(pos - 1, psi).numpy(), packed.leftenv(pos - 1, psi).numpy())
