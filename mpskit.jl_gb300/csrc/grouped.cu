@@ -483,14 +483,15 @@ void gmix_run(gb_ctx* ctx, const MixDev& m, const GMixEntry* ent, int64_t span_m
 
 template <typename E>
 __global__ void gmix_staged_kernel(int NL, int64_t nJ, int64_t xn, const int64_t* __restrict__ in_off,
-                                   const int* __restrict__ row_ptr, const int* __restrict__ lcol,
-                                   const float* __restrict__ vhi, const float* __restrict__ vlo,
-                                   const float* __restrict__ x,
+                                   const float* __restrict__ whi, const float* __restrict__ wlo,
+                                   const int* __restrict__ wstart, const float* __restrict__ x,
                                    const GMixEntry* __restrict__ ent, const int2* __restrict__ rng,
                                    const int* __restrict__ jlist, const int* __restrict__ jstart,
                                    const int* __restrict__ ilist, const int* __restrict__ istart,
                                    int chunk, E* __restrict__ hi, int64_t plane, int64_t kmax) {
-  extern __shared__ float stage[];
+  constexpr bool TF = std::is_same<E, float>::value;
+  constexpr int RJ = 4, RA = 2;  // rows x (32-lane) columns per thread
+  extern __shared__ float sm[];
   const int g = blockIdx.y;
   const int64_t n = blockIdx.x;
   const int2 r = rng[n * NL + g];
@@ -498,6 +499,14 @@ __global__ void gmix_staged_kernel(int NL, int64_t nJ, int64_t xn, const int64_t
   const int i0 = istart[g], ni = istart[g + 1] - i0;
   const int j0 = jstart[g], nj = jstart[g + 1] - j0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  // the group's coefficients, dense [nj][ni] (hi, and lo for TF32 planes), then the inputs
+  float* wh = sm;
+  float* wl = wh + nj * ni;
+  float* stage = wl + (TF ? nj * ni : 0);
+  for (int e = threadIdx.x; e < nj * ni; e += blockDim.x) {
+    wh[e] = whi[wstart[g] + e];
+    if (TF) wl[e] = wlo[wstart[g] + e];
+  }
   E* lo = hi + plane;
   for (int a0 = r.x; a0 < r.y; a0 += chunk) {
     const int w = min(chunk, r.y - a0);
@@ -506,30 +515,52 @@ __global__ void gmix_staged_kernel(int NL, int64_t nJ, int64_t xn, const int64_t
       stage[idx] = x[(int64_t)(a0 + a) + in_off[ilist[i0 + i]] + n * xn];
     }
     __syncthreads();
-    for (int jj = warp; jj < nj; jj += nw) {
-      const int J = jlist[j0 + jj];
-      const GMixEntry en = ent[n * nJ + J];
-      if (en.row < 0) continue;
-      const int64_t base = (int64_t)en.row * kmax + en.kst - en.lo;
-      const int e0 = row_ptr[J], e1 = row_ptr[J + 1];
-      for (int a = lane; a < w; a += 32) {
-        // FP32 arithmetic (GB300's FP64 rate is a small fraction of it): a plain sum for the
-        // 16 bits of BF16 planes; for the 22 bits of TF32 planes a compensated one (exact
-        // product and sum errors carried in a second word, coefficients as two floats)
-        float s = 0.0f, c = 0.0f;
-        for (int e = e0; e < e1; ++e) {
-          const float xv = stage[lcol[e] * w + a];
-          if (std::is_same<E, float>::value) {
-            const float p = vhi[e] * xv;
-            const float pe = fmaf(vhi[e], xv, -p) + vlo[e] * xv;
-            const float t = s + p, z = t - s;
-            c += ((s - (t - z)) + (p - z)) + pe;
-            s = t;
-          } else {
-            s = fmaf(vhi[e], xv, s);
+    for (int jb = warp * RJ; jb < nj; jb += nw * RJ) {
+      for (int ab = 0; ab < w; ab += 32 * RA) {
+        float s[RJ][RA], c[RJ][RA];
+#pragma unroll
+        for (int q = 0; q < RJ; ++q)
+#pragma unroll
+          for (int k = 0; k < RA; ++k) s[q][k] = c[q][k] = 0.0f;
+        for (int i = 0; i < ni; ++i) {
+          float xv[RA];
+#pragma unroll
+          for (int k = 0; k < RA; ++k) {
+            const int a = ab + lane + 32 * k;
+            xv[k] = a < w ? stage[i * w + a] : 0.0f;
+          }
+#pragma unroll
+          for (int q = 0; q < RJ; ++q) {
+            const bool rowok = jb + q < nj;
+            const float vh = rowok ? wh[(jb + q) * ni + i] : 0.0f;
+            if (TF) {
+              const float vl = rowok ? wl[(jb + q) * ni + i] : 0.0f;
+#pragma unroll
+              for (int k = 0; k < RA; ++k) {
+                const float p = vh * xv[k];
+                const float pe = fmaf(vh, xv[k], -p) + vl * xv[k];
+                const float t = s[q][k] + p, z = t - s[q][k];
+                c[q][k] += ((s[q][k] - (t - z)) + (p - z)) + pe;
+                s[q][k] = t;
+              }
+            } else {
+#pragma unroll
+              for (int k = 0; k < RA; ++k) s[q][k] = fmaf(vh, xv[k], s[q][k]);
+            }
           }
         }
-        split_put_f(hi, lo, base + a0 + a, s + c);
+#pragma unroll
+        for (int q = 0; q < RJ; ++q) {
+          if (jb + q >= nj) break;
+          const GMixEntry en = ent[n * nJ + jlist[j0 + jb + q]];
+          if (en.row < 0) continue;
+          const int64_t base = (int64_t)en.row * kmax + en.kst - en.lo;
+#pragma unroll
+          for (int k = 0; k < RA; ++k) {
+            const int a = ab + lane + 32 * k;
+            if (a < w) split_put_f(hi, lo, base + a0 + a, s[q][k] + c[q][k]);
+          }
+        }
       }
     }
     __syncthreads();
@@ -549,15 +580,16 @@ void gmix_staged_run(gb_ctx* ctx, const MixDev& m, const GMixStaged& g, const GM
     cudaFuncSetAttribute(gmix_staged_kernel<__nv_bfloat16>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
   });
-  GB_REQUIRE(g.smem <= 96 * 1024, "grouped mix: staging buffer too large");
+  GB_REQUIRE(g.smem <= 96 * 1024 && g.smem_tf32 <= 96 * 1024,
+             "grouped mix: staging buffer too large");
   if (out.esz == 4)
-    gmix_staged_kernel<float><<<grid, 256, g.smem, ctx->stream>>>(
-        g.NL, m.nJ, m.xn, m.in_off, m.row_ptr, g.lcol, g.vhi, g.vlo, t1, ent, g.rng, g.jlist,
-        g.jstart, g.ilist, g.istart, g.chunk, (float*)out.data, plane, out.kmax);
+    gmix_staged_kernel<float><<<grid, 256, g.smem_tf32, ctx->stream>>>(
+        g.NL, m.nJ, m.xn, m.in_off, g.whi, g.wlo, g.wstart, t1, ent, g.rng, g.jlist, g.jstart,
+        g.ilist, g.istart, g.chunk_tf32, (float*)out.data, plane, out.kmax);
   else
     gmix_staged_kernel<__nv_bfloat16><<<grid, 256, g.smem, ctx->stream>>>(
-        g.NL, m.nJ, m.xn, m.in_off, m.row_ptr, g.lcol, g.vhi, g.vlo, t1, ent, g.rng, g.jlist,
-        g.jstart, g.ilist, g.istart, g.chunk, (__nv_bfloat16*)out.data, plane, out.kmax);
+        g.NL, m.nJ, m.xn, m.in_off, g.whi, g.wlo, g.wstart, t1, ent, g.rng, g.jlist, g.jstart,
+        g.ilist, g.istart, g.chunk, (__nv_bfloat16*)out.data, plane, out.kmax);
   GB_CHECK_CUDA(cudaGetLastError());
   count_launch(ctx);
 }

@@ -131,21 +131,24 @@ void gmix_run(gb_ctx* ctx, const MixDev& m, const GMixEntry* ent, int64_t span_m
               const float* t1, GOperand& out);
 // The same mix staged through shared memory.  The output rows J fall into groups whose
 // input range [lo, hi) is the same at every column n (rows of one charge); a block per
-// (column, group) loads the inputs its rows read -- once, coalesced -- and computes every
-// row of the group from shared memory, with the sums in the same order as gmix_run (the
-// results are identical).
+// (column, group) loads the group's coefficients (dense, [rows][inputs]) and the inputs its
+// rows read -- once, coalesced -- and computes every row of the group from shared memory, a
+// few rows and columns per thread.  The sums run over the inputs in increasing order, as in
+// gmix_run (whose missing coefficients are exact zeros here): the results are identical.
 struct GMixStaged {
   int NL = 0;              // row groups
-  int chunk = 0;           // input rows a staged per pass
-  size_t smem = 0;         // dynamic shared memory per block
+  int chunk = 0;           // input rows a staged per pass (BF16 planes)
+  int chunk_tf32 = 0;      // the same with the TF32 coefficient halves in shared memory
+  size_t smem = 0;         // dynamic shared memory per block (BF16 planes)
+  size_t smem_tf32 = 0;    // (TF32 planes)
   const int2* rng = nullptr;    // [N][NL]: (lo, hi) of group g at column n
   const int* jlist = nullptr;   // rows of group g: jlist[jstart[g] .. jstart[g + 1])
   const int* jstart = nullptr;
   const int* ilist = nullptr;   // inputs read by group g: ilist[istart[g] .. istart[g + 1])
   const int* istart = nullptr;
-  const int* lcol = nullptr;    // per mix entry e: position of col[e] in its row's input list
-  const float* vhi = nullptr;   // mix coefficient of entry e as hi + lo floats
-  const float* vlo = nullptr;
+  const float* whi = nullptr;   // coefficients of group g at whi[wstart[g]], [rows][inputs],
+  const float* wlo = nullptr;   // as hi + lo floats
+  const int* wstart = nullptr;
 };
 void gmix_staged_run(gb_ctx* ctx, const MixDev& m, const GMixStaged& g, const GMixEntry* ent,
                      const float* t1, GOperand& out);

@@ -1676,9 +1676,10 @@ static void build_staged_mix(gb_heff* h, int64_t Dr) {
     if (h->lam_J[J] != INT64_MIN) byq[h->lam_J[J]].push_back((int)J);
   const int NL = (int)byq.size();
   if (NL == 0) return;
-  std::vector<int> jlist, jstart{0}, ilist, istart{0}, lcol(mp.col.size(), 0);
+  std::vector<int> jlist, jstart{0}, ilist, istart{0}, wstart;
+  std::vector<float> whi, wlo;  // per group: dense [rows][inputs] coefficients, hi + lo
   std::vector<int2> rng((size_t)Dr * NL);
-  int max_ni = 0;
+  size_t max_w = 0, max_ni = 0;
   int g = 0;
   for (const auto& kv : byq) {
     const std::vector<int>& Js = kv.second;
@@ -1687,9 +1688,17 @@ static void build_staged_mix(gb_heff* h, int64_t Dr) {
       for (int e = mp.row_ptr[J]; e < mp.row_ptr[J + 1]; ++e) ins.push_back(mp.col[e]);
     std::sort(ins.begin(), ins.end());
     ins.erase(std::unique(ins.begin(), ins.end()), ins.end());
-    for (int J : Js)
-      for (int e = mp.row_ptr[J]; e < mp.row_ptr[J + 1]; ++e)
-        lcol[e] = (int)(std::lower_bound(ins.begin(), ins.end(), mp.col[e]) - ins.begin());
+    const size_t ni = ins.size();
+    wstart.push_back((int)whi.size());
+    whi.resize(whi.size() + Js.size() * ni, 0.0f);
+    wlo.resize(whi.size(), 0.0f);
+    for (size_t jj = 0; jj < Js.size(); ++jj)
+      for (int e = mp.row_ptr[Js[jj]]; e < mp.row_ptr[Js[jj] + 1]; ++e) {
+        const size_t i = std::lower_bound(ins.begin(), ins.end(), mp.col[e]) - ins.begin();
+        const float vh = (float)mp.val[e];
+        whi[wstart.back() + jj * ni + i] = vh;
+        wlo[wstart.back() + jj * ni + i] = (float)(mp.val[e] - (double)vh);
+      }
     // one input range per (column, group): every row of the group must agree
     for (int64_t n = 0; n < Dr; ++n) {
       const int2 r0 = h->arange_h[(size_t)n * nJ + Js[0]];
@@ -1703,13 +1712,22 @@ static void build_staged_mix(gb_heff* h, int64_t Dr) {
     jstart.push_back((int)jlist.size());
     ilist.insert(ilist.end(), ins.begin(), ins.end());
     istart.push_back((int)ilist.size());
-    max_ni = std::max<int>(max_ni, (int)ins.size());
+    max_ni = std::max(max_ni, ni);
+    max_w = std::max(max_w, Js.size() * ni);
     ++g;
   }
-  const int64_t cap = 96 * 1024 / 4;  // floats of staging
-  int64_t chunk = std::min<int64_t>(std::max<int64_t>(h->arange_max, 1), cap / std::max(max_ni, 1));
-  if (chunk < 32 && chunk < h->arange_max) return;
-  chunk = std::max<int64_t>(chunk, 1);
+  // shared memory: the coefficients (hi, and lo for TF32 planes) plus a chunk of inputs
+  const int64_t cap = 96 * 1024 / 4;  // floats
+  const int64_t amax = std::max<int64_t>(h->arange_max, 1);
+  auto chunk_for = [&](int64_t wfloats) -> int64_t {
+    const int64_t room = cap - wfloats;
+    if (room <= 0) return 0;
+    return std::min<int64_t>(amax, room / (int64_t)std::max<size_t>(max_ni, 1));
+  };
+  const int64_t chunk = chunk_for((int64_t)max_w), chunk_tf = chunk_for(2 * (int64_t)max_w);
+  if ((chunk < 32 && chunk < amax) || (chunk_tf < 32 && chunk_tf < amax) || chunk < 1 ||
+      chunk_tf < 1)
+    return;
   // one device blob for the tables
   std::vector<char> blob;
   auto put = [&](const void* src, size_t bytes) {
@@ -1721,13 +1739,8 @@ static void build_staged_mix(gb_heff* h, int64_t Dr) {
   const size_t o_r = put(rng.data(), rng.size() * sizeof(int2));
   const size_t o_jl = put(jlist.data(), jlist.size() * 4), o_js = put(jstart.data(), jstart.size() * 4);
   const size_t o_il = put(ilist.data(), ilist.size() * 4), o_is = put(istart.data(), istart.size() * 4);
-  const size_t o_lc = put(lcol.data(), lcol.size() * 4);
-  std::vector<float> vhi(mp.val.size()), vlo(mp.val.size());
-  for (size_t e = 0; e < mp.val.size(); ++e) {
-    vhi[e] = (float)mp.val[e];
-    vlo[e] = (float)(mp.val[e] - (double)vhi[e]);
-  }
-  const size_t o_vh = put(vhi.data(), vhi.size() * 4), o_vl = put(vlo.data(), vlo.size() * 4);
+  const size_t o_wh = put(whi.data(), whi.size() * 4), o_wl = put(wlo.data(), wlo.size() * 4);
+  const size_t o_ws = put(wstart.data(), wstart.size() * 4);
   char* d = (char*)dalloc(h, blob.size());
   GB_CHECK_CUDA(cudaMemcpyAsync(d, blob.data(), blob.size(), cudaMemcpyHostToDevice,
                                 h->ctx->stream));
@@ -1738,15 +1751,17 @@ static void build_staged_mix(gb_heff* h, int64_t Dr) {
   st.jstart = (const int*)(d + o_js);
   st.ilist = (const int*)(d + o_il);
   st.istart = (const int*)(d + o_is);
-  st.lcol = (const int*)(d + o_lc);
-  st.vhi = (const float*)(d + o_vh);
-  st.vlo = (const float*)(d + o_vl);
+  st.whi = (const float*)(d + o_wh);
+  st.wlo = (const float*)(d + o_wl);
+  st.wstart = (const int*)(d + o_ws);
   st.chunk = (int)chunk;
-  st.smem = (size_t)chunk * max_ni * 4;
+  st.chunk_tf32 = (int)chunk_tf;
+  st.smem = (size_t)(max_w + chunk * max_ni) * 4;
+  st.smem_tf32 = (size_t)(2 * max_w + chunk_tf * max_ni) * 4;
   st.NL = NL;
 }
 
-// y = H x through the grouped plans.// y = H x through the grouped plans.  x: dense embedding, zero outside the sectors; every
+// y = H x through the grouped plans.  x: dense embedding, zero outside the sectors; every
 // allowed entry of y is written (the first GEMM into y overwrites, the rest accumulate);
 // entries outside the sectors are zeroed only when y is not the operator's own staging
 // vector (whose outside entries are never read).

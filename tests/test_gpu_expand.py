@@ -149,4 +149,4 @@ def test_single_site_dmrg_with_expansion_reaches_ed(ctx, kind):
     assert len(hist) == len(ohist)
     for a, b in zip(hist, ohist):
         assert abs(a["energy"] - b[1]) <= 1e-8 * abs(b[1]), (a, b)
-    assert 0.0 <= hist[-1]["energy"] - e_ed < bar
+    assert -1e-12 * abs(e_ed) <= hist[-1]["energy"] - e_ed < bar
