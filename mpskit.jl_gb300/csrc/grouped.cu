@@ -159,7 +159,7 @@ void gplan_build(GPlan& p, const std::vector<int32_t>& labM, const std::vector<i
   {
     int64_t total = 0;
     for (const GTile& t : p.tiles) total += t.nkb;
-    const int64_t target = std::max<int64_t>(8, (total + 2 * sms - 1) / (2 * std::max(sms, 1)));
+    const int64_t target = std::max<int64_t>(4, (total + 2 * sms - 1) / (2 * std::max(sms, 1)));
     std::vector<GTile> units;
     for (const GTile& t : p.tiles) {
       if (t.nkb <= target + target / 2) {
@@ -483,14 +483,16 @@ void gmix_run(gb_ctx* ctx, const MixDev& m, const GMixEntry* ent, int64_t span_m
 
 template <typename E>
 __global__ void gmix_staged_kernel(int NL, int64_t nJ, int64_t xn, const int64_t* __restrict__ in_off,
-                                   const float* __restrict__ whi, const float* __restrict__ wlo,
-                                   const int* __restrict__ wstart, const float* __restrict__ x,
-                                   const GMixEntry* __restrict__ ent, const int2* __restrict__ rng,
-                                   const int* __restrict__ jlist, const int* __restrict__ jstart,
-                                   const int* __restrict__ ilist, const int* __restrict__ istart,
-                                   int chunk, E* __restrict__ hi, int64_t plane, int64_t kmax) {
+                                   const int* __restrict__ grp, const int* __restrict__ gli,
+                                   const float* __restrict__ gvh, const float* __restrict__ gvl,
+                                   const int* __restrict__ rstart, const int* __restrict__ cstart,
+                                   const float* __restrict__ x, const GMixEntry* __restrict__ ent,
+                                   const int2* __restrict__ rng, const int* __restrict__ jlist,
+                                   const int* __restrict__ jstart, const int* __restrict__ ilist,
+                                   const int* __restrict__ istart, int chunk, int csr_floats,
+                                   E* __restrict__ hi, int64_t plane, int64_t kmax) {
   constexpr bool TF = std::is_same<E, float>::value;
-  constexpr int RJ = 4, RA = 2;  // rows x (32-lane) columns per thread
+  constexpr int RA = 4;  // 32-lane columns per thread
   extern __shared__ float sm[];
   const int g = blockIdx.y;
   const int64_t n = blockIdx.x;
@@ -499,13 +501,18 @@ __global__ void gmix_staged_kernel(int NL, int64_t nJ, int64_t xn, const int64_t
   const int i0 = istart[g], ni = istart[g + 1] - i0;
   const int j0 = jstart[g], nj = jstart[g + 1] - j0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  // the group's coefficients, dense [nj][ni] (hi, and lo for TF32 planes), then the inputs
-  float* wh = sm;
-  float* wl = wh + nj * ni;
-  float* stage = wl + (TF ? nj * ni : 0);
-  for (int e = threadIdx.x; e < nj * ni; e += blockDim.x) {
-    wh[e] = whi[wstart[g] + e];
-    if (TF) wl[e] = wlo[wstart[g] + e];
+  // the group's rows in shared memory: row pointers, local input index, coefficient hi (lo)
+  const int e0 = cstart[g], ne = cstart[g + 1] - e0;
+  int* rp = (int*)sm;
+  int* li = rp + nj + 1;
+  float* vh = (float*)(li + ne);
+  float* vl = vh + ne;
+  float* stage = sm + csr_floats;
+  for (int k = threadIdx.x; k <= nj; k += blockDim.x) rp[k] = grp[rstart[g] + k] - e0;
+  for (int k = threadIdx.x; k < ne; k += blockDim.x) {
+    li[k] = gli[e0 + k];
+    vh[k] = gvh[e0 + k];
+    if (TF) vl[k] = gvl[e0 + k];
   }
   E* lo = hi + plane;
   for (int a0 = r.x; a0 < r.y; a0 += chunk) {
@@ -515,51 +522,36 @@ __global__ void gmix_staged_kernel(int NL, int64_t nJ, int64_t xn, const int64_t
       stage[idx] = x[(int64_t)(a0 + a) + in_off[ilist[i0 + i]] + n * xn];
     }
     __syncthreads();
-    for (int jb = warp * RJ; jb < nj; jb += nw * RJ) {
+    for (int jj = warp; jj < nj; jj += nw) {
+      const GMixEntry en = ent[n * nJ + jlist[j0 + jj]];
+      if (en.row < 0) continue;
+      const int64_t base = (int64_t)en.row * kmax + en.kst - en.lo;
+      const int b0 = rp[jj], b1 = rp[jj + 1];
       for (int ab = 0; ab < w; ab += 32 * RA) {
-        float s[RJ][RA], c[RJ][RA];
+        float s[RA], c[RA];
 #pragma unroll
-        for (int q = 0; q < RJ; ++q)
-#pragma unroll
-          for (int k = 0; k < RA; ++k) s[q][k] = c[q][k] = 0.0f;
-        for (int i = 0; i < ni; ++i) {
-          float xv[RA];
+        for (int k = 0; k < RA; ++k) s[k] = c[k] = 0.0f;
+        for (int e = b0; e < b1; ++e) {
+          const float* xr = stage + li[e] * w + ab + lane;
+          const float h = vh[e];
 #pragma unroll
           for (int k = 0; k < RA; ++k) {
-            const int a = ab + lane + 32 * k;
-            xv[k] = a < w ? stage[i * w + a] : 0.0f;
-          }
-#pragma unroll
-          for (int q = 0; q < RJ; ++q) {
-            const bool rowok = jb + q < nj;
-            const float vh = rowok ? wh[(jb + q) * ni + i] : 0.0f;
+            const float xv = (ab + lane + 32 * k < w) ? xr[32 * k] : 0.0f;
             if (TF) {
-              const float vl = rowok ? wl[(jb + q) * ni + i] : 0.0f;
-#pragma unroll
-              for (int k = 0; k < RA; ++k) {
-                const float p = vh * xv[k];
-                const float pe = fmaf(vh, xv[k], -p) + vl * xv[k];
-                const float t = s[q][k] + p, z = t - s[q][k];
-                c[q][k] += ((s[q][k] - (t - z)) + (p - z)) + pe;
-                s[q][k] = t;
-              }
+              const float p = h * xv;
+              const float pe = fmaf(h, xv, -p) + vl[e] * xv;
+              const float t = s[k] + p, z = t - s[k];
+              c[k] += ((s[k] - (t - z)) + (p - z)) + pe;
+              s[k] = t;
             } else {
-#pragma unroll
-              for (int k = 0; k < RA; ++k) s[q][k] = fmaf(vh, xv[k], s[q][k]);
+              s[k] = fmaf(h, xv, s[k]);
             }
           }
         }
 #pragma unroll
-        for (int q = 0; q < RJ; ++q) {
-          if (jb + q >= nj) break;
-          const GMixEntry en = ent[n * nJ + jlist[j0 + jb + q]];
-          if (en.row < 0) continue;
-          const int64_t base = (int64_t)en.row * kmax + en.kst - en.lo;
-#pragma unroll
-          for (int k = 0; k < RA; ++k) {
-            const int a = ab + lane + 32 * k;
-            if (a < w) split_put_f(hi, lo, base + a0 + a, s[q][k] + c[q][k]);
-          }
+        for (int k = 0; k < RA; ++k) {
+          const int a = ab + lane + 32 * k;
+          if (a < w) split_put_f(hi, lo, base + a0 + a, s[k] + c[k]);
         }
       }
     }
@@ -584,12 +576,14 @@ void gmix_staged_run(gb_ctx* ctx, const MixDev& m, const GMixStaged& g, const GM
              "grouped mix: staging buffer too large");
   if (out.esz == 4)
     gmix_staged_kernel<float><<<grid, 256, g.smem_tf32, ctx->stream>>>(
-        g.NL, m.nJ, m.xn, m.in_off, g.whi, g.wlo, g.wstart, t1, ent, g.rng, g.jlist, g.jstart,
-        g.ilist, g.istart, g.chunk_tf32, (float*)out.data, plane, out.kmax);
+        g.NL, m.nJ, m.xn, m.in_off, g.rp, g.li, g.vh, g.vl, g.rstart, g.cstart, t1, ent, g.rng,
+        g.jlist, g.jstart, g.ilist, g.istart, g.chunk_tf32, g.csr_floats_tf32, (float*)out.data,
+        plane, out.kmax);
   else
     gmix_staged_kernel<__nv_bfloat16><<<grid, 256, g.smem, ctx->stream>>>(
-        g.NL, m.nJ, m.xn, m.in_off, g.whi, g.wlo, g.wstart, t1, ent, g.rng, g.jlist, g.jstart,
-        g.ilist, g.istart, g.chunk, (__nv_bfloat16*)out.data, plane, out.kmax);
+        g.NL, m.nJ, m.xn, m.in_off, g.rp, g.li, g.vh, g.vl, g.rstart, g.cstart, t1, ent, g.rng,
+        g.jlist, g.jstart, g.ilist, g.istart, g.chunk, g.csr_floats, (__nv_bfloat16*)out.data,
+        plane, out.kmax);
   GB_CHECK_CUDA(cudaGetLastError());
   count_launch(ctx);
 }
@@ -776,6 +770,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
     const bool f32 = args.c_f32 != 0;
     const double alpha = args.alpha, beta = args.beta;
     const bool copy_f32 = f32 && alpha == 1.0 && beta == 0.0;
+    const bool alpha_one = alpha == 1.0, beta_one = beta == 1.0;
     auto loadC = [&](int64_t e) -> double {
       return f32 ? (double)((const float*)args.C)[e] : ((const double*)args.C)[e];
     };
@@ -823,7 +818,8 @@ __global__ void __launch_bounds__(G_THREADS, 1)
 #pragma unroll
             for (int jj = 0; jj < 16; ++jj) {
               co[jj] = __shfl_sync(0xffffffffu, myco, h + jj);
-              val[jj] = alpha * (double)__uint_as_float(v[h + jj]);
+              const double x = (double)__uint_as_float(v[h + jj]);
+              val[jj] = alpha_one ? x : alpha * x;
             }
             if (beta != 0.0 && rvalid) {
               double cv[16];
@@ -831,7 +827,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
               for (int jj = 0; jj < 16; ++jj)
                 cv[jj] = ((int64_t)T.n0 + c0 + h + jj < nend) ? loadC(roff + co[jj]) : 0.0;
 #pragma unroll
-              for (int jj = 0; jj < 16; ++jj) val[jj] = fma(beta, cv[jj], val[jj]);
+              for (int jj = 0; jj < 16; ++jj) val[jj] = beta_one ? cv[jj] + val[jj] : fma(beta, cv[jj], val[jj]);
             }
             if (rvalid) {
 #pragma unroll
@@ -854,7 +850,8 @@ __global__ void __launch_bounds__(G_THREADS, 1)
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
               ro[i] = __shfl_sync(0xffffffffu, roff, h + i);
-              val[i] = alpha * (double)xb[(h + i) * 33 + lane];
+              const double x = (double)xb[(h + i) * 33 + lane];
+              val[i] = alpha_one ? x : alpha * x;
             }
             if (beta != 0.0 && cvalid) {
               double cv[16];
@@ -862,7 +859,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
               for (int i = 0; i < 16; ++i)
                 cv[i] = (mrow0 + h + i < T.mlim) ? loadC(ro[i] + co) : 0.0;
 #pragma unroll
-              for (int i = 0; i < 16; ++i) val[i] = fma(beta, cv[i], val[i]);
+              for (int i = 0; i < 16; ++i) val[i] = beta_one ? cv[i] + val[i] : fma(beta, cv[i], val[i]);
             }
             if (cvalid) {
 #pragma unroll
@@ -932,11 +929,28 @@ __global__ void __launch_bounds__(G_THREADS, 1)
           float sum[32];
 #pragma unroll
           for (int jj = 0; jj < 32; ++jj) sum[jj] = 0.0f;
-          for (int u = 0; u < T.nsplit; ++u) {
-            const float* pu = args.partial + (size_t)(T.pslot + u) * (G_BM * G_BN) +
-                              (size_t)c0 * G_BM + 32 * q + lane;
+          // 8 columns x up to 8 units of loads in flight at a time; each column still sums
+          // its units in order 0, 1, 2, ...
+          const float* p0 = args.partial + (size_t)T.pslot * (G_BM * G_BN) + (size_t)c0 * G_BM +
+                            32 * q + lane;
 #pragma unroll
-            for (int jj = 0; jj < 32; ++jj) sum[jj] += __ldcg(pu + (size_t)jj * G_BM);
+          for (int cb = 0; cb < 32; cb += 8) {
+            for (int u0 = 0; u0 < T.nsplit; u0 += 8) {
+              float t[8][8];
+#pragma unroll
+              for (int uu = 0; uu < 8; ++uu)
+#pragma unroll
+                for (int jj = 0; jj < 8; ++jj)
+                  t[uu][jj] = (u0 + uu < T.nsplit)
+                                  ? __ldcg(p0 + (size_t)(u0 + uu) * (G_BM * G_BN) +
+                                           (size_t)(cb + jj) * G_BM)
+                                  : 0.0f;
+#pragma unroll
+              for (int uu = 0; uu < 8; ++uu)
+#pragma unroll
+                for (int jj = 0; jj < 8; ++jj)
+                  if (u0 + uu < T.nsplit) sum[cb + jj] += t[uu][jj];
+            }
           }
           uint32_t v[32];
 #pragma unroll

@@ -131,24 +131,29 @@ void gmix_run(gb_ctx* ctx, const MixDev& m, const GMixEntry* ent, int64_t span_m
               const float* t1, GOperand& out);
 // The same mix staged through shared memory.  The output rows J fall into groups whose
 // input range [lo, hi) is the same at every column n (rows of one charge); a block per
-// (column, group) loads the group's coefficients (dense, [rows][inputs]) and the inputs its
-// rows read -- once, coalesced -- and computes every row of the group from shared memory, a
-// few rows and columns per thread.  The sums run over the inputs in increasing order, as in
-// gmix_run (whose missing coefficients are exact zeros here): the results are identical.
+// (column, group) loads the group's rows (local CSR) and the inputs they read -- once,
+// coalesced -- into shared memory and computes every row of the group from there, four
+// columns per thread.  The sums run over each row's entries in the order of gmix_run: the
+// results are identical.
 struct GMixStaged {
   int NL = 0;              // row groups
   int chunk = 0;           // input rows a staged per pass (BF16 planes)
-  int chunk_tf32 = 0;      // the same with the TF32 coefficient halves in shared memory
-  size_t smem = 0;         // dynamic shared memory per block (BF16 planes)
-  size_t smem_tf32 = 0;    // (TF32 planes)
+  int chunk_tf32 = 0;      // (TF32 planes: the coefficients' lo halves are staged too)
+  int csr_floats = 0;      // shared-memory words of the largest group's rows
+  int csr_floats_tf32 = 0;
+  size_t smem = 0;         // dynamic shared memory per block
+  size_t smem_tf32 = 0;
   const int2* rng = nullptr;    // [N][NL]: (lo, hi) of group g at column n
   const int* jlist = nullptr;   // rows of group g: jlist[jstart[g] .. jstart[g + 1])
   const int* jstart = nullptr;
   const int* ilist = nullptr;   // inputs read by group g: ilist[istart[g] .. istart[g + 1])
   const int* istart = nullptr;
-  const float* whi = nullptr;   // coefficients of group g at whi[wstart[g]], [rows][inputs],
-  const float* wlo = nullptr;   // as hi + lo floats
-  const int* wstart = nullptr;
+  const int* rp = nullptr;      // row pointers of group g at rp[rstart[g]] (nj_g + 1 entries)
+  const int* rstart = nullptr;
+  const int* li = nullptr;      // entries of group g at [cstart[g], cstart[g + 1]): local
+  const float* vh = nullptr;    // input index and coefficient as hi + lo floats
+  const float* vl = nullptr;
+  const int* cstart = nullptr;
 };
 void gmix_staged_run(gb_ctx* ctx, const MixDev& m, const GMixStaged& g, const GMixEntry* ent,
                      const float* t1, GOperand& out);

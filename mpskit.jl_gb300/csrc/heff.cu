@@ -1676,10 +1676,10 @@ static void build_staged_mix(gb_heff* h, int64_t Dr) {
     if (h->lam_J[J] != INT64_MIN) byq[h->lam_J[J]].push_back((int)J);
   const int NL = (int)byq.size();
   if (NL == 0) return;
-  std::vector<int> jlist, jstart{0}, ilist, istart{0}, wstart;
-  std::vector<float> whi, wlo;  // per group: dense [rows][inputs] coefficients, hi + lo
+  std::vector<int> jlist, jstart{0}, ilist, istart{0}, rp, rstart, li, cstart{0};
+  std::vector<float> vh, vl;  // per group: its rows' entries (local input, coefficient hi + lo)
   std::vector<int2> rng((size_t)Dr * NL);
-  size_t max_w = 0, max_ni = 0;
+  size_t max_ni = 0, max_csr = 0, max_csr_tf = 0;
   int g = 0;
   for (const auto& kv : byq) {
     const std::vector<int>& Js = kv.second;
@@ -1689,16 +1689,18 @@ static void build_staged_mix(gb_heff* h, int64_t Dr) {
     std::sort(ins.begin(), ins.end());
     ins.erase(std::unique(ins.begin(), ins.end()), ins.end());
     const size_t ni = ins.size();
-    wstart.push_back((int)whi.size());
-    whi.resize(whi.size() + Js.size() * ni, 0.0f);
-    wlo.resize(whi.size(), 0.0f);
-    for (size_t jj = 0; jj < Js.size(); ++jj)
-      for (int e = mp.row_ptr[Js[jj]]; e < mp.row_ptr[Js[jj] + 1]; ++e) {
-        const size_t i = std::lower_bound(ins.begin(), ins.end(), mp.col[e]) - ins.begin();
-        const float vh = (float)mp.val[e];
-        whi[wstart.back() + jj * ni + i] = vh;
-        wlo[wstart.back() + jj * ni + i] = (float)(mp.val[e] - (double)vh);
+    rstart.push_back((int)rp.size());
+    for (int J : Js) {
+      rp.push_back((int)li.size());
+      for (int e = mp.row_ptr[J]; e < mp.row_ptr[J + 1]; ++e) {
+        li.push_back((int)(std::lower_bound(ins.begin(), ins.end(), mp.col[e]) - ins.begin()));
+        const float h = (float)mp.val[e];
+        vh.push_back(h);
+        vl.push_back((float)(mp.val[e] - (double)h));
       }
+    }
+    rp.push_back((int)li.size());
+    cstart.push_back((int)li.size());
     // one input range per (column, group): every row of the group must agree
     for (int64_t n = 0; n < Dr; ++n) {
       const int2 r0 = h->arange_h[(size_t)n * nJ + Js[0]];
@@ -1712,19 +1714,24 @@ static void build_staged_mix(gb_heff* h, int64_t Dr) {
     jstart.push_back((int)jlist.size());
     ilist.insert(ilist.end(), ins.begin(), ins.end());
     istart.push_back((int)ilist.size());
+    const size_t ne = (size_t)(cstart[g + 1] - cstart[g]);
     max_ni = std::max(max_ni, ni);
-    max_w = std::max(max_w, Js.size() * ni);
+    max_csr = std::max(max_csr, Js.size() + 1 + 2 * ne);        // rows, index, hi
+    max_csr_tf = std::max(max_csr_tf, Js.size() + 1 + 3 * ne);  // + lo
     ++g;
   }
-  // shared memory: the coefficients (hi, and lo for TF32 planes) plus a chunk of inputs
-  const int64_t cap = 96 * 1024 / 4;  // floats
+  // shared memory: the rows' entries plus a chunk of inputs
+  const int64_t cap = 96 * 1024 / 4;  // words
   const int64_t amax = std::max<int64_t>(h->arange_max, 1);
-  auto chunk_for = [&](int64_t wfloats) -> int64_t {
-    const int64_t room = cap - wfloats;
+  auto chunk_for = [&](int64_t words) -> int64_t {
+    const int64_t room = cap - words;
     if (room <= 0) return 0;
     return std::min<int64_t>(amax, room / (int64_t)std::max<size_t>(max_ni, 1));
   };
-  const int64_t chunk = chunk_for((int64_t)max_w), chunk_tf = chunk_for(2 * (int64_t)max_w);
+  // the staged inputs start 16-byte aligned after the entries
+  max_csr = (max_csr + 3) / 4 * 4;
+  max_csr_tf = (max_csr_tf + 3) / 4 * 4;
+  const int64_t chunk = chunk_for((int64_t)max_csr), chunk_tf = chunk_for((int64_t)max_csr_tf);
   if ((chunk < 32 && chunk < amax) || (chunk_tf < 32 && chunk_tf < amax) || chunk < 1 ||
       chunk_tf < 1)
     return;
@@ -1739,8 +1746,9 @@ static void build_staged_mix(gb_heff* h, int64_t Dr) {
   const size_t o_r = put(rng.data(), rng.size() * sizeof(int2));
   const size_t o_jl = put(jlist.data(), jlist.size() * 4), o_js = put(jstart.data(), jstart.size() * 4);
   const size_t o_il = put(ilist.data(), ilist.size() * 4), o_is = put(istart.data(), istart.size() * 4);
-  const size_t o_wh = put(whi.data(), whi.size() * 4), o_wl = put(wlo.data(), wlo.size() * 4);
-  const size_t o_ws = put(wstart.data(), wstart.size() * 4);
+  const size_t o_rp = put(rp.data(), rp.size() * 4), o_rs = put(rstart.data(), rstart.size() * 4);
+  const size_t o_li = put(li.data(), li.size() * 4), o_cs = put(cstart.data(), cstart.size() * 4);
+  const size_t o_vh = put(vh.data(), vh.size() * 4), o_vl = put(vl.data(), vl.size() * 4);
   char* d = (char*)dalloc(h, blob.size());
   GB_CHECK_CUDA(cudaMemcpyAsync(d, blob.data(), blob.size(), cudaMemcpyHostToDevice,
                                 h->ctx->stream));
@@ -1751,13 +1759,18 @@ static void build_staged_mix(gb_heff* h, int64_t Dr) {
   st.jstart = (const int*)(d + o_js);
   st.ilist = (const int*)(d + o_il);
   st.istart = (const int*)(d + o_is);
-  st.whi = (const float*)(d + o_wh);
-  st.wlo = (const float*)(d + o_wl);
-  st.wstart = (const int*)(d + o_ws);
+  st.rp = (const int*)(d + o_rp);
+  st.rstart = (const int*)(d + o_rs);
+  st.li = (const int*)(d + o_li);
+  st.cstart = (const int*)(d + o_cs);
+  st.vh = (const float*)(d + o_vh);
+  st.vl = (const float*)(d + o_vl);
   st.chunk = (int)chunk;
   st.chunk_tf32 = (int)chunk_tf;
-  st.smem = (size_t)(max_w + chunk * max_ni) * 4;
-  st.smem_tf32 = (size_t)(2 * max_w + chunk_tf * max_ni) * 4;
+  st.csr_floats = (int)max_csr;
+  st.csr_floats_tf32 = (int)max_csr_tf;
+  st.smem = (size_t)(st.csr_floats + chunk * max_ni) * 4;
+  st.smem_tf32 = (size_t)(st.csr_floats_tf32 + chunk_tf * max_ni) * 4;
   st.NL = NL;
 }
 
