@@ -159,7 +159,7 @@ void gplan_build(GPlan& p, const std::vector<int32_t>& labM, const std::vector<i
   {
     int64_t total = 0;
     for (const GTile& t : p.tiles) total += t.nkb;
-    const int64_t target = std::max<int64_t>(4, (total + 2 * sms - 1) / (2 * std::max(sms, 1)));
+    const int64_t target = std::max<int64_t>(8, (total + 2 * sms - 1) / (2 * std::max(sms, 1)));
     std::vector<GTile> units;
     for (const GTile& t : p.tiles) {
       if (t.nkb <= target + target / 2) {
@@ -929,28 +929,11 @@ __global__ void __launch_bounds__(G_THREADS, 1)
           float sum[32];
 #pragma unroll
           for (int jj = 0; jj < 32; ++jj) sum[jj] = 0.0f;
-          // 8 columns x up to 8 units of loads in flight at a time; each column still sums
-          // its units in order 0, 1, 2, ...
-          const float* p0 = args.partial + (size_t)T.pslot * (G_BM * G_BN) + (size_t)c0 * G_BM +
-                            32 * q + lane;
+          for (int u = 0; u < T.nsplit; ++u) {
+            const float* pu = args.partial + (size_t)(T.pslot + u) * (G_BM * G_BN) +
+                              (size_t)c0 * G_BM + 32 * q + lane;
 #pragma unroll
-          for (int cb = 0; cb < 32; cb += 8) {
-            for (int u0 = 0; u0 < T.nsplit; u0 += 8) {
-              float t[8][8];
-#pragma unroll
-              for (int uu = 0; uu < 8; ++uu)
-#pragma unroll
-                for (int jj = 0; jj < 8; ++jj)
-                  t[uu][jj] = (u0 + uu < T.nsplit)
-                                  ? __ldcg(p0 + (size_t)(u0 + uu) * (G_BM * G_BN) +
-                                           (size_t)(cb + jj) * G_BM)
-                                  : 0.0f;
-#pragma unroll
-              for (int uu = 0; uu < 8; ++uu)
-#pragma unroll
-                for (int jj = 0; jj < 8; ++jj)
-                  if (u0 + uu < T.nsplit) sum[cb + jj] += t[uu][jj];
-            }
+            for (int jj = 0; jj < 32; ++jj) sum[jj] += __ldcg(pu + (size_t)jj * G_BM);
           }
           uint32_t v[32];
 #pragma unroll

@@ -164,6 +164,20 @@ std::vector<Sector> make_sectors(const std::vector<int32_t>& qrow,
   return out;
 }
 
+// Sectors in decreasing order of factorisation work (the cube of the smaller side times the
+// larger): the lanes take the largest first, so the last sector to start is a small one.
+std::vector<int64_t> largest_first(const std::vector<Sector>& ss) {
+  std::vector<int64_t> o(ss.size());
+  std::iota(o.begin(), o.end(), 0);
+  auto work = [&](int64_t c) {
+    const double a = (double)ss[c].rows.size(), b = (double)ss[c].cols.size();
+    return std::min(a, b) * std::min(a, b) * std::max(a, b);
+  };
+  std::stable_sort(o.begin(), o.end(), [&](int64_t x, int64_t y) { return work(x) > work(y); });
+  return o;
+}
+
+
 // upload every sector's row and column lists into one device table
 struct IndexTable {
   DevBuf buf;
@@ -348,7 +362,9 @@ void u1_left_orth(gb_ctx* ctx, const gb_tensor* AC, const int32_t* ql, const int
   }
   std::vector<double> nrm(ss.size(), 0.0);
   // sectors are independent: one per lane at a time
-  run_on_lanes(ctx, (int64_t)ss.size(), [&](gb_ctx* L, int64_t c) {
+  const std::vector<int64_t> order = largest_first(ss);
+  run_on_lanes(ctx, (int64_t)ss.size(), [&](gb_ctx* L, int64_t oc) {
+    const int64_t c = order[oc];
     const Sector& s = ss[c];
     const int64_t ni = s.rows.size(), nj = s.cols.size(), kc = std::min(ni, nj);
     DevBuf Mb(L, ni * nj * es + 256), Qb(L, ni * kc * es + 256), Rb(L, kc * nj * es + 256);
@@ -398,7 +414,9 @@ void u1_right_orth(gb_ctx* ctx, const gb_tensor* AC, const int32_t* ql, const in
     ko += kc;
   }
   std::vector<double> nrm(ss.size(), 0.0);
-  run_on_lanes(ctx, (int64_t)ss.size(), [&](gb_ctx* L, int64_t c) {
+  const std::vector<int64_t> order = largest_first(ss);
+  run_on_lanes(ctx, (int64_t)ss.size(), [&](gb_ctx* L, int64_t oc) {
+    const int64_t c = order[oc];
     const Sector& s = ss[c];
     const int64_t ni = s.rows.size(), nj = s.cols.size(), kc = std::min(ni, nj);
     const size_t blk = ni * nj * es + 256;
@@ -480,7 +498,9 @@ void u1_svd_trunc(gb_ctx* ctx, const gb_tensor* AC2, const int32_t* ql, const in
   }
   DevBuf W(ctx, nsig * sizeof(double) + 256), info(ctx, ss.size() * sizeof(int) + 256);
   // sectors are independent: one per lane at a time
-  run_on_lanes(ctx, (int64_t)ss.size(), [&](gb_ctx* L, int64_t c) {
+  const std::vector<int64_t> order = largest_first(ss);
+  run_on_lanes(ctx, (int64_t)ss.size(), [&](gb_ctx* L, int64_t oc) {
+    const int64_t c = order[oc];
     const Fac& f = fs[c];
     void* Mc = at(f.oM);
     double* sc = sig.as<double>() + f.oS;
@@ -592,6 +612,13 @@ void u1_svd_trunc(gb_ctx* ctx, const gb_tensor* AC2, const int32_t* ql, const in
     ko += kc[c];
   }
   GB_TRACE(ctx);  // host-side truncation and output set-up end here
+  {
+    const std::vector<int64_t> order = largest_first(ss);
+    std::vector<int64_t> rank(ss.size());
+    for (size_t i = 0; i < order.size(); ++i) rank[order[i]] = (int64_t)i;
+    std::stable_sort(kept.begin(), kept.end(),
+                     [&](int64_t x, int64_t y) { return rank[x] < rank[y]; });
+  }
   run_on_lanes(ctx, (int64_t)kept.size(), [&](gb_ctx* L, int64_t idx) {
     const size_t c = (size_t)kept[idx];
     const Fac& f = fs[c];
