@@ -28,6 +28,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <climits>
 #include <map>
 #include <mutex>
 #include <numeric>
@@ -61,12 +62,18 @@ std::vector<int32_t> leg_labels(const std::vector<LegSpec>& legs,
   int64_t stride = 1;
   for (const LegSpec& l : legs) {
     const int32_t* c = (l.which > Q_NONE && l.which < Q_COUNT) ? q[l.which] : nullptr;
-    if (c)
-      for (int64_t i = 0; i < n; ++i) {
-        if (lab[i] == NO_LABEL) continue;
-        const int32_t ch = c[(i / stride) % l.n];
-        lab[i] = (ch == NO_LABEL) ? NO_LABEL : lab[i] + l.sign * ch;
-      }
+    if (c) {
+      // index i = inner + stride * (j + l.n * outer): leg value j, no divisions
+      for (int64_t base = 0; base < n; base += stride * l.n)
+        for (int64_t j = 0; j < l.n; ++j) {
+          const int32_t ch = c[j];
+          int32_t* dst = lab.data() + base + stride * j;
+          for (int64_t i = 0; i < stride; ++i) {
+            if (dst[i] == NO_LABEL) continue;
+            dst[i] = (ch == NO_LABEL) ? NO_LABEL : dst[i] + l.sign * ch;
+          }
+        }
+    }
     stride *= l.n;
   }
   return lab;
@@ -75,20 +82,28 @@ std::vector<int32_t> leg_labels(const std::vector<LegSpec>& legs,
 void gplan_build(GPlan& p, const std::vector<int32_t>& labM, const std::vector<int32_t>& labK,
                  const std::vector<int32_t>& labN, bool first_writer, int64_t ldc, int sms) {
   p = GPlan();
-  std::map<int32_t, int> cntM, cntN, cntK;
+  // labels are small integers (sums of charges): count them in dense arrays over their range
+  int32_t lo = INT32_MAX, hi = INT32_MIN;
+  for (const auto* lab : {&labM, &labN, &labK})
+    for (int32_t v : *lab)
+      if (v != NO_LABEL) {
+        lo = std::min(lo, v);
+        hi = std::max(hi, v);
+      }
+  const int64_t span = hi >= lo ? (int64_t)hi - lo + 1 : 0;
+  std::vector<int64_t> cntM(span, 0), cntN(span, 0), cntK(span, 0);
   for (int32_t v : labM)
-    if (v != NO_LABEL) ++cntM[v];
+    if (v != NO_LABEL) ++cntM[v - lo];
   for (int32_t v : labN)
-    if (v != NO_LABEL) ++cntN[v];
+    if (v != NO_LABEL) ++cntN[v - lo];
   for (int32_t v : labK)
-    if (v != NO_LABEL) ++cntK[v];
-  std::map<int32_t, int> gid;
-  for (const auto& kv : cntM) {
-    if (!cntN.count(kv.first)) continue;
-    if (!cntK.count(kv.first) && !first_writer) continue;
-    const int g = (int)p.label.size();
-    gid[kv.first] = g;
-    p.label.push_back(kv.first);
+    if (v != NO_LABEL) ++cntK[v - lo];
+  std::vector<int32_t> gid(span, -1);  // label - lo -> group
+  for (int64_t t = 0; t < span; ++t) {
+    if (!cntM[t] || !cntN[t]) continue;
+    if (!cntK[t] && !first_writer) continue;
+    gid[t] = (int32_t)p.label.size();
+    p.label.push_back((int32_t)(t + lo));
   }
   p.G = (int)p.label.size();
   const int G = p.G;
@@ -99,10 +114,10 @@ void gplan_build(GPlan& p, const std::vector<int32_t>& labM, const std::vector<i
     start.assign(G + 1, 0);
     for (size_t i = 0; i < lab.size(); ++i) {
       if (lab[i] == NO_LABEL) continue;
-      auto it = gid.find(lab[i]);
-      if (it == gid.end()) continue;
-      g_of[i] = it->second;
-      ++start[it->second + 1];
+      const int32_t g = gid[lab[i] - lo];
+      if (g < 0) continue;
+      g_of[i] = g;
+      ++start[g + 1];
     }
     for (int g = 0; g < G; ++g) start[g + 1] += start[g];
     dense.assign(start[G], 0);
@@ -285,11 +300,24 @@ __global__ void gpack_kernel(const GPackTile* __restrict__ tiles, const int32_t*
                              const int32_t* __restrict__ kdense, const int32_t* __restrict__ kstart,
                              const int32_t* __restrict__ klen, const double* __restrict__ src,
                              int64_t rs, int64_t ks, int rowfast, E* __restrict__ hi,
-                             int64_t plane, int64_t kmax, unsigned long long* nnz) {
+                             int64_t plane, int64_t kmax, unsigned long long* nnz, int64_t klo,
+                             int64_t khi) {
   __shared__ float t[32][33];
+  __shared__ unsigned char in[32];  // column in this pack's K range
   const GPackTile T = tiles[blockIdx.x];
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int32_t kl = klen[T.g], k0 = kstart[T.g];
+  const bool full = klo == 0 && khi == INT64_MAX;
+  if (ty == 0) {
+    const int kp = T.kp0 + tx;
+    bool inr = full;
+    if (kp < kl) {
+      const int64_t kd = kdense[k0 + kp];
+      inr = kd >= klo && kd < khi;
+    }
+    in[tx] = inr ? 1 : 0;
+  }
+  __syncthreads();
   // load with the source's contiguous index on threadIdx.x; the planes keep at most 22 bits,
   // so the value is rounded to FP32 once and split there
   for (int j = ty; j < 32; j += 8) {
@@ -297,18 +325,19 @@ __global__ void gpack_kernel(const GPackTile* __restrict__ tiles, const int32_t*
     const int kk = rowfast ? j : tx;   // column within the block
     const int kp = T.kp0 + kk;
     float v = 0.0f;
-    if (i < T.nr && kp < kl)
-      v = (float)src[(int64_t)rdense[T.rp0 + i] * rs + (int64_t)kdense[k0 + kp] * ks];
+    if (i < T.nr && kp < kl && in[kk])
+      v = (float)src[(int64_t)rdense[T.rp0 + i] * rs + ((int64_t)kdense[k0 + kp] - klo) * ks];
     t[i][kk] = v;
   }
   __syncthreads();
   E* lo = hi + plane;
   int nz = 0;
-  for (int i = ty; i < T.nr; i += 8) {
-    const float v = t[i][tx];
-    nz += (v != 0.0f);
-    split_put_f(hi, lo, (int64_t)(T.rp0 + i) * kmax + T.kp0 + tx, v);
-  }
+  if (in[tx])
+    for (int i = ty; i < T.nr; i += 8) {
+      const float v = t[i][tx];
+      nz += (v != 0.0f);
+      split_put_f(hi, lo, (int64_t)(T.rp0 + i) * kmax + T.kp0 + tx, v);
+    }
   if (nnz) {
     for (int o = 16; o > 0; o >>= 1) nz += __shfl_down_sync(0xffffffffu, nz, o);
     if ((threadIdx.x & 31) == 0 && nz) atomicAdd(nnz, (unsigned long long)nz);
@@ -368,7 +397,7 @@ static int64_t nnz_read(gb_ctx* ctx, unsigned long long* d) {
 }
 
 int64_t gpack(gb_ctx* ctx, const GPlan& p, int side, const double* src, int64_t rs, int64_t ks,
-              GOperand& op, bool count_nnz) {
+              GOperand& op, bool count_nnz, int64_t klo, int64_t khi) {
   const GSide& sd = p.side[side];
   if (sd.ptiles.empty()) return 0;
   unsigned long long* cnt = count_nnz ? nnz_counter(ctx) : nullptr;
@@ -378,11 +407,11 @@ int64_t gpack(gb_ctx* ctx, const GPlan& p, int side, const double* src, int64_t 
   if (op.esz == 4)
     gpack_kernel<float><<<grid, dim3(32, 8), 0, ctx->stream>>>(
         p.d_ptiles[side], p.d_dense[side], p.d_kdense, p.d_kstart, p.d_klen, src, rs, ks,
-        rowfast, (float*)op.data, plane, op.kmax, cnt);
+        rowfast, (float*)op.data, plane, op.kmax, cnt, klo, khi);
   else
     gpack_kernel<__nv_bfloat16><<<grid, dim3(32, 8), 0, ctx->stream>>>(
         p.d_ptiles[side], p.d_dense[side], p.d_kdense, p.d_kstart, p.d_klen, src, rs, ks,
-        rowfast, (__nv_bfloat16*)op.data, plane, op.kmax, cnt);
+        rowfast, (__nv_bfloat16*)op.data, plane, op.kmax, cnt, klo, khi);
   GB_CHECK_CUDA(cudaGetLastError());
   count_launch(ctx);
   return cnt ? nnz_read(ctx, cnt) : 0;

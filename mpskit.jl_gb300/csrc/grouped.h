@@ -111,9 +111,12 @@ size_t goperand_bytes(const GPlan& p, int side, int prec);
 void goperand_init(gb_ctx* ctx, GOperand& op, const GPlan& p, int side, void* data, int prec);
 // pack the original operand of `side` from a dense FP64 matrix: element (row r, k) of the
 // operand at src[r * rs + k * ks]; returns the nonzero count of the packed blocks when
-// count_nnz is set (synchronises), else 0
+// count_nnz is set (synchronises), else 0.  With a range [klo, khi) of the plan's dense K
+// index only those K members are packed, from src[r * rs + (k - klo) * ks], and nothing else
+// of the operand is written: two sources stacked along K (a merged GEMM) pack separately.
 int64_t gpack(gb_ctx* ctx, const GPlan& p, int side, const double* src, int64_t rs, int64_t ks,
-              GOperand& op, bool count_nnz = false);
+              GOperand& op, bool count_nnz = false, int64_t klo = 0,
+              int64_t khi = INT64_MAX);
 // nonzero count of a dense column-major FP64 matrix rows x cols (leading dimension ld)
 int64_t dense_nnz(gb_ctx* ctx, const double* src, int64_t rows, int64_t cols, int64_t ld);
 // nonzero entries (r, k) of an operand (element at src[r * rs + k * ks]) whose labels

@@ -181,6 +181,11 @@ struct gb_heff {
   std::vector<int32_t> q_l, q_r, q_p1, q_p2, dq_l, dq_r;  // charges (host)
   std::vector<int2> arange_h;    // host copy of arange
   std::vector<GStep> gsteps;     // index-aligned with steps
+  // a step whose GEMM runs inside another's (the constant-x term CA / C stacked along K
+  // onto the chain's last GEMM, same output blocks): merged_into[i] = that step, else -1;
+  // merged_k[j] = K of step j's own part when step j carries a merged step
+  std::vector<int> merged_into;
+  std::vector<int64_t> merged_k;
   gb::GMixEntry* gmix = nullptr;
   gb::GMixStaged gmix_st;        // staged form of the same mix (gmix_st.NL > 0 when built)
   std::vector<int64_t> lam_J;    // charge of every chain row J (INT64_MIN: channel absent)
@@ -1573,15 +1578,47 @@ static void grouped_prepare(gb_heff* h) {
   auto alloc = [h](size_t b) { return dalloc(h, b); };
   h->gsteps.assign(h->steps.size(), GStep());
   h->t2_step = -1;
+  // the term X . M with the chain's last GEMM's output blocks (CA for AC2, C for AC) runs
+  // inside that GEMM: both are Y[l, (s r)] (+)= A[l, k] B[k, (s r)], so their K spaces stack
+  // (GLc | X) . (T2 ; M) and Y is written once
+  h->merged_into.assign(h->steps.size(), -1);
+  h->merged_k.assign(h->steps.size(), 0);
+  {
+    int i3 = -1, ic = -1;
+    for (size_t i = 0; i < h->steps.size(); ++i) {
+      const Step& st = h->steps[i];
+      if (st.is_gemm && st.t2_consumer) i3 = (int)i;
+      if (st.is_gemm && (st.name == "CA" || st.name == "C") && st.srcA == S_X &&
+          st.srcB == S_CONST && st.dst == S_Y)
+        ic = (int)i;
+    }
+    if (i3 >= 0 && ic > i3) {
+      const Step &a = h->steps[i3], &c = h->steps[ic];
+      if (a.dst == S_Y && a.M == c.M && a.N == c.N && a.ldc == c.ldc && c.accumulate &&
+          a.opA == 'N' && a.opB == 'N' && c.opA == 'N' && c.opB == 'N') {
+        h->merged_into[ic] = i3;
+        h->merged_k[i3] = a.K;
+      }
+    }
+  }
   for (size_t i = 0; i < h->steps.size(); ++i) {
     const Step& st = h->steps[i];
-    if (!st.is_gemm) continue;
+    if (!st.is_gemm || h->merged_into[i] >= 0) continue;
     GB_REQUIRE(st.opA == 'N' && st.opB == 'N', "grouped: transposed operands");
-    const std::vector<int32_t> lM = leg_labels(st.lM, q), lK = leg_labels(st.lK, q),
-                               lN = leg_labels(st.lN, q);
+    const std::vector<int32_t> lM = leg_labels(st.lM, q), lN = leg_labels(st.lN, q);
+    std::vector<int32_t> lK = leg_labels(st.lK, q);
     GB_REQUIRE((int64_t)lM.size() == st.M && (int64_t)lK.size() == st.K &&
                    (int64_t)lN.size() == st.N,
                "grouped: labels do not match the GEMM shape of step " + st.name);
+    const Step* mc = nullptr;  // the merged step, if any
+    std::vector<int32_t> lKc;
+    for (size_t j = 0; j < h->steps.size(); ++j)
+      if (h->merged_into[j] == (int)i) mc = &h->steps[j];
+    if (mc) {
+      lKc = leg_labels(mc->lK, q);
+      GB_REQUIRE((int64_t)lKc.size() == mc->K, "grouped: labels of the merged step");
+      lK.insert(lK.end(), lKc.begin(), lKc.end());
+    }
     GStep& gs = h->gsteps[i];
     gplan_build(gs.plan, lM, lK, lN, !st.accumulate, st.ldc, std::max(1, ctx->num_sms));
     gplan_upload(ctx, gs.plan, alloc);
@@ -1592,15 +1629,26 @@ static void grouped_prepare(gb_heff* h) {
     // whose row and column labels differ would be dropped by the blocks: refuse it (entries
     // of a conserved label that has no group on the other side of the GEMM meet only zeros
     // of x and are dropped rightly)
+    const std::vector<int32_t> lKs(lK.begin(), lK.begin() + st.K);  // this step's own K
+    const int64_t kown = mc ? st.K : INT64_MAX;
     if (st.srcA == S_CONST) {
-      GB_REQUIRE(label_violations(ctx, (const double*)st.cA, st.M, st.K, 1, st.lda, lM, lK) == 0,
+      GB_REQUIRE(label_violations(ctx, (const double*)st.cA, st.M, st.K, 1, st.lda, lM, lKs) == 0,
                  "grouped: operator term " + st.name + " does not conserve the given charges");
-      gpack(ctx, gs.plan, 0, (const double*)st.cA, 1, st.lda, gs.op[0]);
+      gpack(ctx, gs.plan, 0, (const double*)st.cA, 1, st.lda, gs.op[0], false, 0, kown);
     }
     if (st.srcB == S_CONST) {
-      GB_REQUIRE(label_violations(ctx, (const double*)st.cB, st.N, st.K, st.ldb, 1, lN, lK) == 0,
+      GB_REQUIRE(label_violations(ctx, (const double*)st.cB, st.N, st.K, st.ldb, 1, lN, lKs) == 0,
                  "grouped: operator term " + st.name + " does not conserve the given charges");
-      gpack(ctx, gs.plan, 1, (const double*)st.cB, st.ldb, 1, gs.op[1]);
+      gpack(ctx, gs.plan, 1, (const double*)st.cB, st.ldb, 1, gs.op[1], false, 0, kown);
+    }
+    if (mc) {
+      // the merged step's constant B at K offset st.K (its A is x, packed every apply)
+      GB_REQUIRE(mc->srcB == S_CONST && mc->srcA == S_X, "grouped: merged step operands");
+      GB_REQUIRE(label_violations(ctx, (const double*)mc->cB, mc->N, mc->K, mc->ldb, 1, lN,
+                                  lKc) == 0,
+                 "grouped: operator term " + mc->name + " does not conserve the given charges");
+      gpack(ctx, gs.plan, 1, (const double*)mc->cB, mc->ldb, 1, gs.op[1], false, st.K,
+            st.K + mc->K);
     }
     if (st.t2_consumer) {
       GB_REQUIRE(st.srcB == S_T2, "grouped: T2 is the B operand of its consumer");
@@ -1784,10 +1832,17 @@ static void heff_apply_grouped(gb_heff* h, const void* x, void* y) {
   if (h->y_zero_first || y != h->yfull) fill_zero(ctx, y, (size_t)h->xnumel * elem_size(h->dtype));
   for (size_t i = 0; i < h->steps.size(); ++i) {
     const Step& st = h->steps[i];
+    if (st.is_gemm && h->merged_into[i] >= 0) continue;  // runs inside its carrier's GEMM
     if (st.is_gemm) {
       GStep& gs = h->gsteps[i];
-      if (st.srcA == S_X) gpack(ctx, gs.plan, 0, (const double*)x, 1, st.lda, gs.op[0]);
-      if (st.srcB == S_X) gpack(ctx, gs.plan, 1, (const double*)x, st.ldb, 1, gs.op[1]);
+      const int64_t kown = h->merged_k[i] ? st.K : INT64_MAX;
+      if (st.srcA == S_X) gpack(ctx, gs.plan, 0, (const double*)x, 1, st.lda, gs.op[0], false, 0, kown);
+      if (st.srcB == S_X) gpack(ctx, gs.plan, 1, (const double*)x, st.ldb, 1, gs.op[1], false, 0, kown);
+      if (h->merged_k[i])
+        for (size_t j = 0; j < h->steps.size(); ++j)
+          if (h->merged_into[j] == (int)i)  // the merged term's x . M: A = x at K offset st.K
+            gpack(ctx, gs.plan, 0, (const double*)x, 1, h->steps[j].lda, gs.op[0], false, st.K,
+                  st.K + h->steps[j].K);
       const bool t1 = st.dst == S_T1;
       gemm_grouped(ctx, gs.plan, gs.op[0], gs.op[1], 1.0, st.accumulate ? 1.0 : 0.0,
                    t1 ? h->t1 : y, t1);
@@ -1909,6 +1964,8 @@ std::string heff_describe(const gb_heff* h) {
     const Step& s = h->steps[i];
     os << s.name << (s.is_gemm ? " gemm" : " mix");
     if (s.is_gemm) os << " M=" << s.M << " N=" << s.N << " K=" << s.K;
+    if (i < h->merged_into.size() && h->merged_into[i] >= 0)
+      os << " (stacked along K into " << h->steps[h->merged_into[i]].name << ")";
     if (i < h->gsteps.size() && !h->gsteps[i].plan.tiles.empty()) {
       const GPlan& p = h->gsteps[i].plan;
       int64_t maxkb = 0, kb = 0;
