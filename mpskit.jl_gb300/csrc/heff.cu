@@ -1666,6 +1666,8 @@ static void grouped_prepare(gb_heff* h) {
         ngrp[P.side[1].dense[r]] = g;
       }
       for (int32_t k = P.kstart[g]; k < P.kstart[g + 1]; ++k) {
+        // K members past T2's rows belong to a term stacked along K (its x . M part)
+        if (P.kdense[k] >= h->t2K) continue;
         kpos[P.kdense[k]] = k - P.kstart[g];
         kgrp[P.kdense[k]] = g;
       }
