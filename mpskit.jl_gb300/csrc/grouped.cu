@@ -510,25 +510,23 @@ void gmix_run(gb_ctx* ctx, const MixDev& m, const GMixEntry* ent, int64_t span_m
   count_launch(ctx);
 }
 
-constexpr int GMIX_CPB = 8;     // columns per block of the staged mix
-constexpr int GMIX_PREF = 48;   // inputs per thread prefetched into registers
-
 template <typename E>
-__global__ void __launch_bounds__(256)
-    gmix_staged_kernel(int NL, int64_t N, int64_t nJ, int64_t xn,
-                       const int64_t* __restrict__ in_off, const int* __restrict__ grp,
-                       const int* __restrict__ gli, const float* __restrict__ gvh,
-                       const float* __restrict__ gvl, const int* __restrict__ rstart,
-                       const int* __restrict__ cstart, const float* __restrict__ x,
-                       const GMixEntry* __restrict__ ent, const int2* __restrict__ rng,
-                       const int* __restrict__ jlist, const int* __restrict__ jstart,
-                       const int* __restrict__ ilist, const int* __restrict__ istart, int chunk,
-                       int csr_floats, E* __restrict__ hi, int64_t plane, int64_t kmax) {
+__global__ void gmix_staged_kernel(int NL, int64_t nJ, int64_t xn, const int64_t* __restrict__ in_off,
+                                   const int* __restrict__ grp, const int* __restrict__ gli,
+                                   const float* __restrict__ gvh, const float* __restrict__ gvl,
+                                   const int* __restrict__ rstart, const int* __restrict__ cstart,
+                                   const float* __restrict__ x, const GMixEntry* __restrict__ ent,
+                                   const int2* __restrict__ rng, const int* __restrict__ jlist,
+                                   const int* __restrict__ jstart, const int* __restrict__ ilist,
+                                   const int* __restrict__ istart, int chunk, int csr_floats,
+                                   E* __restrict__ hi, int64_t plane, int64_t kmax) {
   constexpr bool TF = std::is_same<E, float>::value;
   constexpr int RA = 4;  // 32-lane columns per thread
   extern __shared__ float sm[];
   const int g = blockIdx.y;
-  const int64_t nb = (int64_t)blockIdx.x * GMIX_CPB;
+  const int64_t n = blockIdx.x;
+  const int2 r = rng[n * NL + g];
+  if (r.y <= r.x) return;
   const int i0 = istart[g], ni = istart[g + 1] - i0;
   const int j0 = jstart[g], nj = jstart[g + 1] - j0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -546,17 +544,27 @@ __global__ void __launch_bounds__(256)
     if (TF) vl[k] = gvl[e0 + k];
   }
   E* lo = hi + plane;
-  // rows of the group from the inputs staged for columns [a0, a0 + w) of column n
-  auto compute = [&](int64_t n, int a0, int w) {
+  // base offset of every staged input of this column (one dependent lookup per input)
+  int64_t* ibase = (int64_t*)(stage + ni * chunk + (ni * chunk & 1));
+  for (int i = threadIdx.x; i < ni; i += blockDim.x) ibase[i] = in_off[ilist[i0 + i]] + n * xn;
+  __syncthreads();
+  for (int a0 = r.x; a0 < r.y; a0 += chunk) {
+    const int w = min(chunk, r.y - a0);
+#pragma unroll 4
+    for (int idx = threadIdx.x; idx < ni * w; idx += blockDim.x) {
+      const int i = idx / w, a = idx - i * w;
+      stage[idx] = x[(int64_t)(a0 + a) + ibase[i]];
+    }
+    __syncthreads();
     for (int jj = warp; jj < nj; jj += nw) {
       const GMixEntry en = ent[n * nJ + jlist[j0 + jj]];
       if (en.row < 0) continue;
       const int64_t base = (int64_t)en.row * kmax + en.kst - en.lo;
       const int b0 = rp[jj], b1 = rp[jj + 1];
       for (int ab = 0; ab < w; ab += 32 * RA) {
-        float sacc[RA], cacc[RA];
+        float s[RA], c[RA];
 #pragma unroll
-        for (int k = 0; k < RA; ++k) sacc[k] = cacc[k] = 0.0f;
+        for (int k = 0; k < RA; ++k) s[k] = c[k] = 0.0f;
         for (int e = b0; e < b1; ++e) {
           const float* xr = stage + li[e] * w + ab + lane;
           const float h = vh[e];
@@ -566,77 +574,22 @@ __global__ void __launch_bounds__(256)
             if (TF) {
               const float p = h * xv;
               const float pe = fmaf(h, xv, -p) + vl[e] * xv;
-              const float t = sacc[k] + p, z = t - sacc[k];
-              cacc[k] += ((sacc[k] - (t - z)) + (p - z)) + pe;
-              sacc[k] = t;
+              const float t = s[k] + p, z = t - s[k];
+              c[k] += ((s[k] - (t - z)) + (p - z)) + pe;
+              s[k] = t;
             } else {
-              sacc[k] = fmaf(h, xv, sacc[k]);
+              s[k] = fmaf(h, xv, s[k]);
             }
           }
         }
 #pragma unroll
         for (int k = 0; k < RA; ++k) {
           const int a = ab + lane + 32 * k;
-          if (a < w) split_put_f(hi, lo, base + a0 + a, sacc[k] + cacc[k]);
+          if (a < w) split_put_f(hi, lo, base + a0 + a, s[k] + c[k]);
         }
       }
     }
-  };
-  // the columns of this block; the inputs of the next column are loaded into registers
-  // while the current one is computed (when they fit), else staged chunk by chunk
-  float pre[GMIX_PREF];
-  auto fits = [&](int2 r) {
-    return r.y - r.x <= chunk && (int64_t)ni * (r.y - r.x) <= (int64_t)GMIX_PREF * blockDim.x;
-  };
-  auto prefetch = [&](int64_t n, int2 r) {
-    const int w = r.y - r.x;
-#pragma unroll
-    for (int k = 0; k < GMIX_PREF; ++k) {
-      const int idx = threadIdx.x + k * blockDim.x;
-      pre[k] = 0.0f;
-      if (idx < ni * w) {
-        const int i = idx / w, a = idx - i * w;
-        pre[k] = x[(int64_t)(r.x + a) + in_off[ilist[i0 + i]] + n * xn];
-      }
-    }
-  };
-  const int64_t nend = min(N, nb + GMIX_CPB);
-  int2 rcur = nb < nend ? rng[nb * NL + g] : int2{0, 0};
-  if (nb < nend && rcur.y > rcur.x && fits(rcur)) prefetch(nb, rcur);
-  __syncthreads();  // the rows' entries are in shared memory
-  for (int64_t n = nb; n < nend; ++n) {
-    const int2 r = rcur;
-    const int2 rnext = n + 1 < nend ? rng[(n + 1) * NL + g] : int2{0, 0};
-    if (r.y <= r.x) {
-      rcur = rnext;
-      if (rnext.y > rnext.x && fits(rnext)) prefetch(n + 1, rnext);
-      continue;
-    }
-    const int w = r.y - r.x;
-    if (fits(r)) {
-#pragma unroll
-      for (int k = 0; k < GMIX_PREF; ++k) {
-        const int idx = threadIdx.x + k * blockDim.x;
-        if (idx < ni * w) stage[idx] = pre[k];
-      }
-      __syncthreads();
-      if (n + 1 < nend && rnext.y > rnext.x && fits(rnext)) prefetch(n + 1, rnext);
-      compute(n, r.x, w);
-      __syncthreads();
-    } else {
-      for (int a0 = r.x; a0 < r.y; a0 += chunk) {
-        const int wc = min(chunk, r.y - a0);
-        for (int idx = threadIdx.x; idx < ni * wc; idx += blockDim.x) {
-          const int i = idx / wc, a = idx - i * wc;
-          stage[idx] = x[(int64_t)(a0 + a) + in_off[ilist[i0 + i]] + n * xn];
-        }
-        __syncthreads();
-        compute(n, a0, wc);
-        __syncthreads();
-      }
-      if (n + 1 < nend && rnext.y > rnext.x && fits(rnext)) prefetch(n + 1, rnext);
-    }
-    rcur = rnext;
+    __syncthreads();
   }
 }
 
@@ -644,7 +597,7 @@ void gmix_staged_run(gb_ctx* ctx, const MixDev& m, const GMixStaged& g, const GM
                      const float* t1, GOperand& out) {
   GB_REQUIRE(!m.cplx && m.xa == 1, "grouped mix: real data with unit input stride");
   GB_REQUIRE(g.NL <= 65535 && m.N <= 0x7fffffff, "grouped mix: grid too large");
-  dim3 grid((unsigned)((m.N + GMIX_CPB - 1) / GMIX_CPB), (unsigned)g.NL);
+  dim3 grid((unsigned)m.N, (unsigned)g.NL);
   const int64_t plane = out.rows * out.kmax;
   static std::once_flag attr_once;
   std::call_once(attr_once, [] {
@@ -657,14 +610,14 @@ void gmix_staged_run(gb_ctx* ctx, const MixDev& m, const GMixStaged& g, const GM
              "grouped mix: staging buffer too large");
   if (out.esz == 4)
     gmix_staged_kernel<float><<<grid, 256, g.smem_tf32, ctx->stream>>>(
-        g.NL, m.N, m.nJ, m.xn, m.in_off, g.rp, g.li, g.vh, g.vl, g.rstart, g.cstart, t1, ent,
-        g.rng, g.jlist, g.jstart, g.ilist, g.istart, g.chunk_tf32, g.csr_floats_tf32,
-        (float*)out.data, plane, out.kmax);
+        g.NL, m.nJ, m.xn, m.in_off, g.rp, g.li, g.vh, g.vl, g.rstart, g.cstart, t1, ent, g.rng,
+        g.jlist, g.jstart, g.ilist, g.istart, g.chunk_tf32, g.csr_floats_tf32, (float*)out.data,
+        plane, out.kmax);
   else
     gmix_staged_kernel<__nv_bfloat16><<<grid, 256, g.smem, ctx->stream>>>(
-        g.NL, m.N, m.nJ, m.xn, m.in_off, g.rp, g.li, g.vh, g.vl, g.rstart, g.cstart, t1, ent,
-        g.rng, g.jlist, g.jstart, g.ilist, g.istart, g.chunk, g.csr_floats,
-        (__nv_bfloat16*)out.data, plane, out.kmax);
+        g.NL, m.nJ, m.xn, m.in_off, g.rp, g.li, g.vh, g.vl, g.rstart, g.cstart, t1, ent, g.rng,
+        g.jlist, g.jstart, g.ilist, g.istart, g.chunk, g.csr_floats, (__nv_bfloat16*)out.data,
+        plane, out.kmax);
   GB_CHECK_CUDA(cudaGetLastError());
   count_launch(ctx);
 }

@@ -1774,7 +1774,8 @@ static void build_staged_mix(gb_heff* h, int64_t Dr) {
   const int64_t cap = 96 * 1024 / 4;  // words
   const int64_t amax = std::max<int64_t>(h->arange_max, 1);
   auto chunk_for = [&](int64_t words) -> int64_t {
-    const int64_t room = cap - words;
+    // the inputs' base offsets (int64 each, 8-byte aligned) follow the staged chunk
+    const int64_t room = cap - words - 2 * (int64_t)max_ni - 4;
     if (room <= 0) return 0;
     return std::min<int64_t>(amax, room / (int64_t)std::max<size_t>(max_ni, 1));
   };
@@ -1819,8 +1820,8 @@ static void build_staged_mix(gb_heff* h, int64_t Dr) {
   st.chunk_tf32 = (int)chunk_tf;
   st.csr_floats = (int)max_csr;
   st.csr_floats_tf32 = (int)max_csr_tf;
-  st.smem = (size_t)(st.csr_floats + chunk * max_ni) * 4;
-  st.smem_tf32 = (size_t)(st.csr_floats_tf32 + chunk_tf * max_ni) * 4;
+  st.smem = (size_t)(st.csr_floats + chunk * max_ni + 1) * 4 + (size_t)max_ni * 8;
+  st.smem_tf32 = (size_t)(st.csr_floats_tf32 + chunk_tf * max_ni + 1) * 4 + (size_t)max_ni * 8;
   st.NL = NL;
 }
 
