@@ -344,9 +344,11 @@ int gb_ctx_set_svd_method(gb_ctx* ctx, int method);
 enum { GB_EIG_SYEVD = 0, GB_EIG_SYEVJ = 1 };
 int gb_ctx_set_gauge(gb_ctx* ctx, int eig_method, int lanes);
 /* Implementation switches that leave every result unchanged (for comparisons):
- *   GB_OPT_STAGED_MIX (default 1): the U(1) chain mix of the grouped schedule stages the
- *   inputs of each charge's rows through shared memory (0: one warp per output row and
- *   column reading the intermediate directly); both sum in the same order. */
+ *   GB_OPT_STAGED_MIX: the U(1) chain mix of the grouped schedule either stages the inputs
+ *   of each charge's rows through shared memory or runs one warp per output row and column
+ *   reading the intermediate directly; both sum in the same order.  0: direct, 2: staged,
+ *   1 (default): staged when the mix has at least 4 entries per row (a long-range MPO's
+ *   chain mix is close to a permutation, ~1 entry per row, where the direct form wins). */
 enum { GB_OPT_STAGED_MIX = 0 };
 int gb_ctx_set_option(gb_ctx* ctx, int option, int64_t value);
 /* Truncated SVD of a two-site tensor, gauge2! (src/states/orthoview.jl:401-420) with

@@ -963,7 +963,10 @@ int gb_ctx_set_option(gb_ctx* ctx, int option, int64_t value) {
   API_BEGIN
   GB_REQUIRE(ctx, "null context");
   switch (option) {
-    case GB_OPT_STAGED_MIX: ctx->staged_mix = value != 0; break;
+    case GB_OPT_STAGED_MIX:
+      GB_REQUIRE(value >= 0 && value <= 2, "staged_mix: 0, 1 or 2");
+      ctx->staged_mix = (int)value;
+      break;
     default: throw Error(GB_ERR_ARG, "unknown option");
   }
   API_END

@@ -84,7 +84,8 @@ struct gb_ctx {
   int svd_method = 0;            // GB_SVD_* of gb_svd_trunc
   int eig_method = 0;            // GB_EIG_* of the Gram eigenproblems
   int lane_max = 8;              // host-thread lanes for per-sector work
-  bool staged_mix = true;        // the grouped chain mix staged through shared memory
+  int staged_mix = 1;            // chain mix staged through shared memory: 0 never, 1 when
+                                 // its rows have >= 4 entries on average, 2 always
   // split-precision GEMM schedule (GB_SCHED_*) and output tile width (0 = chosen per shape)
   int gemm_schedule = GB_SCHED_GROUPED;
   int gemm_bn = 0;

@@ -140,6 +140,7 @@ void gmix_run(gb_ctx* ctx, const MixDev& m, const GMixEntry* ent, int64_t span_m
 // results are identical.
 struct GMixStaged {
   int NL = 0;              // row groups
+  double nnz_per_row = 0;  // mix entries per output row (the staged form pays off when dense)
   int chunk = 0;           // input rows a staged per pass (BF16 planes)
   int chunk_tf32 = 0;      // (TF32 planes: the coefficients' lo halves are staged too)
   int csr_floats = 0;      // shared-memory words of the largest group's rows

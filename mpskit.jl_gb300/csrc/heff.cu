@@ -1818,6 +1818,7 @@ static void build_staged_mix(gb_heff* h, int64_t Dr) {
   st.vl = (const float*)(d + o_vl);
   st.chunk = (int)chunk;
   st.chunk_tf32 = (int)chunk_tf;
+  st.nnz_per_row = jlist.empty() ? 0.0 : (double)li.size() / (double)jlist.size();
   st.csr_floats = (int)max_csr;
   st.csr_floats_tf32 = (int)max_csr_tf;
   st.smem = (size_t)(st.csr_floats + chunk * max_ni + 1) * 4 + (size_t)max_ni * 8;
@@ -1851,7 +1852,10 @@ static void heff_apply_grouped(gb_heff* h, const void* x, void* y) {
                    t1 ? h->t1 : y, t1);
       if (ctx->counting) gcount_products(ctx, gs.plan, gs.op[0], gs.op[1]);
     } else if (st.t2_producer) {
-      if (h->gmix_st.NL > 0 && ctx->staged_mix)
+      const bool staged = h->gmix_st.NL > 0 &&
+                          (ctx->staged_mix == 2 ||
+                           (ctx->staged_mix == 1 && h->gmix_st.nnz_per_row >= 4.0));
+      if (staged)
         gmix_staged_run(ctx, st.mix, h->gmix_st, h->gmix, (const float*)h->t1,
                         h->gsteps[h->t2_step].op[1]);
       else

@@ -77,7 +77,7 @@ class Context:
 
     def set_option(self, name, value):
         """Implementation switches that leave results unchanged (gb_ctx_set_option):
-        'staged_mix'."""
+        'staged_mix' (0 direct, 1 by density, 2 staged)."""
         L.check(L.lib().gb_ctx_set_option(self.handle, {"staged_mix": 0}[name], int(value)))
 
     def profile_begin(self):
