@@ -61,7 +61,7 @@ def parse():
                          "source site (gb_ctx_trace_begin/end)")
     ap.add_argument("--seed", type=int, default=1234 + 5)
     ap.add_argument("--svd", default="gram", choices=["gesvd", "gesvdp", "gram"])
-    ap.add_argument("--eig", default="syevd", choices=["syevd", "syevj"],
+    ap.add_argument("--eig", default="syevd", choices=["syevd", "syevj", "syevd32"],
                     help="eigensolver of the Gram factorisations")
     ap.add_argument("--lanes", type=int, default=8, help="host-thread lanes of the gauge step")
     ap.add_argument("--symmetry", default="u1", choices=["u1", "none"],

@@ -338,10 +338,11 @@ enum {
 };
 int gb_ctx_set_svd_method(gb_ctx* ctx, int method);
 /* Gauge-step options: the Hermitian eigensolver of the Gram route (GB_EIG_SYEVD: cuSOLVER
- * divide and conquer, the default; GB_EIG_SYEVJ: cuSOLVER cyclic Jacobi at machine-accuracy
- * tolerance, all on the device) and the number of host-thread lanes (1..32, default 8) over
- * which the per-sector factorisations of a U(1) tensor are spread. */
-enum { GB_EIG_SYEVD = 0, GB_EIG_SYEVJ = 1 };
+ * divide and conquer through its 64-bit interface, the default; GB_EIG_SYEVJ: cuSOLVER cyclic
+ * Jacobi at machine-accuracy tolerance; GB_EIG_SYEVD_DEVICE: divide and conquer through the
+ * 32-bit interface, which takes no host workspace) and the number of host-thread lanes
+ * (1..32, default 8) over which the per-sector factorisations of a U(1) tensor are spread. */
+enum { GB_EIG_SYEVD = 0, GB_EIG_SYEVJ = 1, GB_EIG_SYEVD_DEVICE = 2 };
 int gb_ctx_set_gauge(gb_ctx* ctx, int eig_method, int lanes);
 /* Implementation switches that leave every result unchanged (for comparisons):
  *   GB_OPT_STAGED_MIX: the U(1) chain mix of the grouped schedule either stages the inputs

@@ -975,7 +975,9 @@ int gb_ctx_set_option(gb_ctx* ctx, int option, int64_t value) {
 int gb_ctx_set_gauge(gb_ctx* ctx, int eig_method, int lanes) {
   API_BEGIN
   GB_REQUIRE(ctx, "null context");
-  GB_REQUIRE(eig_method == GB_EIG_SYEVD || eig_method == GB_EIG_SYEVJ, "unknown eigensolver");
+  GB_REQUIRE(eig_method == GB_EIG_SYEVD || eig_method == GB_EIG_SYEVJ ||
+                 eig_method == GB_EIG_SYEVD_DEVICE,
+             "unknown eigensolver");
   GB_REQUIRE(lanes >= 1 && lanes <= 32, "lanes must be in 1..32");
   ctx->eig_method = eig_method;
   ctx->lane_max = lanes;

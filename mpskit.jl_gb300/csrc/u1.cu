@@ -316,6 +316,31 @@ void sym_eig(gb_ctx* L, int dt, int64_t g, void* G, double* W, int* info) {
     cusolverDnDestroySyevjInfo(p);
     return;
   }
+  if (L->eig_method == GB_EIG_SYEVD_DEVICE) {
+    // the 32-bit divide-and-conquer interface (no host workspace)
+    GB_REQUIRE(g < (int64_t)1 << 31, "syevd: matrix too large");
+    int lwork = 0;
+    if (cx)
+      CUSOLVER_CHECK_U1(cusolverDnZheevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR,
+                                                    CUBLAS_FILL_MODE_LOWER, (int)g,
+                                                    (cuDoubleComplex*)G, (int)g, W, &lwork));
+    else
+      CUSOLVER_CHECK_U1(cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR,
+                                                    CUBLAS_FILL_MODE_LOWER, (int)g, (double*)G,
+                                                    (int)g, W, &lwork));
+    DevBuf wk(L, (size_t)lwork * elem_size(dt) + 256);
+    if (cx)
+      CUSOLVER_CHECK_U1(cusolverDnZheevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+                                         (int)g, (cuDoubleComplex*)G, (int)g, W,
+                                         wk.as<cuDoubleComplex>(), lwork, info));
+    else
+      CUSOLVER_CHECK_U1(cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+                                         (int)g, (double*)G, (int)g, W, wk.as<double>(), lwork,
+                                         info));
+    count_launch(L);
+    GB_CHECK_CUDA(cudaStreamSynchronize(L->stream));
+    return;
+  }
   const cudaDataType t = cx ? CUDA_C_64F : CUDA_R_64F;
   size_t dws = 0, hws = 0;
   CUSOLVER_CHECK_U1(cusolverDnXsyevd_bufferSize(h, (cusolverDnParams_t)L->solver_params,

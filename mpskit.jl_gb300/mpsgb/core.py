@@ -71,9 +71,11 @@ class Context:
         L.check(L.lib().gb_ctx_set_svd_method(self.handle, code))
 
     def set_gauge(self, eig="syevd", lanes=8):
-        """Gauge-step options (gb_ctx_set_gauge): the Gram route's eigensolver ('syevd' or
-        'syevj') and the number of host-thread lanes for per-sector factorisations."""
-        L.check(L.lib().gb_ctx_set_gauge(self.handle, {"syevd": 0, "syevj": 1}[eig], int(lanes)))
+        """Gauge-step options (gb_ctx_set_gauge): the Gram route's eigensolver ('syevd',
+        'syevj' or 'syevd32') and the number of host-thread lanes for per-sector
+        factorisations."""
+        L.check(L.lib().gb_ctx_set_gauge(self.handle, {"syevd": 0, "syevj": 1, "syevd32": 2}[eig],
+                                         int(lanes)))
 
     def set_option(self, name, value):
         """Implementation switches that leave results unchanged (gb_ctx_set_option):
