@@ -461,6 +461,13 @@ def run_ours(args):
                              "launches": prof["persistent"]["launches"]} if grouped else None,
         "traffic": None,
     }
+    if (grouped and u1 and prec == "bf16x3" and D == 2048 and args.Lx == 24 and args.Ly == 6
+            and args.seed == 1234 + 5):
+        # DRAM bytes (read + write) per grouped launch of this workload's AC2 matvec, from the
+        # ncu capture summarised in profiles/gemm_grouped_D2048_u1_dram.txt (the three
+        # launches of one matvec: 298.5 + 574.8 + 46.5 MB)
+        roofline["traffic"] = 306.6e6
+        roofline["traffic_source"] = "profiles/gemm_grouped_D2048_u1_dram.txt"
 
     # ---------------- end to end through the C ABI with host buffers
     log(f"timed region done: {t_wall:.3f}s wall, {t_dev:.3f}s device; status {ctx.device_status()}")
