@@ -1436,7 +1436,7 @@ int gb_env_transfer_left(gb_ctx* ctx, const gb_tensor* GL, const gb_tensor* W, c
        Dket, 0, 0.0, T1, Dbra, Dbra * d * Dkn, wl);
   // T2[bra, s, kn, w'] = W[w, s, s', w'] T1[bra, s', kn, w]
   const MixDev& m = transfer_plan(ctx, W, 0, Dbra, Dkn, 0, is_cplx(dt));
-  mix_run(ctx, m, dt, T1, T2, 0.0, prec != GB_PREC_FP64);
+  mix_run(ctx, m, dt, T1, T2, 0.0);
   // GL'[bn, (kn w')] = conj(Abar)[(bra s), bn]^T T2[(bra s), (kn w')]
   gemm(ctx, prec, dt, 'C', 'N', Dbn, Dkn * wr, Dbra * d, 1.0, Abar->data, Dbra * d, 0, T2,
        Dbra * d, 0, 0.0, GL_out->data, Dbn, 0);
@@ -1472,7 +1472,7 @@ int gb_env_transfer_right(gb_ctx* ctx, const gb_tensor* GR, const gb_tensor* W, 
        0, 0.0, T1, Dk * d, 0);
   // T2[a, w, s, r] = W[w, s, t, v] T1[a, t, v, r]
   const MixDev& m = transfer_plan(ctx, W, 1, Dk, 0, Dbra, is_cplx(dt));
-  mix_run(ctx, m, dt, T1, T2, 0.0, prec != GB_PREC_FP64);
+  mix_run(ctx, m, dt, T1, T2, 0.0);
   // GR'[(a w), b] = T2[(a w), (s r)] conj(Abar[b, (s r)])^T
   gemm(ctx, prec, dt, 'N', 'C', Dk * wl, Db, d * Dbra, 1.0, T2, Dk * wl, 0, Abar->data, Db, 0, 0.0,
        GR_out->data, Dk * wl, 0);

@@ -210,9 +210,7 @@ struct MixDev {
 };
 MixDev mix_upload(gb_ctx* ctx, const MixPlan& p);
 void mix_free(MixDev& m);
-// fp32_arith: FP32 arithmetic for real data (for a mix feeding a split-precision GEMM)
-void mix_run(gb_ctx* ctx, const MixDev& m, int dtype, const void* x, void* y, double beta,
-             bool fp32_arith = false);
+void mix_run(gb_ctx* ctx, const MixDev& m, int dtype, const void* x, void* y, double beta);
 
 // y[off_J + i*ds] += val_J for i < count (diagonal additions of delta terms)
 void add_diag(gb_ctx* ctx, int dtype, void* y, const std::vector<int64_t>& offs,

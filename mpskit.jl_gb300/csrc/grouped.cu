@@ -458,51 +458,32 @@ __global__ void gmix_kernel(int64_t nJ, int64_t N, int64_t xn, const int64_t* __
                             const double* __restrict__ val, const float* __restrict__ x,
                             const GMixEntry* __restrict__ ent, E* __restrict__ hi, int64_t plane,
                             int64_t kmax) {
-  constexpr bool TF = std::is_same<E, float>::value;
-  constexpr int RE = 4;  // entries of the row held in registers (most rows have one or two)
   const int J = blockIdx.y;
-  const int e0 = row_ptr[J], ne = row_ptr[J + 1] - e0;
+  const int e0 = row_ptr[J], e1 = row_ptr[J + 1];
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  int64_t off[RE];
-  float vh[RE], vl[RE];
-#pragma unroll
-  for (int k = 0; k < RE; ++k) {
-    off[k] = 0;
-    vh[k] = vl[k] = 0.0f;
-    if (k < ne) {
-      off[k] = in_off[col[e0 + k]];
-      vh[k] = (float)val[e0 + k];
-      vl[k] = (float)(val[e0 + k] - (double)vh[k]);
-    }
-  }
   E* lo = hi + plane;
-  // one term of the sum, as in gmix_staged_kernel (identical results)
-  auto term = [&](float& s, float& c, float h, float l, float xv) {
-    if (TF) {
-      const float p = h * xv;
-      const float pe = fmaf(h, xv, -p) + l * xv;
-      const float t = s + p, z = t - s;
-      c += ((s - (t - z)) + (p - z)) + pe;
-      s = t;
-    } else {
-      s = fmaf(h, xv, s);
-    }
-  };
   for (int64_t n = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); n < N;
        n += warps) {
     const GMixEntry en = ent[n * nJ + J];
     if (en.hi <= en.lo || en.row < 0) continue;
     const int64_t base = (int64_t)en.row * kmax + en.kst - en.lo;
-    const float* xn_ = x + n * xn;
     for (int64_t a = en.lo + lane; a < en.hi; a += 32) {
+      // the arithmetic of gmix_staged_kernel, term for term (identical results)
       float s = 0.0f, c = 0.0f;
-#pragma unroll
-      for (int k = 0; k < RE; ++k)
-        if (k < ne) term(s, c, vh[k], vl[k], xn_[a + off[k]]);
-      for (int e = e0 + RE; e < e0 + ne; ++e) {
-        const float h = (float)val[e];
-        term(s, c, h, (float)(val[e] - (double)h), xn_[a + in_off[col[e]]]);
+      for (int e = e0; e < e1; ++e) {
+        const float xv = x[a + in_off[col[e]] + n * xn];
+        const float vh = (float)val[e];
+        if (std::is_same<E, float>::value) {
+          const float vl = (float)(val[e] - (double)vh);
+          const float p = vh * xv;
+          const float pe = fmaf(vh, xv, -p) + vl * xv;
+          const float t = s + p, z = t - s;
+          c += ((s - (t - z)) + (p - z)) + pe;
+          s = t;
+        } else {
+          s = fmaf(vh, xv, s);
+        }
       }
       split_put_f(hi, lo, base + a, s + c);
     }

@@ -135,28 +135,6 @@ __global__ void mix_kernel(int64_t A, int64_t N, int64_t xa, int64_t xn, int64_t
   }
 }
 
-// the same mix with FP32 arithmetic for real data (its result feeds a split-precision GEMM,
-// whose hi/lo planes keep at most 22 bits; GB300's FP64 rate is a small fraction of FP32's)
-__global__ void mix_f32_kernel(int64_t A, int64_t N, int64_t xa, int64_t xn, int64_t ya,
-                               int64_t yn, const int64_t* __restrict__ in_off,
-                               const int64_t* __restrict__ out_off, const int* __restrict__ row_ptr,
-                               const int* __restrict__ col, const double* __restrict__ val,
-                               const double* __restrict__ x, double* __restrict__ y, double beta) {
-  const int J = blockIdx.y;
-  const int e0 = row_ptr[J], e1 = row_ptr[J + 1];
-  const int64_t yo = out_off[J];
-  for (int64_t n = blockIdx.z; n < N; n += gridDim.z) {
-    for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < A;
-         a += (int64_t)gridDim.x * blockDim.x) {
-      float acc = 0.0f;
-      const int64_t xb = a * xa + n * xn;
-      for (int e = e0; e < e1; ++e) acc = fmaf((float)val[e], (float)x[xb + in_off[col[e]]], acc);
-      double* yp = y + a * ya + yo + n * yn;
-      *yp = beta != 0.0 ? (double)acc + beta * *yp : (double)acc;
-    }
-  }
-}
-
 MixDev mix_upload(gb_ctx* ctx, const MixPlan& p) {
   MixDev m;
   m.A = p.A;
@@ -212,17 +190,11 @@ void mix_free(MixDev& m) {
   m.buf = nullptr;
 }
 
-void mix_run(gb_ctx* ctx, const MixDev& m, int dtype, const void* x, void* y, double beta,
-             bool fp32_arith) {
+void mix_run(gb_ctx* ctx, const MixDev& m, int dtype, const void* x, void* y, double beta) {
   if (m.nJ == 0 || m.A == 0 || m.N == 0) return;
   GB_REQUIRE(m.nJ <= 65535, "mix: too many output rows");
   dim3 grid(nblocks(m.A, 128, 64), (unsigned)m.nJ, (unsigned)std::min<int64_t>(m.N, 65535));
-  if (fp32_arith && !is_cplx(dtype)) {
-    GB_REQUIRE(!m.cplx, "mix: real data needs real coefficients");
-    mix_f32_kernel<<<grid, 128, 0, ctx->stream>>>(m.A, m.N, m.xa, m.xn, m.ya, m.yn, m.in_off,
-                                                  m.out_off, m.row_ptr, m.col, m.val,
-                                                  (const double*)x, (double*)y, beta);
-  } else if (is_cplx(dtype)) {
+  if (is_cplx(dtype)) {
     GB_REQUIRE(m.cplx, "mix: complex data needs complex coefficients");
     mix_kernel<dcx><<<grid, 128, 0, ctx->stream>>>(m.A, m.N, m.xa, m.xn, m.ya, m.yn, m.in_off,
                                                    m.out_off, m.row_ptr, m.col, (const dcx*)m.val,
