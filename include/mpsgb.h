@@ -299,6 +299,21 @@ int gb_project_complement(gb_ctx* ctx, gb_tensor* Y, const gb_tensor* X);
 int gb_project_complement_right(gb_ctx* ctx, gb_tensor* Y, const gb_tensor* X);
 /* contract_mpo_expval-style scalar <x|y> after a heff apply is gb_tensor_dot. */
 
+/* ---------------------------------------------------------------- projections */
+/* One application of a generic (non-Jordan) derivative operator between two different
+ * states (C_projection / AC_projection / AC2_projection with below != above,
+ * src/algorithms/derivatives/derivatives.jl:194-216, through MPO_C/AC_Hamiltonian,
+ * mpo_derivatives.jl:37-55, 92-107): GL[bra l, w; ket l'] and GR[ket r', w; bra r] carry
+ * different bra and ket bonds.
+ *   W = NULL : y[l; r]    = GL[l w; l'] x[l'; r'] GR[r' w; r]              (GB_KIND_BOND)
+ *   W        : y[l s; r]  = GL[l w; l'] x[l' s'; r'] W[w s; s' w'] GR[r' w'; r]  (GB_KIND_MPS)
+ * The two-site form is the one-site form with the two physical legs fused: W1 W2 contracted
+ * over their shared channel into one MPO tensor (wl, d1 d2, d1 d2, wr), x and y two-site
+ * tensors relabelled (gb_tensor_reshape) as MPS tensors (Dl, d1 d2, Dr) -- their device orders
+ * agree.  x holds the ket bonds, y (caller-created) the bra bonds. */
+int gb_mpo_project(gb_ctx* ctx, const gb_tensor* GL, const gb_tensor* W, const gb_tensor* GR,
+                   const gb_tensor* x, int precision, gb_tensor* y);
+
 /* ---------------------------------------------------------------- bond expansion */
 /* The DMRG3S perturbation MPO_AC_Hamiltonian(env, W, combiner) * AC
  * (src/algorithms/post_expand/dmrg3s.jl:133-192), the combiner fusing the bond with the MPO

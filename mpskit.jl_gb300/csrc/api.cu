@@ -1479,6 +1479,59 @@ int gb_env_transfer_right(gb_ctx* ctx, const gb_tensor* GR, const gb_tensor* W, 
   API_END
 }
 
+// ---------------------------------------------------------------- projections
+int gb_mpo_project(gb_ctx* ctx, const gb_tensor* GL, const gb_tensor* W, const gb_tensor* GR,
+                   const gb_tensor* x, int precision, gb_tensor* y) {
+  API_BEGIN
+  GB_REQUIRE(ctx && GL && GR && x && y, "null argument");
+  for (const gb_tensor* t : {GL, GR, x, (const gb_tensor*)y}) check_ctx(t, ctx);
+  if (W) check_ctx(W, ctx);
+  GB_REQUIRE(GL->kind == GB_KIND_GL && GR->kind == GB_KIND_GR, "project: environment kinds");
+  const int dt = x->dtype;
+  GB_REQUIRE(GL->dtype == dt && GR->dtype == dt && y->dtype == dt, "project: dtypes");
+  // GL[bra l, w, ket l'] (device (a, a', w)); GR[ket r', w, bra r] (device (b', w, b))
+  const int64_t Dlb = GL->dims[0], wl = GL->dims[1], Dlk = GL->dims[2];
+  const int64_t Drk = GR->dims[0], wr = GR->dims[1], Drb = GR->dims[2];
+  DevGuard g(ctx->device);
+  const size_t es = elem_size(dt);
+  if (!W) {
+    // C_projection: y[l, r] = GL[l w; l'] x[l'; r'] GR[r' w; r]
+    GB_REQUIRE(x->kind == GB_KIND_BOND && y->kind == GB_KIND_BOND, "project: bond tensors");
+    GB_REQUIRE(wl == wr, "project: environment channels differ");
+    GB_REQUIRE(x->dims[0] == Dlk && x->dims[1] == Drk, "project: x shape (ket bonds)");
+    GB_REQUIRE(y->dims[0] == Dlb && y->dims[1] == Drb, "project: y shape (bra bonds)");
+    void* T1 = scratch(ctx, SLOT_T1, (size_t)Dlk * wr * Drb * es);
+    // T1[l', (w r)] = x[l', r'] GR[r', (w r)];  y[l, r] = GL[l, (l' w)] T1[(l' w), r]
+    gemm(ctx, precision, dt, 'N', 'N', Dlk, wr * Drb, Drk, 1.0, x->data, Dlk, 0, GR->data, Drk,
+         0, 0.0, T1, Dlk, 0);
+    gemm(ctx, precision, dt, 'N', 'N', Dlb, Drb, Dlk * wl, 1.0, GL->data, Dlb, 0, T1, Dlk * wl,
+         0, 0.0, y->data, Dlb, 0);
+  } else {
+    // AC_projection: y[l s; r] = GL[l w; l'] x[l' s'; r'] W[w s; s' w'] GR[r' w'; r]
+    GB_REQUIRE(W->kind == GB_KIND_MPO, "project: W must be an MPO tensor");
+    GB_REQUIRE(!(is_cplx(W->dtype) && !is_cplx(dt)), "project: complex MPO on real data");
+    GB_REQUIRE(x->kind == GB_KIND_MPS && y->kind == GB_KIND_MPS, "project: MPS tensors");
+    const int64_t d = W->dims[1];
+    GB_REQUIRE(W->dims[0] == wl && W->dims[3] == wr && W->dims[2] == d, "project: MPO shape");
+    GB_REQUIRE(x->dims[0] == Dlk && x->dims[1] == d && x->dims[2] == Drk,
+               "project: x shape (ket bonds)");
+    GB_REQUIRE(y->dims[0] == Dlb && y->dims[1] == d && y->dims[2] == Drb,
+               "project: y shape (bra bonds)");
+    void* T1 = scratch(ctx, SLOT_T1, (size_t)Dlk * d * wr * Drb * es);
+    void* T2 = scratch(ctx, SLOT_T2, (size_t)Dlk * wl * d * Drb * es);
+    // T1[(l' s'), (w' r)] = x[(l' s'), r'] GR[r', (w' r)]  (the first step of transfer_right)
+    gemm(ctx, precision, dt, 'N', 'N', Dlk * d, wr * Drb, Drk, 1.0, x->data, Dlk * d, 0,
+         GR->data, Drk, 0, 0.0, T1, Dlk * d, 0);
+    // T2[l', w, s, r] = W[w, s, s', w'] T1[l', s', w', r]
+    const MixDev& m = transfer_plan(ctx, W, 1, Dlk, 0, Drb, is_cplx(dt));
+    mix_run(ctx, m, dt, T1, T2, 0.0);
+    // y[l, (s r)] = GL[l, (l' w)] T2[(l' w), (s r)]
+    gemm(ctx, precision, dt, 'N', 'N', Dlb, d * Drb, Dlk * wl, 1.0, GL->data, Dlb, 0, T2,
+         Dlk * wl, 0, 0.0, y->data, Dlb, 0);
+  }
+  API_END
+}
+
 // ---------------------------------------------------------------- bond expansion
 int gb_mps_perturb(gb_ctx* ctx, int side, const gb_tensor* env, const gb_tensor* W,
                    const gb_tensor* AC, int precision, gb_tensor* out) {

@@ -8,7 +8,8 @@ from . import _lib
 from .core import Context, DeviceTensor, context
 from .derivatives import (AC2_hamiltonian, AC_hamiltonian, C_hamiltonian, DerivativeOperator,
                           GB300Backend, Lanczos, MPO_AC2_Hamiltonian, MPO_AC_Hamiltonian,
-                          exponentiate, fixedpoint, integrate)
+                          exponentiate, fixedpoint, integrate, mpo_projection,
+                          transfer_left, transfer_right)
 from .operators import (FiniteMPOHamiltonian, InfiniteMPOHamiltonian, MPOHamiltonian,
                         heisenberg_XXX, j1j2_cylinder, transverse_field_ising, xxz)
 from .states import (FiniteEnvironments, FiniteMPS, ac2_from, left_orth, mul_front, mul_tail,
@@ -25,7 +26,8 @@ from . import cell
 __all__ = [
     "Context", "DeviceTensor", "context", "AC2_hamiltonian", "AC_hamiltonian", "C_hamiltonian",
     "DerivativeOperator", "GB300Backend", "Lanczos", "exponentiate", "fixedpoint", "integrate",
-    "MPO_AC_Hamiltonian", "MPO_AC2_Hamiltonian",
+    "MPO_AC_Hamiltonian", "MPO_AC2_Hamiltonian", "mpo_projection", "transfer_left",
+    "transfer_right",
     "FiniteMPOHamiltonian", "InfiniteMPOHamiltonian", "MPOHamiltonian", "heisenberg_XXX",
     "j1j2_cylinder", "transverse_field_ising", "xxz", "FiniteEnvironments", "FiniteMPS",
     "ac2_from", "left_orth", "mul_front", "mul_tail", "project_complement_", "right_orth",

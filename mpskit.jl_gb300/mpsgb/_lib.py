@@ -127,6 +127,7 @@ _SIGS = {
     "gb_packed_info": ([P, PI64, PI64, ctypes.POINTER(ctypes.c_size_t)], INT),
     "gb_packed_free": ([P], INT),
     "gb_mps_perturb": ([P, INT, P, P, P, INT, P], INT),
+    "gb_mpo_project": ([P, P, P, P, P, INT, P], INT),
     "gb_mps_cat": ([P, P, P, INT, P], INT),
     "gb_tensor_reshape": ([P, INT, INT, PI64], INT),
     "gb_svd_trunc": ([P, P, I64, D, INT, ctypes.POINTER(P), ctypes.POINTER(P), ctypes.POINTER(P), PD], INT),

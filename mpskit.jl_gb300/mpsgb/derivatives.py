@@ -5,6 +5,10 @@
          src/algorithms/derivatives/mpo_derivatives.jl:37-45
   MPO_AC_Hamiltonian / MPO_AC2_Hamiltonian (an arbitrary MPO, no Jordan structure)
       -- src/algorithms/derivatives/mpo_derivatives.jl:46-66
+  mpo_projection (C/AC/AC2_projection between different bra and ket states)
+      -- src/algorithms/derivatives/derivatives.jl:194-216
+  transfer_left / transfer_right (one environment step, bra and ket given separately)
+      -- src/algorithms/toolbox/transfer.jl:125-130 (also src/environments/finite_envs.jl)
   fixedpoint(H, x0, :SR, Lanczos)       -- src/algorithms/fixedpoint.jl:15-18
   integrate(H, y0, t, dt, Lanczos)      -- src/algorithms/timestep/integrators.jl:44-53
 
@@ -159,6 +163,77 @@ def MPO_AC2_Hamiltonian(GL, W1, W2, GR, backend=None):
     144-153)."""
     return DerivativeOperator(GL.ctx, L.GB_HEFF_AC2_MPO, GL, W1, W2, GR,
                               backend or GB300Backend())
+
+
+def _fuse_two_site(W1, W2):
+    """W1 W2 over their shared channel as one MPO tensor (wl, d1 d2, d1 d2, wr), physical
+    index s1 + d1 s2 (the device order of a two-site tensor's physical legs)."""
+    wl, d1, _, _ = W1.shape
+    _, d2, _, wr = W2.shape
+    W = np.einsum("asum,mtvb->astuvb", W1, W2)  # (wl, s1, s2, t1, t2, wr)
+    return np.asfortranarray(W.reshape(wl, d1 * d2, d1 * d2, wr, order="F"))
+
+
+def mpo_projection(GL, GR, x, W1=None, W2=None, backend=None):
+    """One application of a generic derivative operator between different bra and ket states
+    (C_projection / AC_projection / AC2_projection with below != above,
+    derivatives.jl:194-216, through MPO_C/AC/AC2_Hamiltonian, mpo_derivatives.jl:37-66):
+    GL[bra l w; ket l'], GR[ket r' w; bra r]; W1 (and W2) as host arrays (wl, d, d, wr) or
+    None for the bond operator.  Returns y on the bra bonds (gb_mpo_project)."""
+    backend = backend or GB300Backend()
+    ctx = x.ctx
+    Dlb, Drb = GL.dims[0], GR.dims[2]
+    if W1 is None:
+        y = DeviceTensor(ctx, L.GB_KIND_BOND, x.dtype, (Dlb, Drb))
+        L.check(L.lib().gb_mpo_project(ctx.handle, GL.handle, None, GR.handle, x.handle,
+                                       backend.code, y.handle))
+        return y
+    if W2 is None:
+        W = DeviceTensor.from_numpy(ctx, L.GB_KIND_MPO, np.asarray(W1))
+        y = DeviceTensor(ctx, L.GB_KIND_MPS, x.dtype, (Dlb, W1.shape[1], Drb))
+        L.check(L.lib().gb_mpo_project(ctx.handle, GL.handle, W.handle, GR.handle, x.handle,
+                                       backend.code, y.handle))
+        return y
+    d1, d2 = W1.shape[1], W2.shape[1]
+    W = DeviceTensor.from_numpy(ctx, L.GB_KIND_MPO, _fuse_two_site(np.asarray(W1), np.asarray(W2)))
+    xf = x.copy().reshape_(L.GB_KIND_MPS, (x.dims[0], d1 * d2, x.dims[2]))
+    y = DeviceTensor(ctx, L.GB_KIND_MPS, x.dtype, (Dlb, d1 * d2, Drb))
+    L.check(L.lib().gb_mpo_project(ctx.handle, GL.handle, W.handle, GR.handle, xf.handle,
+                                   backend.code, y.handle))
+    return y.reshape_(L.GB_KIND_AC2, (Dlb, d1, Drb, d2))
+
+
+def _mpo_tensor(ctx, W):
+    return W if isinstance(W, DeviceTensor) else DeviceTensor.from_numpy(ctx, L.GB_KIND_MPO,
+                                                                          np.asarray(W))
+
+
+def transfer_left(GL, W, A, Abar=None, backend=None):
+    """transfer_left(GL, O, A, Abar) (transfer.jl:125-127): GL'[a w'; a'] =
+    GL[b w; b'] A[b' s'; a'] W[w s; s' w'] conj(Abar[b s; a]); Abar defaults to A.  W is a
+    device MPO tensor or a host array (wl, d, d, wr).  Runs gb_env_transfer_left."""
+    backend = backend or GB300Backend()
+    ctx = A.ctx
+    Abar = A if Abar is None else Abar
+    Wd = _mpo_tensor(ctx, W)
+    out = DeviceTensor(ctx, L.GB_KIND_GL, GL.dtype, (Abar.dims[2], Wd.dims[3], A.dims[2]))
+    L.check(L.lib().gb_env_transfer_left(ctx.handle, GL.handle, Wd.handle, A.handle, Abar.handle,
+                                         backend.code, out.handle))
+    return out
+
+
+def transfer_right(GR, W, A, Abar=None, backend=None):
+    """transfer_right(GR, O, A, Abar) (transfer.jl:128-130): GR'[a' w; a] =
+    A[a' s'; b'] W[w s; s' w'] GR[b' w'; b] conj(Abar[a s; b]); Abar defaults to A.
+    Runs gb_env_transfer_right."""
+    backend = backend or GB300Backend()
+    ctx = A.ctx
+    Abar = A if Abar is None else Abar
+    Wd = _mpo_tensor(ctx, W)
+    out = DeviceTensor(ctx, L.GB_KIND_GR, GR.dtype, (A.dims[0], Wd.dims[0], Abar.dims[0]))
+    L.check(L.lib().gb_env_transfer_right(ctx.handle, GR.handle, Wd.handle, A.handle, Abar.handle,
+                                          backend.code, out.handle))
+    return out
 
 
 def C_hamiltonian(site, psi, H, envs, backend=None):
