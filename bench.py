@@ -589,7 +589,7 @@ def cpu_baseline_sample(psi, H, envs, pos, matvecs):
                       f"{threads} threads; the block SVD and the environment step left out"}
 
 
-def accuracy_compare(ctx, psi, H, envs, backend, pos, fp64_maxiter=4):
+def accuracy_compare(ctx, psi, H, envs, backend, pos, fp64_maxiter=8):
     """The precision condition of the metric at the bench bond: from the same state,
     environments and start vector, the split-precision Lanczos solve followed by its FP64
     refinement step (one FP64 matvec: Rayleigh quotient and residual of the split solution

@@ -161,11 +161,13 @@ int heff_eigsolve_raw(gb_ctx* ctx, gb_heff* h, int64_t n_dense, int dtype, void*
   std::vector<double> D, U;
   std::vector<double> f;
   // With split-precision contractions the residual cannot fall below the operator's own
-  // accuracy (~1e-6 relative); a restart that no longer reduces it by 10% ends the solve
-  // (reported as not converged, as when maxiter runs out) instead of spending the remaining
-  // restarts on rounding noise.  FP64 operators keep KrylovKit's plain maxiter rule.
+  // accuracy (~1e-6 relative); two restarts in a row that do not bring it 10% below the
+  // best value so far end the solve (reported as not converged, as when maxiter runs out)
+  // instead of spending the remaining restarts on rounding noise.  A single slow restart of
+  // a hard problem does not.  FP64 operators keep KrylovKit's plain maxiter rule.
   const bool split = heff_precision(h) != GB_PREC_FP64;
-  double last_res = INFINITY;
+  double best_res = INFINITY;
+  int stalls = 0;
   while (true) {
     sp.apply(vec(K), w);
     ++numops;
@@ -198,8 +200,12 @@ int heff_eigsolve_raw(gb_ctx* ctx, gb_heff* h, int64_t n_dense, int dtype, void*
     if (numiter == maxiter) break;
     if (split) {
       const double res = std::fabs(f[0]);
-      if (res > 0.9 * last_res) break;
-      last_res = res;
+      if (res > 0.9 * best_res) {
+        if (++stalls >= 2) break;
+      } else {
+        stalls = 0;
+      }
+      best_res = std::min(best_res, res);
     }
     // thick restart: V[:keep] <- V[:K] U[:, :keep]
     int keep = (3 * kd + 2 * howmany) / 5;

@@ -18,6 +18,8 @@ from .algorithms import (DMRG, DMRG2, DMRG3S, TDVP, AdaptiveKrylov, OptimalExpan
                          expectation_value, find_groundstate, timestep)
 from .infinite import (IDMRG, VUMPS, InfiniteEnvironments, InfiniteMPS,
                        find_groundstate_idmrg, find_groundstate_vumps, timestep_infinite)
+from .grassmann import GradientGrassmann
+from . import optim
 from . import u1
 from . import batched
 from . import io
@@ -32,7 +34,7 @@ __all__ = [
     "j1j2_cylinder", "transverse_field_ising", "xxz", "FiniteEnvironments", "FiniteMPS",
     "ac2_from", "left_orth", "mul_front", "mul_tail", "project_complement_", "right_orth",
     "svd_trunc", "DMRG", "DMRG2", "DMRG3S", "OptimalExpand", "AdaptiveKrylov",
-    "expectation_value", "find_groundstate",
+    "expectation_value", "find_groundstate", "GradientGrassmann", "optim",
     "TDVP", "timestep", "VUMPS", "IDMRG", "InfiniteEnvironments", "InfiniteMPS",
     "find_groundstate_vumps", "find_groundstate_idmrg", "timestep_infinite", "u1", "batched", "io",
     "cell",

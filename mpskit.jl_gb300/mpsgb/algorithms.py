@@ -251,8 +251,13 @@ def expectation_value(psi, H, envs, site=0, backend=None):
 
 
 def find_groundstate(psi, H, alg, envs=None, maxsweeps=None, callback=None):
-    """find_groundstate(psi, H, DMRG2()/DMRG()) on the device.  The input state is
-    modified in place (find_groundstate! semantics).  Returns (psi, envs, eps, history)."""
+    """find_groundstate(psi, H, DMRG2()/DMRG()/GradientGrassmann()) on the device.  DMRG
+    modifies the input state in place (find_groundstate! semantics); GradientGrassmann
+    returns a new state (gradient_grassmann.jl:80-121).  Returns (psi, envs, eps, history):
+    eps is the truncation error of DMRG, the final gradient norm of GradientGrassmann."""
+    from .grassmann import GradientGrassmann, find_groundstate_grassmann
+    if isinstance(alg, GradientGrassmann):
+        return find_groundstate_grassmann(psi, H, alg, envs)
     if isinstance(alg, DMRG2):
         return _sweep_dmrg2(psi, H, alg, envs, maxsweeps, callback)
     if isinstance(alg, DMRG):

@@ -69,6 +69,7 @@ class Context:
         """'gesvd' (default), 'gesvdp' or 'gram' for gb_svd_trunc."""
         code = {"gesvd": 0, "gesvdp": 1, "gram": 2}[method]
         L.check(L.lib().gb_ctx_set_svd_method(self.handle, code))
+        self._svd_method = method
 
     def set_gauge(self, eig="syevd", lanes=8):
         """Gauge-step options (gb_ctx_set_gauge): the Gram route's eigensolver ('syevd',

@@ -1,0 +1,102 @@
+"""GradientGrassmann on the device (src/algorithms/grassmann.jl, gradient_grassmann.jl)
+against the oracle: fg, precondition, retract and transport at the same point and direction,
+then whole optimisations reaching exact diagonalisation, as the reference's groundstate test
+(test/algorithms/groundstate.jl:177-192: TFIM g = 4, L = 10, D = 6)."""
+import numpy as np
+import pytest
+
+import mpsgb
+from mpsgb import grassmann as G
+from oracle import grassmann as OG
+from oracle import models as M
+from oracle import mps as P
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    return mpsgb.context(0)
+
+
+def _point(L_, D, seed):
+    psi = P.finite_mps_from_tensors(P.random_initial_tensors(L_, 2, D, seed))
+    AL, X = [], psi.C[0]
+    for i in range(L_):
+        A = np.einsum("ab,bsc->asc", X, psi.AR[i])
+        Q, X = P.qr_pos(A.reshape(-1, A.shape[2], order="F"))
+        AL.append(Q.reshape(A.shape[0], 2, Q.shape[1], order="F"))
+    return AL, X / np.linalg.norm(X)
+
+
+def _dev_point(ctx, AL, C):
+    T = lambda k, a: mpsgb.DeviceTensor.from_numpy(ctx, k, a)
+    return G.GrassmannPoint([T("mps", a) for a in AL], T("bond", C))
+
+
+def _dev_tangent(x, Z):
+    return [G.GrassmannTangent(x.AL[i], mpsgb.DeviceTensor.from_numpy(x.psi.ctx, "mps", z))
+            for i, z in enumerate(Z)]
+
+
+def _nontrivial(AL):
+    # sites whose tangent space is not empty (Dl d > Dr)
+    return [i for i, a in enumerate(AL) if a.shape[0] * a.shape[1] > a.shape[2]]
+
+
+def test_grassmann_steps_match_the_oracle(ctx):
+    L_, D = 8, 6
+    H = M.finite_mpo_hamiltonian(L_, 2, M.tfim_terms(L_, g=1.0))
+    Hd = mpsgb.transverse_field_ising(L_, g=1.0)
+    AL, C = _point(L_, D, 71)
+    x = _dev_point(ctx, AL, C)
+    envs = mpsgb.FiniteEnvironments(x.psi, Hd, ctx)
+    # fg
+    f_o, g_o = OG.fg(AL, C, H)
+    f_d, g_d = G.fg(x, Hd, envs)
+    assert abs(f_d - f_o) <= 1e-12 * abs(f_o)
+    gmax = max(np.linalg.norm(z) for z in g_o)
+    for i in range(L_):
+        assert np.linalg.norm(g_d[i].Z.numpy() - g_o[i]) <= 1e-12 * gmax, i
+    assert abs(G.inner(x, g_d, g_d) - OG.inner(g_o, g_o)) <= 1e-12 * OG.inner(g_o, g_o)
+    # precondition (the sites with an empty tangent space carry amplified rounding noise)
+    Pg_o = OG.precondition(AL, C, g_o)
+    Pg_d = G.precondition(x, _dev_tangent(x, g_o))
+    nt = _nontrivial(AL)
+    pmax = max(np.linalg.norm(Pg_o[i]) for i in nt)
+    for i in nt:
+        assert np.linalg.norm(Pg_d[i].Z.numpy() - Pg_o[i]) <= 1e-11 * pmax, i
+    # retract and transport along the same direction
+    d = [-z if i in nt else np.zeros_like(z) for i, z in enumerate(Pg_o)]
+    a = 0.37
+    ALn_o, Cn_o, xi_o = OG.retract(AL, C, d, a)
+    xn, xi_d = G.retract(x, _dev_tangent(x, d), a)
+    for i in range(L_):
+        assert np.abs(xn.AL[i].numpy() - ALn_o[i]).max() <= 1e-12, i
+        assert np.abs(xi_d[i].Z.numpy() - xi_o[i]).max() <= 1e-12 * max(1.0, pmax), i
+    h_o = OG.transport(g_o, AL, d, a, ALn_o)
+    h_d = G.transport(_dev_tangent(x, g_o), x, _dev_tangent(x, d), a, xn)
+    for i in range(L_):
+        assert np.abs(h_d[i].Z.numpy() - h_o[i]).max() <= 1e-12 * gmax, i
+    # transport is an isometry of the tangent spaces
+    n0, n1 = OG.inner(g_o, g_o), G.inner(xn, h_d, h_d)
+    assert abs(n1 - n0) <= 1e-10 * n0
+
+
+@pytest.mark.parametrize("gx,bar", [(4.0, 1e-9), (1.0, 2e-9)])
+def test_gradient_grassmann_reaches_ed(ctx, gx, bar):
+    L_, D = 10, 6
+    terms = M.tfim_terms(L_, g=gx)
+    e_ed = M.ed_ground_energy(L_, 2, terms)[0]
+    psi = mpsgb.FiniteMPS.from_tensors(P.random_initial_tensors(L_, 2, D, 5), ctx)
+    alg = mpsgb.GradientGrassmann(tol=1e-8, maxiter=300)
+    out, envs, normgrad, hist = mpsgb.find_groundstate(psi, mpsgb.transverse_field_ising(L_, g=gx),
+                                                       alg)
+    assert normgrad <= 1e-8, hist["normgrad"][-5:]
+    e = mpsgb.expectation_value(out, mpsgb.transverse_field_ising(L_, g=gx), envs)
+    assert abs(e - hist["energy"]) <= 1e-10 * abs(e)
+    assert -1e-12 * abs(e_ed) <= e - e_ed < bar * abs(e_ed), (e, e_ed)
+    for A in out.AR:
+        a = A.numpy()
+        Q = a.reshape(a.shape[0], -1, order="F")
+        assert np.abs(Q @ Q.conj().T - np.eye(Q.shape[0])).max() < 1e-12

@@ -1,0 +1,99 @@
+"""The host side of GradientGrassmann (mpsgb.optim: conjugate gradients with the Hager-Zhang
+line search) driven by numpy points: a Rayleigh quotient on a Grassmann manifold, and the
+finite-MPS energy through the oracle's fg / retract / transport (grassmann.jl:61-169),
+converging to exact diagonalisation (gradient_grassmann.jl:80-121)."""
+import numpy as np
+import pytest
+
+from mpsgb import optim
+from oracle import grassmann as OG
+from oracle import models as M
+from oracle import mps as P
+
+
+def _np_ops():
+    add = lambda v, w, a, b: [a * x + b * y for x, y in zip(v, w)]
+    scale = lambda v, a: [a * x for x in v]
+    return add, scale
+
+
+def test_cg_minimises_a_rayleigh_quotient():
+    rng = np.random.default_rng(3)
+    n, p = 30, 3
+    A = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    A = A + A.conj().T
+    W0, _ = np.linalg.qr(rng.standard_normal((n, p)) + 1j * rng.standard_normal((n, p)))
+    sh = (n, 1, p)
+
+    def fg(W):
+        Wm = W[0].reshape(n, p, order="F")
+        AW = A @ Wm
+        G = AW - Wm @ (Wm.conj().T @ AW)
+        return float(np.real(np.trace(Wm.conj().T @ AW))), [G.reshape(sh, order="F")]
+
+    def retract(W, d, a):
+        Wn, Zn = OG.retract_site(W[0], d[0], a)
+        return [Wn], [Zn]
+
+    def transport(v, W, d, a, Wn):
+        return [OG.transport_site(v[0], W[0], d[0], a, Wn[0])]
+
+    add, scale = _np_ops()
+    alg = optim.ConjugateGradient(gradtol=1e-10, maxiter=500)
+    W, f, g, nfg, hist = optim.optimize(fg, [W0.reshape(sh, order="F")], alg, retract,
+                                        transport, lambda x, a, b: OG.inner(a, b), add, scale)
+    assert hist[-1] <= 1e-10
+    assert abs(f - np.sum(np.linalg.eigvalsh(A)[:p])) < 1e-10 * np.abs(A).max() * n
+    Wm = W[0].reshape(n, p, order="F")
+    assert np.abs(Wm.conj().T @ Wm - np.eye(p)).max() < 1e-12
+
+
+def test_line_search_accepts_wolfe_points_only():
+    # phi(c) = (c - 2)^2 along a straight line: the accepted step satisfies the Wolfe
+    # conditions (sufficient decrease and the curvature condition)
+    ls = optim.HagerZhangLineSearch()
+    fg = lambda x: (float((x[0] - 2.0) ** 2), [np.array(2.0 * (x[0] - 2.0))])
+    retract = lambda x, d, a: ([x[0] + a * d[0]], d)
+    inner = lambda x, a, b: float(a[0] * b[0])
+    x, f, g, xi, c, n = ls(fg, [np.array(0.0)], [np.array(1.0)], 4.0, [np.array(-4.0)], 0.1,
+                           retract, inner)
+    assert 0 < c and f - 4.0 <= 0.1 * c * -4.0 and g[0] * 1.0 >= 0.9 * -4.0 and n <= 10
+    # from a step far beyond the minimiser the bracket and secant steps come back to it
+    x, f, g, xi, c, n = ls(fg, [np.array(0.0)], [np.array(1.0)], 4.0, [np.array(-4.0)], 50.0,
+                           retract, inner)
+    assert f - 4.0 <= 0.1 * c * -4.0 and abs(g[0]) <= 0.9 * 4.0 and n <= 10
+
+
+@pytest.mark.parametrize("L_,D,gx,bar", [(6, 4, 4.0, 1e-9), (10, 6, 1.0, 2e-9)])
+def test_gradient_grassmann_reaches_ed_on_the_oracle(L_, D, gx, bar):
+    # TFIM in its paramagnetic phase and at the critical point (where the bond matrices have
+    # small singular values and the preconditioner amplifies rounding noise)
+    terms = M.tfim_terms(L_, g=gx)
+    H = M.finite_mpo_hamiltonian(L_, 2, terms)
+    e_ed = M.ed_ground_energy(L_, 2, terms)[0]
+    psi = P.finite_mps_from_tensors(P.random_initial_tensors(L_, 2, D, 17))
+    # the point: the left-canonical form and the normalised last-bond factor
+    AL, X = [], psi.C[0]
+    for i in range(L_):
+        A = np.einsum("ab,bsc->asc", X, psi.AR[i])
+        Q, X = P.qr_pos(A.reshape(-1, A.shape[2], order="F"))
+        AL.append(Q.reshape(A.shape[0], 2, Q.shape[1], order="F"))
+    x0 = (AL, X / np.linalg.norm(X))
+    add, scale = _np_ops()
+    fg = lambda x: OG.fg(x[0], x[1], H)
+
+    def retract(x, g, a):
+        ALn, Cn, gn = OG.retract(x[0], x[1], g, a)
+        return (ALn, Cn), gn
+
+    transport = lambda h, x, g, a, xn: OG.transport(h, x[0], g, a, xn[0])
+    precondition = lambda x, g: OG.precondition(x[0], x[1], g)
+    alg = optim.ConjugateGradient(gradtol=1e-8, maxiter=300)
+    x, f, g, nfg, hist = optim.optimize(fg, x0, alg, retract, transport,
+                                        lambda x, a, b: OG.inner(a, b), add, scale,
+                                        precondition)
+    assert hist[-1] <= 1e-8, hist[-5:]
+    assert -1e-12 * abs(e_ed) <= f - e_ed < bar * abs(e_ed), (f, e_ed)
+    for A in x[0]:
+        Q = A.reshape(-1, A.shape[2], order="F")
+        assert np.abs(Q.conj().T @ Q - np.eye(Q.shape[1])).max() < 1e-13
