@@ -15,7 +15,7 @@ from .operators import (FiniteMPOHamiltonian, InfiniteMPOHamiltonian, MPOHamilto
 from .states import (FiniteEnvironments, FiniteMPS, ac2_from, left_orth, mul_front, mul_tail,
                      project_complement_, right_orth, svd_trunc)
 from .algorithms import (DMRG, DMRG2, DMRG3S, TDVP, AdaptiveKrylov, OptimalExpand,
-                         expectation_value, find_groundstate, timestep)
+                         SketchedExpand, expectation_value, find_groundstate, timestep)
 from .infinite import (IDMRG, VUMPS, InfiniteEnvironments, InfiniteMPS,
                        find_groundstate_idmrg, find_groundstate_vumps, timestep_infinite)
 from .grassmann import GradientGrassmann
@@ -33,7 +33,7 @@ __all__ = [
     "FiniteMPOHamiltonian", "InfiniteMPOHamiltonian", "MPOHamiltonian", "heisenberg_XXX",
     "j1j2_cylinder", "transverse_field_ising", "xxz", "FiniteEnvironments", "FiniteMPS",
     "ac2_from", "left_orth", "mul_front", "mul_tail", "project_complement_", "right_orth",
-    "svd_trunc", "DMRG", "DMRG2", "DMRG3S", "OptimalExpand", "AdaptiveKrylov",
+    "svd_trunc", "DMRG", "DMRG2", "DMRG3S", "OptimalExpand", "SketchedExpand", "AdaptiveKrylov",
     "expectation_value", "find_groundstate", "GradientGrassmann", "optim",
     "TDVP", "timestep", "VUMPS", "IDMRG", "InfiniteEnvironments", "InfiniteMPS",
     "find_groundstate_vumps", "find_groundstate_idmrg", "timestep_infinite", "u1", "batched", "io",

@@ -13,8 +13,10 @@ import time
 import numpy as np
 
 from . import _lib as L
+from .core import DeviceTensor
 from .derivatives import (AC2_hamiltonian, AC_hamiltonian, C_hamiltonian, GB300Backend, Lanczos,
-                          exponentiate, fixedpoint)
+                          exponentiate, fixedpoint, mpo_projection, transfer_left,
+                          transfer_right)
 from .states import (FiniteEnvironments, ac2_from, left_orth, mps_cat, mul_front, mul_tail,
                      perturb, project_complement_, project_complement_right_, right_orth,
                      svd_trunc)
@@ -149,6 +151,101 @@ def optimal_expand(pos, right, psi, H, envs, alg, backend=None):
         nc, nar = right_orth(mps_cat(rt, None, 0, nb=k))  # [AC ; 0] regauged
         nc.scale_(1.0 / nc.norm())
         psi.AL[pos - 1], psi.C[pos], psi.AR[pos] = nal, nc, nar
+        psi.center = pos
+
+
+class SketchedExpand:
+    """SketchedExpand(; trunc = truncrank(add), oversampling) (sketchedexpand.jl:41-73):
+    `add` directions per bond from a random sketch of `add + oversampling` columns.  The
+    random isometries are drawn on the host from numpy's PCG64 seeded with `seed`, one
+    Gaussian matrix per expansion in call order, and orthonormalised on the device."""
+
+    def __init__(self, add, oversampling=0, seed=0):
+        self.add, self.oversampling = add, oversampling
+        self.rng = np.random.default_rng(seed)
+
+    def gaussian(self, m, n, dtype):
+        g = self.rng.standard_normal((m, n))
+        if np.dtype(dtype).kind == "c":
+            g = g + 1j * self.rng.standard_normal((m, n))
+        return g.astype(dtype)
+
+    def sketch(self, comp, other):
+        """(l, k): sketch columns and target directions in the sketched complement `comp`,
+        both capped by the other site's complement (beyond it the new directions could not
+        stay orthogonal to the state)."""
+        cap = min(comp, other)
+        k = min(self.add, cap)
+        return min(k + self.oversampling, cap), k
+
+
+def sketched_expand(pos, right, psi, H, envs, alg, backend=None):
+    """changebond!(site, dir, psi, H, ::SketchedExpand, envs) (sketchedexpand.jl:75-162):
+    a random sketch Q of one site's complement folded into that site's environment (a
+    transfer with bra Q), one MPO_AC projection of the neighbouring site (gb_mpo_project),
+    projected onto the neighbour's complement and orthonormalised (LQ / QR, or a truncated
+    SVD when oversampled), then appended to the bond with zero weight: the state is
+    unchanged.  At single-site cost: no two-site tensor is formed."""
+    _dense_only(psi, "SketchedExpand")
+    backend = backend or GB300Backend()
+    ctx = envs.ctx
+    W = H.device(ctx, envs.dtype)
+    if right:
+        left, rt = psi.ac(pos), psi.AR[pos + 1]
+        Dl, d, D = left.dims
+        d2, Dn = rt.dims[1], rt.dims[2]
+        compL, compR = Dl * d - D, d2 * Dn - D
+        if compL <= 0 or compR <= 0:
+            return
+        l, k = alg.sketch(compL, compR)
+        AL = psi.al(pos)
+        G = DeviceTensor.from_numpy(ctx, L.GB_KIND_MPS,
+                                    alg.gaussian(Dl * d, l, left.dtype).reshape(Dl, d, l, order="F"))
+        Om, _ = left_orth(G)                                   # randisometry
+        Q, _ = left_orth(project_complement_(Om, AL))          # qr_compact of the complement part
+        GLq = transfer_left(envs.leftenv(pos, psi), W[pos], left, Q, backend)
+        Y = mpo_projection(GLq, envs.rightenv(pos + 1, psi), rt, W[pos + 1], backend=backend)
+        project_complement_right_(Y, rt)
+        if l == k:
+            _, ar = right_orth(Y)
+        else:
+            Y.reshape_(L.GB_KIND_AC2, (l, 1, Dn, d2))
+            _, _, ar, _ = svd_trunc(Y, k, 0.0, normalize=False)
+        kk = ar.dims[0]
+        nar = mps_cat(rt, ar, 0)
+        nal, nc = left_orth(mps_cat(left, None, 2, nb=kk))
+        nc.scale_(1.0 / nc.norm())
+        psi.AL[pos], psi.C[pos + 1], psi.AR[pos + 1] = nal, nc, nar
+        psi.center = pos + 1
+    else:
+        lf, rgt = psi.AL[pos - 1], psi.ac(pos)
+        Dp, d, Dl = lf.dims
+        d2, Dr = rgt.dims[1], rgt.dims[2]
+        compL, compR = Dp * d - Dl, d2 * Dr - Dl
+        if compL <= 0 or compR <= 0:
+            return
+        l, k = alg.sketch(compR, compL)
+        _, ARtt = right_orth(rgt)
+        G = DeviceTensor.from_numpy(ctx, L.GB_KIND_MPS,
+                                    alg.gaussian(d2 * Dr, l, rgt.dtype).reshape(1, d2 * Dr, l,
+                                                                                order="F"))
+        Om, _ = left_orth(G)                                   # randisometry (d2 Dr) x l
+        from .infinite import adjoint
+        Om = adjoint(Om.reshape_(L.GB_KIND_BOND, (d2 * Dr, l)))
+        Om.reshape_(L.GB_KIND_MPS, (l, d2, Dr))                # its adjoint, l x (s r)
+        _, Qr = right_orth(project_complement_right_(Om, ARtt))
+        GRq = transfer_right(envs.rightenv(pos, psi), W[pos], rgt, Qr, backend)
+        Y = mpo_projection(envs.leftenv(pos - 1, psi), GRq, lf, W[pos - 1], backend=backend)
+        project_complement_(Y, lf)
+        if l == k:
+            Qn, _ = left_orth(Y)
+        else:
+            Y.reshape_(L.GB_KIND_AC2, (Dp, d, l, 1))
+            Qn, _, _, _ = svd_trunc(Y, k, 0.0, normalize=False)
+        kk = Qn.dims[2]
+        nc, nar = right_orth(mps_cat(rgt, None, 0, nb=kk))
+        nc.scale_(1.0 / nc.norm())
+        psi.AL[pos - 1], psi.C[pos], psi.AR[pos] = mps_cat(lf, Qn, 2), nc, nar
         psi.center = pos
 
 
@@ -308,7 +405,8 @@ def dmrg1_local_update(pos, right, psi, H, alg, envs, eps_global, decay_rate, it
     project_complement_(y, psi.al(pos))
     eps_local = y.norm()
     if alg.alg_expand is not None:
-        optimal_expand(pos, right, psi, H, envs, alg.alg_expand, alg.backend)
+        expand = sketched_expand if isinstance(alg.alg_expand, SketchedExpand) else optimal_expand
+        expand(pos, right, psi, H, envs, alg.alg_expand, alg.backend)
         ac = psi.ac(pos)
         Heff = AC_hamiltonian(pos, psi, H, envs, alg.backend)
     solver = alg.alg_eigsolve.adapt(decay_rate, eps_local, eps_global, 0.0)

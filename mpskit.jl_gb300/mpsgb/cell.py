@@ -428,8 +428,19 @@ class IDMRG2:
 
 
 def _inv_bond(C):
-    """C^-1 of a (small) bond tensor, through the host."""
-    return DeviceTensor.from_numpy(C.ctx, L.GB_KIND_BOND, np.linalg.inv(C.numpy()))
+    """C^-1 of a square bond tensor on the device: C = U S V' (cuSOLVER gesvd), C^-1 =
+    V S^-1 U'.  Only the singular values cross to the host (to form S^-1)."""
+    from .grassmann import _bond_as_mps, _diag, _mps_as_bond, _svd
+    from .infinite import adjoint
+    n = C.dims[0]
+    if C.dims[1] != n:
+        raise ValueError("inverse of a non-square bond tensor")
+    U, s, Vh = _svd(_bond_as_mps(C), (n, 1, n))
+    if s.size < n or not s[-1] > 0.0:
+        raise np.linalg.LinAlgError("bond tensor is singular")
+    V = _bond_as_mps(adjoint(Vh))
+    return _mps_as_bond(mul_tail(mul_tail(V, _diag(C.ctx, 1.0 / s, C.dtype)),
+                                 adjoint(_mps_as_bond(U))))
 
 
 def find_groundstate_idmrg2(psi, H, alg, envs=None):

@@ -174,12 +174,18 @@ def _fuse_two_site(W1, W2):
     return np.asfortranarray(W.reshape(wl, d1 * d2, d1 * d2, wr, order="F"))
 
 
+def _mpo_tensor(ctx, W):
+    return W if isinstance(W, DeviceTensor) else DeviceTensor.from_numpy(ctx, L.GB_KIND_MPO,
+                                                                          np.asarray(W))
+
+
 def mpo_projection(GL, GR, x, W1=None, W2=None, backend=None):
     """One application of a generic derivative operator between different bra and ket states
     (C_projection / AC_projection / AC2_projection with below != above,
     derivatives.jl:194-216, through MPO_C/AC/AC2_Hamiltonian, mpo_derivatives.jl:37-66):
-    GL[bra l w; ket l'], GR[ket r' w; bra r]; W1 (and W2) as host arrays (wl, d, d, wr) or
-    None for the bond operator.  Returns y on the bra bonds (gb_mpo_project)."""
+    GL[bra l w; ket l'], GR[ket r' w; bra r]; W1 a device MPO tensor or a host array
+    (wl, d, d, wr) (W1 and W2 host arrays for the two-site form), or None for the bond
+    operator.  Returns y on the bra bonds (gb_mpo_project)."""
     backend = backend or GB300Backend()
     ctx = x.ctx
     Dlb, Drb = GL.dims[0], GR.dims[2]
@@ -189,8 +195,8 @@ def mpo_projection(GL, GR, x, W1=None, W2=None, backend=None):
                                        backend.code, y.handle))
         return y
     if W2 is None:
-        W = DeviceTensor.from_numpy(ctx, L.GB_KIND_MPO, np.asarray(W1))
-        y = DeviceTensor(ctx, L.GB_KIND_MPS, x.dtype, (Dlb, W1.shape[1], Drb))
+        W = _mpo_tensor(ctx, W1)
+        y = DeviceTensor(ctx, L.GB_KIND_MPS, x.dtype, (Dlb, W.dims[1], Drb))
         L.check(L.lib().gb_mpo_project(ctx.handle, GL.handle, W.handle, GR.handle, x.handle,
                                        backend.code, y.handle))
         return y
@@ -201,11 +207,6 @@ def mpo_projection(GL, GR, x, W1=None, W2=None, backend=None):
     L.check(L.lib().gb_mpo_project(ctx.handle, GL.handle, W.handle, GR.handle, xf.handle,
                                    backend.code, y.handle))
     return y.reshape_(L.GB_KIND_AC2, (Dlb, d1, Drb, d2))
-
-
-def _mpo_tensor(ctx, W):
-    return W if isinstance(W, DeviceTensor) else DeviceTensor.from_numpy(ctx, L.GB_KIND_MPO,
-                                                                          np.asarray(W))
 
 
 def transfer_left(GL, W, A, Abar=None, backend=None):

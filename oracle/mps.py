@@ -390,6 +390,99 @@ def optimal_expand(pos, right, psi, H, envs, alg):
         psi.center = pos
 
 
+class SketchedExpand:
+    """SketchedExpand(; trunc = truncrank(add), oversampling) (changebonds/sketchedexpand.jl:
+    41-73).  The random isometries (randisometry) are drawn from numpy's PCG64 seeded with
+    `seed`, one Gaussian matrix per expansion in call order (the reference draws from Julia's
+    RNG, which cannot be reproduced here)."""
+
+    def __init__(self, add, oversampling=0, seed=0):
+        self.add, self.oversampling = add, oversampling
+        self.rng = np.random.default_rng(seed)
+
+    def gaussian(self, m, n, dtype):
+        g = self.rng.standard_normal((m, n))
+        if np.dtype(dtype).kind == "c":
+            g = g + 1j * self.rng.standard_normal((m, n))
+        return g.astype(dtype)
+
+    def sketch(self, comp, other):
+        """sketch_space: (l, k) = (sketch columns, target added directions) in the sketched
+        complement `comp`.  Both are also capped by the other site's complement `other`:
+        beyond it the orthonormalised directions cannot stay orthogonal to the state (the
+        reference leaves them arbitrary)."""
+        cap = min(comp, other)
+        k = min(self.add, cap)
+        return min(k + self.oversampling, cap), k
+
+
+def sketched_expand(pos, right, psi, H, envs, alg):
+    """changebond!(site, dir, psi, H, ::SketchedExpand, envs) (sketchedexpand.jl:75-162): a
+    random sketch Q of the left (right) complement folded into the left (right) environment
+    (transfer with bra Q), one MPO_AC application of the neighbouring site, its projection
+    onto that site's complement orthonormalised (LQ / QR, or an SVD truncated back to the
+    target when oversampled) and appended to the bond with zero weight."""
+    if right:
+        left, rt = psi.ac(pos), psi.AR[pos + 1]
+        Dl, d, D = left.shape
+        d2, Dn = rt.shape[1], rt.shape[2]
+        lmat = left.reshape(Dl * d, D, order="F")
+        RT = rt.reshape(D, d2 * Dn, order="F")
+        AL, _ = qr_pos(lmat)
+        compL, compR = Dl * d - D, d2 * Dn - D
+        if compL <= 0 or compR <= 0:
+            return
+        l, k = alg.sketch(compL, compR)
+        Om, _ = qr_pos(alg.gaussian(Dl * d, l, left.dtype))          # randisometry
+        Q, _ = qr_pos(Om - AL @ (AL.conj().T @ Om))
+        GLq = dv.transfer_left(envs.leftenv(pos, psi), H[pos], left,
+                               Q.reshape(Dl, d, l, order="F"))         # bra Q, ket AC
+        Y = dv.mpo_ac_apply(GLq, H[pos + 1], envs.rightenv(pos + 1, psi), rt)
+        B = Y.reshape(l, d2 * Dn, order="F")
+        B = B - (B @ RT.conj().T) @ RT
+        if l == k:
+            _, ar = lq_pos(B)
+        else:
+            _, _, Vh = np.linalg.svd(B, full_matrices=False)
+            ar = Vh[:k]
+        kk = ar.shape[0]
+        nal, nc = qr_pos(np.concatenate([lmat, np.zeros((Dl * d, kk), dtype=lmat.dtype)], axis=1))
+        psi.AL[pos] = nal.reshape(Dl, d, nal.shape[1], order="F")
+        psi.C[pos + 1] = nc / np.linalg.norm(nc)
+        psi.AR[pos + 1] = np.concatenate([RT, ar], axis=0).reshape(D + kk, d2, Dn, order="F")
+        psi.center = pos + 1
+    else:
+        lf, rgt = psi.AL[pos - 1], psi.ac(pos)
+        Dp, d, Dl = lf.shape
+        d2, Dr = rgt.shape[1], rgt.shape[2]
+        lmat = lf.reshape(Dp * d, Dl, order="F")
+        RT = rgt.reshape(Dl, d2 * Dr, order="F")
+        _, ARtt = lq_pos(RT)
+        compL, compR = Dp * d - Dl, d2 * Dr - Dl
+        if compL <= 0 or compR <= 0:
+            return
+        l, k = alg.sketch(compR, compL)
+        Om, _ = qr_pos(alg.gaussian(d2 * Dr, l, rgt.dtype))
+        Om = Om.conj().T                                                # adjoint(randisometry)
+        _, Qr = lq_pos(Om - (Om @ ARtt.conj().T) @ ARtt)
+        GRq = dv.transfer_right(envs.rightenv(pos, psi), H[pos], rgt,
+                                Qr.reshape(l, d2, Dr, order="F"))     # bra Qr, ket AC
+        Y = dv.mpo_ac_apply(envs.leftenv(pos - 1, psi), H[pos - 1], GRq, lf)
+        B = Y.reshape(Dp * d, l, order="F")
+        B = B - lmat @ (lmat.conj().T @ B)
+        if l == k:
+            Qn, _ = qr_pos(B)
+        else:
+            U, _, _ = np.linalg.svd(B, full_matrices=False)
+            Qn = U[:, :k]
+        kk = Qn.shape[1]
+        nc, Qr2 = lq_pos(np.concatenate([RT, np.zeros((kk, d2 * Dr), dtype=RT.dtype)], axis=0))
+        psi.AR[pos] = Qr2.reshape(Qr2.shape[0], d2, Dr, order="F")
+        psi.C[pos] = nc / np.linalg.norm(nc)
+        psi.AL[pos - 1] = np.concatenate([lmat, Qn], axis=1).reshape(Dp, d, Dl + kk, order="F")
+        psi.center = pos
+
+
 class DMRG3S:
     """DMRG3S(noise, ExponentialDecay(decay_rate)) with the truncated SVD DMRG fills in
     (post_expand/dmrg3s.jl:83-153; trunc = truncrank(maxdim) & trunctol(atol)): the noise
@@ -560,7 +653,8 @@ def dmrg1_local_update(pos, right, psi, H, alg, envs, eps_global, eps_trunc, dec
     eps_local = float(np.linalg.norm(project_complement(y, psi.al(pos))))
     if getattr(alg, "alg_expand", None) is not None:
         # 1. expand (dmrg.jl:128-134), then the update from the expanded tensor
-        optimal_expand(pos, right, psi, H, envs, alg.alg_expand)
+        expand = sketched_expand if isinstance(alg.alg_expand, SketchedExpand) else optimal_expand
+        expand(pos, right, psi, H, envs, alg.alg_expand)
         ac = psi.ac(pos)
         Heff = AC_hamiltonian(pos, psi, H, envs)
     Dl, d, Dr = ac.shape

@@ -257,7 +257,8 @@ def GC(monkeypatch):
                      _as_bond_t=_as_bond, _diff_norm=_diff_norm,
                      _arnoldi_dominant=_arnoldi_dominant, regauge=regauge,
                      project_complement_=project_complement_, DerivativeOperator=Op,
-                     fixedpoint=fixedpoint, L=FakeL, context=lambda *a: CTX)
+                     fixedpoint=fixedpoint, L=FakeL, context=lambda *a: CTX,
+                     _inv_bond=lambda C: T.of(np.linalg.inv(C.a)))
     for name, f in stand_ins.items():
         monkeypatch.setattr(cell, name, f)
     return cell

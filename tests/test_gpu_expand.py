@@ -1,7 +1,8 @@
 """Bond expansion on the device against the oracle: the DMRG3S perturbation
 (post_expand/dmrg3s.jl:133-192), concatenation along a bond, the two-sided complement
-projection, OptimalExpand (changebonds/optimalexpand.jl:122-187) and single-site DMRG with
-either expansion from a D = 2 start (the oracle reaches exact diagonalisation with both,
+projection, OptimalExpand (changebonds/optimalexpand.jl:122-187), SketchedExpand
+(changebonds/sketchedexpand.jl:75-162) and single-site DMRG with each expansion from a D = 2
+start (the oracle reaches exact diagonalisation with both,
 tests/test_oracle.py)."""
 import numpy as np
 import pytest
@@ -128,7 +129,53 @@ def test_optimal_expand_matches_the_oracle(ctx):
     assert np.abs(new_d.conj().T @ new_d - new_o.conj().T @ new_o).max() < 1e-10
 
 
-@pytest.mark.parametrize("kind", ["optimal_expand", "dmrg3s"])
+def _oracle_centre(As, pos):
+    """Oracle FiniteMPS with AL left of bond `pos`, C[pos] and AR right of it."""
+    psi = P.finite_mps_from_tensors(As)
+    for i in range(pos):
+        A = np.einsum("ab,bsc->asc", psi.C[i], psi.AR[i])
+        Q, R = P.qr_pos(A.reshape(-1, A.shape[2], order="F"))
+        psi.AL[i], psi.C[i + 1], psi.center = Q.reshape(A.shape[0], 2, Q.shape[1], order="F"), R, i + 1
+    return psi
+
+
+@pytest.mark.parametrize("right", [True, False])
+@pytest.mark.parametrize("ov", [0, 2])
+def test_sketched_expand_matches_the_oracle(ctx, right, ov):
+    """SketchedExpand (sketchedexpand.jl:75-162) with the same random sketch: the same bond
+    growth and added directions, the state unchanged."""
+    L_, pos = 8, 3
+    H = M.finite_mpo_hamiltonian(L_, 2, M.heisenberg_terms(L_))
+    As = P.random_initial_tensors(L_, 2, 3, 6)
+    opsi = _oracle_centre(As, pos)
+    P.sketched_expand(pos, right, opsi, H, P.FiniteEnvironments(opsi, H),
+                      P.SketchedExpand(2, oversampling=ov, seed=23))
+    Hd = mpsgb.heisenberg_XXX(L_)
+    psi = mpsgb.FiniteMPS.from_tensors(As, ctx, center=pos)
+    full = lambda ps: _vector([ps.AL[i].numpy() for i in range(ps.center)]
+                              + [ps.ac(ps.center).numpy()]
+                              + [ps.AR[i].numpy() for i in range(ps.center + 1, L_)])
+    v0 = full(psi)
+    envs = mpsgb.FiniteEnvironments(psi, Hd)
+    mpsgb.algorithms.sketched_expand(pos, right, psi, Hd, envs,
+                                     mpsgb.SketchedExpand(2, oversampling=ov, seed=23))
+    assert psi.center == opsi.center
+    v1 = full(psi)
+    assert np.linalg.norm(v1 / np.linalg.norm(v1) - v0 / np.linalg.norm(v0)) < 1e-12
+    if right:
+        a, b = psi.AR[pos + 1].numpy(), opsi.AR[pos + 1]
+        a, b = (x.reshape(x.shape[0], -1, order="F") for x in (a, b))
+    else:
+        a, b = psi.AL[pos - 1].numpy(), opsi.AL[pos - 1]
+        a, b = (x.reshape(-1, x.shape[2], order="F").T for x in (a, b))
+    assert a.shape == b.shape
+    if ov == 0:
+        assert np.abs(a - b).max() < 1e-10          # QR / LQ: the same rows
+    else:
+        assert np.abs(a.conj().T @ a - b.conj().T @ b).max() < 1e-10   # SVD: the same span
+
+
+@pytest.mark.parametrize("kind", ["optimal_expand", "dmrg3s", "sketched_expand"])
 def test_single_site_dmrg_with_expansion_reaches_ed(ctx, kind):
     L_ = 10
     terms = M.heisenberg_terms(L_)
@@ -139,6 +186,10 @@ def test_single_site_dmrg_with_expansion_reaches_ed(ctx, kind):
         oalg = P.DMRG(tol=1e-10, maxiter=12, alg_expand=P.OptimalExpand(4))
         alg = mpsgb.DMRG(tol=1e-10, maxiter=12, alg_expand=mpsgb.OptimalExpand(4))
         bar = 1e-10
+    elif kind == "sketched_expand":
+        oalg = P.DMRG(tol=1e-10, maxiter=12, alg_expand=P.SketchedExpand(4, seed=3))
+        alg = mpsgb.DMRG(tol=1e-10, maxiter=12, alg_expand=mpsgb.SketchedExpand(4, seed=3))
+        bar = 1e-9
     else:
         oalg = P.DMRG(tol=1e-10, maxiter=12, alg_gauge=P.DMRG3S(0.1, 0.8, 16, 1e-12))
         alg = mpsgb.DMRG(tol=1e-10, maxiter=12, alg_gauge=mpsgb.DMRG3S(0.1, 0.8, 16, 1e-12))

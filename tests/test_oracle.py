@@ -349,3 +349,48 @@ def test_oracle_optimal_expand_preserves_the_state_and_reaches_ed():
     _, _, eps, hist = P.find_groundstate_dmrg(psi0, H, alg)
     assert eps <= 1e-10
     assert abs(hist[-1][1] - e_ed) < 1e-10
+
+
+@pytest.mark.parametrize("ov", [0, 2])
+def test_oracle_sketched_expand_preserves_the_state_and_reaches_ed(ov):
+    """SketchedExpand (changebonds/sketchedexpand.jl:75-162): the sketched directions are
+    appended with zero weight (state unchanged, bond grown by `add`, orthonormal new rows
+    orthogonal to the old ones), both directions; ahead of every single-site update it lets
+    DMRG from a D = 2 start reach exact diagonalisation."""
+    L_ = 8
+    H = M.finite_mpo_hamiltonian(L_, 2, M.heisenberg_terms(L_))
+    for right in (True, False):
+        psi = P.finite_mps_from_tensors(P.random_initial_tensors(L_, 2, 2, 6))
+        pos = 3
+        # centre bond at pos (AC[pos] = C[pos] AR[pos]) with AL left of it
+        psi_l = P.finite_mps_from_tensors(P.random_initial_tensors(L_, 2, 2, 6))
+        for i in range(pos):
+            A = np.einsum("ab,bsc->asc", psi_l.C[i], psi_l.AR[i])
+            Q, R = P.qr_pos(A.reshape(-1, A.shape[2], order="F"))
+            psi_l.AL[i] = Q.reshape(A.shape[0], 2, Q.shape[1], order="F")
+            psi_l.C[i + 1] = R
+            psi_l.center = i + 1
+        psi = psi_l
+        v0 = _mps_vector(psi)
+        D0 = psi.C[pos].shape[0] if not right else psi.AR[pos + 1].shape[0]
+        alg = P.SketchedExpand(2, oversampling=ov, seed=11)
+        P.sketched_expand(pos, right, psi, H, P.FiniteEnvironments(psi, H), alg)
+        v1 = _mps_vector(psi)
+        assert np.linalg.norm(v1 / np.linalg.norm(v1) - v0 / np.linalg.norm(v0)) < 1e-12
+        if right:
+            D1 = psi.AR[pos + 1].shape[0]
+            assert psi.center == pos + 1 and D1 == D0 + 2
+            R_ = psi.AR[pos + 1].reshape(D1, -1, order="F")
+            assert np.abs(R_ @ R_.conj().T - np.eye(D1)).max() < 1e-12
+        else:
+            D1 = psi.AL[pos - 1].shape[2]
+            assert psi.center == pos and D1 == D0 + 2
+            A_ = psi.AL[pos - 1].reshape(-1, D1, order="F")
+            assert np.abs(A_.conj().T @ A_ - np.eye(D1)).max() < 1e-12
+    L_ = 10
+    H = M.finite_mpo_hamiltonian(L_, 2, M.heisenberg_terms(L_))
+    e_ed = M.ed_ground_energy(L_, 2, M.heisenberg_terms(L_))[0]
+    psi0 = P.finite_mps_from_tensors(P.random_initial_tensors(L_, 2, 2, 5))
+    alg = P.DMRG(tol=1e-10, maxiter=12, alg_expand=P.SketchedExpand(4, oversampling=ov, seed=3))
+    _, _, eps, hist = P.find_groundstate_dmrg(psi0, H, alg)
+    assert abs(hist[-1][1] - e_ed) < 1e-9, (hist[-1][1], e_ed)
