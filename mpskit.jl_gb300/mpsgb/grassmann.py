@@ -1,5 +1,6 @@
-"""GradientGrassmann for finite MPS on the device: the left-canonical tensors AL[i] as points
-of Grassmann manifolds, optimised by Riemannian conjugate gradients (mpsgb.optim).
+"""GradientGrassmann on the device (finite MPS and one-site InfiniteMPS): the left-canonical
+tensors AL[i] as points of Grassmann manifolds, optimised by Riemannian conjugate gradients
+(mpsgb.optim).
 
   GradientGrassmann, find_groundstate  -- src/algorithms/groundstate/gradient_grassmann.jl:1-121
   fg, precondition, retract, transport, inner, rho_inv_regularized
@@ -266,12 +267,52 @@ class GradientGrassmann:
                                             verbosity=self.verbosity)
 
 
+# ------------------------------------------------------------------ one-site InfiniteMPS
+def fg_infinite(x, H, envs, backend=None):
+    """fg(state::InfiniteMPS, H::InfiniteMPOHamiltonian, envs) (grassmann.jl:171-190): the
+    fixed-point environments recalculated, the energy density, and the projected AC
+    derivative times C'."""
+    from .infinite import _heff_ac, energy_density
+    backend = backend or GB300Backend()
+    envs.recalculate(x)
+    f = energy_density(x, envs, backend)
+    y = _heff_ac(envs, backend)(x.AC)
+    g = project(y, x.AL)
+    return f, [GrassmannTangent(x.AL, mul_tail(g.Z, adjoint(x.C)))]
+
+
+def retract_infinite(x, g, a):
+    """retract(state::InfiniteMPS, g, a) (grassmann.jl:109-122): AL along its geodesic, then
+    InfiniteMPS(AL', C) -- the right uniform gauge fixed from the old C."""
+    from .infinite import InfiniteMPS, uniform_rightorth
+    ALn, xi = retract_site(x.AL, g[0], a)
+    AR, C = uniform_rightorth(ALn, x.C)
+    return InfiniteMPS(ALn, AR, C), [xi]
+
+
+def transport_infinite(h, x, g, a, xn):
+    return [transport_site(h[0], x.AL, g[0], a, xn.AL)]
+
+
+def precondition_infinite(x, g):
+    rtol = max(np.finfo(np.float64).eps ** 0.75, g[0].norm())
+    return [GrassmannTangent(g[0].W, mul_tail(g[0].Z, rho_inv_regularized(x.C, rtol)))]
+
+
 def find_groundstate_grassmann(psi, H, alg=None, envs=None):
     """find_groundstate(psi, H, GradientGrassmann) (gradient_grassmann.jl:80-121) ->
-    (psi, envs, normgrad, history): the optimised state (left-canonical, centre bond 0
-    after the closing LQ sweep), its environments, the final gradient norm and the
-    gradient-norm history."""
+    (psi, envs, normgrad, history): the optimised state (finite: left-canonical, centre bond
+    0 after the closing LQ sweep; infinite: uniformly gauged), its environments, the final
+    gradient norm and the gradient-norm history."""
     alg = alg or GradientGrassmann()
+    from .infinite import InfiniteEnvironments, InfiniteMPS
+    if isinstance(psi, InfiniteMPS):
+        envs = envs or InfiniteEnvironments(psi, H)
+        x, f, g, numfg, hist = optimize(
+            lambda x_: fg_infinite(x_, H, envs, alg.backend), psi, alg.method,
+            retract_infinite, transport_infinite, inner, add, scale, precondition_infinite)
+        envs.recalculate(x)
+        return x, envs, hist[-1], {"energy": f, "numfg": numfg, "normgrad": hist}
     if psi.C[psi.center].charges is not None or (psi.AR[0] is not None
                                                  and psi.AR[0].charges is not None):
         raise NotImplementedError("GradientGrassmann: U(1)-charged states are not supported")

@@ -100,3 +100,44 @@ def test_gradient_grassmann_reaches_ed(ctx, gx, bar):
         a = A.numpy()
         Q = a.reshape(a.shape[0], -1, order="F")
         assert np.abs(Q @ Q.conj().T - np.eye(Q.shape[0])).max() < 1e-12
+
+
+def _A(D, seed):
+    rng = np.random.default_rng(seed)
+    return rng.standard_normal((D, 2, D)) + 1j * rng.standard_normal((D, 2, D))
+
+
+def test_infinite_gradient_is_the_derivative_of_the_energy(ctx):
+    """fg(::InfiniteMPS) (grassmann.jl:171-190): along the geodesic of a direction d the
+    energy density changes at the rate inner(g, d) (central differences)."""
+    H = mpsgb.transverse_field_ising(1, g=0.8, infinite=True)
+    psi = mpsgb.InfiniteMPS.from_tensor(_A(8, 4), ctx)
+    envs = mpsgb.InfiniteEnvironments(psi, H)
+    f0, g0 = G.fg_infinite(psi, H, envs)
+    d = G.scale(G.precondition_infinite(psi, g0), -1.0)
+    slope = G.inner(psi, g0, d)
+    assert slope < 0
+    h = 1e-4
+    fp = G.fg_infinite(G.retract_infinite(psi, d, h)[0], H, envs)[0]
+    fm = G.fg_infinite(G.retract_infinite(psi, d, -h)[0], H, envs)[0]
+    assert abs((fp - fm) / (2 * h) - slope) <= 1e-5 * abs(slope)
+
+
+@pytest.mark.parametrize("gx,D", [(4.0, 6), (0.8, 10)])
+def test_infinite_gradient_grassmann_matches_vumps(ctx, gx, D):
+    """GradientGrassmann on a one-site InfiniteMPS (the reference's infinite groundstate
+    test, test/algorithms/groundstate.jl:268-292) reaches the VUMPS fixed point of the same
+    bond dimension and the TFIM closed form within the truncation."""
+    H = mpsgb.transverse_field_ising(1, g=gx, infinite=True)
+    psi = mpsgb.InfiniteMPS.from_tensor(_A(D, 1), ctx)
+    out, envs, normgrad, hist = mpsgb.find_groundstate(psi, H,
+                                                       mpsgb.GradientGrassmann(tol=1e-8, maxiter=300))
+    assert normgrad <= 1e-8, hist["normgrad"][-5:]
+    e = mpsgb.infinite.energy_density(out, envs)
+    vpsi = mpsgb.InfiniteMPS.from_tensor(_A(D, 1), ctx)
+    vpsi, venvs, eps, vhist = mpsgb.find_groundstate_vumps(vpsi, H, mpsgb.VUMPS(tol=1e-10,
+                                                                                maxiter=200))
+    e_exact = M.tfim_infinite_energy_density(gx)
+    assert e >= e_exact - 1e-10
+    assert abs(e - vhist[-1]["energy"]) <= 1e-9 * abs(e), (e, vhist[-1]["energy"])
+    assert mpsgb.infinite.galerkin(out, envs) < 1e-6
