@@ -67,7 +67,8 @@ def parse():
     ap.add_argument("--symmetry", default="u1", choices=["u1", "none"],
                     help="u1: U(1) (total Sz = 0) block-sparse state and MPO; none: dense")
     ap.add_argument("--workload", default="dmrg2",
-                    choices=["dmrg2", "dmrg2-sweep", "matvec", "vumps-sweep", "vumps-xxz"],
+                    choices=["dmrg2", "dmrg2-sweep", "matvec", "vumps-sweep", "vumps-xxz",
+                             "grassmann"],
                     help="dmrg2: the headline DMRG2 step; dmrg2-sweep: full DMRG2 sweeps of "
                          "the same state (checkpointed environments); matvec: repeated H_eff "
                          "applications at the central bond (a small case for profiling); "
@@ -76,7 +77,8 @@ def parse():
                          "chains (VUMPS, g in [0.1, 2], D in {64..256}) solved concurrently; "
                          "vumps-xxz: one-site VUMPS of the XXZ chain (Jz = 1.5, sublattice-"
                          "rotated) at D = 256, "
-                         "plain FP64 against the split precision")
+                         "plain FP64 against the split precision; grassmann: GradientGrassmann "
+                         "cost+gradient evaluations on a finite TFIM chain (L=64, D=128)")
     ap.add_argument("--schedule", default="grouped",
                     choices=["grouped", "persistent", "persistent_dense", "tile"],
                     help="split GEMM schedule: grouped (one launch per contraction over its "
@@ -945,6 +947,78 @@ def run_vumps_xxz(args):
     print(json.dumps(line), flush=True)
 
 
+def run_grassmann(args):
+    """GradientGrassmann on a finite chain: TFIM at its critical point (g = 1), L = 64,
+    D = 128, ComplexF64, seeded random state.  One step = one evaluation of the cost and
+    gradient at a new point (grassmann.jl:150-169: environments of the new AL/AR, the energy,
+    one AC projection per site, the Grassmann projection) plus the retraction that produced
+    the point; after the timed steps a short CG run reports the gradient-norm decay.
+    cpu_baseline: the oracle's fg at the same point on the host cores."""
+    import mpsgb
+    from mpsgb import grassmann as G
+    from oracle import grassmann as OG
+    from oracle import models as M
+    from oracle import mps as P
+    L_, D, gx = 64, 128, 1.0
+    ctx = mpsgb.context(0)
+    H = mpsgb.transverse_field_ising(L_, g=gx)
+    As = P.random_initial_tensors(L_, 2, D, args.seed)
+    psi = mpsgb.FiniteMPS.from_tensors(As, ctx)
+    x = G.GrassmannPoint.from_state(psi)
+    envs = mpsgb.FiniteEnvironments(x.psi, H, ctx)
+    f, g = G.fg(x, H, envs)
+    d = G.scale(G.precondition(x, g), -1.0)
+    a = 1e-3
+    n0 = ctx.kernel_launches()
+
+    def step(k):
+        xn, _ = G.retract(x, d, a * (1 + k))
+        return G.fg(xn, H, envs)
+
+    for k in range(args.warmup):
+        step(k)
+    ctx.synchronize()
+    n0 = ctx.kernel_launches()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        fk, _ = step(args.warmup + k)
+    ctx.synchronize()
+    t = (time.perf_counter() - t0) / args.steps
+    launches = ctx.kernel_launches() - n0
+    log(f"grassmann: {1e3 * t:.1f} ms per retract + fg, {launches} launches")
+    # a short optimisation from the same state
+    t1 = time.perf_counter()
+    _, _, ng, hist = mpsgb.find_groundstate(mpsgb.FiniteMPS.from_tensors(As, ctx), H,
+                                            mpsgb.GradientGrassmann(tol=1e-8, maxiter=20))
+    t_opt = time.perf_counter() - t1
+    cpu = None
+    if not args.no_cpu_baseline:
+        oH = M.finite_mpo_hamiltonian(L_, 2, M.tfim_terms(L_, g=gx))
+        AL = [a_.numpy() for a_ in x.AL]
+        Cend = x.psi.C[L_].numpy()
+        t2 = time.perf_counter()
+        of, og = OG.fg(AL, Cend, oH)
+        tc = time.perf_counter() - t2
+        cpu = {"value": tc, "unit": "s/fg", "cores": os.cpu_count(), "kind": "port",
+               "sample": "one oracle fg (environments, energy, 64 AC projections) at the "
+                         "device's first point; numpy/BLAS",
+               "energy_difference": abs(of - f)}
+    line = {
+        "metric": "GradientGrassmann s per cost+gradient evaluation, TFIM g=1, L=64, D=128",
+        "value": t, "unit": "s/fg", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c128 (fp64)", "data": "synthetic",
+        "config": {"workload": "finite TFIM g=1 L=64, D=128, ComplexF64, seeded random MPS; "
+                               "step = Grassmann retraction + fg", "l2": "working set < L2"},
+        "gpu_launches": launches,
+        "cg_20_iterations": {"seconds": t_opt, "fg_evaluations": hist["numfg"],
+                             "normgrad_first_last": [hist["normgrad"][0], hist["normgrad"][-1]],
+                             "energy": hist["energy"]},
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -957,6 +1031,8 @@ def main():
         run_dmrg2_sweep(args)
     elif args.workload == "vumps-xxz":
         run_vumps_xxz(args)
+    elif args.workload == "grassmann":
+        run_grassmann(args)
     else:
         run_ours(args)
 

@@ -558,7 +558,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       for (int j = 0; j < 32; ++j) {
         int64_t n = n0 + c0 + j;
         if (n >= args.N) break;
-        double v = args.alpha * (double)__uint_as_float(r[j]);
+        double v = widen_f32(r[j]);
+        if (args.alpha != 1.0) v *= args.alpha;
         double* p;
         if (args.cplx) {
           int64_t nn = n < args.Nlog ? n : n - args.Nlog;
@@ -868,10 +869,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
         return cz + m + args.ldc * n;
       };
+      const bool alpha_one = args.alpha == 1.0;
       auto store = [&](int64_t e, double val) {
         if (args.c_f32) {
           float* p = (float*)args.C + e;
-          if (args.beta != 0.0) val = fma(args.beta, (double)*p, val);
+          if (args.beta != 0.0) val = fma(args.beta, widen_f32(*p), val);
           *p = (float)val;
         } else {
           double* p = args.C + e;
@@ -901,7 +903,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         for (int jj = 0; jj < 32; ++jj) {
           const int64_t n = n0 + c0 + jj;
           if (n >= args.N) break;
-          store(off(n), args.alpha * (double)__uint_as_float(v[jj]));
+          const double x = widen_f32(v[jj]);
+          store(off(n), alpha_one ? x : args.alpha * x);
         }
       }
       tc_fence_before();

@@ -468,24 +468,42 @@ __global__ void gmix_kernel(int64_t nJ, int64_t N, int64_t xn, const int64_t* __
     const GMixEntry en = ent[n * nJ + J];
     if (en.hi <= en.lo || en.row < 0) continue;
     const int64_t base = (int64_t)en.row * kmax + en.kst - en.lo;
-    for (int64_t a = en.lo + lane; a < en.hi; a += 32) {
+    // four 32-element chunks per pass with their loads issued together (more bytes in
+    // flight per warp: the mix is a short strided copy when its rows hold one entry)
+    constexpr int U = 4;
+    for (int64_t a0 = en.lo + lane; a0 < en.hi; a0 += 32 * U) {
       // the arithmetic of gmix_staged_kernel, term for term (identical results)
-      float s = 0.0f, c = 0.0f;
+      float s[U], c[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) s[u] = c[u] = 0.0f;
       for (int e = e0; e < e1; ++e) {
-        const float xv = x[a + in_off[col[e]] + n * xn];
+        const float* xp = x + in_off[col[e]] + n * xn;
+        float xv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int64_t a = a0 + 32 * u;
+          xv[u] = a < en.hi ? xp[a] : 0.0f;
+        }
         const float vh = (float)val[e];
-        if (std::is_same<E, float>::value) {
-          const float vl = (float)(val[e] - (double)vh);
-          const float p = vh * xv;
-          const float pe = fmaf(vh, xv, -p) + vl * xv;
-          const float t = s + p, z = t - s;
-          c += ((s - (t - z)) + (p - z)) + pe;
-          s = t;
-        } else {
-          s = fmaf(vh, xv, s);
+        const float vl = (float)(val[e] - (double)vh);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          if (std::is_same<E, float>::value) {
+            const float p = vh * xv[u];
+            const float pe = fmaf(vh, xv[u], -p) + vl * xv[u];
+            const float t = s[u] + p, z = t - s[u];
+            c[u] += ((s[u] - (t - z)) + (p - z)) + pe;
+            s[u] = t;
+          } else {
+            s[u] = fmaf(vh, xv[u], s[u]);
+          }
         }
       }
-      split_put_f(hi, lo, base + a, s + c);
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int64_t a = a0 + 32 * u;
+        if (a < en.hi) split_put_f(hi, lo, base + a, s[u] + c[u]);
+      }
     }
   }
 }
@@ -806,7 +824,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
     const bool copy_f32 = f32 && alpha == 1.0 && beta == 0.0;
     const bool alpha_one = alpha == 1.0, beta_one = beta == 1.0;
     auto loadC = [&](int64_t e) -> double {
-      return f32 ? (double)((const float*)args.C)[e] : ((const double*)args.C)[e];
+      return f32 ? widen_f32(((const float*)args.C)[e]) : ((const double*)args.C)[e];
     };
     auto putC = [&](int64_t e, double v) {
       if (f32) ((float*)args.C)[e] = (float)v;
@@ -852,8 +870,11 @@ __global__ void __launch_bounds__(G_THREADS, 1)
 #pragma unroll
             for (int jj = 0; jj < 16; ++jj) {
               co[jj] = __shfl_sync(0xffffffffu, myco, h + jj);
-              const double x = (double)__uint_as_float(v[h + jj]);
-              val[jj] = alpha_one ? x : alpha * x;
+              val[jj] = widen_f32(v[h + jj]);
+            }
+            if (!alpha_one) {
+#pragma unroll
+              for (int jj = 0; jj < 16; ++jj) val[jj] *= alpha;
             }
             if (beta != 0.0 && rvalid) {
               double cv[16];
@@ -884,8 +905,11 @@ __global__ void __launch_bounds__(G_THREADS, 1)
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
               ro[i] = __shfl_sync(0xffffffffu, roff, h + i);
-              const double x = (double)xb[(h + i) * 33 + lane];
-              val[i] = alpha_one ? x : alpha * x;
+              val[i] = widen_f32(xb[(h + i) * 33 + lane]);
+            }
+            if (!alpha_one) {
+#pragma unroll
+              for (int i = 0; i < 16; ++i) val[i] *= alpha;
             }
             if (beta != 0.0 && cvalid) {
               double cv[16];

@@ -129,29 +129,23 @@ def test_optimal_expand_matches_the_oracle(ctx):
     assert np.abs(new_d.conj().T @ new_d - new_o.conj().T @ new_o).max() < 1e-10
 
 
-def _oracle_centre(As, pos):
-    """Oracle FiniteMPS with AL left of bond `pos`, C[pos] and AR right of it."""
-    psi = P.finite_mps_from_tensors(As)
-    for i in range(pos):
-        A = np.einsum("ab,bsc->asc", psi.C[i], psi.AR[i])
-        Q, R = P.qr_pos(A.reshape(-1, A.shape[2], order="F"))
-        psi.AL[i], psi.C[i + 1], psi.center = Q.reshape(A.shape[0], 2, Q.shape[1], order="F"), R, i + 1
-    return psi
-
-
 @pytest.mark.parametrize("right", [True, False])
 @pytest.mark.parametrize("ov", [0, 2])
 def test_sketched_expand_matches_the_oracle(ctx, right, ov):
     """SketchedExpand (sketchedexpand.jl:75-162) with the same random sketch: the same bond
     growth and added directions, the state unchanged."""
     L_, pos = 8, 3
-    H = M.finite_mpo_hamiltonian(L_, 2, M.heisenberg_terms(L_))
     As = P.random_initial_tensors(L_, 2, 3, 6)
-    opsi = _oracle_centre(As, pos)
-    P.sketched_expand(pos, right, opsi, H, P.FiniteEnvironments(opsi, H),
-                      P.SketchedExpand(2, oversampling=ov, seed=23))
     Hd = mpsgb.heisenberg_XXX(L_)
     psi = mpsgb.FiniteMPS.from_tensors(As, ctx, center=pos)
+    # the oracle state in the device state's gauge, and the device MPO's channel basis
+    n = lambda t: None if t is None else t.numpy()
+    opsi = P.FiniteMPS([n(psi.AL[i]) if i < pos else None for i in range(L_)],
+                       [n(psi.AR[i]) if i >= pos else None for i in range(L_)],
+                       [n(psi.C[i]) if i == pos else None for i in range(L_ + 1)], pos)
+    H = M.MPOHam([np.asarray(w, dtype=np.complex128) for w in Hd.W], Hd.chans)
+    P.sketched_expand(pos, right, opsi, H, P.FiniteEnvironments(opsi, H),
+                      P.SketchedExpand(2, oversampling=ov, seed=23))
     full = lambda ps: _vector([ps.AL[i].numpy() for i in range(ps.center)]
                               + [ps.ac(ps.center).numpy()]
                               + [ps.AR[i].numpy() for i in range(ps.center + 1, L_)])
