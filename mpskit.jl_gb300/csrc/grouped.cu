@@ -898,6 +898,16 @@ __global__ void __launch_bounds__(G_THREADS, 1)
           __syncwarp();
           const bool cvalid = nl < nend;
           const int64_t co = cvalid ? args.coloff[nl] : 0;
+          if (copy_f32) {
+            // FP32 output that is the accumulator itself: no FP64 arithmetic or conversion
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+              const int64_t r = __shfl_sync(0xffffffffu, roff, i);
+              if (cvalid && mrow0 + i < T.mlim) ((float*)args.C)[r + co] = xb[i * 33 + lane];
+            }
+            __syncwarp();
+            return;
+          }
 #pragma unroll
           for (int h = 0; h < 32; h += 16) {
             int64_t ro[16];

@@ -105,6 +105,29 @@ def project(X, W):
     return GrassmannTangent(W, project_complement_(X.copy(), W))
 
 
+def polar_factor(W, maxiter=6):
+    """The unitary polar factor of a near-isometry W (its columns), the projectisometric
+    of the retraction, by Newton-Schulz iterations W <- W (3 - W'W) / 2 (quadratic
+    convergence to the polar factor while |W'W - 1| < 1): GEMMs only, no SVD.  Stops once
+    |W'W - 1| is at rounding level; falls back to the SVD (U V') if the iteration does not
+    settle."""
+    ctx, k = W.ctx, W.dims[2]
+    eye = DeviceTensor.from_numpy(ctx, L.GB_KIND_BOND, np.eye(k, dtype=W.dtype))
+    for _ in range(maxiter):
+        G = _left_overlap(W, W)
+        G.axpy_(-1.0, eye)
+        err = float(np.abs(G.numpy()).max())
+        if err <= 4.0 * np.finfo(np.float64).eps * k:
+            return W
+        if err >= 0.5:
+            break
+        G.scale_(-0.5)
+        G.axpy_(1.0, eye)          # (3 - W'W) / 2 = 1 - (W'W - 1) / 2
+        W = mul_tail(W, G)
+    U, _, Vh = _svd(W, W.dims)
+    return mul_tail(U, Vh)
+
+
 def retract_site(W, D, a):
     """Grassmann.retract(W, D, a) -> (W(a), D(a)): the geodesic from W along D."""
     ctx, dt = W.ctx, W.dtype
@@ -118,8 +141,7 @@ def retract_site(W, D, a):
     # projectisometric: the polar factor.  Directions carry rounding noise off the tangent
     # space (most of all where the tangent space is empty and the preconditioner large);
     # without this the AL drift away from isometries over the iterations.
-    Uw, _, Vw = _svd(Wn, Wn.dims)
-    Wn = mul_tail(Uw, Vw)
+    Wn = polar_factor(Wn)
     T = mul_tail(WV, _diag(ctx, -sn * s, dt))
     T.axpy_(1.0, mul_tail(U, _diag(ctx, cs * s, dt)))
     Zn = project_complement_(mul_tail(T, Vh), Wn)
