@@ -113,7 +113,7 @@ __global__ void pack_kernel(PackArgs p, const double* __restrict__ src, E* __res
     double re = tre[j][tx], im = tim[j][tx];
     nz |= (re != 0.0 || im != 0.0);
     auto put = [&](int64_t row, int64_t col, double v) {
-      split_put_f(hi, lo, row * p.Kp + col, (float)v);
+      split_put_f(hi, lo, row * p.Kp + col, narrow_f64(v));
     };
     if (!p.cplx) {
       put(r, k, re);
@@ -281,7 +281,9 @@ __global__ void mixpack_kernel(int64_t A, int64_t N, int64_t xn, const int64_t* 
   const int e0 = row_ptr[J], e1 = row_ptr[J + 1];
   const int lane = threadIdx.x % 32;
   E* lo = hi + plane;
-  auto put = [&](int64_t row, int64_t c, double v) { split_put_f(hi, lo, row * Kp + c, (float)v); };
+  auto put = [&](int64_t row, int64_t c, double v) {
+    split_put_f(hi, lo, row * Kp + c, narrow_f64(v));
+  };
   auto mark = [&](int64_t row, int64_t kb) {
     atomicOr(&mask[(row / MASK_ROWS) * kw + kb / 32], 1u << (kb % 32));
   };

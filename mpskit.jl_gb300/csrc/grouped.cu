@@ -326,7 +326,7 @@ __global__ void gpack_kernel(const GPackTile* __restrict__ tiles, const int32_t*
     const int kp = T.kp0 + kk;
     float v = 0.0f;
     if (i < T.nr && kp < kl && in[kk])
-      v = (float)src[(int64_t)rdense[T.rp0 + i] * rs + ((int64_t)kdense[k0 + kp] - klo) * ks];
+      v = narrow_f64(src[(int64_t)rdense[T.rp0 + i] * rs + ((int64_t)kdense[k0 + kp] - klo) * ks]);
     t[i][kk] = v;
   }
   __syncthreads();

@@ -64,6 +64,46 @@ __device__ __forceinline__ double widen_f32(uint32_t b) {
   return __hiloint2double((int)hi, (int)(m << 29));
 }
 __device__ __forceinline__ double widen_f32(float f) { return widen_f32(__float_as_uint(f)); }
+// FP64 -> FP32 rounding to nearest, ties to even, with integer operations only: the same
+// result as the FP64-pipe conversion (the operand packs round every element once).
+__device__ __forceinline__ float narrow_f64(double x) {
+  const uint64_t b = (uint64_t)__double_as_longlong(x);
+  const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+  const int e = (int)((b >> 52) & 0x7FF);
+  const uint64_t m = b & 0xFFFFFFFFFFFFFull;
+  uint32_t bits;
+  if (e == 0x7FF) {
+    bits = sign | 0x7F800000u | (m ? 0x400000u : 0u);
+  } else if (e == 0) {
+    bits = sign;  // double subnormals lie far below half the smallest float
+  } else {
+    int fe = e - 896;  // float biased exponent
+    if (fe >= 255) {
+      bits = sign | 0x7F800000u;
+    } else {
+      const int shift = fe >= 1 ? 29 : 30 - fe;  // significand bits dropped
+      if (shift > 54) {
+        bits = sign;
+      } else {
+        const uint64_t mant = m | (1ull << 52);
+        uint64_t q = mant >> shift;
+        const uint64_t rem = mant & ((1ull << shift) - 1), half = 1ull << (shift - 1);
+        if (rem > half || (rem == half && (q & 1))) ++q;
+        if (fe >= 1) {
+          if (q >> 24) {
+            q >>= 1;
+            ++fe;
+          }
+          bits = fe >= 255 ? (sign | 0x7F800000u)
+                           : (sign | ((uint32_t)fe << 23) | ((uint32_t)q & 0x7FFFFFu));
+        } else {
+          bits = sign | (uint32_t)q;  // subnormal (rounding up to 2^23 gives the smallest normal)
+        }
+      }
+    }
+  }
+  return __uint_as_float(bits);
+}
 __device__ __forceinline__ bool plane_nz(__nv_bfloat16 a) { return __bfloat162float(a) != 0.f; }
 __device__ __forceinline__ bool plane_nz(float a) { return a != 0.f; }
 inline bool is_tf32(int prec) { return prec == GB_PREC_TF32X3; }
