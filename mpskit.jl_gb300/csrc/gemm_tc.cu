@@ -113,7 +113,7 @@ __global__ void pack_kernel(PackArgs p, const double* __restrict__ src, E* __res
     double re = tre[j][tx], im = tim[j][tx];
     nz |= (re != 0.0 || im != 0.0);
     auto put = [&](int64_t row, int64_t col, double v) {
-      split_put_f(hi, lo, row * p.Kp + col, narrow_f64(v));
+      split_put_f(hi, lo, row * p.Kp + col, (float)v);
     };
     if (!p.cplx) {
       put(r, k, re);
@@ -281,9 +281,7 @@ __global__ void mixpack_kernel(int64_t A, int64_t N, int64_t xn, const int64_t* 
   const int e0 = row_ptr[J], e1 = row_ptr[J + 1];
   const int lane = threadIdx.x % 32;
   E* lo = hi + plane;
-  auto put = [&](int64_t row, int64_t c, double v) {
-    split_put_f(hi, lo, row * Kp + c, narrow_f64(v));
-  };
+  auto put = [&](int64_t row, int64_t c, double v) { split_put_f(hi, lo, row * Kp + c, (float)v); };
   auto mark = [&](int64_t row, int64_t kb) {
     atomicOr(&mask[(row / MASK_ROWS) * kw + kb / 32], 1u << (kb % 32));
   };
@@ -560,7 +558,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       for (int j = 0; j < 32; ++j) {
         int64_t n = n0 + c0 + j;
         if (n >= args.N) break;
-        double v = widen_f32(r[j]);
+        double v = (double)__uint_as_float(r[j]);
         if (args.alpha != 1.0) v *= args.alpha;
         double* p;
         if (args.cplx) {
@@ -875,7 +873,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       auto store = [&](int64_t e, double val) {
         if (args.c_f32) {
           float* p = (float*)args.C + e;
-          if (args.beta != 0.0) val = fma(args.beta, widen_f32(*p), val);
+          if (args.beta != 0.0) val = fma(args.beta, (double)*p, val);
           *p = (float)val;
         } else {
           double* p = args.C + e;
@@ -905,7 +903,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         for (int jj = 0; jj < 32; ++jj) {
           const int64_t n = n0 + c0 + jj;
           if (n >= args.N) break;
-          const double x = widen_f32(v[jj]);
+          const double x = (double)__uint_as_float(v[jj]);
           store(off(n), alpha_one ? x : args.alpha * x);
         }
       }

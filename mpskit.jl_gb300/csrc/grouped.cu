@@ -326,7 +326,7 @@ __global__ void gpack_kernel(const GPackTile* __restrict__ tiles, const int32_t*
     const int kp = T.kp0 + kk;
     float v = 0.0f;
     if (i < T.nr && kp < kl && in[kk])
-      v = narrow_f64(src[(int64_t)rdense[T.rp0 + i] * rs + ((int64_t)kdense[k0 + kp] - klo) * ks]);
+      v = (float)src[(int64_t)rdense[T.rp0 + i] * rs + ((int64_t)kdense[k0 + kp] - klo) * ks];
     t[i][kk] = v;
   }
   __syncthreads();
@@ -824,7 +824,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
     const bool copy_f32 = f32 && alpha == 1.0 && beta == 0.0;
     const bool alpha_one = alpha == 1.0, beta_one = beta == 1.0;
     auto loadC = [&](int64_t e) -> double {
-      return f32 ? widen_f32(((const float*)args.C)[e]) : ((const double*)args.C)[e];
+      return f32 ? (double)((const float*)args.C)[e] : ((const double*)args.C)[e];
     };
     auto putC = [&](int64_t e, double v) {
       if (f32) ((float*)args.C)[e] = (float)v;
@@ -870,7 +870,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
 #pragma unroll
             for (int jj = 0; jj < 16; ++jj) {
               co[jj] = __shfl_sync(0xffffffffu, myco, h + jj);
-              val[jj] = widen_f32(v[h + jj]);
+              val[jj] = (double)__uint_as_float(v[h + jj]);
             }
             if (!alpha_one) {
 #pragma unroll
@@ -899,11 +899,16 @@ __global__ void __launch_bounds__(G_THREADS, 1)
           const bool cvalid = nl < nend;
           const int64_t co = cvalid ? args.coloff[nl] : 0;
           if (copy_f32) {
-            // FP32 output that is the accumulator itself: no FP64 arithmetic or conversion
+            // FP32 output that is the accumulator itself: no FP64 arithmetic or conversion.
+            // All 32 values are read from shared memory before the first global store, so the
+            // stores issue back to back.
+            float fv[32];
+#pragma unroll
+            for (int i = 0; i < 32; ++i) fv[i] = xb[i * 33 + lane];
 #pragma unroll
             for (int i = 0; i < 32; ++i) {
               const int64_t r = __shfl_sync(0xffffffffu, roff, i);
-              if (cvalid && mrow0 + i < T.mlim) ((float*)args.C)[r + co] = xb[i * 33 + lane];
+              if (cvalid && mrow0 + i < T.mlim) ((float*)args.C)[r + co] = fv[i];
             }
             __syncwarp();
             return;
@@ -915,7 +920,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
               ro[i] = __shfl_sync(0xffffffffu, roff, h + i);
-              val[i] = widen_f32(xb[(h + i) * 33 + lane]);
+              val[i] = (double)xb[(h + i) * 33 + lane];
             }
             if (!alpha_one) {
 #pragma unroll

@@ -41,69 +41,6 @@ __device__ __forceinline__ void split_put_f(float* hi, float* lo, int64_t i, flo
   hi[i] = h;
   lo[i] = tf32_rna(v - h);
 }
-// FP32 -> FP64 widening from the IEEE-754 bit fields with integer operations only (every
-// float is a double, so the result is exact): the FP64-pipe conversion would make the
-// epilogue of an FP64-output GEMM bound by GB300's small FP64 rate.  Subnormals are
-// normalised with a leading-zero count; infinities keep their sign, NaNs stay NaN.
-__device__ __forceinline__ double widen_f32(uint32_t b) {
-  const uint32_t sign = b & 0x80000000u;
-  const uint32_t e = (b >> 23) & 0xFFu;
-  uint32_t m = b & 0x7FFFFFu;
-  uint32_t hi;
-  if (e == 0xFFu) {
-    hi = sign | 0x7FF00000u | (m >> 3) | (m ? 0x80000u : 0u);
-  } else if (e != 0u) {
-    hi = sign | ((e + 896u) << 20) | (m >> 3);
-  } else if (m == 0u) {
-    hi = sign;
-  } else {
-    const uint32_t sh = (uint32_t)__clz((int)m) - 8u;  // brings the leading one to bit 23
-    m = (m << sh) & 0x7FFFFFu;
-    hi = sign | ((897u - sh) << 20) | (m >> 3);
-  }
-  return __hiloint2double((int)hi, (int)(m << 29));
-}
-__device__ __forceinline__ double widen_f32(float f) { return widen_f32(__float_as_uint(f)); }
-// FP64 -> FP32 rounding to nearest, ties to even, with integer operations only: the same
-// result as the FP64-pipe conversion (the operand packs round every element once).
-__device__ __forceinline__ float narrow_f64(double x) {
-  const uint64_t b = (uint64_t)__double_as_longlong(x);
-  const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
-  const int e = (int)((b >> 52) & 0x7FF);
-  const uint64_t m = b & 0xFFFFFFFFFFFFFull;
-  uint32_t bits;
-  if (e == 0x7FF) {
-    bits = sign | 0x7F800000u | (m ? 0x400000u : 0u);
-  } else if (e == 0) {
-    bits = sign;  // double subnormals lie far below half the smallest float
-  } else {
-    int fe = e - 896;  // float biased exponent
-    if (fe >= 255) {
-      bits = sign | 0x7F800000u;
-    } else {
-      const int shift = fe >= 1 ? 29 : 30 - fe;  // significand bits dropped
-      if (shift > 54) {
-        bits = sign;
-      } else {
-        const uint64_t mant = m | (1ull << 52);
-        uint64_t q = mant >> shift;
-        const uint64_t rem = mant & ((1ull << shift) - 1), half = 1ull << (shift - 1);
-        if (rem > half || (rem == half && (q & 1))) ++q;
-        if (fe >= 1) {
-          if (q >> 24) {
-            q >>= 1;
-            ++fe;
-          }
-          bits = fe >= 255 ? (sign | 0x7F800000u)
-                           : (sign | ((uint32_t)fe << 23) | ((uint32_t)q & 0x7FFFFFu));
-        } else {
-          bits = sign | (uint32_t)q;  // subnormal (rounding up to 2^23 gives the smallest normal)
-        }
-      }
-    }
-  }
-  return __uint_as_float(bits);
-}
 __device__ __forceinline__ bool plane_nz(__nv_bfloat16 a) { return __bfloat162float(a) != 0.f; }
 __device__ __forceinline__ bool plane_nz(float a) { return a != 0.f; }
 inline bool is_tf32(int prec) { return prec == GB_PREC_TF32X3; }
