@@ -926,8 +926,16 @@ def run_vumps_xxz(args):
         env64 = mpsgb.InfiniteEnvironments(psi, H, L.GB_PREC_FP64)
         env64.recalculate(psi, tol=1e-12)
         e = mpsgb.infinite.energy_density(psi, env64)
+        phases = {}
+        for h in hist:
+            for k_, v_ in h["phase_s"].items():
+                phases[k_] = phases.get(k_, 0.0) + v_ / len(hist)
         res[prec] = {"seconds": t, "iterations": len(hist), "s_per_iteration": t / len(hist),
-                     "energy_density": e, "error_vs_exact": e - exact, "galerkin_eps": eps}
+                     "energy_density": e, "error_vs_exact": e - exact, "galerkin_eps": eps,
+                     "phase_s_per_iteration": phases,
+                     "matvecs_per_iteration": {
+                         "ac": sum(h["matvecs"]["ac"] for h in hist) / len(hist),
+                         "c": sum(h["matvecs"]["c"] for h in hist) / len(hist)}}
         log(f"vumps xxz {prec}: {t:.2f} s, {len(hist)} iterations, e = {e:.12f} "
             f"(exact {exact:.12f}), eps = {eps:.2e}")
     line = {

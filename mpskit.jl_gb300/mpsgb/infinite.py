@@ -14,6 +14,7 @@ iterations use the reference's acceleration (gauge_eigsolve_step!, ortho.jl:258-
 mixed transfer map before the QR/LQ step.
 """
 import ctypes
+import time
 
 import numpy as np
 
@@ -390,19 +391,31 @@ def find_groundstate_vumps(psi, H, alg, envs=None):
     eps = galerkin(psi, envs, alg.backend)
     envs.recalculate(psi, tol=_dyn_tol(eps, it, 1e-4))
     hist = []
+    clock = time.perf_counter
     while True:
+        # phase wall times (every phase ends on a host read of a device result)
+        t0 = clock()
         et = _dyn_tol(eps, it, 1e-3)
         solver = Lanczos(krylovdim=30, maxiter=200, tol=et, eager=True)
-        _, AC, _ = fixedpoint(_heff_ac(envs, alg.backend), psi.AC, "SR", solver)
-        _, C, _ = fixedpoint(_heff_c(envs, alg.backend), psi.C, "SR", solver)
+        _, AC, iac = fixedpoint(_heff_ac(envs, alg.backend), psi.AC, "SR", solver)
+        t1 = clock()
+        _, C, ic = fixedpoint(_heff_c(envs, alg.backend), psi.C, "SR", solver)
+        t2 = clock()
         AL = regauge(AC, C)
         AR, C = uniform_rightorth(AL, psi.C, tol=_dyn_tol(eps, it, 1e-6))
         psi = InfiniteMPS(AL, AR, C)
+        t3 = clock()
         envs.recalculate(psi, tol=_dyn_tol(eps, it, 1e-4))
+        t4 = clock()
         eps = galerkin(psi, envs, alg.backend)
         it += 1
         e = energy_density(psi, envs, alg.backend)
-        hist.append({"iter": it, "energy": e, "eps": eps})
+        t5 = clock()
+        hist.append({"iter": it, "energy": e, "eps": eps,
+                     "phase_s": {"ac_eigsolve": t1 - t0, "c_eigsolve": t2 - t1,
+                                 "gauge": t3 - t2, "environments": t4 - t3,
+                                 "galerkin_energy": t5 - t4},
+                     "matvecs": {"ac": iac.numops, "c": ic.numops}})
         if alg.verbosity:
             print(f"VUMPS {it}: e = {e:.14f}  eps = {eps:.3e}")
         if eps <= alg.tol or it >= alg.maxiter:
