@@ -59,6 +59,7 @@ enum ScratchSlot {
   SLOT_GAUGE3,
   SLOT_TMP,       // short-lived helper buffers
   SLOT_TMP2,
+  SLOT_SPLITK,    // split-K partial products of the FP64 GEMM
   SLOT_COUNT
 };
 

@@ -291,25 +291,33 @@ __global__ void __launch_bounds__(256)
                      const T* __restrict__ A, int64_t lda, int64_t sA, const T* __restrict__ B,
                      int64_t ldb, int64_t sB, T beta, bool use_beta, T* __restrict__ C,
                      int64_t ldc, int64_t sC, const uint32_t* __restrict__ mA,
-                     const uint32_t* __restrict__ mB, int kw, int64_t mAb, int64_t mBb) {
+                     const uint32_t* __restrict__ mB, int kw, int64_t mAb, int64_t mBb,
+                     int64_t kchunk) {
   __shared__ T As[GBK][GBM + 1];
   __shared__ T Bs[GBK][GBN + 1];
+  // kchunk > 0: split K (batch 1): slice z covers k in [z kchunk, (z + 1) kchunk) and writes
+  // its partial product to C + z sC (no beta); the slices are summed by a reduction kernel
   const int64_t bz = blockIdx.z;
-  A += bz * sA;
-  B += bz * sB;
+  const int64_t kbeg = kchunk ? bz * kchunk : 0;
+  const int64_t kend = kchunk ? min(K, kbeg + kchunk) : K;
+  if (!kchunk) {
+    A += bz * sA;
+    B += bz * sB;
+  }
   C += bz * sC;
   const int64_t m0 = (int64_t)blockIdx.x * GBM, n0 = (int64_t)blockIdx.y * GBN;
   const int tid = threadIdx.x;
   const int tm = (tid % 16) * 4, tn = (tid / 16) * 4;
   // zero-tile skipping: 64-wide k-blocks in which this A row tile or B column tile is zero
-  const uint32_t* ma = mA ? mA + (sA ? bz : 0) * mAb + (int64_t)blockIdx.x * kw : nullptr;
-  const uint32_t* mb = mB ? mB + (sB ? bz : 0) * mBb + (int64_t)blockIdx.y * kw : nullptr;
+  const int64_t bm = kchunk ? 0 : bz;
+  const uint32_t* ma = mA ? mA + (sA ? bm : 0) * mAb + (int64_t)blockIdx.x * kw : nullptr;
+  const uint32_t* mb = mB ? mB + (sB ? bm : 0) * mBb + (int64_t)blockIdx.y * kw : nullptr;
   T acc[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j] = Ops<T>::zero();
-  for (int64_t k0 = 0; k0 < K; k0 += GBK) {
+  for (int64_t k0 = kbeg; k0 < kend; k0 += GBK) {
     if (ma) {
       const int64_t kb = k0 / 64;
       if (!((ma[kb / 32] & mb[kb / 32]) >> (kb % 32) & 1u)) {
@@ -329,7 +337,7 @@ __global__ void __launch_bounds__(256)
         c = e % GBK;
         r = e / GBK;
       }
-      As[c][r] = load_op(A, lda, opA, m0 + r, k0 + c, M, K);
+      As[c][r] = load_op(A, lda, opA, m0 + r, k0 + c, M, kend);
     }
 #pragma unroll
     for (int l = 0; l < 4; ++l) {
@@ -342,7 +350,7 @@ __global__ void __launch_bounds__(256)
         c = e % GBN;
         r = e / GBN;
       }
-      Bs[r][c] = load_op(B, ldb, opB, k0 + r, n0 + c, K, N);
+      Bs[r][c] = load_op(B, ldb, opB, k0 + r, n0 + c, kend, N);
     }
     __syncthreads();
 #pragma unroll
@@ -371,6 +379,21 @@ __global__ void __launch_bounds__(256)
       if (use_beta) v = Ops<T>::fmaop(beta, C[m + ldc * n], v);
       C[m + ldc * n] = v;
     }
+  }
+}
+
+// C = beta C + sum_z W[z] over the split-K slices, summed in slice order (deterministic)
+template <typename T>
+__global__ void splitk_reduce_kernel(int64_t M, int64_t N, int nsplit, const T* __restrict__ W,
+                                     T beta, bool use_beta, T* __restrict__ C, int64_t ldc) {
+  const int64_t MN = M * N;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < MN;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    T v = W[e];
+    for (int z = 1; z < nsplit; ++z) v = Ops<T>::add(v, W[(int64_t)z * MN + e]);
+    const int64_t m = e % M, n = e / M;
+    if (use_beta) v = Ops<T>::fmaop(beta, C[m + ldc * n], v);
+    C[m + ldc * n] = v;
   }
 }
 
@@ -425,17 +448,50 @@ void gemm_fp64(gb_ctx* ctx, int dtype, char opA, char opB, int64_t M, int64_t N,
   }
   const uint32_t* mA_ = masks;
   const uint32_t* mB_ = masks ? masks + bA * mt * kw : nullptr;
-  if (is_cplx(dtype)) {
+  // a grid that fills less than half the GPU splits K over more CTAs (FP64 runs at a few
+  // operations per clock per SM on GB300: every SM has to take part); slices of at least 128
+  // (a multiple of the 64-wide zero-block granularity), summed in order by a second kernel
+  int nsplit = 1;
+  const int64_t tiles = mt * nt;
+  if (batch == 1 && ctx->num_sms > 0 && tiles * 2 <= ctx->num_sms && K >= 256) {
+    nsplit = (int)std::min<int64_t>({(int64_t)ctx->num_sms / tiles, K / 128, 16});
+    if (nsplit < 2) nsplit = 1;
+  }
+  const size_t es = elem_size(dtype);
+  if (nsplit > 1) {
+    const int64_t kchunk = ((K + nsplit - 1) / nsplit + 63) / 64 * 64;
+    nsplit = (int)((K + kchunk - 1) / kchunk);
+    void* W = scratch(ctx, SLOT_SPLITK, (size_t)nsplit * M * N * es);
+    dim3 gs(grid.x, grid.y, (unsigned)nsplit);
+    const unsigned rb = (unsigned)std::min<int64_t>((M * N + 255) / 256, 4096);
+    if (is_cplx(dtype)) {
+      gemm_simt_kernel<dcx><<<gs, 256, 0, ctx->stream>>>(
+          opA, opB, M, N, K, mk(alpha.re, alpha.im), (const dcx*)A, lda, 0, (const dcx*)B, ldb,
+          0, mk(0.0, 0.0), false, (dcx*)W, M, M * N, mA_, mB_, kw, mt * kw, nt * kw, kchunk);
+      splitk_reduce_kernel<dcx><<<rb, 256, 0, ctx->stream>>>(
+          M, N, nsplit, (const dcx*)W, mk(beta.re, beta.im), use_beta, (dcx*)C, ldc);
+    } else {
+      gemm_simt_kernel<double><<<gs, 256, 0, ctx->stream>>>(
+          opA, opB, M, N, K, alpha.re, (const double*)A, lda, 0, (const double*)B, ldb, 0, 0.0,
+          false, (double*)W, M, M * N, mA_, mB_, kw, mt * kw, nt * kw, kchunk);
+      splitk_reduce_kernel<double><<<rb, 256, 0, ctx->stream>>>(
+          M, N, nsplit, (const double*)W, beta.re, use_beta, (double*)C, ldc);
+    }
+    LAUNCH_CHECK();
+    count_launch_n(ctx, 2);
+  } else if (is_cplx(dtype)) {
     gemm_simt_kernel<dcx><<<grid, 256, 0, ctx->stream>>>(
         opA, opB, M, N, K, mk(alpha.re, alpha.im), (const dcx*)A, lda, sA, (const dcx*)B, ldb,
-        sB, mk(beta.re, beta.im), use_beta, (dcx*)C, ldc, sC, mA_, mB_, kw, mt * kw, nt * kw);
+        sB, mk(beta.re, beta.im), use_beta, (dcx*)C, ldc, sC, mA_, mB_, kw, mt * kw, nt * kw, 0);
+    LAUNCH_CHECK();
+    count_launch(ctx);
   } else {
     gemm_simt_kernel<double><<<grid, 256, 0, ctx->stream>>>(
         opA, opB, M, N, K, alpha.re, (const double*)A, lda, sA, (const double*)B, ldb, sB,
-        beta.re, use_beta, (double*)C, ldc, sC, mA_, mB_, kw, mt * kw, nt * kw);
+        beta.re, use_beta, (double*)C, ldc, sC, mA_, mB_, kw, mt * kw, nt * kw, 0);
+    LAUNCH_CHECK();
+    count_launch(ctx);
   }
-  LAUNCH_CHECK();
-  count_launch(ctx);
   if (masks) GB_CHECK_CUDA(cudaFreeAsync(masks, ctx->stream));
 }
 
@@ -451,12 +507,12 @@ cudaError_t gemm_fp64_on_stream(cudaStream_t stream, int dtype, char opA, char o
   if (is_cplx(dtype)) {
     gemm_simt_kernel<dcx><<<grid, 256, 0, stream>>>(
         opA, opB, M, N, K, mk(alpha.re, alpha.im), (const dcx*)A, lda, 0, (const dcx*)B, ldb, 0,
-        mk(beta.re, beta.im), use_beta, (dcx*)C, ldc, 0, nullptr, nullptr, 0, 0, 0);
+        mk(beta.re, beta.im), use_beta, (dcx*)C, ldc, 0, nullptr, nullptr, 0, 0, 0, 0);
   } else {
     gemm_simt_kernel<double><<<grid, 256, 0, stream>>>(opA, opB, M, N, K, alpha.re,
                                                        (const double*)A, lda, 0, (const double*)B,
                                                        ldb, 0, beta.re, use_beta, (double*)C, ldc, 0,
-                                                       nullptr, nullptr, 0, 0, 0);
+                                                       nullptr, nullptr, 0, 0, 0, 0);
   }
   return cudaGetLastError();
 }
