@@ -297,6 +297,20 @@ int gb_project_complement(gb_ctx* ctx, gb_tensor* Y, const gb_tensor* X);
  * src/algorithms/changebonds/optimalexpand.jl:122-135, 148-161) without forming the null
  * spaces: the right singular vectors of the projected Y are Vh * NR. */
 int gb_project_complement_right(gb_ctx* ctx, gb_tensor* Y, const gb_tensor* X);
+/* Krylov-basis helpers for host-driven Krylov loops over operators that have no device solver
+ * of their own (the Arnoldi of uniform_leftorth!/uniform_rightorth!, src/states/ortho.jl:
+ * 254-263, 315-324, which KrylovKit runs with the basis in memory): `basis` is a
+ * GB_KIND_GENERIC tensor (n, kmax) whose column j holds a vector of n elements.
+ *   gb_basis_set:           column j <- v
+ *   gb_basis_orthogonalize: w <- w - sum_j <v_j, w> v_j over columns 0..k-1, classical
+ *                           Gram-Schmidt in two passes; h[2j], h[2j+1] = the projection
+ *                           (re, im) summed over both passes
+ *   gb_basis_combine:       out <- sum_j coef[j] v_j (coef as re, im pairs) */
+int gb_basis_set(gb_ctx* ctx, gb_tensor* basis, int64_t j, const gb_tensor* v);
+int gb_basis_orthogonalize(gb_ctx* ctx, const gb_tensor* basis, int64_t k, gb_tensor* w,
+                           double* h);
+int gb_basis_combine(gb_ctx* ctx, const gb_tensor* basis, int64_t k, const double* coef,
+                     gb_tensor* out);
 /* contract_mpo_expval-style scalar <x|y> after a heff apply is gb_tensor_dot. */
 
 /* ---------------------------------------------------------------- projections */

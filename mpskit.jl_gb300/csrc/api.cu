@@ -1263,6 +1263,75 @@ int gb_tensor_copy(gb_tensor* dst, const gb_tensor* src) {
   API_END
 }
 
+// ---------------------------------------------------------------- Krylov basis helpers
+// A basis is a GB_KIND_GENERIC tensor (n, kmax): column j holds a vector of n elements.  Used
+// by host-driven Krylov loops over operators without a device solver of their own (the
+// Arnoldi of the uniform gauge), so that one orthogonalisation is two passes of batched
+// dot products and updates instead of one host round trip per basis vector.
+static void basis_check(const gb_tensor* basis, const gb_tensor* v, int64_t j) {
+  GB_REQUIRE(basis && v, "null tensor");
+  GB_REQUIRE(basis->kind == GB_KIND_GENERIC && basis->ndim == 2, "basis: a 2-leg generic tensor");
+  GB_REQUIRE(basis->dtype == v->dtype, "basis: dtypes");
+  GB_REQUIRE(!needs_permute(v->kind), "basis: vectors in reference leg order only");
+  GB_REQUIRE(numel(v) == basis->dims[0], "basis: vector length");
+  GB_REQUIRE(j >= 0 && j <= basis->dims[1], "basis: column index");
+}
+
+int gb_basis_set(gb_ctx* ctx, gb_tensor* basis, int64_t j, const gb_tensor* v) {
+  API_BEGIN
+  check_ctx(basis, ctx);
+  check_ctx(v, ctx);
+  basis_check(basis, v, j);
+  GB_REQUIRE(j < basis->dims[1], "basis: column index");
+  DevGuard g(ctx->device);
+  const size_t bytes = (size_t)basis->dims[0] * elem_size(v->dtype);
+  GB_CHECK_CUDA(cudaMemcpyAsync((char*)basis->data + (size_t)j * bytes, v->data, bytes,
+                                cudaMemcpyDeviceToDevice, ctx->stream));
+  API_END
+}
+
+int gb_basis_orthogonalize(gb_ctx* ctx, const gb_tensor* basis, int64_t k, gb_tensor* w,
+                           double* h) {
+  API_BEGIN
+  check_ctx(basis, ctx);
+  check_ctx(w, ctx);
+  basis_check(basis, w, k);
+  GB_REQUIRE(h || k == 0, "null output");
+  DevGuard g(ctx->device);
+  const int dt = w->dtype;
+  const int64_t n = basis->dims[0];
+  // classical Gram-Schmidt, two passes; h = the sum of both passes' projections
+  std::vector<cplx> c1(k), c2(k), neg(k);
+  for (int pass = 0; pass < 2; ++pass) {
+    std::vector<cplx>& c = pass ? c2 : c1;
+    multi_dot(ctx, dt, n, (int)k, basis->data, n, w->data, c.data());
+    for (int64_t j = 0; j < k; ++j) neg[j] = cplx{-c[j].re, -c[j].im};
+    multi_axpy(ctx, dt, n, (int)k, basis->data, n, neg.data(), w->data);
+  }
+  for (int64_t j = 0; j < k; ++j) {
+    h[2 * j] = c1[j].re + c2[j].re;
+    h[2 * j + 1] = c1[j].im + c2[j].im;
+  }
+  API_END
+}
+
+int gb_basis_combine(gb_ctx* ctx, const gb_tensor* basis, int64_t k, const double* coef,
+                     gb_tensor* out) {
+  API_BEGIN
+  check_ctx(basis, ctx);
+  check_ctx(out, ctx);
+  basis_check(basis, out, k);
+  GB_REQUIRE(coef || k == 0, "null coefficients");
+  DevGuard g(ctx->device);
+  std::vector<cplx> c(k);
+  const bool cx = is_cplx(out->dtype);
+  for (int64_t j = 0; j < k; ++j) c[j] = cplx{coef[2 * j], cx ? coef[2 * j + 1] : 0.0};
+  fill_zero(ctx, out->data, out->bytes);
+  multi_axpy(ctx, out->dtype, basis->dims[0], (int)k, basis->data, basis->dims[0], c.data(),
+             out->data);
+  API_END
+}
+
 int gb_tensor_scale(gb_tensor* t, double re, double im) {
   API_BEGIN
   GB_REQUIRE(t, "null tensor");

@@ -119,6 +119,9 @@ _SIGS = {
     "gb_mps_mul_tail": ([P, P, P, P], INT),
     "gb_project_complement": ([P, P, P], INT),
     "gb_project_complement_right": ([P, P, P], INT),
+    "gb_basis_set": ([P, P, I64, P], INT),
+    "gb_basis_orthogonalize": ([P, P, I64, P, ctypes.POINTER(ctypes.c_double)], INT),
+    "gb_basis_combine": ([P, P, I64, ctypes.POINTER(ctypes.c_double), P], INT),
     "gb_heff_describe": ([P, ctypes.c_char_p, ctypes.c_size_t], INT),
     "gb_ctx_set_gauge": ([P, INT, INT], INT),
     "gb_ctx_set_option": ([P, INT, ctypes.c_int64], INT),

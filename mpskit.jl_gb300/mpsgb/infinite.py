@@ -107,20 +107,25 @@ def _transfer_bond(side, A, B, X):
 
 def _arnoldi_dominant(op, x0, tol, krylovdim=30, maxiter=200):
     """Eigenvector of the largest-magnitude eigenvalue of `op` (KrylovKit Arnoldi, :LM, eager;
-    explicit restarts from the Ritz vector), device vectors, Hessenberg on the host."""
+    explicit restarts from the Ritz vector).  The basis lives in one device tensor and every
+    new vector is orthogonalised against it by two batched Gram-Schmidt passes
+    (gb_basis_orthogonalize); the Hessenberg matrix and its eigenproblem stay on the host."""
     real = x0.dtype.kind != "c"
+    ctx = x0.ctx
+    n = int(np.prod(x0.dims))
+    basis = DeviceTensor(ctx, L.GB_KIND_GENERIC, x0.dtype, (n, krylovdim + 1))
+    h = np.zeros(2 * (krylovdim + 1))
+    hp = h.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
     x = x0.copy().normalize_()
     for _ in range(maxiter):
-        V = [x]
+        L.check(L.lib().gb_basis_set(ctx.handle, basis.handle, 0, x.handle))
         Hm = np.zeros((krylovdim + 1, krylovdim), dtype=np.complex128)
         y = np.ones(1)
+        v = x
         for j in range(krylovdim):
-            w = op(V[j])
-            for _pass in range(2):
-                for i in range(j + 1):
-                    h = V[i].dot(w)
-                    Hm[i, j] += h
-                    w.axpy_(-h, V[i])
+            w = op(v)
+            L.check(L.lib().gb_basis_orthogonalize(ctx.handle, basis.handle, j + 1, w.handle, hp))
+            Hm[:j + 1, j] = h[0:2 * (j + 1):2] + 1j * h[1:2 * (j + 1):2]
             hn = w.norm()
             Hm[j + 1, j] = hn
             k = j + 1
@@ -131,13 +136,17 @@ def _arnoldi_dominant(op, x0, tol, krylovdim=30, maxiter=200):
             breakdown = hn <= 1e-14 * max(1.0, np.linalg.norm(Hm[:k, :k]))
             if abs(hn * y[-1]) <= tol or breakdown:
                 break
-            V.append(w.scale_(1.0 / hn))
+            v = w.scale_(1.0 / hn)
+            L.check(L.lib().gb_basis_set(ctx.handle, basis.handle, k, v.handle))
         if real:
             y = y.real * np.sign(y.real[np.argmax(np.abs(y.real))])
-        x = V[0].similar()
-        L.check(L.lib().gb_tensor_scale(x.handle, 0.0, 0.0))
-        for i in range(len(y)):
-            x.axpy_(complex(y[i]) if not real else float(y[i]), V[i])
+        c = np.zeros(2 * len(y))
+        c[0::2] = np.real(y)
+        c[1::2] = 0.0 if real else np.imag(y)
+        x = x0.similar()
+        L.check(L.lib().gb_basis_combine(ctx.handle, basis.handle, len(y),
+                                         c.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                         x.handle))
         x.normalize_()
         if abs(hn * y[-1]) <= tol or breakdown:
             break
