@@ -387,6 +387,14 @@ int gb_ctx_set_option(gb_ctx* ctx, int option, int64_t value);
  * AR[k s2; r].  Returns the discarded-weight norm eps.  Outputs are newly created. */
 int gb_svd_trunc(gb_ctx* ctx, const gb_tensor* AC2, int64_t maxdim, double atol,
                  int normalize, gb_tensor** AL, gb_tensor** S, gb_tensor** AR, double* eps);
+/* Compact SVDs of `count` independent matrices at once (svd_compact, the factorisations of
+ * GradientGrassmann's retraction and preconditioner, src/algorithms/grassmann.jl:93-122,
+ * 243-255): M[i] an MPS tensor (Dl, d, Dr) read as (Dl d) x Dr, or a bond tensor; rows >=
+ * columns.  Outputs created: U[i] (the input's kind, last leg of size Dr), Vh[i] (Dr x Dr
+ * bond), and the singular values, descending, concatenated into the host array S (sum of
+ * the Dr).  The factorisations run on the context's lanes (cuSOLVER gesvd). */
+int gb_svd_batch(gb_ctx* ctx, int64_t count, const gb_tensor* const* M, gb_tensor** U,
+                 gb_tensor** Vh, double* S);
 /* left_gauge(AC) with Householder(positive = true): AC = AL * C
  * (src/states/orthoview.jl:322-326); outputs created. */
 int gb_left_orth(gb_ctx* ctx, const gb_tensor* AC, gb_tensor** AL, gb_tensor** C);

@@ -5,6 +5,7 @@
 #include <cusolverDn.h>
 
 #include <algorithm>
+#include <numeric>
 #include <atomic>
 #include <cmath>
 #include <condition_variable>
@@ -2019,6 +2020,86 @@ int gb_svd_trunc(gb_ctx* ctx, const gb_tensor* AC2, int64_t maxdim, double atol,
   *AL = al;
   *AR = ar;
   *S = sc;
+  API_END
+}
+
+// stream-ordered device buffer of a (lane) context
+struct StreamBuf {
+  gb_ctx* ctx;
+  void* p = nullptr;
+  StreamBuf(gb_ctx* c, size_t bytes) : ctx(c) {
+    GB_CHECK_CUDA(cudaMallocAsync(&p, bytes, c->stream));
+  }
+  ~StreamBuf() {
+    if (p) cudaFreeAsync(p, ctx->stream);
+  }
+  StreamBuf(const StreamBuf&) = delete;
+  StreamBuf& operator=(const StreamBuf&) = delete;
+};
+
+int gb_svd_batch(gb_ctx* ctx, int64_t count, const gb_tensor* const* M, gb_tensor** U,
+                 gb_tensor** Vh, double* S) {
+  API_BEGIN
+  GB_REQUIRE(count >= 0 && (count == 0 || (M && U && Vh && S)), "null argument");
+  DevGuard g(ctx->device);
+  struct Item {
+    int64_t m, n;
+    size_t soff;
+  };
+  std::vector<Item> it(count);
+  size_t stot = 0;
+  for (int64_t i = 0; i < count; ++i) {
+    const gb_tensor* t = M[i];
+    GB_REQUIRE(t, "null tensor");
+    check_ctx(t, ctx);
+    GB_REQUIRE(t->kind == GB_KIND_MPS || t->kind == GB_KIND_BOND, "svd_batch: MPS or bond tensors");
+    const int64_t n = t->dims[t->ndim - 1], m = numel(t) / std::max<int64_t>(n, 1);
+    GB_REQUIRE(m >= n && n > 0, "svd_batch: each matrix must have at least as many rows as columns");
+    it[i] = Item{m, n, stot};
+    stot += (size_t)n;
+    U[i] = Vh[i] = nullptr;
+  }
+  try {
+    for (int64_t i = 0; i < count; ++i) {
+      const gb_tensor* t = M[i];
+      if (t->kind == GB_KIND_MPS) {
+        int64_t du[3] = {t->dims[0], t->dims[1], it[i].n};
+        U[i] = new_tensor(ctx, GB_KIND_MPS, t->dtype, 3, du);
+      } else {
+        int64_t du[2] = {it[i].m, it[i].n};
+        U[i] = new_tensor(ctx, GB_KIND_BOND, t->dtype, 2, du);
+      }
+      int64_t dv[2] = {it[i].n, it[i].n};
+      Vh[i] = new_tensor(ctx, GB_KIND_BOND, t->dtype, 2, dv);
+    }
+    StreamBuf sdev(ctx, stot * sizeof(double) + 256);
+    GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+    // one factorisation per lane at a time, largest first
+    std::vector<int64_t> order(count);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
+      return it[a].m * it[a].n * it[a].n > it[b].m * it[b].n * it[b].n;
+    });
+    run_on_lanes(ctx, count, [&](gb_ctx* L, int64_t oi) {
+      const int64_t i = order[oi];
+      const gb_tensor* t = M[i];
+      StreamBuf A(L, (size_t)it[i].m * it[i].n * elem_size(t->dtype) + 256);
+      GB_CHECK_CUDA(cudaMemcpyAsync(A.p, t->data, t->bytes, cudaMemcpyDeviceToDevice, L->stream));
+      svd_tall(L, t->dtype, it[i].m, it[i].n, A.p, U[i]->data, (double*)sdev.p + it[i].soff,
+               Vh[i]->data);
+      GB_CHECK_CUDA(cudaStreamSynchronize(L->stream));
+    });
+    GB_CHECK_CUDA(cudaMemcpyAsync(S, sdev.p, stot * sizeof(double), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+  } catch (...) {
+    for (int64_t i = 0; i < count; ++i) {
+      if (U[i]) free_tensor(U[i]);
+      if (Vh[i]) free_tensor(Vh[i]);
+      U[i] = Vh[i] = nullptr;
+    }
+    throw;
+  }
   API_END
 }
 

@@ -23,6 +23,7 @@ Every tensor operation runs in libmpsgb (gemm-backed MPS products, the positive 
 gauge, the cuSOLVER SVD of the tangent and bond matrices, the Jordan AC derivative); the
 host keeps only scalars and the singular values that scale the bond directions.
 """
+import ctypes
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -61,6 +62,35 @@ def _svd(M, dims):
     return U, s, Vb
 
 
+def _svd_batch(ts):
+    """Compact SVDs of several tall device matrices in one call (gb_svd_batch, on the
+    context's lanes): [(U, s, Vh)] with U of each input's kind, s on the host, Vh a bond."""
+    if not ts:
+        return []
+    ctx = ts[0].ctx
+    n = len(ts)
+    hv = lambda h: h.value if isinstance(h, ctypes.c_void_p) else h
+    arr = (ctypes.c_void_p * n)(*[hv(t.handle) for t in ts])
+    U, V = (ctypes.c_void_p * n)(), (ctypes.c_void_p * n)()
+    S = np.zeros(sum(t.dims[-1] for t in ts))
+    L.check(L.lib().gb_svd_batch(ctx.handle, n, arr, U, V,
+                                 S.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+    out, off = [], 0
+    for i, t in enumerate(ts):
+        k = t.dims[-1]
+        out.append((DeviceTensor.wrap(ctx, ctypes.c_void_p(U[i])), S[off:off + k].copy(),
+                    DeviceTensor.wrap(ctx, ctypes.c_void_p(V[i]))))
+        off += k
+    return out
+
+
+def _fill_svds(tangents):
+    """Factorise every tangent whose SVD is not cached yet, all in one batch."""
+    todo = [t for t in tangents if t._svd is None]
+    for t, r in zip(todo, _svd_batch([t.Z for t in todo])):
+        t._svd = r
+
+
 def _bond_as_mps(C):
     return C.copy().reshape_(L.GB_KIND_MPS, (C.dims[0], 1, C.dims[1]))
 
@@ -93,7 +123,7 @@ class GrassmannTangent:
 
     def svd(self):
         if self._svd is None:
-            self._svd = _svd(self.Z, self.Z.dims)
+            self._svd = _svd_batch([self.Z])[0]
         return self._svd
 
     def norm(self):
@@ -161,15 +191,16 @@ def transport_site(Th, W, D, a, Wn):
     return GrassmannTangent(Wn, project_complement_(Z, Wn))
 
 
-def rho_inv_regularized(C, rtol):
+def rho_inv_regularized(C, rtol, svd=None):
     """U (S^2 + delta^2)^-1 U' with C = U S V' and delta = rtol * max(S) (Tikhonov
-    regularised inverse of rho = C C', grassmann.jl:243-255)."""
+    regularised inverse of rho = C C', grassmann.jl:243-255); `svd` = (U, s, Vh) of C when
+    already computed."""
     ctx, dt = C.ctx, C.dtype
-    U, s, _ = _svd(_bond_as_mps(C), (C.dims[0], 1, C.dims[1]))
+    U, s, _ = svd if svd is not None else _svd_batch([C])[0]
     d2 = (rtol * (s.max() if s.size else 0.0)) ** 2
-    Ub = _mps_as_bond(U)
-    return _mps_as_bond(mul_tail(mul_tail(U, _diag(ctx, 1.0 / (s * s + d2), dt)),
-                                 adjoint(Ub)))
+    Um = _bond_as_mps(U)
+    return _mps_as_bond(mul_tail(mul_tail(Um, _diag(ctx, 1.0 / (s * s + d2), dt)),
+                                 adjoint(U)))
 
 
 # ------------------------------------------------------------------ points
@@ -218,16 +249,19 @@ def precondition(x, g):
     """g_i -> g_i rho_i^-1 with rho = C C' Tikhonov-regularised at
     max(eps^(3/4), |g_i|) (grassmann.jl:73-91)."""
     rtolmin = np.finfo(np.float64).eps ** 0.75
+    svds = _svd_batch([x.C_right(i) for i in range(len(g))])
     out = []
     for i, gi in enumerate(g):
         rtol = max(rtolmin, gi.norm())
-        out.append(GrassmannTangent(gi.W, mul_tail(gi.Z, rho_inv_regularized(x.C_right(i), rtol))))
+        rho = rho_inv_regularized(x.C_right(i), rtol, svds[i])
+        out.append(GrassmannTangent(gi.W, mul_tail(gi.Z, rho)))
     return out
 
 
 def retract(x, g, a):
     """retract(state::FiniteMPS, g, a) (grassmann.jl:93-108): every AL[i] along its
     geodesic; the new state keeps the old norm factor of the last bond, normalised."""
+    _fill_svds(g)
     res = [retract_site(x.AL[i], g[i], a) for i in range(len(x))]
     Cend = x.psi.C[len(x)].copy().normalize_()
     return GrassmannPoint([r[0] for r in res], Cend), [r[1] for r in res]
@@ -235,6 +269,7 @@ def retract(x, g, a):
 
 def transport(h, x, g, a, xn):
     """transport!(h, state, g, a, state') (grassmann.jl:124-136)."""
+    _fill_svds(g)
     return [transport_site(h[i], x.AL[i], g[i], a, xn.AL[i]) for i in range(len(x))]
 
 
