@@ -1019,12 +1019,17 @@ def run_grassmann(args):
         oH = M.finite_mpo_hamiltonian(L_, 2, M.tfim_terms(L_, g=gx))
         AL = [a_.numpy() for a_ in x.AL]
         Cend = x.psi.C[L_].numpy()
-        t2 = time.perf_counter()
+        od = [t_.Z.numpy() for t_ in d]
         of, og = OG.fg(AL, Cend, oH)
+        t2 = time.perf_counter()
+        ALn, Cn, _ = OG.retract(AL, Cend, od, a)
+        of2, og2 = OG.fg(ALn, Cn, oH)
+        OG.precondition(ALn, Cn, og2)
         tc = time.perf_counter() - t2
         cpu = {"value": tc, "unit": "s/fg", "cores": os.cpu_count(), "kind": "port",
-               "sample": "one oracle fg (environments, energy, 64 AC projections) at the "
-                         "device's first point; numpy/BLAS",
+               "sample": "one oracle line-search point (retract of the 64 sites, fg: "
+                         "environments, energy, 64 AC projections; precondition) from the "
+                         "device's first point along the same direction; numpy/BLAS",
                "energy_difference": abs(of - f)}
     line = {
         "metric": ("GradientGrassmann s per line-search point (retract + fg + precondition), "
