@@ -805,6 +805,7 @@ void run_on_lanes_at(gb_ctx* ctx, int64_t n, const char* file, int line,
     gb_ctx* l = nullptr;
     const int rc = gb_ctx_create(ctx->device, 0, &l);
     if (rc != GB_OK) throw Error(rc, "lane context: " + std::string(gb_last_error()));
+    l->lane = true;
     ctx->lanes.push_back(l);
   }
   std::vector<int64_t> before(K);

@@ -81,6 +81,7 @@ struct gb_ctx {
   double* h_pinned = nullptr;    // small pinned host buffer for scalar readback
   size_t h_pinned_elems = 0;
   int num_sms = 0;
+  bool lane = false;             // an auxiliary lane context (its GPU is shared with the others)
   int aux_prec = GB_PREC_FP64;   // precision of auxiliary state contractions
   int svd_method = 0;            // GB_SVD_* of gb_svd_trunc
   int eig_method = 0;            // GB_EIG_* of the Gram eigenproblems

@@ -450,10 +450,11 @@ void gemm_fp64(gb_ctx* ctx, int dtype, char opA, char opB, int64_t M, int64_t N,
   const uint32_t* mB_ = masks ? masks + bA * mt * kw : nullptr;
   // a grid that fills less than half the GPU splits K over more CTAs (FP64 runs at a few
   // operations per clock per SM on GB300: every SM has to take part); slices of at least 128
-  // (a multiple of the 64-wide zero-block granularity), summed in order by a second kernel
+  // (a multiple of the 64-wide zero-block granularity), summed in order by a second kernel.
+  // Not on lane contexts: their GEMMs run concurrently and fill the GPU together.
   int nsplit = 1;
   const int64_t tiles = mt * nt;
-  if (batch == 1 && ctx->num_sms > 0 && tiles * 2 <= ctx->num_sms && K >= 256) {
+  if (batch == 1 && !ctx->lane && ctx->num_sms > 0 && tiles * 2 <= ctx->num_sms && K >= 256) {
     nsplit = (int)std::min<int64_t>({(int64_t)ctx->num_sms / tiles, K / 128, 16});
     if (nsplit < 2) nsplit = 1;
   }
