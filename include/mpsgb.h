@@ -344,6 +344,11 @@ int gb_mps_perturb(gb_ctx* ctx, int side, const gb_tensor* env, const gb_tensor*
  * appends zeros (zeros(T, Vpert <- domain(B)), dmrg3s.jl:153).  The other legs must agree;
  * out (caller-created) has the summed dimension. */
 int gb_mps_cat(gb_ctx* ctx, const gb_tensor* A, const gb_tensor* B, int leg, gb_tensor* out);
+/* out = A with its left (leg 0) or right (leg 2) bond index permuted: out[i] = A[perm[i]]
+ * along that leg (perm: host array of the leg's length).  Used to keep a U(1) bond sorted by
+ * charge after directions are appended to it (catdomain / catcodomain of charged spaces). */
+int gb_mps_permute(gb_ctx* ctx, const gb_tensor* A, int leg, const int64_t* perm,
+                   gb_tensor* out);
 /* Relabel the kind and shape of an MPS, two-site, bond or generic tensor without moving
  * data: the new shape reads the same device storage in its own device order (MPS (l, s, r),
  * two-site (l, s1, s2, r), bond (l, r)).  E.g. an MPS tensor (l, s, r) is the two-site tensor

@@ -1690,6 +1690,53 @@ int gb_mps_cat(gb_ctx* ctx, const gb_tensor* A, const gb_tensor* B, int leg, gb_
   API_END
 }
 
+// out(i, s, r) = A(perm[i], s, r) (leg 0) or out(l, s, i) = A(l, s, perm[i]) (leg 2); element
+// words of 8 bytes (a complex element is two)
+__global__ void leg_permute_kernel(int64_t n0, int64_t mid, int64_t n2, int leg, int words,
+                                   const int64_t* __restrict__ perm,
+                                   const double* __restrict__ A, double* __restrict__ out) {
+  const int64_t total = n0 * mid * n2;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e % n0, rest = e / n0, s = rest % mid, r = rest / mid;
+    const int64_t src = leg == 0 ? perm[i] + n0 * (s + mid * r) : i + n0 * (s + mid * perm[r]);
+    for (int w = 0; w < words; ++w) out[words * e + w] = A[words * src + w];
+  }
+}
+
+int gb_mps_permute(gb_ctx* ctx, const gb_tensor* A, int leg, const int64_t* perm,
+                   gb_tensor* out) {
+  API_BEGIN
+  GB_REQUIRE(ctx && A && out && perm, "null argument");
+  check_ctx(A, ctx);
+  check_ctx(out, ctx);
+  GB_REQUIRE(A->kind == GB_KIND_MPS && out->kind == GB_KIND_MPS, "permute: MPS tensors only");
+  GB_REQUIRE(leg == 0 || leg == 2, "permute: leg must be 0 (left bond) or 2 (right bond)");
+  GB_REQUIRE(out->dtype == A->dtype && out->dims[0] == A->dims[0] &&
+                 out->dims[1] == A->dims[1] && out->dims[2] == A->dims[2],
+             "permute: output shape");
+  const int64_t n = A->dims[leg];
+  std::vector<char> seen(n, 0);
+  for (int64_t i = 0; i < n; ++i) {
+    GB_REQUIRE(perm[i] >= 0 && perm[i] < n && !seen[perm[i]], "permute: not a permutation");
+    seen[perm[i]] = 1;
+  }
+  DevGuard g(ctx->device);
+  int64_t* dp = (int64_t*)scratch(ctx, SLOT_TMP2, (size_t)std::max<int64_t>(n, 1) * 8 + 256);
+  GB_CHECK_CUDA(cudaMemcpyAsync(dp, perm, (size_t)n * 8, cudaMemcpyHostToDevice, ctx->stream));
+  const int64_t total = numel(A);
+  if (total) {
+    const unsigned nb = (unsigned)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, 4096));
+    leg_permute_kernel<<<nb, 256, 0, ctx->stream>>>(
+        A->dims[0], A->dims[1], A->dims[2], leg, is_cplx(A->dtype) ? 2 : 1, dp,
+        (const double*)A->data, (double*)out->data);
+    GB_CHECK_CUDA(cudaGetLastError());
+    count_launch(ctx);
+  }
+  GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));  // perm is borrowed for the call only
+  API_END
+}
+
 int gb_tensor_reshape(gb_tensor* t, int kind, int ndim, const int64_t* dims) {
   API_BEGIN
   GB_REQUIRE(t && dims, "null argument");

@@ -121,6 +121,7 @@ _SIGS = {
     "gb_project_complement_right": ([P, P, P], INT),
     "gb_svd_batch": ([P, I64, ctypes.POINTER(P), ctypes.POINTER(P), ctypes.POINTER(P),
                       ctypes.POINTER(ctypes.c_double)], INT),
+    "gb_mps_permute": ([P, P, INT, PI64, P], INT),
     "gb_basis_set": ([P, P, I64, P], INT),
     "gb_basis_orthogonalize": ([P, P, I64, P, ctypes.POINTER(ctypes.c_double)], INT),
     "gb_basis_combine": ([P, P, I64, ctypes.POINTER(ctypes.c_double), P], INT),

@@ -17,9 +17,9 @@ from .core import DeviceTensor
 from .derivatives import (AC2_hamiltonian, AC_hamiltonian, C_hamiltonian, GB300Backend, Lanczos,
                           exponentiate, fixedpoint, mpo_projection, transfer_left,
                           transfer_right)
-from .states import (FiniteEnvironments, ac2_from, left_orth, mps_cat, mul_front, mul_tail,
-                     perturb, project_complement_, project_complement_right_, right_orth,
-                     svd_trunc)
+from .states import (FiniteEnvironments, ac2_from, left_orth, mps_cat, mps_permute, mul_front,
+                     mul_tail, perturb, project_complement_, project_complement_right_,
+                     right_orth, svd_trunc)
 
 EPS34 = np.finfo(np.float64).eps ** 0.75
 
@@ -114,8 +114,9 @@ def optimal_expand(pos, right, psi, H, envs, alg, backend=None):
     projectors (1 - AL AL') Y (1 - AR' AR) instead of null-space bases: the singular
     vectors of the projected Y are those of NL' Y NR' mapped back by NL / NR.  Directions
     whose singular value is below eps^(3/4) of the normalised Y (arbitrary in the
-    reference) are not added."""
-    _dense_only(psi, "OptimalExpand")
+    reference) are not added.  For a U(1) state the SVD runs per charge block and the
+    enlarged bond is re-sorted by charge (gb_mps_permute), as TensorKit's catdomain /
+    catcodomain keeps a graded space sorted."""
     backend = backend or GB300Backend()
     b = pos if right else pos - 1
     if right:
@@ -138,17 +139,30 @@ def optimal_expand(pos, right, psi, H, envs, alg, backend=None):
         return
     Y.scale_(1.0 / nrm)
     u, _, vh, _ = svd_trunc(Y, alg.add, EPS34, normalize=False)
+    u1 = rt.charges is not None and left.charges is not None
     if right:
         k = vh.dims[0]
         nar = mps_cat(rt, vh, 0)                         # AR[pos+1] with the new rows
-        nal, nc = left_orth(mps_cat(left, None, 2, nb=k))  # [AC | 0] regauged
+        pad = mps_cat(left, None, 2, nb=k)               # [AC | 0]
+        if u1:
+            q = np.concatenate([rt.charges[0], vh.charges[0]])
+            perm = np.argsort(q, kind="stable")
+            nar = mps_permute(nar, 0, perm, (q[perm], rt.charges[1], rt.charges[2]))
+            pad = mps_permute(pad, 2, perm, (left.charges[0], left.charges[1], q[perm]))
+        nal, nc = left_orth(pad)                         # regauged
         nc.scale_(1.0 / nc.norm())
         psi.AL[pos], psi.C[pos + 1], psi.AR[pos + 1] = nal, nc, nar
         psi.center = pos + 1
     else:
         k = u.dims[2]
         nal = mps_cat(left, u, 2)                        # AL[pos-1] with the new columns
-        nc, nar = right_orth(mps_cat(rt, None, 0, nb=k))  # [AC ; 0] regauged
+        pad = mps_cat(rt, None, 0, nb=k)                 # [AC ; 0]
+        if u1:
+            q = np.concatenate([left.charges[2], u.charges[2]])
+            perm = np.argsort(q, kind="stable")
+            nal = mps_permute(nal, 2, perm, (left.charges[0], left.charges[1], q[perm]))
+            pad = mps_permute(pad, 0, perm, (q[perm], rt.charges[1], rt.charges[2]))
+        nc, nar = right_orth(pad)                        # regauged
         nc.scale_(1.0 / nc.norm())
         psi.AL[pos - 1], psi.C[pos], psi.AR[pos] = nal, nc, nar
         psi.center = pos

@@ -141,6 +141,17 @@ def mps_cat(A, B, leg, nb=None):
     return out
 
 
+def mps_permute(A, leg, perm, charges=None):
+    """A with its bond leg 0 or 2 permuted, out[i] = A[perm[i]] along that leg
+    (gb_mps_permute); `charges` of the result."""
+    p = np.ascontiguousarray(perm, dtype=np.int64)
+    out = DeviceTensor(A.ctx, L.GB_KIND_MPS, A.dtype, A.dims)
+    L.check(L.lib().gb_mps_permute(A.ctx.handle, A.handle, int(leg),
+                                   p.ctypes.data_as(L.PI64), out.handle))
+    out.charges = charges
+    return out
+
+
 def perturb(env, W, AC, side, precision=L.GB_PREC_FP64):
     """The DMRG3S perturbation (gb_mps_perturb): side 0 with GL -> (Dl, d, Dr * wr),
     side 1 with GR -> (Dl * wl, d, Dr)."""

@@ -195,3 +195,58 @@ def test_single_site_dmrg_with_expansion_reaches_ed(ctx, kind):
     for a, b in zip(hist, ohist):
         assert abs(a["energy"] - b[1]) <= 1e-8 * abs(b[1]), (a, b)
     assert -1e-12 * abs(e_ed) <= hist[-1]["energy"] - e_ed < bar
+
+
+@pytest.mark.parametrize("right", [True, False])
+def test_u1_optimal_expand_keeps_the_state_and_sorted_bond(ctx, right):
+    """OptimalExpand on a U(1) state: the SVD of the projected two-site update runs per charge
+    block and the enlarged bond is re-sorted by charge (gb_mps_permute); the state vector is
+    unchanged, the bond grows, its charges stay sorted and the new tensors are isometries."""
+    from mpsgb import u1 as HU
+    from mpsgb.operators import SPIN_HALF_CHARGES as QP
+    L_, pos = 8, 3
+    H = mpsgb.heisenberg_XXX(L_, dtype=np.float64, u1=True)
+    As, qb = HU.random_u1_tensors(L_, 2, 31, 0, np.float64)
+    psi = mpsgb.FiniteMPS.from_tensors(As, ctx, center=pos, charges=(qb, QP))
+    full = lambda ps: _vector([ps.AL[i].numpy() for i in range(ps.center)]
+                              + [ps.ac(ps.center).numpy()]
+                              + [ps.AR[i].numpy() for i in range(ps.center + 1, L_)])
+    v0 = full(psi)
+    D0 = psi.C[pos].dims[0]
+    mpsgb.algorithms.optimal_expand(pos, right, psi, H, mpsgb.FiniteEnvironments(psi, H),
+                                    mpsgb.OptimalExpand(3))
+    v1 = full(psi)
+    assert np.linalg.norm(v1 / np.linalg.norm(v1) - v0 / np.linalg.norm(v0)) < 1e-12
+    if right:
+        A = psi.AR[pos + 1]
+        q = A.charges[0]
+        m = A.numpy().reshape(A.dims[0], -1, order="F")
+        assert np.abs(m @ m.T - np.eye(A.dims[0])).max() < 1e-12
+        assert psi.center == pos + 1 and A.dims[0] > 2
+        assert np.array_equal(psi.AL[pos].charges[2], q)
+    else:
+        A = psi.AL[pos - 1]
+        q = A.charges[2]
+        m = A.numpy().reshape(-1, A.dims[2], order="F")
+        assert np.abs(m.T @ m - np.eye(A.dims[2])).max() < 1e-12
+        assert psi.center == pos and A.dims[2] > D0
+        assert np.array_equal(psi.AR[pos].charges[0], q)
+    assert np.all(np.diff(q) >= 0)
+    # every entry outside the charge blocks is exactly zero
+    ql, qs, qr = A.charges
+    mask = HU.block_mask(ql, qs, qr)
+    assert np.all(A.numpy()[~mask] == 0)
+
+
+def test_u1_single_site_dmrg_with_optimal_expand_reaches_ed(ctx):
+    from mpsgb import u1 as HU
+    from mpsgb.operators import SPIN_HALF_CHARGES as QP
+    L_ = 10
+    terms = M.heisenberg_terms(L_)
+    e_ed = M.ed_ground_energy(L_, 2, terms)[0]
+    As, qb = HU.random_u1_tensors(L_, 2, 5, 0, np.float64)
+    psi = mpsgb.FiniteMPS.from_tensors(As, ctx, charges=(qb, QP))
+    alg = mpsgb.DMRG(tol=1e-10, maxiter=12, alg_expand=mpsgb.OptimalExpand(4))
+    psi, envs, eps, hist = mpsgb.find_groundstate(psi, mpsgb.heisenberg_XXX(L_, dtype=np.float64,
+                                                                            u1=True), alg)
+    assert -1e-12 * abs(e_ed) <= hist[-1]["energy"] - e_ed < 1e-9 * abs(e_ed), (hist[-1], e_ed)
