@@ -394,3 +394,35 @@ def test_oracle_sketched_expand_preserves_the_state_and_reaches_ed(ov):
     alg = P.DMRG(tol=1e-10, maxiter=12, alg_expand=P.SketchedExpand(4, oversampling=ov, seed=3))
     _, _, eps, hist = P.find_groundstate_dmrg(psi0, H, alg)
     assert abs(hist[-1][1] - e_ed) < 1e-9, (hist[-1][1], e_ed)
+
+
+@pytest.mark.parametrize("right", [True, False])
+def test_oracle_sketched_expand_with_a_full_sketch_is_optimal_expand(right):
+    """A sketch spanning the whole complement (oversampling up to its dimension) makes the
+    randomized selection of sketchedexpand.jl the exact one of optimalexpand.jl: the same
+    enlarged bond space."""
+    L_, pos = 8, 3
+    H = M.finite_mpo_hamiltonian(L_, 2, M.heisenberg_terms(L_))
+    As = P.random_initial_tensors(L_, 2, 3, 6)
+
+    def centre():
+        psi = P.finite_mps_from_tensors(As)
+        for i in range(pos):
+            A = np.einsum("ab,bsc->asc", psi.C[i], psi.AR[i])
+            Q, R = P.qr_pos(A.reshape(-1, A.shape[2], order="F"))
+            psi.AL[i], psi.C[i + 1] = Q.reshape(A.shape[0], 2, Q.shape[1], order="F"), R
+            psi.center = i + 1
+        return psi
+
+    a, b = centre(), centre()
+    P.sketched_expand(pos, right, a, H, P.FiniteEnvironments(a, H),
+                      P.SketchedExpand(2, oversampling=8, seed=23))
+    P.optimal_expand(pos, right, b, H, P.FiniteEnvironments(b, H), P.OptimalExpand(2))
+    if right:
+        x, y = (t.AR[pos + 1] for t in (a, b))
+        x, y = (m.reshape(m.shape[0], -1, order="F") for m in (x, y))
+    else:
+        x, y = (t.AL[pos - 1] for t in (a, b))
+        x, y = (m.reshape(-1, m.shape[2], order="F").T for m in (x, y))
+    assert x.shape == y.shape
+    assert np.abs(x.conj().T @ x - y.conj().T @ y).max() < 1e-10
