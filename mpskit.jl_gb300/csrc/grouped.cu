@@ -468,9 +468,9 @@ __global__ void gmix_kernel(int64_t nJ, int64_t N, int64_t xn, const int64_t* __
     const GMixEntry en = ent[n * nJ + J];
     if (en.hi <= en.lo || en.row < 0) continue;
     const int64_t base = (int64_t)en.row * kmax + en.kst - en.lo;
-    // four 32-element chunks per pass with their loads issued together (more bytes in
+    // eight 32-element chunks per pass with their loads issued together (more bytes in
     // flight per warp: the mix is a short strided copy when its rows hold one entry)
-    constexpr int U = 4;
+    constexpr int U = 8;
     for (int64_t a0 = en.lo + lane; a0 < en.hi; a0 += 32 * U) {
       // the arithmetic of gmix_staged_kernel, term for term (identical results)
       float s[U], c[U];
