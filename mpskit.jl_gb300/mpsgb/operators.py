@@ -107,6 +107,41 @@ class MPOHamiltonian:
     def widths(self):
         return [w.shape[3] for w in self.W]
 
+    # ---------------------------------------------------------------- linear algebra
+    # (mpohamiltonian.jl:741-786, 815-820: the Jordan blocks of a sum are A = A1 (+) A2 on
+    # the continuing channels, B and C stacked along them, D = D1 + D2; the identity corners
+    # stay single.  A scalar multiplies every term once: the C and D blocks.)
+    def __add__(self, other):
+        if not isinstance(other, MPOHamiltonian):
+            return NotImplemented
+        if len(self) != len(other) or self.finite != other.finite:
+            raise ValueError("sum of MPOHamiltonians of different lengths or kinds")
+        W = [_jordan_sum(a, b) for a, b in zip(self.W, other.W)]
+        chans = None
+        if self.chans is not None and other.chans is not None:
+            chans = [list(a) if len(a) == 1 else [a[0]] + list(a[1:-1]) + list(b[1:-1]) + [a[-1]]
+                     for a, b in zip(self.chans, other.chans)]
+        return MPOHamiltonian(W, finite=self.finite, chans=chans)
+
+    def __mul__(self, lam):
+        if not np.isscalar(lam):
+            return NotImplemented
+        W = []
+        for w in self.W:
+            w = w.astype(np.result_type(w.dtype, np.asarray(lam).dtype), copy=True)
+            first = 1 if w.shape[3] > 1 else 0   # the start column continues unscaled
+            w[0, :, :, first:] *= lam
+            W.append(w)
+        return MPOHamiltonian(W, finite=self.finite, chans=self.chans)
+
+    __rmul__ = __mul__
+
+    def __neg__(self):
+        return self * -1.0
+
+    def __sub__(self, other):
+        return self + (-other)
+
     def device(self, ctx, dtype=None):
         """GB_KIND_MPO tensors of every site (cached per context and dtype)."""
         dtype = np.dtype(dtype or self.dtype)
@@ -114,6 +149,46 @@ class MPOHamiltonian:
         if key not in self._dev:
             self._dev[key] = [DeviceTensor.from_numpy(ctx, L.GB_KIND_MPO, w, dtype) for w in self.W]
         return self._dev[key]
+
+
+def _jordan_sum(W1, W2):
+    """The site tensor of H1 + H2 (one site of mpohamiltonian.jl:741-786): left channels
+    [start, mid(H1), mid(H2), finish] (only [start] at a finite chain's first site), right
+    channels likewise (only [finish] at its last site)."""
+    wl1, d, _, wr1 = W1.shape
+    wl2, wr2 = W2.shape[0], W2.shape[3]
+    if (wl1 == 1) != (wl2 == 1) or (wr1 == 1) != (wr2 == 1) or W2.shape[1] != d:
+        raise ValueError("sum of MPO site tensors of different boundary structure")
+    lm1 = list(range(1, wl1 - 1)) if wl1 > 1 else []
+    lm2 = list(range(1, wl2 - 1)) if wl2 > 1 else []
+    rm1 = list(range(1, wr1 - 1)) if wr1 > 1 else []
+    rm2 = list(range(1, wr2 - 1)) if wr2 > 1 else []
+    nl = 1 if wl1 == 1 else 2 + len(lm1) + len(lm2)
+    nr = 1 if wr1 == 1 else 2 + len(rm1) + len(rm2)
+
+    def maps(wl, wr, lm, rm, loff, roff):
+        Lm, Rm = {0: 0}, {wr - 1: nr - 1}
+        if wl > 1:
+            Lm[wl - 1] = nl - 1
+        if wr > 1:
+            Rm[0] = 0
+        Lm.update({i: 1 + loff + k for k, i in enumerate(lm)})
+        Rm.update({j: 1 + roff + k for k, j in enumerate(rm)})
+        return Lm, Rm
+
+    W = np.zeros((nl, d, d, nr), dtype=np.result_type(W1.dtype, W2.dtype))
+    L1, R1 = maps(wl1, wr1, lm1, rm1, 0, 0)
+    L2, R2 = maps(wl2, wr2, lm2, rm2, len(lm1), len(rm1))
+    for i in range(wl1):
+        for j in range(wr1):
+            W[L1[i], :, :, R1[j]] += W1[i, :, :, j]
+    for i in range(wl2):
+        for j in range(wr2):
+            start_start = wr2 > 1 and i == 0 and j == 0
+            finish_finish = wl2 > 1 and i == wl2 - 1 and j == wr2 - 1
+            if not (start_start or finish_finish):   # identity corners once
+                W[L2[i], :, :, R2[j]] += W2[i, :, :, j]
+    return W
 
 
 def _site_pieces(sites, op, qphys=None):

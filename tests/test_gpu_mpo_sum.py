@@ -1,0 +1,49 @@
+"""A summed MPOHamiltonian (mpohamiltonian.jl:741-786) on the device: the two-site operator of
+H1 + H2 applies as the sum of the two operators (the linearity the reference tests for LazySum,
+test/operators/lazysum.jl:79-260), and DMRG2 on a U(1) sum reaches exact diagonalisation."""
+import numpy as np
+import pytest
+
+import mpsgb
+from mpsgb import u1 as HU
+from mpsgb.operators import SPIN_HALF_CHARGES as QP
+from oracle import models as M
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    return mpsgb.context(0)
+
+
+def test_sum_operator_is_the_sum_of_operators(ctx):
+    L_, pos = 8, 3
+    H1 = mpsgb.heisenberg_XXX(L_, dtype=np.float64)
+    H2 = mpsgb.transverse_field_ising(L_, g=0.7, dtype=np.float64)
+    S = H1 + 0.5 * H2
+    rng = np.random.default_rng(7)
+    As = [rng.standard_normal((min(2 ** i, 8, 2 ** (L_ - i)), 2, min(2 ** (i + 1), 8, 2 ** (L_ - i - 1))))
+          for i in range(L_)]
+    psi = mpsgb.FiniteMPS.from_tensors(As, ctx, center=pos)
+    x = mpsgb.ac2_from(psi.ac(pos), psi.AR[pos + 1])
+    ys = []
+    for H in (S, H1, H2):
+        envs = mpsgb.FiniteEnvironments(psi, H)
+        ys.append(mpsgb.AC2_hamiltonian(pos, psi, H, envs)(x).numpy())
+    ref = ys[1] + 0.5 * ys[2]
+    assert np.linalg.norm(ys[0] - ref) <= 1e-12 * np.linalg.norm(ref)
+
+
+def test_u1_dmrg2_on_a_sum_reaches_ed(ctx):
+    L_ = 10
+    H = mpsgb.heisenberg_XXX(L_, dtype=np.float64, u1=True) + \
+        mpsgb.xxz(L_, 0.0, 1.0, 0.0, dtype=np.float64, u1=True) * 0.3
+    terms = M.heisenberg_terms(L_, dtype=np.float64) + [
+        (s, 0.3 * op) for s, op in M.xxz_terms(L_, 0.0, 1.0, 0.0, dtype=np.float64)]
+    e_ed = M.ed_ground_energy(L_, 2, terms)[0]
+    As, qb = HU.random_u1_tensors(L_, 16, 3, 0, np.float64)
+    psi = mpsgb.FiniteMPS.from_tensors(As, ctx, charges=(qb, QP))
+    psi, envs, eps, hist = mpsgb.find_groundstate(psi, H, mpsgb.DMRG2(maxdim=32, cutoff=1e-12),
+                                                  maxsweeps=6)
+    assert abs(hist[-1]["energy"] - e_ed) < 1e-9 * abs(e_ed), (hist[-1], e_ed)
