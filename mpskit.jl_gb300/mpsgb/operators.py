@@ -112,6 +112,8 @@ class MPOHamiltonian:
     # the continuing channels, B and C stacked along them, D = D1 + D2; the identity corners
     # stay single.  A scalar multiplies every term once: the C and D blocks.)
     def __add__(self, other):
+        if np.isscalar(other) or isinstance(other, (list, tuple, np.ndarray)):
+            return self._add_onsite(other)
         if not isinstance(other, MPOHamiltonian):
             return NotImplemented
         if len(self) != len(other) or self.finite != other.finite:
@@ -122,6 +124,19 @@ class MPOHamiltonian:
             chans = [list(a) if len(a) == 1 else [a[0]] + list(a[1:-1]) + list(b[1:-1]) + [a[-1]]
                      for a, b in zip(self.chans, other.chans)]
         return MPOHamiltonian(W, finite=self.finite, chans=chans)
+
+    __radd__ = __add__
+
+    def _add_onsite(self, lams):
+        """H + lambdas (mpohamiltonian.jl:788-813): lambda_i times the identity on site i,
+        added to the D (start -> finish) block; a scalar applies to every site."""
+        lams = np.broadcast_to(np.asarray(lams), (len(self),))
+        W = []
+        for w, lam in zip(self.W, lams):
+            w = w.astype(np.result_type(w.dtype, np.asarray(lam).dtype), copy=True)
+            w[0, :, :, w.shape[3] - 1] += lam * np.eye(w.shape[1], dtype=w.dtype)
+            W.append(w)
+        return MPOHamiltonian(W, finite=self.finite, chans=self.chans)
 
     def __mul__(self, lam):
         if not np.isscalar(lam):
@@ -140,7 +155,9 @@ class MPOHamiltonian:
         return self * -1.0
 
     def __sub__(self, other):
-        return self + (-other)
+        if isinstance(other, MPOHamiltonian):
+            return self + (-other)
+        return self + (-np.asarray(other))
 
     def device(self, ctx, dtype=None):
         """GB_KIND_MPO tensors of every site (cached per context and dtype)."""

@@ -56,3 +56,13 @@ def test_infinite_sum_keeps_the_jordan_blocks():
     assert np.allclose(w[1 + n1:-1, :, :, 1 + n1:-1], w2[1:-1, :, :, 1:-1])         # A
     assert np.allclose(w[1:1 + n1, :, :, 1 + n1:-1], 0)
     assert np.allclose(w[1 + n1:-1, :, :, -1], w2[1:-1, :, :, -1])                  # B
+
+
+def test_onsite_shift():
+    L_ = 4
+    H = mpsgb.heisenberg_XXX(L_, dtype=np.float64)
+    lam = np.array([0.1, -0.2, 0.3, 0.05])
+    A = _matrix(H)
+    assert np.abs(_matrix(H + lam) - (A + lam.sum() * np.eye(A.shape[0]))).max() < 1e-13
+    assert np.abs(_matrix(H - 0.7) - (A - 0.7 * L_ * np.eye(A.shape[0]))).max() < 1e-13
+    assert np.abs(_matrix(0.7 + H) - (A + 0.7 * L_ * np.eye(A.shape[0]))).max() < 1e-13
