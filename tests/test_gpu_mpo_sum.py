@@ -27,12 +27,16 @@ def test_sum_operator_is_the_sum_of_operators(ctx):
           for i in range(L_)]
     psi = mpsgb.FiniteMPS.from_tensors(As, ctx, center=pos)
     x = mpsgb.ac2_from(psi.ac(pos), psi.AR[pos + 1])
-    ys = []
+    ac, c = psi.ac(pos), psi.C[pos]
+    ys = {"AC2": [], "AC": [], "C": []}
     for H in (S, H1, H2):
         envs = mpsgb.FiniteEnvironments(psi, H)
-        ys.append(mpsgb.AC2_hamiltonian(pos, psi, H, envs)(x).numpy())
-    ref = ys[1] + 0.5 * ys[2]
-    assert np.linalg.norm(ys[0] - ref) <= 1e-12 * np.linalg.norm(ref)
+        ys["AC2"].append(mpsgb.AC2_hamiltonian(pos, psi, H, envs)(x).numpy())
+        ys["AC"].append(mpsgb.AC_hamiltonian(pos, psi, H, envs)(ac).numpy())
+        ys["C"].append(mpsgb.C_hamiltonian(pos - 1, psi, H, envs)(c).numpy())
+    for kind, (y_sum, y1, y2) in ys.items():
+        ref = y1 + 0.5 * y2
+        assert np.linalg.norm(y_sum - ref) <= 1e-12 * np.linalg.norm(ref), kind
 
 
 def test_u1_dmrg2_on_a_sum_reaches_ed(ctx):
