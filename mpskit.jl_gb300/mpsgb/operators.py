@@ -121,7 +121,8 @@ class MPOHamiltonian:
         W = [_jordan_sum(a, b) for a, b in zip(self.W, other.W)]
         chans = None
         if self.chans is not None and other.chans is not None:
-            chans = [list(a) if len(a) == 1 else [a[0]] + list(a[1:-1]) + list(b[1:-1]) + [a[-1]]
+            chans = [list(a) if len(a) == 1
+                     else [a[0]] + list(a[1:-1]) + list(b[1:-1]) + [a[-1]]
                      for a, b in zip(self.chans, other.chans)]
         return MPOHamiltonian(W, finite=self.finite, chans=chans)
 

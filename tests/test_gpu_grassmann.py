@@ -130,8 +130,8 @@ def test_infinite_gradient_grassmann_matches_vumps(ctx, gx, D):
     bond dimension and the TFIM closed form within the truncation."""
     H = mpsgb.transverse_field_ising(1, g=gx, infinite=True)
     psi = mpsgb.InfiniteMPS.from_tensor(_A(D, 1), ctx)
-    out, envs, normgrad, hist = mpsgb.find_groundstate(psi, H,
-                                                       mpsgb.GradientGrassmann(tol=1e-8, maxiter=300))
+    alg = mpsgb.GradientGrassmann(tol=1e-8, maxiter=300)
+    out, envs, normgrad, hist = mpsgb.find_groundstate(psi, H, alg)
     assert normgrad <= 1e-8, hist["normgrad"][-5:]
     e = mpsgb.infinite.energy_density(out, envs)
     vpsi = mpsgb.InfiniteMPS.from_tensor(_A(D, 1), ctx)

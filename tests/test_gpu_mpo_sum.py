@@ -23,8 +23,8 @@ def test_sum_operator_is_the_sum_of_operators(ctx):
     H2 = mpsgb.transverse_field_ising(L_, g=0.7, dtype=np.float64)
     S = H1 + 0.5 * H2
     rng = np.random.default_rng(7)
-    As = [rng.standard_normal((min(2 ** i, 8, 2 ** (L_ - i)), 2, min(2 ** (i + 1), 8, 2 ** (L_ - i - 1))))
-          for i in range(L_)]
+    bond = lambda b: min(2 ** b, 8, 2 ** (L_ - b))
+    As = [rng.standard_normal((bond(i), 2, bond(i + 1))) for i in range(L_)]
     psi = mpsgb.FiniteMPS.from_tensors(As, ctx, center=pos)
     x = mpsgb.ac2_from(psi.ac(pos), psi.AR[pos + 1])
     ac, c = psi.ac(pos), psi.C[pos]
