@@ -361,6 +361,17 @@ def expectation_value(psi, H, envs, site=0, backend=None):
     return float(np.real(ac.dot(Heff(ac)) / ac.dot(ac)))
 
 
+def variance(psi, H, envs=None, backend=None):
+    """variance(state::FiniteMPS, H) (toolbox.jl:125-128): <H H> - <H>^2, with H H the
+    MPO product (its own environments)."""
+    envs = envs or FiniteEnvironments(psi, H)
+    site = min(psi.center, len(psi) - 1)
+    e = expectation_value(psi, H, envs, site, backend)
+    H2 = H * H
+    e2 = expectation_value(psi, H2, FiniteEnvironments(psi, H2), site, backend)
+    return float(e2 - e * e)
+
+
 def find_groundstate(psi, H, alg, envs=None, maxsweeps=None, callback=None):
     """find_groundstate(psi, H, DMRG2()/DMRG()/GradientGrassmann()) on the device.  DMRG
     modifies the input state in place (find_groundstate! semantics); GradientGrassmann

@@ -140,6 +140,8 @@ class MPOHamiltonian:
         return MPOHamiltonian(W, finite=self.finite, chans=self.chans)
 
     def __mul__(self, lam):
+        if isinstance(lam, MPOHamiltonian):
+            return self._product(lam)
         if not np.isscalar(lam):
             return NotImplemented
         W = []
@@ -150,7 +152,26 @@ class MPOHamiltonian:
             W.append(w)
         return MPOHamiltonian(W, finite=self.finite, chans=self.chans)
 
-    __rmul__ = __mul__
+    def __rmul__(self, lam):
+        return self.__mul__(lam)
+
+    def _product(self, other):
+        """H1 * H2 (mpohamiltonian.jl:848-852, fuse_mul_mpo per site): the operator product
+        (H1 H2)[s; s'] = sum_t H1[s; t] H2[t; s'] with the channel pairs (c1, c2) fused, c1
+        major -- upper triangular again, start (start, start) first and finish (finish,
+        finish) last."""
+        if len(self) != len(other) or self.finite != other.finite:
+            raise ValueError("product of MPOHamiltonians of different lengths or kinds")
+        W = []
+        for a, b in zip(self.W, other.W):
+            # (a1, s, t, b1) x (a2, t, s', b2) -> (a1, a2, s, s', b1, b2)
+            w = np.einsum("astb,ctud->acsubd", a, b)
+            W.append(w.reshape(a.shape[0] * b.shape[0], a.shape[1], b.shape[2],
+                               a.shape[3] * b.shape[3]))
+        chans = None
+        if self.chans is not None and other.chans is not None:
+            chans = [[x * y for x in ca for y in cb] for ca, cb in zip(self.chans, other.chans)]
+        return MPOHamiltonian(W, finite=self.finite, chans=chans)
 
     def __neg__(self):
         return self * -1.0

@@ -51,3 +51,35 @@ def test_u1_dmrg2_on_a_sum_reaches_ed(ctx):
     psi, envs, eps, hist = mpsgb.find_groundstate(psi, H, mpsgb.DMRG2(maxdim=32, cutoff=1e-12),
                                                   maxsweeps=6)
     assert abs(hist[-1]["energy"] - e_ed) < 1e-9 * abs(e_ed), (hist[-1], e_ed)
+
+
+def _matrix(H):
+    T = H.W[0][0]
+    for w in H.W[1:]:
+        T = np.tensordot(T, w, axes=([-1], [0]))
+    T = T[..., 0]
+    L_ = len(H.W)
+    d = H.W[0].shape[1]
+    perm = [2 * i for i in range(L_)] + [2 * i + 1 for i in range(L_)]
+    return T.transpose(perm).reshape(d ** L_, d ** L_)
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.complex128])
+def test_variance_matches_the_dense_state(ctx, dt):
+    """variance(::FiniteMPS, H) (toolbox.jl:125-128) through the MPO product H * H."""
+    L_ = 6
+    H = mpsgb.transverse_field_ising(L_, g=0.8, dtype=dt)
+    rng = np.random.default_rng(9)
+    bond = lambda b: min(2 ** b, 4, 2 ** (L_ - b))
+    As = [rng.standard_normal((bond(i), 2, bond(i + 1))).astype(dt) for i in range(L_)]
+    psi = mpsgb.FiniteMPS.from_tensors(As, ctx)
+    v = mpsgb.variance(psi, H)
+    T = psi.C[0].numpy()
+    for i in range(L_):
+        T = np.tensordot(T, psi.AR[i].numpy(), axes=([-1], [0]))
+    vec = T.reshape(-1)
+    Hm = _matrix(H)
+    nrm = np.vdot(vec, vec).real
+    e = np.vdot(vec, Hm @ vec).real / nrm
+    e2 = np.vdot(Hm @ vec, Hm @ vec).real / nrm
+    assert abs(v - (e2 - e * e)) <= 1e-10 * max(1.0, e2), (v, e2 - e * e)

@@ -66,3 +66,20 @@ def test_onsite_shift():
     assert np.abs(_matrix(H + lam) - (A + lam.sum() * np.eye(A.shape[0]))).max() < 1e-13
     assert np.abs(_matrix(H - 0.7) - (A - 0.7 * L_ * np.eye(A.shape[0]))).max() < 1e-13
     assert np.abs(_matrix(0.7 + H) - (A + 0.7 * L_ * np.eye(A.shape[0]))).max() < 1e-13
+
+
+@pytest.mark.parametrize("u1", [False, True])
+def test_product_is_the_operator_product(u1):
+    L_ = 4
+    H1 = mpsgb.heisenberg_XXX(L_, dtype=np.float64, u1=u1)
+    H2 = mpsgb.xxz(L_, 1.0, 0.4, 0.3, dtype=np.float64, u1=u1)
+    P_ = H1 * H2
+    assert np.abs(_matrix(P_) - _matrix(H1) @ _matrix(H2)).max() < 1e-12
+    assert all(sum(c) == P_.W[i].shape[0] for i, c in enumerate(P_.chans[:-1]))
+    # upper triangular channel structure, identity corners
+    w = P_.W[1]
+    I = np.eye(2)
+    assert np.allclose(w[0, :, :, 0], I) and np.allclose(w[-1, :, :, -1], I)
+    for a in range(w.shape[0]):
+        for b in range(a):
+            assert np.all(w[a, :, :, b] == 0)
