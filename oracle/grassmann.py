@@ -111,3 +111,34 @@ def transport(h, AL, g, a, ALn):
 
 def inner(g1, g2):
     return 2.0 * sum(np.real(np.vdot(a, b)) for a, b in zip(g1, g2))
+
+
+# ---------------------------------------------------------------- one-site InfiniteMPS
+def point_infinite(AL, C0):
+    """InfiniteMPS(AL, C0) (infinitemps.jl:215-233): the right uniform gauge fixed from C0."""
+    from . import vumps as V
+    AR, C = V.uniform_rightorth(AL, C0)
+    return V.InfiniteMPS1(AL, AR, C)
+
+
+def fg_infinite(psi, W, chans):
+    """fg(state::InfiniteMPS, H::InfiniteMPOHamiltonian) (grassmann.jl:171-190): fixed-point
+    environments, energy density, Grassmann.project(AC_projection, AL) * C'."""
+    from . import derivatives as dv
+    from . import vumps as V
+    GL, GR = V.infinite_envs(psi, W, chans, tol=1e-13)
+    f = V.energy_density(psi, W, GL, GR)
+    y = dv.JordanAC(GL, W, GR)(psi.AC)
+    Y, A = _mat(y), _mat(psi.AL)
+    Z = (Y - A @ (A.conj().T @ Y)) @ psi.C.conj().T
+    return float(f), [_ten(Z, psi.AL.shape)]
+
+
+def retract_infinite(psi, g, a):
+    ALn, Zn = retract_site(psi.AL, g[0], a)
+    return point_infinite(ALn, psi.C), [Zn]
+
+
+def precondition_infinite(psi, g):
+    rtol = max(np.finfo(np.float64).eps ** 0.75, np.linalg.norm(g[0]))
+    return [_ten(_mat(g[0]) @ rho_inv_regularized(psi.C, rtol), g[0].shape)]

@@ -97,3 +97,26 @@ def test_gradient_grassmann_reaches_ed_on_the_oracle(L_, D, gx, bar):
     for A in x[0]:
         Q = A.reshape(-1, A.shape[2], order="F")
         assert np.abs(Q.conj().T @ Q - np.eye(Q.shape[1])).max() < 1e-13
+
+
+def test_infinite_gradient_grassmann_on_the_oracle_reaches_the_closed_form():
+    """One-site InfiniteMPS (grassmann.jl:109-122, 171-190): the restated optimiser with the
+    oracle's fixed-point environments reaches the TFIM energy density of the closed form
+    within the D = 4 truncation (paramagnetic g = 4, as the reference's infinite test)."""
+    from oracle import vumps as V
+    g = 4.0
+    H = M.infinite_mpo_hamiltonian(1, 2, M.tfim_terms(1, g=g, periodic=True))
+    rng = np.random.default_rng(2)
+    A = rng.standard_normal((4, 2, 4)) + 1j * rng.standard_normal((4, 2, 4))
+    psi = V.infinite_mps(A)
+    add, scale = _np_ops()
+    fg = lambda x: OG.fg_infinite(x, H[0], H.chans[0])
+    transport = lambda h, x, gg, a, xn: [OG.transport_site(h[0], x.AL, gg[0], a, xn.AL)]
+    x, f, gg, nfg, hist = optim.optimize(fg, psi, optim.ConjugateGradient(gradtol=1e-8,
+                                                                          maxiter=200),
+                                         OG.retract_infinite, transport,
+                                         lambda x, a, b: OG.inner(a, b), add, scale,
+                                         OG.precondition_infinite)
+    assert hist[-1] <= 1e-8, hist[-5:]
+    e_exact = M.tfim_infinite_energy_density(g)
+    assert e_exact - 1e-12 <= f < e_exact + 1e-8, (f, e_exact)
