@@ -101,11 +101,6 @@ class DMRG3S:
         return self.noise * self.decay_rate ** it
 
 
-def _dense_only(psi, what):
-    if psi.C[psi.center].charges is not None:
-        raise NotImplementedError(f"{what} of a U(1)-symmetric state")
-
-
 def optimal_expand(pos, right, psi, H, envs, alg, backend=None):
     """changebond!(site, dir, psi, H, ::OptimalExpand, envs) (optimalexpand.jl:122-187):
     the two-site update AC2_projection projected onto the complements of both sites, its
@@ -192,6 +187,47 @@ class SketchedExpand:
         k = min(self.add, cap)
         return min(k + self.oversampling, cap), k
 
+    def sketch_u1(self, comp, other):
+        """The U(1) form of `sketch`: `comp`, `other` map charge -> complement dimension.
+        sample_space (randexpand.jl:160-165) gives every direction of the (capped) complement
+        a uniform random weight and keeps the `add` largest -- a uniform random subset, whose
+        per-sector counts are k_c; the oversampling adds up to `oversampling` directions in
+        every sector (sketch_space, sketchedexpand.jl:61-66).  Returns (charges, l_c, k_c)."""
+        qs = [c for c in sorted(comp) if min(comp[c], other.get(c, 0)) > 0]
+        cap = np.array([min(comp[c], other[c]) for c in qs], dtype=np.int64)
+        tot = int(cap.sum())
+        w = self.rng.random(tot)
+        keep = np.argsort(-w, kind="stable")[:min(self.add, tot)]
+        kc = np.bincount(np.repeat(np.arange(len(qs)), cap)[keep], minlength=len(qs))
+        return np.asarray(qs, dtype=np.int32), np.minimum(cap, kc + self.oversampling), kc
+
+
+def _complement_dims(q_fused, q_bond):
+    """charge -> dimension of the complement of a bond inside a fused leg (U(1))."""
+    u, n = np.unique(np.asarray(q_fused), return_counts=True)
+    out = dict(zip(u.tolist(), n.tolist()))
+    for c, m in zip(*np.unique(np.asarray(q_bond), return_counts=True)):
+        out[int(c)] = out.get(int(c), 0) - int(m)
+    return {c: v for c, v in out.items() if v > 0}
+
+
+def _fuse(qa, qb):
+    return (np.asarray(qa)[:, None] + np.asarray(qb)[None, :]).reshape(-1, order="F").astype(
+        np.int32)
+
+
+def _sector_select(q_sorted, qs, kc, dtype, ctx):
+    """The 0/1 bond matrix (k x n) picking, in every charge sector of a charge-sorted leg
+    whose directions come in descending singular value, its first kc[c] directions
+    (truncspace(Vk) of the reference).  Returns (matrix, charges of the kept directions)."""
+    q_sorted = np.asarray(q_sorted)
+    idx = []
+    for c, k in zip(qs.tolist(), kc.tolist()):
+        idx += np.nonzero(q_sorted == c)[0][:k].tolist()
+    S = np.zeros((len(idx), len(q_sorted)), dtype=dtype)
+    S[np.arange(len(idx)), idx] = 1
+    return DeviceTensor.from_numpy(ctx, L.GB_KIND_BOND, S), q_sorted[idx].astype(np.int32)
+
 
 def sketched_expand(pos, right, psi, H, envs, alg, backend=None):
     """changebond!(site, dir, psi, H, ::SketchedExpand, envs) (sketchedexpand.jl:75-162):
@@ -199,8 +235,10 @@ def sketched_expand(pos, right, psi, H, envs, alg, backend=None):
     transfer with bra Q), one MPO_AC projection of the neighbouring site (gb_mpo_project),
     projected onto the neighbour's complement and orthonormalised (LQ / QR, or a truncated
     SVD when oversampled), then appended to the bond with zero weight: the state is
-    unchanged.  At single-site cost: no two-site tensor is formed."""
-    _dense_only(psi, "SketchedExpand")
+    unchanged.  At single-site cost: no two-site tensor is formed.  For a U(1) state the
+    sketch is drawn per charge sector (`SketchedExpand.sketch_u1`), every factorisation runs
+    per block, an oversampled sketch is cut back to k_c directions in each sector, and the
+    enlarged bond is re-sorted by charge (gb_mps_permute)."""
     backend = backend or GB300Backend()
     ctx = envs.ctx
     W = H.device(ctx, envs.dtype)
@@ -208,26 +246,56 @@ def sketched_expand(pos, right, psi, H, envs, alg, backend=None):
         left, rt = psi.ac(pos), psi.AR[pos + 1]
         Dl, d, D = left.dims
         d2, Dn = rt.dims[1], rt.dims[2]
-        compL, compR = Dl * d - D, d2 * Dn - D
-        if compL <= 0 or compR <= 0:
-            return
-        l, k = alg.sketch(compL, compR)
+        u1 = left.charges is not None and rt.charges is not None
+        if u1:
+            ql, qp, qr = left.charges
+            qn, qp2 = rt.charges[2], rt.charges[1]
+            qrow = _fuse(ql, qp)
+            qs, lc, kc = alg.sketch_u1(_complement_dims(qrow, qr),
+                                       _complement_dims(_fuse(-np.asarray(qp2), qn), qr))
+            l, k = int(lc.sum()), int(kc.sum())
+            if k == 0:
+                return
+            qo = np.repeat(qs, lc).astype(np.int32)
+            g = alg.gaussian(Dl * d, l, left.dtype) * (qrow[:, None] == qo[None, :])
+            G = DeviceTensor.from_numpy(ctx, L.GB_KIND_MPS, g.reshape(Dl, d, l, order="F"))
+            G.charges = (ql, qp, qo)
+        else:
+            compL, compR = Dl * d - D, d2 * Dn - D
+            if compL <= 0 or compR <= 0:
+                return
+            l, k = alg.sketch(compL, compR)
+            G = DeviceTensor.from_numpy(ctx, L.GB_KIND_MPS, alg.gaussian(Dl * d, l, left.dtype)
+                                        .reshape(Dl, d, l, order="F"))
         AL = psi.al(pos)
-        G = DeviceTensor.from_numpy(ctx, L.GB_KIND_MPS,
-                                    alg.gaussian(Dl * d, l, left.dtype).reshape(Dl, d, l, order="F"))
         Om, _ = left_orth(G)                                   # randisometry
         Q, _ = left_orth(project_complement_(Om, AL))          # qr_compact of the complement part
         GLq = transfer_left(envs.leftenv(pos, psi), W[pos], left, Q, backend)
         Y = mpo_projection(GLq, envs.rightenv(pos + 1, psi), rt, W[pos + 1], backend=backend)
+        if u1:
+            Y.charges = (Q.charges[2], qp2, qn)
         project_complement_right_(Y, rt)
         if l == k:
             _, ar = right_orth(Y)
         else:
             Y.reshape_(L.GB_KIND_AC2, (l, 1, Dn, d2))
-            _, _, ar, _ = svd_trunc(Y, k, 0.0, normalize=False)
+            if u1:
+                Y.charges = (Q.charges[2], np.zeros(1, np.int32), qn, qp2)
+                _, _, arf, _ = svd_trunc(Y, None, 0.0, normalize=False)
+                Sel, qsel = _sector_select(arf.charges[0], qs, kc, arf.dtype, ctx)
+                ar = mul_front(Sel, arf)
+                ar.charges = (qsel, qp2, qn)
+            else:
+                _, _, ar, _ = svd_trunc(Y, k, 0.0, normalize=False)
         kk = ar.dims[0]
         nar = mps_cat(rt, ar, 0)
-        nal, nc = left_orth(mps_cat(left, None, 2, nb=kk))
+        pad = mps_cat(left, None, 2, nb=kk)
+        if u1:
+            q = np.concatenate([qr, ar.charges[0]])
+            perm = np.argsort(q, kind="stable")
+            nar = mps_permute(nar, 0, perm, (q[perm], qp2, qn))
+            pad = mps_permute(pad, 2, perm, (ql, qp, q[perm]))
+        nal, nc = left_orth(pad)
         nc.scale_(1.0 / nc.norm())
         psi.AL[pos], psi.C[pos + 1], psi.AR[pos + 1] = nal, nc, nar
         psi.center = pos + 1
@@ -235,31 +303,63 @@ def sketched_expand(pos, right, psi, H, envs, alg, backend=None):
         lf, rgt = psi.AL[pos - 1], psi.ac(pos)
         Dp, d, Dl = lf.dims
         d2, Dr = rgt.dims[1], rgt.dims[2]
-        compL, compR = Dp * d - Dl, d2 * Dr - Dl
-        if compL <= 0 or compR <= 0:
-            return
-        l, k = alg.sketch(compR, compL)
+        u1 = lf.charges is not None and rgt.charges is not None
+        if u1:
+            qpp, qp = lf.charges[0], lf.charges[1]
+            ql, qp2, qr = rgt.charges
+            qcol = _fuse(-np.asarray(qp2), qr)
+            qs, lc, kc = alg.sketch_u1(_complement_dims(qcol, ql),
+                                       _complement_dims(_fuse(qpp, qp), ql))
+            l, k = int(lc.sum()), int(kc.sum())
+            if k == 0:
+                return
+            qo = np.repeat(qs, lc).astype(np.int32)
+            g = alg.gaussian(d2 * Dr, l, rgt.dtype) * (qcol[:, None] == qo[None, :])
+        else:
+            compL, compR = Dp * d - Dl, d2 * Dr - Dl
+            if compL <= 0 or compR <= 0:
+                return
+            l, k = alg.sketch(compR, compL)
+            g = alg.gaussian(d2 * Dr, l, rgt.dtype)
         _, ARtt = right_orth(rgt)
-        G = DeviceTensor.from_numpy(ctx, L.GB_KIND_MPS,
-                                    alg.gaussian(d2 * Dr, l, rgt.dtype).reshape(1, d2 * Dr, l,
-                                                                                order="F"))
+        G = DeviceTensor.from_numpy(ctx, L.GB_KIND_MPS, g.reshape(1, d2 * Dr, l, order="F"))
+        if u1:
+            G.charges = (np.zeros(1, np.int32), qcol, qo)
         Om, _ = left_orth(G)                                   # randisometry (d2 Dr) x l
         from .infinite import adjoint
         Om = adjoint(Om.reshape_(L.GB_KIND_BOND, (d2 * Dr, l)))
         Om.reshape_(L.GB_KIND_MPS, (l, d2, Dr))                # its adjoint, l x (s r)
+        if u1:
+            Om.charges = (qo, qp2, qr)
         _, Qr = right_orth(project_complement_right_(Om, ARtt))
         GRq = transfer_right(envs.rightenv(pos, psi), W[pos], rgt, Qr, backend)
         Y = mpo_projection(envs.leftenv(pos - 1, psi), GRq, lf, W[pos - 1], backend=backend)
+        if u1:
+            Y.charges = (qpp, qp, Qr.charges[0])
         project_complement_(Y, lf)
         if l == k:
             Qn, _ = left_orth(Y)
         else:
             Y.reshape_(L.GB_KIND_AC2, (Dp, d, l, 1))
-            Qn, _, _, _ = svd_trunc(Y, k, 0.0, normalize=False)
+            if u1:
+                Y.charges = (qpp, qp, Qr.charges[0], np.zeros(1, np.int32))
+                Qf, _, _, _ = svd_trunc(Y, None, 0.0, normalize=False)
+                Sel, qsel = _sector_select(Qf.charges[2], qs, kc, Qf.dtype, ctx)
+                Qn = mul_tail(Qf, adjoint(Sel))
+                Qn.charges = (qpp, qp, qsel)
+            else:
+                Qn, _, _, _ = svd_trunc(Y, k, 0.0, normalize=False)
         kk = Qn.dims[2]
-        nc, nar = right_orth(mps_cat(rgt, None, 0, nb=kk))
+        nal = mps_cat(lf, Qn, 2)
+        pad = mps_cat(rgt, None, 0, nb=kk)
+        if u1:
+            q = np.concatenate([ql, Qn.charges[2]])
+            perm = np.argsort(q, kind="stable")
+            nal = mps_permute(nal, 2, perm, (qpp, qp, q[perm]))
+            pad = mps_permute(pad, 0, perm, (q[perm], qp2, qr))
+        nc, nar = right_orth(pad)
         nc.scale_(1.0 / nc.norm())
-        psi.AL[pos - 1], psi.C[pos], psi.AR[pos] = mps_cat(lf, Qn, 2), nc, nar
+        psi.AL[pos - 1], psi.C[pos], psi.AR[pos] = nal, nc, nar
         psi.center = pos
 
 
@@ -268,36 +368,66 @@ def dmrg3s_gauge(pos, right, psi, H, envs, AC, noise, maxdim, atol):
     perturbation noise * GL[pos] W[pos] AC with the right bond and the MPO channel fused
     (bond index fastest) is appended to AC along its right bond, the truncated SVD gives
     AL[pos] and C = S Vh, and AR[pos+1] gets zero rows for the new directions.  Left: the
-    mirror image with GR[pos], zero columns appended to AL[pos-1].  Returns the truncation
-    error."""
-    _dense_only(psi, "DMRG3S")
+    mirror image with GR[pos], zero columns appended to AL[pos-1].  For a U(1) state the fused
+    leg carries q_bond + q_channel (the channel charges of the MPO), the enlarged bond is
+    re-sorted by charge (gb_mps_permute) and the SVD runs per charge block.  Returns the
+    truncation error."""
     W = H.device(envs.ctx, envs.dtype)[pos]
     Dl, d, Dr = AC.dims
+    u1 = AC.charges is not None
+    if u1:
+        ql, qp, qr = (np.asarray(q, np.int32) for q in AC.charges)
+        qw = H.channel_charges(qp)
     if right:
         P = perturb(envs.leftenv(pos, psi), W, AC, 0, envs.precision)
         P.scale_(noise)
         ACe = mps_cat(AC, P, 2)
-        ACe.reshape_(L.GB_KIND_AC2, (Dl, d, ACe.dims[2], 1))   # left_gauge as an SVD
+        De = ACe.dims[2]
+        if u1:
+            qe = np.concatenate([qr, (qr[:, None] + qw[pos + 1][None, :]).reshape(-1, order="F")])
+            perm = np.argsort(qe, kind="stable")
+            qe = qe[perm].astype(np.int32)
+            ACe = mps_permute(ACe, 2, perm)
+        ACe.reshape_(L.GB_KIND_AC2, (Dl, d, De, 1))             # left_gauge as an SVD
+        if u1:
+            ACe.charges = (ql, qp, qe, np.zeros(1, np.int32))
         al, S, vh, eps = svd_trunc(ACe, maxdim, atol, normalize=True)
         k = S.dims[0]
         C = mul_front(S, vh)
-        C.reshape_(L.GB_KIND_BOND, (k, C.dims[2]))
+        C.reshape_(L.GB_KIND_BOND, (k, De))
+        ar = mps_cat(psi.AR[pos + 1], None, 0, nb=P.dims[2])
+        if u1:
+            C.charges = (S.charges[0], qe)
+            qa = psi.AR[pos + 1].charges
+            ar = mps_permute(ar, 0, perm, (qe, qa[1], qa[2]))
         psi.AL[pos] = al
-        psi.AR[pos + 1] = mps_cat(psi.AR[pos + 1], None, 0, nb=P.dims[2])
+        psi.AR[pos + 1] = ar
         psi.C[pos + 1] = C
         psi.center = pos + 1
     else:
         P = perturb(envs.rightenv(pos, psi), W, AC, 1, envs.precision)
         P.scale_(noise)
         ACe = mps_cat(AC, P, 0)
-        Dl2 = ACe.dims[0]
-        ACe.reshape_(L.GB_KIND_AC2, (Dl2, 1, Dr, d))           # right_gauge as an SVD
+        De = ACe.dims[0]
+        if u1:
+            qe = np.concatenate([ql, (ql[:, None] + qw[pos][None, :]).reshape(-1, order="F")])
+            perm = np.argsort(qe, kind="stable")
+            qe = qe[perm].astype(np.int32)
+            ACe = mps_permute(ACe, 0, perm)
+        ACe.reshape_(L.GB_KIND_AC2, (De, 1, Dr, d))             # right_gauge as an SVD
+        if u1:
+            ACe.charges = (qe, np.zeros(1, np.int32), qr, qp)
         u, S, ar, eps = svd_trunc(ACe, maxdim, atol, normalize=True)
         k = S.dims[0]
         C = mul_tail(u, S)
-        C.reshape_(L.GB_KIND_BOND, (Dl2, k))
+        C.reshape_(L.GB_KIND_BOND, (De, k))
+        al = mps_cat(psi.AL[pos - 1], None, 2, nb=P.dims[0])
+        if u1:
+            C.charges = (qe, S.charges[1])
+            qa = psi.AL[pos - 1].charges
+            al = mps_permute(al, 2, perm, (qa[0], qa[1], qe))
         psi.AR[pos] = ar
-        psi.AL[pos - 1] = mps_cat(psi.AL[pos - 1], None, 2, nb=P.dims[0])
+        psi.AL[pos - 1] = al
         psi.C[pos] = C
         psi.center = pos
     return eps

@@ -181,6 +181,15 @@ class MPOHamiltonian:
             return self + (-other)
         return self + (-np.asarray(other))
 
+    def channel_charges(self, qphys):
+        """U(1) charges of the channels on every bond (`u1.channel_charges`), cached per
+        physical charge assignment."""
+        from .u1 import channel_charges
+        key = ("charges",) + tuple(int(x) for x in qphys)
+        if key not in self._dev:
+            self._dev[key] = channel_charges(self.W, qphys)
+        return self._dev[key]
+
     def device(self, ctx, dtype=None):
         """GB_KIND_MPO tensors of every site (cached per context and dtype)."""
         dtype = np.dtype(dtype or self.dtype)

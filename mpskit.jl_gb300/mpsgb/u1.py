@@ -122,3 +122,40 @@ def sector_dims(q):
     """(charges, sizes) of a sorted charge array."""
     u, c = np.unique(np.asarray(q), return_counts=True)
     return u, c
+
+
+def channel_charges(W, qphys):
+    """U(1) charges of the virtual channels of a finite MPO with charge-definite channels
+    (the charge labels TensorKit's graded MPO spaces carry).  A nonzero W[a, s, t, c] (s the
+    bra, t the ket physical index) moves q_s - q_t into the channel: q_c = q_a + q_s - q_t.
+    The boundary channels carry 0; the rule is applied in both directions until no label
+    changes, and a channel no nonzero entry links to a labelled one carries 0 (its operator
+    blocks vanish).  Returns L + 1 int32 arrays, array b for the bond left of site b; raises
+    ValueError when two entries give one channel different charges."""
+    qp = np.asarray(qphys, dtype=np.int64)
+    unset = np.iinfo(np.int64).min
+    n = len(W)
+    q = [np.full(W[0].shape[0], unset, dtype=np.int64)]
+    q += [np.full(w.shape[3], unset, dtype=np.int64) for w in W]
+    q[0][:] = 0
+    q[n][:] = 0
+    links = []
+    for w in W:
+        nz = np.argwhere(np.asarray(w) != 0)
+        dq = qp[nz[:, 1]] - qp[nz[:, 2]]
+        links.append(np.unique(np.stack([nz[:, 0], nz[:, 3], dq], axis=1), axis=0))
+    changed = True
+    while changed:
+        changed = False
+        for i, trip in enumerate(links):
+            for a, c, dq in trip.tolist():
+                qa, qc = q[i][a], q[i + 1][c]
+                if qa != unset and qc == unset:
+                    q[i + 1][c] = qa + dq
+                    changed = True
+                elif qc != unset and qa == unset:
+                    q[i][a] = qc - dq
+                    changed = True
+                elif qa != unset and qa + dq != qc:
+                    raise ValueError(f"MPO channel {c} right of site {i} has no definite charge")
+    return [np.where(x == unset, 0, x).astype(np.int32) for x in q]

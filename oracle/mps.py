@@ -415,6 +415,125 @@ class SketchedExpand:
         k = min(self.add, cap)
         return min(k + self.oversampling, cap), k
 
+    def sketch_u1(self, comp, other):
+        """sketch_space for a U(1) complement (charge -> dimension maps, capped by `other`):
+        sample_space (randexpand.jl:160-165) draws a uniform weight per direction and keeps
+        the `add` largest, giving per-sector counts k_c; the oversampling adds
+        min(dim, oversampling) per sector, capped (infimum).  Returns (charges, l_c, k_c)."""
+        qs = [c for c in sorted(comp) if min(comp[c], other.get(c, 0)) > 0]
+        cap = np.array([min(comp[c], other[c]) for c in qs], dtype=np.int64)
+        weights = self.rng.random(int(cap.sum()))
+        owner = np.repeat(np.arange(len(qs)), cap)
+        chosen = np.argsort(-weights, kind="stable")[:min(self.add, int(cap.sum()))]
+        kc = np.array([np.sum(owner[chosen] == i) for i in range(len(qs))], dtype=np.int64)
+        return np.asarray(qs, dtype=np.int32), np.minimum(cap, kc + self.oversampling), kc
+
+
+def _u1_comp(q_fused, q_bond):
+    """charge -> dimension of fused(...) minus the bond (the complement space, U(1))."""
+    out = {}
+    for c in np.asarray(q_fused).tolist():
+        out[c] = out.get(c, 0) + 1
+    for c in np.asarray(q_bond).tolist():
+        out[c] = out.get(c, 0) - 1
+    return {c: v for c, v in out.items() if v > 0}
+
+
+def _u1_keep(q_sorted, qs, kc):
+    """Indices of the first kc[c] directions of every sector c of a charge-sorted leg
+    (truncspace(Vk): the target of an oversampled sketch)."""
+    idx = []
+    for c, k in zip(qs.tolist(), kc.tolist()):
+        idx += [i for i, q in enumerate(np.asarray(q_sorted).tolist()) if q == c][:k]
+    return np.asarray(idx, dtype=np.int64)
+
+
+def _sketched_expand_u1(pos, right, psi, H, envs, alg):
+    """U(1) SketchedExpand: the steps of `sketched_expand`, each factorisation per charge
+    block (oracle.u1), the Gaussian sketch restricted to the charge blocks of the sketched
+    complement, and the enlarged bond sorted by charge."""
+    from .u1 import fuse, left_orth_u1, right_orth_u1, svd_trunc_u1
+    qp = psi.qp
+    if right:
+        left, rt = psi.ac(pos), psi.AR[pos + 1]
+        Dl, d, D = left.shape
+        d2, Dn = rt.shape[1], rt.shape[2]
+        ql, qr, qn = psi.qb[pos], psi.qb[pos + 1], psi.qb[pos + 2]
+        qrow, qcolR = fuse(ql, qp), _col_charges(qp, qn)
+        qs, lc, kc = alg.sketch_u1(_u1_comp(qrow, qr), _u1_comp(qcolR, qr))
+        l, k = int(lc.sum()), int(kc.sum())
+        if k == 0:
+            return
+        qo = np.repeat(qs, lc)
+        lmat = left.reshape(Dl * d, D, order="F")
+        RT = rt.reshape(D, d2 * Dn, order="F")
+        AL, _, _ = left_orth_u1(lmat, qrow, qr)
+        Om = alg.gaussian(Dl * d, l, left.dtype) * (qrow[:, None] == qo[None, :])
+        Om, _, _ = left_orth_u1(Om, qrow, qo)
+        Q, _, qq = left_orth_u1(Om - AL @ (AL.conj().T @ Om), qrow, qo)
+        GLq = dv.transfer_left(envs.leftenv(pos, psi), H[pos], left,
+                               Q.reshape(Dl, d, l, order="F"))
+        Y = dv.mpo_ac_apply(GLq, H[pos + 1], envs.rightenv(pos + 1, psi), rt)
+        B = Y.reshape(l, d2 * Dn, order="F")
+        B = B - (B @ RT.conj().T) @ RT
+        if l == k:
+            _, ar, qa = right_orth_u1(B, qq, qcolR)
+        else:
+            _, _, Vh, qa, _ = svd_trunc_u1(B, qq, qcolR)
+            keep = _u1_keep(qa, qs, kc)
+            ar, qa = Vh[keep], qa[keep]
+        q = np.concatenate([qr, qa])
+        perm = np.argsort(q, kind="stable")
+        pad = np.concatenate([lmat, np.zeros((Dl * d, len(qa)), dtype=lmat.dtype)], axis=1)
+        nal, nc, qk = left_orth_u1(pad[:, perm], qrow, q[perm])
+        assert np.array_equal(qk, q[perm])
+        psi.AL[pos] = nal.reshape(Dl, d, len(q), order="F")
+        psi.C[pos + 1] = nc / np.linalg.norm(nc)
+        psi.AR[pos + 1] = np.concatenate([RT, ar], axis=0)[perm].reshape(len(q), d2, Dn,
+                                                                          order="F")
+        psi.qb[pos + 1] = q[perm].astype(np.int32)
+        psi.center = pos + 1
+    else:
+        lf, rgt = psi.AL[pos - 1], psi.ac(pos)
+        Dp, d, Dl = lf.shape
+        d2, Dr = rgt.shape[1], rgt.shape[2]
+        qpp, ql, qr = psi.qb[pos - 1], psi.qb[pos], psi.qb[pos + 1]
+        qrowL, qcol = fuse(qpp, qp), _col_charges(qp, qr)
+        qs, lc, kc = alg.sketch_u1(_u1_comp(qcol, ql), _u1_comp(qrowL, ql))
+        l, k = int(lc.sum()), int(kc.sum())
+        if k == 0:
+            return
+        qo = np.repeat(qs, lc)
+        lmat = lf.reshape(Dp * d, Dl, order="F")
+        RT = rgt.reshape(Dl, d2 * Dr, order="F")
+        _, ARtt, _ = right_orth_u1(RT, ql, qcol)
+        Om = alg.gaussian(d2 * Dr, l, rgt.dtype) * (qcol[:, None] == qo[None, :])
+        Om, _, _ = left_orth_u1(Om, qcol, qo)
+        Om = Om.conj().T
+        _, Qr, qq = right_orth_u1(Om - (Om @ ARtt.conj().T) @ ARtt, qo, qcol)
+        GRq = dv.transfer_right(envs.rightenv(pos, psi), H[pos], rgt,
+                                Qr.reshape(l, d2, Dr, order="F"))
+        Y = dv.mpo_ac_apply(envs.leftenv(pos - 1, psi), H[pos - 1], GRq, lf)
+        B = Y.reshape(Dp * d, l, order="F")
+        B = B - lmat @ (lmat.conj().T @ B)
+        if l == k:
+            Qn, _, qa = left_orth_u1(B, qrowL, qq)
+        else:
+            U, _, _, qa, _ = svd_trunc_u1(B, qrowL, qq)
+            keep = _u1_keep(qa, qs, kc)
+            Qn, qa = U[:, keep], qa[keep]
+        q = np.concatenate([ql, qa])
+        perm = np.argsort(q, kind="stable")
+        pad = np.concatenate([RT, np.zeros((len(qa), d2 * Dr), dtype=RT.dtype)], axis=0)
+        nc, Qr2, qk = right_orth_u1(pad[perm], q[perm], qcol)
+        assert np.array_equal(qk, q[perm])
+        psi.AR[pos] = Qr2.reshape(len(q), d2, Dr, order="F")
+        psi.C[pos] = nc / np.linalg.norm(nc)
+        psi.AL[pos - 1] = np.concatenate([lmat, Qn], axis=1)[:, perm].reshape(Dp, d, len(q),
+                                                                              order="F")
+        psi.qb[pos] = q[perm].astype(np.int32)
+        psi.center = pos
+
 
 def sketched_expand(pos, right, psi, H, envs, alg):
     """changebond!(site, dir, psi, H, ::SketchedExpand, envs) (sketchedexpand.jl:75-162): a
@@ -422,6 +541,8 @@ def sketched_expand(pos, right, psi, H, envs, alg):
     (transfer with bra Q), one MPO_AC application of the neighbouring site, its projection
     onto that site's complement orthonormalised (LQ / QR, or an SVD truncated back to the
     target when oversampled) and appended to the bond with zero weight."""
+    if psi.qb is not None:
+        return _sketched_expand_u1(pos, right, psi, H, envs, alg)
     if right:
         left, rt = psi.ac(pos), psi.AR[pos + 1]
         Dl, d, D = left.shape
@@ -501,7 +622,9 @@ def dmrg3s_gauge(pos, right, psi, H, envs, AC, noise, maxdim, atol):
     perturbation noise * GL[pos] W[pos] AC with the right bond and the MPO leg fused
     (r fastest) is appended to AC along its right bond, the truncated SVD gives AL[pos] and
     C = S Vh, and AR[pos+1] gets zero rows for the new directions.  Left: the mirror image,
-    with the perturbation GR[pos]-side and zero columns appended to AL[pos-1].  Returns the
+    with the perturbation GR[pos]-side and zero columns appended to AL[pos-1].  For a U(1)
+    state the fused leg carries q_bond + q_channel (oracle.u1.mpo_channel_charges), the
+    enlarged bond is sorted by charge and the SVD runs block by block.  Returns the
     truncation error."""
     W = H[pos]
     Dl, d, Dr = AC.shape
@@ -512,14 +635,25 @@ def dmrg3s_gauge(pos, right, psi, H, envs, AC, noise, maxdim, atol):
             comb[np.arange(Dr), w, w * Dr + np.arange(Dr)] = 1
         pert = noise * dv.mpo_ac_apply(envs.leftenv(pos, psi), W, comb, AC)
         ACe = np.concatenate([AC, pert], axis=2)
-        U, S, Vh, eps = svd_trunc(ACe.reshape(Dl * d, -1, order="F"), maxdim, atol)
+        perm = np.arange(ACe.shape[2])
+        if psi.qb is not None:
+            # the fused (r, w) leg carries q_r + q_w; the enlarged bond is kept sorted
+            from .u1 import fuse, mpo_channel_charges, svd_trunc_u1
+            qw = mpo_channel_charges([H[i] for i in range(len(psi))], psi.qp)[pos + 1]
+            qe = np.concatenate([psi.qb[pos + 1], fuse(psi.qb[pos + 1], qw)])
+            perm = np.argsort(qe, kind="stable")
+            U, S, Vh, qk, eps = svd_trunc_u1(ACe[:, :, perm].reshape(Dl * d, -1, order="F"),
+                                             fuse(psi.qb[pos], psi.qp), qe[perm], maxdim, atol)
+            psi.qb[pos + 1] = qk
+        else:
+            U, S, Vh, eps = svd_trunc(ACe.reshape(Dl * d, -1, order="F"), maxdim, atol)
         k = S.size
         C = S[:, None] * Vh
         C = C / np.linalg.norm(C)
         B = psi.AR[pos + 1]
         psi.AL[pos] = np.ascontiguousarray(U.reshape(Dl, d, k, order="F"))
         psi.AR[pos + 1] = np.concatenate(
-            [B, np.zeros((Dr * wr,) + B.shape[1:], dtype=B.dtype)], axis=0)
+            [B, np.zeros((Dr * wr,) + B.shape[1:], dtype=B.dtype)], axis=0)[perm]
         psi.C[pos + 1] = C
         psi.center = pos + 1
     else:
@@ -529,14 +663,26 @@ def dmrg3s_gauge(pos, right, psi, H, envs, AC, noise, maxdim, atol):
             comb[w * Dl + np.arange(Dl), w, np.arange(Dl)] = 1
         pert = noise * dv.mpo_ac_apply(comb, W, envs.rightenv(pos, psi), AC)
         ACe = np.concatenate([AC, pert], axis=0)
-        U, S, Vh, eps = svd_trunc(ACe.reshape(ACe.shape[0], d * Dr, order="F"), maxdim, atol)
+        perm = np.arange(ACe.shape[0])
+        if psi.qb is not None:
+            # the fused (l, w) leg carries q_l + q_w
+            from .u1 import fuse, mpo_channel_charges, svd_trunc_u1
+            qw = mpo_channel_charges([H[i] for i in range(len(psi))], psi.qp)[pos]
+            qe = np.concatenate([psi.qb[pos], fuse(psi.qb[pos], qw)])
+            perm = np.argsort(qe, kind="stable")
+            U, S, Vh, qk, eps = svd_trunc_u1(ACe[perm].reshape(len(qe), d * Dr, order="F"),
+                                             qe[perm], _col_charges(psi.qp, psi.qb[pos + 1]),
+                                             maxdim, atol)
+            psi.qb[pos] = qk
+        else:
+            U, S, Vh, eps = svd_trunc(ACe.reshape(ACe.shape[0], d * Dr, order="F"), maxdim, atol)
         k = S.size
         C = U * S[None, :]
         C = C / np.linalg.norm(C)
         B = psi.AL[pos - 1]
         psi.AR[pos] = np.ascontiguousarray(Vh.reshape(k, d, Dr, order="F"))
         psi.AL[pos - 1] = np.concatenate(
-            [B, np.zeros(B.shape[:2] + (Dl * wl,), dtype=B.dtype)], axis=2)
+            [B, np.zeros(B.shape[:2] + (Dl * wl,), dtype=B.dtype)], axis=2)[:, :, perm]
         psi.C[pos] = C
         psi.center = pos
     return eps

@@ -113,3 +113,29 @@ def svd_trunc_u1(M, qrow, qcol, maxdim=None, atol=0.0):
         qk[o:o + n] = q
         o += n
     return U, S, Vh, qk, eps
+
+
+def mpo_channel_charges(W, qp):
+    """Channel charges of a finite MPO with charge-definite channels (TensorKit's graded MPO
+    spaces; the DMRG3S combiner fuses a bond with them, post_expand/dmrg3s.jl:122-131).
+    W[a, s, t, c] != 0 (s bra, t ket) fixes q_c = q_a + q_s - q_t.  Forward sweep from the
+    charge-0 left boundary, then a backward sweep from the charge-0 right boundary for channels
+    reached only from the right; unlinked channels carry 0."""
+    qp = [int(x) for x in qp]
+    q = [dict() for _ in range(len(W) + 1)]
+    q[0] = {a: 0 for a in range(W[0].shape[0])}
+    q[-1] = {c: 0 for c in range(W[-1].shape[3])}
+    nzs = [np.argwhere(np.asarray(w) != 0) for w in W]
+    for i, nz in enumerate(nzs):                       # forward
+        for a, s, t, c in nz:
+            if a in q[i]:
+                v = q[i][a] + qp[s] - qp[t]
+                assert q[i + 1].setdefault(c, v) == v, "channel without a definite charge"
+    for i in range(len(W) - 1, -1, -1):                # backward
+        for a, s, t, c in nzs[i]:
+            if c in q[i + 1]:
+                v = q[i + 1][c] - qp[s] + qp[t]
+                assert q[i].setdefault(a, v) == v, "channel without a definite charge"
+    dims = [W[0].shape[0]] + [w.shape[3] for w in W]
+    return [np.array([q[b].get(c, 0) for c in range(dims[b])], dtype=np.int32)
+            for b in range(len(W) + 1)]

@@ -250,3 +250,45 @@ def test_u1_single_site_dmrg_with_optimal_expand_reaches_ed(ctx):
     psi, envs, eps, hist = mpsgb.find_groundstate(psi, mpsgb.heisenberg_XXX(L_, dtype=np.float64,
                                                                             u1=True), alg)
     assert -1e-12 * abs(e_ed) <= hist[-1]["energy"] - e_ed < 1e-9 * abs(e_ed), (hist[-1], e_ed)
+
+
+def _u1_blocks_ok(psi):
+    """Every stored site tensor of a U(1) state is exactly zero outside its charge blocks and
+    its bonds are sorted by charge."""
+    from mpsgb import u1 as HU
+    for i in range(len(psi.AL)):
+        A = psi.AL[i] if i < psi.center else psi.AR[i]
+        ql, qs, qr = A.charges
+        assert np.all(np.diff(ql) >= 0) and np.all(np.diff(qr) >= 0)
+        assert np.all(A.numpy()[~HU.block_mask(ql, qs, qr)] == 0), i
+
+
+@pytest.mark.parametrize("kind", ["dmrg3s", "sketched_expand", "sketched_oversampled"])
+def test_u1_single_site_dmrg_with_expansion_matches_the_oracle(ctx, kind):
+    """U(1) DMRG3S (the perturbation's fused leg labelled by q_bond + q_channel) and U(1)
+    SketchedExpand (per-sector sketch) from a D = 2 start: the sweep energies follow the
+    oracle's, the state reaches exact diagonalisation and stays block sparse."""
+    from mpsgb import u1 as HU
+    from mpsgb.operators import SPIN_HALF_CHARGES as QP
+    L_ = 10
+    e_ed = M.ed_ground_energy(L_, 2, M.heisenberg_terms(L_, dtype=np.float64))[0]
+    As, qb = HU.random_u1_tensors(L_, 2, 5, 0, np.float64)
+    H = mpsgb.heisenberg_XXX(L_, dtype=np.float64, u1=True)
+    if kind == "dmrg3s":
+        oalg = P.DMRG(tol=1e-10, maxiter=12, alg_gauge=P.DMRG3S(0.1, 0.8, 16, 1e-12))
+        alg = mpsgb.DMRG(tol=1e-10, maxiter=12, alg_gauge=mpsgb.DMRG3S(0.1, 0.8, 16, 1e-12))
+        bar = 1e-7
+    else:
+        ov = 2 if kind == "sketched_oversampled" else 0
+        oalg = P.DMRG(tol=1e-10, maxiter=12, alg_expand=P.SketchedExpand(4, ov, seed=3))
+        alg = mpsgb.DMRG(tol=1e-10, maxiter=12, alg_expand=mpsgb.SketchedExpand(4, ov, seed=3))
+        bar = 1e-9
+    _, _, _, ohist = P.find_groundstate_dmrg(P.finite_mps_from_tensors(As, charges=(qb, QP)),
+                                             H, oalg)
+    psi = mpsgb.FiniteMPS.from_tensors(As, ctx, charges=(qb, QP))
+    psi, envs, eps, hist = mpsgb.find_groundstate(psi, H, alg)
+    assert len(hist) == len(ohist)
+    for a, b in zip(hist, ohist):
+        assert abs(a["energy"] - b[1]) <= 1e-8 * abs(b[1]), (a, b)
+    assert -1e-12 * abs(e_ed) <= hist[-1]["energy"] - e_ed < bar * abs(e_ed)
+    _u1_blocks_ok(psi)

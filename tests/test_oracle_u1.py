@@ -102,3 +102,106 @@ def test_u1_dmrg2_matches_ed_sector():
         if a is not None:
             mask = HU.block_mask(psi.qb[i], psi.qp, psi.qb[i + 1])
             assert np.all(a[~mask] == 0)
+
+
+def test_mpo_channel_charges_host_and_oracle_agree():
+    """The charge labels of the MPO channels: every nonzero W[a, s, t, c] moves q_s - q_t into
+    the channel, for plain, summed and product Hamiltonians."""
+    L_ = 6
+    H = O.heisenberg_XXX(L_, dtype=np.float64, u1=True)
+    for Hx in (H, H + O.xxz(L_, 0.0, 1.0, 0.2, dtype=np.float64, u1=True), H * H):
+        qh = HU.channel_charges(Hx.W, O.SPIN_HALF_CHARGES)
+        qo = U.mpo_channel_charges(Hx.W, O.SPIN_HALF_CHARGES)
+        qp = np.asarray(O.SPIN_HALF_CHARGES)
+        for i, w in enumerate(Hx.W):
+            assert np.array_equal(qh[i], qo[i])
+            for a, s, t, c in np.argwhere(w != 0):
+                assert qh[i + 1][c] == qh[i][a] + qp[s] - qp[t]
+    assert qh[0].tolist() == [0] and qh[-1].tolist() == [0]
+    with pytest.raises(ValueError):
+        HU.channel_charges(O.heisenberg_XXX(L_, dtype=np.float64).W, O.SPIN_HALF_CHARGES)
+
+
+@pytest.mark.parametrize("right", [True, False])
+def test_u1_dmrg3s_perturbation_is_block_sparse(right):
+    """The DMRG3S perturbation of a U(1) state lives on the charge blocks of the fused
+    (bond, channel) leg, so the enlarged tensor is symmetric and its bond sorts by charge."""
+    L_, pos = 8, 3
+    H = O.heisenberg_XXX(L_, dtype=np.float64, u1=True)
+    As, qb = HU.random_u1_tensors(L_, 8, 4, 0, np.float64)
+    psi = P.finite_mps_from_tensors(As, charges=(qb, O.SPIN_HALF_CHARGES))
+    psi.center = pos if right else pos + 1          # every AL, AR and C is valid
+    envs = P.FiniteEnvironments(psi, H)
+    AC = psi.ac(pos)
+    v0 = [psi.qb[b].copy() for b in range(L_ + 1)]
+    P.dmrg3s_gauge(pos, right, psi, H, envs, AC, 0.3, 64, 0.0)
+    b = pos + 1 if right else pos
+    qk = psi.qb[b]
+    assert np.all(np.diff(qk) >= 0) and len(qk) > len(v0[b])
+    if right:
+        A, ql, qr = psi.AL[pos], psi.qb[pos], qk
+    else:
+        A, ql, qr = psi.AR[pos], qk, psi.qb[pos + 1]
+    mask = HU.block_mask(ql, psi.qp, qr)
+    assert np.all(A[~mask] == 0)
+    m = A.reshape(-1, A.shape[2], order="F") if right else A.reshape(A.shape[0], -1, order="F")
+    g = m.conj().T @ m if right else m @ m.conj().T
+    assert np.abs(g - np.eye(len(g))).max() < 1e-12
+
+
+def test_u1_single_site_dmrg3s_reaches_ed():
+    L_ = 10
+    As, qb = HU.random_u1_tensors(L_, 2, 5, 0, np.float64)
+    H = O.heisenberg_XXX(L_, dtype=np.float64, u1=True)
+    psi = P.finite_mps_from_tensors(As, charges=(qb, O.SPIN_HALF_CHARGES))
+    alg = P.DMRG(tol=1e-10, maxiter=12, alg_gauge=P.DMRG3S(0.1, 0.8, 16, 1e-12))
+    psi, envs, eps, hist = P.find_groundstate_dmrg(psi, H, alg)
+    e_ed = M.ed_ground_energy(L_, 2, M.heisenberg_terms(L_, dtype=np.float64))[0]
+    assert -1e-12 * abs(e_ed) <= hist[-1][1] - e_ed < 1e-7 * abs(e_ed), (hist[-1], e_ed)
+
+
+def _dense_state(psi):
+    """The state vector of an oracle FiniteMPS (AL left of the centre bond, AR right of it)."""
+    T = np.ones((1, 1))
+    for i in range(psi.center):
+        T = np.tensordot(T, psi.AL[i], axes=([-1], [0]))
+    T = np.tensordot(T, psi.C[psi.center], axes=([-1], [0]))
+    for i in range(psi.center, len(psi)):
+        T = np.tensordot(T, psi.AR[i], axes=([-1], [0]))
+    return T.reshape(-1)
+
+
+@pytest.mark.parametrize("right", [True, False])
+@pytest.mark.parametrize("ov", [0, 2])
+def test_u1_sketched_expand_keeps_the_state_and_sorted_bond(right, ov):
+    L_, pos = 8, 3
+    H = O.heisenberg_XXX(L_, dtype=np.float64, u1=True)
+    As, qb = HU.random_u1_tensors(L_, 4, 21, 0, np.float64)
+    psi = P.finite_mps_from_tensors(As, charges=(qb, O.SPIN_HALF_CHARGES))
+    psi.center = pos if right else pos + 1
+    v0 = _dense_state(psi)
+    envs = P.FiniteEnvironments(psi, H)
+    b = pos + 1 if right else pos
+    n0 = len(psi.qb[b])
+    P.sketched_expand(pos, right, psi, H, envs, P.SketchedExpand(3, oversampling=ov, seed=4))
+    v1 = _dense_state(psi)
+    assert np.linalg.norm(v1 / np.linalg.norm(v1) - v0 / np.linalg.norm(v0)) < 1e-12
+    q = psi.qb[b]
+    assert len(q) > n0 and np.all(np.diff(q) >= 0)
+    A = psi.AR[pos + 1] if right else psi.AL[pos - 1]
+    ql, qr = (q, psi.qb[pos + 2]) if right else (psi.qb[pos - 1], q)
+    assert np.all(A[~HU.block_mask(ql, psi.qp, qr)] == 0)
+    m = A.reshape(A.shape[0], -1, order="F") if right else A.reshape(-1, A.shape[2], order="F")
+    g = m @ m.conj().T if right else m.conj().T @ m
+    assert np.abs(g - np.eye(len(g))).max() < 1e-12
+
+
+def test_u1_single_site_dmrg_with_sketched_expand_reaches_ed():
+    L_ = 10
+    As, qb = HU.random_u1_tensors(L_, 2, 5, 0, np.float64)
+    H = O.heisenberg_XXX(L_, dtype=np.float64, u1=True)
+    psi = P.finite_mps_from_tensors(As, charges=(qb, O.SPIN_HALF_CHARGES))
+    alg = P.DMRG(tol=1e-10, maxiter=12, alg_expand=P.SketchedExpand(4, seed=3))
+    psi, envs, eps, hist = P.find_groundstate_dmrg(psi, H, alg)
+    e_ed = M.ed_ground_energy(L_, 2, M.heisenberg_terms(L_, dtype=np.float64))[0]
+    assert -1e-12 * abs(e_ed) <= hist[-1][1] - e_ed < 1e-9 * abs(e_ed), (hist[-1], e_ed)
