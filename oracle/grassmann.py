@@ -142,3 +142,45 @@ def retract_infinite(psi, g, a):
 def precondition_infinite(psi, g):
     rtol = max(np.finfo(np.float64).eps ** 0.75, np.linalg.norm(g[0]))
     return [_ten(_mat(g[0]) @ rho_inv_regularized(psi.C, rtol), g[0].shape)]
+
+
+# ---------------------------------------------------------------- InfiniteMPS, L-site cell
+def point_cell(AL, Cend):
+    """InfiniteMPS(AL, C[end]) for a cell: AR and every C from the right uniform gauge."""
+    from . import cell as Ce
+    AR, C = Ce.uniform_rightorth(AL, Cend)
+    return Ce.InfiniteMPSCell(AL, AR, C)
+
+
+def fg_cell(psi, H):
+    """fg(state::InfiniteMPS, H::InfiniteMPOHamiltonian) (grassmann.jl:171-190) for an L-site
+    cell: the cell's fixed-point environments, the energy of the cell (expectation_value sums
+    its sites, expval.jl:150-161) and per site Grassmann.project(AC_projection, AL[i]) C[i]'."""
+    from . import cell as Ce
+    from . import derivatives as dv
+    GL, GR = Ce.infinite_envs(psi, H, tol=1e-13)
+    f = Ce.energy(psi, H, GL, GR)
+    gs = []
+    for s in range(len(psi)):
+        Y, A = _mat(dv.JordanAC(GL[s], H.W[s], GR[s])(psi.AC(s))), _mat(psi.AL[s])
+        Z = (Y - A @ (A.conj().T @ Y)) @ psi.C[s].conj().T
+        gs.append(_ten(Z, psi.AL[s].shape))
+    return float(f), gs
+
+
+def retract_cell(psi, g, a):
+    """retract(state::InfiniteMPS, g, a) (grassmann.jl:106-115): every AL along its geodesic,
+    then InfiniteMPS(AL', C[end])."""
+    out = [retract_site(psi.AL[s], g[s], a) for s in range(len(psi))]
+    return point_cell([o[0] for o in out], psi.C[-1]), [o[1] for o in out]
+
+
+def transport_cell(h, psi, g, a, psin):
+    return [transport_site(h[s], psi.AL[s], g[s], a, psin.AL[s]) for s in range(len(psi))]
+
+
+def precondition_cell(psi, g):
+    """precondition(state, g) (grassmann.jl:85-94): g[i] rho_inv_regularized(C[i])."""
+    eps34 = np.finfo(np.float64).eps ** 0.75
+    return [_ten(_mat(g[s]) @ rho_inv_regularized(psi.C[s], max(eps34, np.linalg.norm(g[s]))),
+                 g[s].shape) for s in range(len(psi))]

@@ -120,3 +120,41 @@ def test_infinite_gradient_grassmann_on_the_oracle_reaches_the_closed_form():
     assert hist[-1] <= 1e-8, hist[-5:]
     e_exact = M.tfim_infinite_energy_density(g)
     assert e_exact - 1e-12 <= f < e_exact + 1e-8, (f, e_exact)
+
+
+def _cell_start(D, seed, n=2):
+    from oracle import cell as Ce
+    rng = np.random.default_rng(seed)
+    As = [rng.standard_normal((D, 2, D)) + 1j * rng.standard_normal((D, 2, D)) for _ in range(n)]
+    return Ce.infinite_mps(As)
+
+
+def test_cell_gradient_is_the_derivative_of_the_cell_energy():
+    """fg(::InfiniteMPS) with a two-site cell (grassmann.jl:171-190): along the geodesic of a
+    direction d the energy of the cell changes at the rate inner(g, d)."""
+    H = M.infinite_mpo_hamiltonian(2, 2, M.tfim_terms(2, g=0.8, periodic=True))
+    psi = _cell_start(4, 5)
+    f0, g0 = OG.fg_cell(psi, H)
+    d = [-x for x in OG.precondition_cell(psi, g0)]
+    slope = OG.inner(g0, d)
+    assert slope < 0
+    h = 1e-4
+    fp = OG.fg_cell(OG.retract_cell(psi, d, h)[0], H)[0]
+    fm = OG.fg_cell(OG.retract_cell(psi, d, -h)[0], H)[0]
+    assert abs((fp - fm) / (2 * h) - slope) <= 1e-5 * abs(slope)
+
+
+def test_cell_gradient_grassmann_on_the_oracle_reaches_the_closed_form():
+    """GradientGrassmann on a two-site InfiniteMPS cell: the restated optimiser reaches the
+    TFIM energy per site of the closed form within the D = 4 truncation."""
+    g = 4.0
+    H = M.infinite_mpo_hamiltonian(2, 2, M.tfim_terms(2, g=g, periodic=True))
+    add, scale = _np_ops()
+    x, f, gg, nfg, hist = optim.optimize(lambda x: OG.fg_cell(x, H), _cell_start(4, 2),
+                                         optim.ConjugateGradient(gradtol=1e-8, maxiter=300),
+                                         OG.retract_cell, OG.transport_cell,
+                                         lambda x, a, b: OG.inner(a, b), add, scale,
+                                         OG.precondition_cell)
+    assert hist[-1] <= 1e-8, hist[-5:]
+    e_exact = M.tfim_infinite_energy_density(g)
+    assert e_exact - 1e-12 <= f / 2 < e_exact + 1e-8, (f / 2, e_exact)
