@@ -1,6 +1,6 @@
-"""GradientGrassmann on the device (finite MPS and one-site InfiniteMPS): the left-canonical
-tensors AL[i] as points of Grassmann manifolds, optimised by Riemannian conjugate gradients
-(mpsgb.optim).
+"""GradientGrassmann on the device (finite MPS, one-site InfiniteMPS and InfiniteMPS unit
+cells): the left-canonical tensors AL[i] as points of Grassmann manifolds, optimised by
+Riemannian conjugate gradients (mpsgb.optim).
 
   GradientGrassmann, find_groundstate  -- src/algorithms/groundstate/gradient_grassmann.jl:1-121
   fg, precondition, retract, transport, inner, rho_inv_regularized
@@ -356,13 +356,62 @@ def precondition_infinite(x, g):
     return [GrassmannTangent(g[0].W, mul_tail(g[0].Z, rho_inv_regularized(x.C, rtol)))]
 
 
+# ------------------------------------------------------------------ InfiniteMPS, L-site cell
+def fg_cell(x, H, envs, backend=None):
+    """fg(state::InfiniteMPS, H::InfiniteMPOHamiltonian, envs) (grassmann.jl:171-190) for an
+    L-site cell: the cell's fixed-point environments recalculated, the energy of the cell
+    (expectation_value sums its sites, expval.jl:150-161) and per site the projected AC
+    derivative times C[s]'."""
+    from .cell import _heff_ac, energy
+    backend = backend or GB300Backend()
+    envs.recalculate(x)
+    f = energy(x, envs)
+    gs = []
+    for s in range(len(x)):
+        g = project(_heff_ac(envs, s, backend)(x.AC(s)), x.AL[s])
+        gs.append(GrassmannTangent(x.AL[s], mul_tail(g.Z, adjoint(x.C[s]))))
+    return f, gs
+
+
+def retract_cell(x, g, a):
+    """retract(state::InfiniteMPS, g, a) (grassmann.jl:106-115): every AL[s] along its
+    geodesic, then InfiniteMPS(AL', C[end]) -- the cell's right uniform gauge."""
+    from .cell import InfiniteMPSCell, uniform_rightorth
+    out = [retract_site(x.AL[s], g[s], a) for s in range(len(x))]
+    ALn = [o[0] for o in out]
+    AR, C = uniform_rightorth(ALn, x.C[-1])
+    return InfiniteMPSCell(ALn, AR, C), [o[1] for o in out]
+
+
+def transport_cell(h, x, g, a, xn):
+    return [transport_site(h[s], x.AL[s], g[s], a, xn.AL[s]) for s in range(len(x))]
+
+
+def precondition_cell(x, g):
+    """precondition(state, g) (grassmann.jl:85-94): g[s] rho_inv_regularized(C[s]) with the
+    bond SVDs of the cell batched."""
+    rtolmin = np.finfo(np.float64).eps ** 0.75
+    svds = _svd_batch(list(x.C))
+    return [GrassmannTangent(gs.W, mul_tail(gs.Z, rho_inv_regularized(
+        x.C[s], max(rtolmin, gs.norm()), svds[s]))) for s, gs in enumerate(g)]
+
+
 def find_groundstate_grassmann(psi, H, alg=None, envs=None):
     """find_groundstate(psi, H, GradientGrassmann) (gradient_grassmann.jl:80-121) ->
     (psi, envs, normgrad, history): the optimised state (finite: left-canonical, centre bond
     0 after the closing LQ sweep; infinite: uniformly gauged), its environments, the final
     gradient norm and the gradient-norm history."""
     alg = alg or GradientGrassmann()
+    from .cell import InfiniteEnvironmentsCell, InfiniteMPSCell
     from .infinite import InfiniteEnvironments, InfiniteMPS
+    if isinstance(psi, InfiniteMPSCell):
+        envs = envs or InfiniteEnvironmentsCell(psi, H, alg.backend.code)
+        x, f, g, numfg, hist = optimize(
+            lambda x_: fg_cell(x_, H, envs, alg.backend), psi, alg.method, retract_cell,
+            transport_cell, inner, add, scale, precondition_cell)
+        envs.recalculate(x)
+        return x, envs, hist[-1], {"energy": f / len(x), "energy_cell": f, "numfg": numfg,
+                                   "normgrad": hist}
     if isinstance(psi, InfiniteMPS):
         envs = envs or InfiniteEnvironments(psi, H)
         x, f, g, numfg, hist = optimize(

@@ -141,3 +141,54 @@ def test_infinite_gradient_grassmann_matches_vumps(ctx, gx, D):
     assert e >= e_exact - 1e-10
     assert abs(e - vhist[-1]["energy"]) <= 1e-9 * abs(e), (e, vhist[-1]["energy"])
     assert mpsgb.infinite.galerkin(out, envs) < 1e-6
+
+
+def _cell_As(D, seed, n=2):
+    rng = np.random.default_rng(seed)
+    return [rng.standard_normal((D, 2, D)) + 1j * rng.standard_normal((D, 2, D))
+            for _ in range(n)]
+
+
+def _relerr(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def test_cell_fg_precondition_and_retract_match_the_oracle(ctx):
+    """GradientGrassmann's pieces on a two-site InfiniteMPS cell (grassmann.jl:85-122,
+    171-190) against the oracle's cell restatement at the same point: the cell energy, the
+    per-site gradients, the preconditioned direction and the retracted point."""
+    from mpsgb import cell as GC
+    from oracle import cell as Ce
+    As = _cell_As(6, 5)
+    H = mpsgb.transverse_field_ising(2, g=0.8, infinite=True)
+    oH = M.infinite_mpo_hamiltonian(2, 2, M.tfim_terms(2, g=0.8, periodic=True))
+    opsi = Ce.infinite_mps(As)
+    psi = GC.InfiniteMPSCell.from_tensors(As, ctx)
+    envs = GC.InfiniteEnvironmentsCell(psi, H)
+    f, g = G.fg_cell(psi, H, envs)
+    of, og = OG.fg_cell(opsi, oH)
+    assert abs(f - of) <= 1e-9 * abs(of), (f, of)
+    p, op = G.precondition_cell(psi, g), OG.precondition_cell(opsi, og)
+    for s in range(2):
+        assert _relerr(g[s].Z.numpy(), og[s]) <= 1e-6, s
+        assert _relerr(p[s].Z.numpy(), op[s]) <= 1e-5, s
+    xn, _ = G.retract_cell(psi, G.scale(p, -1.0), 0.05)
+    oxn, _ = OG.retract_cell(opsi, [-x for x in op], 0.05)
+    for s in range(2):
+        assert _relerr(xn.AL[s].numpy(), oxn.AL[s]) <= 1e-6, s
+        assert _relerr(xn.C[s].numpy(), oxn.C[s]) <= 1e-6, s
+
+
+def test_cell_gradient_grassmann_reaches_the_closed_form(ctx):
+    """GradientGrassmann on a two-site InfiniteMPS cell (TFIM g = 4, D = 4): the gradient
+    vanishes, the energy per site is the closed form within the truncation, and the state is
+    a VUMPS fixed point (Galerkin error)."""
+    from mpsgb import cell as GC
+    H = mpsgb.transverse_field_ising(2, g=4.0, infinite=True)
+    psi = GC.InfiniteMPSCell.from_tensors(_cell_As(4, 2), ctx)
+    out, envs, normgrad, hist = mpsgb.find_groundstate(
+        psi, H, mpsgb.GradientGrassmann(tol=1e-8, maxiter=300))
+    assert normgrad <= 1e-8, hist["normgrad"][-5:]
+    e_exact = M.tfim_infinite_energy_density(4.0)
+    assert e_exact - 1e-12 <= hist["energy"] < e_exact + 1e-8, (hist["energy"], e_exact)
+    assert GC.galerkin(out, envs) < 1e-6
