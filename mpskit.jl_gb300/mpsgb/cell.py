@@ -1,11 +1,12 @@
 """InfiniteMPS with a unit cell of L >= 1 sites on the device: uniform gauge, environments,
-VUMPS and IDMRG2.
+VUMPS, IDMRG and IDMRG2.
 
   uniform_leftorth! / uniform_rightorth! over the cell  -- src/states/ortho.jl:214-340
   compute_leftenvs! / compute_rightenvs!, left_cyclethrough! / right_cyclethrough!
                                                          -- src/environments/infinite_envs.jl:207-346
   VUMPS (per-site AC and C eigensolves, gauge step, environments)
                                                          -- src/algorithms/groundstate/vumps.jl:101-192
+  IDMRG (one-site sweeps through the cell)              -- src/algorithms/groundstate/idmrg.jl:85-229
   IDMRG2 (two-site sweeps with the edge updates)        -- src/algorithms/groundstate/idmrg.jl:143-338
 
 Sites are counted from 0; C[i] is the bond tensor right of site i and C[-1] = C[L-1] the one
@@ -414,6 +415,57 @@ def find_groundstate_vumps(psi, H, alg, envs=None):
         hist.append({"iter": it, "energy": energy(psi, envs) / n, "eps": eps})
         if eps <= alg.tol or it >= alg.maxiter:
             break
+    return psi, envs, eps, hist
+
+
+def find_groundstate_idmrg(psi, H, alg, envs=None):
+    """find_groundstate(::InfiniteMPS, H, IDMRG()) for a cell of n >= 1 sites
+    (idmrg.jl:85-229): per site from left to right an AC eigensolve (started from the stored
+    AC), the positive QR AC = AL[s] C[s] and GL[s+1] <- GL[s] T(AL[s]); then from right to
+    left an AC eigensolve, the positive LQ AC = C[s-1] AR[s] and GR[s-1] <- T(AR[s]) GR[s]
+    (un-normalised transfers, infinite_envs.jl:359-369).  The error is the change of the
+    boundary bond tensor C[n-1]; the result is InfiniteMPS(AR) with recalculated
+    environments.  Returns (psi, envs, eps, history), history entries carrying the energy
+    change (E - E_old) / 2."""
+    n = len(psi)
+    ctx = psi.ctx
+    envs = envs or InfiniteEnvironmentsCell(psi, H, alg.backend.code)
+    envs.recalculate(psi, tol=1e-10)
+    eps = galerkin(psi, envs, alg.backend)
+    E_old = energy(psi, envs)
+    Wd = H.device(ctx, envs.dtype)
+    prec = envs.precision
+    AL, AR, C = list(psi.AL), list(psi.AR), list(psi.C)
+    AC = [psi.AC(s) for s in range(n)]
+    GL, GR = list(envs.GL), list(envs.GR)
+
+    def eig(pos, solver):
+        h = DerivativeOperator(ctx, L.GB_HEFF_AC, GL[pos], Wd[pos], None, GR[pos], alg.backend)
+        val, x, _ = fixedpoint(h, AC[pos], "SR", solver)
+        return val, x
+
+    it = 0
+    hist = []
+    while True:
+        solver = Lanczos(krylovdim=30, maxiter=200, tol=_dyn_tol(eps, it, 1e-3), eager=True)
+        C_old = C[n - 1]
+        for pos in range(n):
+            _, AC[pos] = eig(pos, solver)
+            AL[pos], C[pos] = left_orth(AC[pos])
+            GL[(pos + 1) % n] = _transfer("L", ctx, GL[pos], Wd[pos], AL[pos], prec)
+        for pos in range(n - 1, -1, -1):
+            E, AC[pos] = eig(pos, solver)
+            C[pos - 1], AR[pos] = right_orth(AC[pos])
+            GR[pos - 1] = _transfer("R", ctx, GR[pos], Wd[pos], AR[pos], prec)
+        eps = _diff_norm(C[n - 1], C_old)
+        it += 1
+        hist.append({"iter": it, "energy_change": (E - E_old) / 2, "eps": eps})
+        E_old = E
+        if eps <= alg.tol or it >= alg.maxiter:
+            break
+    psi = InfiniteMPSCell.from_tensors(AR, tol=_dyn_tol(eps, it, 1e-6), maxiter=200)
+    envs = InfiniteEnvironmentsCell(psi, H, alg.backend.code)
+    envs.recalculate(psi, tol=1e-10)
     return psi, envs, eps, hist
 
 

@@ -401,3 +401,52 @@ def idmrg2(psi, H, maxdim, atol=1e-10, tol=1e-10, maxiter=200):
     psi = InfiniteMPSCell(ALn, ARn, Cn)
     GL, GR = infinite_envs(psi, H, tol=1e-10)
     return psi, GL, GR, eps, hist
+
+
+def idmrg1(psi, H, tol=1e-10, maxiter=200):
+    """find_groundstate(::InfiniteMPS, H, IDMRG()) for a cell of L >= 1 sites
+    (idmrg.jl:85-229): per site from left to right an AC eigensolve (started from the stored
+    AC), the positive QR AC = AL C and GL[s+1] <- GL[s] T(AL[s]); then per site from right to
+    left an AC eigensolve, the positive LQ AC = C[s-1] AR[s] and GR[s-1] <- T(AR[s]) GR[s]
+    (un-normalised transfers, infinite_envs.jl:359-369).  The error is the change of the
+    boundary bond tensor C[L-1]; dE = (E - E_old) / 2.  The result is InfiniteMPS(AR).
+    Returns (psi, GL, GR, eps, history) with history entries (iteration, dE, eps)."""
+    L = len(psi)
+    Ws = H.W
+    GL, GR = infinite_envs(psi, H, tol=1e-10)
+    eps = galerkin(psi, H, GL, GR)
+    E_old = energy(psi, H, GL, GR)
+    AL, AR, C = list(psi.AL), list(psi.AR), list(psi.C)
+    AC = [psi.AC(s) for s in range(L)]
+    it = 0
+    hist = []
+    while True:
+        et = dyn_tol(eps, it, 1e-3)
+        C_old = C[L - 1]
+        for pos in range(L):
+            _, AC[pos], _ = lanczos_eigsolve(dv.JordanAC(GL[pos], Ws[pos], GR[pos]), AC[pos],
+                                             krylovdim=30, maxiter=200, tol=et, eager=True)
+            Dl, d, Dr = AC[pos].shape
+            Q, R = qr_pos(AC[pos].reshape(Dl * d, Dr, order="F"))
+            AL[pos], C[pos] = Q.reshape(Dl, d, Q.shape[1], order="F"), R
+            GL[(pos + 1) % L] = dv.transfer_left(GL[pos], Ws[pos], AL[pos], AL[pos])
+        for pos in range(L - 1, -1, -1):
+            E, AC[pos], _ = lanczos_eigsolve(dv.JordanAC(GL[pos], Ws[pos], GR[pos]), AC[pos],
+                                             krylovdim=30, maxiter=200, tol=et, eager=True)
+            Dl, d, Dr = AC[pos].shape
+            Lm, Q = lq_pos(AC[pos].reshape(Dl, d * Dr, order="F"))
+            AR[pos], C[pos - 1] = Q.reshape(Q.shape[0], d, Dr, order="F"), Lm
+            GR[pos - 1] = dv.transfer_right(GR[pos], Ws[pos], AR[pos], AR[pos])
+        eps = _c_change(C[L - 1], C_old)
+        it += 1
+        hist.append((it, float(np.real(E - E_old)) / 2, eps))
+        E_old = E
+        if eps <= tol or it >= maxiter:
+            break
+    gtol = dyn_tol(eps, it, 1e-6)
+    D0 = AR[0].shape[0]
+    ALn, Cn = uniform_leftorth(AR, np.eye(D0, dtype=AR[0].dtype), gtol)
+    ARn, Cn = uniform_rightorth(ALn, Cn[-1], gtol)
+    psi = InfiniteMPSCell(ALn, ARn, Cn)
+    GL, GR = infinite_envs(psi, H, tol=1e-10)
+    return psi, GL, GR, eps, hist

@@ -158,3 +158,26 @@ def test_cell_gradient_grassmann_on_the_oracle_reaches_the_closed_form():
     assert hist[-1] <= 1e-8, hist[-5:]
     e_exact = M.tfim_infinite_energy_density(g)
     assert e_exact - 1e-12 <= f / 2 < e_exact + 1e-8, (f / 2, e_exact)
+
+
+def test_cell_idmrg_on_the_oracle():
+    """IDMRG (one-site updates) on InfiniteMPS cells (idmrg.jl:85-229): on a one-site cell the
+    cell restatement repeats the one-site oracle step for step, and on a two-site TFIM cell it
+    reaches the VUMPS energy per site of the same bond dimension."""
+    from oracle import cell as Ce
+    from oracle import vumps as V
+    g = 0.9
+    rng = np.random.default_rng(4)
+    A = rng.standard_normal((6, 2, 6)) + 1j * rng.standard_normal((6, 2, 6))
+    H1 = M.infinite_mpo_hamiltonian(1, 2, M.tfim_terms(1, g=g, periodic=True))
+    _, _, _, e1, h1 = V.idmrg(V.infinite_mps(A), H1, tol=1e-9, maxiter=40)
+    _, _, _, ec, hc = Ce.idmrg1(Ce.infinite_mps([A]), H1, tol=1e-9, maxiter=40)
+    assert len(h1) == len(hc)
+    for a, b in zip(h1, hc):
+        assert abs(a[2] - b[2]) <= 1e-8 * max(1.0, a[2]) and abs(np.real(a[1]) - b[1]) < 1e-10
+    H2 = M.infinite_mpo_hamiltonian(2, 2, M.tfim_terms(2, g=g, periodic=True))
+    As = [rng.standard_normal((6, 2, 6)) + 1j * rng.standard_normal((6, 2, 6)) for _ in range(2)]
+    psi, GL, GR, eps, hist = Ce.idmrg1(Ce.infinite_mps(As), H2, tol=1e-9, maxiter=200)
+    assert eps <= 1e-9
+    vpsi, vGL, vGR, veps, vhist = Ce.vumps(Ce.infinite_mps(As), H2, tol=1e-10, maxiter=100)
+    assert abs(Ce.energy(psi, H2, GL, GR) - Ce.energy(vpsi, H2, vGL, vGR)) / 2 < 1e-8

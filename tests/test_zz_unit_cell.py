@@ -58,3 +58,19 @@ def test_idmrg2_matches_oracle(ctx):
     assert abs(len(hist) - len(ohist)) <= 1
     assert abs(e - Ce.energy(opsi, oH, GL, GR) / 2) < 1e-10
     assert abs(e - M.tfim_infinite_energy_density(0.5)) < 1e-9
+
+
+def test_idmrg_on_a_cell_matches_oracle(ctx):
+    """IDMRG (one-site updates, idmrg.jl:85-229) on a two-site TFIM cell at D = 6: the same
+    iteration count, energy changes and final energy per site as the oracle's cell
+    restatement."""
+    As = _As(6, 2, 23)
+    oH = M.infinite_mpo_hamiltonian(2, 2, M.tfim_terms(2, g=0.9, periodic=True))
+    H = mpsgb.transverse_field_ising(2, g=0.9, infinite=True)
+    opsi, GL, GR, oeps, ohist = Ce.idmrg1(Ce.infinite_mps(As), oH, tol=1e-9, maxiter=200)
+    psi = GC.InfiniteMPSCell.from_tensors(As, ctx)
+    psi, envs, eps, hist = GC.find_groundstate_idmrg(psi, H, mpsgb.IDMRG(tol=1e-9, maxiter=200))
+    assert eps <= 1e-9 and oeps <= 1e-9
+    assert abs(len(hist) - len(ohist)) <= 1
+    assert abs(np.real(hist[-1]["energy_change"]) - ohist[-1][1]) < 1e-8
+    assert abs(GC.energy(psi, envs) / 2 - Ce.energy(opsi, oH, GL, GR) / 2) < 1e-10
