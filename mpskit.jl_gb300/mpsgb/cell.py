@@ -1,5 +1,5 @@
 """InfiniteMPS with a unit cell of L >= 1 sites on the device: uniform gauge, environments,
-VUMPS, IDMRG and IDMRG2.
+VUMPS, IDMRG, IDMRG2 and TDVP time steps.
 
   uniform_leftorth! / uniform_rightorth! over the cell  -- src/states/ortho.jl:214-340
   compute_leftenvs! / compute_rightenvs!, left_cyclethrough! / right_cyclethrough!
@@ -7,6 +7,7 @@ VUMPS, IDMRG and IDMRG2.
   VUMPS (per-site AC and C eigensolves, gauge step, environments)
                                                          -- src/algorithms/groundstate/vumps.jl:101-192
   IDMRG (one-site sweeps through the cell)              -- src/algorithms/groundstate/idmrg.jl:85-229
+  TDVP timestep (per-site AC and C integration)          -- src/algorithms/timestep/tdvp.jl:72-133
   IDMRG2 (two-site sweeps with the edge updates)        -- src/algorithms/groundstate/idmrg.jl:143-338
 
 Sites are counted from 0; C[i] is the bond tensor right of site i and C[-1] = C[L-1] the one
@@ -416,6 +417,35 @@ def find_groundstate_vumps(psi, H, alg, envs=None):
         if eps <= alg.tol or it >= alg.maxiter:
             break
     return psi, envs, eps, hist
+
+
+def timestep(psi, H, t, dt, alg=None, envs=None, imaginary_evolution=False, tolgauge=1e-14):
+    """timestep(::InfiniteMPS, H, t, dt, TDVP()) for a cell (tdvp.jl:72-133,
+    leftorthflag = true): every AC[s] and C[s] integrated with the same environments,
+    AL[s] = regauge(AC[s], C[s]), the state rebuilt as InfiniteMPS(AL, C[end]) by the cell's
+    uniform right gauge and the environments recalculated.  Returns (psi, envs)."""
+    from .algorithms import TDVP
+    from .derivatives import integrate
+    from .infinite import regauge as _regauge
+    alg = alg or TDVP()
+    if psi.dtype.kind != "c" and not imaginary_evolution:
+        raise TypeError("real-time evolution needs a complex InfiniteMPS")
+    if envs is None:
+        envs = InfiniteEnvironmentsCell(psi, H, alg.backend.code)
+    if envs.GL is None:
+        envs.recalculate(psi)
+    n = len(psi)
+    AL = []
+    for s in range(n):
+        AC = integrate(_heff_ac(envs, s, alg.backend), psi.AC(s), t, dt, alg.integrator,
+                       imaginary_evolution)
+        C = integrate(_heff_c(envs, s, alg.backend), psi.C[s], t, dt, alg.integrator,
+                      imaginary_evolution)
+        AL.append(_regauge(AC, C))
+    AR, C = uniform_rightorth(AL, psi.C[n - 1], tol=tolgauge)
+    psi = InfiniteMPSCell(AL, AR, C)
+    envs.recalculate(psi)
+    return psi, envs
 
 
 def find_groundstate_idmrg(psi, H, alg, envs=None):

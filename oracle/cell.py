@@ -450,3 +450,28 @@ def idmrg1(psi, H, tol=1e-10, maxiter=200):
     psi = InfiniteMPSCell(ALn, ARn, Cn)
     GL, GR = infinite_envs(psi, H, tol=1e-10)
     return psi, GL, GR, eps, hist
+
+
+def tdvp_timestep(psi, H, dt, GL=None, GR=None, imaginary=False, tol=1e-12):
+    """One TDVP step of an InfiniteMPS cell (tdvp.jl:91-133, leftorthflag = true): per site
+    AC'[s] = exp(-i dt H_AC[s]) AC[s] and C'[s] = exp(-i dt H_C[s]) C[s] with the
+    environments of psi (-dt for imaginary time), AL[s] = regauge(AC'[s], C'[s]), then
+    InfiniteMPS(AL, C[end]) -- the cell's uniform right gauge.  Returns (psi', GL, GR) with
+    the environments of psi'."""
+    from .krylov import lanczos_exponentiate
+    from .vumps import regauge
+    L = len(psi)
+    if GL is None:
+        GL, GR = infinite_envs(psi, H, tol=tol)
+    tt = -dt if imaginary else -1j * dt
+    AL = []
+    for s in range(L):
+        AC, _ = lanczos_exponentiate(dv.JordanAC(GL[s], H.W[s], GR[s]), tt, psi.AC(s),
+                                     krylovdim=30, tol=tol)
+        C, _ = lanczos_exponentiate(dv.CHam(GL[(s + 1) % L], GR[s]), tt,
+                                    psi.C[s].astype(np.complex128), krylovdim=30, tol=tol)
+        AL.append(regauge(AC, C))
+    AR, C2 = uniform_rightorth(AL, psi.C[-1], tol=1e-14)
+    psi2 = InfiniteMPSCell(AL, AR, C2)
+    GL, GR = infinite_envs(psi2, H, tol=tol)
+    return psi2, GL, GR

@@ -181,3 +181,27 @@ def test_cell_idmrg_on_the_oracle():
     assert eps <= 1e-9
     vpsi, vGL, vGR, veps, vhist = Ce.vumps(Ce.infinite_mps(As), H2, tol=1e-10, maxiter=100)
     assert abs(Ce.energy(psi, H2, GL, GR) - Ce.energy(vpsi, H2, vGL, vGR)) / 2 < 1e-8
+
+
+def test_cell_tdvp_on_the_oracle():
+    """TDVP on InfiniteMPS cells (tdvp.jl:72-133): the cell restatement on a one-site cell
+    repeats the one-site oracle step, a real-time step of a two-site ground state keeps its
+    energy, and an imaginary-time step lowers the energy of a random state."""
+    from oracle import cell as Ce
+    from oracle import vumps as V
+    rng = np.random.default_rng(6)
+    A = rng.standard_normal((4, 2, 4)) + 1j * rng.standard_normal((4, 2, 4))
+    H1 = M.infinite_mpo_hamiltonian(1, 2, M.tfim_terms(1, g=0.7, periodic=True))
+    p1, _, _ = V.tdvp_timestep_infinite(V.infinite_mps(A), H1, 0.05)
+    pc, _, _ = Ce.tdvp_timestep(Ce.infinite_mps([A]), H1, 0.05)
+    assert np.abs(p1.AL - pc.AL[0]).max() < 1e-10 and np.abs(p1.C - pc.C[0]).max() < 1e-10
+    H2 = M.infinite_mpo_hamiltonian(2, 2, M.tfim_terms(2, g=0.7, periodic=True))
+    As = [rng.standard_normal((6, 2, 6)) + 1j * rng.standard_normal((6, 2, 6)) for _ in range(2)]
+    gs, GL, GR, _, _ = Ce.vumps(Ce.infinite_mps(As), H2, tol=1e-10, maxiter=100)
+    e0 = Ce.energy(gs, H2, GL, GR)
+    p2, GL2, GR2 = Ce.tdvp_timestep(gs, H2, 0.1, GL, GR)
+    assert abs(Ce.energy(p2, H2, GL2, GR2) - e0) < 1e-8
+    psi = Ce.infinite_mps(As)
+    GL, GR = Ce.infinite_envs(psi, H2)
+    p3, GL3, GR3 = Ce.tdvp_timestep(psi, H2, 0.1, GL, GR, imaginary=True)
+    assert Ce.energy(p3, H2, GL3, GR3) < Ce.energy(psi, H2, GL, GR)

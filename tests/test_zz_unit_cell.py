@@ -74,3 +74,18 @@ def test_idmrg_on_a_cell_matches_oracle(ctx):
     assert abs(len(hist) - len(ohist)) <= 1
     assert abs(np.real(hist[-1]["energy_change"]) - ohist[-1][1]) < 1e-8
     assert abs(GC.energy(psi, envs) / 2 - Ce.energy(opsi, oH, GL, GR) / 2) < 1e-10
+
+
+def test_tdvp_step_on_a_cell_matches_oracle(ctx):
+    """One real-time TDVP step of a two-site cell (tdvp.jl:72-133): the same AL, C and
+    energy as the oracle's cell restatement."""
+    As = _As(6, 2, 24)
+    oH = M.infinite_mpo_hamiltonian(2, 2, M.tfim_terms(2, g=0.7, periodic=True))
+    H = mpsgb.transverse_field_ising(2, g=0.7, infinite=True)
+    op2, GL, GR = Ce.tdvp_timestep(Ce.infinite_mps(As), oH, 0.05)
+    p2, envs = GC.timestep(GC.InfiniteMPSCell.from_tensors(As, ctx), H, 0.0, 0.05)
+    AL, AR, C = p2.to_numpy()
+    for s in range(2):
+        assert np.abs(AL[s] - op2.AL[s]).max() < 1e-8, s
+        assert np.abs(C[s] - op2.C[s]).max() < 1e-8, s
+    assert abs(GC.energy(p2, envs) - Ce.energy(op2, oH, GL, GR)) < 1e-9
