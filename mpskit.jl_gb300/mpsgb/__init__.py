@@ -25,6 +25,7 @@ from . import u1
 from . import batched
 from . import io
 from . import cell
+from .cell import IDMRG2, InfiniteMPSCell, find_groundstate_idmrg2
 
 __all__ = [
     "Context", "DeviceTensor", "context", "AC2_hamiltonian", "AC_hamiltonian", "C_hamiltonian",
@@ -38,5 +39,5 @@ __all__ = [
     "expectation_value", "find_groundstate", "variance", "GradientGrassmann", "optim",
     "TDVP", "timestep", "VUMPS", "IDMRG", "InfiniteEnvironments", "InfiniteMPS",
     "find_groundstate_vumps", "find_groundstate_idmrg", "timestep_infinite", "u1", "batched", "io",
-    "cell",
+    "cell", "IDMRG2", "InfiniteMPSCell", "find_groundstate_idmrg2",
 ]

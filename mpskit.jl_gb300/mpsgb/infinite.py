@@ -392,8 +392,12 @@ class VUMPS:
 
 
 def find_groundstate_vumps(psi, H, alg, envs=None):
-    """find_groundstate(::InfiniteMPS, H, VUMPS()) for a one-site cell.
-    Returns (psi, envs, eps, history)."""
+    """find_groundstate(::InfiniteMPS, H, VUMPS()) for a one-site cell (an InfiniteMPSCell
+    goes to the cell form, `cell.find_groundstate_vumps`).  Returns (psi, envs, eps,
+    history)."""
+    from . import cell
+    if isinstance(psi, cell.InfiniteMPSCell):
+        return cell.find_groundstate_vumps(psi, H, alg, envs)
     envs = envs or InfiniteEnvironments(psi, H, alg.backend.code)
     it = 0
     envs.recalculate(psi, tol=1e-10)
@@ -448,7 +452,11 @@ def find_groundstate_idmrg(psi, H, alg, envs=None):
     transfer_leftenv!, infinite_envs.jl:359-363); AC eigensolve again, positive LQ
     AC = C AR, GR <- T(AR) GR; error |C - C_old|.  The result is InfiniteMPS(AR) with the
     DynamicTol gauge tolerance and recalculated environments.  Returns (psi, envs, eps,
-    history); history entries carry the energy change per site (E - E_old) / 2."""
+    history); history entries carry the energy change per site (E - E_old) / 2.  An
+    InfiniteMPSCell goes to the cell form (`cell.find_groundstate_idmrg`)."""
+    from . import cell
+    if isinstance(psi, cell.InfiniteMPSCell):
+        return cell.find_groundstate_idmrg(psi, H, alg, envs)
     envs = envs or InfiniteEnvironments(psi, H, alg.backend.code)
     ctx = psi.ctx
     envs.recalculate(psi, tol=1e-10)  # environments(psi, H): GMRES at Defaults.tol
@@ -485,7 +493,11 @@ def timestep_infinite(psi, H, t, dt, alg=None, envs=None, imaginary_evolution=Fa
     """timestep(::InfiniteMPS, H, t, dt, TDVP()) for a one-site cell (tdvp.jl:72-133,
     leftorthflag = true): AC and C are integrated with the same environments, AL =
     regauge(AC, C), the state is rebuilt by the uniform right gauge from AL (old C as the
-    starting point) and the environments are recalculated.  Returns (psi, envs)."""
+    starting point) and the environments are recalculated.  Returns (psi, envs).  An
+    InfiniteMPSCell goes to the cell form (`cell.timestep`)."""
+    from . import cell
+    if isinstance(psi, cell.InfiniteMPSCell):
+        return cell.timestep(psi, H, t, dt, alg, envs, imaginary_evolution, tolgauge)
     from .algorithms import TDVP
     alg = alg or TDVP()
     if psi.dtype.kind != "c" and not imaginary_evolution:

@@ -318,3 +318,22 @@ def test_idmrg2_orchestration(GC):
     assert len(hist) == len(ohist)
     assert abs(GC.energy(psi, envs) - Ce.energy(opsi, oH, oGL, oGR)) < 1e-12
     assert abs(hist[-1]["energy_change"] - ohist[-1][1]) < 1e-10
+
+
+def test_infinite_drivers_hand_cells_to_the_cell_forms(monkeypatch):
+    """find_groundstate_vumps / find_groundstate_idmrg / timestep_infinite take an
+    InfiniteMPSCell to the cell forms (one entry point per algorithm, as the reference's
+    find_groundstate and timestep take any unit cell)."""
+    import mpsgb
+    from mpsgb import cell, infinite
+    seen = []
+    monkeypatch.setattr(cell, "find_groundstate_vumps", lambda *a: seen.append("vumps") or a)
+    monkeypatch.setattr(cell, "find_groundstate_idmrg", lambda *a: seen.append("idmrg") or a)
+    monkeypatch.setattr(cell, "timestep", lambda *a: seen.append("tdvp") or a)
+    psi = cell.InfiniteMPSCell([], [], [])
+    infinite.find_groundstate_vumps(psi, None, None)
+    infinite.find_groundstate_idmrg(psi, None, None)
+    out = infinite.timestep_infinite(psi, None, 0.0, 0.1, None, None, True, 1e-12)
+    assert seen == ["vumps", "idmrg", "tdvp"]
+    assert out == (psi, None, 0.0, 0.1, None, None, True, 1e-12)
+    assert mpsgb.InfiniteMPSCell is cell.InfiniteMPSCell and mpsgb.IDMRG2 is cell.IDMRG2
