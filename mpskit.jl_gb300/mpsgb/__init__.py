@@ -15,8 +15,8 @@ from .operators import (FiniteMPOHamiltonian, InfiniteMPOHamiltonian, MPOHamilto
 from .states import (FiniteEnvironments, FiniteMPS, ac2_from, left_orth, mul_front, mul_tail,
                      project_complement_, right_orth, svd_trunc)
 from .algorithms import (DMRG, DMRG2, DMRG3S, TDVP, AdaptiveKrylov, OptimalExpand,
-                         SketchedExpand, expectation_value, find_groundstate, timestep,
-                         variance)
+                         SketchedExpand, changebonds, expectation_value, find_groundstate,
+                         timestep, variance)
 from .infinite import (IDMRG, VUMPS, InfiniteEnvironments, InfiniteMPS,
                        find_groundstate_idmrg, find_groundstate_vumps, timestep_infinite)
 from .grassmann import GradientGrassmann
@@ -36,6 +36,7 @@ __all__ = [
     "j1j2_cylinder", "transverse_field_ising", "xxz", "FiniteEnvironments", "FiniteMPS",
     "ac2_from", "left_orth", "mul_front", "mul_tail", "project_complement_", "right_orth",
     "svd_trunc", "DMRG", "DMRG2", "DMRG3S", "OptimalExpand", "SketchedExpand", "AdaptiveKrylov",
+    "changebonds",
     "expectation_value", "find_groundstate", "variance", "GradientGrassmann", "optim",
     "TDVP", "timestep", "VUMPS", "IDMRG", "InfiniteEnvironments", "InfiniteMPS",
     "find_groundstate_vumps", "find_groundstate_idmrg", "timestep_infinite", "u1", "batched", "io",

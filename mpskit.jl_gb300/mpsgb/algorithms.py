@@ -363,6 +363,23 @@ def sketched_expand(pos, right, psi, H, envs, alg, backend=None):
         psi.center = pos
 
 
+def changebonds(psi, H, alg, envs=None, backend=None):
+    """changebonds!(psi, H, ::OptimalExpand / ::SketchedExpand, envs)
+    (optimalexpand.jl:191-199, sketchedexpand.jl:165-173): changebond!(i, :right) at every
+    bond from the left.  The state is changed in place (only its gauge and bond spaces: the
+    added directions carry zero weight); the centre bond walks from the left end to the right
+    end, with a positive QR step where a bond has nothing to add.  Returns (psi, envs)."""
+    envs = envs or FiniteEnvironments(psi, H)
+    expand = sketched_expand if isinstance(alg, SketchedExpand) else optimal_expand
+    psi.right_canonicalize(0)
+    for i in range(len(psi) - 1):
+        expand(i, True, psi, H, envs, alg, backend)
+        if psi.center == i:
+            q, R = left_orth(psi.ac(i))
+            psi.AL[i], psi.C[i + 1], psi.center = q, R, i + 1
+    return psi, envs
+
+
 def dmrg3s_gauge(pos, right, psi, H, envs, AC, noise, maxdim, atol):
     """gauge!(psi, pos, dir, H, envs, AC, ::DMRG3S) (dmrg3s.jl:133-192).  Right: the
     perturbation noise * GL[pos] W[pos] AC with the right bond and the MPO channel fused

@@ -604,6 +604,30 @@ def sketched_expand(pos, right, psi, H, envs, alg):
         psi.center = pos
 
 
+def changebonds(psi, H, alg, envs=None):
+    """changebonds!(psi, H, ::OptimalExpand / ::SketchedExpand, envs)
+    (optimalexpand.jl:191-199, sketchedexpand.jl:165-173): changebond!(i, :right) at every
+    bond from the left (the centre walks right; a positive QR step where nothing is added)."""
+    envs = envs or FiniteEnvironments(psi, H)
+    expand = sketched_expand if isinstance(alg, SketchedExpand) else optimal_expand
+    assert psi.center == 0 or all(a is not None for a in psi.AR)
+    psi.center = 0
+    for i in range(len(psi) - 1):
+        expand(i, True, psi, H, envs, alg)
+        if psi.center == i:
+            ac = psi.ac(i)
+            Dl, d, Dr = ac.shape
+            if psi.qb is not None:
+                from .u1 import fuse, left_orth_u1
+                Q, R, _ = left_orth_u1(ac.reshape(Dl * d, Dr, order="F"),
+                                       fuse(psi.qb[i], psi.qp), psi.qb[i + 1])
+            else:
+                Q, R = qr_pos(ac.reshape(Dl * d, Dr, order="F"))
+            psi.AL[i], psi.C[i + 1] = Q.reshape(Dl, d, Q.shape[1], order="F"), R
+            psi.center = i + 1
+    return psi, envs
+
+
 class DMRG3S:
     """DMRG3S(noise, ExponentialDecay(decay_rate)) with the truncated SVD DMRG fills in
     (post_expand/dmrg3s.jl:83-153; trunc = truncrank(maxdim) & trunctol(atol)): the noise

@@ -292,3 +292,24 @@ def test_u1_single_site_dmrg_with_expansion_matches_the_oracle(ctx, kind):
         assert abs(a["energy"] - b[1]) <= 1e-8 * abs(b[1]), (a, b)
     assert -1e-12 * abs(e_ed) <= hist[-1]["energy"] - e_ed < bar * abs(e_ed)
     _u1_blocks_ok(psi)
+
+
+@pytest.mark.parametrize("kind", ["optimal", "sketched"])
+def test_changebonds_matches_the_oracle(ctx, kind):
+    """changebonds!(psi, H, ::OptimalExpand / ::SketchedExpand) (optimalexpand.jl:191-199,
+    sketchedexpand.jl:165-173) over a whole chain: the same enlarged bonds as the oracle and
+    the same (unchanged) state."""
+    L_ = 8
+    As = P.random_initial_tensors(L_, 2, 3, 9)
+    oH = M.finite_mpo_hamiltonian(L_, 2, M.heisenberg_terms(L_))
+    oalg = P.OptimalExpand(2) if kind == "optimal" else P.SketchedExpand(2, seed=1)
+    alg = mpsgb.OptimalExpand(2) if kind == "optimal" else mpsgb.SketchedExpand(2, seed=1)
+    opsi, _ = P.changebonds(P.finite_mps_from_tensors(As), oH, oalg)
+    psi, _ = mpsgb.changebonds(mpsgb.FiniteMPS.from_tensors(As, ctx), mpsgb.heisenberg_XXX(L_),
+                               alg)
+    assert psi.center == L_ - 1
+    assert [psi.AL[b].dims[2] for b in range(L_ - 1)] == \
+        [opsi.AL[b].shape[2] for b in range(L_ - 1)]
+    v = _vector([psi.AL[b].numpy() for b in range(L_ - 1)] + [psi.ac(L_ - 1).numpy()])
+    ov = _vector([opsi.AL[b] for b in range(L_ - 1)] + [opsi.ac(L_ - 1)])
+    assert abs(abs(np.vdot(v, ov)) / (np.linalg.norm(v) * np.linalg.norm(ov)) - 1) < 1e-10

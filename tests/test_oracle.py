@@ -426,3 +426,39 @@ def test_oracle_sketched_expand_with_a_full_sketch_is_optimal_expand(right):
         x, y = (m.reshape(-1, m.shape[2], order="F").T for m in (x, y))
     assert x.shape == y.shape
     assert np.abs(x.conj().T @ x - y.conj().T @ y).max() < 1e-10
+
+
+def _state_vector(psi):
+    """The state of an oracle FiniteMPS with its centre bond at psi.center."""
+    T = np.ones((1, 1))
+    for i in range(psi.center):
+        T = np.tensordot(T, psi.AL[i], axes=([-1], [0]))
+    T = np.tensordot(T, psi.C[psi.center], axes=([-1], [0]))
+    for i in range(psi.center, len(psi)):
+        T = np.tensordot(T, psi.AR[i], axes=([-1], [0]))
+    return T.reshape(-1)
+
+
+@pytest.mark.parametrize("kind", ["optimal", "sketched"])
+def test_changebonds_grows_every_bond_and_keeps_the_state(kind):
+    """changebonds!(psi, H, ::OptimalExpand / ::SketchedExpand) (optimalexpand.jl:191-199,
+    sketchedexpand.jl:165-173): every bond with a nonempty complement grows by at most
+    `add`, the state is unchanged and the left-canonical tensors stay isometric."""
+    L_ = 8
+    H = M.finite_mpo_hamiltonian(L_, 2, M.heisenberg_terms(L_))
+    psi = P.finite_mps_from_tensors(P.random_initial_tensors(L_, 2, 3, 9))
+    dims0 = [psi.C[b].shape[0] for b in range(1, L_)]
+    v0 = _state_vector(psi)
+    alg = P.OptimalExpand(2) if kind == "optimal" else P.SketchedExpand(2, seed=1)
+    psi, _ = P.changebonds(psi, H, alg)
+    assert psi.center == L_ - 1
+    dims1 = [psi.AL[b].shape[2] for b in range(L_ - 1)]
+    full = [min(2 ** (b + 1), 2 ** (L_ - b - 1)) for b in range(L_ - 1)]
+    for a, b, f in zip(dims0, dims1, full):
+        assert a <= b <= min(a + 2, f)
+    assert sum(dims1) > sum(dims0)
+    v1 = _state_vector(psi)
+    assert abs(abs(np.vdot(v0, v1)) / (np.linalg.norm(v0) * np.linalg.norm(v1)) - 1) < 1e-12
+    for b in range(L_ - 1):
+        m = psi.AL[b].reshape(-1, psi.AL[b].shape[2], order="F")
+        assert np.abs(m.conj().T @ m - np.eye(m.shape[1])).max() < 1e-12
