@@ -109,7 +109,8 @@ def test_mpo_channel_charges_host_and_oracle_agree():
     the channel, for plain, summed and product Hamiltonians."""
     L_ = 6
     H = O.heisenberg_XXX(L_, dtype=np.float64, u1=True)
-    for Hx in (H, H + O.xxz(L_, 0.0, 1.0, 0.2, dtype=np.float64, u1=True), H * H):
+    cyl = O.j1j2_cylinder(4, 6, dtype=np.float64, u1=True)     # long-range channels
+    for Hx in (H, H + O.xxz(L_, 0.0, 1.0, 0.2, dtype=np.float64, u1=True), H * H, cyl):
         qh = HU.channel_charges(Hx.W, O.SPIN_HALF_CHARGES)
         qo = U.mpo_channel_charges(Hx.W, O.SPIN_HALF_CHARGES)
         qp = np.asarray(O.SPIN_HALF_CHARGES)
@@ -117,7 +118,7 @@ def test_mpo_channel_charges_host_and_oracle_agree():
             assert np.array_equal(qh[i], qo[i])
             for a, s, t, c in np.argwhere(w != 0):
                 assert qh[i + 1][c] == qh[i][a] + qp[s] - qp[t]
-    assert qh[0].tolist() == [0] and qh[-1].tolist() == [0]
+        assert qh[0].tolist() == [0] and qh[-1].tolist() == [0]
     with pytest.raises(ValueError):
         HU.channel_charges(O.heisenberg_XXX(L_, dtype=np.float64).W, O.SPIN_HALF_CHARGES)
 
