@@ -206,3 +206,23 @@ def test_u1_single_site_dmrg_with_sketched_expand_reaches_ed():
     psi, envs, eps, hist = P.find_groundstate_dmrg(psi, H, alg)
     e_ed = M.ed_ground_energy(L_, 2, M.heisenberg_terms(L_, dtype=np.float64))[0]
     assert -1e-12 * abs(e_ed) <= hist[-1][1] - e_ed < 1e-9 * abs(e_ed), (hist[-1], e_ed)
+
+
+def test_u1_changebonds_keeps_the_state_and_the_block_structure():
+    """changebonds! with SketchedExpand on a U(1) state (sketchedexpand.jl:165-173): bonds
+    grow, stay sorted by charge, the tensors stay block sparse and the state is unchanged."""
+    L_ = 8
+    H = O.heisenberg_XXX(L_, dtype=np.float64, u1=True)
+    As, qb = HU.random_u1_tensors(L_, 3, 8, 0, np.float64)
+    psi = P.finite_mps_from_tensors(As, charges=(qb, O.SPIN_HALF_CHARGES))
+    psi.center = 0
+    v0 = _dense_state(psi)
+    n0 = sum(len(q) for q in psi.qb)
+    psi, _ = P.changebonds(psi, H, P.SketchedExpand(2, seed=5))
+    assert psi.center == L_ - 1 and sum(len(q) for q in psi.qb) > n0
+    v1 = _dense_state(psi)
+    assert abs(abs(np.vdot(v0, v1)) / (np.linalg.norm(v0) * np.linalg.norm(v1)) - 1) < 1e-12
+    for b in range(L_ - 1):
+        assert np.all(np.diff(psi.qb[b + 1]) >= 0)
+        A = psi.AL[b]
+        assert np.all(A[~HU.block_mask(psi.qb[b], psi.qp, psi.qb[b + 1])] == 0)
